@@ -1,0 +1,168 @@
+/*
+ * peec_gb300.h -- C ABI of the GB300 FFT-PEEC solver path.
+ *
+ * The three reference entry points this library replaces (paths relative to the
+ * Draco112358/Solver project) are
+ *   compute_FFT_mutual_coupling_mats  src/lib/solverFFT/compute_FFT_mutual_coupling_mats.jl:1
+ *   ComputeMatrixVectorFTT            src/lib/solverFFT/compute_Matrix_vector_fft.jl:1
+ *   gmres_custom                      src/lib/solverFFT/gmres_custom.jl:1
+ * and the per-port solve of the frequency loop FFT_solver_QS_S_type
+ * (src/lib/solverFFT/FFT_solver_QS_S_type.jl:121-140, 237-262).
+ *
+ * Conventions: plain pointers and sizes; complex values are interleaved
+ * (re, im) doubles, the layout of Julia ComplexF64 and C double _Complex; all
+ * indices are 0-based (a Julia caller subtracts 1). Host buffers are
+ * caller-owned and only read/written during the call. Every function returns
+ * PEEC_OK or a negative PEEC_ERR_* code; peec_last_error() then describes it.
+ * A context holds one geometry on one GPU with its own CUDA stream; contexts are
+ * independent (no global state), so concurrent jobs use separate contexts.
+ */
+#ifndef PEEC_GB300_H
+#define PEEC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PEEC_OK 0
+#define PEEC_ERR_CUDA (-1)
+#define PEEC_ERR_OOM (-2)
+#define PEEC_ERR_CANCELLED (-3)
+#define PEEC_ERR_TIMEOUT (-4)
+#define PEEC_ERR_BADARG (-5)
+#define PEEC_ERR_UNSUPPORTED (-6)
+#define PEEC_ERR_STATE (-7)
+
+/* precision of the circulant convolutions */
+#define PEEC_PREC_FP64 0
+#define PEEC_PREC_FP32 1
+
+typedef struct peec_ctx peec_ctx;
+
+/* ABI version (major*100 + minor). */
+int peec_version(void);
+
+/* Create / destroy a context on CUDA device `device`. */
+int peec_ctx_create(peec_ctx** out, int device);
+void peec_ctx_destroy(peec_ctx* ctx);
+/* Last error message of the context (never NULL). */
+const char* peec_last_error(const peec_ctx* ctx);
+
+/*
+ * Geometry and topology: the content of the reference's incidence_selection and
+ * expansions dictionaries (mesher_FFT.jl:36-84, create_mapping_Gamma_no_rep.jl:381-419).
+ *   Nx, Ny, Nz      voxel grid
+ *   mx, my, mz      edges per direction; edges are ordered x, then y, then z
+ *   edge_cell[m]    lattice cell of each edge in its direction lattice
+ *                   ((Nx-1)xNyxNz, Nx(Ny-1)Nz, NxNy(Nz-1); x fastest) -- the row of
+ *                   its 1 in mat_map_Lp[c,1]
+ *   edge_n1/n2[m]   the nodes with A(e,n1) = -1, A(e,n2) = +1
+ *   ns              surfaces; surf_fam[s] in 0..2 is the face family (reference
+ *                   families 12, 34, 56), surf_cell[s] its cell in the family
+ *                   lattice (Nx(Ny+1)Nz, (Nx+1)NyNz, NxNy(Nz+1)) -- the row of its 1
+ *                   in exp_P[f,f]; surf_node[s] the node of its 1 in Gamma
+ *   n               nodes
+ * The cross-family exp_P blocks are implied by this placement (their lattice rows
+ * are fixed functions of the family cells), so they are not passed.
+ */
+int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t mx, int64_t my, int64_t mz,
+                      const int64_t* edge_cell, const int64_t* edge_n1, const int64_t* edge_n2,
+                      int64_t ns, const int32_t* surf_fam, const int64_t* surf_cell,
+                      const int64_t* surf_node, int64_t n);
+
+/* P self terms diag(P) per surface (diagonals["P"]); invP = 1 ./ diagP. */
+int peec_set_pdiag(peec_ctx* ctx, const double* diagP);
+
+/*
+ * Generating rows of the nine circulant blocks, escaled, on the reference
+ * lattices (column-major, x fastest), in the order
+ *   Lpx, Lpy, Lpz, p12_se, p34_se, p56_se, p1234, p1256, p3456
+ * i.e. the first row of each block before store_circulant_fft
+ * (compute_FFT_mutual_coupling_mats.jl:52-125; Lp self entry already zeroed).
+ * Builds the device spectra. Replaces passing FFTCLp / FFTCP.
+ */
+int peec_set_rows(peec_ctx* ctx, const double* const rows[9]);
+
+/*
+ * GPU fill of the nine generating rows and their spectra -- the drop-in for
+ * compute_FFT_mutual_coupling_mats with QS_Rcc_FW == 1. origin is the mesh
+ * origin (unscaled, as the reference passes it), s* the escaled cell sizes.
+ * rows_out may be NULL, or hold nine host buffers (or NULL entries) that receive
+ * the rows. Returns PEEC_ERR_UNSUPPORTED if an entry needs a far-field
+ * (suppressed) branch of the reference integrals.
+ */
+int peec_fill(peec_ctx* ctx, const double origin[3], double sx, double sy, double sz,
+              double escal_Lp, double escal_P, double* const rows_out[9]);
+
+/*
+ * Per-frequency state (FFT_solver_QS_S_type.jl:105-119): scaled angular
+ * frequency w, DZ[m] (complex), Yle as COO (complex values), and the sparse LU
+ * factors of SS with Pr*SS*Pc = L*U in CSR form (L unit lower, U upper; both
+ * include their diagonal), perm_r / perm_c as in SuperLU (row i of SS goes to
+ * row perm_r[i]; column i to column perm_c[i]).
+ */
+int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,
+                       const int64_t* yle_row, const int64_t* yle_col, const double* yle_val,
+                       const int64_t* L_ptr, const int64_t* L_col, const double* L_val,
+                       const int64_t* U_ptr, const int64_t* U_col, const double* U_val,
+                       const int64_t* perm_r, const int64_t* perm_c);
+
+/* y = M^-1 K x (ComputeMatrixVectorFTT); x, y host, length N = m + ns + n complex. */
+int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precision);
+/* same on device pointers (complex double) */
+int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precision);
+
+/*
+ * Right-hand side of port (n1, n2): M^-1 [0; 0; is] with is = +Is at n1, -Is at
+ * n2 (precond_3_3_Kt_fft!, FFT_solver_QS_S_type.jl:124-127,237-262). tn host, N.
+ */
+int peec_port_rhs(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, double* tn);
+
+/*
+ * Householder GMRES with the reference's MATLAB semantics (gmres_custom):
+ * b, x_inout host (N complex); restarted = 0 runs one cycle of maxit inner steps
+ * (the reference's only call form), restarted = 1 runs maxit cycles of `restart`
+ * steps. flag: 0 converged, 1 not converged, 3 stagnation, 99 stopped.
+ * iter[2] = (outer, inner). resvec receives up to resvec_cap norms; *nres their
+ * count. relres is the left-preconditioned relative residual.
+ */
+int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, double tol, int maxit,
+               int restarted, int restart, int precision, int* flag, double* relres,
+               int* iter, double* resvec, int resvec_cap, int* nres);
+
+/*
+ * Mixed-precision solve: GMRES inner solves on the FP32-convolution operator inside
+ * FP64 iterative refinement (FP64 residual recomputation), to relative residual tol.
+ * inner_tol / inner_maxit bound each inner solve, max_outer the refinements.
+ * outer_out / inner_total report the work; relres the final FP64 relative residual.
+ */
+int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout, double tol,
+                     double inner_tol, int inner_maxit, int max_outer, int* flag,
+                     double* relres, int* outer_out, int* inner_total);
+
+/*
+ * Cooperative cancellation (is_stop_requested, solver_start.jl:370-374): a host
+ * int the caller may set to nonzero at any time; the solvers poll it between
+ * Krylov steps and return PEEC_ERR_CANCELLED (gmres flag 99). NULL disables.
+ */
+int peec_set_stop_flag(peec_ctx* ctx, volatile int* flag);
+
+/*
+ * Timing of the last peec_matvec / peec_matvec_dev call on the context stream
+ * (CUDA events): total, convolutions, sparse epilogue + LU, in milliseconds.
+ */
+int peec_last_timing(peec_ctx* ctx, double* total_ms, double* conv_ms, double* sparse_ms);
+
+/* Counters: kernel launches issued by the context since creation. */
+int64_t peec_launch_count(const peec_ctx* ctx);
+
+/* Vector sizes of the current topology: m, ns, n (N = m+ns+n). */
+int peec_sizes(const peec_ctx* ctx, int64_t* m, int64_t* ns, int64_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PEEC_GB300_H */

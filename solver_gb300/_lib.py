@@ -1,0 +1,101 @@
+"""ctypes binding of ``lib/libpeec_gb300.so`` (the C ABI in include/peec_gb300.h).
+
+Loading fails loudly: there is no CPU fallback anywhere in the product path.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIBDIR / "libpeec_gb300.so"
+
+PEEC_OK = 0
+ERRORS = {-1: "PEEC_ERR_CUDA", -2: "PEEC_ERR_OOM", -3: "PEEC_ERR_CANCELLED",
+          -4: "PEEC_ERR_TIMEOUT", -5: "PEEC_ERR_BADARG", -6: "PEEC_ERR_UNSUPPORTED",
+          -7: "PEEC_ERR_STATE"}
+
+# every symbol declared in include/peec_gb300.h
+EXPORTS = ("peec_version", "peec_ctx_create", "peec_ctx_destroy", "peec_last_error",
+           "peec_set_topology", "peec_set_pdiag", "peec_set_rows", "peec_fill",
+           "peec_set_frequency", "peec_matvec", "peec_matvec_dev", "peec_port_rhs",
+           "peec_gmres", "peec_solve_mixed", "peec_set_stop_flag", "peec_last_timing",
+           "peec_launch_count", "peec_sizes")
+
+
+class PeecError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class PeecCancelled(PeecError):
+    pass
+
+
+_lib = None
+
+P = ctypes.c_void_p
+I64P = ctypes.POINTER(ctypes.c_int64)
+DP = ctypes.POINTER(ctypes.c_double)
+
+
+def load(build_if_missing: bool = True):
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        if not build_if_missing:
+            raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA extension first")
+        _build.build_cuda()
+    L = ctypes.CDLL(str(LIB_PATH))
+    for name in EXPORTS:
+        if not hasattr(L, name):
+            raise RuntimeError(f"libpeec_gb300.so does not export {name}")
+    L.peec_version.restype = ctypes.c_int
+    L.peec_ctx_create.argtypes = [ctypes.POINTER(P), ctypes.c_int]
+    L.peec_ctx_destroy.argtypes = [P]
+    L.peec_ctx_destroy.restype = None
+    L.peec_last_error.argtypes = [P]
+    L.peec_last_error.restype = ctypes.c_char_p
+    L.peec_set_topology.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64,
+                                    ctypes.c_int64, ctypes.c_int64, P, P, P, ctypes.c_int64, P, P,
+                                    P, ctypes.c_int64]
+    L.peec_set_pdiag.argtypes = [P, P]
+    L.peec_set_rows.argtypes = [P, ctypes.POINTER(P)]
+    L.peec_fill.argtypes = [P, P, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                            ctypes.c_double, ctypes.c_double, ctypes.POINTER(P)]
+    L.peec_set_frequency.argtypes = [P, ctypes.c_double, P, ctypes.c_int64, P, P, P, P, P, P, P,
+                                     P, P, P, P]
+    L.peec_matvec.argtypes = [P, P, P, ctypes.c_int]
+    L.peec_matvec_dev.argtypes = [P, P, P, ctypes.c_int]
+    L.peec_port_rhs.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, P]
+    L.peec_gmres.argtypes = [P, P, P, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                             ctypes.c_int, ctypes.POINTER(ctypes.c_int), DP,
+                             ctypes.POINTER(ctypes.c_int), DP, ctypes.c_int,
+                             ctypes.POINTER(ctypes.c_int)]
+    L.peec_solve_mixed.argtypes = [P, P, P, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                   ctypes.c_int, ctypes.POINTER(ctypes.c_int), DP,
+                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.peec_set_stop_flag.argtypes = [P, P]
+    L.peec_last_timing.argtypes = [P, DP, DP, DP]
+    L.peec_launch_count.argtypes = [P]
+    L.peec_launch_count.restype = ctypes.c_int64
+    L.peec_sizes.argtypes = [P, I64P, I64P, I64P]
+    _lib = L
+    return L
+
+
+def ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def check(ctx, rc):
+    if rc != PEEC_OK:
+        msg = load().peec_last_error(ctx).decode(errors="replace")
+        if rc == -3:
+            raise PeecCancelled(rc, msg)
+        raise PeecError(rc, msg)

@@ -1,0 +1,214 @@
+"""Drop-in mirrors of the reference's FFT-PEEC entry points, running on the GPU.
+
+Same names, positional arguments and return values as the Julia functions:
+
+* ``compute_FFT_mutual_coupling_mats`` -- compute_FFT_mutual_coupling_mats.jl:1-33
+* ``ComputeMatrixVectorFTT``           -- compute_Matrix_vector_fft.jl:1-81
+* ``gmres_custom``                     -- gmres_custom.jl:1-331
+* ``FFT_solver_QS_S_type``             -- FFT_solver_QS_S_type.jl:1-234
+
+The FFTW plan arguments of the reference (PLIVector, PVector, ...) are accepted
+and ignored. The GPU context of a geometry is cached in ``expansions["gpu_ctx"]``,
+as a Julia caller would stash it. ``FFTCP`` / ``FFTCLp`` may be the handle this
+module returns, or the reference's own 2N-extent spectra (numpy), from which the
+generating rows are recovered once on the host.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import frequency as fq
+from .operator import GpuOperator, row_dims
+
+_P_KEYS = {(0, 0): "p12_se", (1, 1): "p34_se", (2, 2): "p56_se", (0, 1): "p1234",
+           (0, 2): "p1256", (1, 2): "p3456"}
+_LP_KEYS = ("Lpx", "Lpy", "Lpz")
+
+
+class CirculantSpectra:
+    """Device-resident spectra of the nine blocks (handle returned as FFTCP and FFTCLp)."""
+
+    def __init__(self, op: GpuOperator, rows: dict | None = None):
+        self.op = op
+        self.rows = rows
+
+
+def get_operator(incidence_selection, expansions, diagonals, device=0) -> GpuOperator:
+    op = expansions.get("gpu_ctx")
+    if op is None or op.h is None:
+        op = GpuOperator(incidence_selection, expansions, diagonals["P"], device=device)
+        expansions["gpu_ctx"] = op
+    return op
+
+
+def rows_from_reference_spectra(FFTCP, FFTCLp, grid):
+    """Generating rows from reference-format spectra: the first octant of the
+    inverse FFT of each 2N-extent circulant (store_circulant_fft's inverse)."""
+    dims = row_dims(*grid)
+    rows = {}
+    for c, key in enumerate(_LP_KEYS):
+        spec = FFTCLp[c] if not isinstance(FFTCLp[c], (list, tuple)) else FFTCLp[c][0]
+        if np.prod(dims[key]) == 0 or spec is None or np.size(spec) == 0:
+            continue
+        full = np.fft.ifftn(spec)
+        d = dims[key]
+        rows[key] = np.real(full[:d[0], :d[1], :d[2]]).ravel(order="F")
+    for (i, j), key in _P_KEYS.items():
+        full = np.fft.ifftn(FFTCP[i][j])
+        d = dims[key]
+        rows[key] = np.real(full[:d[0], :d[1], :d[2]]).ravel(order="F")
+    return rows
+
+
+def _ensure_spectra(op, FFTCP, FFTCLp):
+    if isinstance(FFTCP, CirculantSpectra):
+        if FFTCP.op is not op:
+            raise ValueError("spectra belong to another operator context")
+        return
+    key = (id(FFTCP), id(FFTCLp))
+    if getattr(op, "_spec_key", None) == key:
+        return
+    op.set_rows(rows_from_reference_spectra(FFTCP, FFTCLp, op.grid))
+    op._spec_key = key
+
+
+def compute_FFT_mutual_coupling_mats(circulant_centers, escalings, Nx, Ny, Nz, QS_Rcc_FW=1,
+                                     id=None, chan=None, *, incidence_selection=None,
+                                     expansions=None, diagonals=None, return_rows=False):
+    """GPU fill of the Lp/P generating rows and their spectra. Returns
+    (FFTCP, FFTCLp) as one device handle (the reference returns host spectra).
+    The operator context is taken from / stored in ``expansions``."""
+    if QS_Rcc_FW != 1:
+        raise NotImplementedError("only the quasi-static fill (QS_Rcc_FW == 1) is implemented")
+    op = get_operator(incidence_selection, expansions, diagonals)
+    if tuple(op.grid) != (Nx, Ny, Nz):
+        raise ValueError("grid does not match the operator's topology")
+    rows = op.fill(circulant_centers["origin"], circulant_centers["sx"], circulant_centers["sy"],
+                   circulant_centers["sz"], escalings["Lp"], escalings["P"],
+                   return_rows=return_rows)
+    h = CirculantSpectra(op, rows)
+    return h, h
+
+
+def _set_freq(op, w, DZ, Yle, lu):
+    op.set_frequency(w, DZ, Yle, lu, key=(float(w), id(DZ), id(Yle), id(lu)))
+
+
+def _lu_object(lu):
+    # the reference passes the factorisation object; accept scipy SuperLU or
+    # a FrequencyState carrying one
+    return getattr(lu, "lu", lu)
+
+
+def ComputeMatrixVectorFTT(x, w, incidence_selection, FFTCP, FFTCLp, DZ, Yle, expansions, invZ,
+                           invP, lu, PLIVector=None, PVector=None, PLI2Vector=None, P2Vector=None,
+                           chi2Vector=None, *, precision=0, diagonals=None):
+    """y = M^-1 K x on the GPU (compute_Matrix_vector_fft.jl:1-81)."""
+    op = expansions.get("gpu_ctx")
+    if op is None:
+        diagP = diagonals["P"] if diagonals is not None else 1.0 / np.asarray(invP.diagonal())
+        op = get_operator(incidence_selection, expansions, {"P": diagP})
+    _ensure_spectra(op, FFTCP, FFTCLp)
+    _set_freq(op, w, DZ, Yle, _lu_object(lu))
+    return op.matvec(x, precision)
+
+
+def gmres_custom(b, restarted, tol, maxit, x, wk, incidence_selection, FFTCP, FFTCLp, DZ, Yle,
+                 expansions, invZ, invP, lu, PLIVector=None, PVector=None, PLI2Vector=None,
+                 P2Vector=None, chi2Vector=None, id=None, chan=None, portIndex=None, *,
+                 restart=None, precision=0, stop_flag=None):
+    """Householder GMRES with MATLAB semantics on the GPU (gmres_custom.jl:1-331).
+    Returns (x, flag, relres, iter, resvec); flag 99 when stop_flag is set."""
+    op = expansions.get("gpu_ctx")
+    if op is None:
+        op = get_operator(incidence_selection, expansions,
+                          {"P": 1.0 / np.asarray(invP.diagonal())})
+    _ensure_spectra(op, FFTCP, FFTCLp)
+    _set_freq(op, wk, DZ, Yle, _lu_object(lu))
+    if stop_flag is not None:
+        op.set_stop_flag(stop_flag)
+    if restarted and restart is None:
+        raise ValueError("restarted GMRES needs an explicit restart length")
+    return op.gmres(b, x, tol, maxit, restarted=restarted, restart=restart or 0,
+                    precision=precision)
+
+
+def s2z_fft(S, Zo):
+    npt, _, nf = S.shape
+    I = np.eye(npt)
+    return np.stack([Zo * np.linalg.solve(I - S[:, :, k], I + S[:, :, k]) for k in range(nf)], 2)
+
+
+def s2y_fft(S, Zo):
+    npt, _, nf = S.shape
+    I = np.eye(npt)
+    return np.stack([Zo * np.linalg.solve(I + S[:, :, k], I - S[:, :, k]) for k in range(nf)], 2)
+
+
+def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, diagonals, ports,
+                         ports_scatter_value, lumped_elements, expansions, GMRES_settings,
+                         Zs_info, QS_Rcc_FW=1, id=None, chan=None, commentsEnabled=False, *,
+                         mode="fp64", mixed_inner_tol=1e-5, stop_flag=None, on_solve=None):
+    """Frequency x port sweep with warm starts (FFT_solver_QS_S_type.jl:1-234).
+
+    mode "fp64": the reference algorithm (FP64 convolutions, Householder GMRES).
+    mode "mixed": FP32 convolutions inside FP64 iterative refinement to the same
+    relative residual. Returns {"S","Z","Y","f","info"}; None if stopped.
+    """
+    if QS_Rcc_FW != 1:
+        raise NotImplementedError("only the quasi-static operator (QS_Rcc_FW == 1) is implemented")
+    freq = np.asarray(freq, dtype=np.float64).ravel() * escalings["freq"]
+    inner = int(GMRES_settings["Inner_Iter"])
+    A = incidence_selection["A"]
+    m, n = A.shape
+    ns = incidence_selection["Gamma"].shape[1]
+    op = get_operator(incidence_selection, expansions, diagonals)
+    _ensure_spectra(op, FFTCP, FFTCLp)
+    if stop_flag is not None:
+        op.set_stop_flag(stop_flag)
+    w = 2 * np.pi * freq
+    pn = np.asarray(ports["port_nodes"], dtype=np.int64).reshape(-1, 2)
+    npt = pn.shape[0]
+    S = np.zeros((npt, npt, w.size), dtype=np.complex128)
+    Vrest = np.zeros((m + n + ns, npt), dtype=np.complex128)
+    tol = GMRES_settings["tol"]
+    info = []
+    for k in range(w.size):
+        if stop_flag is not None and stop_flag.value:
+            return None
+        fs = fq.FrequencyState(w[k], escalings, incidence_selection, diagonals, Zs_info,
+                               lumped_elements, ports, ports_scatter_value)
+        op.set_frequency(w[k], fs.DZ, fs.Yle, fs.lu, key=("sweep", k, float(w[k])))
+        tk = float(tol[k]) if np.ndim(tol) else float(tol)
+        for c1 in range(npt):
+            n1, n2 = pn[c1]
+            tn = op.port_rhs(n1, n2, escalings["Is"])
+            if mode == "fp64":
+                V, flag, relres, it, resvec = op.gmres(tn, Vrest[:, c1], tk, inner)
+                rec = {"flag": flag, "relres": relres, "iter": it, "niter": len(resvec) - 1}
+            elif mode == "mixed":
+                V, flag, relres, outer, ninner = op.solve_mixed(tn, Vrest[:, c1], tk,
+                                                                inner_tol=mixed_inner_tol,
+                                                                inner_maxit=inner)
+                rec = {"flag": flag, "relres": relres, "outer": outer, "niter": ninner}
+            else:
+                raise ValueError(mode)
+            if flag == 99:
+                return None
+            rec.update(freq=k, port=c1)
+            info.append(rec)
+            if on_solve:
+                on_solve(k, c1, V)
+            Vrest[:, c1] = V
+            for c2 in range(c1, npt):
+                n3, n4 = pn[c2]
+                val = 2 * (V[m + ns + n3] - V[m + ns + n4])
+                if c1 == c2:
+                    S[c1, c2, k] = (val - ports_scatter_value) / ports_scatter_value
+                else:
+                    S[c1, c2, k] = val / ports_scatter_value
+                    S[c2, c1, k] = S[c1, c2, k]
+    return {"S": S, "Z": s2z_fft(S, ports_scatter_value), "Y": s2y_fft(S, ports_scatter_value),
+            "f": freq / escalings["freq"], "info": info, "Vrest": Vrest}

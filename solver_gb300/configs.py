@@ -1,0 +1,109 @@
+"""Synthetic voxel geometries of the benchmark configurations.
+
+Every geometry is produced as a solve request in the reference's JSON schema
+(mesherOutput / solverInput / solverAlgoParams, do_solving_fft.jl:1-62) so that it
+goes through the same parsing and mesher as a real request. Inputs are seeded
+synthetic stand-ins with the stated shapes, sizes and distributions.
+
+* crossbar_20x20x4  -- two copper bars (4 voxels wide, 1 thick) crossing at right
+  angles on layers 1 and 3 of a 20x20x4 grid of 1e-4 m voxels, one port between the
+  bar ends, 1 GHz, tol 1e-6.
+* random_128x128x64 -- 128x128x64 grid of 5e-5 m voxels, occupancy Bernoulli(0.3)
+  (seed 2), copper / FR4-like dielectric (eps_r 4.4) 50/50, 4 ports between random
+  occupied copper voxels on the outer faces, 10 frequencies log-spaced
+  10 MHz - 10 GHz, tol 1e-8.
+* random_copper(a, b, c, p, seed) -- copper-only Bernoulli(p) grids.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+COPPER = {"name": "copper", "color": "#b87333", "permeability": 1, "permittivity": 1,
+          "conductivity": 5.8e7}
+DIELECTRIC = {"name": "dielectric", "color": "#00aa00", "permeability": 1, "permittivity": 4.4,
+              "conductivity": 0}
+
+
+def _centre(idx, s, origin=(0.0, 0.0, 0.0)):
+    return [origin[d] + s[d] * idx[d] + s[d] / 2 for d in range(3)]
+
+
+def make_request(grids: dict, materials: list, cell, ports, freqs, tol, inner=100):
+    """grids: name -> bool array (Nx,Ny,Nz); ports: list of (voxel_a, voxel_b) 0-based."""
+    names = list(grids.keys())
+    shape = grids[names[0]].shape
+    mm = {k: np.asarray(v, dtype=bool).tolist() for k, v in grids.items()}
+    return {
+        "mesherOutput": {
+            "cell_size": {"cell_size_x": cell[0], "cell_size_y": cell[1], "cell_size_z": cell[2]},
+            "origin": {"origin_x": 0.0, "origin_y": 0.0, "origin_z": 0.0},
+            "n_cells": {"n_cells_x": shape[0], "n_cells_y": shape[1], "n_cells_z": shape[2]},
+            "n_materials": len(names),
+            "mesher_matrices": mm,
+        },
+        "solverInput": {
+            "unit": "m",
+            "materials": materials,
+            "ports": [{"name": f"Port{i + 1}", "type": 1,
+                       "inputElement": _centre(a, cell), "outputElement": _centre(b, cell),
+                       "rlcParams": {"resistance": 50}} for i, (a, b) in enumerate(ports)],
+            "lumped_elements": [],
+            "frequencies": [float(f) for f in freqs],
+            "ports_scattering_value": 50.0,
+        },
+        "solverAlgoParams": {"innerIteration": inner, "outerIteration": 1,
+                             "convergenceThreshold": tol},
+        "solverType": 1,
+    }
+
+
+def crossbar_20x20x4():
+    N = (20, 20, 4)
+    cu = np.zeros(N, dtype=bool)
+    cu[0:20, 8:12, 0] = True   # bar A: x = 1..20, y = 9..12, z = 1 (1-based)
+    cu[8:12, 0:20, 2] = True   # bar B: x = 9..12, y = 1..20, z = 3
+    return make_request({"copper": cu}, [dict(COPPER)], (1e-4, 1e-4, 1e-4),
+                        [((19, 9, 0), (9, 19, 2))], [1e9], 1e-6, inner=100)
+
+
+def _draw(shape, p, rng):
+    n = int(np.prod(shape))
+    return (rng.random(n) < p).reshape(shape, order="F")
+
+
+def _boundary_ports(mask, nports, rng):
+    Nx, Ny, Nz = mask.shape
+    face = np.zeros_like(mask)
+    face[[0, -1], :, :] = True
+    face[:, [0, -1], :] = True
+    face[:, :, [0, -1]] = True
+    cand = np.argwhere(mask & face)
+    pick = rng.choice(len(cand), size=2 * nports, replace=False)
+    v = [tuple(int(t) for t in cand[i]) for i in pick]
+    return [(v[2 * k], v[2 * k + 1]) for k in range(nports)]
+
+
+def random_mixed(shape=(128, 128, 64), s=5e-5, p=0.3, seed=2, nports=4,
+                 freqs=None, tol=1e-8, inner=100):
+    """Bernoulli(p) occupancy, copper/dielectric 50/50 drawn from the seed."""
+    rng = np.random.default_rng(seed)
+    occ = _draw(shape, p, rng)
+    is_cu = _draw(shape, 0.5, rng)
+    cu = occ & is_cu
+    di = occ & ~is_cu
+    ports = _boundary_ports(cu, nports, rng)
+    if freqs is None:
+        freqs = np.logspace(7, 10, 10)
+    return make_request({"copper": cu, "dielectric": di}, [dict(COPPER), dict(DIELECTRIC)],
+                        (s, s, s), ports, freqs, tol, inner=inner)
+
+
+def random_128x128x64():
+    return random_mixed()
+
+
+def random_copper(shape, s=5e-5, p=0.3, seed=5, nports=1, freqs=(1e9,), tol=1e-8, inner=100):
+    rng = np.random.default_rng(seed)
+    cu = _draw(shape, p, rng)
+    ports = _boundary_ports(cu, nports, rng)
+    return make_request({"copper": cu}, [dict(COPPER)], (s, s, s), ports, freqs, tol, inner=inner)

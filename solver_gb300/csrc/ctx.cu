@@ -1,0 +1,1285 @@
+// Context, C ABI and host-side drivers of the GB300 FFT-PEEC path.
+//
+// The context owns one geometry on one GPU: lattice maps, spectra, topology lists,
+// per-frequency operator state (DZ, Yle, LU factors) and the Krylov workspace.
+// Host code only sequences kernels and runs the small dense parts of GMRES
+// (Givens rotations, triangular solves on <= maxit unknowns) in FP64.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ctx.hpp"
+#include "peec_gb300.h"
+
+namespace peec {
+
+static thread_local std::string g_err;
+void set_error(const std::string& msg) { g_err = msg; }
+int fail_cuda(cudaError_t e, const char* expr, const char* file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "CUDA error %s (%d) at %s:%d in %s", cudaGetErrorString(e), (int)e,
+           file, line, expr);
+  g_err = buf;
+  return e == cudaErrorMemoryAllocation ? PEEC_ERR_OOM : PEEC_ERR_CUDA;
+}
+
+// launchers defined in the other translation units
+int conv_prepare(const ConvApp& a);
+size_t conv_smem_yz(const ConvApp& a, int prec);
+void launch_edge_rows(const c64*, const c64*, const c64*, const c64*, const int32_t*,
+                      const int32_t*, double, int, c64*, c64*, cudaStream_t);
+void launch_surf_rows(const c64*, const c64*, const int32_t*, const double*, int, c64*, c64*,
+                      cudaStream_t);
+void launch_node_rows(const c64*, const c64*, const c64*, const c64*, const c64*, const int32_t*,
+                      const int32_t*, const int32_t*, const int32_t*, const int32_t*,
+                      const int32_t*, const c64*, double, int, c64*, cudaStream_t);
+void launch_final_rows(const c64*, const c64*, const c64*, const c64*, const int32_t*,
+                       const int32_t*, const int32_t*, const double*, int, int, int, c64*,
+                       cudaStream_t);
+void launch_perm_gather(const c64*, const int32_t*, const double*, int, c64*, cudaStream_t);
+void launch_trsv_level(const int32_t*, int, const int32_t*, const int32_t*, const c64*,
+                       const c64*, c64*, cudaStream_t);
+int red_blocks(size_t N);
+void launch_multidot(const c64*, size_t, const c64*, size_t, int, c64*, c64*, cudaStream_t);
+void launch_multiaxpy(const c64*, size_t, const c64*, int, const c64*, int, size_t, c64*, size_t,
+                      double*, cudaStream_t);
+void launch_norm2(const c64*, size_t, size_t, double*, double*, cudaStream_t);
+void launch_sum_parts(const double*, int, double*, cudaStream_t);
+void launch_scale_rnorm(c64*, size_t, const double*, cudaStream_t);
+void launch_make_reflector(const c64*, size_t, int, c64, double, c64*, cudaStream_t);
+void launch_sub(const c64*, const c64*, size_t, c64*, cudaStream_t);
+void launch_add(const c64*, const c64*, size_t, c64*, cudaStream_t);
+void launch_xupdate(const c64*, const c64*, size_t, const c64*, const c64*, int, size_t, c64*,
+                    cudaStream_t);
+int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, double escal_Lp,
+                  double escal_P, int Nx, int Ny, int Nz, double* const d_rows[9],
+                  const int64_t row_len[9], int* d_bad, cudaStream_t st);
+
+}  // namespace peec
+
+using namespace peec;
+using cd = std::complex<double>;
+
+struct LevelTri {  // triangular factor without its diagonal, level-scheduled
+  int32_t *ptr = nullptr, *col = nullptr, *rows = nullptr;
+  c64 *val = nullptr, *dinv = nullptr;
+  std::vector<int> lvl_off;  // offsets into rows per level
+};
+
+struct peec_ctx {
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::string err;
+  int64_t launches = 0;
+  // twiddle master tables
+  int twmax = 0;
+  void* tw64 = nullptr;
+  void* tw32 = nullptr;
+  // sizes
+  int Nx = 0, Ny = 0, Nz = 0;
+  int64_t mx = 0, my = 0, mz = 0, m = 0, ns = 0, n = 0, N = 0;
+  bool have_topo = false, have_spec = false, have_freq = false, have_pdiag = false;
+  // topology
+  int32_t *n1 = nullptr, *n2 = nullptr, *snode = nullptr;
+  double* invP = nullptr;
+  int32_t *ne_ptr = nullptr, *ne_idx = nullptr, *nsn_ptr = nullptr, *nsn_idx = nullptr;
+  int32_t* fmap[6] = {};
+  int fdims[6][3] = {};
+  std::vector<ConvApp> apps;
+  Spectrum spec[9];
+  int row_dims[9][3] = {};
+  // frequency state
+  double w = 0.0;
+  c64* DZ = nullptr;
+  int32_t *yle_ptr = nullptr, *yle_col = nullptr;
+  c64* yle_val = nullptr;
+  int32_t *g_in = nullptr, *g_out = nullptr;  // LU permutations as gathers
+  LevelTri Lf, Uf;
+  // matvec work
+  c64 *LpI = nullptr, *PQ = nullptr, *Y1 = nullptr, *U1 = nullptr, *Y2 = nullptr, *U2 = nullptr;
+  c64 *tvec = nullptr, *Mvec = nullptr, *lutmp = nullptr;
+  // host staging
+  c64 *hx = nullptr, *hy = nullptr;  // pinned N
+  c64 *dx = nullptr, *dy = nullptr;  // device N
+  // krylov workspace
+  int kcap = 0;
+  c64* U = nullptr;
+  c64 *gb = nullptr, *gx = nullptr, *gr = nullptr, *gv = nullptr, *gw = nullptr, *gxm = nullptr,
+      *gxmin = nullptr, *gtmp = nullptr, *gzero = nullptr;
+  c64 *dcoef = nullptr, *dcoef2 = nullptr, *dpart = nullptr;
+  double *dred = nullptr, *dscal = nullptr;
+  c64* hsmall = nullptr;  // pinned small staging
+  double* hscal = nullptr;
+  volatile int* stop = nullptr;
+  float t_total = 0, t_conv = 0, t_sparse = 0;
+};
+
+#define CTX_TRY(expr)                 \
+  do {                                \
+    int _rc = (expr);                 \
+    if (_rc != PEEC_OK) {             \
+      ctx->err = g_err;               \
+      return _rc;                     \
+    }                                 \
+  } while (0)
+#define CTX_CUDA(expr) CTX_TRY(([&]() -> int { PEEC_CUDA_TRY(expr); return PEEC_OK; })())
+
+static int bad(peec_ctx* ctx, int code, const std::string& msg) {
+  ctx->err = msg;
+  g_err = msg;
+  return code;
+}
+
+template <typename T>
+static int dalloc(T** p, size_t count) {
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  if (count == 0) count = 1;
+  PEEC_CUDA_TRY(cudaMalloc((void**)p, count * sizeof(T)));
+  return PEEC_OK;
+}
+
+template <typename T>
+static int upload(T** p, const std::vector<T>& h, cudaStream_t st) {
+  int rc = dalloc(p, h.size());
+  if (rc) return rc;
+  if (!h.empty()) PEEC_CUDA_TRY(cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T),
+                                                cudaMemcpyHostToDevice, st));
+  return PEEC_OK;
+}
+
+static int pow2ceil(int v) {
+  int r = 1;
+  while (r < v) r <<= 1;
+  return r;
+}
+
+extern "C" int peec_version(void) { return 100; }
+
+extern "C" const char* peec_last_error(const peec_ctx* ctx) {
+  if (!ctx) return g_err.c_str();
+  return ctx->err.c_str();
+}
+
+extern "C" int64_t peec_launch_count(const peec_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" int peec_sizes(const peec_ctx* ctx, int64_t* m, int64_t* ns, int64_t* n) {
+  if (!ctx) return PEEC_ERR_BADARG;
+  if (m) *m = ctx->m;
+  if (ns) *ns = ctx->ns;
+  if (n) *n = ctx->n;
+  return PEEC_OK;
+}
+
+extern "C" int peec_ctx_create(peec_ctx** out, int device) {
+  if (!out) return PEEC_ERR_BADARG;
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    g_err = std::string("no CUDA device available: ") + cudaGetErrorString(e);
+    return PEEC_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) {
+    g_err = "device index out of range";
+    return PEEC_ERR_BADARG;
+  }
+  peec_ctx* ctx = new peec_ctx();
+  ctx->dev = device;
+  auto fail = [&](int rc) {
+    peec_ctx_destroy(ctx);
+    return rc;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return fail(fail_cuda(cudaGetLastError(), "cudaSetDevice", __FILE__, __LINE__));
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(fail_cuda(cudaGetLastError(), "cudaStreamCreate", __FILE__, __LINE__));
+  for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+  // twiddle master table exp(-2 pi i e / twmax), long-double accurate
+  ctx->twmax = 8192;
+  std::vector<c64> t64(ctx->twmax);
+  std::vector<c32> t32(ctx->twmax);
+  for (int e = 0; e < ctx->twmax; ++e) {
+    long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)e /
+                    (long double)ctx->twmax;
+    t64[e] = mk<double>((double)cosl(a), (double)sinl(a));
+    t32[e] = mk<float>((float)cosl(a), (float)sinl(a));
+  }
+  if (cudaMalloc(&ctx->tw64, sizeof(c64) * ctx->twmax) != cudaSuccess ||
+      cudaMalloc(&ctx->tw32, sizeof(c32) * ctx->twmax) != cudaSuccess)
+    return fail(fail_cuda(cudaErrorMemoryAllocation, "cudaMalloc twiddles", __FILE__, __LINE__));
+  cudaMemcpy(ctx->tw64, t64.data(), sizeof(c64) * ctx->twmax, cudaMemcpyHostToDevice);
+  cudaMemcpy(ctx->tw32, t32.data(), sizeof(c32) * ctx->twmax, cudaMemcpyHostToDevice);
+  cudaMallocHost(&ctx->hsmall, sizeof(c64) * 4096);
+  cudaMallocHost(&ctx->hscal, sizeof(double) * 64);
+  *out = ctx;
+  return PEEC_OK;
+}
+
+static void free_tri(LevelTri& t) {
+  cudaFree(t.ptr); cudaFree(t.col); cudaFree(t.rows); cudaFree(t.val); cudaFree(t.dinv);
+  t = LevelTri();
+}
+
+extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->dev);
+  if (ctx->st) cudaStreamSynchronize(ctx->st);
+  void* ptrs[] = {ctx->tw64, ctx->tw32, ctx->n1, ctx->n2, ctx->snode, ctx->invP, ctx->ne_ptr,
+                  ctx->ne_idx, ctx->nsn_ptr, ctx->nsn_idx, ctx->DZ, ctx->yle_ptr, ctx->yle_col,
+                  ctx->yle_val, ctx->g_in, ctx->g_out, ctx->LpI, ctx->PQ, ctx->Y1, ctx->U1,
+                  ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->dx, ctx->dy, ctx->U,
+                  ctx->gb, ctx->gx, ctx->gr, ctx->gv, ctx->gw, ctx->gxm, ctx->gxmin, ctx->gtmp,
+                  ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (auto& f : ctx->fmap)
+    if (f) cudaFree(f);
+  for (auto& a : ctx->apps)
+    for (int p = 0; p < 2; ++p) {
+      if (a.T1[p]) cudaFree(a.T1[p]);
+      if (a.T4[p]) cudaFree(a.T4[p]);
+    }
+  for (auto& s : ctx->spec)
+    for (int p = 0; p < 2; ++p)
+      if (s.d[p]) cudaFree(s.d[p]);
+  free_tri(ctx->Lf);
+  free_tri(ctx->Uf);
+  if (ctx->hx) cudaFreeHost(ctx->hx);
+  if (ctx->hy) cudaFreeHost(ctx->hy);
+  if (ctx->hsmall) cudaFreeHost(ctx->hsmall);
+  if (ctx->hscal) cudaFreeHost(ctx->hscal);
+  for (auto& ev : ctx->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (ctx->st) cudaStreamDestroy(ctx->st);
+  delete ctx;
+}
+
+extern "C" int peec_set_stop_flag(peec_ctx* ctx, volatile int* flag) {
+  if (!ctx) return PEEC_ERR_BADARG;
+  ctx->stop = flag;
+  return PEEC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// topology
+// ------------------------------------------------------------------------------------
+
+// FFT length along one dimension: a symmetric block needs L >= 2N-2, a general
+// Toeplitz block L >= na+nb-1; rounded up to a power of two.
+static int fft_len(int na, int nb, bool sym) {
+  int need = sym ? (na > 1 ? 2 * na - 2 : 1) : na + nb - 1;
+  return pow2ceil(need < 1 ? 1 : need);
+}
+
+extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t mx, int64_t my,
+                                 int64_t mz, const int64_t* edge_cell, const int64_t* edge_n1,
+                                 const int64_t* edge_n2, int64_t ns, const int32_t* surf_fam,
+                                 const int64_t* surf_cell, const int64_t* surf_node, int64_t n) {
+  if (!ctx) return PEEC_ERR_BADARG;
+  if (Nx < 1 || Ny < 1 || Nz < 1 || mx < 0 || my < 0 || mz < 0 || ns < 0 || n < 1)
+    return bad(ctx, PEEC_ERR_BADARG, "peec_set_topology: invalid sizes");
+  const int64_t m = mx + my + mz;
+  if (m + ns + n > INT32_MAX) return bad(ctx, PEEC_ERR_UNSUPPORTED, "problem too large for int32 indexing");
+  cudaSetDevice(ctx->dev);
+  ctx->Nx = Nx; ctx->Ny = Ny; ctx->Nz = Nz;
+  ctx->mx = mx; ctx->my = my; ctx->mz = mz; ctx->m = m; ctx->ns = ns; ctx->n = n;
+  ctx->N = m + ns + n;
+  // family lattices: P faces 0..2, Lp edge directions 3..5
+  const int fd[6][3] = {{Nx, Ny + 1, Nz}, {Nx + 1, Ny, Nz}, {Nx, Ny, Nz + 1},
+                        {Nx - 1, Ny, Nz}, {Nx, Ny - 1, Nz}, {Nx, Ny, Nz - 1}};
+  std::memcpy(ctx->fdims, fd, sizeof(fd));
+  std::vector<std::vector<int32_t>> maps(6);
+  for (int f = 0; f < 6; ++f) maps[f].assign((size_t)fd[f][0] * fd[f][1] * fd[f][2], -1);
+  const int64_t offs[4] = {0, mx, mx + my, m};
+  for (int c = 0; c < 3; ++c)
+    for (int64_t e = offs[c]; e < offs[c + 1]; ++e) {
+      const int64_t cell = edge_cell[e];
+      if (cell < 0 || cell >= (int64_t)maps[3 + c].size() || maps[3 + c][cell] != -1)
+        return bad(ctx, PEEC_ERR_BADARG, "edge lattice cell out of range or duplicated");
+      maps[3 + c][cell] = (int32_t)e;
+    }
+  for (int64_t s = 0; s < ns; ++s) {
+    const int f = surf_fam[s];
+    if (f < 0 || f > 2) return bad(ctx, PEEC_ERR_BADARG, "surface family out of range");
+    const int64_t cell = surf_cell[s];
+    if (cell < 0 || cell >= (int64_t)maps[f].size() || maps[f][cell] != -1)
+      return bad(ctx, PEEC_ERR_BADARG, "surface lattice cell out of range or duplicated");
+    maps[f][cell] = (int32_t)s;
+  }
+  for (int f = 0; f < 6; ++f) CTX_TRY(upload(&ctx->fmap[f], maps[f], ctx->st));
+  // incidence lists
+  std::vector<int32_t> hn1(m), hn2(m), hsn(ns);
+  std::vector<int32_t> deg(n + 1, 0), sdeg(n + 1, 0);
+  for (int64_t e = 0; e < m; ++e) {
+    if (edge_n1[e] < 0 || edge_n1[e] >= n || edge_n2[e] < 0 || edge_n2[e] >= n)
+      return bad(ctx, PEEC_ERR_BADARG, "edge node out of range");
+    hn1[e] = (int32_t)edge_n1[e];
+    hn2[e] = (int32_t)edge_n2[e];
+    deg[hn1[e] + 1]++;
+    deg[hn2[e] + 1]++;
+  }
+  for (int64_t s = 0; s < ns; ++s) {
+    if (surf_node[s] < 0 || surf_node[s] >= n) return bad(ctx, PEEC_ERR_BADARG, "surface node out of range");
+    hsn[s] = (int32_t)surf_node[s];
+    sdeg[hsn[s] + 1]++;
+  }
+  for (int64_t v = 0; v < n; ++v) {
+    deg[v + 1] += deg[v];
+    sdeg[v + 1] += sdeg[v];
+  }
+  std::vector<int32_t> nei(deg[n]), nsi(sdeg[n]);
+  {
+    std::vector<int32_t> fill(deg.begin(), deg.end() - 1);
+    for (int64_t e = 0; e < m; ++e) {
+      nei[fill[hn1[e]]++] = (int32_t)(2 * e);      // A = -1
+      nei[fill[hn2[e]]++] = (int32_t)(2 * e + 1);  // A = +1
+    }
+    std::vector<int32_t> sf(sdeg.begin(), sdeg.end() - 1);
+    for (int64_t s = 0; s < ns; ++s) nsi[sf[hsn[s]]++] = (int32_t)s;
+  }
+  CTX_TRY(upload(&ctx->n1, hn1, ctx->st));
+  CTX_TRY(upload(&ctx->n2, hn2, ctx->st));
+  CTX_TRY(upload(&ctx->snode, hsn, ctx->st));
+  CTX_TRY(upload(&ctx->ne_ptr, deg, ctx->st));
+  CTX_TRY(upload(&ctx->ne_idx, nei, ctx->st));
+  CTX_TRY(upload(&ctx->nsn_ptr, sdeg, ctx->st));
+  CTX_TRY(upload(&ctx->nsn_idx, nsi, ctx->st));
+  // block applications
+  for (auto& a : ctx->apps)
+    for (int p = 0; p < 2; ++p) {
+      cudaFree(a.T1[p]);
+      cudaFree(a.T4[p]);
+    }
+  ctx->apps.clear();
+  // reference row lattices: Lpx, Lpy, Lpz, p12, p34, p56, p1234, p1256, p3456
+  const int rd[9][3] = {{Nx - 1, Ny, Nz}, {Nx, Ny - 1, Nz}, {Nx, Ny, Nz - 1},
+                        {Nx, Ny + 1, Nz}, {Nx + 1, Ny, Nz}, {Nx, Ny, Nz + 1},
+                        {2 * Nx + 1, 2 * Ny + 1, Nz}, {Nx, 2 * Ny + 1, 2 * Nz + 1},
+                        {2 * Nx + 1, Ny, 2 * Nz + 1}};
+  std::memcpy(ctx->row_dims, rd, sizeof(rd));
+  struct Def { int spec, in, out, conj, s[3], o[3]; bool sym; };
+  const Def defs[12] = {
+      {0, 3, 3, 0, {1, 1, 1}, {0, 0, 0}, true},  {1, 4, 4, 0, {1, 1, 1}, {0, 0, 0}, true},
+      {2, 5, 5, 0, {1, 1, 1}, {0, 0, 0}, true},  {3, 0, 0, 0, {1, 1, 1}, {0, 0, 0}, true},
+      {4, 1, 1, 0, {1, 1, 1}, {0, 0, 0}, true},  {5, 2, 2, 0, {1, 1, 1}, {0, 0, 0}, true},
+      {6, 1, 0, 0, {2, 2, 1}, {1, -1, 0}, false}, {6, 0, 1, 1, {2, 2, 1}, {1, -1, 0}, false},
+      {7, 2, 0, 0, {1, 2, 2}, {0, -1, 1}, false}, {7, 0, 2, 1, {1, 2, 2}, {0, -1, 1}, false},
+      {8, 2, 1, 0, {2, 1, 2}, {-1, 0, 1}, false}, {8, 1, 2, 1, {2, 1, 2}, {-1, 0, 1}, false}};
+  for (int i = 0; i < 12; ++i) {
+    const Def& d = defs[i];
+    ConvApp a;
+    a.spec_id = d.spec;
+    a.in_fam = d.in;
+    a.out_fam = d.out;
+    a.conj = d.conj;
+    bool empty = false;
+    for (int k = 0; k < 3; ++k) {
+      a.nb[k] = fd[d.in][k];
+      a.na[k] = fd[d.out][k];
+      if (a.nb[k] <= 0 || a.na[k] <= 0) empty = true;
+    }
+    if (empty) continue;  // e.g. Nx == 1 has no x edges
+    // the spectrum of a cross block is built for its first application (conj = 0)
+    // and serves the transposed one, so both use the lattice pair of app conj = 0
+    const int fa = d.conj ? d.in : d.out, fb = d.conj ? d.out : d.in;
+    for (int k = 0; k < 3; ++k) {
+      a.L[k] = fft_len(fd[fa][k], fd[fb][k], d.sym);
+      a.logL[k] = ilog2(a.L[k]);
+    }
+    if (a.L[0] > ctx->twmax || a.L[1] > ctx->twmax || a.L[2] > ctx->twmax)
+      return bad(ctx, PEEC_ERR_UNSUPPORTED, "FFT length beyond twiddle table");
+    ctx->apps.push_back(a);
+  }
+  // ky split so the y/z plane fits in shared memory (<= 200 KB)
+  for (auto& a : ctx->apps) {
+    a.R = 1;
+    a.logR = 0;
+    while (conv_smem_yz(a, 0) > 200 * 1024 && a.R < a.L[1]) {
+      a.R <<= 1;
+      a.logR++;
+    }
+    if (conv_smem_yz(a, 0) > 220 * 1024)
+      return bad(ctx, PEEC_ERR_UNSUPPORTED, "z extent too large for the fused y/z pass");
+    for (int p = 0; p < 2; ++p) {
+      const size_t es = p == 0 ? sizeof(c64) : sizeof(c32);
+      const size_t t1 = (size_t)a.L[0] * a.nb[1] * a.nb[2] * es;
+      const size_t t4 = (size_t)a.R * a.L[0] * a.na[1] * a.na[2] * es;
+      PEEC_CUDA_TRY(cudaMalloc(&a.T1[p], t1));
+      PEEC_CUDA_TRY(cudaMalloc(&a.T4[p], t4));
+    }
+    CTX_TRY(conv_prepare(a));
+  }
+  // spectra share the lengths of their first application
+  for (auto& s : ctx->spec)
+    for (int p = 0; p < 2; ++p) {
+      if (s.d[p]) cudaFree(s.d[p]);
+      s.d[p] = nullptr;
+    }
+  for (auto& a : ctx->apps) std::memcpy(ctx->spec[a.spec_id].L, a.L, sizeof(a.L));
+  // work vectors
+  CTX_TRY(dalloc(&ctx->LpI, m));
+  CTX_TRY(dalloc(&ctx->PQ, ns));
+  CTX_TRY(dalloc(&ctx->Y1, m));
+  CTX_TRY(dalloc(&ctx->U1, m));
+  CTX_TRY(dalloc(&ctx->Y2, ns));
+  CTX_TRY(dalloc(&ctx->U2, ns));
+  CTX_TRY(dalloc(&ctx->tvec, n));
+  CTX_TRY(dalloc(&ctx->Mvec, n));
+  CTX_TRY(dalloc(&ctx->lutmp, n));
+  CTX_TRY(dalloc(&ctx->dx, ctx->N));
+  CTX_TRY(dalloc(&ctx->dy, ctx->N));
+  if (ctx->hx) cudaFreeHost(ctx->hx);
+  if (ctx->hy) cudaFreeHost(ctx->hy);
+  PEEC_CUDA_TRY(cudaMallocHost(&ctx->hx, sizeof(c64) * ctx->N));
+  PEEC_CUDA_TRY(cudaMallocHost(&ctx->hy, sizeof(c64) * ctx->N));
+  ctx->kcap = 0;
+  ctx->have_topo = true;
+  ctx->have_spec = ctx->have_freq = ctx->have_pdiag = false;
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return PEEC_OK;
+}
+
+extern "C" int peec_set_pdiag(peec_ctx* ctx, const double* diagP) {
+  if (!ctx || !diagP) return PEEC_ERR_BADARG;
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  std::vector<double> inv(ctx->ns);
+  for (int64_t s = 0; s < ctx->ns; ++s) inv[s] = 1.0 / diagP[s];
+  CTX_TRY(upload(&ctx->invP, inv, ctx->st));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  ctx->have_pdiag = true;
+  return PEEC_OK;
+}
+
+// spectra from device rows
+static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
+  static const int sdim[9][3] = {{1, 1, 1}, {1, 1, 1}, {1, 1, 1}, {1, 1, 1}, {1, 1, 1},
+                                 {1, 1, 1}, {2, 2, 1}, {1, 2, 2}, {2, 1, 2}};
+  static const int odim[9][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0},
+                                 {0, 0, 0}, {1, -1, 0}, {0, -1, 1}, {-1, 0, 1}};
+  bool done[9] = {false};
+  for (auto& a : ctx->apps) {
+    if (a.conj || done[a.spec_id]) continue;
+    const int sid = a.spec_id;
+    if (!d_rows[sid]) return bad(ctx, PEEC_ERR_BADARG, "missing generating row");
+    Spectrum& S = ctx->spec[sid];
+    CTX_TRY(spectrum_build(S, d_rows[sid], ctx->row_dims[sid], a.na, a.nb, sdim[sid], odim[sid],
+                           sid < 6 ? 1 : 0, ctx->tw64, ctx->twmax, ctx->st));
+    ctx->launches += 6;
+    done[sid] = true;
+  }
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  ctx->have_spec = true;
+  return PEEC_OK;
+}
+
+extern "C" int peec_set_rows(peec_ctx* ctx, const double* const rows[9]) {
+  if (!ctx || !rows) return PEEC_ERR_BADARG;
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  cudaSetDevice(ctx->dev);
+  double* d_rows[9] = {};
+  int rc = PEEC_OK;
+  for (int i = 0; i < 9 && rc == PEEC_OK; ++i) {
+    const size_t len = (size_t)ctx->row_dims[i][0] * ctx->row_dims[i][1] * ctx->row_dims[i][2];
+    if (len == 0 || !rows[i]) continue;
+    if (cudaMalloc(&d_rows[i], len * sizeof(double)) != cudaSuccess) {
+      rc = bad(ctx, PEEC_ERR_OOM, "row upload allocation");
+      break;
+    }
+    cudaMemcpyAsync(d_rows[i], rows[i], len * sizeof(double), cudaMemcpyHostToDevice, ctx->st);
+  }
+  if (rc == PEEC_OK) rc = build_spectra(ctx, d_rows);
+  cudaStreamSynchronize(ctx->st);
+  for (auto p : d_rows)
+    if (p) cudaFree(p);
+  return rc;
+}
+
+extern "C" int peec_fill(peec_ctx* ctx, const double origin[3], double sx, double sy, double sz,
+                         double escal_Lp, double escal_P, double* const rows_out[9]) {
+  if (!ctx || !origin) return PEEC_ERR_BADARG;
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  cudaSetDevice(ctx->dev);
+  double* d_rows[9] = {};
+  int64_t len[9];
+  int rc = PEEC_OK;
+  int* d_bad = nullptr;
+  PEEC_CUDA_TRY(cudaMalloc(&d_bad, sizeof(int)));
+  PEEC_CUDA_TRY(cudaMemsetAsync(d_bad, 0, sizeof(int), ctx->st));
+  for (int i = 0; i < 9; ++i) {
+    len[i] = (int64_t)ctx->row_dims[i][0] * ctx->row_dims[i][1] * ctx->row_dims[i][2];
+    if (len[i] > 0 && cudaMalloc(&d_rows[i], len[i] * sizeof(double)) != cudaSuccess) {
+      rc = bad(ctx, PEEC_ERR_OOM, "row allocation");
+      break;
+    }
+  }
+  if (rc == PEEC_OK) {
+    rc = fill_rows_gpu(origin, sx, sy, sz, escal_Lp, escal_P, ctx->Nx, ctx->Ny, ctx->Nz, d_rows,
+                       len, d_bad, ctx->st);
+    ctx->launches += 9;
+    if (rc) ctx->err = g_err;
+  }
+  int hbad = 0;
+  if (rc == PEEC_OK) {
+    cudaMemcpyAsync(&hbad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->st);
+    if (cudaStreamSynchronize(ctx->st) != cudaSuccess)
+      rc = fail_cuda(cudaGetLastError(), "fill", __FILE__, __LINE__);
+    else if (hbad)
+      rc = bad(ctx, PEEC_ERR_UNSUPPORTED,
+               "fill: an entry needs a far-field (suppressed) branch of the reference integrals");
+  }
+  if (rc == PEEC_OK && rows_out) {
+    for (int i = 0; i < 9; ++i)
+      if (rows_out[i] && d_rows[i])
+        cudaMemcpyAsync(rows_out[i], d_rows[i], len[i] * sizeof(double), cudaMemcpyDeviceToHost,
+                        ctx->st);
+  }
+  if (rc == PEEC_OK) rc = build_spectra(ctx, d_rows);
+  cudaStreamSynchronize(ctx->st);
+  for (auto p : d_rows)
+    if (p) cudaFree(p);
+  cudaFree(d_bad);
+  return rc;
+}
+
+// ------------------------------------------------------------------------------------
+// frequency state
+// ------------------------------------------------------------------------------------
+
+// Splits a CSR triangular factor into off-diagonal CSR + inverse diagonal and
+// computes dependency levels (lower: increasing, upper: decreasing row order).
+static int make_tri(peec_ctx* ctx, LevelTri& T, int64_t n, const int64_t* ptr, const int64_t* col,
+                    const double* val, bool lower) {
+  free_tri(T);
+  std::vector<int32_t> p(n + 1, 0), c;
+  std::vector<c64> v, dinv(n);
+  c.reserve(ptr[n]);
+  v.reserve(ptr[n]);
+  std::vector<int> level(n, 0);
+  for (int64_t r = 0; r < n; ++r) {
+    cd diag(0.0, 0.0);
+    for (int64_t q = ptr[r]; q < ptr[r + 1]; ++q) {
+      const int64_t j = col[q];
+      const cd x(val[2 * q], val[2 * q + 1]);
+      if (j == r) {
+        diag = x;
+      } else {
+        if ((lower && j > r) || (!lower && j < r))
+          return bad(ctx, PEEC_ERR_BADARG, "triangular factor has entries on the wrong side");
+        if (j < 0 || j >= n) return bad(ctx, PEEC_ERR_BADARG, "triangular factor column out of range");
+        c.push_back((int32_t)j);
+        v.push_back(mk<double>(x.real(), x.imag()));
+      }
+    }
+    if (diag == cd(0.0, 0.0)) return bad(ctx, PEEC_ERR_BADARG, "zero pivot in triangular factor");
+    const cd di = 1.0 / diag;
+    dinv[r] = mk<double>(di.real(), di.imag());
+    p[r + 1] = (int32_t)c.size();
+  }
+  // levels
+  int maxl = 0;
+  if (lower) {
+    for (int64_t r = 0; r < n; ++r) {
+      int l = 0;
+      for (int32_t q = p[r]; q < p[r + 1]; ++q) l = std::max(l, level[c[q]] + 1);
+      level[r] = l;
+      maxl = std::max(maxl, l);
+    }
+  } else {
+    for (int64_t r = n - 1; r >= 0; --r) {
+      int l = 0;
+      for (int32_t q = p[r]; q < p[r + 1]; ++q) l = std::max(l, level[c[q]] + 1);
+      level[r] = l;
+      maxl = std::max(maxl, l);
+    }
+  }
+  std::vector<int> cnt(maxl + 2, 0);
+  for (int64_t r = 0; r < n; ++r) cnt[level[r] + 1]++;
+  for (int l = 0; l <= maxl; ++l) cnt[l + 1] += cnt[l];
+  std::vector<int32_t> rows(n);
+  std::vector<int> fillp(cnt.begin(), cnt.end() - 1);
+  for (int64_t r = 0; r < n; ++r) rows[fillp[level[r]]++] = (int32_t)r;
+  T.lvl_off.assign(cnt.begin(), cnt.end());
+  CTX_TRY(upload(&T.ptr, p, ctx->st));
+  CTX_TRY(upload(&T.col, c, ctx->st));
+  CTX_TRY(upload(&T.val, v, ctx->st));
+  CTX_TRY(upload(&T.dinv, dinv, ctx->st));
+  CTX_TRY(upload(&T.rows, rows, ctx->st));
+  return PEEC_OK;
+}
+
+extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,
+                                  const int64_t* yle_row, const int64_t* yle_col,
+                                  const double* yle_val, const int64_t* L_ptr,
+                                  const int64_t* L_col, const double* L_val,
+                                  const int64_t* U_ptr, const int64_t* U_col,
+                                  const double* U_val, const int64_t* perm_r,
+                                  const int64_t* perm_c) {
+  if (!ctx || !DZ || !L_ptr || !U_ptr || !perm_r || !perm_c) return PEEC_ERR_BADARG;
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  cudaSetDevice(ctx->dev);
+  const int64_t n = ctx->n, m = ctx->m;
+  ctx->w = w;
+  std::vector<c64> dz(m);
+  for (int64_t e = 0; e < m; ++e) dz[e] = mk<double>(DZ[2 * e], DZ[2 * e + 1]);
+  CTX_TRY(upload(&ctx->DZ, dz, ctx->st));
+  // Yle COO -> CSR (duplicates summed, as sparse() does)
+  std::vector<int32_t> yp(n + 1, 0), yc;
+  std::vector<c64> yv;
+  {
+    std::vector<std::vector<std::pair<int32_t, cd>>> rowsv(n);
+    for (int64_t q = 0; q < yle_nnz; ++q) {
+      if (yle_row[q] < 0 || yle_row[q] >= n || yle_col[q] < 0 || yle_col[q] >= n)
+        return bad(ctx, PEEC_ERR_BADARG, "Yle index out of range");
+      rowsv[yle_row[q]].push_back({(int32_t)yle_col[q], cd(yle_val[2 * q], yle_val[2 * q + 1])});
+    }
+    for (int64_t r = 0; r < n; ++r) {
+      auto& rv = rowsv[r];
+      std::sort(rv.begin(), rv.end(),
+                [](const std::pair<int32_t, cd>& a, const std::pair<int32_t, cd>& b) {
+                  return a.first < b.first;
+                });
+      for (size_t i = 0; i < rv.size(); ++i) {
+        if (!yc.empty() && (int64_t)yp[r] < (int64_t)yc.size() && yc.back() == rv[i].first &&
+            yc.size() > (size_t)yp[r]) {
+          c64& t = yv.back();
+          t.x += rv[i].second.real();
+          t.y += rv[i].second.imag();
+        } else {
+          yc.push_back(rv[i].first);
+          yv.push_back(mk<double>(rv[i].second.real(), rv[i].second.imag()));
+        }
+      }
+      yp[r + 1] = (int32_t)yc.size();
+    }
+  }
+  CTX_TRY(upload(&ctx->yle_ptr, yp, ctx->st));
+  CTX_TRY(upload(&ctx->yle_col, yc, ctx->st));
+  CTX_TRY(upload(&ctx->yle_val, yv, ctx->st));
+  // LU: b' = b[iperm_r]; x = z[perm_c]
+  std::vector<int32_t> gin(n), gout(n);
+  for (int64_t i = 0; i < n; ++i) {
+    if (perm_r[i] < 0 || perm_r[i] >= n || perm_c[i] < 0 || perm_c[i] >= n)
+      return bad(ctx, PEEC_ERR_BADARG, "LU permutation out of range");
+    gin[perm_r[i]] = (int32_t)i;
+    gout[i] = (int32_t)perm_c[i];
+  }
+  CTX_TRY(upload(&ctx->g_in, gin, ctx->st));
+  CTX_TRY(upload(&ctx->g_out, gout, ctx->st));
+  CTX_TRY(make_tri(ctx, ctx->Lf, n, L_ptr, L_col, L_val, true));
+  CTX_TRY(make_tri(ctx, ctx->Uf, n, U_ptr, U_col, U_val, false));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  ctx->have_freq = true;
+  return PEEC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// operator
+// ------------------------------------------------------------------------------------
+
+static void lu_solve(peec_ctx* ctx, const c64* b, c64* x) {
+  const int n = (int)ctx->n;
+  launch_perm_gather(b, ctx->g_in, nullptr, n, ctx->lutmp, ctx->st);
+  ctx->launches++;
+  for (LevelTri* T : {&ctx->Lf, &ctx->Uf}) {
+    for (size_t l = 0; l + 1 < T->lvl_off.size(); ++l) {
+      const int cnt = T->lvl_off[l + 1] - T->lvl_off[l];
+      if (cnt <= 0) continue;
+      launch_trsv_level(T->rows + T->lvl_off[l], cnt, T->ptr, T->col, T->val, T->dinv, ctx->lutmp,
+                        ctx->st);
+      ctx->launches++;
+    }
+  }
+  launch_perm_gather(ctx->lutmp, ctx->g_out, nullptr, n, x, ctx->st);
+  ctx->launches++;
+}
+
+static int matvec_dev(peec_ctx* ctx, const c64* x, c64* y, int prec, bool timed) {
+  if (!ctx->have_topo || !ctx->have_spec || !ctx->have_freq || !ctx->have_pdiag)
+    return bad(ctx, PEEC_ERR_STATE, "operator incomplete (topology, pdiag, rows, frequency)");
+  const int64_t m = ctx->m, ns = ctx->ns, n = ctx->n;
+  cudaStream_t st = ctx->st;
+  if (timed) cudaEventRecord(ctx->ev[0], st);
+  cudaMemsetAsync(ctx->LpI, 0, sizeof(c64) * (m > 0 ? m : 1), st);
+  cudaMemsetAsync(ctx->PQ, 0, sizeof(c64) * (ns > 0 ? ns : 1), st);
+  for (const auto& a : ctx->apps) {
+    const bool lp = a.in_fam >= 3;
+    const c64* xin = lp ? x : x + m;
+    c64* yout = lp ? ctx->LpI : ctx->PQ;
+    conv_apply(a, ctx->spec[a.spec_id], ctx->fmap[a.in_fam], ctx->fmap[a.out_fam], xin, yout, prec,
+               ctx->tw64, ctx->tw32, ctx->twmax, st);
+    ctx->launches += 3;
+  }
+  if (timed) cudaEventRecord(ctx->ev[1], st);
+  const c64* I = x;
+  const c64* Q = x + m;
+  const c64* Phi = x + m + ns;
+  launch_edge_rows(I, Phi, ctx->LpI, ctx->DZ, ctx->n1, ctx->n2, ctx->w, (int)m, ctx->Y1, ctx->U1,
+                   st);
+  launch_surf_rows(ctx->PQ, Phi, ctx->snode, ctx->invP, (int)ns, ctx->Y2, ctx->U2, st);
+  launch_node_rows(I, Q, Phi, ctx->U1, ctx->U2, ctx->ne_ptr, ctx->ne_idx, ctx->nsn_ptr,
+                   ctx->nsn_idx, ctx->yle_ptr, ctx->yle_col, ctx->yle_val, ctx->w, (int)n,
+                   ctx->tvec, st);
+  ctx->launches += 3;
+  lu_solve(ctx, ctx->tvec, ctx->Mvec);
+  launch_final_rows(ctx->Y1, ctx->Y2, ctx->Mvec, ctx->DZ, ctx->n1, ctx->n2, ctx->snode, ctx->invP,
+                    (int)m, (int)ns, (int)n, y, st);
+  ctx->launches++;
+  if (timed) cudaEventRecord(ctx->ev[2], st);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail_cuda(e, "matvec launch", __FILE__, __LINE__);
+  return PEEC_OK;
+}
+
+extern "C" int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precision) {
+  if (!ctx || !x || !y) return PEEC_ERR_BADARG;
+  if (precision != 0 && precision != 1) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0 or 1");
+  cudaSetDevice(ctx->dev);
+  CTX_TRY(matvec_dev(ctx, (const c64*)x, (c64*)y, precision, true));
+  PEEC_CUDA_TRY(cudaEventSynchronize(ctx->ev[2]));
+  cudaEventElapsedTime(&ctx->t_total, ctx->ev[0], ctx->ev[2]);
+  cudaEventElapsedTime(&ctx->t_conv, ctx->ev[0], ctx->ev[1]);
+  cudaEventElapsedTime(&ctx->t_sparse, ctx->ev[1], ctx->ev[2]);
+  return PEEC_OK;
+}
+
+extern "C" int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precision) {
+  if (!ctx || !x || !y) return PEEC_ERR_BADARG;
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  cudaSetDevice(ctx->dev);
+  const size_t bytes = sizeof(c64) * ctx->N;
+  PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->dx, x, bytes, cudaMemcpyHostToDevice, ctx->st));
+  CTX_TRY(peec_matvec_dev(ctx, ctx->dx, ctx->dy, precision));
+  PEEC_CUDA_TRY(cudaMemcpyAsync(y, ctx->dy, bytes, cudaMemcpyDeviceToHost, ctx->st));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return PEEC_OK;
+}
+
+extern "C" int peec_last_timing(peec_ctx* ctx, double* total_ms, double* conv_ms,
+                                double* sparse_ms) {
+  if (!ctx) return PEEC_ERR_BADARG;
+  if (total_ms) *total_ms = ctx->t_total;
+  if (conv_ms) *conv_ms = ctx->t_conv;
+  if (sparse_ms) *sparse_ms = ctx->t_sparse;
+  return PEEC_OK;
+}
+
+extern "C" int peec_port_rhs(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, double* tn) {
+  if (!ctx || !tn) return PEEC_ERR_BADARG;
+  if (!ctx->have_freq || !ctx->have_pdiag) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
+  if (n1 < 0 || n1 >= ctx->n || n2 < 0 || n2 >= ctx->n) return bad(ctx, PEEC_ERR_BADARG, "port node out of range");
+  cudaSetDevice(ctx->dev);
+  const int64_t m = ctx->m, ns = ctx->ns, n = ctx->n;
+  std::vector<c64> is(n, mk<double>(0, 0));
+  is[n1] = mk<double>(Is, 0);
+  is[n2] = mk<double>(-Is, 0);
+  PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->tvec, is.data(), sizeof(c64) * n, cudaMemcpyHostToDevice, ctx->st));
+  lu_solve(ctx, ctx->tvec, ctx->Mvec);
+  // Y1 = Y2 = 0 gives y1 = -invZ*A*M, y2 = invP*Gamma'*M, y3 = M
+  PEEC_CUDA_TRY(cudaMemsetAsync(ctx->Y1, 0, sizeof(c64) * (m > 0 ? m : 1), ctx->st));
+  PEEC_CUDA_TRY(cudaMemsetAsync(ctx->Y2, 0, sizeof(c64) * (ns > 0 ? ns : 1), ctx->st));
+  launch_final_rows(ctx->Y1, ctx->Y2, ctx->Mvec, ctx->DZ, ctx->n1, ctx->n2, ctx->snode, ctx->invP,
+                    (int)m, (int)ns, (int)n, ctx->dy, ctx->st);
+  ctx->launches++;
+  PEEC_CUDA_TRY(cudaMemcpyAsync(tn, ctx->dy, sizeof(c64) * ctx->N, cudaMemcpyDeviceToHost, ctx->st));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return PEEC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Householder GMRES (gmres_custom.jl:1-331) on device vectors
+// ------------------------------------------------------------------------------------
+
+static int ensure_krylov(peec_ctx* ctx, int k) {
+  if (ctx->kcap >= k && ctx->U) return PEEC_OK;
+  const size_t N = ctx->N;
+  CTX_TRY(dalloc(&ctx->U, N * (size_t)k));
+  for (c64** p : {&ctx->gb, &ctx->gx, &ctx->gr, &ctx->gv, &ctx->gw, &ctx->gxm, &ctx->gxmin,
+                  &ctx->gtmp, &ctx->gzero})
+    CTX_TRY(dalloc(p, N));
+  PEEC_CUDA_TRY(cudaMemsetAsync(ctx->gzero, 0, sizeof(c64) * N, ctx->st));
+  CTX_TRY(dalloc(&ctx->dcoef, 2 * (size_t)k + 16));  // apply_Q stages 2k coefficients
+  CTX_TRY(dalloc(&ctx->dcoef2, 2 * (size_t)k + 16));
+  const int nb = red_blocks(N);
+  CTX_TRY(dalloc(&ctx->dpart, (size_t)nb * (k + 8)));
+  CTX_TRY(dalloc(&ctx->dred, nb + 8));
+  CTX_TRY(dalloc(&ctx->dscal, 16));
+  ctx->kcap = k;
+  return PEEC_OK;
+}
+
+namespace {
+
+struct Gm {
+  peec_ctx* ctx;
+  size_t N;
+  int prec;
+  cudaStream_t st;
+  int rc = PEEC_OK;
+
+  double norm(const c64* v, size_t i0 = 0) {
+    launch_norm2(v, N, i0, ctx->dred, ctx->dscal, st);
+    ctx->launches += 2;
+    cudaMemcpyAsync(ctx->hscal, ctx->dscal, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) rc = fail_cuda(cudaGetLastError(), "norm", __FILE__, __LINE__);
+    return std::sqrt(ctx->hscal[0]);
+  }
+  void matvec(const c64* x, c64* y) {
+    if (rc == PEEC_OK) rc = matvec_dev(ctx, x, y, prec, false);
+  }
+  // out = b - A x
+  void residual(const c64* b, const c64* x, c64* out) {
+    matvec(x, ctx->gtmp);
+    launch_sub(b, ctx->gtmp, N, out, st);
+    ctx->launches++;
+  }
+  void copy(c64* dst, const c64* src) {
+    cudaMemcpyAsync(dst, src, sizeof(c64) * N, cudaMemcpyDeviceToDevice, st);
+  }
+  void to_dev(c64* d, const std::vector<cd>& h) {
+    for (size_t i = 0; i < h.size(); ++i) ctx->hsmall[i] = mk<double>(h[i].real(), h[i].imag());
+    cudaMemcpyAsync(d, ctx->hsmall, sizeof(c64) * h.size(), cudaMemcpyHostToDevice, st);
+    cudaStreamSynchronize(st);  // hsmall is reused
+  }
+  std::vector<cd> from_dev(const c64* d, size_t cnt) {
+    cudaMemcpyAsync(ctx->hsmall, d, sizeof(c64) * cnt, cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) rc = fail_cuda(cudaGetLastError(), "d2h", __FILE__, __LINE__);
+    std::vector<cd> h(cnt);
+    for (size_t i = 0; i < cnt; ++i) h[i] = cd(ctx->hsmall[i].x, ctx->hsmall[i].y);
+    return h;
+  }
+};
+
+cd sgn(cd d) {
+  if (d == cd(0.0, 0.0)) return cd(1.0, 0.0);
+  return d / std::abs(d);
+}
+
+// solve upper-triangular R(0:k,0:k) y = rhs (R column-major with leading dim ld)
+std::vector<cd> utri_solve(const std::vector<cd>& R, int ld, int k, std::vector<cd> rhs) {
+  for (int i = k - 1; i >= 0; --i) {
+    cd s = rhs[i];
+    for (int j = i + 1; j < k; ++j) s -= R[(size_t)j * ld + i] * rhs[j];
+    rhs[i] = s / R[(size_t)i * ld + i];
+  }
+  return rhs;
+}
+
+}  // namespace
+
+// Q_k y applied on device: out = [y;0] - U(:,0:k) (T_k (Utop(0:k,0:k)^H y)) (+ base)
+static void apply_Q(Gm& g, const std::vector<cd>& T, const std::vector<cd>& Utop, int ldt, int k,
+                    const std::vector<cd>& y, const c64* base, c64* out) {
+  std::vector<cd> h(k), c(k);
+  for (int col = 0; col < k; ++col) {
+    cd s = 0;
+    for (int row = 0; row < k; ++row) s += std::conj(Utop[(size_t)col * ldt + row]) * y[row];
+    h[col] = s;
+  }
+  for (int i = 0; i < k; ++i) {
+    cd s = 0;
+    for (int j = i; j < k; ++j) s += T[(size_t)j * ldt + i] * h[j];
+    c[i] = s;
+  }
+  std::vector<cd> both(c);
+  both.insert(both.end(), y.begin(), y.begin() + k);
+  g.to_dev(g.ctx->dcoef, both);
+  launch_xupdate(base ? base : g.ctx->gzero, g.ctx->U, g.N, g.ctx->dcoef, g.ctx->dcoef + k, k, g.N,
+                 out, g.st);
+  g.ctx->launches++;
+}
+
+static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, int maxit,
+                     int restarted, int restart, int prec, int* flag_out, double* relres_out,
+                     int* iter_out, std::vector<double>& resvec_out) {
+  const size_t N = ctx->N;
+  int n = (int)N;
+  int outer, inner;
+  if (restarted) {
+    outer = maxit;
+    inner = std::min(restart, n);
+  } else {
+    outer = 1;
+    if (maxit > n) maxit = n;
+    inner = maxit;
+  }
+  if (inner < 1) inner = 1;
+  if (2 * (inner + 1) > 4096) return bad(ctx, PEEC_ERR_UNSUPPORTED, "inner iterations above 2047");
+  CTX_TRY(ensure_krylov(ctx, inner + 1));
+  Gm g{ctx, N, prec, ctx->st};
+  c64 *b = ctx->gb, *x = ctx->gx, *r = ctx->gr, *v = ctx->gv, *xm = ctx->gxm,
+      *xmin = ctx->gxmin, *add = ctx->gw;
+  g.copy(b, b_dev);
+  g.copy(x, x_dev);
+  const double n2b = g.norm(b);
+  if (g.rc) return g.rc;
+  if (n2b == 0) {
+    cudaMemsetAsync(x_dev, 0, sizeof(c64) * N, ctx->st);
+    cudaStreamSynchronize(ctx->st);
+    *flag_out = 0; *relres_out = 0; iter_out[0] = iter_out[1] = 0;
+    resvec_out.assign(1, 0.0);
+    return PEEC_OK;
+  }
+  int flag = 1;
+  g.copy(xmin, x);
+  int imin = 0, jmin = 0;
+  double tolb = tol * n2b;
+  g.copy(xm, x);
+  int evalxm = 0, stag = 0, moresteps = 0;
+  const int maxmsteps = std::min(std::min(n / 50, 5), n - maxit);
+  const int maxstagsteps = 3;
+  int minupdated = 0;
+  g.residual(b, x, r);
+  double normr = g.norm(r);
+  if (g.rc) return g.rc;
+  if (normr <= tolb) {
+    *flag_out = 0; *relres_out = normr / n2b; iter_out[0] = iter_out[1] = 0;
+    resvec_out.assign(1, normr);
+    return PEEC_OK;
+  }
+  const double n2minv_b = n2b;
+  tolb = tol * n2minv_b;
+  std::vector<double> resvec((size_t)inner * outer + 1, 0.0);
+  resvec[0] = normr;
+  double normrmin = normr;
+  const int ld = inner + 1;
+  std::vector<cd> J(2 * (size_t)inner), R((size_t)inner * inner), wv(inner + 1);
+  std::vector<cd> T((size_t)ld * ld), Utop((size_t)ld * ld);
+  int outitercount = 0, initercount = 0;
+  double normr_act = normr;
+  int it0 = 0, it1 = 0;
+  const int headlen = (int)std::min<size_t>(N, (size_t)ld);
+  for (int outiter = 1; outiter <= outer; ++outiter) {
+    outitercount++;
+    std::fill(T.begin(), T.end(), cd(0));
+    std::fill(Utop.begin(), Utop.end(), cd(0));
+    // u = r + sign(r1)*norm(r)*e1, normalised (later restart cycles use the true
+    // residual norm of the end-of-cycle residual)
+    if (outiter > 1) normr = g.norm(r);
+    {
+      const std::vector<cd> rh = g.from_dev(r, 1);
+      const cd beta = sgn(rh[0]) * normr;
+      const double nu2 = normr * normr - std::norm(rh[0]) + std::norm(rh[0] + beta);
+      launch_make_reflector(r, N, 0, mk<double>(beta.real(), beta.imag()), 1.0 / std::sqrt(nu2),
+                            ctx->U, ctx->st);
+      ctx->launches++;
+      const std::vector<cd> uh = g.from_dev(ctx->U, headlen);
+      for (int i = 0; i < headlen; ++i) Utop[i] = uh[i];
+      T[0] = 2.0;
+      wv.assign(inner + 1, cd(0));
+      wv[0] = -beta;
+    }
+    initercount = 0;
+    for (int initer = 1; initer <= inner; ++initer) {
+      if (ctx->stop && *ctx->stop) {
+        *flag_out = 99; *relres_out = 0; iter_out[0] = outiter; iter_out[1] = initer;
+        resvec_out.assign(1, 0.0);
+        return PEEC_ERR_CANCELLED;
+      }
+      initercount++;
+      const int j = initer - 1;
+      // v = P1..Pj e_j = e_j - U T conj(Utop(j,0:j+1))
+      {
+        const int k = initer;
+        std::vector<cd> rb(k), c(k);
+        for (int col = 0; col < k; ++col) rb[col] = std::conj(Utop[(size_t)col * ld + j]);
+        for (int i = 0; i < k; ++i) {
+          cd s = 0;
+          for (int jj = i; jj < k; ++jj) s += T[(size_t)jj * ld + i] * rb[jj];
+          c[i] = s;
+        }
+        g.to_dev(ctx->dcoef, c);
+        launch_multiaxpy(ctx->U, N, nullptr, j, ctx->dcoef, k, N, v, N, nullptr, ctx->st);
+        launch_norm2(v, N, 0, ctx->dred, ctx->dscal, ctx->st);
+        launch_scale_rnorm(v, N, ctx->dscal, ctx->st);
+        ctx->launches += 4;
+      }
+      g.matvec(v, add);  // add <- A v
+      if (g.rc) return g.rc;
+      // v = Pj..P1 A v = (I - U T^H U^H) A v, with the tail norm from index initer
+      double alpha2 = 0.0;
+      std::vector<cd> vh;
+      {
+        const int k = initer;
+        launch_multidot(ctx->U, N, add, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
+        ctx->launches += 2;
+        std::vector<cd> z = g.from_dev(ctx->dcoef2, k);
+        std::vector<cd> c(k);
+        for (int i = 0; i < k; ++i) {  // T^H z
+          cd s = 0;
+          for (int jj = 0; jj <= i; ++jj) s += std::conj(T[(size_t)i * ld + jj]) * z[jj];
+          c[i] = s;
+        }
+        g.to_dev(ctx->dcoef, c);
+        launch_multiaxpy(ctx->U, N, add, 0, ctx->dcoef, k, N, v, (size_t)initer, ctx->dred,
+                         ctx->st);
+        launch_sum_parts(ctx->dred, red_blocks(N), ctx->dscal, ctx->st);
+        ctx->launches += 2;
+        cudaMemcpyAsync(ctx->hscal, ctx->dscal, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+        vh = g.from_dev(v, headlen);
+        alpha2 = ctx->hscal[0];
+        if (g.rc) return g.rc;
+      }
+      std::vector<cd> vs(inner + 1, cd(0));
+      for (int i = 0; i < std::min(inner + 1, headlen); ++i) vs[i] = vh[i];
+      if (initer != n) {
+        double alpha = std::sqrt(alpha2);
+        if (alpha != 0) {
+          const cd vj1 = vh[initer];
+          const cd a = sgn(vj1) * alpha;
+          const double nu2 = alpha2 - std::norm(vj1) + std::norm(vj1 + a);
+          launch_make_reflector(v, N, initer, mk<double>(a.real(), a.imag()),
+                                1.0 / std::sqrt(nu2), ctx->U + (size_t)initer * N, ctx->st);
+          ctx->launches++;
+          const std::vector<cd> uh = g.from_dev(ctx->U + (size_t)initer * N, headlen);
+          for (int i = 0; i < headlen; ++i) Utop[(size_t)initer * ld + i] = uh[i];
+          // T(0:k, k) = -2 T(0:k,0:k) (U(:,0:k)^H u_k), T(k,k) = 2
+          const int k = initer;
+          launch_multidot(ctx->U, N, ctx->U + (size_t)initer * N, N, k, ctx->dpart, ctx->dcoef2,
+                          ctx->st);
+          ctx->launches += 2;
+          const std::vector<cd> gg = g.from_dev(ctx->dcoef2, k);
+          for (int i = 0; i < k; ++i) {
+            cd s = 0;
+            for (int jj = i; jj < k; ++jj) s += T[(size_t)jj * ld + i] * gg[jj];
+            T[(size_t)k * ld + i] = -2.0 * s;
+          }
+          T[(size_t)k * ld + k] = 2.0;
+          for (int i = initer + 1; i <= inner; ++i) vs[i] = 0;
+          vs[initer] = -a;
+        }
+      }
+      // Givens
+      for (int colJ = 0; colJ < initer - 1; ++colJ) {
+        const cd tmpv = vs[colJ];
+        vs[colJ] = std::conj(J[2 * colJ]) * vs[colJ] + std::conj(J[2 * colJ + 1]) * vs[colJ + 1];
+        vs[colJ + 1] = -J[2 * colJ + 1] * tmpv + J[2 * colJ] * vs[colJ + 1];
+      }
+      if (initer != n) {
+        const double rho = std::sqrt(std::norm(vs[j]) + std::norm(vs[j + 1]));
+        J[2 * j] = vs[j] / rho;
+        J[2 * j + 1] = vs[j + 1] / rho;
+        wv[j + 1] = -J[2 * j + 1] * wv[j];
+        wv[j] = std::conj(J[2 * j]) * wv[j];
+        vs[j] = rho;
+        vs[j + 1] = 0;
+      }
+      for (int i = 0; i < inner; ++i) R[(size_t)j * inner + i] = vs[i];
+      normr = std::abs(wv[j + 1]);
+      resvec[(size_t)(outiter - 1) * inner + initer] = normr;
+      normr_act = normr;
+      if (normr <= tolb || stag >= maxstagsteps || moresteps == 1) {
+        if (evalxm == 0) {
+          std::vector<cd> rhs(wv.begin(), wv.begin() + initer);
+          std::vector<cd> ytmp = utri_solve(R, inner, initer, rhs);
+          apply_Q(g, T, Utop, ld, initer, ytmp, nullptr, add);
+          const double na = g.norm(add), nx = g.norm(x);
+          if (na < 2.220446049250313e-16 * nx) stag++;
+          else stag = 0;
+          // xm = x + additive
+          apply_Q(g, T, Utop, ld, initer, ytmp, x, xm);
+          evalxm = 1;
+        } else {
+          const cd wr = wv[j] / R[(size_t)j * inner + j];
+          std::vector<cd> addvc(initer);
+          if (initer > 1) {
+            std::vector<cd> rhs(initer - 1);
+            for (int i = 0; i < initer - 1; ++i) rhs[i] = R[(size_t)j * inner + i];
+            std::vector<cd> hsol = utri_solve(R, inner, initer - 1, rhs);
+            for (int i = 0; i < initer - 1; ++i) addvc[i] = -hsol[i] * wr;
+          }
+          addvc[initer - 1] = wr;
+          double nav = 0;
+          for (auto& q : addvc) nav += std::norm(q);
+          nav = std::sqrt(nav);
+          const double nxm = g.norm(xm);
+          if (nav < 2.220446049250313e-16 * nxm) stag++;
+          else stag = 0;
+          g.copy(ctx->gtmp, xm);
+          apply_Q(g, T, Utop, ld, initer, addvc, ctx->gtmp, xm);
+        }
+        g.residual(b, xm, r);
+        const double nr = g.norm(r);
+        if (g.rc) return g.rc;
+        if (nr <= tol * n2b) {
+          g.copy(x, xm);
+          flag = 0;
+          it0 = outiter;
+          it1 = initer;
+          break;
+        }
+        normr_act = nr;
+        resvec[(size_t)(outiter - 1) * inner + initer] = normr_act;
+        if (normr_act <= normrmin) {
+          normrmin = normr_act;
+          imin = outiter;
+          jmin = initer;
+          g.copy(xmin, xm);
+          minupdated = 1;
+        }
+        if (normr_act <= tolb) {
+          g.copy(x, xm);
+          flag = 0;
+          it0 = outiter;
+          it1 = initer;
+          break;
+        } else {
+          if (stag >= maxstagsteps && moresteps == 0) stag = 0;
+          moresteps++;
+          if (moresteps >= maxmsteps) {
+            flag = 3;
+            it0 = outiter;
+            it1 = initer;
+            break;
+          }
+        }
+      }
+      if (normr_act <= normrmin) {
+        normrmin = normr_act;
+        imin = outiter;
+        jmin = initer;
+        minupdated = 1;
+      }
+      if (stag >= maxstagsteps) {
+        flag = 3;
+        break;
+      }
+    }
+    evalxm = 0;
+    if (flag != 0) {
+      const int idx = minupdated == 1 ? jmin : initercount;
+      if (idx > 0) {
+        std::vector<cd> rhs(wv.begin(), wv.begin() + idx);
+        std::vector<cd> y = utri_solve(R, inner, idx, rhs);
+        g.copy(ctx->gtmp, x);
+        apply_Q(g, T, Utop, ld, idx, y, ctx->gtmp, x);
+      }
+      g.copy(xmin, x);
+      g.residual(b, x, r);
+      normr_act = g.norm(r);
+      if (g.rc) return g.rc;
+    }
+    if (normr_act <= normrmin) {
+      g.copy(xmin, x);
+      normrmin = normr_act;
+      imin = outiter;
+      jmin = initercount;
+    }
+    if (flag == 3) break;
+    if (normr_act <= tolb) {
+      flag = 0;
+      it0 = outitercount;
+      it1 = initercount;
+      break;
+    }
+    minupdated = 0;
+  }
+  double relres;
+  if (flag == 0) {
+    relres = normr_act / n2minv_b;
+    g.copy(x_dev, x);
+  } else {
+    g.copy(x_dev, xmin);
+    it0 = imin;
+    it1 = jmin;
+    relres = normr_act / n2minv_b;
+  }
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  const size_t nres = (size_t)std::max(outitercount - 1, 0) * inner + initercount + 1;
+  resvec_out.assign(resvec.begin(), resvec.begin() + std::min(nres, resvec.size()));
+  *flag_out = flag;
+  *relres_out = relres;
+  iter_out[0] = it0;
+  iter_out[1] = it1;
+  return g.rc;
+}
+
+extern "C" int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, double tol, int maxit,
+                          int restarted, int restart, int precision, int* flag, double* relres,
+                          int* iter, double* resvec, int resvec_cap, int* nres) {
+  if (!ctx || !b || !x_inout || !flag || !relres || !iter) return PEEC_ERR_BADARG;
+  if (maxit < 1 || (restarted && restart < 1)) return bad(ctx, PEEC_ERR_BADARG, "maxit/restart must be >= 1");
+  if (precision != 0 && precision != 1) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0 or 1");
+  if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
+  cudaSetDevice(ctx->dev);
+  const size_t bytes = sizeof(c64) * ctx->N;
+  PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->dx, b, bytes, cudaMemcpyHostToDevice, ctx->st));
+  PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->dy, x_inout, bytes, cudaMemcpyHostToDevice, ctx->st));
+  std::vector<double> rv;
+  int rc = gmres_run(ctx, ctx->dx, ctx->dy, tol, maxit, restarted, restart, precision, flag,
+                     relres, iter, rv);
+  if (rc != PEEC_OK && rc != PEEC_ERR_CANCELLED) return rc;
+  if (rc == PEEC_OK)
+    PEEC_CUDA_TRY(cudaMemcpyAsync(x_inout, ctx->dy, bytes, cudaMemcpyDeviceToHost, ctx->st));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  if (nres) *nres = (int)rv.size();
+  if (resvec)
+    for (int i = 0; i < (int)rv.size() && i < resvec_cap; ++i) resvec[i] = rv[i];
+  if (rc == PEEC_ERR_CANCELLED) ctx->err = "cancelled by stop flag";
+  return rc;
+}
+
+extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout, double tol,
+                                double inner_tol, int inner_maxit, int max_outer, int* flag,
+                                double* relres, int* outer_out, int* inner_total) {
+  if (!ctx || !b || !x_inout || !flag || !relres) return PEEC_ERR_BADARG;
+  if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
+  cudaSetDevice(ctx->dev);
+  const size_t N = ctx->N, bytes = sizeof(c64) * N;
+  c64 *db = nullptr, *dxv = nullptr, *dr = nullptr, *dd = nullptr;
+  PEEC_CUDA_TRY(cudaMalloc(&db, bytes));
+  PEEC_CUDA_TRY(cudaMalloc(&dxv, bytes));
+  PEEC_CUDA_TRY(cudaMalloc(&dr, bytes));
+  PEEC_CUDA_TRY(cudaMalloc(&dd, bytes));
+  auto cleanup = [&]() {
+    cudaFree(db); cudaFree(dxv); cudaFree(dr); cudaFree(dd);
+  };
+  {
+    int rc = ensure_krylov(ctx, std::max(inner_maxit, 1) + 1);
+    if (rc) { cleanup(); return rc; }
+  }
+  cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, ctx->st);
+  cudaMemcpyAsync(dxv, x_inout, bytes, cudaMemcpyHostToDevice, ctx->st);
+  Gm g{ctx, N, 0, ctx->st};
+  const double n2b = g.norm(db);
+  int outer = 0, tot_inner = 0, fl = 1;
+  double rel = 0;
+  if (n2b == 0) {
+    cudaMemsetAsync(dxv, 0, bytes, ctx->st);
+    fl = 0;
+  } else {
+    for (outer = 0; outer <= max_outer; ++outer) {
+      g.residual(db, dxv, dr);  // FP64 operator
+      const double nr = g.norm(dr);
+      if (g.rc) { cleanup(); return g.rc; }
+      rel = nr / n2b;
+      if (rel <= tol) { fl = 0; break; }
+      if (outer == max_outer) break;
+      if (ctx->stop && *ctx->stop) { cleanup(); ctx->err = "cancelled by stop flag"; *flag = 99; return PEEC_ERR_CANCELLED; }
+      // inner correction on the FP32-convolution operator, zero initial guess
+      cudaMemsetAsync(dd, 0, bytes, ctx->st);
+      const double itol = std::max(inner_tol, 0.5 * tol / rel);
+      int ifl, it[2];
+      double irel;
+      std::vector<double> rv;
+      int rc = gmres_run(ctx, dr, dd, std::min(itol, 0.5), inner_maxit, 0, 0, 1, &ifl, &irel, it, rv);
+      if (rc) { cleanup(); return rc; }
+      tot_inner += (int)rv.size() - 1;
+      launch_add(dxv, dd, N, dxv, ctx->st);  // x += d
+      ctx->launches++;
+    }
+  }
+  cudaMemcpyAsync(x_inout, dxv, bytes, cudaMemcpyDeviceToHost, ctx->st);
+  cudaStreamSynchronize(ctx->st);
+  cleanup();
+  *flag = fl;
+  *relres = rel;
+  if (outer_out) *outer_out = outer;
+  if (inner_total) *inner_total = tot_inner;
+  return PEEC_OK;
+}

@@ -1,0 +1,254 @@
+// Vector kernels of the Householder GMRES (compact-WY form).
+//
+// The reflector basis U (N x kmax, column-major, complex double) is applied with
+// two passes per application instead of the reference's one dot+axpy per
+// reflector (gmres_custom.jl:112-127): a multi-dot z = U(:,0:k)^H v, a small
+// triangular product on the host, and a multi-axpy v -= U(:,0:k) c. Reductions
+// are deterministic: warp-shuffle partials per CTA, then a fixed-order sum.
+#include "ctx.hpp"
+
+namespace peec {
+
+constexpr int KB = 8;        // columns per multi-dot tile
+constexpr int RED_TPB = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// partial[blk][c] (complex) = sum over the CTA's rows of conj(U[i,c0+c]) * v[i]
+__global__ void __launch_bounds__(RED_TPB) k_multidot(const c64* __restrict__ U, size_t ldu,
+                                                      const c64* __restrict__ v, size_t N,
+                                                      int k, c64* partial) {
+  __shared__ double red[RED_TPB / 32][2 * KB];
+  const int c0 = blockIdx.y * KB;
+  const int nc = min(KB, k - c0);
+  double ar[KB], ai[KB];
+#pragma unroll
+  for (int c = 0; c < KB; ++c) ar[c] = ai[c] = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const c64 x = v[i];
+#pragma unroll
+    for (int c = 0; c < KB; ++c) {
+      if (c < nc) {
+        const c64 u = U[(size_t)(c0 + c) * ldu + i];
+        ar[c] += u.x * x.x + u.y * x.y;
+        ai[c] += u.x * x.y - u.y * x.x;
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < KB; ++c) {
+    const double sr = warp_sum(ar[c]), si = warp_sum(ai[c]);
+    if (lane == 0) {
+      red[wid][2 * c] = sr;
+      red[wid][2 * c + 1] = si;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 * KB) {
+    double s = 0.0;
+    for (int w = 0; w < RED_TPB / 32; ++w) s += red[w][threadIdx.x];
+    const int c = threadIdx.x >> 1;
+    if (c < nc) {
+      double* p = reinterpret_cast<double*>(partial + (size_t)blockIdx.x * k + c0 + c);
+      p[threadIdx.x & 1] = s;
+    }
+  }
+}
+
+// out[c] = sum_b partial[b][c]  (fixed order)
+__global__ void k_reduce_cols(const c64* __restrict__ partial, int nblk, int k, c64* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= k) return;
+  c64 s = mk<double>(0, 0);
+  for (int b = 0; b < nblk; ++b) s = s + partial[(size_t)b * k + c];
+  out[c] = s;
+}
+
+// v[i] = base[i] (or e_unit) - sum_c U[i,c]*coef[c];  optional tail |v|^2 partials for i >= tail0
+__global__ void __launch_bounds__(RED_TPB) k_multiaxpy(const c64* __restrict__ U, size_t ldu,
+                                                       const c64* __restrict__ base, int unit,
+                                                       const c64* __restrict__ coef, int k,
+                                                       size_t N, c64* out, size_t tail0,
+                                                       double* tailpart) {
+  extern __shared__ c64 sc[];
+  for (int c = threadIdx.x; c < k; c += blockDim.x) sc[c] = coef[c];
+  __syncthreads();
+  double acc = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    c64 x;
+    if (base) x = base[i];
+    else x = mk<double>(i == (size_t)unit ? 1.0 : 0.0, 0.0);
+    for (int c = 0; c < k; ++c) x = x - U[(size_t)c * ldu + i] * sc[c];
+    out[i] = x;
+    if (i >= tail0) acc += x.x * x.x + x.y * x.y;
+  }
+  if (tailpart) {
+    __shared__ double red[RED_TPB / 32];
+    acc = warp_sum(acc);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int w = 0; w < RED_TPB / 32; ++w) s += red[w];
+      tailpart[blockIdx.x] = s;
+    }
+  }
+}
+
+// partial sums of |v[i]|^2 for i >= i0
+__global__ void __launch_bounds__(RED_TPB) k_norm2(const c64* __restrict__ v, size_t N, size_t i0,
+                                                   double* part) {
+  __shared__ double red[RED_TPB / 32];
+  double acc = 0.0;
+  for (size_t i = i0 + blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const c64 x = v[i];
+    acc += x.x * x.x + x.y * x.y;
+  }
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < RED_TPB / 32; ++w) s += red[w];
+    part[blockIdx.x] = s;
+  }
+}
+
+// s = sum part[0..nb); optionally v *= 1/sqrt(s) on device (no host round trip)
+__global__ void k_sum_parts(const double* __restrict__ part, int nb, double* out) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) acc += part[b];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+    s = warp_sum(s);
+    if (threadIdx.x == 0) *out = s;
+  }
+}
+
+__global__ void k_scale_by_rnorm(c64* v, size_t N, const double* __restrict__ ss) {
+  const double inv = 1.0 / sqrt(*ss);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x)
+    v[i] = cscale(v[i], inv);
+}
+
+// new reflector column: u = (w with entries [0,j) zeroed, w[j] += add) * scale
+__global__ void k_make_reflector(const c64* __restrict__ w, size_t N, int j, c64 add,
+                                 double scale, c64* u) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    c64 x = (i < (size_t)j) ? mk<double>(0, 0) : w[i];
+    if (i == (size_t)j) x = x + add;
+    u[i] = cscale(x, scale);
+  }
+}
+
+// out = a - b
+__global__ void k_sub(const c64* __restrict__ a, const c64* __restrict__ b, size_t N, c64* out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = a[i] - b[i];
+}
+
+// out = x + y_pad - sum_c U[i,c] coef[c] where y_pad holds ny leading entries
+__global__ void k_xupdate(const c64* __restrict__ x, const c64* __restrict__ U, size_t ldu,
+                          const c64* __restrict__ coef, const c64* __restrict__ ypad, int k,
+                          size_t N, c64* out) {
+  extern __shared__ c64 sc2[];
+  for (int c = threadIdx.x; c < 2 * k; c += blockDim.x) sc2[c] = c < k ? coef[c] : ypad[c - k];
+  __syncthreads();
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    c64 v = x[i];
+    if (i < (size_t)k) v = v + sc2[k + i];
+    for (int c = 0; c < k; ++c) v = v - U[(size_t)c * ldu + i] * sc2[c];
+    out[i] = v;
+  }
+}
+
+__global__ void k_add(const c64* __restrict__ a, const c64* __restrict__ b, size_t N, c64* out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = a[i] + b[i];
+}
+
+__global__ void k_cast_down(const c64* __restrict__ a, size_t N, c32* out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = ccast<float>(a[i]);
+}
+
+// ------------------------------- launchers ----------------------------------------
+
+static inline unsigned g_stream(size_t n) {
+  size_t g = (n + 255) / 256;
+  if (g > 152 * 8) g = 152 * 8;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+int red_blocks(size_t N) { return (int)g_stream(N); }
+
+void launch_multidot(const c64* U, size_t ldu, const c64* v, size_t N, int k, c64* partial,
+                     c64* out, cudaStream_t st) {
+  if (k <= 0) return;
+  const unsigned nb = g_stream(N);
+  dim3 g(nb, (k + KB - 1) / KB);
+  k_multidot<<<g, RED_TPB, 0, st>>>(U, ldu, v, N, k, partial);
+  k_reduce_cols<<<(k + 127) / 128, 128, 0, st>>>(partial, nb, k, out);
+}
+
+void launch_multiaxpy(const c64* U, size_t ldu, const c64* base, int unit, const c64* coef,
+                      int k, size_t N, c64* out, size_t tail0, double* tailpart,
+                      cudaStream_t st) {
+  const unsigned nb = g_stream(N);
+  k_multiaxpy<<<nb, RED_TPB, sizeof(c64) * (k > 0 ? k : 1), st>>>(U, ldu, base, unit, coef, k, N,
+                                                                   out, tail0, tailpart);
+}
+
+void launch_norm2(const c64* v, size_t N, size_t i0, double* part, double* out, cudaStream_t st) {
+  const unsigned nb = g_stream(N);
+  k_norm2<<<nb, RED_TPB, 0, st>>>(v, N, i0, part);
+  k_sum_parts<<<1, 1024, 0, st>>>(part, nb, out);
+}
+
+void launch_sum_parts(const double* part, int nb, double* out, cudaStream_t st) {
+  k_sum_parts<<<1, 1024, 0, st>>>(part, nb, out);
+}
+
+void launch_scale_rnorm(c64* v, size_t N, const double* ss, cudaStream_t st) {
+  k_scale_by_rnorm<<<g_stream(N), 256, 0, st>>>(v, N, ss);
+}
+
+void launch_make_reflector(const c64* w, size_t N, int j, c64 add, double scale, c64* u,
+                           cudaStream_t st) {
+  k_make_reflector<<<g_stream(N), 256, 0, st>>>(w, N, j, add, scale, u);
+}
+
+void launch_sub(const c64* a, const c64* b, size_t N, c64* out, cudaStream_t st) {
+  k_sub<<<g_stream(N), 256, 0, st>>>(a, b, N, out);
+}
+
+void launch_add(const c64* a, const c64* b, size_t N, c64* out, cudaStream_t st) {
+  k_add<<<g_stream(N), 256, 0, st>>>(a, b, N, out);
+}
+
+void launch_xupdate(const c64* x, const c64* U, size_t ldu, const c64* coef, const c64* ypad,
+                    int k, size_t N, c64* out, cudaStream_t st) {
+  k_xupdate<<<g_stream(N), 256, sizeof(c64) * 2 * (k > 0 ? k : 1), st>>>(x, U, ldu, coef, ypad, k,
+                                                                        N, out);
+}
+
+}  // namespace peec

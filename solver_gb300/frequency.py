@@ -1,0 +1,102 @@
+"""Per-frequency host setup of the operator (FFT_solver_QS_S_type.jl:105-119).
+
+Builds, for scaled angular frequency w, the diagonal DZ, the termination/lumped
+admittance Yle, and the sparse LU factorisation of the node Schur complement
+    SS = Yle + A' diag(1/DZ) A + jw Gamma diag(1/P) Gamma'
+on the host (SuperLU via scipy), as the reference factorises with UMFPACK on the host.
+The factors are exported in the CSR form the GPU triangular solves consume.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+
+def z_self(R, Cd, w):
+    """Sum over the four edge halves of 1/(1/R + jwCd) (compute_Z_self.jl:1-15)."""
+    Z = np.zeros(R.shape[0], dtype=np.complex128)
+    for aux in range(4):
+        r, cd = R[:, aux], Cd[:, aux]
+        rc = (r != 0) & (cd != 0)
+        ro = (r != 0) & (cd == 0)
+        co = (r == 0) & (cd != 0)
+        Z[rc] += 1.0 / (1.0 / r[rc] + 1j * w * cd[rc])
+        Z[ro] += r[ro]
+        Z[co] += 1.0 / (1j * w * cd[co])
+    return Z
+
+
+def lumped_admittance(typ, R, L, C, w):
+    """Type-1 (series RLC) element admittance (build_Yle_FFT.jl:128-136)."""
+    if typ != 1:
+        raise NotImplementedError(f"lumped element type {typ} is not supported")
+    with np.errstate(all="ignore"):
+        z = complex(R + 1j * w * L) + (1 / (1j * w * C) if C != 0 else complex("inf"))
+        if not np.isfinite(z) or abs(z) < 1e-16:
+            z = complex(R + 1j * w * L)
+        y = 1 / z if z != 0 else complex("inf")
+    return y if np.isfinite(y) else 0.0
+
+
+def yle_matrix(lumped_elements, ports, n, w_real, z0, escal_yle):
+    """Sparse n x n admittance of port terminations (1/Z0) and lumped elements
+    (build_Yle_FFT.jl:1-126), escaled."""
+    rows, cols, vals = [], [], []
+
+    def stamp(a, b, y):
+        rows.extend((a, b, a, b))
+        cols.extend((a, b, b, a))
+        vals.extend((y, y, -y, -y))
+
+    le = lumped_elements
+    for k in range(len(le.get("le_nodes", []))):
+        y = lumped_admittance(int(le["type"][k]), float(le["R_value"][k]), float(le["L_value"][k]),
+                              float(le["C_value"][k]), w_real)
+        stamp(int(le["le_nodes"][k][0]), int(le["le_nodes"][k][1]), y)
+    for a, b in np.asarray(ports["port_nodes"], dtype=np.int64):
+        stamp(int(a), int(b), 1.0 / z0)
+    return sp.coo_matrix((np.asarray(vals, dtype=np.complex128) * escal_yle, (rows, cols)),
+                         shape=(n, n)).tocsr()
+
+
+class FrequencyState:
+    """DZ, Yle and the factorised SS at one frequency."""
+
+    def __init__(self, w, escalings, incidence_selection, diagonals, Zs_info, lumped_elements,
+                 ports, z0):
+        A = incidence_selection["A"]
+        Gamma = incidence_selection["Gamma"]
+        n = A.shape[1]
+        self.w = w
+        self.Yle = yle_matrix(lumped_elements, ports, n, w / escalings["freq"], z0,
+                              escalings["Yle"])
+        Zself = z_self(diagonals["R"], diagonals["Cd"], w)
+        Zs = escalings["R"] * (np.asarray(Zs_info["Zs"]).ravel() * math.sqrt(w / escalings["freq"]))
+        se = np.asarray(Zs_info["surface_edges"], dtype=np.int64)
+        d = Zs[se].real - Zself[se].real
+        Zself[se[d > 0]] = 1j * Zself[se[d > 0]].imag
+        Zs = Zs.copy()
+        Zs[se[d < 0]] = 1j * Zs[se[d < 0]].imag
+        self.DZ = Zself + Zs.real + 1j * w * np.asarray(diagonals["Lp"]).ravel()
+        self.invZ = sp.diags(1.0 / self.DZ)
+        self.invP = sp.diags(1.0 / np.asarray(diagonals["P"]).ravel())
+        SS = (self.Yle + A.T @ (self.invZ @ A) + 1j * w * ((Gamma @ self.invP) @ Gamma.T)).tocsc()
+        self.SS = SS
+        self.lu = spla.splu(SS, permc_spec="COLAMD", options={"Equil": False})
+
+
+def export_lu(lu):
+    """CSR factors and permutations with Pr*SS*Pc = L*U from a SuperLU object."""
+    L = lu.L.tocsr()
+    U = lu.U.tocsr()
+    L.sort_indices()
+    U.sort_indices()
+
+    def parts(M):
+        return (M.indptr.astype(np.int64), M.indices.astype(np.int64),
+                np.ascontiguousarray(M.data.astype(np.complex128)).view(np.float64))
+
+    return parts(L), parts(U), lu.perm_r.astype(np.int64), lu.perm_c.astype(np.int64)

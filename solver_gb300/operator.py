@@ -1,0 +1,227 @@
+"""GPU operator: one geometry's circulant Lp/P operator and preconditioner on a GB300.
+
+Wraps a ``peec_ctx`` (include/peec_gb300.h). Everything that touches vectors of
+length N = m + ns + n runs in the CUDA library; this class only converts the
+reference's host data structures into the C ABI's flat arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from .frequency import export_lu
+
+ROW_KEYS = ("Lpx", "Lpy", "Lpz", "p12_se", "p34_se", "p56_se", "p1234", "p1256", "p3456")
+
+
+def row_dims(Nx, Ny, Nz):
+    return {"Lpx": (Nx - 1, Ny, Nz), "Lpy": (Nx, Ny - 1, Nz), "Lpz": (Nx, Ny, Nz - 1),
+            "p12_se": (Nx, Ny + 1, Nz), "p34_se": (Nx + 1, Ny, Nz), "p56_se": (Nx, Ny, Nz + 1),
+            "p1234": (2 * Nx + 1, 2 * Ny + 1, Nz), "p1256": (Nx, 2 * Ny + 1, 2 * Nz + 1),
+            "p3456": (2 * Nx + 1, Ny, 2 * Nz + 1)}
+
+
+def _edge_cells(expansions, mx, my, mz):
+    """Lattice cell of every edge from mat_map_Lp[c][0] (one 1 per column)."""
+    if "edge_cell" in expansions:
+        return np.ascontiguousarray(expansions["edge_cell"], dtype=np.int64)
+    out = []
+    for c, mc in enumerate((mx, my, mz)):
+        M = expansions["mat_map_Lp"][c][0].tocsc()
+        if M.shape[1] != mc or np.any(np.diff(M.indptr) != 1):
+            raise ValueError("mat_map_Lp must hold exactly one 1 per edge column")
+        out.append(M.indices.astype(np.int64))
+    return np.concatenate(out)
+
+
+def _surf_cells(expansions, ns):
+    if "surf_cell" in expansions and "surf_fam" in expansions:
+        return (np.ascontiguousarray(expansions["surf_fam"], dtype=np.int32),
+                np.ascontiguousarray(expansions["surf_cell"], dtype=np.int64))
+    fam = np.full(ns, -1, dtype=np.int32)
+    cell = np.full(ns, -1, dtype=np.int64)
+    for f in range(3):
+        M = expansions["exp_P"][f][f].tocsc()
+        cols = np.nonzero(np.diff(M.indptr))[0]
+        if np.any(np.diff(M.indptr)[cols] != 1):
+            raise ValueError("exp_P[f][f] must hold at most one 1 per surface column")
+        fam[cols] = f
+        cell[cols] = M.indices[M.indptr[cols]]
+    if np.any(fam < 0):
+        raise ValueError("every surface must belong to one face family")
+    return fam, cell
+
+
+class GpuOperator:
+    """Device-resident PEEC operator for one geometry."""
+
+    def __init__(self, incidence_selection, expansions, diagP, grid=None, device=0):
+        self.L = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self.L.peec_ctx_create(ctypes.byref(h), device)
+        if rc != 0:
+            raise _lib.PeecError(rc, self.L.peec_last_error(None).decode())
+        self.h = h
+        A = incidence_selection["A"].tocsr()
+        Gamma = incidence_selection["Gamma"].tocsc()
+        self.m, self.n = A.shape
+        self.ns = Gamma.shape[1]
+        self.N = self.m + self.ns + self.n
+        mx, my, mz = (int(incidence_selection[k]) for k in ("mx", "my", "mz"))
+        if grid is None:
+            grid = expansions["grid"]
+        self.grid = tuple(int(v) for v in grid)
+        ecell = _edge_cells(expansions, mx, my, mz)
+        # A rows hold -1 at n1 and +1 at n2
+        n1 = np.empty(self.m, dtype=np.int64)
+        n2 = np.empty(self.m, dtype=np.int64)
+        for e0, e1 in ((0, self.m),):
+            ind, dat, ptr = A.indices, A.data, A.indptr
+            if np.any(np.diff(ptr) != 2):
+                raise ValueError("A must have two entries per edge row")
+            a = ind[ptr[:-1]]
+            b = ind[ptr[:-1] + 1]
+            va = dat[ptr[:-1]]
+            n1[:] = np.where(va < 0, a, b)
+            n2[:] = np.where(va < 0, b, a)
+        if np.any(np.diff(Gamma.indptr) != 1):
+            raise ValueError("Gamma must have one entry per surface column")
+        snode = Gamma.indices.astype(np.int64)
+        fam, scell = _surf_cells(expansions, self.ns)
+        Nx, Ny, Nz = self.grid
+        _lib.check(self.h, self.L.peec_set_topology(
+            self.h, Nx, Ny, Nz, mx, my, mz, _lib.ptr(ecell), _lib.ptr(n1), _lib.ptr(n2), self.ns,
+            _lib.ptr(fam), _lib.ptr(scell), _lib.ptr(snode), self.n))
+        dp = np.ascontiguousarray(np.asarray(diagP, dtype=np.float64).ravel())
+        _lib.check(self.h, self.L.peec_set_pdiag(self.h, _lib.ptr(dp)))
+        self._freq_key = None
+        self._stop = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.peec_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- circulant blocks ----------------------------------------------------------
+    def set_rows(self, rows: dict):
+        """Upload the nine generating rows (escaled, reference lattices, x fastest)."""
+        dims = row_dims(*self.grid)
+        keep = []
+        arr = (ctypes.c_void_p * 9)()
+        for i, k in enumerate(ROW_KEYS):
+            n = int(np.prod(dims[k]))
+            if n == 0 or k not in rows:
+                arr[i] = None
+                continue
+            r = np.ascontiguousarray(np.asarray(rows[k], dtype=np.float64).ravel())
+            if r.size != n:
+                raise ValueError(f"row {k} has {r.size} entries, expected {n}")
+            keep.append(r)
+            arr[i] = r.ctypes.data
+        _lib.check(self.h, self.L.peec_set_rows(self.h, arr))
+
+    def fill(self, origin, sx, sy, sz, escal_Lp, escal_P, return_rows=False):
+        """GPU fill of the nine rows and their spectra."""
+        dims = row_dims(*self.grid)
+        o = np.ascontiguousarray(np.asarray(origin, dtype=np.float64))
+        outs = {}
+        arr = (ctypes.c_void_p * 9)()
+        for i, k in enumerate(ROW_KEYS):
+            n = int(np.prod(dims[k]))
+            if return_rows and n > 0:
+                outs[k] = np.empty(n)
+                arr[i] = outs[k].ctypes.data
+            else:
+                arr[i] = None
+        _lib.check(self.h, self.L.peec_fill(self.h, _lib.ptr(o), sx, sy, sz, escal_Lp, escal_P,
+                                            arr if return_rows else None))
+        return outs if return_rows else None
+
+    # -- frequency ------------------------------------------------------------------
+    def set_frequency(self, w, DZ, Yle, lu, key=None):
+        if key is not None and key == self._freq_key:
+            return
+        DZ = np.ascontiguousarray(np.asarray(DZ, dtype=np.complex128).ravel())
+        Y = sp.coo_matrix(Yle)
+        yr = Y.row.astype(np.int64)
+        yc = Y.col.astype(np.int64)
+        yv = np.ascontiguousarray(Y.data.astype(np.complex128))
+        (Lp, Lc, Lv), (Up, Uc, Uv), pr, pc = export_lu(lu)
+        _lib.check(self.h, self.L.peec_set_frequency(
+            self.h, float(w), _lib.ptr(DZ.view(np.float64)), int(yr.size), _lib.ptr(yr),
+            _lib.ptr(yc), _lib.ptr(yv.view(np.float64)), _lib.ptr(Lp), _lib.ptr(Lc), _lib.ptr(Lv),
+            _lib.ptr(Up), _lib.ptr(Uc), _lib.ptr(Uv), _lib.ptr(pr), _lib.ptr(pc)))
+        self._freq_key = key
+
+    # -- operator ----------------------------------------------------------------------
+    def matvec(self, x, precision=0):
+        x = np.ascontiguousarray(np.asarray(x, dtype=np.complex128).ravel())
+        if x.size != self.N:
+            raise ValueError(f"x has {x.size} entries, expected {self.N}")
+        y = np.empty(self.N, dtype=np.complex128)
+        _lib.check(self.h, self.L.peec_matvec(self.h, _lib.ptr(x), _lib.ptr(y), precision))
+        return y
+
+    def matvec_dev(self, x_ptr, y_ptr, precision=0):
+        _lib.check(self.h, self.L.peec_matvec_dev(self.h, ctypes.c_void_p(x_ptr),
+                                                  ctypes.c_void_p(y_ptr), precision))
+
+    def last_timing(self):
+        t = [ctypes.c_double() for _ in range(3)]
+        self.L.peec_last_timing(self.h, *[ctypes.byref(v) for v in t])
+        return tuple(v.value for v in t)
+
+    def launch_count(self):
+        return int(self.L.peec_launch_count(self.h))
+
+    def port_rhs(self, n1, n2, Is):
+        tn = np.empty(self.N, dtype=np.complex128)
+        _lib.check(self.h, self.L.peec_port_rhs(self.h, int(n1), int(n2), float(Is), _lib.ptr(tn)))
+        return tn
+
+    def set_stop_flag(self, flag: "ctypes.c_int | None"):
+        self._stop = flag
+        _lib.check(self.h, self.L.peec_set_stop_flag(
+            self.h, ctypes.cast(ctypes.byref(flag), ctypes.c_void_p) if flag is not None else None))
+
+    def gmres(self, b, x0, tol, maxit, restarted=False, restart=0, precision=0):
+        b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())
+        x = np.zeros(self.N, dtype=np.complex128) if x0 is None or np.size(x0) == 0 else \
+            np.array(np.asarray(x0, dtype=np.complex128).ravel())
+        flag = ctypes.c_int()
+        relres = ctypes.c_double()
+        it = (ctypes.c_int * 2)()
+        cap = (maxit if not restarted else maxit * max(restart, 1)) + 2
+        resvec = np.zeros(cap)
+        nres = ctypes.c_int()
+        rc = self.L.peec_gmres(self.h, _lib.ptr(b), _lib.ptr(x), float(tol), int(maxit),
+                               1 if restarted else 0, int(restart), int(precision),
+                               ctypes.byref(flag), ctypes.byref(relres), it,
+                               resvec.ctypes.data_as(_lib.DP), cap, ctypes.byref(nres))
+        if rc == -3:
+            return x, 99, 0.0, [it[0], it[1]], np.zeros(1)
+        _lib.check(self.h, rc)
+        return x, flag.value, relres.value, [it[0], it[1]], resvec[:nres.value].copy()
+
+    def solve_mixed(self, b, x0, tol, inner_tol=1e-5, inner_maxit=100, max_outer=8):
+        b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())
+        x = np.zeros(self.N, dtype=np.complex128) if x0 is None else \
+            np.array(np.asarray(x0, dtype=np.complex128).ravel())
+        flag = ctypes.c_int()
+        relres = ctypes.c_double()
+        outer = ctypes.c_int()
+        inner = ctypes.c_int()
+        _lib.check(self.h, self.L.peec_solve_mixed(
+            self.h, _lib.ptr(b), _lib.ptr(x), float(tol), float(inner_tol), int(inner_maxit),
+            int(max_outer), ctypes.byref(flag), ctypes.byref(relres), ctypes.byref(outer),
+            ctypes.byref(inner)))
+        return x, flag.value, relres.value, outer.value, inner.value

@@ -1,0 +1,170 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Shared fill: both sides use the oracle's generating rows (the fill is compared
+separately, against a long double evaluation), and the same SuperLU factors, so the
+only differences are the FFT grids (the GPU uses reduced power-of-two circulants,
+the oracle the reference's 2N extents) and rounding order.
+Tolerances: FP64 operator 1e-12 relative (max-norm), solutions and port
+impedances 1e-10 relative, FP32 operator 2e-5 relative.
+"""
+import numpy as np
+import pytest
+
+from oracle import peec_oracle as O
+from solver_gb300 import configs, mesher
+from solver_gb300.operator import GpuOperator
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden"
+
+
+def _case(req):
+    out, freqs, settings, z0, grid = mesher.parse_request(req)
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    rows = O.fill_rows(cc, esc, *grid)
+    FFTCP, FFTCLp = O.spectra_from_rows(rows, *grid)
+    return dict(esc=esc, inc=inc, cc=cc, diag=diag, exp=exp, ports=ports, le=le, Zs=Zs,
+                rows=rows, FFTCP=FFTCP, FFTCLp=FFTCLp, freqs=freqs, settings=settings, z0=z0,
+                grid=grid)
+
+
+CASES = {
+    "first_run_data": lambda: mesher.load_request(GOLDEN / "first_run_data.json"),
+    "two_materials": lambda: mesher.load_request(GOLDEN / "first_run_data_2_materials.json"),
+    "crossbar_20x20x4": configs.crossbar_20x20x4,
+    "random_24x20x12": lambda: configs.random_mixed((24, 20, 12), s=5e-5, p=0.35, seed=7,
+                                                    nports=2, freqs=[1e8, 3e9], tol=1e-8),
+}
+
+
+@pytest.fixture(scope="module", params=sorted(CASES))
+def case(request):
+    c = _case(CASES[request.param]())
+    op = GpuOperator(c["inc"], c["exp"], c["diag"]["P"])
+    op.set_rows(c["rows"])
+    c["op"] = op
+    c["name"] = request.param
+    yield c
+    op.close()
+
+
+def _freq(c, k=0):
+    w = 2 * np.pi * c["freqs"][k] * c["esc"]["freq"]
+    fs = O.frequency_setup(w, c["esc"], c["inc"], c["diag"], c["Zs"], c["le"], c["ports"], c["z0"])
+    c["op"].set_frequency(w, fs["DZ"], fs["Yle"], fs["lu"])
+    return w, fs
+
+
+def _oracle_mv(c, w, fs):
+    return lambda x: O.ComputeMatrixVectorFTT(x, w, c["inc"], c["FFTCP"], c["FFTCLp"], fs["DZ"],
+                                              fs["Yle"], c["exp"], fs["invZ"], fs["invP"], fs["F"])
+
+
+def _rel(a, b):
+    return np.max(np.abs(a - b)) / np.max(np.abs(b))
+
+
+def test_matvec_fp64(case):
+    w, fs = _freq(case)
+    rng = np.random.default_rng(3)
+    N = case["op"].N
+    for _ in range(2):
+        x = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+        y_ref = _oracle_mv(case, w, fs)(x)
+        y = case["op"].matvec(x, 0)
+        assert _rel(y, y_ref) < 1e-12, case["name"]
+
+
+def test_matvec_fp32(case):
+    w, fs = _freq(case)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(case["op"].N) + 1j * rng.standard_normal(case["op"].N)
+    y_ref = _oracle_mv(case, w, fs)(x)
+    y = case["op"].matvec(x, 1)
+    assert _rel(y, y_ref) < 2e-5
+
+
+def test_port_rhs(case):
+    w, fs = _freq(case)
+    inc = case["inc"]
+    n1, n2 = case["ports"]["port_nodes"][0]
+    is_ = np.zeros(inc["A"].shape[1])
+    is_[n1] = case["esc"]["Is"]
+    is_[n2] = -case["esc"]["Is"]
+    ref = O.precond_3_3_Kt_fft(fs["F"], fs["invZ"], fs["invP"], inc["A"], inc["Gamma"],
+                               inc["A"].shape[0], inc["Gamma"].shape[1], is_)
+    got = case["op"].port_rhs(n1, n2, case["esc"]["Is"])
+    assert _rel(got, ref) < 1e-13
+
+
+def test_gmres_parity(case):
+    w, fs = _freq(case)
+    tn = case["op"].port_rhs(*case["ports"]["port_nodes"][0], case["esc"]["Is"])
+    tol = 1e-8
+    x_ref, f_ref, rr_ref, it_ref, rv_ref = O.gmres_custom(tn, False, tol, 100, None,
+                                                          _oracle_mv(case, w, fs))
+    x, f, rr, it, rv = case["op"].gmres(tn, None, tol, 100)
+    assert f == f_ref and list(it) == list(it_ref), (f, f_ref, it, it_ref)
+    assert len(rv) == len(rv_ref)
+    assert _rel(x, x_ref) < 1e-10
+    assert abs(rr - rr_ref) <= 1e-10 * max(rr_ref, 1e-300) + 1e-14
+
+
+def test_gmres_restarted(case):
+    w, fs = _freq(case)
+    tn = case["op"].port_rhs(*case["ports"]["port_nodes"][0], case["esc"]["Is"])
+    x_ref, f_ref, rr_ref, it_ref, rv_ref = O.gmres_custom(tn, True, 1e-9, 6, None,
+                                                          _oracle_mv(case, w, fs), restart=3)
+    x, f, rr, it, rv = case["op"].gmres(tn, None, 1e-9, 6, restarted=True, restart=3)
+    assert f == f_ref and list(it) == list(it_ref)
+    assert _rel(x, x_ref) < 1e-9
+
+
+def test_mixed_solve(case):
+    w, fs = _freq(case)
+    tn = case["op"].port_rhs(*case["ports"]["port_nodes"][0], case["esc"]["Is"])
+    x_ref = O.gmres_custom(tn, False, 1e-12, 200, None, _oracle_mv(case, w, fs))[0]
+    x, flag, relres, outer, inner = case["op"].solve_mixed(tn, None, 1e-8)
+    assert flag == 0 and relres <= 1e-8
+    # the FP64 residual check bounds the error by the preconditioned condition number
+    assert _rel(x, x_ref) < 1e-6
+
+
+def test_sweep_parity(case):
+    from solver_gb300 import api
+    c = case
+    st = {"Inner_Iter": c["settings"]["Inner_Iter"],
+          "tol": np.full(len(c["freqs"]), c["settings"]["tol"])}
+    ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
+                                 c["diag"], c["ports"], c["z0"], c["le"], c["exp"], st, c["Zs"])
+    c["exp"]["gpu_ctx"] = c["op"]
+    h = api.CirculantSpectra(c["op"])
+    got = api.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], h, h, c["diag"], c["ports"],
+                                   c["z0"], c["le"], c["exp"], st, c["Zs"])
+    assert [r["niter"] for r in got["info"]] == [len(r["resvec"]) - 1 for r in ref["info"]]
+    assert _rel(got["Z"], ref["Z"]) < 1e-10
+    assert _rel(got["Vrest"], ref["Vrest"]) < 1e-10
+
+
+def test_fill_against_long_double(case):
+    c = case
+    rows_gpu = c["op"].fill(c["cc"]["origin"], c["cc"]["sx"], c["cc"]["sy"], c["cc"]["sz"],
+                            c["esc"]["Lp"], c["esc"]["P"], return_rows=True)
+    ld = O.fill_rows(c["cc"], c["esc"], *c["grid"], precision="long", with_scale=True)
+    eps = np.finfo(float).eps
+    for k, (row_ld, scale) in ld.items():
+        g = rows_gpu[k]
+        err = np.abs(g - row_ld)
+        # a closed form summing up to 64 terms of magnitude <= scale loses
+        # ~eps*scale; allow 64x that
+        bound = 64 * eps * scale + 1e-300
+        bound[0] = max(bound[0], 64 * eps * abs(row_ld[0]))
+        assert np.all(err <= bound), (k, float(np.max(err / bound)))
+    # and the operator built from the GPU fill agrees with the oracle-fill operator
+    w, fs = _freq(c)
+    x = np.random.default_rng(5).standard_normal(c["op"].N) + 0j
+    y_gpu_fill = c["op"].matvec(x, 0)
+    c["op"].set_rows(c["rows"])
+    y_ref = _oracle_mv(c, w, fs)(x)
+    assert _rel(y_gpu_fill, y_ref) < 1e-9
