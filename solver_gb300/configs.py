@@ -11,7 +11,8 @@ synthetic stand-ins with the stated shapes, sizes and distributions.
 * random_128x128x64 -- 128x128x64 grid of 5e-5 m voxels, occupancy Bernoulli(0.3)
   (seed 2), copper / FR4-like dielectric (eps_r 4.4) 50/50, 4 ports between random
   occupied copper voxels on the outer faces, 10 frequencies log-spaced
-  10 MHz - 10 GHz, tol 1e-8.
+  10 MHz - 10 GHz, tol 1e-8. Voxels without any occupied face neighbour are removed
+  (drop_isolated), since the reference algorithm cannot solve a geometry that has them.
 * random_copper(a, b, c, p, seed) -- copper-only Bernoulli(p) grids.
 """
 from __future__ import annotations
@@ -71,6 +72,22 @@ def _draw(shape, p, rng):
     return (rng.random(n) < p).reshape(shape, order="F")
 
 
+def drop_isolated(occ):
+    """Removes voxels with no occupied face neighbour. Such a voxel gets neither an
+    inductive edge nor a charge surface in the reference mesher (every face test of
+    create_mapping_Gamma_no_rep.jl:32,59,86,113 and the x/z analogues needs a
+    neighbour), so its node would leave the Schur complement SS exactly singular."""
+    nb = np.zeros(occ.shape, dtype=np.int32)
+    for ax in range(3):
+        for sh in (1, -1):
+            r = np.roll(occ, sh, axis=ax)
+            sl = [slice(None)] * 3
+            sl[ax] = 0 if sh == 1 else -1
+            r[tuple(sl)] = False
+            nb += r
+    return occ & (nb > 0)
+
+
 def _boundary_ports(mask, nports, rng):
     Nx, Ny, Nz = mask.shape
     face = np.zeros_like(mask)
@@ -89,6 +106,7 @@ def random_mixed(shape=(128, 128, 64), s=5e-5, p=0.3, seed=2, nports=4,
     rng = np.random.default_rng(seed)
     occ = _draw(shape, p, rng)
     is_cu = _draw(shape, 0.5, rng)
+    occ = drop_isolated(occ)
     cu = occ & is_cu
     di = occ & ~is_cu
     ports = _boundary_ports(cu, nports, rng)
@@ -104,6 +122,6 @@ def random_128x128x64():
 
 def random_copper(shape, s=5e-5, p=0.3, seed=5, nports=1, freqs=(1e9,), tol=1e-8, inner=100):
     rng = np.random.default_rng(seed)
-    cu = _draw(shape, p, rng)
+    cu = drop_isolated(_draw(shape, p, rng))
     ports = _boundary_ports(cu, nports, rng)
     return make_request({"copper": cu}, [dict(COPPER)], (s, s, s), ports, freqs, tol, inner=inner)
