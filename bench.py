@@ -1,0 +1,434 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 FFT-PEEC solver path.
+
+Metric: frequency-point solves per second at 1e-8 relative (left-preconditioned)
+residual on the 128x128x64 synthetic voxel geometry (Bernoulli(0.3) occupancy,
+copper / dielectric 50/50, 4 ports, 10 frequencies 10 MHz-10 GHz). One step = one
+frequency point: the host sparse-LU factorisation of that frequency's Schur
+complement, then for each of the 4 ports its right-hand side and a solve warm
+started from the previous frequency's solution (FFT_solver_QS_S_type.jl:60-209).
+
+* value: device throughput of the mixed-precision path (FP32 circulant
+  convolutions inside FP64 iterative refinement) -- CUDA events on the library's
+  stream around the GPU part of each step (frequency upload + 4 port solves), the
+  host LU of each frequency prepared beforehand;
+* e2e: the same steps end to end through the public API with host buffers, wall
+  clock including the host LU, H2D uploads and D2H of each solution;
+* fp64_plain: the reference algorithm (FP64 convolutions, Householder GMRES) timed
+  on the first frequency points;
+* roofline: the fused y/z convolution kernel (FP32), algorithmic bytes from the
+  block descriptors, duration from CUDA events around every launch;
+* cpu_baseline: the CPU oracle restatement (reference 2N extents, scipy FFT on all
+  host cores, SuperLU) -- one operator application + one factorisation, scaled by
+  the FP64 GMRES matvec count measured in this run.
+
+Multi-GPU: the path does not shard; --gpus N runs N independent replicas
+(torchrun, one rank per GPU) and reports their summed throughput.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "freq-point solves/s at 1e-8 residual, mixed vs FP64 plain on 1 GB300; matvec GB/s"
+UNIT = "freq-point solves/s"
+WORKLOAD = ("random_128x128x64: 5e-5 m voxels, Bernoulli(0.3) occupancy (seed 2), Cu/dielectric "
+            "50/50, 4 ports, 10 freqs 10 MHz-10 GHz, tol 1e-8")
+# average FP64 matvecs per port solve of the reference algorithm at this workload
+# (Householder GMRES iterations + true-residual checks), used only by --impl reference,
+# which has no GPU run to count them; the GPU arm measures and reports its own count
+REF_MATVECS_PER_PORT = 32
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=7)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-iters", type=int, default=20)
+    ap.add_argument("--grid", type=int, nargs=3, default=None,
+                    help="smaller random Cu/dielectric grid (profiling captures only)")
+    return ap.parse_args()
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier_max(ws, value):
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={device}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def conv_bytes(info, prec):
+    """Algorithmic bytes of the three convolution kernels per operator application:
+    each intermediate written and read once (no ky-split partials), the spectrum
+    read once, lattice maps (int32) and compact vectors (complex128) once."""
+    c = 16 if prec == 0 else 8
+    xf = yz = xi = 0
+    for a in info:
+        Lx, Ly, Lz = a["L"]
+        nb, na = a["nb"], a["na"]
+        t1 = Lx * nb[1] * nb[2] * c
+        t4 = Lx * na[1] * na[2] * c
+        spec = Lx * Ly * Lz * (c if a["spec_complex"] else c // 2)
+        xf += int(np.prod(nb)) * 4 + t1
+        yz += t1 + spec + t4
+        xi += t4 + int(np.prod(na)) * 4
+    return {"xfwd": xf, "yz": yz, "xinv": xi}
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def setup_problem(device=0, grid=None):
+    from solver_gb300 import configs, mesher
+    from solver_gb300.operator import GpuOperator
+    req = configs.random_128x128x64() if grid is None else configs.random_mixed(tuple(grid))
+    out, freqs, settings, z0, grid = mesher.parse_request(req)
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    op = GpuOperator(inc, exp, diag["P"], device=device)
+    rows = op.fill(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"],
+                   return_rows=True)
+    return dict(req=req, esc=esc, inc=inc, cc=cc, diag=diag, exp=exp, ports=ports, le=le,
+                Zs=Zs, freqs=freqs, settings=settings, z0=z0, grid=grid, op=op, rows=rows)
+
+
+def freq_state(P, k):
+    from solver_gb300 import frequency as fq
+    w = 2 * np.pi * P["freqs"][k] * P["esc"]["freq"]
+    return fq.FrequencyState(w, P["esc"], P["inc"], P["diag"], P["Zs"], P["le"], P["ports"],
+                             P["z0"])
+
+
+def solve_point(P, fs, Vrest, mode, tol):
+    """One frequency point: upload the frequency state, then RHS + solve per port.
+    Returns the S-matrix column values and per-port work counts, and H2D/D2H bytes."""
+    op = P["op"]
+    op.set_frequency(fs.w, fs.DZ, fs.Yle, fs.lu)
+    m, n = P["inc"]["A"].shape
+    ns = P["inc"]["Gamma"].shape[1]
+    pn = np.asarray(P["ports"]["port_nodes"], dtype=np.int64)
+    npt = pn.shape[0]
+    z0 = P["z0"]
+    S = np.zeros((npt, npt), dtype=np.complex128)
+    work = []
+    for c1 in range(npt):
+        tn = op.port_rhs(pn[c1, 0], pn[c1, 1], P["esc"]["Is"])
+        if mode == "mixed":
+            V, flag, relres, outer, ninner = op.solve_mixed(tn, Vrest[:, c1], tol, inner_tol=1e-5,
+                                                            inner_maxit=P["settings"]["Inner_Iter"])
+            work.append({"flag": flag, "relres": relres, "outer": outer, "inner": ninner,
+                         "fp64_matvecs": outer + 1, "fp32_matvecs": ninner + 2 * outer})
+        else:
+            V, flag, relres, it, rv = op.gmres(tn, Vrest[:, c1], tol, P["settings"]["Inner_Iter"])
+            work.append({"flag": flag, "relres": relres, "iter": it,
+                         "fp64_matvecs": len(rv) + 1})
+        Vrest[:, c1] = V
+        for c2 in range(c1, npt):
+            val = 2 * (V[m + ns + pn[c2, 0]] - V[m + ns + pn[c2, 1]])
+            S[c1, c2] = (val - z0) / z0 if c1 == c2 else val / z0
+            S[c2, c1] = S[c1, c2]
+    N = m + ns + n
+    L, U = fs.lu.L, fs.lu.U
+    h2d = (fs.DZ.nbytes + (L.nnz + U.nnz) * 24 + (2 * n + 2) * 8 * 2 + 2 * n * 8 +
+           fs.Yle.nnz * 32 + npt * (2 * N * 16))
+    d2h = npt * 2 * N * 16
+    return S, work, h2d, d2h
+
+
+def cpu_baseline(P, mv_per_port, sample_note):
+    """The CPU oracle on the host cores: one operator application at the reference's
+    2N extents (scipy.fft with all cores) and one SuperLU factorisation."""
+    from oracle import peec_oracle as O
+    cores = os.cpu_count() or 1
+    O.FFT_WORKERS = cores
+    Nx, Ny, Nz = P["grid"]
+    FFTCP, FFTCLp = O.spectra_from_rows(P["rows"], Nx, Ny, Nz)
+    w = 2 * np.pi * P["freqs"][0] * P["esc"]["freq"]
+    t = time.perf_counter()
+    fs = O.frequency_setup(w, P["esc"], P["inc"], P["diag"], P["Zs"], P["le"], P["ports"], P["z0"])
+    t_lu = time.perf_counter() - t
+    x = np.random.default_rng(0).standard_normal(P["op"].N) + 0j
+    t = time.perf_counter()
+    O.ComputeMatrixVectorFTT(x, w, P["inc"], FFTCP, FFTCLp, fs["DZ"], fs["Yle"], P["exp"],
+                             fs["invZ"], fs["invP"], fs["F"])
+    t_mv = time.perf_counter() - t
+    npt = len(P["ports"]["port_nodes"])
+    t_point = t_lu + npt * mv_per_port * t_mv
+    return {"value": 1.0 / t_point, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"one oracle operator application ({t_mv:.2f} s, reference 2N extents, "
+                       f"scipy.fft x{cores} threads, 3 SuperLU solves) + one SuperLU factorisation "
+                       f"({t_lu:.2f} s); freq point = LU + {npt} ports x {mv_per_port:.1f} matvecs "
+                       f"({sample_note})"),
+            "matvec_s": t_mv, "lu_s": t_lu}
+
+
+def run_reference(args):
+    ws, rank, local = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return
+    from oracle import peec_oracle as O
+    from solver_gb300 import configs, mesher
+    cores = os.cpu_count() or 1
+    O.FFT_WORKERS = cores
+    req = configs.random_128x128x64()
+    out, freqs, settings, z0, grid = mesher.parse_request(req)
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    rows = O.fill_rows(cc, esc, *grid)
+    FFTCP, FFTCLp = O.spectra_from_rows(rows, *grid)
+    npt = len(ports["port_nodes"])
+    x = np.random.default_rng(0).standard_normal(inc["A"].shape[0] + inc["A"].shape[1] +
+                                                   inc["Gamma"].shape[1]) + 0j
+    times = []
+    for i in range(args.warmup + args.steps):
+        k = i % len(freqs)
+        w = 2 * np.pi * freqs[k] * esc["freq"]
+        t = time.perf_counter()
+        fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
+        t_lu = time.perf_counter() - t
+        t = time.perf_counter()
+        O.ComputeMatrixVectorFTT(x, w, inc, FFTCP, FFTCLp, fs["DZ"], fs["Yle"], exp, fs["invZ"],
+                                 fs["invP"], fs["F"])
+        t_mv = time.perf_counter() - t
+        if i >= args.warmup:
+            times.append(t_lu + npt * REF_MATVECS_PER_PORT * t_mv)
+    t_point = float(np.mean(times))
+    v = 1.0 / t_point
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_point * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": (f"per step: one SuperLU factorisation + one oracle "
+                                        f"operator application (reference 2N extents, scipy.fft x"
+                                        f"{cores}), freq point = LU + {npt} ports x "
+                                        f"{REF_MATVECS_PER_PORT} matvecs")},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    ws, rank, local = dist_init()
+    P = setup_problem(device=local, grid=args.grid)
+    op = P["op"]
+    nf = len(P["freqs"])
+    tol = float(P["settings"]["tol"])
+    Vrest = np.zeros((op.N, len(P["ports"]["port_nodes"])), dtype=np.complex128)
+    states = {}
+
+    def state(k):
+        if k not in states:
+            states[k] = freq_state(P, k)
+        return states[k]
+
+    # -- operator profile and roofline (FP32 and FP64 convolutions) --------------------------
+    op.set_frequency(state(0).w, state(0).DZ, state(0).Yle, state(0).lu)
+    info = op.conv_info()
+    prof32 = op.profile_matvec(1, args.profile_iters)
+    prof64 = op.profile_matvec(0, max(3, args.profile_iters // 4))
+    b32, b64 = conv_bytes(info, 1), conv_bytes(info, 0)
+    peak, peak_kind = load_peaks()
+
+    # -- mixed-precision timed steps ---------------------------------------------------------
+    import ctypes
+    try:
+        import torch
+        ext = torch.cuda.ExternalStream(op.stream(), device=f"cuda:{local}")
+        ev = lambda: torch.cuda.Event(enable_timing=True)
+        have_torch = True
+    except Exception:
+        have_torch = False
+    S_mixed = {}
+    for i in range(args.warmup):
+        k = i % nf
+        S_mixed[k], _, _, _ = solve_point(P, state(k), Vrest, "mixed", tol)
+    gpu_ms = 0.0
+    h2d = d2h = 0
+    work = []
+    l0 = op.launch_count()
+    barrier(ws)
+    if have_torch:
+        torch.cuda.synchronize()
+    clocks = Clocks(local)
+    t_wall0 = time.perf_counter()
+    for i in range(args.warmup, args.warmup + args.steps):
+        k = i % nf
+        fs = state(k)  # host LU (inside the e2e wall clock, outside the device events)
+        if have_torch:
+            e0, e1 = ev(), ev()
+            e0.record(ext)
+        t0 = time.perf_counter()
+        S_mixed[k], w_, hb, db = solve_point(P, fs, Vrest, "mixed", tol)
+        if have_torch:
+            e1.record(ext)
+            e1.synchronize()
+            gpu_ms += e0.elapsed_time(e1)
+        else:
+            gpu_ms += (time.perf_counter() - t0) * 1e3
+        work += w_
+        h2d += hb
+        d2h += db
+    if have_torch:
+        torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    barrier(ws)
+    clk = clocks.stop()
+    launches = op.launch_count() - l0
+    gpu_s = barrier_max(ws, gpu_ms / 1e3)
+    wall_s = barrier_max(ws, t_wall)
+    value = ws * args.steps / gpu_s
+    e2e_v = ws * args.steps / wall_s
+
+    # -- FP64 plain (reference algorithm) on the first frequency points ------------------------
+    V64 = np.zeros_like(Vrest)
+    fp64_ms = 0.0
+    work64 = []
+    S64 = {}
+    for k in range(args.fp64_steps):
+        fs = state(k)
+        t0 = time.perf_counter()
+        S64[k], w64, _, _ = solve_point(P, fs, V64, "fp64", tol)
+        fp64_ms += (time.perf_counter() - t0) * 1e3
+        work64 += w64
+    fp64_v = args.fp64_steps / (fp64_ms / 1e3) if args.fp64_steps else None
+    # mixed vs FP64 port quantities (S) at the frequencies both ran
+    errs = []
+    for k in S64:
+        if k in S_mixed:
+            a, b = S_mixed[k], S64[k]
+            Za = 50 * np.linalg.solve(np.eye(len(a)) - a, np.eye(len(a)) + a)
+            Zb = 50 * np.linalg.solve(np.eye(len(b)) - b, np.eye(len(b)) + b)
+            errs.append(float(np.max(np.abs(Za - Zb)) / np.max(np.abs(Zb))))
+    mv_per_port = float(np.mean([w_["fp64_matvecs"] for w_ in work64])) if work64 else \
+        float(REF_MATVECS_PER_PORT)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": gpu_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "complex64 convolutions / complex128 refinement", "data": "synthetic",
+        "config": {"workload": WORKLOAD if args.grid is None else f"random {args.grid}",
+                   "grid": list(P["grid"]), "N": int(op.N),
+                   "m_edges": int(op.m), "ns_surfaces": int(op.ns), "n_nodes": int(op.n),
+                   "l2": "inputs larger than L2 (Krylov basis and spectra > 129 MB)",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
+                "d2h_bytes_per_step": int(d2h / args.steps)},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "fp64_plain": {"value": fp64_v, "unit": UNIT, "steps": args.fp64_steps,
+                       "mixed_over_fp64": (value / fp64_v) if fp64_v else None,
+                       "gmres_iters": [w_["iter"][1] for w_ in work64]},
+        "mixed_work": {"outer_mean": float(np.mean([w_["outer"] for w_ in work])),
+                       "inner_mean": float(np.mean([w_["inner"] for w_ in work])),
+                       "max_relres": float(max(w_["relres"] for w_ in work)),
+                       "z_rel_err_vs_fp64": max(errs) if errs else None},
+        "matvec": {"fp32_ms": prof32["total"], "fp64_ms": prof64["total"],
+                   "fp32_conv_gbs": (b32["xfwd"] + b32["yz"] + b32["xinv"]) /
+                   ((prof32["xfwd"] + prof32["yz"] + prof32["xinv"]) * 1e-3) / 1e9,
+                   "fp64_conv_gbs": (b64["xfwd"] + b64["yz"] + b64["xinv"]) /
+                   ((prof64["xfwd"] + prof64["yz"] + prof64["xinv"]) * 1e-3) / 1e9,
+                   "fp32_ms_by_kernel": prof32, "fp64_ms_by_kernel": prof64,
+                   "fp32_bytes_by_kernel": b32},
+        "roofline": {"bound": "hbm", "kernel": "k_yz<float> (fused y/z convolution pass)",
+                     "achieved": b32["yz"] / (prof32["yz"] * 1e-3) / 1e9, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": b32["yz"] / (prof32["yz"] * 1e-3) / 1e9 / peak,
+                     "traffic": None,
+                     "bytes_per_matvec": b32["yz"], "launches_per_matvec": len(info)},
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(P, mv_per_port,
+                                            "matvec count measured by the FP64 run above")
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    op.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

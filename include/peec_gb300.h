@@ -155,6 +155,28 @@ int peec_set_stop_flag(peec_ctx* ctx, volatile int* flag);
  */
 int peec_last_timing(peec_ctx* ctx, double* total_ms, double* conv_ms, double* sparse_ms);
 
+/* The CUDA stream (cudaStream_t) all work of the context is issued on. */
+void* peec_stream(const peec_ctx* ctx);
+
+/* Number of circulant block applications of the operator (12 for 3D grids). */
+int peec_conv_count(const peec_ctx* ctx);
+/*
+ * Descriptor of block application i: FFT grid L[3], input / output lattice
+ * extents nb[3] / na[3], ky split R of the fused y/z pass, and whether its
+ * spectrum is complex (cross blocks) or real (symmetric blocks).
+ */
+int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* nb, int* na, int* R,
+                   int* spec_complex);
+
+/*
+ * Runs `iters` operator applications on an internal vector and reports the mean
+ * per-application device time of each kernel class, measured with CUDA events
+ * around every launch on the context stream: ms[0] x-forward gathers + FFTs,
+ * ms[1] fused y/z passes, ms[2] x-inverse FFTs + scatters, ms[3] sparse epilogue
+ * and LU solve, ms[4] whole application.
+ */
+int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, double* ms);
+
 /* Counters: kernel launches issued by the context since creation. */
 int64_t peec_launch_count(const peec_ctx* ctx);
 

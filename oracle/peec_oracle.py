@@ -30,6 +30,25 @@ from . import build as _obuild
 
 _fill = None
 
+# FFT backend of the oracle operator: None -> numpy.fft (single thread); an int -> scipy.fft
+# with that many workers (the reference runs FFTW with 2 x Julia threads,
+# compute_FFT_mutual_coupling_mats.jl:4).
+FFT_WORKERS = None
+
+
+def _fftn(a):
+    if FFT_WORKERS:
+        import scipy.fft as sf
+        return sf.fftn(a, workers=FFT_WORKERS)
+    return np.fft.fftn(a)
+
+
+def _ifftn(a):
+    if FFT_WORKERS:
+        import scipy.fft as sf
+        return sf.ifftn(a, workers=FFT_WORKERS)
+    return np.fft.ifftn(a)
+
 
 def _fill_lib():
     global _fill
@@ -151,11 +170,11 @@ def spectra_from_rows(rows, Nx, Ny, Nz):
             FFTCLp[c] = np.zeros(ext, dtype=np.complex128)
             continue
         r = rows[key][0] if isinstance(rows[key], tuple) else rows[key]
-        FFTCLp[c] = np.fft.fftn(store_circulant_fft(r, *d[key]))
+        FFTCLp[c] = _fftn(store_circulant_fft(r, *d[key]))
     FFTCP = [[None] * 3 for _ in range(3)]
     for (i, j), key, _, _ in P_ROWS:
         r = rows[key][0] if isinstance(rows[key], tuple) else rows[key]
-        FFTCP[i][j] = np.fft.fftn(store_circulant_fft(r, *d[key]))
+        FFTCP[i][j] = _fftn(store_circulant_fft(r, *d[key]))
     return FFTCP, FFTCLp
 
 
@@ -175,7 +194,7 @@ def _conv(spec, vec_lattice):
     circ = np.reshape(vec_lattice, (Nx, Ny, Nz), order="F")
     padded = np.zeros(spec.shape, dtype=np.complex128)
     padded[:Nx, :Ny, :Nz] = circ
-    res = np.fft.ifftn(spec * np.fft.fftn(padded))
+    res = _ifftn(spec * _fftn(padded))
     return np.reshape(res[:Nx, :Ny, :Nz], Nx * Ny * Nz, order="F")
 
 

@@ -23,7 +23,8 @@ EXPORTS = ("peec_version", "peec_ctx_create", "peec_ctx_destroy", "peec_last_err
            "peec_set_topology", "peec_set_pdiag", "peec_set_rows", "peec_fill",
            "peec_set_frequency", "peec_matvec", "peec_matvec_dev", "peec_port_rhs",
            "peec_gmres", "peec_solve_mixed", "peec_set_stop_flag", "peec_last_timing",
-           "peec_launch_count", "peec_sizes")
+           "peec_launch_count", "peec_sizes", "peec_stream", "peec_conv_count",
+           "peec_conv_info", "peec_profile_matvec")
 
 
 class PeecError(RuntimeError):
@@ -85,6 +86,12 @@ def load(build_if_missing: bool = True):
     L.peec_launch_count.argtypes = [P]
     L.peec_launch_count.restype = ctypes.c_int64
     L.peec_sizes.argtypes = [P, I64P, I64P, I64P]
+    L.peec_stream.argtypes = [P]
+    L.peec_stream.restype = ctypes.c_void_p
+    L.peec_conv_count.argtypes = [P]
+    IP = ctypes.POINTER(ctypes.c_int)
+    L.peec_conv_info.argtypes = [P, ctypes.c_int, IP, IP, IP, IP, IP]
+    L.peec_profile_matvec.argtypes = [P, ctypes.c_int, ctypes.c_int, DP]
     _lib = L
     return L
 

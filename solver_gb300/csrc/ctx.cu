@@ -116,6 +116,10 @@ struct peec_ctx {
   double* hscal = nullptr;
   volatile int* stop = nullptr;
   float t_total = 0, t_conv = 0, t_sparse = 0;
+  // per-class profiling (peec_profile_matvec)
+  bool prof = false;
+  std::vector<cudaEvent_t> pev;
+  double prof_ms[5] = {0, 0, 0, 0, 0};
 };
 
 #define CTX_TRY(expr)                 \
@@ -256,6 +260,7 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   if (ctx->hscal) cudaFreeHost(ctx->hscal);
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
+  for (auto e : ctx->pev) cudaEventDestroy(e);
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
 }
@@ -707,12 +712,15 @@ static int matvec_dev(peec_ctx* ctx, const c64* x, c64* y, int prec, bool timed)
   if (timed) cudaEventRecord(ctx->ev[0], st);
   cudaMemsetAsync(ctx->LpI, 0, sizeof(c64) * (m > 0 ? m : 1), st);
   cudaMemsetAsync(ctx->PQ, 0, sizeof(c64) * (ns > 0 ? ns : 1), st);
+  size_t pe = 0;
   for (const auto& a : ctx->apps) {
     const bool lp = a.in_fam >= 3;
     const c64* xin = lp ? x : x + m;
     c64* yout = lp ? ctx->LpI : ctx->PQ;
+    cudaEvent_t* evs = ctx->prof ? &ctx->pev[pe] : nullptr;
     conv_apply(a, ctx->spec[a.spec_id], ctx->fmap[a.in_fam], ctx->fmap[a.out_fam], xin, yout, prec,
-               ctx->tw64, ctx->tw32, ctx->twmax, st);
+               ctx->tw64, ctx->tw32, ctx->twmax, st, evs);
+    pe += 4;
     ctx->launches += 3;
   }
   if (timed) cudaEventRecord(ctx->ev[1], st);
@@ -757,6 +765,60 @@ extern "C" int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precis
   CTX_TRY(peec_matvec_dev(ctx, ctx->dx, ctx->dy, precision));
   PEEC_CUDA_TRY(cudaMemcpyAsync(y, ctx->dy, bytes, cudaMemcpyDeviceToHost, ctx->st));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return PEEC_OK;
+}
+
+extern "C" void* peec_stream(const peec_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
+
+extern "C" int peec_conv_count(const peec_ctx* ctx) { return ctx ? (int)ctx->apps.size() : 0; }
+
+extern "C" int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* nb, int* na, int* R,
+                              int* spec_complex) {
+  if (!ctx || i < 0 || i >= (int)ctx->apps.size()) return PEEC_ERR_BADARG;
+  const ConvApp& a = ctx->apps[i];
+  for (int k = 0; k < 3; ++k) {
+    if (L) L[k] = a.L[k];
+    if (nb) nb[k] = a.nb[k];
+    if (na) na[k] = a.na[k];
+  }
+  if (R) *R = a.R;
+  if (spec_complex) *spec_complex = ctx->spec[a.spec_id].is_complex;
+  return PEEC_OK;
+}
+
+extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, double* ms) {
+  if (!ctx || !ms || iters < 1) return PEEC_ERR_BADARG;
+  if (precision != 0 && precision != 1) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0 or 1");
+  cudaSetDevice(ctx->dev);
+  const size_t nev = 4 * ctx->apps.size();
+  if (ctx->pev.size() != nev) {
+    for (auto e : ctx->pev) cudaEventDestroy(e);
+    ctx->pev.assign(nev, nullptr);
+    for (auto& e : ctx->pev) PEEC_CUDA_TRY(cudaEventCreate(&e));
+  }
+  double acc[5] = {0, 0, 0, 0, 0};
+  ctx->prof = true;
+  for (int it = 0; it < iters; ++it) {
+    int rc = matvec_dev(ctx, ctx->dx, ctx->dy, precision, true);
+    if (rc) {
+      ctx->prof = false;
+      return rc;
+    }
+    PEEC_CUDA_TRY(cudaEventSynchronize(ctx->ev[2]));
+    float t;
+    for (size_t a = 0; a < ctx->apps.size(); ++a) {
+      for (int c = 0; c < 3; ++c) {
+        cudaEventElapsedTime(&t, ctx->pev[4 * a + c], ctx->pev[4 * a + c + 1]);
+        acc[c] += t;
+      }
+    }
+    cudaEventElapsedTime(&t, ctx->ev[1], ctx->ev[2]);
+    acc[3] += t;
+    cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[2]);
+    acc[4] += t;
+  }
+  ctx->prof = false;
+  for (int c = 0; c < 5; ++c) ms[c] = acc[c] / iters;
   return PEEC_OK;
 }
 

@@ -35,9 +35,11 @@ struct Spectrum {
 };
 
 // Launchers (fftconv.cu). prec: 0 = fp64, 1 = fp32. xin/yout are complex double.
+// evs (nullable): 4 events recorded before/between/after the three kernels
 int conv_apply(const ConvApp& a, const Spectrum& S, const int32_t* in_map,
                const int32_t* out_map, const c64* xin, c64* yout, int prec,
-               const void* twiddles64, const void* twiddles32, int twmax, cudaStream_t st);
+               const void* twiddles64, const void* twiddles32, int twmax, cudaStream_t st,
+               cudaEvent_t* evs = nullptr);
 int spectrum_build(Spectrum& S, const double* d_row, const int M[3], const int na[3],
                    const int nb[3], const int sdim[3], const int odim[3], int symmetric,
                    const void* twiddles64, int twmax, cudaStream_t st);

@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(TPB) k_xinv(const cx<R>* __restrict__ T4, c64*
 template <typename R>
 static int conv_apply_t(const ConvApp& a, const Spectrum& S, const int32_t* in_map,
                         const int32_t* out_map, const c64* xin, c64* yout, const cx<R>* tw,
-                        int twmax, cudaStream_t st) {
+                        int twmax, cudaStream_t st, cudaEvent_t* evs) {
   constexpr int TY = 16;
   const int prec = sizeof(R) == 8 ? 0 : 1;
   const int Lx = a.L[0], Ly = a.L[1], Lz = a.L[2];
@@ -189,12 +189,14 @@ static int conv_apply_t(const ConvApp& a, const Spectrum& S, const int32_t* in_m
   cx<R>* T4 = reinterpret_cast<cx<R>*>(a.T4[prec]);
   size_t sm_x = sizeof(cx<R>) * ((Lx / 2 > 0 ? Lx / 2 : 1) + (size_t)TY * (Lx + 1));
   dim3 gx((a.nb[1] + TY - 1) / TY, a.nb[2]);
+  if (evs) cudaEventRecord(evs[0], st);
   k_xfwd<R, TY><<<gx, TPB, sm_x, st>>>(xin, in_map, T1, Lx, a.logL[0], a.nb[0], a.nb[1], a.nb[2],
                                        tw, twmax);
   const int R_ = a.R, Lyl = Ly / R_;
   size_t sm_yz = sizeof(cx<R>) * ((Lyl / 2 > 0 ? Lyl / 2 : 1) + (Lz / 2 > 0 ? Lz / 2 : 1) +
                                   (R_ > 1 ? Ly : 0) + (size_t)Lyl * (Lz + 1));
   dim3 gyz(Lx, R_);
+  if (evs) cudaEventRecord(evs[1], st);
   if (S.is_complex) {
     k_yz<R, R, true><<<gyz, TPB, sm_yz, st>>>(T1, T4, reinterpret_cast<const R*>(S.d[prec]),
                                              a.conj, Lx, Ly, a.logL[1], Lz, a.logL[2], a.logR,
@@ -205,8 +207,10 @@ static int conv_apply_t(const ConvApp& a, const Spectrum& S, const int32_t* in_m
                                               a.nb[1], a.nb[2], a.na[1], a.na[2], tw, twmax);
   }
   dim3 gi((a.na[1] + TY - 1) / TY, a.na[2]);
+  if (evs) cudaEventRecord(evs[2], st);
   k_xinv<R, TY><<<gi, TPB, sm_x, st>>>(T4, yout, out_map, Lx, a.logL[0], R_, a.na[0], a.na[1],
                                        a.na[2], tw, twmax);
+  if (evs) cudaEventRecord(evs[3], st);
   return 0;
 }
 
@@ -219,12 +223,12 @@ size_t conv_smem_yz(const ConvApp& a, int prec) {
 
 int conv_apply(const ConvApp& a, const Spectrum& S, const int32_t* in_map, const int32_t* out_map,
                const c64* xin, c64* yout, int prec, const void* tw64, const void* tw32, int twmax,
-               cudaStream_t st) {
+               cudaStream_t st, cudaEvent_t* evs) {
   if (prec == 0)
     return conv_apply_t<double>(a, S, in_map, out_map, xin, yout,
-                                reinterpret_cast<const c64*>(tw64), twmax, st);
+                                reinterpret_cast<const c64*>(tw64), twmax, st, evs);
   return conv_apply_t<float>(a, S, in_map, out_map, xin, yout,
-                             reinterpret_cast<const c32*>(tw32), twmax, st);
+                             reinterpret_cast<const c32*>(tw32), twmax, st, evs);
 }
 
 // ------------------------------------------------------------------------------------

@@ -180,6 +180,28 @@ class GpuOperator:
         self.L.peec_last_timing(self.h, *[ctypes.byref(v) for v in t])
         return tuple(v.value for v in t)
 
+    def stream(self):
+        return int(self.L.peec_stream(self.h) or 0)
+
+    def conv_info(self):
+        out = []
+        for i in range(self.L.peec_conv_count(self.h)):
+            L = (ctypes.c_int * 3)()
+            nb = (ctypes.c_int * 3)()
+            na = (ctypes.c_int * 3)()
+            R = ctypes.c_int()
+            cplx = ctypes.c_int()
+            _lib.check(self.h, self.L.peec_conv_info(self.h, i, L, nb, na, ctypes.byref(R),
+                                                     ctypes.byref(cplx)))
+            out.append({"L": tuple(L), "nb": tuple(nb), "na": tuple(na), "R": R.value,
+                        "spec_complex": bool(cplx.value)})
+        return out
+
+    def profile_matvec(self, precision, iters=10):
+        ms = (ctypes.c_double * 5)()
+        _lib.check(self.h, self.L.peec_profile_matvec(self.h, int(precision), int(iters), ms))
+        return {"xfwd": ms[0], "yz": ms[1], "xinv": ms[2], "sparse": ms[3], "total": ms[4]}
+
     def launch_count(self):
         return int(self.L.peec_launch_count(self.h))
 
