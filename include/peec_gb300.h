@@ -177,6 +177,16 @@ int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* nb, int* na, int* R,
  */
 int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, double* ms);
 
+/*
+ * Batched inner products of Krylov vectors (the reductions of the GMRES reflector
+ * updates, gmres_custom.jl:112-127): out[c] = sum_i conj(U[i + c*ldu]) * v[i] for
+ * c < k. U, v, out are device pointers to complex doubles; runs on the context
+ * stream and returns after the result is in `out`. Partial sums go to scratch
+ * owned by the context (grown on demand).
+ */
+int peec_multidot(peec_ctx* ctx, const void* U, int64_t ldu, const void* v, int64_t N, int k,
+                  void* out);
+
 /* Counters: kernel launches issued by the context since creation. */
 int64_t peec_launch_count(const peec_ctx* ctx);
 

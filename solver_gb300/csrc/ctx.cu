@@ -120,6 +120,9 @@ struct peec_ctx {
   bool prof = false;
   std::vector<cudaEvent_t> pev;
   double prof_ms[5] = {0, 0, 0, 0, 0};
+  // scratch of peec_multidot
+  c64* mdpart = nullptr;
+  size_t mdcap = 0;
 };
 
 #define CTX_TRY(expr)                 \
@@ -239,7 +242,8 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
                   ctx->yle_val, ctx->g_in, ctx->g_out, ctx->LpI, ctx->PQ, ctx->Y1, ctx->U1,
                   ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->dx, ctx->dy, ctx->U,
                   ctx->gb, ctx->gx, ctx->gr, ctx->gv, ctx->gw, ctx->gxm, ctx->gxmin, ctx->gtmp,
-                  ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal};
+                  ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal,
+                  ctx->mdpart};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& f : ctx->fmap)
@@ -819,6 +823,26 @@ extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, doub
   }
   ctx->prof = false;
   for (int c = 0; c < 5; ++c) ms[c] = acc[c] / iters;
+  return PEEC_OK;
+}
+
+extern "C" int peec_multidot(peec_ctx* ctx, const void* U, int64_t ldu, const void* v, int64_t N,
+                             int k, void* out) {
+  if (!ctx || !U || !v || !out || N < 1 || k < 1 || ldu < N)
+    return PEEC_ERR_BADARG;
+  cudaSetDevice(ctx->dev);
+  const size_t need = (size_t)red_blocks((size_t)N) * (size_t)k;
+  if (ctx->mdcap < need) {
+    if (ctx->mdpart) cudaFree(ctx->mdpart);
+    ctx->mdpart = nullptr;
+    PEEC_CUDA_TRY(cudaMalloc(&ctx->mdpart, need * sizeof(c64)));
+    ctx->mdcap = need;
+  }
+  launch_multidot((const c64*)U, (size_t)ldu, (const c64*)v, (size_t)N, k, ctx->mdpart, (c64*)out,
+                  ctx->st);
+  ctx->launches += 2;
+  PEEC_CUDA_TRY(cudaGetLastError());
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return PEEC_OK;
 }
 
