@@ -99,15 +99,16 @@ int peec_fill(peec_ctx* ctx, const double origin[3], double sx, double sy, doubl
 /*
  * Per-frequency state (FFT_solver_QS_S_type.jl:105-119): scaled angular
  * frequency w, DZ[m] (complex), Yle as COO (complex values), and the sparse LU
- * factors of SS with Pr*SS*Pc = L*U in CSR form (L unit lower, U upper; both
- * include their diagonal), perm_r / perm_c as in SuperLU (row i of SS goes to
- * row perm_r[i]; column i to column perm_c[i]).
+ * factors of SS with Pr*diag(row_scale)*SS*Pc = L*U in CSR form (L lower, U upper;
+ * both include their diagonal), perm_r / perm_c as in SuperLU (row i goes to row
+ * perm_r[i]; column i to column perm_c[i]). row_scale may be NULL (no scaling; for
+ * UMFPACK factors pass F.Rs).
  */
 int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,
                        const int64_t* yle_row, const int64_t* yle_col, const double* yle_val,
                        const int64_t* L_ptr, const int64_t* L_col, const double* L_val,
                        const int64_t* U_ptr, const int64_t* U_col, const double* U_val,
-                       const int64_t* perm_r, const int64_t* perm_c);
+                       const int64_t* perm_r, const int64_t* perm_c, const double* row_scale);
 
 /* y = M^-1 K x (ComputeMatrixVectorFTT); x, y host, length N = m + ns + n complex. */
 int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precision);

@@ -70,7 +70,7 @@ def load(build_if_missing: bool = True):
     L.peec_fill.argtypes = [P, P, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                             ctypes.c_double, ctypes.c_double, ctypes.POINTER(P)]
     L.peec_set_frequency.argtypes = [P, ctypes.c_double, P, ctypes.c_int64, P, P, P, P, P, P, P,
-                                     P, P, P, P]
+                                     P, P, P, P, P]
     L.peec_matvec.argtypes = [P, P, P, ctypes.c_int]
     L.peec_matvec_dev.argtypes = [P, P, P, ctypes.c_int]
     L.peec_port_rhs.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, P]

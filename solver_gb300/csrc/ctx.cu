@@ -98,6 +98,7 @@ struct peec_ctx {
   int32_t *yle_ptr = nullptr, *yle_col = nullptr;
   c64* yle_val = nullptr;
   int32_t *g_in = nullptr, *g_out = nullptr;  // LU permutations as gathers
+  double* lu_rs = nullptr;                    // optional row scaling of the LU
   LevelTri Lf, Uf;
   // matvec work
   c64 *LpI = nullptr, *PQ = nullptr, *Y1 = nullptr, *U1 = nullptr, *Y2 = nullptr, *U2 = nullptr;
@@ -239,7 +240,7 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   void* ptrs[] = {ctx->tw64, ctx->tw32, ctx->n1, ctx->n2, ctx->snode, ctx->invP, ctx->ne_ptr,
                   ctx->ne_idx, ctx->nsn_ptr, ctx->nsn_idx, ctx->DZ, ctx->yle_ptr, ctx->yle_col,
-                  ctx->yle_val, ctx->g_in, ctx->g_out, ctx->LpI, ctx->PQ, ctx->Y1, ctx->U1,
+                  ctx->yle_val, ctx->g_in, ctx->g_out, ctx->lu_rs, ctx->LpI, ctx->PQ, ctx->Y1, ctx->U1,
                   ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->dx, ctx->dy, ctx->U,
                   ctx->gb, ctx->gx, ctx->gr, ctx->gv, ctx->gw, ctx->gxm, ctx->gxmin, ctx->gtmp,
                   ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal,
@@ -628,7 +629,7 @@ extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int
                                   const int64_t* L_col, const double* L_val,
                                   const int64_t* U_ptr, const int64_t* U_col,
                                   const double* U_val, const int64_t* perm_r,
-                                  const int64_t* perm_c) {
+                                  const int64_t* perm_c, const double* row_scale) {
   if (!ctx || !DZ || !L_ptr || !U_ptr || !perm_r || !perm_c) return PEEC_ERR_BADARG;
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
@@ -680,6 +681,13 @@ extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int
   }
   CTX_TRY(upload(&ctx->g_in, gin, ctx->st));
   CTX_TRY(upload(&ctx->g_out, gout, ctx->st));
+  if (row_scale) {
+    std::vector<double> rs(row_scale, row_scale + n);
+    CTX_TRY(upload(&ctx->lu_rs, rs, ctx->st));
+  } else if (ctx->lu_rs) {
+    cudaFree(ctx->lu_rs);
+    ctx->lu_rs = nullptr;
+  }
   CTX_TRY(make_tri(ctx, ctx->Lf, n, L_ptr, L_col, L_val, true));
   CTX_TRY(make_tri(ctx, ctx->Uf, n, U_ptr, U_col, U_val, false));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
@@ -693,7 +701,7 @@ extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int
 
 static void lu_solve(peec_ctx* ctx, const c64* b, c64* x) {
   const int n = (int)ctx->n;
-  launch_perm_gather(b, ctx->g_in, nullptr, n, ctx->lutmp, ctx->st);
+  launch_perm_gather(b, ctx->g_in, ctx->lu_rs, n, ctx->lutmp, ctx->st);
   ctx->launches++;
   for (LevelTri* T : {&ctx->Lf, &ctx->Uf}) {
     for (size_t l = 0; l + 1 < T->lvl_off.size(); ++l) {

@@ -159,7 +159,7 @@ class GpuOperator:
         _lib.check(self.h, self.L.peec_set_frequency(
             self.h, float(w), _lib.ptr(DZ.view(np.float64)), int(yr.size), _lib.ptr(yr),
             _lib.ptr(yc), _lib.ptr(yv.view(np.float64)), _lib.ptr(Lp), _lib.ptr(Lc), _lib.ptr(Lv),
-            _lib.ptr(Up), _lib.ptr(Uc), _lib.ptr(Uv), _lib.ptr(pr), _lib.ptr(pc)))
+            _lib.ptr(Up), _lib.ptr(Uc), _lib.ptr(Uv), _lib.ptr(pr), _lib.ptr(pc), None))
         self._freq_key = key
 
     # -- operator ----------------------------------------------------------------------
