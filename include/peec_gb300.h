@@ -188,6 +188,26 @@ int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, double* ms);
 int peec_multidot(peec_ctx* ctx, const void* U, int64_t ldu, const void* v, int64_t N, int k,
                   void* out);
 
+/*
+ * Allocation-free variant of peec_multidot, for callers that cannot allocate
+ * device memory when they need the reductions (a runtime whose device memory is
+ * owned by its own pool, or a loop that must not take the implicit device
+ * synchronisation of cudaMalloc/cudaFree). It has no counterpart in the reference.
+ * No context; U, v, out are device pointers to complex doubles on the current
+ * device; `stream` is a cudaStream_t (NULL = legacy default stream); returns after
+ * `out` holds the result.
+ * Scratch: a fixed file-scope device array of PEEC_NOALLOC_MAX_K x 1216 complex
+ * doubles (4.98 MB), resident on every GPU that loads the library until the
+ * process exits. k > PEEC_NOALLOC_MAX_K is rejected with PEEC_ERR_BADARG; any N
+ * is accepted. The first call on a device looks up the array's device address
+ * (one-time set-up); make that first call before any stream capture. All calls
+ * share the array: calls that overlap on the GPU (other threads, other streams)
+ * race on it and must be serialised by the caller. Calls no cudaMalloc/cudaFree.
+ */
+#define PEEC_NOALLOC_MAX_K 256
+int peec_multidot_noalloc(const void* U, int64_t ldu, const void* v, int64_t N, int k,
+                          void* out, void* stream);
+
 /* Counters: kernel launches issued by the context since creation. */
 int64_t peec_launch_count(const peec_ctx* ctx);
 

@@ -5,7 +5,10 @@
 // reflector (gmres_custom.jl:112-127): a multi-dot z = U(:,0:k)^H v, a small
 // triangular product on the host, and a multi-axpy v -= U(:,0:k) c. Reductions
 // are deterministic: warp-shuffle partials per CTA, then a fixed-order sum.
+#include <mutex>
+
 #include "ctx.hpp"
+#include "peec_gb300.h"
 
 namespace peec {
 
@@ -251,4 +254,64 @@ void launch_xupdate(const c64* x, const c64* U, size_t ldu, const c64* coef, con
                                                                         N, out);
 }
 
+// ------------------------------------------------------------------------------------
+// Allocation-free batched inner products (peec_multidot_noalloc)
+//
+// Some callers cannot call cudaMalloc at the point where they need these
+// reductions: a host runtime whose device memory is entirely owned by its own
+// pool allocator, or a latency-critical loop in which the implicit device
+// synchronisation of cudaMalloc/cudaFree is not acceptable. For them the partial
+// sums live in a fixed file-scope device array instead of caller- or
+// context-owned scratch. It holds NOALLOC_BLOCKS x PEEC_NOALLOC_MAX_K complex
+// doubles (4.98 MB) and stays resident on every GPU that loads this library until
+// the process exits.
+// ------------------------------------------------------------------------------------
+
+constexpr int NOALLOC_BLOCKS = 152 * 8;  // = the grid cap of the multi-dot launcher
+static __device__ __align__(256) c64 g_noalloc_partials[(size_t)NOALLOC_BLOCKS * PEEC_NOALLOC_MAX_K];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[256] = {};  // device address of the array, per device ordinal
+
 }  // namespace peec
+
+extern "C" int peec_multidot_noalloc(const void* U, int64_t ldu, const void* v, int64_t N, int k,
+                                     void* out, void* stream) {
+  using namespace peec;
+  if (!U || !v || !out || N < 1 || ldu < N) {
+    set_error("peec_multidot_noalloc: null pointer or N < 1 or ldu < N");
+    return PEEC_ERR_BADARG;
+  }
+  if (k < 1 || k > PEEC_NOALLOC_MAX_K) {
+    set_error("peec_multidot_noalloc: k = " + std::to_string(k) + " outside 1.." +
+              std::to_string(PEEC_NOALLOC_MAX_K) + " (the fixed scratch holds " +
+              std::to_string(PEEC_NOALLOC_MAX_K) + " columns)");
+    return PEEC_ERR_BADARG;
+  }
+  int dev = 0;
+  PEEC_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) {
+    set_error("peec_multidot_noalloc: device ordinal out of range");
+    return PEEC_ERR_BADARG;
+  }
+  void* scratch = nullptr;
+  {
+    // one-time set-up per device, with that device current: the host-side name of
+    // the array is not a device address, so ask the runtime for it
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* p = nullptr;
+      PEEC_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_partials));
+      g_noalloc_addr[dev] = p;
+    }
+    scratch = g_noalloc_addr[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  // every partial[b][c] the reduction reads (b < grid, c < k) is written by this call's
+  // multi-dot first, so the array needs no clearing between calls
+  launch_multidot((const c64*)U, (size_t)ldu, (const c64*)v, (size_t)N, k, (c64*)scratch,
+                  (c64*)out, st);
+  PEEC_CUDA_TRY(cudaGetLastError());
+  PEEC_CUDA_TRY(cudaStreamSynchronize(st));
+  return PEEC_OK;
+}
