@@ -16,8 +16,9 @@ started from the previous frequency's solution (FFT_solver_QS_S_type.jl:60-209).
   clock including the host LU, H2D uploads and D2H of each solution;
 * fp64_plain: the reference algorithm (FP64 convolutions, Householder GMRES) timed
   on the first frequency points;
-* roofline: the fused y/z convolution kernel (FP32), algorithmic bytes from the
-  block descriptors, duration from CUDA events around every launch;
+* roofline: the z passes of the FP32 convolutions (forward FFT, 3x3 spectral
+  product, inverse FFT), algorithmic bytes from the family descriptors, duration from
+  CUDA events around the pass;
 * cpu_baseline: the CPU oracle restatement (reference 2N extents, scipy FFT on all
   host cores, SuperLU) -- one operator application + one factorisation, scaled by
   the FP64 GMRES matvec count measured in this run.
@@ -132,21 +133,32 @@ class Clocks:
 
 
 def conv_bytes(info, prec):
-    """Algorithmic bytes of the three convolution kernels per operator application:
-    each intermediate written and read once (no ky-split partials), the spectrum
-    read once, lattice maps (int32) and compact vectors (complex128) once."""
+    """Algorithmic bytes of the convolution passes per operator application: every
+    per-family intermediate written once and read once by the next pass, each
+    spectrum read once (face families: 3 real + 3 complex spectra on the shared grid;
+    edge families: one real spectrum each), lattice maps (int32) once, compact vectors
+    (complex128) read once by the gather and written once by the scatter."""
     c = 16 if prec == 0 else 8
-    xf = yz = xi = 0
-    for a in info:
-        Lx, Ly, Lz = a["L"]
-        nb, na = a["nb"], a["na"]
-        t1 = Lx * nb[1] * nb[2] * c
-        t4 = Lx * na[1] * na[2] * c
-        spec = Lx * Ly * Lz * (c if a["spec_complex"] else c // 2)
-        xf += int(np.prod(nb)) * 4 + t1
-        yz += t1 + spec + t4
-        xi += t4 + int(np.prod(na)) * 4
-    return {"xfwd": xf, "yz": yz, "xinv": xi}
+    b = {"xfwd": 0, "yfwd": 0, "z": 0, "yinv": 0, "xinv": 0}
+    for f in info:
+        if not f["active"]:
+            continue
+        Lx, Ly, Lz = f["L"]
+        nx, ny, nz = f["dims"]
+        cells = nx * ny * nz
+        t_x = Lx * ny * nz * c          # after / before the x pass
+        t_y = Lx * Ly * nz * c          # after / before the y pass
+        b["xfwd"] += cells * 4 + cells * 16 + t_x
+        b["yfwd"] += t_x + t_y
+        b["z"] += 2 * t_y
+        b["yinv"] += t_y + t_x
+        b["xinv"] += t_x + cells * 4 + cells * 16
+        G = Lx * Ly * Lz
+        b["z"] += (G * c // 2) if f["edge"] else (G * c // 2 + G * c)  # per face family: 1 real + 1 complex
+    return b
+def conv_gbs(b, prof):
+    keys = ("xfwd", "yfwd", "z", "yinv", "xinv")
+    return sum(b[k] for k in keys) / (sum(prof[k] for k in keys) * 1e-3) / 1e9
 
 
 def load_peaks():
@@ -406,18 +418,15 @@ def main():
                        "max_relres": float(max(w_["relres"] for w_ in work)),
                        "z_rel_err_vs_fp64": max(errs) if errs else None},
         "matvec": {"fp32_ms": prof32["total"], "fp64_ms": prof64["total"],
-                   "fp32_conv_gbs": (b32["xfwd"] + b32["yz"] + b32["xinv"]) /
-                   ((prof32["xfwd"] + prof32["yz"] + prof32["xinv"]) * 1e-3) / 1e9,
-                   "fp64_conv_gbs": (b64["xfwd"] + b64["yz"] + b64["xinv"]) /
-                   ((prof64["xfwd"] + prof64["yz"] + prof64["xinv"]) * 1e-3) / 1e9,
-                   "fp32_ms_by_kernel": prof32, "fp64_ms_by_kernel": prof64,
-                   "fp32_bytes_by_kernel": b32},
-        "roofline": {"bound": "hbm", "kernel": "k_yz<float> (fused y/z convolution pass)",
-                     "achieved": b32["yz"] / (prof32["yz"] * 1e-3) / 1e9, "peak": peak,
+                   "fp32_conv_gbs": conv_gbs(b32, prof32), "fp64_conv_gbs": conv_gbs(b64, prof64),
+                   "fp32_ms_by_pass": prof32, "fp64_ms_by_pass": prof64,
+                   "fp32_bytes_by_pass": b32},
+        "roofline": {"bound": "hbm", "kernel": "k_zconv3<float> + k_zconv1<float> (z passes: "
+                     "FFT, spectral product, inverse FFT)",
+                     "achieved": b32["z"] / (prof32["z"] * 1e-3) / 1e9, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": b32["yz"] / (prof32["yz"] * 1e-3) / 1e9 / peak,
-                     "traffic": None,
-                     "bytes_per_matvec": b32["yz"], "launches_per_matvec": len(info)},
+                     "frac": b32["z"] / (prof32["z"] * 1e-3) / 1e9 / peak,
+                     "traffic": None, "bytes_per_matvec": b32["z"], "launches_per_matvec": 4},
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(P, mv_per_port,

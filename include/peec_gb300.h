@@ -159,22 +159,24 @@ int peec_last_timing(peec_ctx* ctx, double* total_ms, double* conv_ms, double* s
 /* The CUDA stream (cudaStream_t) all work of the context is issued on. */
 void* peec_stream(const peec_ctx* ctx);
 
-/* Number of circulant block applications of the operator (12 for 3D grids). */
+/* Number of lattice families of the operator (6: three face families, three edge
+ * directions). */
 int peec_conv_count(const peec_ctx* ctx);
 /*
- * Descriptor of block application i: FFT grid L[3], input / output lattice
- * extents nb[3] / na[3], ky split R of the fused y/z pass, and whether its
- * spectrum is complex (cross blocks) or real (symmetric blocks).
+ * Family i: circulant grid L[3], lattice extents dims[3], whether it is present in
+ * the geometry (*active) and its kind (0 = face family of P, 1 = edge family of Lp).
+ * Face families share one grid and the six P spectra (three real, three complex);
+ * each edge family has one real spectrum on its own grid.
  */
-int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* nb, int* na, int* R,
-                   int* spec_complex);
+int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* dims, int* active, int* kind);
 
 /*
  * Runs `iters` operator applications on an internal vector and reports the mean
- * per-application device time of each kernel class, measured with CUDA events
- * around every launch on the context stream: ms[0] x-forward gathers + FFTs,
- * ms[1] fused y/z passes, ms[2] x-inverse FFTs + scatters, ms[3] sparse epilogue
- * and LU solve, ms[4] whole application.
+ * per-application device time of each pass class, measured with CUDA events on the
+ * context stream: ms[0] x-forward (gather + FFT), ms[1] y-forward FFTs, ms[2] z
+ * passes (FFT, spectral product, inverse FFT), ms[3] y-inverse FFTs, ms[4]
+ * x-inverse (FFT + scatter), ms[5] sparse epilogue and LU solve, ms[6] whole
+ * application.
  */
 int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, double* ms);
 

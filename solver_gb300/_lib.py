@@ -91,7 +91,7 @@ def load(build_if_missing: bool = True):
     L.peec_stream.restype = ctypes.c_void_p
     L.peec_conv_count.argtypes = [P]
     IP = ctypes.POINTER(ctypes.c_int)
-    L.peec_conv_info.argtypes = [P, ctypes.c_int, IP, IP, IP, IP, IP]
+    L.peec_conv_info.argtypes = [P, ctypes.c_int, IP, IP, IP, IP]
     L.peec_profile_matvec.argtypes = [P, ctypes.c_int, ctypes.c_int, DP]
     L.peec_multidot.argtypes = [P, P, ctypes.c_int64, P, ctypes.c_int64, ctypes.c_int, P]
     L.peec_multidot_noalloc.argtypes = [P, ctypes.c_int64, P, ctypes.c_int64, ctypes.c_int, P, P]

@@ -27,8 +27,6 @@ int fail_cuda(cudaError_t e, const char* expr, const char* file, int line) {
 }
 
 // launchers defined in the other translation units
-int conv_prepare(const ConvApp& a);
-size_t conv_smem_yz(const ConvApp& a, int prec);
 void launch_edge_rows(const c64*, const c64*, const c64*, const c64*, const int32_t*,
                       const int32_t*, double, int, c64*, c64*, cudaStream_t);
 void launch_surf_rows(const c64*, const c64*, const int32_t*, const double*, int, c64*, c64*,
@@ -87,9 +85,7 @@ struct peec_ctx {
   int32_t *n1 = nullptr, *n2 = nullptr, *snode = nullptr;
   double* invP = nullptr;
   int32_t *ne_ptr = nullptr, *ne_idx = nullptr, *nsn_ptr = nullptr, *nsn_idx = nullptr;
-  int32_t* fmap[6] = {};
-  int fdims[6][3] = {};
-  std::vector<ConvApp> apps;
+  Family fam[6];
   Spectrum spec[9];
   int row_dims[9][3] = {};
   // frequency state
@@ -247,13 +243,11 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
                   ctx->mdpart};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  for (auto& f : ctx->fmap)
-    if (f) cudaFree(f);
-  for (auto& a : ctx->apps)
-    for (int p = 0; p < 2; ++p) {
-      if (a.T1[p]) cudaFree(a.T1[p]);
-      if (a.T4[p]) cudaFree(a.T4[p]);
-    }
+  for (auto& f : ctx->fam) {
+    if (f.map) cudaFree(f.map);
+    for (int p = 0; p < 2; ++p)
+      if (f.T[p]) cudaFree(f.T[p]);
+  }
   for (auto& s : ctx->spec)
     for (int p = 0; p < 2; ++p)
       if (s.d[p]) cudaFree(s.d[p]);
@@ -303,7 +297,6 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
   // family lattices: P faces 0..2, Lp edge directions 3..5
   const int fd[6][3] = {{Nx, Ny + 1, Nz}, {Nx + 1, Ny, Nz}, {Nx, Ny, Nz + 1},
                         {Nx - 1, Ny, Nz}, {Nx, Ny - 1, Nz}, {Nx, Ny, Nz - 1}};
-  std::memcpy(ctx->fdims, fd, sizeof(fd));
   std::vector<std::vector<int32_t>> maps(6);
   for (int f = 0; f < 6; ++f) maps[f].assign((size_t)fd[f][0] * fd[f][1] * fd[f][2], -1);
   const int64_t offs[4] = {0, mx, mx + my, m};
@@ -322,7 +315,7 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
       return bad(ctx, PEEC_ERR_BADARG, "surface lattice cell out of range or duplicated");
     maps[f][cell] = (int32_t)s;
   }
-  for (int f = 0; f < 6; ++f) CTX_TRY(upload(&ctx->fmap[f], maps[f], ctx->st));
+  for (int f = 0; f < 6; ++f) CTX_TRY(upload(&ctx->fam[f].map, maps[f], ctx->st));
   // incidence lists
   std::vector<int32_t> hn1(m), hn2(m), hsn(ns);
   std::vector<int32_t> deg(n + 1, 0), sdeg(n + 1, 0);
@@ -360,78 +353,49 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
   CTX_TRY(upload(&ctx->ne_idx, nei, ctx->st));
   CTX_TRY(upload(&ctx->nsn_ptr, sdeg, ctx->st));
   CTX_TRY(upload(&ctx->nsn_idx, nsi, ctx->st));
-  // block applications
-  for (auto& a : ctx->apps)
-    for (int p = 0; p < 2; ++p) {
-      cudaFree(a.T1[p]);
-      cudaFree(a.T4[p]);
-    }
-  ctx->apps.clear();
-  // reference row lattices: Lpx, Lpy, Lpz, p12, p34, p56, p1234, p1256, p3456
+  // lattice families and their circulant grids: the three face families share one
+  // grid (every P block, diagonal or cross, lives on it); each edge family has its own
   const int rd[9][3] = {{Nx - 1, Ny, Nz}, {Nx, Ny - 1, Nz}, {Nx, Ny, Nz - 1},
                         {Nx, Ny + 1, Nz}, {Nx + 1, Ny, Nz}, {Nx, Ny, Nz + 1},
                         {2 * Nx + 1, 2 * Ny + 1, Nz}, {Nx, 2 * Ny + 1, 2 * Nz + 1},
                         {2 * Nx + 1, Ny, 2 * Nz + 1}};
   std::memcpy(ctx->row_dims, rd, sizeof(rd));
-  struct Def { int spec, in, out, conj, s[3], o[3]; bool sym; };
-  const Def defs[12] = {
-      {0, 3, 3, 0, {1, 1, 1}, {0, 0, 0}, true},  {1, 4, 4, 0, {1, 1, 1}, {0, 0, 0}, true},
-      {2, 5, 5, 0, {1, 1, 1}, {0, 0, 0}, true},  {3, 0, 0, 0, {1, 1, 1}, {0, 0, 0}, true},
-      {4, 1, 1, 0, {1, 1, 1}, {0, 0, 0}, true},  {5, 2, 2, 0, {1, 1, 1}, {0, 0, 0}, true},
-      {6, 1, 0, 0, {2, 2, 1}, {1, -1, 0}, false}, {6, 0, 1, 1, {2, 2, 1}, {1, -1, 0}, false},
-      {7, 2, 0, 0, {1, 2, 2}, {0, -1, 1}, false}, {7, 0, 2, 1, {1, 2, 2}, {0, -1, 1}, false},
-      {8, 2, 1, 0, {2, 1, 2}, {-1, 0, 1}, false}, {8, 1, 2, 1, {2, 1, 2}, {-1, 0, 1}, false}};
-  for (int i = 0; i < 12; ++i) {
-    const Def& d = defs[i];
-    ConvApp a;
-    a.spec_id = d.spec;
-    a.in_fam = d.in;
-    a.out_fam = d.out;
-    a.conj = d.conj;
-    bool empty = false;
-    for (int k = 0; k < 3; ++k) {
-      a.nb[k] = fd[d.in][k];
-      a.na[k] = fd[d.out][k];
-      if (a.nb[k] <= 0 || a.na[k] <= 0) empty = true;
-    }
-    if (empty) continue;  // e.g. Nx == 1 has no x edges
-    // the spectrum of a cross block is built for its first application (conj = 0)
-    // and serves the transposed one, so both use the lattice pair of app conj = 0
-    const int fa = d.conj ? d.in : d.out, fb = d.conj ? d.out : d.in;
-    for (int k = 0; k < 3; ++k) {
-      a.L[k] = fft_len(fd[fa][k], fd[fb][k], d.sym);
-      a.logL[k] = ilog2(a.L[k]);
-    }
-    if (a.L[0] > ctx->twmax || a.L[1] > ctx->twmax || a.L[2] > ctx->twmax)
-      return bad(ctx, PEEC_ERR_UNSUPPORTED, "FFT length beyond twiddle table");
-    ctx->apps.push_back(a);
+  int LP[3];
+  for (int k = 0; k < 3; ++k) {
+    int need = 1;
+    for (int f = 0; f < 3; ++f) need = std::max(need, fd[f][k] > 1 ? 2 * fd[f][k] - 2 : 1);
+    for (int f = 0; f < 3; ++f)
+      for (int g = f + 1; g < 3; ++g) need = std::max(need, fd[f][k] + fd[g][k] - 1);
+    LP[k] = pow2ceil(need);
   }
-  // ky split so the y/z plane fits in shared memory (<= 200 KB)
-  for (auto& a : ctx->apps) {
-    a.R = 1;
-    a.logR = 0;
-    while (conv_smem_yz(a, 0) > 200 * 1024 && a.R < a.L[1]) {
-      a.R <<= 1;
-      a.logR++;
-    }
-    if (conv_smem_yz(a, 0) > 220 * 1024)
-      return bad(ctx, PEEC_ERR_UNSUPPORTED, "z extent too large for the fused y/z pass");
+  for (int f = 0; f < 6; ++f) {
+    Family& F = ctx->fam[f];
     for (int p = 0; p < 2; ++p) {
-      const size_t es = p == 0 ? sizeof(c64) : sizeof(c32);
-      const size_t t1 = (size_t)a.L[0] * a.nb[1] * a.nb[2] * es;
-      const size_t t4 = (size_t)a.R * a.L[0] * a.na[1] * a.na[2] * es;
-      PEEC_CUDA_TRY(cudaMalloc(&a.T1[p], t1));
-      PEEC_CUDA_TRY(cudaMalloc(&a.T4[p], t4));
+      if (F.T[p]) cudaFree(F.T[p]);
+      F.T[p] = nullptr;
     }
-    CTX_TRY(conv_prepare(a));
+    F.lp = f >= 3;
+    F.active = fd[f][0] > 0 && fd[f][1] > 0 && fd[f][2] > 0;
+    for (int k = 0; k < 3; ++k) {
+      F.dims[k] = fd[f][k];
+      F.L[k] = f < 3 ? LP[k] : fft_len(fd[f][k], fd[f][k], true);
+      F.logL[k] = ilog2(F.L[k]);
+      if (F.L[k] > ctx->twmax) return bad(ctx, PEEC_ERR_UNSUPPORTED, "FFT length beyond twiddle table");
+    }
+    if (!F.active) continue;
+    const size_t cells = (size_t)F.L[0] * F.L[1] * F.dims[2];
+    PEEC_CUDA_TRY(cudaMalloc(&F.T[0], cells * sizeof(c64)));
+    PEEC_CUDA_TRY(cudaMalloc(&F.T[1], cells * sizeof(c32)));
   }
-  // spectra share the lengths of their first application
-  for (auto& s : ctx->spec)
+  if (ctx->fam[0].L[2] * 3 * 16 * sizeof(c64) > 200 * 1024)
+    return bad(ctx, PEEC_ERR_UNSUPPORTED, "z circulant too long for the z pass tile");
+  for (auto& sp : ctx->spec)
     for (int p = 0; p < 2; ++p) {
-      if (s.d[p]) cudaFree(s.d[p]);
-      s.d[p] = nullptr;
+      if (sp.d[p]) cudaFree(sp.d[p]);
+      sp.d[p] = nullptr;
     }
-  for (auto& a : ctx->apps) std::memcpy(ctx->spec[a.spec_id].L, a.L, sizeof(a.L));
+  for (int i = 0; i < 6; ++i) std::memcpy(ctx->spec[i].L, LP, sizeof(LP));
+  for (int i = 6; i < 9; ++i) std::memcpy(ctx->spec[i].L, ctx->fam[i - 3].L, sizeof(LP));
   // work vectors
   CTX_TRY(dalloc(&ctx->LpI, m));
   CTX_TRY(dalloc(&ctx->PQ, ns));
@@ -466,22 +430,25 @@ extern "C" int peec_set_pdiag(peec_ctx* ctx, const double* diagP) {
   return PEEC_OK;
 }
 
-// spectra from device rows
+// spectra from device rows (rows in the order Lpx, Lpy, Lpz, p12, p34, p56, p1234,
+// p1256, p3456). Spectrum i uses row srow[i]: P blocks 00, 11, 22 (symmetric), 01, 02, 12
+// (cross: output family f, input family g), then the three Lp blocks.
 static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
-  static const int sdim[9][3] = {{1, 1, 1}, {1, 1, 1}, {1, 1, 1}, {1, 1, 1}, {1, 1, 1},
-                                 {1, 1, 1}, {2, 2, 1}, {1, 2, 2}, {2, 1, 2}};
-  static const int odim[9][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0},
-                                 {0, 0, 0}, {1, -1, 0}, {0, -1, 1}, {-1, 0, 1}};
-  bool done[9] = {false};
-  for (auto& a : ctx->apps) {
-    if (a.conj || done[a.spec_id]) continue;
-    const int sid = a.spec_id;
-    if (!d_rows[sid]) return bad(ctx, PEEC_ERR_BADARG, "missing generating row");
-    Spectrum& S = ctx->spec[sid];
-    CTX_TRY(spectrum_build(S, d_rows[sid], ctx->row_dims[sid], a.na, a.nb, sdim[sid], odim[sid],
-                           sid < 6 ? 1 : 0, ctx->tw64, ctx->twmax, ctx->st));
+  static const int srow[9] = {3, 4, 5, 6, 7, 8, 0, 1, 2};
+  static const int fout[9] = {0, 1, 2, 0, 0, 1, 3, 4, 5};
+  static const int fin[9] = {0, 1, 2, 1, 2, 2, 3, 4, 5};
+  static const int sdim[9][3] = {{1, 1, 1}, {1, 1, 1}, {1, 1, 1}, {2, 2, 1}, {1, 2, 2},
+                                 {2, 1, 2}, {1, 1, 1}, {1, 1, 1}, {1, 1, 1}};
+  static const int odim[9][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {1, -1, 0}, {0, -1, 1},
+                                 {-1, 0, 1}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int i = 0; i < 9; ++i) {
+    if (!ctx->fam[fout[i]].active || !ctx->fam[fin[i]].active) continue;
+    if (!d_rows[srow[i]]) return bad(ctx, PEEC_ERR_BADARG, "missing generating row");
+    const bool sym = i < 3 || i >= 6;
+    CTX_TRY(spectrum_build(ctx->spec[i], d_rows[srow[i]], ctx->row_dims[srow[i]],
+                           ctx->fam[fout[i]].dims, ctx->fam[fin[i]].dims, sdim[i], odim[i],
+                           sym ? 1 : 0, ctx->tw64, ctx->twmax, ctx->st));
     ctx->launches += 6;
-    done[sid] = true;
   }
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->have_spec = true;
@@ -722,19 +689,10 @@ static int matvec_dev(peec_ctx* ctx, const c64* x, c64* y, int prec, bool timed)
   const int64_t m = ctx->m, ns = ctx->ns, n = ctx->n;
   cudaStream_t st = ctx->st;
   if (timed) cudaEventRecord(ctx->ev[0], st);
-  cudaMemsetAsync(ctx->LpI, 0, sizeof(c64) * (m > 0 ? m : 1), st);
-  cudaMemsetAsync(ctx->PQ, 0, sizeof(c64) * (ns > 0 ? ns : 1), st);
-  size_t pe = 0;
-  for (const auto& a : ctx->apps) {
-    const bool lp = a.in_fam >= 3;
-    const c64* xin = lp ? x : x + m;
-    c64* yout = lp ? ctx->LpI : ctx->PQ;
-    cudaEvent_t* evs = ctx->prof ? &ctx->pev[pe] : nullptr;
-    conv_apply(a, ctx->spec[a.spec_id], ctx->fmap[a.in_fam], ctx->fmap[a.out_fam], xin, yout, prec,
-               ctx->tw64, ctx->tw32, ctx->twmax, st, evs);
-    pe += 4;
-    ctx->launches += 3;
-  }
+  CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, x, ctx->LpI, ctx->PQ, m, prec, ctx->tw64, ctx->tw32,
+                   ctx->twmax, st, ctx->prof ? ctx->pev.data() : nullptr));
+  for (const auto& F : ctx->fam) ctx->launches += F.active ? (F.lp ? 5 : 4) : 0;
+  ctx->launches += 1;  // the shared z pass of the face families
   if (timed) cudaEventRecord(ctx->ev[1], st);
   const c64* I = x;
   const c64* Q = x + m;
@@ -782,19 +740,18 @@ extern "C" int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precis
 
 extern "C" void* peec_stream(const peec_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
 
-extern "C" int peec_conv_count(const peec_ctx* ctx) { return ctx ? (int)ctx->apps.size() : 0; }
+extern "C" int peec_conv_count(const peec_ctx* ctx) { return ctx ? 6 : 0; }
 
-extern "C" int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* nb, int* na, int* R,
-                              int* spec_complex) {
-  if (!ctx || i < 0 || i >= (int)ctx->apps.size()) return PEEC_ERR_BADARG;
-  const ConvApp& a = ctx->apps[i];
+extern "C" int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* dims, int* active,
+                              int* kind) {
+  if (!ctx || i < 0 || i >= 6) return PEEC_ERR_BADARG;
+  const Family& F = ctx->fam[i];
   for (int k = 0; k < 3; ++k) {
-    if (L) L[k] = a.L[k];
-    if (nb) nb[k] = a.nb[k];
-    if (na) na[k] = a.na[k];
+    if (L) L[k] = F.L[k];
+    if (dims) dims[k] = F.dims[k];
   }
-  if (R) *R = a.R;
-  if (spec_complex) *spec_complex = ctx->spec[a.spec_id].is_complex;
+  if (active) *active = F.active ? 1 : 0;
+  if (kind) *kind = F.lp ? 1 : 0;
   return PEEC_OK;
 }
 
@@ -802,13 +759,12 @@ extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, doub
   if (!ctx || !ms || iters < 1) return PEEC_ERR_BADARG;
   if (precision != 0 && precision != 1) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0 or 1");
   cudaSetDevice(ctx->dev);
-  const size_t nev = 4 * ctx->apps.size();
-  if (ctx->pev.size() != nev) {
+  if (ctx->pev.size() != 6) {
     for (auto e : ctx->pev) cudaEventDestroy(e);
-    ctx->pev.assign(nev, nullptr);
+    ctx->pev.assign(6, nullptr);
     for (auto& e : ctx->pev) PEEC_CUDA_TRY(cudaEventCreate(&e));
   }
-  double acc[5] = {0, 0, 0, 0, 0};
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
   ctx->prof = true;
   for (int it = 0; it < iters; ++it) {
     int rc = matvec_dev(ctx, ctx->dx, ctx->dy, precision, true);
@@ -818,19 +774,17 @@ extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, doub
     }
     PEEC_CUDA_TRY(cudaEventSynchronize(ctx->ev[2]));
     float t;
-    for (size_t a = 0; a < ctx->apps.size(); ++a) {
-      for (int c = 0; c < 3; ++c) {
-        cudaEventElapsedTime(&t, ctx->pev[4 * a + c], ctx->pev[4 * a + c + 1]);
-        acc[c] += t;
-      }
+    for (int c = 0; c < 5; ++c) {
+      cudaEventElapsedTime(&t, ctx->pev[c], ctx->pev[c + 1]);
+      acc[c] += t;
     }
     cudaEventElapsedTime(&t, ctx->ev[1], ctx->ev[2]);
-    acc[3] += t;
+    acc[5] += t;
     cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[2]);
-    acc[4] += t;
+    acc[6] += t;
   }
   ctx->prof = false;
-  for (int c = 0; c < 5; ++c) ms[c] = acc[c] / iters;
+  for (int c = 0; c < 7; ++c) ms[c] = acc[c] / iters;
   return PEEC_OK;
 }
 

@@ -13,33 +13,37 @@ namespace peec {
 int fail_cuda(cudaError_t e, const char* expr, const char* file, int line);
 void set_error(const std::string& msg);
 
-// One Toeplitz application y_out(lattice A) += K * x_in(lattice B), computed as a
-// pruned circulant convolution on an Lx x Ly x Lz grid.
-struct ConvApp {
-  int L[3], logL[3];
-  int nb[3];  // input lattice extents
-  int na[3];  // output lattice extents
-  int R = 1, logR = 0;    // ky split of the fused Y/Z pass
-  int spec_id = -1;       // index into the spectrum table
-  int conj = 0;           // use conj(S) (transposed application of a cross block)
-  int in_fam = 0, out_fam = 0;   // lattice families (0..2 P faces, 3..5 Lp edges)
-  // per-precision scratch: T1 = Lx x nbz x nby, T4 = R x Lx x naz x nay
-  void* T1[2] = {nullptr, nullptr};
-  void* T4[2] = {nullptr, nullptr};
+#define CTX_CHECK(expr)      \
+  do {                       \
+    int _r = (expr);         \
+    if (_r) return _r;       \
+  } while (0)
+
+// A lattice family: one face family of the P tensor (reference families 12, 34, 56)
+// or one edge direction of the Lp tensor. Its lattice is both the input and the
+// output lattice of its circulant blocks.
+struct Family {
+  bool active = false;
+  bool lp = false;       // edge family (compact vector I, output LpI) vs face family (Q, PQ)
+  int dims[3] = {0, 0, 0};  // lattice extents, x fastest
+  int L[3] = {1, 1, 1}, logL[3] = {0, 0, 0};  // circulant grid
+  int32_t* map = nullptr;   // lattice cell -> compact index or -1
+  void* T[2] = {nullptr, nullptr};  // work buffer per precision: [z < dims[2]][y < Ly][kx < Lx]
 };
 
 struct Spectrum {
-  int L[3];
+  int L[3] = {1, 1, 1};
   int is_complex = 0;
-  void* d[2] = {nullptr, nullptr};  // [0] fp64, [1] fp32; layout (kx,ky,kz) kz fastest
+  void* d[2] = {nullptr, nullptr};  // [0] fp64, [1] fp32; layout (ky, kz, kx), kx fastest
 };
 
-// Launchers (fftconv.cu). prec: 0 = fp64, 1 = fp32. xin/yout are complex double.
-// evs (nullable): 4 events recorded before/between/after the three kernels
-int conv_apply(const ConvApp& a, const Spectrum& S, const int32_t* in_map,
-               const int32_t* out_map, const c64* xin, c64* yout, int prec,
-               const void* twiddles64, const void* twiddles32, int twmax, cudaStream_t st,
-               cudaEvent_t* evs = nullptr);
+// Launchers (fftconv.cu). prec: 0 = fp64, 1 = fp32. x (input) / LpI / PQ are complex
+// double; families 0..2 are the face families, 3..5 the edge families; spectra
+// 0..5 = P blocks (00, 11, 22, 01, 02, 12), 6..8 = Lp blocks of families 3..5.
+// ev (nullable): 6 events around the five pass classes.
+int conv_all(const Family* F, int nfam, const Spectrum* spec, const c64* x, c64* LpI, c64* PQ,
+             int64_t m, int prec, const void* tw64, const void* tw32, int twmax, cudaStream_t st,
+             cudaEvent_t* ev);
 int spectrum_build(Spectrum& S, const double* d_row, const int M[3], const int na[3],
                    const int nb[3], const int sdim[3], const int odim[3], int symmetric,
                    const void* twiddles64, int twmax, cudaStream_t st);

@@ -184,23 +184,24 @@ class GpuOperator:
         return int(self.L.peec_stream(self.h) or 0)
 
     def conv_info(self):
+        """The six lattice families: circulant grid, extents, presence, kind."""
         out = []
         for i in range(self.L.peec_conv_count(self.h)):
             L = (ctypes.c_int * 3)()
-            nb = (ctypes.c_int * 3)()
-            na = (ctypes.c_int * 3)()
-            R = ctypes.c_int()
-            cplx = ctypes.c_int()
-            _lib.check(self.h, self.L.peec_conv_info(self.h, i, L, nb, na, ctypes.byref(R),
-                                                     ctypes.byref(cplx)))
-            out.append({"L": tuple(L), "nb": tuple(nb), "na": tuple(na), "R": R.value,
-                        "spec_complex": bool(cplx.value)})
+            dims = (ctypes.c_int * 3)()
+            active = ctypes.c_int()
+            kind = ctypes.c_int()
+            _lib.check(self.h, self.L.peec_conv_info(self.h, i, L, dims, ctypes.byref(active),
+                                                     ctypes.byref(kind)))
+            out.append({"L": tuple(L), "dims": tuple(dims), "active": bool(active.value),
+                        "edge": bool(kind.value)})
         return out
 
     def profile_matvec(self, precision, iters=10):
-        ms = (ctypes.c_double * 5)()
+        ms = (ctypes.c_double * 7)()
         _lib.check(self.h, self.L.peec_profile_matvec(self.h, int(precision), int(iters), ms))
-        return {"xfwd": ms[0], "yz": ms[1], "xinv": ms[2], "sparse": ms[3], "total": ms[4]}
+        keys = ("xfwd", "yfwd", "z", "yinv", "xinv", "sparse", "total")
+        return dict(zip(keys, list(ms)))
 
     def launch_count(self):
         return int(self.L.peec_launch_count(self.h))
