@@ -5,6 +5,9 @@
 // Host code only sequences kernels and runs the small dense parts of GMRES
 // (Givens rotations, triangular solves on <= maxit unknowns) in FP64.
 #include <algorithm>
+#include <array>
+#include <map>
+#include <tuple>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -18,6 +21,11 @@ namespace peec {
 
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
+
+static int badarg(const char* fn) {
+  g_err = std::string(fn) + ": null pointer or argument out of range";
+  return PEEC_ERR_BADARG;
+}
 int fail_cuda(cudaError_t e, const char* expr, const char* file, int line) {
   char buf[512];
   snprintf(buf, sizeof(buf), "CUDA error %s (%d) at %s:%d in %s", cudaGetErrorString(e), (int)e,
@@ -40,6 +48,8 @@ void launch_final_rows(const c64*, const c64*, const c64*, const c64*, const int
 void launch_perm_gather(const c64*, const int32_t*, const double*, int, c64*, cudaStream_t);
 void launch_trsv_level(const int32_t*, int, const int32_t*, const int32_t*, const c64*,
                        const c64*, c64*, cudaStream_t);
+void launch_trsv_tail(const int32_t*, const int32_t*, int, int, const int32_t*, const int32_t*,
+                      const c64*, const c64*, c64*, cudaStream_t);
 int red_blocks(size_t N);
 void launch_multidot(const c64*, size_t, const c64*, size_t, int, c64*, c64*, cudaStream_t);
 void launch_multiaxpy(const c64*, size_t, const c64*, int, const c64*, int, size_t, c64*, size_t,
@@ -50,6 +60,7 @@ void launch_scale_rnorm(c64*, size_t, const double*, cudaStream_t);
 void launch_make_reflector(const c64*, size_t, int, c64, double, c64*, cudaStream_t);
 void launch_sub(const c64*, const c64*, size_t, c64*, cudaStream_t);
 void launch_add(const c64*, const c64*, size_t, c64*, cudaStream_t);
+void launch_tri(c64*, int, int, const c64*, c64*, int, cudaStream_t);
 void launch_xupdate(const c64*, const c64*, size_t, const c64*, const c64*, int, size_t, c64*,
                     cudaStream_t);
 int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, double escal_Lp,
@@ -62,9 +73,12 @@ using namespace peec;
 using cd = std::complex<double>;
 
 struct LevelTri {  // triangular factor without its diagonal, level-scheduled
-  int32_t *ptr = nullptr, *col = nullptr, *rows = nullptr;
+  int32_t *ptr = nullptr, *col = nullptr, *rows = nullptr, *doff = nullptr;
   c64 *val = nullptr, *dinv = nullptr;
   std::vector<int> lvl_off;  // offsets into rows per level
+  // schedule: (first level, end level, big) -- a big level is one grid launch, a run of
+  // small levels one single-CTA launch
+  std::vector<std::array<int, 3>> sched;
 };
 
 struct peec_ctx {
@@ -107,9 +121,10 @@ struct peec_ctx {
   c64* U = nullptr;
   c64 *gb = nullptr, *gx = nullptr, *gr = nullptr, *gv = nullptr, *gw = nullptr, *gxm = nullptr,
       *gxmin = nullptr, *gtmp = nullptr, *gzero = nullptr;
-  c64 *dcoef = nullptr, *dcoef2 = nullptr, *dpart = nullptr;
+  c64 *dcoef = nullptr, *dcoef2 = nullptr, *dpart = nullptr, *dT = nullptr;
   double *dred = nullptr, *dscal = nullptr;
-  c64* hsmall = nullptr;  // pinned small staging
+  c64* hsmall = nullptr;  // pinned staging ring for host -> device coefficients
+  c64* hread = nullptr;   // pinned staging for device -> host reads
   double* hscal = nullptr;
   volatile int* stop = nullptr;
   float t_total = 0, t_conv = 0, t_sparse = 0;
@@ -120,7 +135,23 @@ struct peec_ctx {
   // scratch of peec_multidot
   c64* mdpart = nullptr;
   size_t mdcap = 0;
+  // CUDA graphs of operator applications, keyed by (x, y, precision); captured on the
+  // second application with the same key, dropped whenever operator state changes
+  struct GraphEntry {
+    int calls = 0;
+    cudaGraphExec_t exec = nullptr;
+    int64_t kernels = 0;
+  };
+  std::map<std::tuple<const void*, void*, int>, GraphEntry> graphs;
+  bool use_graphs = true;
 };
+
+static void drop_graphs(peec_ctx* ctx) {
+  if (!ctx) return;
+  for (auto& kv : ctx->graphs)
+    if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+  ctx->graphs.clear();
+}
 
 #define CTX_TRY(expr)                 \
   do {                                \
@@ -166,15 +197,17 @@ static int pow2ceil(int v) {
 
 extern "C" int peec_version(void) { return 100; }
 
+// The calling thread's most recent error wins: every failing entry point records its
+// message there, including CUDA failures deep inside a launch sequence.
 extern "C" const char* peec_last_error(const peec_ctx* ctx) {
-  if (!ctx) return g_err.c_str();
+  if (!ctx || !g_err.empty()) return g_err.c_str();
   return ctx->err.c_str();
 }
 
 extern "C" int64_t peec_launch_count(const peec_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 extern "C" int peec_sizes(const peec_ctx* ctx, int64_t* m, int64_t* ns, int64_t* n) {
-  if (!ctx) return PEEC_ERR_BADARG;
+  if (!ctx) return badarg(__func__);
   if (m) *m = ctx->m;
   if (ns) *ns = ctx->ns;
   if (n) *n = ctx->n;
@@ -182,7 +215,7 @@ extern "C" int peec_sizes(const peec_ctx* ctx, int64_t* m, int64_t* ns, int64_t*
 }
 
 extern "C" int peec_ctx_create(peec_ctx** out, int device) {
-  if (!out) return PEEC_ERR_BADARG;
+  if (!out) return badarg(__func__);
   *out = nullptr;
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -219,7 +252,8 @@ extern "C" int peec_ctx_create(peec_ctx** out, int device) {
     return fail(fail_cuda(cudaErrorMemoryAllocation, "cudaMalloc twiddles", __FILE__, __LINE__));
   cudaMemcpy(ctx->tw64, t64.data(), sizeof(c64) * ctx->twmax, cudaMemcpyHostToDevice);
   cudaMemcpy(ctx->tw32, t32.data(), sizeof(c32) * ctx->twmax, cudaMemcpyHostToDevice);
-  cudaMallocHost(&ctx->hsmall, sizeof(c64) * 4096);
+  cudaMallocHost(&ctx->hsmall, sizeof(c64) * 16 * 4096);
+  cudaMallocHost(&ctx->hread, sizeof(c64) * 4096);
   cudaMallocHost(&ctx->hscal, sizeof(double) * 64);
   *out = ctx;
   return PEEC_OK;
@@ -227,6 +261,7 @@ extern "C" int peec_ctx_create(peec_ctx** out, int device) {
 
 static void free_tri(LevelTri& t) {
   cudaFree(t.ptr); cudaFree(t.col); cudaFree(t.rows); cudaFree(t.val); cudaFree(t.dinv);
+  cudaFree(t.doff);
   t = LevelTri();
 }
 
@@ -234,12 +269,13 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->dev);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
+  drop_graphs(ctx);
   void* ptrs[] = {ctx->tw64, ctx->tw32, ctx->n1, ctx->n2, ctx->snode, ctx->invP, ctx->ne_ptr,
                   ctx->ne_idx, ctx->nsn_ptr, ctx->nsn_idx, ctx->DZ, ctx->yle_ptr, ctx->yle_col,
                   ctx->yle_val, ctx->g_in, ctx->g_out, ctx->lu_rs, ctx->LpI, ctx->PQ, ctx->Y1, ctx->U1,
                   ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->dx, ctx->dy, ctx->U,
                   ctx->gb, ctx->gx, ctx->gr, ctx->gv, ctx->gw, ctx->gxm, ctx->gxmin, ctx->gtmp,
-                  ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal,
+                  ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal, ctx->dT,
                   ctx->mdpart};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -256,6 +292,7 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   if (ctx->hx) cudaFreeHost(ctx->hx);
   if (ctx->hy) cudaFreeHost(ctx->hy);
   if (ctx->hsmall) cudaFreeHost(ctx->hsmall);
+  if (ctx->hread) cudaFreeHost(ctx->hread);
   if (ctx->hscal) cudaFreeHost(ctx->hscal);
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
@@ -265,7 +302,7 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
 }
 
 extern "C" int peec_set_stop_flag(peec_ctx* ctx, volatile int* flag) {
-  if (!ctx) return PEEC_ERR_BADARG;
+  if (!ctx) return badarg(__func__);
   ctx->stop = flag;
   return PEEC_OK;
 }
@@ -285,7 +322,8 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
                                  int64_t mz, const int64_t* edge_cell, const int64_t* edge_n1,
                                  const int64_t* edge_n2, int64_t ns, const int32_t* surf_fam,
                                  const int64_t* surf_cell, const int64_t* surf_node, int64_t n) {
-  if (!ctx) return PEEC_ERR_BADARG;
+  drop_graphs(ctx);
+  if (!ctx) return badarg(__func__);
   if (Nx < 1 || Ny < 1 || Nz < 1 || mx < 0 || my < 0 || mz < 0 || ns < 0 || n < 1)
     return bad(ctx, PEEC_ERR_BADARG, "peec_set_topology: invalid sizes");
   const int64_t m = mx + my + mz;
@@ -420,7 +458,8 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
 }
 
 extern "C" int peec_set_pdiag(peec_ctx* ctx, const double* diagP) {
-  if (!ctx || !diagP) return PEEC_ERR_BADARG;
+  drop_graphs(ctx);
+  if (!ctx || !diagP) return badarg(__func__);
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   std::vector<double> inv(ctx->ns);
   for (int64_t s = 0; s < ctx->ns; ++s) inv[s] = 1.0 / diagP[s];
@@ -434,6 +473,7 @@ extern "C" int peec_set_pdiag(peec_ctx* ctx, const double* diagP) {
 // p1256, p3456). Spectrum i uses row srow[i]: P blocks 00, 11, 22 (symmetric), 01, 02, 12
 // (cross: output family f, input family g), then the three Lp blocks.
 static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
+  drop_graphs(ctx);
   static const int srow[9] = {3, 4, 5, 6, 7, 8, 0, 1, 2};
   static const int fout[9] = {0, 1, 2, 0, 0, 1, 3, 4, 5};
   static const int fin[9] = {0, 1, 2, 1, 2, 2, 3, 4, 5};
@@ -456,7 +496,7 @@ static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
 }
 
 extern "C" int peec_set_rows(peec_ctx* ctx, const double* const rows[9]) {
-  if (!ctx || !rows) return PEEC_ERR_BADARG;
+  if (!ctx || !rows) return badarg(__func__);
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
   double* d_rows[9] = {};
@@ -479,7 +519,7 @@ extern "C" int peec_set_rows(peec_ctx* ctx, const double* const rows[9]) {
 
 extern "C" int peec_fill(peec_ctx* ctx, const double origin[3], double sx, double sy, double sz,
                          double escal_Lp, double escal_P, double* const rows_out[9]) {
-  if (!ctx || !origin) return PEEC_ERR_BADARG;
+  if (!ctx || !origin) return badarg(__func__);
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
   double* d_rows[9] = {};
@@ -582,6 +622,26 @@ static int make_tri(peec_ctx* ctx, LevelTri& T, int64_t n, const int64_t* ptr, c
   std::vector<int> fillp(cnt.begin(), cnt.end() - 1);
   for (int64_t r = 0; r < n; ++r) rows[fillp[level[r]]++] = (int32_t)r;
   T.lvl_off.assign(cnt.begin(), cnt.end());
+  // levels with more rows than one CTA handles well get their own grid launch; runs of
+  // consecutive smaller levels share one single-CTA launch
+  constexpr int kSmall = 4096;
+  T.sched.clear();
+  for (int l = 0; l <= maxl;) {
+    const int c0 = cnt[l + 1] - cnt[l];
+    if (c0 > kSmall) {
+      T.sched.push_back({l, l + 1, 1});
+      ++l;
+      continue;
+    }
+    int e = l;
+    while (e <= maxl && cnt[e + 1] - cnt[e] <= kSmall) ++e;
+    T.sched.push_back({l, e, 0});
+    l = e;
+  }
+  {
+    std::vector<int32_t> off32(cnt.begin(), cnt.end());
+    CTX_TRY(upload(&T.doff, off32, ctx->st));
+  }
   CTX_TRY(upload(&T.ptr, p, ctx->st));
   CTX_TRY(upload(&T.col, c, ctx->st));
   CTX_TRY(upload(&T.val, v, ctx->st));
@@ -597,7 +657,8 @@ extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int
                                   const int64_t* U_ptr, const int64_t* U_col,
                                   const double* U_val, const int64_t* perm_r,
                                   const int64_t* perm_c, const double* row_scale) {
-  if (!ctx || !DZ || !L_ptr || !U_ptr || !perm_r || !perm_c) return PEEC_ERR_BADARG;
+  drop_graphs(ctx);
+  if (!ctx || !DZ || !L_ptr || !U_ptr || !perm_r || !perm_c) return badarg(__func__);
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
   const int64_t n = ctx->n, m = ctx->m;
@@ -671,11 +732,16 @@ static void lu_solve(peec_ctx* ctx, const c64* b, c64* x) {
   launch_perm_gather(b, ctx->g_in, ctx->lu_rs, n, ctx->lutmp, ctx->st);
   ctx->launches++;
   for (LevelTri* T : {&ctx->Lf, &ctx->Uf}) {
-    for (size_t l = 0; l + 1 < T->lvl_off.size(); ++l) {
-      const int cnt = T->lvl_off[l + 1] - T->lvl_off[l];
-      if (cnt <= 0) continue;
-      launch_trsv_level(T->rows + T->lvl_off[l], cnt, T->ptr, T->col, T->val, T->dinv, ctx->lutmp,
-                        ctx->st);
+    for (const auto& sg : T->sched) {
+      if (sg[2]) {
+        const int l = sg[0];
+        const int cnt = T->lvl_off[l + 1] - T->lvl_off[l];
+        launch_trsv_level(T->rows + T->lvl_off[l], cnt, T->ptr, T->col, T->val, T->dinv,
+                          ctx->lutmp, ctx->st);
+      } else {
+        launch_trsv_tail(T->rows, T->doff, sg[0], sg[1], T->ptr, T->col, T->val, T->dinv,
+                         ctx->lutmp, ctx->st);
+      }
       ctx->launches++;
     }
   }
@@ -683,17 +749,16 @@ static void lu_solve(peec_ctx* ctx, const c64* b, c64* x) {
   ctx->launches++;
 }
 
-static int matvec_dev(peec_ctx* ctx, const c64* x, c64* y, int prec, bool timed) {
-  if (!ctx->have_topo || !ctx->have_spec || !ctx->have_freq || !ctx->have_pdiag)
-    return bad(ctx, PEEC_ERR_STATE, "operator incomplete (topology, pdiag, rows, frequency)");
+// enqueue one operator application y = M^-1 K x on the context stream
+static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool events) {
   const int64_t m = ctx->m, ns = ctx->ns, n = ctx->n;
   cudaStream_t st = ctx->st;
-  if (timed) cudaEventRecord(ctx->ev[0], st);
+  if (events) cudaEventRecord(ctx->ev[0], st);
   CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, x, ctx->LpI, ctx->PQ, m, prec, ctx->tw64, ctx->tw32,
                    ctx->twmax, st, ctx->prof ? ctx->pev.data() : nullptr));
   for (const auto& F : ctx->fam) ctx->launches += F.active ? (F.lp ? 5 : 4) : 0;
   ctx->launches += 1;  // the shared z pass of the face families
-  if (timed) cudaEventRecord(ctx->ev[1], st);
+  if (events) cudaEventRecord(ctx->ev[1], st);
   const c64* I = x;
   const c64* Q = x + m;
   const c64* Phi = x + m + ns;
@@ -708,14 +773,48 @@ static int matvec_dev(peec_ctx* ctx, const c64* x, c64* y, int prec, bool timed)
   launch_final_rows(ctx->Y1, ctx->Y2, ctx->Mvec, ctx->DZ, ctx->n1, ctx->n2, ctx->snode, ctx->invP,
                     (int)m, (int)ns, (int)n, y, st);
   ctx->launches++;
-  if (timed) cudaEventRecord(ctx->ev[2], st);
+  if (events) cudaEventRecord(ctx->ev[2], st);
+  return PEEC_OK;
+}
+
+static int matvec_dev(peec_ctx* ctx, const c64* x, c64* y, int prec, bool timed) {
+  if (!ctx->have_topo || !ctx->have_spec || !ctx->have_freq || !ctx->have_pdiag)
+    return bad(ctx, PEEC_ERR_STATE, "operator incomplete (topology, pdiag, rows, frequency)");
+  if (timed || ctx->prof || !ctx->use_graphs) {
+    CTX_TRY(matvec_enqueue(ctx, x, y, prec, timed));
+  } else {
+    auto& ge = ctx->graphs[std::make_tuple((const void*)x, (void*)y, prec)];
+    if (ge.exec) {
+      PEEC_CUDA_TRY(cudaGraphLaunch(ge.exec, ctx->st));
+      ctx->launches += ge.kernels;
+    } else if (ge.calls++ == 0) {
+      // first application with these buffers runs eagerly (one-time kernel set-up)
+      CTX_TRY(matvec_enqueue(ctx, x, y, prec, false));
+    } else {
+      const int64_t l0 = ctx->launches;
+      cudaGraph_t g = nullptr;
+      PEEC_CUDA_TRY(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+      const int rc = matvec_enqueue(ctx, x, y, prec, false);
+      const cudaError_t ec = cudaStreamEndCapture(ctx->st, &g);
+      if (rc != PEEC_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (ec != cudaSuccess) return fail_cuda(ec, "cudaStreamEndCapture", __FILE__, __LINE__);
+      const cudaError_t ei = cudaGraphInstantiate(&ge.exec, g, 0);
+      cudaGraphDestroy(g);
+      if (ei != cudaSuccess) return fail_cuda(ei, "cudaGraphInstantiate", __FILE__, __LINE__);
+      ge.kernels = ctx->launches - l0;
+      PEEC_CUDA_TRY(cudaGraphLaunch(ge.exec, ctx->st));
+    }
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail_cuda(e, "matvec launch", __FILE__, __LINE__);
   return PEEC_OK;
 }
 
 extern "C" int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precision) {
-  if (!ctx || !x || !y) return PEEC_ERR_BADARG;
+  if (!ctx || !x || !y) return badarg(__func__);
   if (precision != 0 && precision != 1) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0 or 1");
   cudaSetDevice(ctx->dev);
   CTX_TRY(matvec_dev(ctx, (const c64*)x, (c64*)y, precision, true));
@@ -727,7 +826,7 @@ extern "C" int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precis
 }
 
 extern "C" int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precision) {
-  if (!ctx || !x || !y) return PEEC_ERR_BADARG;
+  if (!ctx || !x || !y) return badarg(__func__);
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
   const size_t bytes = sizeof(c64) * ctx->N;
@@ -744,7 +843,7 @@ extern "C" int peec_conv_count(const peec_ctx* ctx) { return ctx ? 6 : 0; }
 
 extern "C" int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* dims, int* active,
                               int* kind) {
-  if (!ctx || i < 0 || i >= 6) return PEEC_ERR_BADARG;
+  if (!ctx || i < 0 || i >= 6) return badarg(__func__);
   const Family& F = ctx->fam[i];
   for (int k = 0; k < 3; ++k) {
     if (L) L[k] = F.L[k];
@@ -756,7 +855,7 @@ extern "C" int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* dims, int
 }
 
 extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, double* ms) {
-  if (!ctx || !ms || iters < 1) return PEEC_ERR_BADARG;
+  if (!ctx || !ms || iters < 1) return badarg(__func__);
   if (precision != 0 && precision != 1) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0 or 1");
   cudaSetDevice(ctx->dev);
   if (ctx->pev.size() != 6) {
@@ -810,7 +909,7 @@ extern "C" int peec_multidot(peec_ctx* ctx, const void* U, int64_t ldu, const vo
 
 extern "C" int peec_last_timing(peec_ctx* ctx, double* total_ms, double* conv_ms,
                                 double* sparse_ms) {
-  if (!ctx) return PEEC_ERR_BADARG;
+  if (!ctx) return badarg(__func__);
   if (total_ms) *total_ms = ctx->t_total;
   if (conv_ms) *conv_ms = ctx->t_conv;
   if (sparse_ms) *sparse_ms = ctx->t_sparse;
@@ -818,7 +917,7 @@ extern "C" int peec_last_timing(peec_ctx* ctx, double* total_ms, double* conv_ms
 }
 
 extern "C" int peec_port_rhs(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, double* tn) {
-  if (!ctx || !tn) return PEEC_ERR_BADARG;
+  if (!ctx || !tn) return badarg(__func__);
   if (!ctx->have_freq || !ctx->have_pdiag) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
   if (n1 < 0 || n1 >= ctx->n || n2 < 0 || n2 >= ctx->n) return bad(ctx, PEEC_ERR_BADARG, "port node out of range");
   cudaSetDevice(ctx->dev);
@@ -851,8 +950,9 @@ static int ensure_krylov(peec_ctx* ctx, int k) {
                   &ctx->gtmp, &ctx->gzero})
     CTX_TRY(dalloc(p, N));
   PEEC_CUDA_TRY(cudaMemsetAsync(ctx->gzero, 0, sizeof(c64) * N, ctx->st));
-  CTX_TRY(dalloc(&ctx->dcoef, 2 * (size_t)k + 16));  // apply_Q stages 2k coefficients
+  CTX_TRY(dalloc(&ctx->dcoef, 2 * (size_t)k + 16));  // xupdate stages 2k coefficients
   CTX_TRY(dalloc(&ctx->dcoef2, 2 * (size_t)k + 16));
+  CTX_TRY(dalloc(&ctx->dT, (size_t)k * k));            // compact-WY T, ld = k
   const int nb = red_blocks(N);
   CTX_TRY(dalloc(&ctx->dpart, (size_t)nb * (k + 8)));
   CTX_TRY(dalloc(&ctx->dred, nb + 8));
@@ -863,25 +963,38 @@ static int ensure_krylov(peec_ctx* ctx, int k) {
 
 namespace {
 
+// Host side of the Householder GMRES. Vectors of length N live on the device; the
+// compact-WY matrix T (reflector products P1..Pk = I - U T U^H) lives on the device
+// and is only touched by small kernels; the leading rows Utop of the reflectors, the
+// Givens rotations, R and w are host FP64 arrays. Host -> device coefficient vectors
+// go through a ring of pinned slots, so only reads of scalars the control flow needs
+// synchronise the stream.
 struct Gm {
   peec_ctx* ctx;
   size_t N;
   int prec;
   cudaStream_t st;
   int rc = PEEC_OK;
+  int ring = 0;
+  int pending = 0;  // uploads queued since the last stream synchronisation
+
+  void sync() {
+    if (cudaStreamSynchronize(st) != cudaSuccess && rc == PEEC_OK)
+      rc = fail_cuda(cudaGetLastError(), "sync", __FILE__, __LINE__);
+    pending = 0;
+  }
 
   double norm(const c64* v, size_t i0 = 0) {
     launch_norm2(v, N, i0, ctx->dred, ctx->dscal, st);
     ctx->launches += 2;
     cudaMemcpyAsync(ctx->hscal, ctx->dscal, sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) rc = fail_cuda(cudaGetLastError(), "norm", __FILE__, __LINE__);
+    sync();
     return std::sqrt(ctx->hscal[0]);
   }
   void matvec(const c64* x, c64* y) {
     if (rc == PEEC_OK) rc = matvec_dev(ctx, x, y, prec, false);
   }
-  // out = b - A x
-  void residual(const c64* b, const c64* x, c64* out) {
+  void residual(const c64* b, const c64* x, c64* out) {  // out = b - A x
     matvec(x, ctx->gtmp);
     launch_sub(b, ctx->gtmp, N, out, st);
     ctx->launches++;
@@ -889,18 +1002,24 @@ struct Gm {
   void copy(c64* dst, const c64* src) {
     cudaMemcpyAsync(dst, src, sizeof(c64) * N, cudaMemcpyDeviceToDevice, st);
   }
+  // asynchronous upload through the pinned ring (slots of kSlot entries)
   void to_dev(c64* d, const std::vector<cd>& h) {
-    for (size_t i = 0; i < h.size(); ++i) ctx->hsmall[i] = mk<double>(h[i].real(), h[i].imag());
-    cudaMemcpyAsync(d, ctx->hsmall, sizeof(c64) * h.size(), cudaMemcpyHostToDevice, st);
-    cudaStreamSynchronize(st);  // hsmall is reused
+    if (pending == kSlots) sync();  // every slot may still feed a queued copy
+    pending++;
+    const size_t slot = (size_t)(ring++ % kSlots) * kSlot;
+    for (size_t i = 0; i < h.size(); ++i)
+      ctx->hsmall[slot + i] = mk<double>(h[i].real(), h[i].imag());
+    cudaMemcpyAsync(d, ctx->hsmall + slot, sizeof(c64) * h.size(), cudaMemcpyHostToDevice, st);
   }
   std::vector<cd> from_dev(const c64* d, size_t cnt) {
-    cudaMemcpyAsync(ctx->hsmall, d, sizeof(c64) * cnt, cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) rc = fail_cuda(cudaGetLastError(), "d2h", __FILE__, __LINE__);
+    cudaMemcpyAsync(ctx->hread, d, sizeof(c64) * cnt, cudaMemcpyDeviceToHost, st);
+    sync();
     std::vector<cd> h(cnt);
-    for (size_t i = 0; i < cnt; ++i) h[i] = cd(ctx->hsmall[i].x, ctx->hsmall[i].y);
+    for (size_t i = 0; i < cnt; ++i) h[i] = cd(ctx->hread[i].x, ctx->hread[i].y);
     return h;
   }
+  static constexpr int kSlots = 16;
+  static constexpr int kSlot = 4096;
 };
 
 cd sgn(cd d) {
@@ -920,26 +1039,23 @@ std::vector<cd> utri_solve(const std::vector<cd>& R, int ld, int k, std::vector<
 
 }  // namespace
 
-// Q_k y applied on device: out = [y;0] - U(:,0:k) (T_k (Utop(0:k,0:k)^H y)) (+ base)
-static void apply_Q(Gm& g, const std::vector<cd>& T, const std::vector<cd>& Utop, int ldt, int k,
-                    const std::vector<cd>& y, const c64* base, c64* out) {
-  std::vector<cd> h(k), c(k);
+// out = base + Q_k [y; 0] = base + [y;0] - U(:,0:k) (T_k (Utop(0:k,0:k)^H y))
+static void apply_Q(Gm& g, const std::vector<cd>& Utop, int ldt, int k, const std::vector<cd>& y,
+                    const c64* base, c64* out) {
+  peec_ctx* ctx = g.ctx;
+  std::vector<cd> h(k);
   for (int col = 0; col < k; ++col) {
     cd s = 0;
     for (int row = 0; row < k; ++row) s += std::conj(Utop[(size_t)col * ldt + row]) * y[row];
     h[col] = s;
   }
-  for (int i = 0; i < k; ++i) {
-    cd s = 0;
-    for (int j = i; j < k; ++j) s += T[(size_t)j * ldt + i] * h[j];
-    c[i] = s;
-  }
-  std::vector<cd> both(c);
-  both.insert(both.end(), y.begin(), y.begin() + k);
-  g.to_dev(g.ctx->dcoef, both);
-  launch_xupdate(base ? base : g.ctx->gzero, g.ctx->U, g.N, g.ctx->dcoef, g.ctx->dcoef + k, k, g.N,
-                 out, g.st);
-  g.ctx->launches++;
+  std::vector<cd> yy(y.begin(), y.begin() + k);
+  g.to_dev(ctx->dcoef2, h);
+  g.to_dev(ctx->dcoef + k, yy);
+  launch_tri(ctx->dT, ctx->kcap, k, ctx->dcoef2, ctx->dcoef, 0, g.st);  // c = T h
+  launch_xupdate(base ? base : ctx->gzero, ctx->U, g.N, ctx->dcoef, ctx->dcoef + k, k, g.N, out,
+                 g.st);
+  ctx->launches += 2;
 }
 
 static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, int maxit,
@@ -957,9 +1073,10 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
     inner = maxit;
   }
   if (inner < 1) inner = 1;
-  if (2 * (inner + 1) > 4096) return bad(ctx, PEEC_ERR_UNSUPPORTED, "inner iterations above 2047");
+  if (2 * (inner + 1) > Gm::kSlot) return bad(ctx, PEEC_ERR_UNSUPPORTED, "inner iterations above 2047");
   CTX_TRY(ensure_krylov(ctx, inner + 1));
   Gm g{ctx, N, prec, ctx->st};
+  const int ldT = ctx->kcap;
   c64 *b = ctx->gb, *x = ctx->gx, *r = ctx->gr, *v = ctx->gv, *xm = ctx->gxm,
       *xmin = ctx->gxmin, *add = ctx->gw;
   g.copy(b, b_dev);
@@ -997,28 +1114,28 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
   double normrmin = normr;
   const int ld = inner + 1;
   std::vector<cd> J(2 * (size_t)inner), R((size_t)inner * inner), wv(inner + 1);
-  std::vector<cd> T((size_t)ld * ld), Utop((size_t)ld * ld);
+  std::vector<cd> Utop((size_t)ld * ld);
   int outitercount = 0, initercount = 0;
   double normr_act = normr;
   int it0 = 0, it1 = 0;
   const int headlen = (int)std::min<size_t>(N, (size_t)ld);
   for (int outiter = 1; outiter <= outer; ++outiter) {
     outitercount++;
-    std::fill(T.begin(), T.end(), cd(0));
     std::fill(Utop.begin(), Utop.end(), cd(0));
+    PEEC_CUDA_TRY(cudaMemsetAsync(ctx->dT, 0, sizeof(c64) * (size_t)ldT * ldT, ctx->st));
     // u = r + sign(r1)*norm(r)*e1, normalised (later restart cycles use the true
     // residual norm of the end-of-cycle residual)
     if (outiter > 1) normr = g.norm(r);
     {
-      const std::vector<cd> rh = g.from_dev(r, 1);
+      const std::vector<cd> rh = g.from_dev(r, headlen);
       const cd beta = sgn(rh[0]) * normr;
       const double nu2 = normr * normr - std::norm(rh[0]) + std::norm(rh[0] + beta);
-      launch_make_reflector(r, N, 0, mk<double>(beta.real(), beta.imag()), 1.0 / std::sqrt(nu2),
-                            ctx->U, ctx->st);
+      const double sc = 1.0 / std::sqrt(nu2);
+      launch_make_reflector(r, N, 0, mk<double>(beta.real(), beta.imag()), sc, ctx->U, ctx->st);
       ctx->launches++;
-      const std::vector<cd> uh = g.from_dev(ctx->U, headlen);
-      for (int i = 0; i < headlen; ++i) Utop[i] = uh[i];
-      T[0] = 2.0;
+      for (int i = 0; i < headlen; ++i) Utop[i] = (i == 0 ? rh[0] + beta : rh[i]) * sc;
+      launch_tri(ctx->dT, ldT, 0, ctx->dcoef2, ctx->dT, 2, ctx->st);  // T(0,0) = 2
+      ctx->launches++;
       wv.assign(inner + 1, cd(0));
       wv[0] = -beta;
     }
@@ -1027,25 +1144,21 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
       if (ctx->stop && *ctx->stop) {
         *flag_out = 99; *relres_out = 0; iter_out[0] = outiter; iter_out[1] = initer;
         resvec_out.assign(1, 0.0);
-        return PEEC_ERR_CANCELLED;
+        return bad(ctx, PEEC_ERR_CANCELLED, "cancelled by stop flag");
       }
       initercount++;
       const int j = initer - 1;
+      const int k = initer;
       // v = P1..Pj e_j = e_j - U T conj(Utop(j,0:j+1))
       {
-        const int k = initer;
-        std::vector<cd> rb(k), c(k);
+        std::vector<cd> rb(k);
         for (int col = 0; col < k; ++col) rb[col] = std::conj(Utop[(size_t)col * ld + j]);
-        for (int i = 0; i < k; ++i) {
-          cd s = 0;
-          for (int jj = i; jj < k; ++jj) s += T[(size_t)jj * ld + i] * rb[jj];
-          c[i] = s;
-        }
-        g.to_dev(ctx->dcoef, c);
+        g.to_dev(ctx->dcoef2, rb);
+        launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dcoef, 0, ctx->st);
         launch_multiaxpy(ctx->U, N, nullptr, j, ctx->dcoef, k, N, v, N, nullptr, ctx->st);
         launch_norm2(v, N, 0, ctx->dred, ctx->dscal, ctx->st);
         launch_scale_rnorm(v, N, ctx->dscal, ctx->st);
-        ctx->launches += 4;
+        ctx->launches += 5;
       }
       g.matvec(v, add);  // add <- A v
       if (g.rc) return g.rc;
@@ -1053,21 +1166,12 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
       double alpha2 = 0.0;
       std::vector<cd> vh;
       {
-        const int k = initer;
         launch_multidot(ctx->U, N, add, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
-        ctx->launches += 2;
-        std::vector<cd> z = g.from_dev(ctx->dcoef2, k);
-        std::vector<cd> c(k);
-        for (int i = 0; i < k; ++i) {  // T^H z
-          cd s = 0;
-          for (int jj = 0; jj <= i; ++jj) s += std::conj(T[(size_t)i * ld + jj]) * z[jj];
-          c[i] = s;
-        }
-        g.to_dev(ctx->dcoef, c);
+        launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dcoef, 1, ctx->st);  // c = T^H z
         launch_multiaxpy(ctx->U, N, add, 0, ctx->dcoef, k, N, v, (size_t)initer, ctx->dred,
                          ctx->st);
         launch_sum_parts(ctx->dred, red_blocks(N), ctx->dscal, ctx->st);
-        ctx->launches += 2;
+        ctx->launches += 5;
         cudaMemcpyAsync(ctx->hscal, ctx->dscal, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
         vh = g.from_dev(v, headlen);
         alpha2 = ctx->hscal[0];
@@ -1081,23 +1185,16 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
           const cd vj1 = vh[initer];
           const cd a = sgn(vj1) * alpha;
           const double nu2 = alpha2 - std::norm(vj1) + std::norm(vj1 + a);
-          launch_make_reflector(v, N, initer, mk<double>(a.real(), a.imag()),
-                                1.0 / std::sqrt(nu2), ctx->U + (size_t)initer * N, ctx->st);
-          ctx->launches++;
-          const std::vector<cd> uh = g.from_dev(ctx->U + (size_t)initer * N, headlen);
-          for (int i = 0; i < headlen; ++i) Utop[(size_t)initer * ld + i] = uh[i];
-          // T(0:k, k) = -2 T(0:k,0:k) (U(:,0:k)^H u_k), T(k,k) = 2
-          const int k = initer;
-          launch_multidot(ctx->U, N, ctx->U + (size_t)initer * N, N, k, ctx->dpart, ctx->dcoef2,
-                          ctx->st);
-          ctx->launches += 2;
-          const std::vector<cd> gg = g.from_dev(ctx->dcoef2, k);
-          for (int i = 0; i < k; ++i) {
-            cd s = 0;
-            for (int jj = i; jj < k; ++jj) s += T[(size_t)jj * ld + i] * gg[jj];
-            T[(size_t)k * ld + i] = -2.0 * s;
-          }
-          T[(size_t)k * ld + k] = 2.0;
+          const double sc = 1.0 / std::sqrt(nu2);
+          c64* unew = ctx->U + (size_t)initer * N;
+          launch_make_reflector(v, N, initer, mk<double>(a.real(), a.imag()), sc, unew, ctx->st);
+          for (int i = 0; i < headlen; ++i)
+            Utop[(size_t)initer * ld + i] =
+                i < initer ? cd(0) : (i == initer ? (vh[i] + a) * sc : vh[i] * sc);
+          // T(0:k, k) = -2 T(0:k,0:k) (U(:,0:k)^H u_k), T(k,k) = 2 -- all on the device
+          launch_multidot(ctx->U, N, unew, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
+          launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dT + (size_t)k * ldT, 2, ctx->st);
+          ctx->launches += 4;
           for (int i = initer + 1; i <= inner; ++i) vs[i] = 0;
           vs[initer] = -a;
         }
@@ -1125,12 +1222,12 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
         if (evalxm == 0) {
           std::vector<cd> rhs(wv.begin(), wv.begin() + initer);
           std::vector<cd> ytmp = utri_solve(R, inner, initer, rhs);
-          apply_Q(g, T, Utop, ld, initer, ytmp, nullptr, add);
+          apply_Q(g, Utop, ld, initer, ytmp, nullptr, add);
           const double na = g.norm(add), nx = g.norm(x);
           if (na < 2.220446049250313e-16 * nx) stag++;
           else stag = 0;
           // xm = x + additive
-          apply_Q(g, T, Utop, ld, initer, ytmp, x, xm);
+          apply_Q(g, Utop, ld, initer, ytmp, x, xm);
           evalxm = 1;
         } else {
           const cd wr = wv[j] / R[(size_t)j * inner + j];
@@ -1149,7 +1246,7 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
           if (nav < 2.220446049250313e-16 * nxm) stag++;
           else stag = 0;
           g.copy(ctx->gtmp, xm);
-          apply_Q(g, T, Utop, ld, initer, addvc, ctx->gtmp, xm);
+          apply_Q(g, Utop, ld, initer, addvc, ctx->gtmp, xm);
         }
         g.residual(b, xm, r);
         const double nr = g.norm(r);
@@ -1205,7 +1302,7 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
         std::vector<cd> rhs(wv.begin(), wv.begin() + idx);
         std::vector<cd> y = utri_solve(R, inner, idx, rhs);
         g.copy(ctx->gtmp, x);
-        apply_Q(g, T, Utop, ld, idx, y, ctx->gtmp, x);
+        apply_Q(g, Utop, ld, idx, y, ctx->gtmp, x);
       }
       g.copy(xmin, x);
       g.residual(b, x, r);
@@ -1250,7 +1347,7 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
 extern "C" int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, double tol, int maxit,
                           int restarted, int restart, int precision, int* flag, double* relres,
                           int* iter, double* resvec, int resvec_cap, int* nres) {
-  if (!ctx || !b || !x_inout || !flag || !relres || !iter) return PEEC_ERR_BADARG;
+  if (!ctx || !b || !x_inout || !flag || !relres || !iter) return badarg(__func__);
   if (maxit < 1 || (restarted && restart < 1)) return bad(ctx, PEEC_ERR_BADARG, "maxit/restart must be >= 1");
   if (precision != 0 && precision != 1) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0 or 1");
   if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
@@ -1275,7 +1372,7 @@ extern "C" int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, doubl
 extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout, double tol,
                                 double inner_tol, int inner_maxit, int max_outer, int* flag,
                                 double* relres, int* outer_out, int* inner_total) {
-  if (!ctx || !b || !x_inout || !flag || !relres) return PEEC_ERR_BADARG;
+  if (!ctx || !b || !x_inout || !flag || !relres) return badarg(__func__);
   if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
   cudaSetDevice(ctx->dev);
   const size_t N = ctx->N, bytes = sizeof(c64) * N;
@@ -1308,7 +1405,7 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
       rel = nr / n2b;
       if (rel <= tol) { fl = 0; break; }
       if (outer == max_outer) break;
-      if (ctx->stop && *ctx->stop) { cleanup(); ctx->err = "cancelled by stop flag"; *flag = 99; return PEEC_ERR_CANCELLED; }
+      if (ctx->stop && *ctx->stop) { cleanup(); ctx->err = g_err = "cancelled by stop flag"; *flag = 99; return PEEC_ERR_CANCELLED; }
       // inner correction on the FP32-convolution operator, zero initial guess
       cudaMemsetAsync(dd, 0, bytes, ctx->st);
       const double itol = std::max(inner_tol, 0.5 * tol / rel);

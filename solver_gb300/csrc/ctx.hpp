@@ -13,6 +13,8 @@ namespace peec {
 int fail_cuda(cudaError_t e, const char* expr, const char* file, int line);
 void set_error(const std::string& msg);
 
+#define PEEC_ERR_UNSUPPORTED_INTERNAL (-6)
+
 #define CTX_CHECK(expr)      \
   do {                       \
     int _r = (expr);         \

@@ -26,6 +26,10 @@
 // loads, stores and butterflies are bank-conflict free and index math is shifts.
 // Spectra carry the 1/(Lx*Ly*Lz) normalisation and are stored (ky, kz, kx), kx fastest,
 // in the transforms' bit-reversed position order.
+#include <mutex>
+#include <set>
+#include <utility>
+
 #include "ctx.hpp"
 #include "fft.cuh"
 
@@ -256,11 +260,27 @@ __global__ void __launch_bounds__(TPB) k_zconv1(cx<R>* T0, int nz0, const R* __r
 
 // --------------------------------------------------------------------------- host side
 
+// Dynamic shared memory above 48 KB needs a per-kernel opt-in. It is set once per
+// kernel instantiation to the device maximum (at context set-up, outside any launch
+// sequence), so operator applications only launch kernels.
 template <typename K>
 static int smem_optin(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024) {
-    PEEC_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)bytes));
+  // kernels sharing a signature share K, so the record is keyed by address and device
+  static std::mutex mu;
+  static std::set<std::pair<const void*, int>> done;
+  if (bytes > 227 * 1024) {
+    set_error("shared memory tile exceeds 227 KB: grid too large for this build");
+    return PEEC_ERR_UNSUPPORTED_INTERNAL;
+  }
+  int dev = 0;
+  PEEC_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair((const void*)kernel, dev);
+  if (!done.count(key)) {
+    int maxsm = 0;
+    PEEC_CUDA_TRY(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    PEEC_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm));
+    done.insert(key);
   }
   return 0;
 }

@@ -187,6 +187,24 @@ __global__ void k_add(const c64* __restrict__ a, const c64* __restrict__ b, size
     out[i] = a[i] + b[i];
 }
 
+// Small dense triangular products of the compact-WY representation (T upper
+// triangular, column-major with leading dimension ld), one CTA.
+// mode 0: out = T(0:k,0:k) * in;  mode 1: out = T(0:k,0:k)^H * in;
+// mode 2: T(0:k, k) = -2 T(0:k,0:k) * in, T(k,k) = 2 (append a reflector)
+__global__ void k_tri(c64* T, int ld, int k, const c64* __restrict__ in, c64* out, int mode) {
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    c64 s = mk<double>(0, 0);
+    if (mode == 1) {
+      for (int j = 0; j <= i; ++j) s = s + cconj(T[(size_t)i * ld + j]) * in[j];
+    } else {
+      for (int j = i; j < k; ++j) s = s + T[(size_t)j * ld + i] * in[j];
+    }
+    if (mode == 2) out[i] = cscale(s, -2.0);
+    else out[i] = s;
+  }
+  if (mode == 2 && threadIdx.x == 0) out[k] = mk<double>(2.0, 0.0);
+}
+
 __global__ void k_cast_down(const c64* __restrict__ a, size_t N, c32* out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
        i += (size_t)gridDim.x * blockDim.x)
@@ -246,6 +264,10 @@ void launch_sub(const c64* a, const c64* b, size_t N, c64* out, cudaStream_t st)
 
 void launch_add(const c64* a, const c64* b, size_t N, c64* out, cudaStream_t st) {
   k_add<<<g_stream(N), 256, 0, st>>>(a, b, N, out);
+}
+
+void launch_tri(c64* T, int ld, int k, const c64* in, c64* out, int mode, cudaStream_t st) {
+  k_tri<<<1, 256, 0, st>>>(T, ld, k, in, out, mode);
 }
 
 void launch_xupdate(const c64* x, const c64* U, size_t ldu, const c64* coef, const c64* ypad,

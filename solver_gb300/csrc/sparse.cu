@@ -128,6 +128,27 @@ __global__ void k_trsv_level(const int32_t* __restrict__ rows, int nrows,
   }
 }
 
+// a run of consecutive small levels [l0, l1) in one CTA: levels in order, rows of a
+// level spread over the block, __syncthreads() between levels makes each level's
+// results visible to the next (no inter-block dependencies, no waiting)
+__global__ void __launch_bounds__(1024) k_trsv_tail(const int32_t* __restrict__ rows,
+                                                    const int32_t* __restrict__ lvl_off, int l0,
+                                                    int l1, const int32_t* __restrict__ ptr,
+                                                    const int32_t* __restrict__ col,
+                                                    const c64* __restrict__ val,
+                                                    const c64* __restrict__ dinv, c64* x) {
+  for (int l = l0; l < l1; ++l) {
+    const int a = lvl_off[l], b = lvl_off[l + 1];
+    for (int t = a + threadIdx.x; t < b; t += blockDim.x) {
+      const int r = rows[t];
+      c64 acc = x[r];
+      for (int p = ptr[r]; p < ptr[r + 1]; ++p) acc = acc - val[p] * x[col[p]];
+      x[r] = acc * dinv[r];
+    }
+    __syncthreads();
+  }
+}
+
 static inline unsigned grid_for(long long n, int tpb = 256) {
   long long g = (n + tpb - 1) / tpb;
   if (g < 1) g = 1;
@@ -169,4 +190,12 @@ void launch_trsv_level(const int32_t* rows, int nrows, const int32_t* ptr, const
   k_trsv_level<<<grid_for(nrows), 256, 0, st>>>(rows, nrows, ptr, col, val, dinv, x);
 }
 
+}  // namespace peec
+
+namespace peec {
+void launch_trsv_tail(const int32_t* rows, const int32_t* lvl_off, int l0, int l1,
+                      const int32_t* ptr, const int32_t* col, const c64* val, const c64* dinv,
+                      c64* x, cudaStream_t st) {
+  k_trsv_tail<<<1, 1024, 0, st>>>(rows, lvl_off, l0, l1, ptr, col, val, dinv, x);
+}
 }  // namespace peec

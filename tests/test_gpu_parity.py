@@ -227,3 +227,26 @@ def test_native_frequency_sweep():
     e = _rel(got["Z"], ref["Z"])
     assert e < 1e-8, e
     op.close()
+
+
+def test_matvec_large_tiles():
+    """A grid whose FFT lengths (Ly = 256, Lz = 128) put every pass's shared-memory
+    tile above 48 KB, so each kernel instantiation needs its own opt-in: the forward
+    and inverse y passes, the combined and single z passes, in FP64 and FP32."""
+    c = _case(configs.random_mixed((12, 72, 40), s=5e-5, p=0.3, seed=11, nports=1,
+                                   freqs=[1e9], tol=1e-8))
+    op = GpuOperator(c["inc"], c["exp"], c["diag"]["P"])
+    try:
+        op.set_rows(c["rows"])
+        c["op"] = op
+        Ls = [f["L"] for f in op.conv_info() if f["active"]]
+        assert max(L[1] for L in Ls) >= 256 and max(L[2] for L in Ls) >= 128, Ls
+        w, fs = _freq(c)
+        rng = np.random.default_rng(12)
+        x = rng.standard_normal(op.N) + 1j * rng.standard_normal(op.N)
+        y_ref = _oracle_mv(c, w, fs)(x)
+        noise = _rel(_single_solve_oracle(c, w, fs)(x), y_ref)
+        assert _rel(op.matvec(x, 0), y_ref) < max(1e-10, 20 * noise)
+        assert _rel(op.matvec(x, 1), y_ref) < 2e-5
+    finally:
+        op.close()
