@@ -46,10 +46,8 @@ void launch_final_rows(const c64*, const c64*, const c64*, const c64*, const int
                        const int32_t*, const int32_t*, const double*, int, int, int, c64*,
                        cudaStream_t);
 void launch_perm_gather(const c64*, const int32_t*, const double*, int, c64*, cudaStream_t);
-void launch_trsv_level(const int32_t*, int, const int32_t*, const int32_t*, const c64*,
-                       const c64*, c64*, cudaStream_t);
-void launch_trsv_tail(const int32_t*, const int32_t*, int, int, const int32_t*, const int32_t*,
-                      const c64*, const c64*, c64*, cudaStream_t);
+void launch_sptrsv(const int32_t*, int, int, const SfTri&, const SfTri&, const c64*,
+                   const int32_t*, const double*, c64*, c64*, int*, cudaStream_t);
 int red_blocks(size_t N);
 void launch_multidot(const c64*, size_t, const c64*, size_t, int, c64*, c64*, cudaStream_t);
 void launch_multiaxpy(const c64*, size_t, const c64*, int, const c64*, int, size_t, c64*, size_t,
@@ -72,13 +70,12 @@ int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, doubl
 using namespace peec;
 using cd = std::complex<double>;
 
-struct LevelTri {  // triangular factor without its diagonal, level-scheduled
-  int32_t *ptr = nullptr, *col = nullptr, *rows = nullptr, *doff = nullptr;
+struct LevelTri {  // triangular factor without its diagonal (CSR) and its level sets
+  int32_t *ptr = nullptr, *col = nullptr, *flag = nullptr;
   c64 *val = nullptr, *dinv = nullptr;
-  std::vector<int> lvl_off;  // offsets into rows per level
-  // schedule: (first level, end level, big) -- a big level is one grid launch, a run of
-  // small levels one single-CTA launch
-  std::vector<std::array<int, 3>> sched;
+  int64_t nflag = 0;
+  std::vector<int32_t> rows;     // rows sorted by level (host)
+  std::vector<int> lvl_off;      // offsets into rows per level (host)
 };
 
 struct peec_ctx {
@@ -109,10 +106,16 @@ struct peec_ctx {
   c64* yle_val = nullptr;
   int32_t *g_in = nullptr, *g_out = nullptr;  // LU permutations as gathers
   double* lu_rs = nullptr;                    // optional row scaling of the LU
+  // synchronisation-free triangular solves: claim order (L levels then U levels, each
+  // padded with -1 to whole warps), its length, the L part's length, control words
+  int32_t* sf_ord = nullptr;
+  c64 *ir_b = nullptr, *ir_x = nullptr, *ir_r = nullptr, *ir_d = nullptr;  // refinement vectors
+  int sf_total = 0, sf_nL = 0;
+  int* sf_ctl = nullptr;  // [epoch, claim counter, error flag]
   LevelTri Lf, Uf;
   // matvec work
   c64 *LpI = nullptr, *PQ = nullptr, *Y1 = nullptr, *U1 = nullptr, *Y2 = nullptr, *U2 = nullptr;
-  c64 *tvec = nullptr, *Mvec = nullptr, *lutmp = nullptr;
+  c64 *tvec = nullptr, *Mvec = nullptr, *lutmp = nullptr, *lutmp2 = nullptr;
   // host staging
   c64 *hx = nullptr, *hy = nullptr;  // pinned N
   c64 *dx = nullptr, *dy = nullptr;  // device N
@@ -260,8 +263,7 @@ extern "C" int peec_ctx_create(peec_ctx** out, int device) {
 }
 
 static void free_tri(LevelTri& t) {
-  cudaFree(t.ptr); cudaFree(t.col); cudaFree(t.rows); cudaFree(t.val); cudaFree(t.dinv);
-  cudaFree(t.doff);
+  cudaFree(t.ptr); cudaFree(t.col); cudaFree(t.val); cudaFree(t.dinv); cudaFree(t.flag);
   t = LevelTri();
 }
 
@@ -273,7 +275,7 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   void* ptrs[] = {ctx->tw64, ctx->tw32, ctx->n1, ctx->n2, ctx->snode, ctx->invP, ctx->ne_ptr,
                   ctx->ne_idx, ctx->nsn_ptr, ctx->nsn_idx, ctx->DZ, ctx->yle_ptr, ctx->yle_col,
                   ctx->yle_val, ctx->g_in, ctx->g_out, ctx->lu_rs, ctx->LpI, ctx->PQ, ctx->Y1, ctx->U1,
-                  ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->dx, ctx->dy, ctx->U,
+                  ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->lutmp2, ctx->dx, ctx->dy, ctx->U,
                   ctx->gb, ctx->gx, ctx->gr, ctx->gv, ctx->gw, ctx->gxm, ctx->gxmin, ctx->gtmp,
                   ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal, ctx->dT,
                   ctx->mdpart};
@@ -289,6 +291,9 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
       if (s.d[p]) cudaFree(s.d[p]);
   free_tri(ctx->Lf);
   free_tri(ctx->Uf);
+  cudaFree(ctx->sf_ord);
+  cudaFree(ctx->sf_ctl);
+  for (c64* p : {ctx->ir_b, ctx->ir_x, ctx->ir_r, ctx->ir_d}) cudaFree(p);
   if (ctx->hx) cudaFreeHost(ctx->hx);
   if (ctx->hy) cudaFreeHost(ctx->hy);
   if (ctx->hsmall) cudaFreeHost(ctx->hsmall);
@@ -444,8 +449,10 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
   CTX_TRY(dalloc(&ctx->tvec, n));
   CTX_TRY(dalloc(&ctx->Mvec, n));
   CTX_TRY(dalloc(&ctx->lutmp, n));
+  CTX_TRY(dalloc(&ctx->lutmp2, n));
   CTX_TRY(dalloc(&ctx->dx, ctx->N));
   CTX_TRY(dalloc(&ctx->dy, ctx->N));
+  for (c64** p : {&ctx->ir_b, &ctx->ir_x, &ctx->ir_r, &ctx->ir_d}) CTX_TRY(dalloc(p, ctx->N));
   if (ctx->hx) cudaFreeHost(ctx->hx);
   if (ctx->hy) cudaFreeHost(ctx->hy);
   PEEC_CUDA_TRY(cudaMallocHost(&ctx->hx, sizeof(c64) * ctx->N));
@@ -622,31 +629,15 @@ static int make_tri(peec_ctx* ctx, LevelTri& T, int64_t n, const int64_t* ptr, c
   std::vector<int> fillp(cnt.begin(), cnt.end() - 1);
   for (int64_t r = 0; r < n; ++r) rows[fillp[level[r]]++] = (int32_t)r;
   T.lvl_off.assign(cnt.begin(), cnt.end());
-  // levels with more rows than one CTA handles well get their own grid launch; runs of
-  // consecutive smaller levels share one single-CTA launch
-  constexpr int kSmall = 4096;
-  T.sched.clear();
-  for (int l = 0; l <= maxl;) {
-    const int c0 = cnt[l + 1] - cnt[l];
-    if (c0 > kSmall) {
-      T.sched.push_back({l, l + 1, 1});
-      ++l;
-      continue;
-    }
-    int e = l;
-    while (e <= maxl && cnt[e + 1] - cnt[e] <= kSmall) ++e;
-    T.sched.push_back({l, e, 0});
-    l = e;
-  }
-  {
-    std::vector<int32_t> off32(cnt.begin(), cnt.end());
-    CTX_TRY(upload(&T.doff, off32, ctx->st));
-  }
+  T.rows = std::move(rows);
   CTX_TRY(upload(&T.ptr, p, ctx->st));
   CTX_TRY(upload(&T.col, c, ctx->st));
   CTX_TRY(upload(&T.val, v, ctx->st));
   CTX_TRY(upload(&T.dinv, dinv, ctx->st));
-  CTX_TRY(upload(&T.rows, rows, ctx->st));
+  // ready flags start below every epoch the solve will use (epochs start at 1)
+  CTX_TRY(dalloc(&T.flag, (size_t)n));
+  PEEC_CUDA_TRY(cudaMemsetAsync(T.flag, 0, sizeof(int32_t) * n, ctx->st));
+  T.nflag = n;
   return PEEC_OK;
 }
 
@@ -718,6 +709,24 @@ extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int
   }
   CTX_TRY(make_tri(ctx, ctx->Lf, n, L_ptr, L_col, L_val, true));
   CTX_TRY(make_tri(ctx, ctx->Uf, n, U_ptr, U_col, U_val, false));
+  {
+    std::vector<int32_t> ord;
+    ord.reserve(2 * n + 64 * (ctx->Lf.lvl_off.size() + ctx->Uf.lvl_off.size()));
+    for (const LevelTri* T : {&ctx->Lf, &ctx->Uf}) {
+      for (size_t l = 0; l + 1 < T->lvl_off.size(); ++l) {
+        for (int q = T->lvl_off[l]; q < T->lvl_off[l + 1]; ++q) ord.push_back(T->rows[q]);
+        while (ord.size() % 32) ord.push_back(-1);
+      }
+      if (T == &ctx->Lf) ctx->sf_nL = (int)ord.size();
+    }
+    if (ord.size() > (size_t)INT32_MAX - 64) return bad(ctx, PEEC_ERR_UNSUPPORTED, "LU too large");
+    ctx->sf_total = (int)ord.size();
+    CTX_TRY(upload(&ctx->sf_ord, ord, ctx->st));
+    if (!ctx->sf_ctl) {
+      CTX_TRY(dalloc(&ctx->sf_ctl, 4));
+      PEEC_CUDA_TRY(cudaMemsetAsync(ctx->sf_ctl, 0, sizeof(int) * 4, ctx->st));
+    }
+  }
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->have_freq = true;
   return PEEC_OK;
@@ -729,24 +738,26 @@ extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int
 
 static void lu_solve(peec_ctx* ctx, const c64* b, c64* x) {
   const int n = (int)ctx->n;
-  launch_perm_gather(b, ctx->g_in, ctx->lu_rs, n, ctx->lutmp, ctx->st);
-  ctx->launches++;
-  for (LevelTri* T : {&ctx->Lf, &ctx->Uf}) {
-    for (const auto& sg : T->sched) {
-      if (sg[2]) {
-        const int l = sg[0];
-        const int cnt = T->lvl_off[l + 1] - T->lvl_off[l];
-        launch_trsv_level(T->rows + T->lvl_off[l], cnt, T->ptr, T->col, T->val, T->dinv,
-                          ctx->lutmp, ctx->st);
-      } else {
-        launch_trsv_tail(T->rows, T->doff, sg[0], sg[1], T->ptr, T->col, T->val, T->dinv,
-                         ctx->lutmp, ctx->st);
-      }
-      ctx->launches++;
-    }
+  const LevelTri &L = ctx->Lf, &U = ctx->Uf;
+  launch_sptrsv(ctx->sf_ord, ctx->sf_nL, ctx->sf_total,
+                SfTri{L.ptr, L.col, L.val, L.dinv, L.flag}, SfTri{U.ptr, U.col, U.val, U.dinv, U.flag},
+                b, ctx->g_in, ctx->lu_rs, ctx->lutmp, ctx->lutmp2, ctx->sf_ctl, ctx->st);
+  launch_perm_gather(ctx->lutmp2, ctx->g_out, nullptr, n, x, ctx->st);
+  ctx->launches += 3;
+}
+
+// A triangular-solve wait that ran into its limit leaves an error word on the device;
+// entry points read it once their work is complete.
+static int check_solve_errors(peec_ctx* ctx) {
+  if (!ctx->sf_ctl) return PEEC_OK;
+  int e = 0;
+  PEEC_CUDA_TRY(cudaMemcpyAsync(&e, ctx->sf_ctl + 2, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  if (e) {
+    cudaMemsetAsync(ctx->sf_ctl + 2, 0, sizeof(int), ctx->st);
+    return bad(ctx, PEEC_ERR_TIMEOUT, "LU solve: a row dependency wait ran into its limit");
   }
-  launch_perm_gather(ctx->lutmp, ctx->g_out, nullptr, n, x, ctx->st);
-  ctx->launches++;
+  return PEEC_OK;
 }
 
 // enqueue one operator application y = M^-1 K x on the context stream
@@ -822,6 +833,7 @@ extern "C" int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precis
   cudaEventElapsedTime(&ctx->t_total, ctx->ev[0], ctx->ev[2]);
   cudaEventElapsedTime(&ctx->t_conv, ctx->ev[0], ctx->ev[1]);
   cudaEventElapsedTime(&ctx->t_sparse, ctx->ev[1], ctx->ev[2]);
+  CTX_TRY(check_solve_errors(ctx));
   return PEEC_OK;
 }
 
@@ -884,6 +896,7 @@ extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, doub
   }
   ctx->prof = false;
   for (int c = 0; c < 7; ++c) ms[c] = acc[c] / iters;
+  CTX_TRY(check_solve_errors(ctx));
   return PEEC_OK;
 }
 
@@ -1058,9 +1071,11 @@ static void apply_Q(Gm& g, const std::vector<cd>& Utop, int ldt, int k, const st
   ctx->launches += 2;
 }
 
+// x0_zero: the caller guarantees x_dev == 0, so the initial residual is b itself (A*0 is
+// exactly 0 in every precision) and its operator application is skipped
 static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, int maxit,
                      int restarted, int restart, int prec, int* flag_out, double* relres_out,
-                     int* iter_out, std::vector<double>& resvec_out) {
+                     int* iter_out, std::vector<double>& resvec_out, bool x0_zero = false) {
   const size_t N = ctx->N;
   int n = (int)N;
   int outer, inner;
@@ -1099,8 +1114,14 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
   const int maxmsteps = std::min(std::min(n / 50, 5), n - maxit);
   const int maxstagsteps = 3;
   int minupdated = 0;
-  g.residual(b, x, r);
-  double normr = g.norm(r);
+  double normr;
+  if (x0_zero) {
+    g.copy(r, b);
+    normr = n2b;
+  } else {
+    g.residual(b, x, r);
+    normr = g.norm(r);
+  }
   if (g.rc) return g.rc;
   if (normr <= tolb) {
     *flag_out = 0; *relres_out = normr / n2b; iter_out[0] = iter_out[1] = 0;
@@ -1366,6 +1387,7 @@ extern "C" int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, doubl
   if (resvec)
     for (int i = 0; i < (int)rv.size() && i < resvec_cap; ++i) resvec[i] = rv[i];
   if (rc == PEEC_ERR_CANCELLED) ctx->err = "cancelled by stop flag";
+  else CTX_TRY(check_solve_errors(ctx));
   return rc;
 }
 
@@ -1376,18 +1398,9 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
   if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
   cudaSetDevice(ctx->dev);
   const size_t N = ctx->N, bytes = sizeof(c64) * N;
-  c64 *db = nullptr, *dxv = nullptr, *dr = nullptr, *dd = nullptr;
-  PEEC_CUDA_TRY(cudaMalloc(&db, bytes));
-  PEEC_CUDA_TRY(cudaMalloc(&dxv, bytes));
-  PEEC_CUDA_TRY(cudaMalloc(&dr, bytes));
-  PEEC_CUDA_TRY(cudaMalloc(&dd, bytes));
-  auto cleanup = [&]() {
-    cudaFree(db); cudaFree(dxv); cudaFree(dr); cudaFree(dd);
-  };
-  {
-    int rc = ensure_krylov(ctx, std::max(inner_maxit, 1) + 1);
-    if (rc) { cleanup(); return rc; }
-  }
+  c64 *db = ctx->ir_b, *dxv = ctx->ir_x, *dr = ctx->ir_r, *dd = ctx->ir_d;
+  auto cleanup = [&]() {};
+  CTX_TRY(ensure_krylov(ctx, std::max(inner_maxit, 1) + 1));
   cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, ctx->st);
   cudaMemcpyAsync(dxv, x_inout, bytes, cudaMemcpyHostToDevice, ctx->st);
   Gm g{ctx, N, 0, ctx->st};
@@ -1412,7 +1425,8 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
       int ifl, it[2];
       double irel;
       std::vector<double> rv;
-      int rc = gmres_run(ctx, dr, dd, std::min(itol, 0.5), inner_maxit, 0, 0, 1, &ifl, &irel, it, rv);
+      int rc = gmres_run(ctx, dr, dd, std::min(itol, 0.5), inner_maxit, 0, 0, 1, &ifl, &irel, it, rv,
+                         true);
       if (rc) { cleanup(); return rc; }
       tot_inner += (int)rv.size() - 1;
       launch_add(dxv, dd, N, dxv, ctx->st);  // x += d
@@ -1420,8 +1434,8 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
     }
   }
   cudaMemcpyAsync(x_inout, dxv, bytes, cudaMemcpyDeviceToHost, ctx->st);
-  cudaStreamSynchronize(ctx->st);
-  cleanup();
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  CTX_TRY(check_solve_errors(ctx));
   *flag = fl;
   *relres = rel;
   if (outer_out) *outer_out = outer;

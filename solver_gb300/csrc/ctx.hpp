@@ -15,6 +15,16 @@ void set_error(const std::string& msg);
 
 #define PEEC_ERR_UNSUPPORTED_INTERNAL (-6)
 
+// one triangle of the synchronisation-free LU solve (CSR without the diagonal)
+struct SfTri {
+  const int32_t* ptr;
+  const int32_t* col;
+  const c64* val;
+  const c64* dinv;
+  int* flag;  // per row: the epoch of the solve that last finished the row
+};
+constexpr int SF_TPB = 128;
+
 #define CTX_CHECK(expr)      \
   do {                       \
     int _r = (expr);         \

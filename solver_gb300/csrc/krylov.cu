@@ -14,6 +14,7 @@ namespace peec {
 
 constexpr int KB = 8;        // columns per multi-dot tile
 constexpr int RED_TPB = 256;
+constexpr int MD_BLOCKS_MAX = 152 * 2;
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -58,19 +59,27 @@ __global__ void __launch_bounds__(RED_TPB) k_multidot(const c64* __restrict__ U,
     for (int w = 0; w < RED_TPB / 32; ++w) s += red[w][threadIdx.x];
     const int c = threadIdx.x >> 1;
     if (c < nc) {
-      double* p = reinterpret_cast<double*>(partial + (size_t)blockIdx.x * k + c0 + c);
+      double* p = reinterpret_cast<double*>(partial + (size_t)(c0 + c) * gridDim.x + blockIdx.x);
       p[threadIdx.x & 1] = s;
     }
   }
 }
 
-// out[c] = sum_b partial[b][c]  (fixed order)
+// out[c] = sum_b partial[c][b]: one warp per column, lane-strided then a shuffle tree
+// (fixed order for a fixed block count)
 __global__ void k_reduce_cols(const c64* __restrict__ partial, int nblk, int k, c64* out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= k) return;
-  c64 s = mk<double>(0, 0);
-  for (int b = 0; b < nblk; ++b) s = s + partial[(size_t)b * k + c];
-  out[c] = s;
+  const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (c >= k) return;  // whole warps leave together
+  double sr = 0.0, si = 0.0;
+  for (int b = lane; b < nblk; b += 32) {
+    const c64 p = partial[(size_t)c * nblk + b];
+    sr += p.x;
+    si += p.y;
+  }
+  sr = warp_sum(sr);
+  si = warp_sum(si);
+  if (lane == 0) out[c] = mk<double>(sr, si);
 }
 
 // v[i] = base[i] (or e_unit) - sum_c U[i,c]*coef[c];  optional tail |v|^2 partials for i >= tail0
@@ -222,13 +231,21 @@ static inline unsigned g_stream(size_t n) {
 
 int red_blocks(size_t N) { return (int)g_stream(N); }
 
+// multi-dot CTAs per column tile: at least 4 rows per thread, at most 2 CTAs per SM
+static inline unsigned md_blocks(size_t N) {
+  size_t g = (N + 4 * RED_TPB - 1) / (4 * RED_TPB);
+  if (g > MD_BLOCKS_MAX) g = MD_BLOCKS_MAX;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
 void launch_multidot(const c64* U, size_t ldu, const c64* v, size_t N, int k, c64* partial,
                      c64* out, cudaStream_t st) {
   if (k <= 0) return;
-  const unsigned nb = g_stream(N);
+  const unsigned nb = md_blocks(N);
   dim3 g(nb, (k + KB - 1) / KB);
   k_multidot<<<g, RED_TPB, 0, st>>>(U, ldu, v, N, k, partial);
-  k_reduce_cols<<<(k + 127) / 128, 128, 0, st>>>(partial, nb, k, out);
+  k_reduce_cols<<<(k + 7) / 8, 256, 0, st>>>(partial, nb, k, out);
 }
 
 void launch_multiaxpy(const c64* U, size_t ldu, const c64* base, int unit, const c64* coef,
@@ -289,7 +306,8 @@ void launch_xupdate(const c64* x, const c64* U, size_t ldu, const c64* coef, con
 // the process exits.
 // ------------------------------------------------------------------------------------
 
-constexpr int NOALLOC_BLOCKS = 152 * 8;  // = the grid cap of the multi-dot launcher
+constexpr int NOALLOC_BLOCKS = 152 * 8;  // >= the grid cap of the multi-dot launcher
+static_assert(NOALLOC_BLOCKS >= MD_BLOCKS_MAX, "scratch smaller than the multi-dot grid");
 static __device__ __align__(256) c64 g_noalloc_partials[(size_t)NOALLOC_BLOCKS * PEEC_NOALLOC_MAX_K];
 
 static std::mutex g_noalloc_mu;
@@ -329,7 +347,7 @@ extern "C" int peec_multidot_noalloc(const void* U, int64_t ldu, const void* v, 
     scratch = g_noalloc_addr[dev];
   }
   cudaStream_t st = (cudaStream_t)stream;
-  // every partial[b][c] the reduction reads (b < grid, c < k) is written by this call's
+  // every partial[c][b] the reduction reads (c < k, b < grid) is written by this call's
   // multi-dot first, so the array needs no clearing between calls
   launch_multidot((const c64*)U, (size_t)ldu, (const c64*)v, (size_t)N, k, (c64*)scratch,
                   (c64*)out, st);

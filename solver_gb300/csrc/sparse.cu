@@ -98,8 +98,14 @@ __global__ void k_final_rows(const c64* __restrict__ Y1, const c64* __restrict__
 }
 
 // ---------------------------------------------------------------------------------------
-// sparse LU solve x = Pc * (U \ (L \ (Pr * (Rs .* b)))) with level-scheduled
-// triangular sweeps; one launch per level, rows of a level independent.
+// sparse LU solve x = Pc * (U \ (L \ (Pr * (Rs .* b)))), both triangles in one launch,
+// synchronisation-free: every row carries a ready flag (the solve's epoch once its value
+// is final); a warp claims 32 rows of one level at a time from a global counter, in
+// level order (all L levels, then all U levels), waits until the rows it depends on are
+// flagged, and publishes its results with release stores. A row only ever waits on rows
+// claimed before it, by warps that are already running, so the solve always progresses;
+// every wait is bounded nonetheless (after the limit the kernel records an error in
+// ctl[2] and stops waiting, and all later waits return at once).
 // ---------------------------------------------------------------------------------------
 
 __global__ void k_perm_gather(const c64* __restrict__ b, const int32_t* __restrict__ perm,
@@ -116,36 +122,83 @@ __global__ void k_perm_scatter(const c64* __restrict__ z, const int32_t* __restr
     out[perm[i]] = z[i];
 }
 
-// rows of one level: x[r] = (x[r] - sum_{j != r} T[r,j] x[j]) / T[r,r]
-__global__ void k_trsv_level(const int32_t* __restrict__ rows, int nrows,
-                             const int32_t* __restrict__ ptr, const int32_t* __restrict__ col,
-                             const c64* __restrict__ val, const c64* __restrict__ dinv, c64* x) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nrows; t += gridDim.x * blockDim.x) {
-    const int r = rows[t];
-    c64 acc = x[r];
-    for (int p = ptr[r]; p < ptr[r + 1]; ++p) acc = acc - val[p] * x[col[p]];
-    x[r] = acc * dinv[r];
+// L2-coherent loads and stores of values other SMs publish during the same launch
+__device__ __forceinline__ c64 ld_cg(const c64* p) {
+  const double2 v = __ldcg(reinterpret_cast<const double2*>(p));
+  return mk<double>(v.x, v.y);
+}
+__device__ __forceinline__ void st_cg(c64* p, c64 v) {
+  __stcg(reinterpret_cast<double2*>(p), make_double2(v.x, v.y));
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// ctl[0] epoch, ctl[1] claim counter, ctl[2] error flag
+__global__ void k_sptrsv_begin(int* ctl) {
+  ctl[0] += 1;
+  ctl[1] = 0;
+}
+
+__device__ __forceinline__ void sf_wait(const int* f, int epoch, int* err, int limit) {
+  int it = 0;
+  while (ld_acquire(f) != epoch) {
+    ++it;
+    if (it >= limit) {
+      atomicExch(err, 1);
+      return;
+    }
+    if ((it & 63) == 0) {
+      if (*(volatile int*)err) return;
+      __nanosleep(64);
+    }
   }
 }
 
-// a run of consecutive small levels [l0, l1) in one CTA: levels in order, rows of a
-// level spread over the block, __syncthreads() between levels makes each level's
-// results visible to the next (no inter-block dependencies, no waiting)
-__global__ void __launch_bounds__(1024) k_trsv_tail(const int32_t* __restrict__ rows,
-                                                    const int32_t* __restrict__ lvl_off, int l0,
-                                                    int l1, const int32_t* __restrict__ ptr,
-                                                    const int32_t* __restrict__ col,
-                                                    const c64* __restrict__ val,
-                                                    const c64* __restrict__ dinv, c64* x) {
-  for (int l = l0; l < l1; ++l) {
-    const int a = lvl_off[l], b = lvl_off[l + 1];
-    for (int t = a + threadIdx.x; t < b; t += blockDim.x) {
-      const int r = rows[t];
-      c64 acc = x[r];
-      for (int p = ptr[r]; p < ptr[r + 1]; ++p) acc = acc - val[p] * x[col[p]];
-      x[r] = acc * dinv[r];
+__global__ void __launch_bounds__(SF_TPB) k_sptrsv(const int32_t* __restrict__ ord, int nL,
+                                                   int total, SfTri L, SfTri U,
+                                                   const c64* __restrict__ b,
+                                                   const int32_t* __restrict__ g_in,
+                                                   const double* __restrict__ rs, c64* y,
+                                                   c64* z, int* ctl, int limit) {
+  const int lane = threadIdx.x & 31;
+  const int epoch = ctl[0];
+  int* err = ctl + 2;
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(ctl + 1, 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= total) break;
+    const int r = ord[base + lane];
+    if (r >= 0) {
+      // L rows: y = L \ (Pr b); U rows: z = U \ y. Separate outputs: a U row may finish
+      // while an L row that reads the same index is still pending.
+      const bool up = base >= nL;
+      const SfTri& T = up ? U : L;
+      c64* out = up ? z : y;
+      c64 acc;
+      if (!up) {
+        const int j = g_in[r];
+        acc = rs ? cscale(b[j], rs[j]) : b[j];
+      } else {
+        sf_wait(L.flag + r, epoch, err, limit);
+        acc = ld_cg(y + r);
+      }
+      for (int p = T.ptr[r]; p < T.ptr[r + 1]; ++p) {
+        const int c = T.col[p];
+        sf_wait(T.flag + c, epoch, err, limit);
+        const c64 xc = ld_cg(out + c);
+        acc = acc - T.val[p] * xc;
+      }
+      st_cg(out + r, acc * T.dinv[r]);
+      st_release(T.flag + r, epoch);
     }
-    __syncthreads();
   }
 }
 
@@ -185,17 +238,18 @@ void launch_perm_gather(const c64* b, const int32_t* perm, const double* rs, int
 void launch_perm_scatter(const c64* z, const int32_t* perm, int n, c64* out, cudaStream_t st) {
   k_perm_scatter<<<grid_for(n), 256, 0, st>>>(z, perm, n, out);
 }
-void launch_trsv_level(const int32_t* rows, int nrows, const int32_t* ptr, const int32_t* col,
-                       const c64* val, const c64* dinv, c64* x, cudaStream_t st) {
-  k_trsv_level<<<grid_for(nrows), 256, 0, st>>>(rows, nrows, ptr, col, val, dinv, x);
+void launch_sptrsv(const int32_t* ord, int nL, int total, const SfTri& L, const SfTri& U,
+                   const c64* b, const int32_t* g_in, const double* rs, c64* y, c64* z,
+                   int* ctl, cudaStream_t st) {
+  k_sptrsv_begin<<<1, 1, 0, st>>>(ctl);
+  // enough warps to cover the widest levels; later blocks simply claim later rows
+  const int warps = (total + 31) / 32;
+  int blocks = (warps + SF_TPB / 32 - 1) / (SF_TPB / 32);
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks < 1) blocks = 1;
+  k_sptrsv<<<blocks, SF_TPB, 0, st>>>(ord, nL, total, L, U, b, g_in, rs, y, z, ctl,
+                                        1 << 20);
 }
 
 }  // namespace peec
 
-namespace peec {
-void launch_trsv_tail(const int32_t* rows, const int32_t* lvl_off, int l0, int l1,
-                      const int32_t* ptr, const int32_t* col, const c64* val, const c64* dinv,
-                      c64* x, cudaStream_t st) {
-  k_trsv_tail<<<1, 1024, 0, st>>>(rows, lvl_off, l0, l1, ptr, col, val, dinv, x);
-}
-}  // namespace peec
