@@ -150,7 +150,8 @@ def s2y_fft(S, Zo):
 def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, diagonals, ports,
                          ports_scatter_value, lumped_elements, expansions, GMRES_settings,
                          Zs_info, QS_Rcc_FW=1, id=None, chan=None, commentsEnabled=False, *,
-                         mode="fp64", mixed_inner_tol=1e-5, stop_flag=None, on_solve=None):
+                         mode="fp64", mixed_inner_tol=1e-5, mixed_warm_start=True,
+                         stop_flag=None, on_solve=None):
     """Frequency x port sweep with warm starts (FFT_solver_QS_S_type.jl:1-234).
 
     mode "fp64": the reference algorithm (FP64 convolutions, Householder GMRES).
@@ -175,11 +176,27 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
     Vrest = np.zeros((m + n + ns, npt), dtype=np.complex128)
     tol = GMRES_settings["tol"]
     info = []
+    pf = fq.StatePrefetcher(
+        lambda k: fq.FrequencyState(w[k], escalings, incidence_selection, diagonals, Zs_info,
+                                    lumped_elements, ports, ports_scatter_value),
+        range(w.size), keep=False)
+    try:
+        res = _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode,
+                     mixed_inner_tol, mixed_warm_start, stop_flag, on_solve, info, m, ns,
+                     ports_scatter_value)
+    finally:
+        pf.close()
+    if res is not None:
+        res["f"] = freq / escalings["freq"]
+    return res
+
+
+def _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode, mixed_inner_tol,
+           mixed_warm_start, stop_flag, on_solve, info, m, ns, ports_scatter_value):
     for k in range(w.size):
         if stop_flag is not None and stop_flag.value:
             return None
-        fs = fq.FrequencyState(w[k], escalings, incidence_selection, diagonals, Zs_info,
-                               lumped_elements, ports, ports_scatter_value)
+        fs = pf.get(k)
         op.set_frequency(w[k], fs.DZ, fs.Yle, fs.lu, key=("sweep", k, float(w[k])))
         tk = float(tol[k]) if np.ndim(tol) else float(tol)
         for c1 in range(npt):
@@ -189,7 +206,8 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
                 V, flag, relres, it, resvec = op.gmres(tn, Vrest[:, c1], tk, inner)
                 rec = {"flag": flag, "relres": relres, "iter": it, "niter": len(resvec) - 1}
             elif mode == "mixed":
-                V, flag, relres, outer, ninner = op.solve_mixed(tn, Vrest[:, c1], tk,
+                x0 = Vrest[:, c1] if mixed_warm_start else np.zeros_like(Vrest[:, c1])
+                V, flag, relres, outer, ninner = op.solve_mixed(tn, x0, tk,
                                                                 inner_tol=mixed_inner_tol,
                                                                 inner_maxit=inner)
                 rec = {"flag": flag, "relres": relres, "outer": outer, "niter": ninner}
@@ -211,4 +229,4 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
                     S[c1, c2, k] = val / ports_scatter_value
                     S[c2, c1, k] = S[c1, c2, k]
     return {"S": S, "Z": s2z_fft(S, ports_scatter_value), "Y": s2y_fft(S, ports_scatter_value),
-            "f": freq / escalings["freq"], "info": info, "Vrest": Vrest}
+            "info": info, "Vrest": Vrest}

@@ -1411,9 +1411,17 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
     cudaMemsetAsync(dxv, 0, bytes, ctx->st);
     fl = 0;
   } else {
+    // a zero initial guess makes the first residual b itself (A*0 is exactly 0)
+    const bool x_zero = g.norm(dxv) == 0.0;
     for (outer = 0; outer <= max_outer; ++outer) {
-      g.residual(db, dxv, dr);  // FP64 operator
-      const double nr = g.norm(dr);
+      double nr;
+      if (outer == 0 && x_zero) {
+        g.copy(dr, db);
+        nr = n2b;
+      } else {
+        g.residual(db, dxv, dr);  // FP64 operator
+        nr = g.norm(dr);
+      }
       if (g.rc) { cleanup(); return g.rc; }
       rel = nr / n2b;
       if (rel <= tol) { fl = 0; break; }

@@ -15,15 +15,18 @@
 // T_f[z][y][kx] (kx fastest, Lx x Ly x nz_f), in place:
 //   k_xfwd   gather the family's compact vector through its lattice map, zero pad,
 //            forward FFT along x (16 pencils per CTA)
-//   k_ypass  forward / inverse FFT along y (32 or 16 consecutive kx per CTA)
+//   k_ypass  forward / inverse FFT along y (16 consecutive kx per CTA)
 //   k_zconv3 forward FFT along z of the three face families, 3x3 spectral product,
 //            inverse FFT along z (one ky, a kx tile per CTA)
 //   k_zconv1 same for one edge family with its real spectrum
 //   k_xinv   inverse FFT along x and plain store into the compact output through the
 //            lattice map (each compact index belongs to exactly one family)
-// Only the occupied lattice octant is transformed in each pass (pruning). All tiles
-// keep sequences contiguous in shared memory (element (pos, seq) at pos*rs + seq), so
-// loads, stores and butterflies are bank-conflict free and index math is shifts.
+// Only the occupied lattice octant is transformed in each pass (pruning). Inside a
+// pass the first radix group reads global memory straight into registers and the
+// last group writes straight back (fft_reg.cuh); in the z passes the last forward
+// group, the spectral product and the first inverse group run back to back in
+// registers. Shared-memory tiles keep sequences contiguous (element (pos, seq) at
+// pos*rs + seq), so the middle groups are bank-conflict free.
 // Spectra carry the 1/(Lx*Ly*Lz) normalisation and are stored (ky, kz, kx), kx fastest,
 // in the transforms' bit-reversed position order.
 #include <mutex>
@@ -32,6 +35,7 @@
 
 #include "ctx.hpp"
 #include "fft.cuh"
+#include "fft_reg.cuh"
 
 namespace peec {
 
@@ -44,122 +48,298 @@ __device__ void load_tw(cx<R>* dst, const cx<R>* __restrict__ master, int twmax,
   for (int e = threadIdx.x; e < n; e += blockDim.x) dst[e] = master[e * step];
 }
 
-// FFT of the 1<<LNS contiguous sequences of a tile: element (pos, seq) at buf[pos*rs + seq]
-template <typename R, bool INV, int LNS>
-__device__ void fft_cols(cx<R>* buf, int rs, int logL, const cx<R>* __restrict__ W) {
-  if (logL == 0) {
-    __syncthreads();
-    return;
-  }
-  int groups[16], ng = 0;
-  for (int s = 0; s < logL;) {
-    const int q = (logL - s) >= 3 ? 3 : (logL - s);
-    groups[ng++] = (s << 4) | q;
-    s += q;
-  }
-  for (int gi = 0; gi < ng; ++gi) {
-    const int g = INV ? groups[ng - 1 - gi] : groups[gi];
-    const int s = g >> 4, q = g & 15;
-    const int total = 1 << (logL - q + LNS);
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-      const int sq = t & ((1 << LNS) - 1);
-      const int c = t >> LNS;
-      cx<R>* seq = buf + sq;
-      if (q == 3) fft_group<R, 3, INV>(seq, rs, s, logL, W, c);
-      else if (q == 2) fft_group<R, 2, INV>(seq, rs, s, logL, W, c);
-      else fft_group<R, 1, INV>(seq, rs, s, logL, W, c);
-    }
-    __syncthreads();
-  }
-}
-
 // --------------------------------------------------------------------------- x passes
+// CTA: TY = 16 consecutive y rows of one z plane. Tile element (pos, yy) at
+// buf[pos*(TY+1) + yy]; the first/last group threads run along x so map reads and
+// output gathers are contiguous.
 
-template <typename R, int LTY>
+constexpr int LTY = 4;
+constexpr int TY = 1 << LTY;
+constexpr int XRS = TY + 1;
+
+template <typename R, int Q>
+__device__ __forceinline__ void xfwd_first(const c64* __restrict__ xin,
+                                           const int32_t* __restrict__ map, cx<R>* buf,
+                                           const AxPlan& p, int y0, int z, int nx, int ny,
+                                           const cx<R>* W) {
+  constexpr int N = 1 << Q;
+  const int lh = p.n - Q;
+  const int tasks = TY << lh;
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int k = t & ((1 << lh) - 1);
+    const int yy = t >> lh;
+    const int y = y0 + yy;
+    cx<R> v[N];
+    const int32_t* mrow = map + ((size_t)z * ny + y) * nx;
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+      const int x = k + (r << lh);
+      v[r] = mk<R>(0, 0);
+      if (y < ny && x < nx) {
+        const int idx = mrow[x];
+        if (idx >= 0) v[r] = ccast<R>(xin[idx]);
+      }
+    }
+    dft_dif<R, Q>(v);
+    if (p.ng > 1) group_twiddle<R, Q, false>(v, k, 0, W);
+#pragma unroll
+    for (int r = 0; r < N; ++r) buf[(k + (r << lh)) * XRS + yy] = v[r];
+  }
+}
+
+template <typename R, int Q, bool INV>
+__device__ __forceinline__ void x_last_inplace(cx<R>* buf, const AxPlan& p) {
+  // the group at the end of the stage order (forward) / its mirror (inverse):
+  // contiguous positions, no table twiddles
+  constexpr int N = 1 << Q;
+  const int tasks = TY << (p.n - Q);
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int yy = t & (TY - 1);
+    const int start = (t >> LTY) << Q;
+    cx<R> v[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) v[r] = buf[(start + r) * XRS + yy];
+    if (!INV) dft_dif<R, Q>(v);
+    else dft_dit<R, Q>(v);
+#pragma unroll
+    for (int r = 0; r < N; ++r) buf[(start + r) * XRS + yy] = v[r];
+  }
+}
+
+template <typename R>
 __global__ void __launch_bounds__(TPB) k_xfwd(const c64* __restrict__ xin,
-                                              const int32_t* __restrict__ map, cx<R>* T, int Lx,
-                                              int logLx, int Ly, int nx, int ny, int nz,
+                                              const int32_t* __restrict__ map, cx<R>* T,
+                                              AxPlan p, int Ly, int nx, int ny,
                                               const cx<R>* __restrict__ twm, int twmax) {
-  constexpr int TY = 1 << LTY;
   extern __shared__ unsigned char smem_raw[];
+  const int Lx = 1 << p.n;
   cx<R>* W = reinterpret_cast<cx<R>*>(smem_raw);
-  cx<R>* buf = W + (Lx > 1 ? Lx / 2 : 1);
-  const int rs = TY + 1;
+  cx<R>* buf = W + Lx;
   const int y0 = blockIdx.x * TY, z = blockIdx.y;
-  load_tw<R>(W, twm, twmax, Lx, Lx / 2);
-  for (int p = threadIdx.x; p < TY << logLx; p += blockDim.x) {
-    const int yy = p >> logLx, x = p & (Lx - 1);
-    const int y = y0 + yy;
-    cx<R> v = mk<R>(0, 0);
-    if (y < ny && x < nx) {
-      const int idx = map[((size_t)z * ny + y) * nx + x];
-      if (idx >= 0) v = ccast<R>(xin[idx]);
-    }
-    buf[x * rs + yy] = v;
-  }
+  load_twiddles<R>(W, twm, twmax, Lx);
   __syncthreads();
-  fft_cols<R, false, LTY>(buf, rs, logLx, W);
-  for (int p = threadIdx.x; p < TY << logLx; p += blockDim.x) {
-    const int yy = p >> logLx, kx = p & (Lx - 1);
+  qswitch<4>(p.q[0], [&](auto QC) {
+    xfwd_first<R, decltype(QC)::value>(xin, map, buf, p, y0, z, nx, ny, W);
+  });
+  __syncthreads();
+  if (p.ng > 1) {
+    middle_groups<R, false, LTY>(buf, XRS, p, W);
+    qswitch<4>(p.q[p.ng - 1],
+               [&](auto QC) { x_last_inplace<R, decltype(QC)::value, false>(buf, p); });
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < TY << p.n; q += blockDim.x) {
+    const int yy = q >> p.n, kx = q & (Lx - 1);
     const int y = y0 + yy;
-    if (y < ny) T[((size_t)z * Ly + y) * Lx + kx] = buf[kx * rs + yy];
+    if (y < ny) T[((size_t)z * Ly + y) * Lx + kx] = buf[kx * XRS + yy];
   }
 }
 
-template <typename R, int LTY>
-__global__ void __launch_bounds__(TPB) k_xinv(const cx<R>* __restrict__ T, c64* yout,
-                                              const int32_t* __restrict__ map, int Lx, int logLx,
-                                              int Ly, int nx, int ny, int nz,
-                                              const cx<R>* __restrict__ twm, int twmax) {
-  constexpr int TY = 1 << LTY;
-  extern __shared__ unsigned char smem_raw[];
-  cx<R>* W = reinterpret_cast<cx<R>*>(smem_raw);
-  cx<R>* buf = W + (Lx > 1 ? Lx / 2 : 1);
-  const int rs = TY + 1;
-  const int y0 = blockIdx.x * TY, z = blockIdx.y;
-  load_tw<R>(W, twm, twmax, Lx, Lx / 2);
-  for (int p = threadIdx.x; p < TY << logLx; p += blockDim.x) {
-    const int yy = p >> logLx, kx = p & (Lx - 1);
+template <typename R, int Q>
+__device__ __forceinline__ void xinv_last(const cx<R>* buf, c64* yout,
+                                          const int32_t* __restrict__ map, const AxPlan& p,
+                                          int y0, int z, int nx, int ny, const cx<R>* W) {
+  constexpr int N = 1 << Q;
+  const int lh = p.n - Q;
+  const int tasks = TY << lh;
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int k = t & ((1 << lh) - 1);
+    const int yy = t >> lh;
     const int y = y0 + yy;
-    buf[kx * rs + yy] = (y < ny) ? T[((size_t)z * Ly + y) * Lx + kx] : mk<R>(0, 0);
-  }
-  __syncthreads();
-  fft_cols<R, true, LTY>(buf, rs, logLx, W);
-  for (int p = threadIdx.x; p < TY << logLx; p += blockDim.x) {
-    const int yy = p >> logLx, x = p & (Lx - 1);
-    const int y = y0 + yy;
-    if (y >= ny || x >= nx) continue;
-    const int idx = map[((size_t)z * ny + y) * nx + x];
-    if (idx >= 0) {
-      const cx<R> v = buf[x * rs + yy];
-      yout[idx] = mk<double>((double)v.x, (double)v.y);
+    if (y >= ny || k >= nx) continue;
+    cx<R> v[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) v[r] = buf[(k + (r << lh)) * XRS + yy];
+    if (p.ng > 1) group_twiddle<R, Q, true>(v, k, 0, W);
+    dft_dit<R, Q>(v);
+    const int32_t* mrow = map + ((size_t)z * ny + y) * nx;
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+      const int x = k + (r << lh);
+      if (x < nx) {
+        const int idx = mrow[x];
+        if (idx >= 0) yout[idx] = mk<double>((double)v[r].x, (double)v[r].y);
+      }
     }
   }
 }
+
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_xinv(const cx<R>* __restrict__ T, c64* yout,
+                                              const int32_t* __restrict__ map, AxPlan p, int Ly,
+                                              int nx, int ny, const cx<R>* __restrict__ twm,
+                                              int twmax) {
+  extern __shared__ unsigned char smem_raw[];
+  const int Lx = 1 << p.n;
+  cx<R>* W = reinterpret_cast<cx<R>*>(smem_raw);
+  cx<R>* buf = W + Lx;
+  const int y0 = blockIdx.x * TY, z = blockIdx.y;
+  load_twiddles<R>(W, twm, twmax, Lx);
+  for (int q = threadIdx.x; q < TY << p.n; q += blockDim.x) {
+    const int yy = q >> p.n, kx = q & (Lx - 1);
+    const int y = y0 + yy;
+    buf[kx * XRS + yy] = (y < ny) ? T[((size_t)z * Ly + y) * Lx + kx] : mk<R>(0, 0);
+  }
+  __syncthreads();
+  if (p.ng > 1) {
+    qswitch<4>(p.q[p.ng - 1],
+               [&](auto QC) { x_last_inplace<R, decltype(QC)::value, true>(buf, p); });
+    __syncthreads();
+    middle_groups<R, true, LTY>(buf, XRS, p, W);
+  }
+  qswitch<4>(p.q[0], [&](auto QC) {
+    xinv_last<R, decltype(QC)::value>(buf, yout, map, p, y0, z, nx, ny, W);
+  });
+}
+
+// --------------------------------------------------------------------------- column passes
+// y and z passes work on columns of TX = 16 consecutive kx: element (pos, col) of the
+// tile at buf[pos*TX + col]; global row pos of the column tile at g + pos*gstride.
+
+constexpr int LTX = 4;
+constexpr int TX = 1 << LTX;
+
+// forward first group from global rows < n_in (zero beyond), into registers, then the
+// tile (or, for a single-group plan, back to global in full)
+template <typename R, int Q>
+__device__ __forceinline__ void col_first_fwd(const cx<R>* g, size_t gstride, int ncols,
+                                              int n_in, cx<R>* buf, const AxPlan& p,
+                                              const cx<R>* W, cx<R>* gout) {
+  constexpr int N = 1 << Q;
+  const int lh = p.n - Q;
+  const int tasks = TX << lh;
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int col = t & (TX - 1);
+    const int k = t >> LTX;
+    cx<R> v[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+      const int row = k + (r << lh);
+      v[r] = (col < ncols && row < n_in) ? g[row * gstride + col] : mk<R>(0, 0);
+    }
+    dft_dif<R, Q>(v);
+    if (p.ng > 1) {
+      group_twiddle<R, Q, false>(v, k, 0, W);
+#pragma unroll
+      for (int r = 0; r < N; ++r) buf[((k + (r << lh)) << LTX) + col] = v[r];
+    } else if (col < ncols) {
+#pragma unroll
+      for (int r = 0; r < N; ++r) gout[r * gstride + col] = v[r];
+    }
+  }
+}
+
+// forward last group: tile -> global, contiguous positions
+template <typename R, int Q>
+__device__ __forceinline__ void col_last_fwd(const cx<R>* buf, cx<R>* g, size_t gstride,
+                                             int ncols, const AxPlan& p) {
+  constexpr int N = 1 << Q;
+  const int tasks = TX << (p.n - Q);
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int col = t & (TX - 1);
+    const int start = (t >> LTX) << Q;
+    cx<R> v[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) v[r] = buf[((start + r) << LTX) + col];
+    dft_dif<R, Q>(v);
+    if (col < ncols) {
+#pragma unroll
+      for (int r = 0; r < N; ++r) g[(start + r) * gstride + col] = v[r];
+    }
+  }
+}
+
+// inverse first group (mirror of the forward last group): global -> tile, or for a
+// single-group plan global -> global rows < n_out
+template <typename R, int Q>
+__device__ __forceinline__ void col_first_inv(const cx<R>* g, size_t gstride, int ncols,
+                                              int n_out, cx<R>* buf, const AxPlan& p,
+                                              cx<R>* gout) {
+  constexpr int N = 1 << Q;
+  const int tasks = TX << (p.n - Q);
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int col = t & (TX - 1);
+    const int start = (t >> LTX) << Q;
+    cx<R> v[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r)
+      v[r] = col < ncols ? g[(start + r) * gstride + col] : mk<R>(0, 0);
+    dft_dit<R, Q>(v);
+    if (p.ng > 1) {
+#pragma unroll
+      for (int r = 0; r < N; ++r) buf[((start + r) << LTX) + col] = v[r];
+    } else if (col < ncols) {
+#pragma unroll
+      for (int r = 0; r < N; ++r)
+        if (start + r < n_out) gout[(start + r) * gstride + col] = v[r];
+    }
+  }
+}
+
+// inverse last group (mirror of the forward first group): tile -> global rows < n_out
+template <typename R, int Q>
+__device__ __forceinline__ void col_last_inv(const cx<R>* buf, cx<R>* g, size_t gstride,
+                                             int ncols, int n_out, const AxPlan& p,
+                                             const cx<R>* W) {
+  constexpr int N = 1 << Q;
+  const int lh = p.n - Q;
+  const int tasks = TX << lh;
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int col = t & (TX - 1);
+    const int k = t >> LTX;
+    if (k >= n_out) continue;
+    cx<R> v[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) v[r] = buf[((k + (r << lh)) << LTX) + col];
+    group_twiddle<R, Q, true>(v, k, 0, W);
+    dft_dit<R, Q>(v);
+    if (col < ncols) {
+#pragma unroll
+      for (int r = 0; r < N; ++r) {
+        const int row = k + (r << lh);
+        if (row < n_out) g[row * gstride + col] = v[r];
+      }
+    }
+  }
+}
+
+// register-group caps per kernel (see make_plan): x/y passes 16 points at both ends;
+// z passes hold three families (P) or one (Lp) at the fused spectral step
+template <typename R>
+struct QCap {
+  static constexpr int XY = 4;
+  static constexpr int Z3 = sizeof(R) == 8 ? 2 : 3;
+  static constexpr int Z1 = sizeof(R) == 8 ? 3 : 4;
+};
 
 // --------------------------------------------------------------------------- y pass
-
 // planes z < nz; rows y < n_in are read (zero padded to Ly), rows y < n_out written
-template <typename R, bool INV, int LTX>
-__global__ void __launch_bounds__(TPB) k_ypass(cx<R>* T, int Lx, int Ly, int logLy, int n_in,
-                                               int n_out, const cx<R>* __restrict__ twm,
-                                               int twmax) {
-  constexpr int TX = 1 << LTX;
+template <typename R, bool INV>
+__global__ void __launch_bounds__(TPB) k_ypass(cx<R>* T, int Lx, AxPlan p, int n_in, int n_out,
+                                               const cx<R>* __restrict__ twm, int twmax) {
   extern __shared__ unsigned char smem_raw[];
+  const int Ly = 1 << p.n;
   cx<R>* W = reinterpret_cast<cx<R>*>(smem_raw);
-  cx<R>* buf = W + (Ly > 1 ? Ly / 2 : 1);
+  cx<R>* buf = W + Ly;
   const int kx0 = blockIdx.x * TX, z = blockIdx.y;
-  load_tw<R>(W, twm, twmax, Ly, Ly / 2);
+  const int ncols = min(TX, Lx - kx0);
   cx<R>* col = T + (size_t)z * Ly * Lx + kx0;
-  for (int p = threadIdx.x; p < Ly << LTX; p += blockDim.x) {
-    const int y = p >> LTX, tx = p & (TX - 1);
-    buf[p] = (y < n_in) ? col[(size_t)y * Lx + tx] : mk<R>(0, 0);
-  }
+  load_twiddles<R>(W, twm, twmax, Ly);
   __syncthreads();
-  fft_cols<R, INV, LTX>(buf, TX, logLy, W);
-  for (int p = threadIdx.x; p < n_out << LTX; p += blockDim.x) {
-    const int y = p >> LTX, tx = p & (TX - 1);
-    col[(size_t)y * Lx + tx] = buf[p];
+  if (!INV) {
+    qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(col, (size_t)Lx, ncols, n_in, buf, p, W, col); });
+    if (p.ng > 1) {
+      __syncthreads();
+      middle_groups<R, false, LTX>(buf, TX, p, W);
+      qswitch<QCap<R>::XY>(p.q[p.ng - 1], [&](auto QC) { col_last_fwd<R, decltype(QC)::value>(buf, col, (size_t)Lx, ncols, p); });
+    }
+  } else {
+    qswitch<QCap<R>::XY>(p.q[p.ng - 1], [&](auto QC) { col_first_inv<R, decltype(QC)::value>(col, (size_t)Lx, ncols, n_out, buf, p, col); });
+    if (p.ng > 1) {
+      __syncthreads();
+      middle_groups<R, true, LTX>(buf, TX, p, W);
+      qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf, col, (size_t)Lx, ncols, n_out, p, W); });
+    }
   }
 }
 
@@ -174,88 +354,212 @@ struct PSpec {
   const void* s12;  // complex
 };
 
-template <typename R, int LTX>
-__global__ void __launch_bounds__(TPB) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>* T2, int nz0, int nz1,
-                                                int nz2, PSpec S, int Lx, int Ly, int Lz, int logLz,
-                                                const cx<R>* __restrict__ twm, int twmax) {
-  constexpr int TX = 1 << LTX;
-  extern __shared__ unsigned char smem_raw[];
-  cx<R>* W = reinterpret_cast<cx<R>*>(smem_raw);
-  cx<R>* b0 = W + (Lz > 1 ? Lz / 2 : 1);
-  cx<R>* b1 = b0 + (Lz << LTX);
-  cx<R>* b2 = b1 + (Lz << LTX);
-  const int kx0 = blockIdx.x * TX, ky = blockIdx.y;
-  load_tw<R>(W, twm, twmax, Lz, Lz / 2);
-  const size_t pl = (size_t)Ly * Lx;
-  const size_t off = (size_t)ky * Lx + kx0;
-  for (int p = threadIdx.x; p < Lz << LTX; p += blockDim.x) {
-    const int z = p >> LTX, tx = p & (TX - 1);
-    const size_t g = z * pl + off + tx;
-    b0[p] = z < nz0 ? T0[g] : mk<R>(0, 0);
-    b1[p] = z < nz1 ? T1[g] : mk<R>(0, 0);
-    b2[p] = z < nz2 ? T2[g] : mk<R>(0, 0);
-  }
-  __syncthreads();
-  fft_cols<R, false, LTX>(b0, TX, logLz, W);
-  fft_cols<R, false, LTX>(b1, TX, logLz, W);
-  fft_cols<R, false, LTX>(b2, TX, logLz, W);
+// Y_f = sum_g S_fg X_g with S_gf = conj(S_fg), at spectrum index si
+template <typename R>
+__device__ __forceinline__ void pspec_apply(const PSpec& S, size_t si, cx<R>& a0, cx<R>& a1,
+                                            cx<R>& a2) {
   const R* s00 = reinterpret_cast<const R*>(S.s00);
   const R* s11 = reinterpret_cast<const R*>(S.s11);
   const R* s22 = reinterpret_cast<const R*>(S.s22);
   const cx<R>* s01 = reinterpret_cast<const cx<R>*>(S.s01);
   const cx<R>* s02 = reinterpret_cast<const cx<R>*>(S.s02);
   const cx<R>* s12 = reinterpret_cast<const cx<R>*>(S.s12);
-  for (int p = threadIdx.x; p < Lz << LTX; p += blockDim.x) {
-    const int kz = p >> LTX, tx = p & (TX - 1);
-    const size_t si = ((size_t)ky * Lz + kz) * Lx + kx0 + tx;
-    const cx<R> a0 = b0[p], a1 = b1[p], a2 = b2[p];
-    const cx<R> c01 = s01[si], c02 = s02[si], c12 = s12[si];
-    // Y_f = sum_g S_fg X_g with S_gf = conj(S_fg)
-    b0[p] = cscale(a0, s00[si]) + c01 * a1 + c02 * a2;
-    b1[p] = cmulc(a0, c01) + cscale(a1, s11[si]) + c12 * a2;
-    b2[p] = cmulc(a0, c02) + cmulc(a1, c12) + cscale(a2, s22[si]);
-  }
-  __syncthreads();
-  fft_cols<R, true, LTX>(b0, TX, logLz, W);
-  fft_cols<R, true, LTX>(b1, TX, logLz, W);
-  fft_cols<R, true, LTX>(b2, TX, logLz, W);
-  for (int p = threadIdx.x; p < Lz << LTX; p += blockDim.x) {
-    const int z = p >> LTX, tx = p & (TX - 1);
-    const size_t g = z * pl + off + tx;
-    if (z < nz0) T0[g] = b0[p];
-    if (z < nz1) T1[g] = b1[p];
-    if (z < nz2) T2[g] = b2[p];
+  const cx<R> c01 = s01[si], c02 = s02[si], c12 = s12[si];
+  const cx<R> b0 = cscale(a0, s00[si]) + c01 * a1 + c02 * a2;
+  const cx<R> b1 = cmulc(a0, c01) + cscale(a1, s11[si]) + c12 * a2;
+  const cx<R> b2 = cmulc(a0, c02) + cmulc(a1, c12) + cscale(a2, s22[si]);
+  a0 = b0;
+  a1 = b1;
+  a2 = b2;
+}
+
+// single-group z transform of all three face families in registers
+template <typename R, int Q>
+__device__ __forceinline__ void z3_single(cx<R>* T0, cx<R>* T1, cx<R>* T2, int nz0, int nz1,
+                                          int nz2, size_t pl, int ncols, const PSpec& S,
+                                          size_t sbase, size_t sstride) {
+  constexpr int N = 1 << Q;
+  for (int col = threadIdx.x; col < TX; col += blockDim.x) {
+    if (col >= ncols) continue;
+    cx<R> v[3][N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+      v[0][r] = r < nz0 ? T0[r * pl + col] : mk<R>(0, 0);
+      v[1][r] = r < nz1 ? T1[r * pl + col] : mk<R>(0, 0);
+      v[2][r] = r < nz2 ? T2[r * pl + col] : mk<R>(0, 0);
+    }
+#pragma unroll
+    for (int f = 0; f < 3; ++f) dft_dif<R, Q>(v[f]);
+#pragma unroll
+    for (int r = 0; r < N; ++r)
+      pspec_apply<R>(S, sbase + r * sstride + col, v[0][r], v[1][r], v[2][r]);
+#pragma unroll
+    for (int f = 0; f < 3; ++f) dft_dit<R, Q>(v[f]);
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+      if (r < nz0) T0[r * pl + col] = v[0][r];
+      if (r < nz1) T1[r * pl + col] = v[1][r];
+      if (r < nz2) T2[r * pl + col] = v[2][r];
+    }
   }
 }
 
-template <typename R, int LTX>
-__global__ void __launch_bounds__(TPB) k_zconv1(cx<R>* T0, int nz0, const R* __restrict__ s00,
-                                                int Lx, int Ly, int Lz, int logLz,
+// fused middle step: last forward group of the three families, spectral product,
+// first inverse group, tile -> tile (the three tiles are consecutive: tile f at
+// buf + f*tsz)
+template <typename R, int Q>
+__device__ __forceinline__ void z3_fused(cx<R>* buf, size_t tsz, const AxPlan& p, int ncols,
+                                         const PSpec& S, size_t sbase, size_t sstride) {
+  constexpr int N = 1 << Q;
+  const int tasks = TX << (p.n - Q);
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int col = t & (TX - 1);
+    const int start = (t >> LTX) << Q;
+    cx<R> v[3][N];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+#pragma unroll
+      for (int r = 0; r < N; ++r) v[f][r] = buf[f * tsz + ((start + r) << LTX) + col];
+      dft_dif<R, Q>(v[f]);
+    }
+    if (col < ncols) {
+#pragma unroll
+      for (int r = 0; r < N; ++r)
+        pspec_apply<R>(S, sbase + (start + r) * sstride + col, v[0][r], v[1][r], v[2][r]);
+    }
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      dft_dit<R, Q>(v[f]);
+#pragma unroll
+      for (int r = 0; r < N; ++r) buf[f * tsz + ((start + r) << LTX) + col] = v[f][r];
+    }
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(TPB, 2) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>* T2, int nz0, int nz1,
+                                                int nz2, PSpec S, int Lx, int Ly, AxPlan p,
                                                 const cx<R>* __restrict__ twm, int twmax) {
-  constexpr int TX = 1 << LTX;
   extern __shared__ unsigned char smem_raw[];
+  const int Lz = 1 << p.n;
+  const size_t tsz = (size_t)Lz << LTX;
   cx<R>* W = reinterpret_cast<cx<R>*>(smem_raw);
-  cx<R>* b0 = W + (Lz > 1 ? Lz / 2 : 1);
+  cx<R>* buf = W + Lz;  // three tiles, family f at buf + f*tsz
   const int kx0 = blockIdx.x * TX, ky = blockIdx.y;
-  load_tw<R>(W, twm, twmax, Lz, Lz / 2);
+  const int ncols = min(TX, Lx - kx0);
   const size_t pl = (size_t)Ly * Lx;
   const size_t off = (size_t)ky * Lx + kx0;
-  for (int p = threadIdx.x; p < Lz << LTX; p += blockDim.x) {
-    const int z = p >> LTX, tx = p & (TX - 1);
-    b0[p] = z < nz0 ? T0[z * pl + off + tx] : mk<R>(0, 0);
-  }
+  T0 += off;
+  T1 += off;
+  T2 += off;
+  // spectrum index of (ky, kz, kx0 + col) = sbase + kz*Lx + col
+  const size_t sbase = (size_t)ky * Lz * Lx + kx0;
+  load_twiddles<R>(W, twm, twmax, Lz);
   __syncthreads();
-  fft_cols<R, false, LTX>(b0, TX, logLz, W);
-  for (int p = threadIdx.x; p < Lz << LTX; p += blockDim.x) {
-    const int kz = p >> LTX, tx = p & (TX - 1);
-    b0[p] = cscale(b0[p], s00[((size_t)ky * Lz + kz) * Lx + kx0 + tx]);
+  if (p.ng == 1) {
+    qswitch<QCap<R>::Z3>(p.q[0], [&](auto QC) { z3_single<R, decltype(QC)::value>(T0, T1, T2, nz0, nz1, nz2, pl, ncols, S, sbase, (size_t)Lx); });
+    return;
   }
+  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(T0, pl, ncols, nz0, buf, p, W, T0); });
+  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(T1, pl, ncols, nz1, buf + tsz, p, W, T1); });
+  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(T2, pl, ncols, nz2, buf + 2 * tsz, p, W, T2); });
   __syncthreads();
-  fft_cols<R, true, LTX>(b0, TX, logLz, W);
-  for (int p = threadIdx.x; p < nz0 << LTX; p += blockDim.x) {
-    const int z = p >> LTX, tx = p & (TX - 1);
-    T0[z * pl + off + tx] = b0[p];
+  {
+    int s = p.q[0];
+    for (int g = 1; g + 1 < p.ng; ++g) {
+      smem_group_q<R, false, LTX>(buf, TX, p.q[g], p.n, s, W);
+      smem_group_q<R, false, LTX>(buf + tsz, TX, p.q[g], p.n, s, W);
+      smem_group_q<R, false, LTX>(buf + 2 * tsz, TX, p.q[g], p.n, s, W);
+      s += p.q[g];
+      __syncthreads();
+    }
   }
+  qswitch<QCap<R>::Z3>(p.q[p.ng - 1], [&](auto QC) { z3_fused<R, decltype(QC)::value>(buf, tsz, p, ncols, S, sbase, (size_t)Lx); });
+  __syncthreads();
+  {
+    int s = p.n - p.q[p.ng - 1];
+    for (int g = p.ng - 2; g >= 1; --g) {
+      s -= p.q[g];
+      smem_group_q<R, true, LTX>(buf, TX, p.q[g], p.n, s, W);
+      smem_group_q<R, true, LTX>(buf + tsz, TX, p.q[g], p.n, s, W);
+      smem_group_q<R, true, LTX>(buf + 2 * tsz, TX, p.q[g], p.n, s, W);
+      __syncthreads();
+    }
+  }
+  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf, T0, pl, ncols, nz0, p, W); });
+  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf + tsz, T1, pl, ncols, nz1, p, W); });
+  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf + 2 * tsz, T2, pl, ncols, nz2, p, W); });
+}
+
+// one edge family with its real spectrum
+template <typename R, int Q>
+__device__ __forceinline__ void z1_single(cx<R>* Tg, int nz, size_t pl, int ncols,
+                                          const R* __restrict__ s, size_t sbase,
+                                          size_t sstride) {
+  constexpr int N = 1 << Q;
+  for (int col = threadIdx.x; col < TX; col += blockDim.x) {
+    if (col >= ncols) continue;
+    cx<R> v[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) v[r] = r < nz ? Tg[r * pl + col] : mk<R>(0, 0);
+    dft_dif<R, Q>(v);
+#pragma unroll
+    for (int r = 0; r < N; ++r) v[r] = cscale(v[r], s[sbase + r * sstride + col]);
+    dft_dit<R, Q>(v);
+#pragma unroll
+    for (int r = 0; r < N; ++r)
+      if (r < nz) Tg[r * pl + col] = v[r];
+  }
+}
+
+template <typename R, int Q>
+__device__ __forceinline__ void z1_fused(cx<R>* buf, const AxPlan& p, int ncols,
+                                         const R* __restrict__ s, size_t sbase, size_t sstride) {
+  constexpr int N = 1 << Q;
+  const int tasks = TX << (p.n - Q);
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int col = t & (TX - 1);
+    const int start = (t >> LTX) << Q;
+    cx<R> v[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) v[r] = buf[((start + r) << LTX) + col];
+    dft_dif<R, Q>(v);
+    if (col < ncols) {
+#pragma unroll
+      for (int r = 0; r < N; ++r) v[r] = cscale(v[r], s[sbase + (start + r) * sstride + col]);
+    }
+    dft_dit<R, Q>(v);
+#pragma unroll
+    for (int r = 0; r < N; ++r) buf[((start + r) << LTX) + col] = v[r];
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_zconv1(cx<R>* T0, int nz0, const R* __restrict__ s00,
+                                                int Lx, int Ly, AxPlan p,
+                                                const cx<R>* __restrict__ twm, int twmax) {
+  extern __shared__ unsigned char smem_raw[];
+  const int Lz = 1 << p.n;
+  cx<R>* W = reinterpret_cast<cx<R>*>(smem_raw);
+  cx<R>* buf = W + Lz;
+  const int kx0 = blockIdx.x * TX, ky = blockIdx.y;
+  const int ncols = min(TX, Lx - kx0);
+  const size_t pl = (size_t)Ly * Lx;
+  cx<R>* Tg = T0 + (size_t)ky * Lx + kx0;
+  const size_t sbase = (size_t)ky * Lz * Lx + kx0;
+  load_twiddles<R>(W, twm, twmax, Lz);
+  __syncthreads();
+  if (p.ng == 1) {
+    qswitch<QCap<R>::Z1>(p.q[0], [&](auto QC) { z1_single<R, decltype(QC)::value>(Tg, nz0, pl, ncols, s00, sbase, (size_t)Lx); });
+    return;
+  }
+  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(Tg, pl, ncols, nz0, buf, p, W, Tg); });
+  __syncthreads();
+  middle_groups<R, false, LTX>(buf, TX, p, W);
+  qswitch<QCap<R>::Z1>(p.q[p.ng - 1], [&](auto QC) { z1_fused<R, decltype(QC)::value>(buf, p, ncols, s00, sbase, (size_t)Lx); });
+  __syncthreads();
+  middle_groups<R, true, LTX>(buf, TX, p, W);
+  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf, Tg, pl, ncols, nz0, p, W); });
 }
 
 // --------------------------------------------------------------------------- host side
@@ -285,102 +589,68 @@ static int smem_optin(K kernel, size_t bytes) {
   return 0;
 }
 
-static inline int ltile(int logL, int want) { return logL < want ? logL : want; }
+// radix plans per pass: x/y passes take up to 16 points per register group at both
+// ends; the z passes hold 3 families (P) at the fused step, so their last group is
+// smaller (FP64 registers are twice as wide)
+template <typename R>
+struct Plans {
+  static AxPlan xy(int n) { return make_plan(n, 4, 4, 4); }
+  static AxPlan z3(int n) { return sizeof(R) == 8 ? make_plan(n, 2, 4, 2) : make_plan(n, 3, 4, 3); }
+  static AxPlan z1(int n) { return sizeof(R) == 8 ? make_plan(n, 3, 4, 3) : make_plan(n, 4, 4, 4); }
+};
 
-// one pass-class of launches; dispatches the compile-time tile widths
 template <typename R>
 struct Launch {
-  static constexpr int LT = sizeof(R) == 8 ? 4 : 5;  // 16 (fp64) / 32 (fp32) kx per CTA
-  static constexpr int LTY = 4;                      // 16 pencils per x-pass CTA
-
+  static cx<R>* buf(const Family& f) {
+    return reinterpret_cast<cx<R>*>(f.T[sizeof(R) == 8 ? 0 : 1]);
+  }
   static int xfwd(const Family& f, const c64* xin, const cx<R>* tw, int twmax, cudaStream_t st) {
-    cx<R>* T = reinterpret_cast<cx<R>*>(f.T[sizeof(R) == 8 ? 0 : 1]);
     const int Lx = f.L[0];
-    const size_t sm = sizeof(cx<R>) * ((Lx > 1 ? Lx / 2 : 1) + (size_t)Lx * ((1 << LTY) + 1));
-    CTX_CHECK(smem_optin(k_xfwd<R, LTY>, sm));
-    dim3 g((f.dims[1] + (1 << LTY) - 1) >> LTY, f.dims[2]);
-    k_xfwd<R, LTY><<<g, TPB, sm, st>>>(xin, f.map, T, Lx, f.logL[0], f.L[1], f.dims[0], f.dims[1],
-                                       f.dims[2], tw, twmax);
+    const size_t sm = sizeof(cx<R>) * (Lx + (size_t)Lx * XRS);
+    CTX_CHECK(smem_optin(k_xfwd<R>, sm));
+    dim3 g((f.dims[1] + TY - 1) / TY, f.dims[2]);
+    k_xfwd<R><<<g, TPB, sm, st>>>(xin, f.map, buf(f), Plans<R>::xy(f.logL[0]), f.L[1], f.dims[0],
+                                  f.dims[1], tw, twmax);
     return 0;
   }
   static int xinv(const Family& f, c64* yout, const cx<R>* tw, int twmax, cudaStream_t st) {
-    cx<R>* T = reinterpret_cast<cx<R>*>(f.T[sizeof(R) == 8 ? 0 : 1]);
     const int Lx = f.L[0];
-    const size_t sm = sizeof(cx<R>) * ((Lx > 1 ? Lx / 2 : 1) + (size_t)Lx * ((1 << LTY) + 1));
-    CTX_CHECK(smem_optin(k_xinv<R, LTY>, sm));
-    dim3 g((f.dims[1] + (1 << LTY) - 1) >> LTY, f.dims[2]);
-    k_xinv<R, LTY><<<g, TPB, sm, st>>>(T, yout, f.map, Lx, f.logL[0], f.L[1], f.dims[0], f.dims[1],
-                                       f.dims[2], tw, twmax);
-    return 0;
-  }
-  template <bool INV, int LTX>
-  static int ypass_t(const Family& f, const cx<R>* tw, int twmax, cudaStream_t st) {
-    cx<R>* T = reinterpret_cast<cx<R>*>(f.T[sizeof(R) == 8 ? 0 : 1]);
-    const int Ly = f.L[1];
-    const size_t sm = sizeof(cx<R>) * ((Ly > 1 ? Ly / 2 : 1) + ((size_t)Ly << LTX));
-    CTX_CHECK(smem_optin(k_ypass<R, INV, LTX>, sm));
-    dim3 g(f.L[0] >> LTX, f.dims[2]);
-    k_ypass<R, INV, LTX><<<g, TPB, sm, st>>>(T, f.L[0], Ly, f.logL[1], INV ? Ly : f.dims[1],
-                                             INV ? f.dims[1] : Ly, tw, twmax);
+    const size_t sm = sizeof(cx<R>) * (Lx + (size_t)Lx * XRS);
+    CTX_CHECK(smem_optin(k_xinv<R>, sm));
+    dim3 g((f.dims[1] + TY - 1) / TY, f.dims[2]);
+    k_xinv<R><<<g, TPB, sm, st>>>(buf(f), yout, f.map, Plans<R>::xy(f.logL[0]), f.L[1], f.dims[0],
+                                  f.dims[1], tw, twmax);
     return 0;
   }
   template <bool INV>
   static int ypass(const Family& f, const cx<R>* tw, int twmax, cudaStream_t st) {
-    switch (ltile(f.logL[0], LT)) {
-      case 0: return ypass_t<INV, 0>(f, tw, twmax, st);
-      case 1: return ypass_t<INV, 1>(f, tw, twmax, st);
-      case 2: return ypass_t<INV, 2>(f, tw, twmax, st);
-      case 3: return ypass_t<INV, 3>(f, tw, twmax, st);
-      case 4: return ypass_t<INV, 4>(f, tw, twmax, st);
-      default: return ypass_t<INV, LT>(f, tw, twmax, st);
-    }
-  }
-  template <int LTX>
-  static int zconv3_t(const Family* F, const PSpec& S, const cx<R>* tw, int twmax,
-                      cudaStream_t st) {
-    const int p = sizeof(R) == 8 ? 0 : 1;
-    const int Lz = F[0].L[2];
-    const size_t sm = sizeof(cx<R>) * ((Lz > 1 ? Lz / 2 : 1) + 3 * ((size_t)Lz << LTX));
-    CTX_CHECK(smem_optin(k_zconv3<R, LTX>, sm));
-    dim3 g(F[0].L[0] >> LTX, F[0].L[1]);
-    k_zconv3<R, LTX><<<g, TPB, sm, st>>>(
-        reinterpret_cast<cx<R>*>(F[0].T[p]), reinterpret_cast<cx<R>*>(F[1].T[p]),
-        reinterpret_cast<cx<R>*>(F[2].T[p]), F[0].dims[2], F[1].dims[2], F[2].dims[2], S, F[0].L[0],
-        F[0].L[1], Lz, F[0].logL[2], tw, twmax);
+    const int Ly = f.L[1];
+    const size_t sm = sizeof(cx<R>) * (Ly + ((size_t)Ly << LTX));
+    CTX_CHECK(smem_optin(k_ypass<R, INV>, sm));
+    dim3 g((f.L[0] + TX - 1) / TX, f.dims[2]);
+    k_ypass<R, INV><<<g, TPB, sm, st>>>(buf(f), f.L[0], Plans<R>::xy(f.logL[1]),
+                                        INV ? Ly : f.dims[1], INV ? f.dims[1] : Ly, tw, twmax);
     return 0;
   }
-  static int zconv3(const Family* F, const PSpec& S, const cx<R>* tw, int twmax, cudaStream_t st) {
-    switch (ltile(F[0].logL[0], LT)) {
-      case 0: return zconv3_t<0>(F, S, tw, twmax, st);
-      case 1: return zconv3_t<1>(F, S, tw, twmax, st);
-      case 2: return zconv3_t<2>(F, S, tw, twmax, st);
-      case 3: return zconv3_t<3>(F, S, tw, twmax, st);
-      case 4: return zconv3_t<4>(F, S, tw, twmax, st);
-      default: return zconv3_t<LT>(F, S, tw, twmax, st);
-    }
-  }
-  template <int LTX>
-  static int zconv1_t(const Family& f, const void* s, const cx<R>* tw, int twmax,
-                      cudaStream_t st) {
-    const int p = sizeof(R) == 8 ? 0 : 1;
-    const int Lz = f.L[2];
-    const size_t sm = sizeof(cx<R>) * ((Lz > 1 ? Lz / 2 : 1) + ((size_t)Lz << LTX));
-    CTX_CHECK(smem_optin(k_zconv1<R, LTX>, sm));
-    dim3 g(f.L[0] >> LTX, f.L[1]);
-    k_zconv1<R, LTX><<<g, TPB, sm, st>>>(reinterpret_cast<cx<R>*>(f.T[p]), f.dims[2],
-                                         reinterpret_cast<const R*>(s), f.L[0], f.L[1], Lz,
-                                         f.logL[2], tw, twmax);
+  static int zconv3(const Family* F, const PSpec& S, const cx<R>* tw, int twmax,
+                    cudaStream_t st) {
+    const int Lz = F[0].L[2];
+    const size_t sm = sizeof(cx<R>) * (Lz + 3 * ((size_t)Lz << LTX));
+    CTX_CHECK(smem_optin(k_zconv3<R>, sm));
+    dim3 g((F[0].L[0] + TX - 1) / TX, F[0].L[1]);
+    k_zconv3<R><<<g, TPB, sm, st>>>(buf(F[0]), buf(F[1]), buf(F[2]), F[0].dims[2], F[1].dims[2],
+                                    F[2].dims[2], S, F[0].L[0], F[0].L[1],
+                                    Plans<R>::z3(F[0].logL[2]), tw, twmax);
     return 0;
   }
   static int zconv1(const Family& f, const void* s, const cx<R>* tw, int twmax, cudaStream_t st) {
-    switch (ltile(f.logL[0], LT)) {
-      case 0: return zconv1_t<0>(f, s, tw, twmax, st);
-      case 1: return zconv1_t<1>(f, s, tw, twmax, st);
-      case 2: return zconv1_t<2>(f, s, tw, twmax, st);
-      case 3: return zconv1_t<3>(f, s, tw, twmax, st);
-      case 4: return zconv1_t<4>(f, s, tw, twmax, st);
-      default: return zconv1_t<LT>(f, s, tw, twmax, st);
-    }
+    const int Lz = f.L[2];
+    const size_t sm = sizeof(cx<R>) * (Lz + ((size_t)Lz << LTX));
+    CTX_CHECK(smem_optin(k_zconv1<R>, sm));
+    dim3 g((f.L[0] + TX - 1) / TX, f.L[1]);
+    k_zconv1<R><<<g, TPB, sm, st>>>(buf(f), f.dims[2], reinterpret_cast<const R*>(s), f.L[0],
+                                    f.L[1], Plans<R>::z1(f.logL[2]), tw, twmax);
+    return 0;
   }
 };
 

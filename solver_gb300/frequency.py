@@ -100,3 +100,45 @@ def export_lu(lu):
                 np.ascontiguousarray(M.data.astype(np.complex128)).view(np.float64))
 
     return parts(L), parts(U), lu.perm_r.astype(np.int64), lu.perm_c.astype(np.int64)
+
+
+class StatePrefetcher:
+    """Frequency-loop pipelining: while the GPU solves frequency k, a worker thread
+    builds the host state (Yle, SuperLU factors) of the next frequency in the
+    sequence. The GPU solves run inside foreign calls that release the GIL, so the
+    factorisation proceeds alongside them.
+
+    make(k) -> state; order: the sequence of k the caller will request; keep: hold
+    every built state for repeated requests (otherwise a state is dropped once read)."""
+
+    def __init__(self, make, order, keep=True):
+        from concurrent.futures import ThreadPoolExecutor
+        self._make = make
+        self._order = list(order)
+        self._pos = 0
+        self._pool = ThreadPoolExecutor(max_workers=1)
+        self._pending = {}
+        self._done = {}
+        self._keep = keep
+
+    def get(self, k):
+        if k in self._done:
+            st = self._done[k]
+        elif k in self._pending:
+            st = self._pending.pop(k).result()
+        else:
+            st = self._make(k)
+        if self._keep:
+            self._done[k] = st
+        # start the state the sequence asks for next, if it is not built yet
+        while self._pos < len(self._order) and self._order[self._pos] != k:
+            self._pos += 1
+        self._pos += 1
+        if self._pos < len(self._order):
+            nxt = self._order[self._pos]
+            if nxt not in self._done and nxt not in self._pending:
+                self._pending[nxt] = self._pool.submit(self._make, nxt)
+        return st
+
+    def close(self):
+        self._pool.shutdown(wait=True)

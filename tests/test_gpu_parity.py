@@ -164,6 +164,24 @@ def test_sweep_parity(case):
     assert _rel(got["Vrest"], ref["Vrest"]) < 1e-10
 
 
+def test_mixed_sweep(case):
+    """The port x frequency sweep in mixed precision (zero initial guesses, host LU of
+    the next frequency built on a worker thread) against the oracle's FP64 sweep, both
+    converged to 1e-10: every solve meets the tolerance in the FP64 residual and the
+    port impedances agree to the accuracy that residual bounds."""
+    from solver_gb300 import api
+    c = case
+    st = {"Inner_Iter": c["settings"]["Inner_Iter"], "tol": np.full(len(c["freqs"]), 1e-10)}
+    ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
+                                 c["diag"], c["ports"], c["z0"], c["le"], c["exp"], st, c["Zs"])
+    c["exp"]["gpu_ctx"] = c["op"]
+    h = api.CirculantSpectra(c["op"])
+    got = api.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], h, h, c["diag"], c["ports"],
+                                   c["z0"], c["le"], c["exp"], st, c["Zs"], mode="mixed")
+    assert all(r["flag"] == 0 and r["relres"] <= 1e-10 for r in got["info"]), got["info"]
+    assert _rel(got["Z"], ref["Z"]) < 1e-6
+
+
 def test_fill_against_long_double(case):
     c = case
     rows_gpu = c["op"].fill(c["cc"]["origin"], c["cc"]["sx"], c["cc"]["sy"], c["cc"]["sz"],
