@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--inner-tol", type=float, default=1e-7,
+                    help="floor of the inner FP32 GMRES relative tolerance")
     ap.add_argument("--profile-iters", type=int, default=20)
     ap.add_argument("--grid", type=int, nargs=3, default=None,
                     help="smaller random Cu/dielectric grid (profiling captures only)")
@@ -205,7 +207,8 @@ def solve_point(P, fs, Vrest, mode, tol):
         tn = op.port_rhs(pn[c1, 0], pn[c1, 1], P["esc"]["Is"])
         if mode == "mixed":
             # warm start from the previous frequency's solution, as the reference does
-            V, flag, relres, outer, ninner = op.solve_mixed(tn, Vrest[:, c1], tol, inner_tol=1e-5,
+            V, flag, relres, outer, ninner = op.solve_mixed(tn, Vrest[:, c1], tol,
+                                                            inner_tol=P["inner_tol"],
                                                             inner_maxit=P["settings"]["Inner_Iter"])
             work.append({"flag": flag, "relres": relres, "outer": outer, "inner": ninner,
                          "fp64_matvecs": outer + 1, "fp32_matvecs": ninner + outer})
@@ -305,6 +308,7 @@ def main():
         return
     ws, rank, local = dist_init()
     P = setup_problem(device=local, grid=args.grid)
+    P["inner_tol"] = args.inner_tol
     op = P["op"]
     nf = len(P["freqs"])
     tol = float(P["settings"]["tol"])

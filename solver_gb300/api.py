@@ -150,7 +150,7 @@ def s2y_fft(S, Zo):
 def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, diagonals, ports,
                          ports_scatter_value, lumped_elements, expansions, GMRES_settings,
                          Zs_info, QS_Rcc_FW=1, id=None, chan=None, commentsEnabled=False, *,
-                         mode="fp64", mixed_inner_tol=1e-5, mixed_warm_start=True,
+                         mode="fp64", mixed_inner_tol=1e-7, mixed_warm_start=True,
                          stop_flag=None, on_solve=None):
     """Frequency x port sweep with warm starts (FFT_solver_QS_S_type.jl:1-234).
 

@@ -235,7 +235,7 @@ class GpuOperator:
         _lib.check(self.h, rc)
         return x, flag.value, relres.value, [it[0], it[1]], resvec[:nres.value].copy()
 
-    def solve_mixed(self, b, x0, tol, inner_tol=1e-5, inner_maxit=100, max_outer=8):
+    def solve_mixed(self, b, x0, tol, inner_tol=1e-7, inner_maxit=100, max_outer=8):
         b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())
         x = np.zeros(self.N, dtype=np.complex128) if x0 is None else \
             np.array(np.asarray(x0, dtype=np.complex128).ravel())
