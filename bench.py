@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lanes", type=int, default=4,
+                    help="concurrent port solves (contexts + host threads), at most the ports")
     ap.add_argument("--inner-tol", type=float, default=1e-7,
                     help="floor of the inner FP32 GMRES relative tolerance")
     ap.add_argument("--profile-iters", type=int, default=20)
@@ -191,11 +193,60 @@ def freq_state(P, k):
                              P["z0"])
 
 
+def solve_point_lanes(P, fs, Vrest, tol):
+    """One frequency point in mixed precision with the ports spread over concurrent
+    lanes (one context and host thread each)."""
+    lanes = P["lanes"]
+    t0 = time.perf_counter()
+    lanes.set_frequency(fs.w, fs.DZ, fs.Yle, fs.lu)
+    P["host_ms"]["set_frequency"] += (time.perf_counter() - t0) * 1e3
+    m, n = P["inc"]["A"].shape
+    ns = P["inc"]["Gamma"].shape[1]
+    pn = np.asarray(P["ports"]["port_nodes"], dtype=np.int64)
+    npt = pn.shape[0]
+    z0 = P["z0"]
+
+    def job(c1):
+        def run(op):
+            tn = op.port_rhs(pn[c1, 0], pn[c1, 1], P["esc"]["Is"])
+            return op.solve_mixed(tn, Vrest[:, c1], tol, inner_tol=P["inner_tol"],
+                                  inner_maxit=P["settings"]["Inner_Iter"])
+        return run
+    t0 = time.perf_counter()
+    res = lanes.run([job(c1) for c1 in range(npt)])
+    P["host_ms"]["solve_mixed"] += (time.perf_counter() - t0) * 1e3
+    S = np.zeros((npt, npt), dtype=np.complex128)
+    work = []
+    for c1, (V, flag, relres, outer, ninner) in enumerate(res):
+        work.append({"flag": flag, "relres": relres, "outer": outer, "inner": ninner,
+                     "fp64_matvecs": outer + 1, "fp32_matvecs": ninner + outer})
+        Vrest[:, c1] = V
+    for c1 in range(npt):
+        for c2 in range(c1, npt):
+            val = 2 * (Vrest[m + ns + pn[c2, 0], c1] - Vrest[m + ns + pn[c2, 1], c1])
+            S[c1, c2] = (val - z0) / z0 if c1 == c2 else val / z0
+            S[c2, c1] = S[c1, c2]
+    return S, work, _point_bytes(P, fs, npt), npt * 2 * (m + ns + n) * 16
+
+
+def _point_bytes(P, fs, npt):
+    from solver_gb300.frequency import export_lu
+    m, n = P["inc"]["A"].shape
+    N = m + P["inc"]["Gamma"].shape[1] + n
+    (_, Lc, _), (_, Uc, _), _, _ = export_lu(fs.lu)
+    return (fs.DZ.nbytes + (Lc.size + Uc.size) * 24 + (2 * n + 2) * 8 * 2 + 2 * n * 8 +
+            fs.Yle.nnz * 32 + npt * (2 * N * 16))
+
+
 def solve_point(P, fs, Vrest, mode, tol):
     """One frequency point: upload the frequency state, then RHS + solve per port.
     Returns the S-matrix column values and per-port work counts, and H2D/D2H bytes."""
+    if mode == "mixed" and P.get("lanes") is not None and len(P["lanes"]) > 1:
+        return solve_point_lanes(P, fs, Vrest, tol)
     op = P["op"]
+    t0 = time.perf_counter()
     op.set_frequency(fs.w, fs.DZ, fs.Yle, fs.lu)
+    P["host_ms"]["set_frequency"] += (time.perf_counter() - t0) * 1e3
     m, n = P["inc"]["A"].shape
     ns = P["inc"]["Gamma"].shape[1]
     pn = np.asarray(P["ports"]["port_nodes"], dtype=np.int64)
@@ -204,12 +255,16 @@ def solve_point(P, fs, Vrest, mode, tol):
     S = np.zeros((npt, npt), dtype=np.complex128)
     work = []
     for c1 in range(npt):
+        t0 = time.perf_counter()
         tn = op.port_rhs(pn[c1, 0], pn[c1, 1], P["esc"]["Is"])
+        t1 = time.perf_counter()
+        P["host_ms"]["port_rhs"] += (t1 - t0) * 1e3
         if mode == "mixed":
             # warm start from the previous frequency's solution, as the reference does
             V, flag, relres, outer, ninner = op.solve_mixed(tn, Vrest[:, c1], tol,
                                                             inner_tol=P["inner_tol"],
                                                             inner_maxit=P["settings"]["Inner_Iter"])
+            P["host_ms"]["solve_mixed"] += (time.perf_counter() - t1) * 1e3
             work.append({"flag": flag, "relres": relres, "outer": outer, "inner": ninner,
                          "fp64_matvecs": outer + 1, "fp32_matvecs": ninner + outer})
         else:
@@ -222,11 +277,7 @@ def solve_point(P, fs, Vrest, mode, tol):
             S[c1, c2] = (val - z0) / z0 if c1 == c2 else val / z0
             S[c2, c1] = S[c1, c2]
     N = m + ns + n
-    L, U = fs.lu.L, fs.lu.U
-    h2d = (fs.DZ.nbytes + (L.nnz + U.nnz) * 24 + (2 * n + 2) * 8 * 2 + 2 * n * 8 +
-           fs.Yle.nnz * 32 + npt * (2 * N * 16))
-    d2h = npt * 2 * N * 16
-    return S, work, h2d, d2h
+    return S, work, _point_bytes(P, fs, npt), npt * 2 * N * 16
 
 
 def cpu_baseline(P, mv_per_port, sample_note):
@@ -309,14 +360,19 @@ def main():
     ws, rank, local = dist_init()
     P = setup_problem(device=local, grid=args.grid)
     P["inner_tol"] = args.inner_tol
+    P["host_ms"] = {"set_frequency": 0.0, "port_rhs": 0.0, "solve_mixed": 0.0}
     op = P["op"]
     nf = len(P["freqs"])
     tol = float(P["settings"]["tol"])
     Vrest = np.zeros((op.N, len(P["ports"]["port_nodes"])), dtype=np.complex128)
-    # host LU of the next frequency is built on a worker thread while the GPU solves
-    from solver_gb300.frequency import StatePrefetcher
+    # host states (Yle, SuperLU factors) of the next frequencies are built by spawned
+    # worker processes while the GPU solves the current one
+    from solver_gb300.frequency import FrequencyPool
     order = [0] + [i % nf for i in range(args.warmup + args.steps)] + list(range(args.fp64_steps))
-    pf = StatePrefetcher(lambda k: freq_state(P, k), order, keep=True)
+    static = (P["esc"], P["inc"], P["diag"], P["Zs"], P["le"], P["ports"], P["z0"])
+    nworkers = max(2, min(12, (os.cpu_count() or 4) - 4))
+    pf = FrequencyPool(static, lambda k: 2 * np.pi * P["freqs"][k] * P["esc"]["freq"], order,
+                       workers=nworkers, lookahead=nworkers, keep=True)
     state = pf.get
 
     # -- operator profile and roofline (FP32 and FP64 convolutions) --------------------------
@@ -324,14 +380,20 @@ def main():
     info = op.conv_info()
     prof32 = op.profile_matvec(1, args.profile_iters)
     prof64 = op.profile_matvec(0, max(3, args.profile_iters // 4))
+    profff = op.profile_matvec(2, max(3, args.profile_iters // 4))
     b32, b64 = conv_bytes(info, 1), conv_bytes(info, 0)
     peak, peak_kind = load_peaks()
 
     # -- mixed-precision timed steps ---------------------------------------------------------
-    import ctypes
+    from solver_gb300.api import PortLanes
+    nlanes = max(1, min(args.lanes, len(P["ports"]["port_nodes"])))
+    P["lanes"] = PortLanes(op, nlanes)
+    lane_streams = [op.stream()] + [o.stream() for o in P["lanes"].ops[1:]]
     try:
         import torch
         ext = torch.cuda.ExternalStream(op.stream(), device=f"cuda:{local}")
+        lane_ext = [ext] + [torch.cuda.ExternalStream(h, device=f"cuda:{local}")
+                            for h in lane_streams[1:]]
         ev = lambda: torch.cuda.Event(enable_timing=True)
         have_torch = True
     except Exception:
@@ -348,16 +410,28 @@ def main():
     if have_torch:
         torch.cuda.synchronize()
     clocks = Clocks(local)
+    host_wait = 0.0
+    P["host_ms"] = {k: 0.0 for k in P["host_ms"]}
     t_wall0 = time.perf_counter()
     for i in range(args.warmup, args.warmup + args.steps):
         k = i % nf
-        fs = state(k)  # host LU, built on the worker thread while the previous point solved
+        th = time.perf_counter()
+        fs = state(k)  # host LU, built by the worker processes while earlier points solved
+        host_wait += time.perf_counter() - th
         if have_torch:
+            # the step spans every lane: the other lanes' streams wait on e0, and the
+            # first lane's stream waits on each lane's end before e1
             e0, e1 = ev(), ev()
             e0.record(ext)
+            for xs in lane_ext[1:]:
+                xs.wait_event(e0)
         t0 = time.perf_counter()
         S_mixed[k], w_, hb, db = solve_point(P, fs, Vrest, "mixed", tol)
         if have_torch:
+            for xs in lane_ext[1:]:
+                ei = ev()
+                ei.record(xs)
+                ext.wait_event(ei)
             e1.record(ext)
             e1.synchronize()
             gpu_ms += e0.elapsed_time(e1)
@@ -404,14 +478,18 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": gpu_s * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "complex64 convolutions / complex128 refinement", "data": "synthetic",
+        "dtype": "complex64 convolutions in the inner solves; float-float (48-bit) "
+                 "convolutions + complex128 sparse part in the refinement residuals", "data": "synthetic",
         "config": {"workload": WORKLOAD if args.grid is None else f"random {args.grid}",
                    "grid": list(P["grid"]), "N": int(op.N),
                    "m_edges": int(op.m), "ns_surfaces": int(op.ns), "n_nodes": int(op.n),
                    "l2": "inputs larger than L2 (Krylov basis and spectra > 129 MB)",
-                   "parallelism": f"replicas x{ws}"},
+                   "parallelism": f"replicas x{ws}", "port_lanes": nlanes},
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
-                "d2h_bytes_per_step": int(d2h / args.steps)},
+                "d2h_bytes_per_step": int(d2h / args.steps),
+                "host_state_wait_ms_per_step": host_wait * 1e3 / args.steps,
+                "host_state_workers": nworkers,
+                "host_ms_per_step": {k: v / args.steps for k, v in P["host_ms"].items()}},
         "gpu_launches": int(launches),
         "clocks": clk,
         "fp64_plain": {"value": fp64_v, "unit": UNIT, "steps": args.fp64_steps,
@@ -422,6 +500,7 @@ def main():
                        "max_relres": float(max(w_["relres"] for w_ in work)),
                        "z_rel_err_vs_fp64": max(errs) if errs else None},
         "matvec": {"fp32_ms": prof32["total"], "fp64_ms": prof64["total"],
+                   "ff_ms": profff["total"], "ff_ms_by_pass": profff,
                    "fp32_conv_gbs": conv_gbs(b32, prof32), "fp64_conv_gbs": conv_gbs(b64, prof64),
                    "fp32_ms_by_pass": prof32, "fp64_ms_by_pass": prof64,
                    "fp32_bytes_by_pass": b32},
@@ -438,6 +517,7 @@ def main():
     if rank == 0:
         print(json.dumps(line), flush=True)
     pf.close()
+    P["lanes"].close()
     op.close()
     if ws > 1:
         import torch.distributed as dist

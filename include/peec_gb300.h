@@ -35,9 +35,14 @@ extern "C" {
 #define PEEC_ERR_UNSUPPORTED (-6)
 #define PEEC_ERR_STATE (-7)
 
-/* precision of the circulant convolutions */
+/* arithmetic of the circulant convolutions (the sparse part is always FP64):
+ * FP64, FP32, or float-float (hi + lo FP32 pairs, about 48 significant bits; the
+ * FP64 data and spectra are split on load). Float-float has no counterpart in the
+ * reference; it serves the refinement residuals of peec_solve_mixed, where GB300's
+ * FP32 pipes are far faster than its FP64 ones. */
 #define PEEC_PREC_FP64 0
 #define PEEC_PREC_FP32 1
+#define PEEC_PREC_FF 2
 
 typedef struct peec_ctx peec_ctx;
 
@@ -135,13 +140,22 @@ int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, double tol, int 
 
 /*
  * Mixed-precision solve: GMRES inner solves on the FP32-convolution operator inside
- * FP64 iterative refinement (FP64 residual recomputation), to relative residual tol.
- * inner_tol / inner_maxit bound each inner solve, max_outer the refinements.
- * outer_out / inner_total report the work; relres the final FP64 relative residual.
+ * iterative refinement with FP64 vectors, to relative residual tol. The refinement
+ * residuals b - A x use the operator in the residual precision (float-float by
+ * default, see peec_set_residual_precision). inner_tol / inner_maxit bound each
+ * inner solve, max_outer the refinements. outer_out / inner_total report the work;
+ * relres the final relative residual. No counterpart in the reference (which solves
+ * with FP64 GMRES only, FFT_solver_QS_S_type.jl:140).
  */
 int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout, double tol,
                      double inner_tol, int inner_maxit, int max_outer, int* flag,
                      double* relres, int* outer_out, int* inner_total);
+
+/*
+ * Arithmetic of the refinement residuals of peec_solve_mixed: PEEC_PREC_FF (default)
+ * or PEEC_PREC_FP64. No counterpart in the reference.
+ */
+int peec_set_residual_precision(peec_ctx* ctx, int precision);
 
 /*
  * Cooperative cancellation (is_stop_requested, solver_start.jl:370-374): a host

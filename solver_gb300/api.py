@@ -147,6 +147,49 @@ def s2y_fft(S, Zo):
     return np.stack([Zo * np.linalg.solve(I + S[:, :, k], I - S[:, :, k]) for k in range(nf)], 2)
 
 
+class PortLanes:
+    """Concurrent port solves of one frequency: one context per lane (its own CUDA
+    stream, FFT buffers, Krylov workspace and LU-solve control words; same topology
+    and circulant rows), each lane driven by its own host thread. The library calls
+    release the GIL, so the lanes' kernels overlap on the GPU: the latency-bound
+    parts of one port's iteration (triangular solves, small reductions, host round
+    trips) fill in around the bandwidth-bound transforms of the others."""
+
+    def __init__(self, op, nlanes):
+        from concurrent.futures import ThreadPoolExecutor
+        self.ops = [op] + [op.clone() for _ in range(max(1, nlanes) - 1)]
+        self._pool = ThreadPoolExecutor(max_workers=len(self.ops))
+
+    def __len__(self):
+        return len(self.ops)
+
+    def set_frequency(self, w, DZ, Yle, lu, key=None):
+        list(self._pool.map(lambda o: o.set_frequency(w, DZ, Yle, lu, key=key), self.ops))
+
+    def run(self, jobs):
+        """jobs[i](op) runs on lane i % lanes; jobs of a lane run in order. Returns the
+        results in job order."""
+        L = len(self.ops)
+
+        def lane(i):
+            return [(j, jobs[j](self.ops[i])) for j in range(i, len(jobs), L)]
+        out = [None] * len(jobs)
+        for res in self._pool.map(lane, range(L)):
+            for j, r in res:
+                out[j] = r
+        return out
+
+    def close(self):
+        self._pool.shutdown(wait=True)
+        for o in self.ops[1:]:
+            o.close()
+
+
+# node count from which the per-frequency host factorisations run in worker processes
+# (below it, process start-up costs more than the factorisations)
+POOL_MIN_NODES = 50000
+
+
 def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, diagonals, ports,
                          ports_scatter_value, lumped_elements, expansions, GMRES_settings,
                          Zs_info, QS_Rcc_FW=1, id=None, chan=None, commentsEnabled=False, *,
@@ -176,10 +219,16 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
     Vrest = np.zeros((m + n + ns, npt), dtype=np.complex128)
     tol = GMRES_settings["tol"]
     info = []
-    pf = fq.StatePrefetcher(
-        lambda k: fq.FrequencyState(w[k], escalings, incidence_selection, diagonals, Zs_info,
-                                    lumped_elements, ports, ports_scatter_value),
-        range(w.size), keep=False)
+    if n >= POOL_MIN_NODES and w.size > 2:
+        # large node systems: factorise ahead in spawned worker processes
+        pf = fq.FrequencyPool((escalings, incidence_selection, diagonals, Zs_info,
+                               lumped_elements, ports, ports_scatter_value),
+                              lambda k: w[k], range(w.size), workers=4, lookahead=4, keep=False)
+    else:
+        pf = fq.StatePrefetcher(
+            lambda k: fq.FrequencyState(w[k], escalings, incidence_selection, diagonals, Zs_info,
+                                        lumped_elements, ports, ports_scatter_value),
+            range(w.size), keep=False)
     try:
         res = _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode,
                      mixed_inner_tol, mixed_warm_start, stop_flag, on_solve, info, m, ns,

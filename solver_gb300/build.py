@@ -28,8 +28,10 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "-I", str(INCLUDE), "-I", str(CSRC)]
 
 MESH_SOURCES = ["mesher.cpp"]
-CUDA_SOURCES = ["ctx.cu", "fftconv.cu", "krylov.cu", "sparse.cu", "fill.cu"]
-CUDA_HEADERS = ["common.cuh", "fft.cuh", "integrals.cuh", "ctx.hpp"]
+CUDA_SOURCES = ["ctx.cu", "fftconv.cu", "fftconv_f32.cu", "fftconv_f64.cu", "fftconv_ff.cu",
+                "krylov.cu", "sparse.cu", "fill.cu"]
+CUDA_HEADERS = ["common.cuh", "fft.cuh", "fft_reg.cuh", "fftconv_impl.cuh", "integrals.cuh",
+                "ctx.hpp"]
 
 
 def nvcc_path() -> str:

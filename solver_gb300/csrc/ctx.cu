@@ -88,6 +88,8 @@ struct peec_ctx {
   int twmax = 0;
   void* tw64 = nullptr;
   void* tw32 = nullptr;
+  void* twff = nullptr;
+  int resid_prec = PEEC_PREC_FF;  // arithmetic of the refinement residuals
   // sizes
   int Nx = 0, Ny = 0, Nz = 0;
   int64_t mx = 0, my = 0, mz = 0, m = 0, ns = 0, n = 0, N = 0;
@@ -244,17 +246,27 @@ extern "C" int peec_ctx_create(peec_ctx** out, int device) {
   ctx->twmax = 8192;
   std::vector<c64> t64(ctx->twmax);
   std::vector<c32> t32(ctx->twmax);
+  std::vector<cff> tff(ctx->twmax);
+  // float-float split of a long double: hi the nearest float, lo the nearest float of
+  // the remainder
+  auto split = [](long double v) {
+    const float h = (float)v;
+    return ff(h, (float)(v - (long double)h));
+  };
   for (int e = 0; e < ctx->twmax; ++e) {
     long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)e /
                     (long double)ctx->twmax;
     t64[e] = mk<double>((double)cosl(a), (double)sinl(a));
     t32[e] = mk<float>((float)cosl(a), (float)sinl(a));
+    tff[e] = mk<ff>(split(cosl(a)), split(sinl(a)));
   }
   if (cudaMalloc(&ctx->tw64, sizeof(c64) * ctx->twmax) != cudaSuccess ||
-      cudaMalloc(&ctx->tw32, sizeof(c32) * ctx->twmax) != cudaSuccess)
+      cudaMalloc(&ctx->tw32, sizeof(c32) * ctx->twmax) != cudaSuccess ||
+      cudaMalloc(&ctx->twff, sizeof(cff) * ctx->twmax) != cudaSuccess)
     return fail(fail_cuda(cudaErrorMemoryAllocation, "cudaMalloc twiddles", __FILE__, __LINE__));
   cudaMemcpy(ctx->tw64, t64.data(), sizeof(c64) * ctx->twmax, cudaMemcpyHostToDevice);
   cudaMemcpy(ctx->tw32, t32.data(), sizeof(c32) * ctx->twmax, cudaMemcpyHostToDevice);
+  cudaMemcpy(ctx->twff, tff.data(), sizeof(cff) * ctx->twmax, cudaMemcpyHostToDevice);
   cudaMallocHost(&ctx->hsmall, sizeof(c64) * 16 * 4096);
   cudaMallocHost(&ctx->hread, sizeof(c64) * 4096);
   cudaMallocHost(&ctx->hscal, sizeof(double) * 64);
@@ -272,7 +284,7 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   cudaSetDevice(ctx->dev);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   drop_graphs(ctx);
-  void* ptrs[] = {ctx->tw64, ctx->tw32, ctx->n1, ctx->n2, ctx->snode, ctx->invP, ctx->ne_ptr,
+  void* ptrs[] = {ctx->tw64, ctx->tw32, ctx->twff, ctx->n1, ctx->n2, ctx->snode, ctx->invP, ctx->ne_ptr,
                   ctx->ne_idx, ctx->nsn_ptr, ctx->nsn_idx, ctx->DZ, ctx->yle_ptr, ctx->yle_col,
                   ctx->yle_val, ctx->g_in, ctx->g_out, ctx->lu_rs, ctx->LpI, ctx->PQ, ctx->Y1, ctx->U1,
                   ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->lutmp2, ctx->dx, ctx->dy, ctx->U,
@@ -765,8 +777,9 @@ static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool ev
   const int64_t m = ctx->m, ns = ctx->ns, n = ctx->n;
   cudaStream_t st = ctx->st;
   if (events) cudaEventRecord(ctx->ev[0], st);
-  CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, x, ctx->LpI, ctx->PQ, m, prec, ctx->tw64, ctx->tw32,
-                   ctx->twmax, st, ctx->prof ? ctx->pev.data() : nullptr));
+  const void* tw[3] = {ctx->tw64, ctx->tw32, ctx->twff};
+  CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, x, ctx->LpI, ctx->PQ, m, prec, tw, ctx->twmax, st,
+                   ctx->prof ? ctx->pev.data() : nullptr));
   for (const auto& F : ctx->fam) ctx->launches += F.active ? (F.lp ? 5 : 4) : 0;
   ctx->launches += 1;  // the shared z pass of the face families
   if (events) cudaEventRecord(ctx->ev[1], st);
@@ -826,7 +839,7 @@ static int matvec_dev(peec_ctx* ctx, const c64* x, c64* y, int prec, bool timed)
 
 extern "C" int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precision) {
   if (!ctx || !x || !y) return badarg(__func__);
-  if (precision != 0 && precision != 1) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0 or 1");
+  if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
   cudaSetDevice(ctx->dev);
   CTX_TRY(matvec_dev(ctx, (const c64*)x, (c64*)y, precision, true));
   PEEC_CUDA_TRY(cudaEventSynchronize(ctx->ev[2]));
@@ -868,7 +881,7 @@ extern "C" int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* dims, int
 
 extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, double* ms) {
   if (!ctx || !ms || iters < 1) return badarg(__func__);
-  if (precision != 0 && precision != 1) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0 or 1");
+  if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
   cudaSetDevice(ctx->dev);
   if (ctx->pev.size() != 6) {
     for (auto e : ctx->pev) cudaEventDestroy(e);
@@ -876,6 +889,9 @@ extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, doub
     for (auto& e : ctx->pev) PEEC_CUDA_TRY(cudaEventCreate(&e));
   }
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  // one untimed application first: kernel modules load lazily at their first launch
+  CTX_TRY(matvec_dev(ctx, ctx->dx, ctx->dy, precision, true));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->prof = true;
   for (int it = 0; it < iters; ++it) {
     int rc = matvec_dev(ctx, ctx->dx, ctx->dy, precision, true);
@@ -1370,7 +1386,7 @@ extern "C" int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, doubl
                           int* iter, double* resvec, int resvec_cap, int* nres) {
   if (!ctx || !b || !x_inout || !flag || !relres || !iter) return badarg(__func__);
   if (maxit < 1 || (restarted && restart < 1)) return bad(ctx, PEEC_ERR_BADARG, "maxit/restart must be >= 1");
-  if (precision != 0 && precision != 1) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0 or 1");
+  if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
   if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
   cudaSetDevice(ctx->dev);
   const size_t bytes = sizeof(c64) * ctx->N;
@@ -1403,7 +1419,7 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
   CTX_TRY(ensure_krylov(ctx, std::max(inner_maxit, 1) + 1));
   cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, ctx->st);
   cudaMemcpyAsync(dxv, x_inout, bytes, cudaMemcpyHostToDevice, ctx->st);
-  Gm g{ctx, N, 0, ctx->st};
+  Gm g{ctx, N, ctx->resid_prec, ctx->st};
   const double n2b = g.norm(db);
   int outer = 0, tot_inner = 0, fl = 1;
   double rel = 0;
@@ -1419,7 +1435,7 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
         g.copy(dr, db);
         nr = n2b;
       } else {
-        g.residual(db, dxv, dr);  // FP64 operator
+        g.residual(db, dxv, dr);  // FP64 or float-float operator
         nr = g.norm(dr);
       }
       if (g.rc) { cleanup(); return g.rc; }
@@ -1448,5 +1464,13 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
   *relres = rel;
   if (outer_out) *outer_out = outer;
   if (inner_total) *inner_total = tot_inner;
+  return PEEC_OK;
+}
+
+extern "C" int peec_set_residual_precision(peec_ctx* ctx, int precision) {
+  if (!ctx) return badarg(__func__);
+  if (precision != PEEC_PREC_FP64 && precision != PEEC_PREC_FF)
+    return bad(ctx, PEEC_ERR_BADARG, "residual precision must be PEEC_PREC_FP64 or PEEC_PREC_FF");
+  ctx->resid_prec = precision;
   return PEEC_OK;
 }

@@ -49,12 +49,13 @@ struct Spectrum {
   void* d[2] = {nullptr, nullptr};  // [0] fp64, [1] fp32; layout (ky, kz, kx), kx fastest
 };
 
-// Launchers (fftconv.cu). prec: 0 = fp64, 1 = fp32. x (input) / LpI / PQ are complex
-// double; families 0..2 are the face families, 3..5 the edge families; spectra
-// 0..5 = P blocks (00, 11, 22, 01, 02, 12), 6..8 = Lp blocks of families 3..5.
+// Launchers (fftconv.cu). prec: 0 = fp64, 1 = fp32, 2 = float-float; tw[prec] the master
+// twiddle table of that arithmetic. x (input) / LpI / PQ are complex double; families
+// 0..2 are the face families, 3..5 the edge families; spectra 0..5 = P blocks
+// (00, 11, 22, 01, 02, 12), 6..8 = Lp blocks of families 3..5.
 // ev (nullable): 6 events around the five pass classes.
 int conv_all(const Family* F, int nfam, const Spectrum* spec, const c64* x, c64* LpI, c64* PQ,
-             int64_t m, int prec, const void* tw64, const void* tw32, int twmax, cudaStream_t st,
+             int64_t m, int prec, const void* const* tw, int twmax, cudaStream_t st,
              cudaEvent_t* ev);
 int spectrum_build(Spectrum& S, const double* d_row, const int M[3], const int na[3],
                    const int nb[3], const int sdim[3], const int odim[3], int symmetric,

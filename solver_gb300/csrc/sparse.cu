@@ -161,6 +161,8 @@ __device__ __forceinline__ void sf_wait(const int* f, int epoch, int* err, int l
   }
 }
 
+constexpr int SF_CHUNK = 4;  // row entries whose column and value are held in registers
+
 __global__ void __launch_bounds__(SF_TPB) k_sptrsv(const int32_t* __restrict__ ord, int nL,
                                                    int total, SfTri L, SfTri U,
                                                    const c64* __restrict__ b,
@@ -182,21 +184,46 @@ __global__ void __launch_bounds__(SF_TPB) k_sptrsv(const int32_t* __restrict__ o
       const bool up = base >= nL;
       const SfTri& T = up ? U : L;
       c64* out = up ? z : y;
+      // everything that does not depend on other rows is loaded before the first wait
+      const int p0 = T.ptr[r], p1 = T.ptr[r + 1];
+      const c64 dr = T.dinv[r];
       c64 acc;
       if (!up) {
         const int j = g_in[r];
         acc = rs ? cscale(b[j], rs[j]) : b[j];
-      } else {
+      }
+      int cc[SF_CHUNK];
+      c64 vv[SF_CHUNK];
+#pragma unroll
+      for (int q = 0; q < SF_CHUNK; ++q) {
+        if (p0 + q < p1) {
+          cc[q] = T.col[p0 + q];
+          vv[q] = T.val[p0 + q];
+        }
+      }
+      if (up) {
         sf_wait(L.flag + r, epoch, err, limit);
         acc = ld_cg(y + r);
       }
-      for (int p = T.ptr[r]; p < T.ptr[r + 1]; ++p) {
-        const int c = T.col[p];
-        sf_wait(T.flag + c, epoch, err, limit);
-        const c64 xc = ld_cg(out + c);
-        acc = acc - T.val[p] * xc;
+      for (int p = p0; p < p1; p += SF_CHUNK) {
+        if (p > p0) {
+#pragma unroll
+          for (int q = 0; q < SF_CHUNK; ++q) {
+            if (p + q < p1) {
+              cc[q] = T.col[p + q];
+              vv[q] = T.val[p + q];
+            }
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < SF_CHUNK; ++q) {
+          if (p + q < p1) {
+            sf_wait(T.flag + cc[q], epoch, err, limit);
+            acc = acc - vv[q] * ld_cg(out + cc[q]);
+          }
+        }
       }
-      st_cg(out + r, acc * T.dinv[r]);
+      st_cg(out + r, acc * dr);
       st_release(T.flag + r, epoch);
     }
   }

@@ -63,7 +63,8 @@ def yle_matrix(lumped_elements, ports, n, w_real, z0, escal_yle):
 
 
 class FrequencyState:
-    """DZ, Yle and the factorised SS at one frequency."""
+    """DZ, Yle and the factorised SS at one frequency (the reference factorises with
+    UMFPACK, FFT_solver_QS_S_type.jl:119; any sparse LU of SS gives the same operator)."""
 
     def __init__(self, w, escalings, incidence_selection, diagonals, Zs_info, lumped_elements,
                  ports, z0):
@@ -85,11 +86,23 @@ class FrequencyState:
         self.invP = sp.diags(1.0 / np.asarray(diagonals["P"]).ravel())
         SS = (self.Yle + A.T @ (self.invZ @ A) + 1j * w * ((Gamma @ self.invP) @ Gamma.T)).tocsc()
         self.SS = SS
-        self.lu = spla.splu(SS, permc_spec="COLAMD", options={"Equil": False})
+        # SS is structurally symmetric: minimum degree on A'+A keeps the fill of COLAMD
+        # and gives shallower elimination trees (fewer dependent levels in the GPU
+        # triangular solves)
+        self.lu = spla.splu(SS, permc_spec="MMD_AT_PLUS_A", options={"Equil": False})
+
+
+class ExportedLU:
+    """Factors already in the exported CSR form (picklable, unlike a SuperLU object)."""
+
+    def __init__(self, parts):
+        self.parts = parts
 
 
 def export_lu(lu):
     """CSR factors and permutations with Pr*SS*Pc = L*U from a SuperLU object."""
+    if isinstance(lu, ExportedLU):
+        return lu.parts
     L = lu.L.tocsr()
     U = lu.U.tocsr()
     L.sort_indices()
@@ -141,4 +154,77 @@ class StatePrefetcher:
         return st
 
     def close(self):
+        self._pool.shutdown(wait=True)
+
+
+class HostFrequency:
+    """Per-frequency host state in picklable form: w, DZ, Yle and the exported LU."""
+
+    def __init__(self, w, DZ, Yle, lu_parts):
+        self.w = w
+        self.DZ = DZ
+        self.Yle = Yle
+        self.lu = ExportedLU(lu_parts)
+
+
+_worker_static = None
+
+
+def _worker_init(static):
+    global _worker_static
+    _worker_static = static
+
+
+def _worker_state(w):
+    fs = FrequencyState(w, *_worker_static)
+    return HostFrequency(w, fs.DZ, fs.Yle, export_lu(fs.lu))
+
+
+class FrequencyPool:
+    """Frequency-loop pipelining across processes: spawned workers build the host
+    states (Yle, SuperLU factorisation, exported factors) of the next `lookahead`
+    frequencies of the sequence while the GPU solves the current one. SuperLU holds
+    the GIL for its allocations, so threads would serialise; processes do not.
+
+    static: (escalings, incidence_selection, diagonals, Zs_info, lumped_elements,
+    ports, z0), sent to each worker once; w_of(k) the angular frequency of key k."""
+
+    def __init__(self, static, w_of, order, workers=4, lookahead=4, keep=True):
+        import multiprocessing
+        from concurrent.futures import ProcessPoolExecutor
+        self._pool = ProcessPoolExecutor(max_workers=workers,
+                                         mp_context=multiprocessing.get_context("spawn"),
+                                         initializer=_worker_init, initargs=(static,))
+        self._w_of = w_of
+        self._order = list(order)
+        self._pos = 0
+        self._ahead = max(1, lookahead)
+        self._pending = {}
+        self._done = {}
+        self._keep = keep
+
+    def _submit(self, k):
+        if k not in self._done and k not in self._pending:
+            self._pending[k] = self._pool.submit(_worker_state, self._w_of(k))
+
+    def get(self, k):
+        while self._pos < len(self._order) and self._order[self._pos] != k:
+            self._pos += 1
+        for nxt in self._order[self._pos:self._pos + 1 + self._ahead]:
+            self._submit(nxt)
+        if k in self._done:
+            st = self._done[k]
+        else:
+            self._submit(k)
+            st = self._pending.pop(k).result()
+        if self._keep:
+            self._done[k] = st
+        self._pos += 1
+        for nxt in self._order[self._pos:self._pos + self._ahead]:
+            self._submit(nxt)
+        return st
+
+    def close(self):
+        for f in self._pending.values():
+            f.cancel()
         self._pool.shutdown(wait=True)

@@ -60,6 +60,8 @@ class GpuOperator:
 
     def __init__(self, incidence_selection, expansions, diagP, grid=None, device=0):
         self.L = _lib.load()
+        self._init_args = (incidence_selection, expansions, diagP, grid, device)
+        self._rows = None
         h = ctypes.c_void_p()
         rc = self.L.peec_ctx_create(ctypes.byref(h), device)
         if rc != 0:
@@ -128,6 +130,7 @@ class GpuOperator:
             keep.append(r)
             arr[i] = r.ctypes.data
         _lib.check(self.h, self.L.peec_set_rows(self.h, arr))
+        self._rows = {k: v for k, v in rows.items()}
 
     def fill(self, origin, sx, sy, sz, escal_Lp, escal_P, return_rows=False):
         """GPU fill of the nine rows and their spectra."""
@@ -137,14 +140,27 @@ class GpuOperator:
         arr = (ctypes.c_void_p * 9)()
         for i, k in enumerate(ROW_KEYS):
             n = int(np.prod(dims[k]))
-            if return_rows and n > 0:
+            if n > 0:
                 outs[k] = np.empty(n)
                 arr[i] = outs[k].ctypes.data
             else:
                 arr[i] = None
         _lib.check(self.h, self.L.peec_fill(self.h, _lib.ptr(o), sx, sy, sz, escal_Lp, escal_P,
-                                            arr if return_rows else None))
+                                            arr))
+        self._rows = outs  # kept for clone()
         return outs if return_rows else None
+
+    def clone(self):
+        """A second context on the same device with the same topology and circulant
+        rows: its own CUDA stream and workspaces, so several port solves of one
+        frequency run concurrently (one context per port, each driven from its own
+        host thread). The frequency state is set per context."""
+        if self._rows is None:
+            raise RuntimeError("clone() needs the generating rows: call fill or set_rows first")
+        inc, exp, dP, grid, dev = self._init_args
+        c = GpuOperator(inc, exp, dP, grid=grid, device=dev)
+        c.set_rows(self._rows)
+        return c
 
     # -- frequency ------------------------------------------------------------------
     def set_frequency(self, w, DZ, Yle, lu, key=None):
@@ -234,6 +250,11 @@ class GpuOperator:
             return x, 99, 0.0, [it[0], it[1]], np.zeros(1)
         _lib.check(self.h, rc)
         return x, flag.value, relres.value, [it[0], it[1]], resvec[:nres.value].copy()
+
+    def set_residual_precision(self, precision):
+        """Arithmetic of the refinement residuals of solve_mixed: PREC_FF (float-float,
+        default) or PREC_FP64."""
+        _lib.check(self.h, self.L.peec_set_residual_precision(self.h, int(precision)))
 
     def solve_mixed(self, b, x0, tol, inner_tol=1e-7, inner_maxit=100, max_outer=8):
         b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())

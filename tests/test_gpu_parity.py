@@ -90,6 +90,23 @@ def test_matvec_fp64(case):
         assert e < max(1e-10, 20 * noise), (case["name"], k, e, noise)
 
 
+def test_matvec_ff(case):
+    """Float-float convolutions (the refinement residual operator) meet the FP64 gate:
+    within max(1e-10, 20 x the problem's rounding noise) of the oracle, and within
+    1e-11 of the GPU's own FP64 operator."""
+    rng = np.random.default_rng(5)
+    N = case["op"].N
+    for k in range(len(case["freqs"])):
+        w, fs = _freq(case, k)
+        x = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+        y_ref = _oracle_mv(case, w, fs)(x)
+        noise = _rel(_single_solve_oracle(case, w, fs)(x), y_ref)
+        y_ff = case["op"].matvec(x, 2)
+        y_64 = case["op"].matvec(x, 0)
+        assert _rel(y_ff, y_ref) < max(1e-10, 20 * noise), (case["name"], k)
+        assert _rel(y_ff, y_64) < max(1e-11, 20 * noise), (case["name"], k, _rel(y_ff, y_64))
+
+
 def test_matvec_fp32(case):
     w, fs = _freq(case)
     rng = np.random.default_rng(4)
@@ -138,13 +155,22 @@ def test_gmres_restarted(case):
     assert _rel(x, x_ref) < 1e-9
 
 
-def test_mixed_solve(case):
+@pytest.mark.parametrize("resid", ["ff", "fp64"])
+def test_mixed_solve(case, resid):
+    from solver_gb300 import _lib
     w, fs = _freq(case)
     tn = case["op"].port_rhs(*case["ports"]["port_nodes"][0], case["esc"]["Is"])
     x_ref = O.gmres_custom(tn, False, 1e-12, 200, None, _oracle_mv(case, w, fs))[0]
-    x, flag, relres, outer, inner = case["op"].solve_mixed(tn, None, 1e-8)
+    case["op"].set_residual_precision(_lib.PREC_FF if resid == "ff" else _lib.PREC_FP64)
+    try:
+        x, flag, relres, outer, inner = case["op"].solve_mixed(tn, None, 1e-8)
+    finally:
+        case["op"].set_residual_precision(_lib.PREC_FF)
     assert flag == 0 and relres <= 1e-8
-    # the FP64 residual check bounds the error by the preconditioned condition number
+    # the oracle's own FP64 residual of the returned solution
+    r = tn - _oracle_mv(case, w, fs)(x)
+    assert np.linalg.norm(r) <= 1.01e-8 * np.linalg.norm(tn)
+    # the residual check bounds the error by the preconditioned condition number
     assert _rel(x, x_ref) < 1e-6
 
 
@@ -265,6 +291,7 @@ def test_matvec_large_tiles():
         y_ref = _oracle_mv(c, w, fs)(x)
         noise = _rel(_single_solve_oracle(c, w, fs)(x), y_ref)
         assert _rel(op.matvec(x, 0), y_ref) < max(1e-10, 20 * noise)
+        assert _rel(op.matvec(x, 2), y_ref) < max(1e-10, 20 * noise)
         assert _rel(op.matvec(x, 1), y_ref) < 2e-5
     finally:
         op.close()
