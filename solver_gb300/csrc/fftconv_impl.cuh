@@ -14,6 +14,9 @@
 namespace peec {
 
 constexpr int TPB = 256;
+// z passes: 128 threads, so that with Lz = 128 every phase splits evenly (first and
+// last groups 3 x 16 columns x 8 pencils, fused step 16 x 16) and four CTAs share an SM
+constexpr int ZTPB = 128;
 
 // --------------------------------------------------------------------------- x passes
 // CTA: TY = 16 consecutive y rows of one z plane. Tile element (pos, yy) at
@@ -425,7 +428,7 @@ __device__ __forceinline__ void z3_fused(cx<R>* buf, size_t tsz, const AxPlan& p
 }
 
 template <typename R>
-__global__ void __launch_bounds__(TPB, 2) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>* T2, int nz0, int nz1,
+__global__ void __launch_bounds__(ZTPB, 4) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>* T2, int nz0, int nz1,
                                                 int nz2, PSpec S, int Lx, int Ly, AxPlan p,
                                                 const cx<R>* __restrict__ twm, int twmax) {
   extern __shared__ unsigned char smem_raw[];
@@ -525,7 +528,7 @@ __device__ __forceinline__ void z1_fused(cx<R>* buf, const AxPlan& p, int ncols,
 }
 
 template <typename R>
-__global__ void __launch_bounds__(TPB) k_zconv1(cx<R>* T0, int nz0, const void* __restrict__ s00,
+__global__ void __launch_bounds__(ZTPB, 4) k_zconv1(cx<R>* T0, int nz0, const void* __restrict__ s00,
                                                 int Lx, int Ly, AxPlan p,
                                                 const cx<R>* __restrict__ twm, int twmax) {
   extern __shared__ unsigned char smem_raw[];
@@ -630,7 +633,7 @@ struct Launch {
     const size_t sm = sizeof(cx<R>) * (Lz + 3 * ((size_t)Lz << LTX));
     CTX_CHECK(smem_optin(k_zconv3<R>, sm));
     dim3 g((F[0].L[0] + TX - 1) / TX, F[0].L[1]);
-    k_zconv3<R><<<g, TPB, sm, st>>>(buf(F[0]), buf(F[1]), buf(F[2]), F[0].dims[2], F[1].dims[2],
+    k_zconv3<R><<<g, ZTPB, sm, st>>>(buf(F[0]), buf(F[1]), buf(F[2]), F[0].dims[2], F[1].dims[2],
                                     F[2].dims[2], S, F[0].L[0], F[0].L[1],
                                     Plans<R>::z3(F[0].logL[2]), tw, twmax);
     return 0;
@@ -640,7 +643,7 @@ struct Launch {
     const size_t sm = sizeof(cx<R>) * (Lz + ((size_t)Lz << LTX));
     CTX_CHECK(smem_optin(k_zconv1<R>, sm));
     dim3 g((f.L[0] + TX - 1) / TX, f.L[1]);
-    k_zconv1<R><<<g, TPB, sm, st>>>(buf(f), f.dims[2], s, f.L[0],
+    k_zconv1<R><<<g, ZTPB, sm, st>>>(buf(f), f.dims[2], s, f.L[0],
                                     f.L[1], Plans<R>::z1(f.logL[2]), tw, twmax);
     return 0;
   }

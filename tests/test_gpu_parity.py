@@ -295,3 +295,32 @@ def test_matvec_large_tiles():
         assert _rel(op.matvec(x, 1), y_ref) < 2e-5
     finally:
         op.close()
+
+
+def test_mixed_crossbar_per_frequency():
+    """The crossbar geometry (20x20x4) in mixed precision (FP32 convolutions in the
+    inner GMRES, float-float residuals) to relative residual 1e-8, at 1 GHz and five
+    log-spaced frequencies 100 MHz - 10 GHz: per-frequency port impedance error
+    against the oracle's FP64 sweep at 1e-12 stays at or below 1e-7."""
+    from solver_gb300 import api
+    freqs = [1e9] + list(np.logspace(8, 10, 5))
+    c = _case(_at(configs.crossbar_20x20x4(), freqs))
+    op = GpuOperator(c["inc"], c["exp"], c["diag"]["P"])
+    try:
+        op.set_rows(c["rows"])
+        c["exp"]["gpu_ctx"] = op
+        nf = len(c["freqs"])
+        ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
+                                     c["diag"], c["ports"], c["z0"], c["le"], c["exp"],
+                                     {"Inner_Iter": 200, "tol": np.full(nf, 1e-12)}, c["Zs"])
+        h = api.CirculantSpectra(op)
+        got = api.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], h, h, c["diag"],
+                                       c["ports"], c["z0"], c["le"], c["exp"],
+                                       {"Inner_Iter": 100, "tol": np.full(nf, 1e-8)}, c["Zs"],
+                                       mode="mixed")
+        assert all(r["flag"] == 0 and r["relres"] <= 1e-8 for r in got["info"])
+        errs = [float(np.max(np.abs(got["Z"][:, :, k] - ref["Z"][:, :, k])) /
+                      np.max(np.abs(ref["Z"][:, :, k]))) for k in range(nf)]
+        assert max(errs) <= 1e-7, dict(zip([float(f) for f in freqs], errs))
+    finally:
+        op.close()
