@@ -152,6 +152,15 @@ int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout, double tol
                      double* relres, int* outer_out, int* inner_total);
 
 /*
+ * Work split of the LU solves inside the operator: rows of connected components of
+ * the factors with at most max_rows rows (0..512, default 512) are solved one
+ * component per warp; all other rows by the synchronisation-free global scheme. Both
+ * give the same results; 0 routes every row through the global scheme. Takes effect
+ * at once. No counterpart in the reference (UMFPACK solves, FFT_solver_QS_S_type.jl:119).
+ */
+int peec_set_lu_component_max(peec_ctx* ctx, int max_rows);
+
+/*
  * Arithmetic of the refinement residuals of peec_solve_mixed: PEEC_PREC_FF (default)
  * or PEEC_PREC_FP64. No counterpart in the reference.
  */

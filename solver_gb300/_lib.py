@@ -25,7 +25,8 @@ EXPORTS = ("peec_version", "peec_ctx_create", "peec_ctx_destroy", "peec_last_err
            "peec_gmres", "peec_solve_mixed", "peec_set_stop_flag", "peec_last_timing",
            "peec_launch_count", "peec_sizes", "peec_stream", "peec_conv_count",
            "peec_conv_info", "peec_profile_matvec", "peec_multidot",
-           "peec_multidot_noalloc", "peec_set_residual_precision")
+           "peec_multidot_noalloc", "peec_set_residual_precision",
+           "peec_set_lu_component_max")
 
 
 PREC_FP64, PREC_FP32, PREC_FF = 0, 1, 2
@@ -62,6 +63,7 @@ def load(build_if_missing: bool = True):
             raise RuntimeError(f"libpeec_gb300.so does not export {name}")
     L.peec_version.restype = ctypes.c_int
     L.peec_set_residual_precision.argtypes = [P, ctypes.c_int]
+    L.peec_set_lu_component_max.argtypes = [P, ctypes.c_int]
     L.peec_ctx_create.argtypes = [ctypes.POINTER(P), ctypes.c_int]
     L.peec_ctx_destroy.argtypes = [P]
     L.peec_ctx_destroy.restype = None

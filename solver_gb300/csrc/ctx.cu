@@ -46,10 +46,10 @@ void launch_final_rows(const c64*, const c64*, const c64*, const c64*, const int
                        const int32_t*, const int32_t*, const double*, int, int, int, c64*,
                        cudaStream_t);
 void launch_perm_gather(const c64*, const int32_t*, const double*, int, c64*, cudaStream_t);
-void launch_sptrsv(const int32_t*, int, int, const SfTri&, const SfTri&, const c64*,
-                   const int32_t*, const double*, c64*, c64*, int*, cudaStream_t);
+int launch_sptrsv(const CompPlan&, const int32_t*, int, int, const SfTri&, const SfTri&,
+                  const c64*, const int32_t*, const double*, c64*, c64*, int*, cudaStream_t);
 int red_blocks(size_t N);
-void launch_multidot(const c64*, size_t, const c64*, size_t, int, c64*, c64*, cudaStream_t);
+int launch_multidot(const c64*, size_t, const c64*, size_t, int, c64*, c64*, cudaStream_t);
 void launch_multiaxpy(const c64*, size_t, const c64*, int, const c64*, int, size_t, c64*, size_t,
                       double*, cudaStream_t);
 void launch_norm2(const c64*, size_t, size_t, double*, double*, cudaStream_t);
@@ -76,6 +76,7 @@ struct LevelTri {  // triangular factor without its diagonal (CSR) and its level
   int64_t nflag = 0;
   std::vector<int32_t> rows;     // rows sorted by level (host)
   std::vector<int> lvl_off;      // offsets into rows per level (host)
+  std::vector<int32_t> hptr, hcol;  // host copy of the structure
 };
 
 struct peec_ctx {
@@ -111,6 +112,13 @@ struct peec_ctx {
   // synchronisation-free triangular solves: claim order (L levels then U levels, each
   // padded with -1 to whole warps), its length, the L part's length, control words
   int32_t* sf_ord = nullptr;
+  // per-warp component solves: component offsets into the row lists, rows in L-level and
+  // U-level order, level segment ends and their per-component offsets, local indices
+  int cmp_n = 0;
+  int comp_max = SF_COMP_MAX;  // largest component solved per warp
+  int32_t *cmp_off = nullptr, *cmp_rowsL = nullptr, *cmp_rowsU = nullptr, *cmp_segL = nullptr,
+          *cmp_segU = nullptr, *cmp_segLoff = nullptr, *cmp_segUoff = nullptr,
+          *cmp_local = nullptr;
   c64 *ir_b = nullptr, *ir_x = nullptr, *ir_r = nullptr, *ir_d = nullptr;  // refinement vectors
   int sf_total = 0, sf_nL = 0;
   int* sf_ctl = nullptr;  // [epoch, claim counter, error flag]
@@ -305,6 +313,9 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   free_tri(ctx->Uf);
   cudaFree(ctx->sf_ord);
   cudaFree(ctx->sf_ctl);
+  for (int32_t* p : {ctx->cmp_off, ctx->cmp_rowsL, ctx->cmp_rowsU, ctx->cmp_segL, ctx->cmp_segU,
+                     ctx->cmp_segLoff, ctx->cmp_segUoff, ctx->cmp_local})
+    cudaFree(p);
   for (c64* p : {ctx->ir_b, ctx->ir_x, ctx->ir_r, ctx->ir_d}) cudaFree(p);
   if (ctx->hx) cudaFreeHost(ctx->hx);
   if (ctx->hy) cudaFreeHost(ctx->hy);
@@ -644,12 +655,114 @@ static int make_tri(peec_ctx* ctx, LevelTri& T, int64_t n, const int64_t* ptr, c
   T.rows = std::move(rows);
   CTX_TRY(upload(&T.ptr, p, ctx->st));
   CTX_TRY(upload(&T.col, c, ctx->st));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));  // the uploads read p and c
+  T.hptr = std::move(p);
+  T.hcol = std::move(c);
   CTX_TRY(upload(&T.val, v, ctx->st));
   CTX_TRY(upload(&T.dinv, dinv, ctx->st));
   // ready flags start below every epoch the solve will use (epochs start at 1)
   CTX_TRY(dalloc(&T.flag, (size_t)n));
   PEEC_CUDA_TRY(cudaMemsetAsync(T.flag, 0, sizeof(int32_t) * n, ctx->st));
   T.nflag = n;
+  return PEEC_OK;
+}
+
+// Work split of the LU solves. The rows of L and U fall into connected components
+// (rows linked by a factor entry); rows of different components never depend on one
+// another. Components of at most SF_COMP_MAX rows are solved by one warp each, level by
+// level with __syncwarp between levels and the component's values in shared memory;
+// the rows of larger components go to the synchronisation-free global scheme.
+static int build_solve_plan(peec_ctx* ctx, int64_t n) {
+  const LevelTri &L = ctx->Lf, &U = ctx->Uf;
+  // union-find over the factor entries
+  std::vector<int32_t> parent(n);
+  for (int64_t r = 0; r < n; ++r) parent[r] = (int32_t)r;
+  auto find = [&](int32_t a) {
+    while (parent[a] != a) {
+      parent[a] = parent[parent[a]];
+      a = parent[a];
+    }
+    return a;
+  };
+  for (const LevelTri* T : {&L, &U})
+    for (int64_t r = 0; r < n; ++r)
+      for (int32_t q = T->hptr[r]; q < T->hptr[r + 1]; ++q) {
+        const int32_t a = find((int32_t)r), b = find(T->hcol[q]);
+        if (a != b) parent[std::max(a, b)] = std::min(a, b);
+      }
+  std::vector<int32_t> comp(n), csize(n, 0);
+  for (int64_t r = 0; r < n; ++r) {
+    comp[r] = find((int32_t)r);
+    csize[comp[r]]++;
+  }
+  // per-row levels
+  std::vector<int32_t> lvL(n), lvU(n);
+  for (size_t l = 0; l + 1 < L.lvl_off.size(); ++l)
+    for (int q = L.lvl_off[l]; q < L.lvl_off[l + 1]; ++q) lvL[L.rows[q]] = (int32_t)l;
+  for (size_t l = 0; l + 1 < U.lvl_off.size(); ++l)
+    for (int q = U.lvl_off[l]; q < U.lvl_off[l + 1]; ++q) lvU[U.rows[q]] = (int32_t)l;
+  // small components, largest first (they have the longest chains)
+  std::vector<int32_t> roots;
+  for (int64_t r = 0; r < n; ++r)
+    if (comp[r] == r && csize[r] <= ctx->comp_max) roots.push_back((int32_t)r);
+  std::stable_sort(roots.begin(), roots.end(),
+                   [&](int32_t a, int32_t b) { return csize[a] > csize[b]; });
+  std::vector<int32_t> cidx(n, -1);
+  for (size_t i = 0; i < roots.size(); ++i) cidx[roots[i]] = (int32_t)i;
+  const size_t nc = roots.size();
+  std::vector<int32_t> coff(nc + 1, 0);
+  for (size_t i = 0; i < nc; ++i) coff[i + 1] = coff[i] + csize[roots[i]];
+  std::vector<int32_t> rowsL(coff[nc]), fill(coff.begin(), coff.end() - 1);
+  for (int64_t r = 0; r < n; ++r) {
+    const int32_t ci = cidx[comp[r]];
+    if (ci >= 0) rowsL[fill[ci]++] = (int32_t)r;
+  }
+  std::vector<int32_t> rowsU(rowsL), local(n, -1), segL, segU, segLoff(nc + 1, 0),
+      segUoff(nc + 1, 0);
+  for (size_t ci = 0; ci < nc; ++ci) {
+    const auto b = rowsL.begin() + coff[ci], e = rowsL.begin() + coff[ci + 1];
+    std::stable_sort(b, e, [&](int32_t x, int32_t y) { return lvL[x] < lvL[y]; });
+    // local index of a row = its position in the L order of its component
+    for (int32_t q = coff[ci]; q < coff[ci + 1]; ++q) local[rowsL[q]] = q - coff[ci];
+    for (int32_t q = coff[ci]; q < coff[ci + 1]; ++q)
+      if (q + 1 == coff[ci + 1] || lvL[rowsL[q + 1]] != lvL[rowsL[q]]) segL.push_back(q + 1);
+    segLoff[ci + 1] = (int32_t)segL.size();
+    const auto bu = rowsU.begin() + coff[ci], eu = rowsU.begin() + coff[ci + 1];
+    std::stable_sort(bu, eu, [&](int32_t x, int32_t y) { return lvU[x] < lvU[y]; });
+    for (int32_t q = coff[ci]; q < coff[ci + 1]; ++q)
+      if (q + 1 == coff[ci + 1] || lvU[rowsU[q + 1]] != lvU[rowsU[q]]) segU.push_back(q + 1);
+    segUoff[ci + 1] = (int32_t)segU.size();
+  }
+  ctx->cmp_n = (int)nc;
+  CTX_TRY(upload(&ctx->cmp_off, coff, ctx->st));
+  CTX_TRY(upload(&ctx->cmp_rowsL, rowsL, ctx->st));
+  CTX_TRY(upload(&ctx->cmp_rowsU, rowsU, ctx->st));
+  CTX_TRY(upload(&ctx->cmp_segL, segL, ctx->st));
+  CTX_TRY(upload(&ctx->cmp_segU, segU, ctx->st));
+  CTX_TRY(upload(&ctx->cmp_segLoff, segLoff, ctx->st));
+  CTX_TRY(upload(&ctx->cmp_segUoff, segUoff, ctx->st));
+  CTX_TRY(upload(&ctx->cmp_local, local, ctx->st));
+  // claim order of the global scheme: rows of the large components only
+  std::vector<int32_t> ord;
+  for (const LevelTri* T : {&L, &U}) {
+    for (size_t l = 0; l + 1 < T->lvl_off.size(); ++l) {
+      const size_t before = ord.size();
+      for (int q = T->lvl_off[l]; q < T->lvl_off[l + 1]; ++q)
+        if (cidx[comp[T->rows[q]]] < 0) ord.push_back(T->rows[q]);
+      if (ord.size() != before)
+        while (ord.size() % 32) ord.push_back(-1);
+    }
+    if (T == &L) ctx->sf_nL = (int)ord.size();
+  }
+  if (ord.size() > (size_t)INT32_MAX - 64) return bad(ctx, PEEC_ERR_UNSUPPORTED, "LU too large");
+  ctx->sf_total = (int)ord.size();
+  if (ord.empty()) ord.push_back(-1);
+  CTX_TRY(upload(&ctx->sf_ord, ord, ctx->st));
+  if (!ctx->sf_ctl) {
+    CTX_TRY(dalloc(&ctx->sf_ctl, 4));
+    PEEC_CUDA_TRY(cudaMemsetAsync(ctx->sf_ctl, 0, sizeof(int) * 4, ctx->st));
+  }
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return PEEC_OK;
 }
 
@@ -721,24 +834,7 @@ extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int
   }
   CTX_TRY(make_tri(ctx, ctx->Lf, n, L_ptr, L_col, L_val, true));
   CTX_TRY(make_tri(ctx, ctx->Uf, n, U_ptr, U_col, U_val, false));
-  {
-    std::vector<int32_t> ord;
-    ord.reserve(2 * n + 64 * (ctx->Lf.lvl_off.size() + ctx->Uf.lvl_off.size()));
-    for (const LevelTri* T : {&ctx->Lf, &ctx->Uf}) {
-      for (size_t l = 0; l + 1 < T->lvl_off.size(); ++l) {
-        for (int q = T->lvl_off[l]; q < T->lvl_off[l + 1]; ++q) ord.push_back(T->rows[q]);
-        while (ord.size() % 32) ord.push_back(-1);
-      }
-      if (T == &ctx->Lf) ctx->sf_nL = (int)ord.size();
-    }
-    if (ord.size() > (size_t)INT32_MAX - 64) return bad(ctx, PEEC_ERR_UNSUPPORTED, "LU too large");
-    ctx->sf_total = (int)ord.size();
-    CTX_TRY(upload(&ctx->sf_ord, ord, ctx->st));
-    if (!ctx->sf_ctl) {
-      CTX_TRY(dalloc(&ctx->sf_ctl, 4));
-      PEEC_CUDA_TRY(cudaMemsetAsync(ctx->sf_ctl, 0, sizeof(int) * 4, ctx->st));
-    }
-  }
+  CTX_TRY(build_solve_plan(ctx, n));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->have_freq = true;
   return PEEC_OK;
@@ -751,11 +847,15 @@ extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int
 static void lu_solve(peec_ctx* ctx, const c64* b, c64* x) {
   const int n = (int)ctx->n;
   const LevelTri &L = ctx->Lf, &U = ctx->Uf;
-  launch_sptrsv(ctx->sf_ord, ctx->sf_nL, ctx->sf_total,
-                SfTri{L.ptr, L.col, L.val, L.dinv, L.flag}, SfTri{U.ptr, U.col, U.val, U.dinv, U.flag},
-                b, ctx->g_in, ctx->lu_rs, ctx->lutmp, ctx->lutmp2, ctx->sf_ctl, ctx->st);
+  const CompPlan C{ctx->cmp_off,    ctx->cmp_rowsL,   ctx->cmp_rowsU,   ctx->cmp_segL,
+                   ctx->cmp_segU,   ctx->cmp_segLoff, ctx->cmp_segUoff, ctx->cmp_local,
+                   ctx->cmp_n};
+  ctx->launches += launch_sptrsv(
+      C, ctx->sf_ord, ctx->sf_nL, ctx->sf_total, SfTri{L.ptr, L.col, L.val, L.dinv, L.flag},
+      SfTri{U.ptr, U.col, U.val, U.dinv, U.flag}, b, ctx->g_in, ctx->lu_rs, ctx->lutmp,
+      ctx->lutmp2, ctx->sf_ctl, ctx->st);
   launch_perm_gather(ctx->lutmp2, ctx->g_out, nullptr, n, x, ctx->st);
-  ctx->launches += 3;
+  ctx->launches += 1;
 }
 
 // A triangular-solve wait that ran into its limit leaves an error word on the device;
@@ -928,9 +1028,8 @@ extern "C" int peec_multidot(peec_ctx* ctx, const void* U, int64_t ldu, const vo
     PEEC_CUDA_TRY(cudaMalloc(&ctx->mdpart, need * sizeof(c64)));
     ctx->mdcap = need;
   }
-  launch_multidot((const c64*)U, (size_t)ldu, (const c64*)v, (size_t)N, k, ctx->mdpart, (c64*)out,
-                  ctx->st);
-  ctx->launches += 2;
+  ctx->launches += launch_multidot((const c64*)U, (size_t)ldu, (const c64*)v, (size_t)N, k,
+                                   ctx->mdpart, (c64*)out, ctx->st);
   PEEC_CUDA_TRY(cudaGetLastError());
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return PEEC_OK;
@@ -1203,12 +1302,12 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
       double alpha2 = 0.0;
       std::vector<cd> vh;
       {
-        launch_multidot(ctx->U, N, add, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
+        ctx->launches += launch_multidot(ctx->U, N, add, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
         launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dcoef, 1, ctx->st);  // c = T^H z
         launch_multiaxpy(ctx->U, N, add, 0, ctx->dcoef, k, N, v, (size_t)initer, ctx->dred,
                          ctx->st);
         launch_sum_parts(ctx->dred, red_blocks(N), ctx->dscal, ctx->st);
-        ctx->launches += 5;
+        ctx->launches += 3;
         cudaMemcpyAsync(ctx->hscal, ctx->dscal, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
         vh = g.from_dev(v, headlen);
         alpha2 = ctx->hscal[0];
@@ -1229,9 +1328,10 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
             Utop[(size_t)initer * ld + i] =
                 i < initer ? cd(0) : (i == initer ? (vh[i] + a) * sc : vh[i] * sc);
           // T(0:k, k) = -2 T(0:k,0:k) (U(:,0:k)^H u_k), T(k,k) = 2 -- all on the device
-          launch_multidot(ctx->U, N, unew, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
+          ctx->launches +=
+              launch_multidot(ctx->U, N, unew, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
           launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dT + (size_t)k * ldT, 2, ctx->st);
-          ctx->launches += 4;
+          ctx->launches += 2;
           for (int i = initer + 1; i <= inner; ++i) vs[i] = 0;
           vs[initer] = -a;
         }
@@ -1472,5 +1572,16 @@ extern "C" int peec_set_residual_precision(peec_ctx* ctx, int precision) {
   if (precision != PEEC_PREC_FP64 && precision != PEEC_PREC_FF)
     return bad(ctx, PEEC_ERR_BADARG, "residual precision must be PEEC_PREC_FP64 or PEEC_PREC_FF");
   ctx->resid_prec = precision;
+  return PEEC_OK;
+}
+
+extern "C" int peec_set_lu_component_max(peec_ctx* ctx, int max_rows) {
+  if (!ctx) return badarg(__func__);
+  if (max_rows < 0 || max_rows > SF_COMP_MAX)
+    return bad(ctx, PEEC_ERR_BADARG, "component size limit outside 0.." + std::to_string(SF_COMP_MAX));
+  cudaSetDevice(ctx->dev);
+  drop_graphs(ctx);
+  ctx->comp_max = max_rows;
+  if (ctx->have_freq) CTX_TRY(build_solve_plan(ctx, ctx->n));
   return PEEC_OK;
 }

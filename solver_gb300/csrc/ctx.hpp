@@ -25,6 +25,21 @@ struct SfTri {
 };
 constexpr int SF_TPB = 128;
 
+// components of the LU factors solved by one warp each (rows at most SF_COMP_MAX)
+constexpr int SF_COMP_MAX = 512;
+constexpr int SFC_TPB = 128;
+struct CompPlan {
+  const int32_t* off;     // ncomp + 1 offsets into the row lists
+  const int32_t* rowsL;   // rows of each component in L-level order
+  const int32_t* rowsU;   // same rows in U-level order
+  const int32_t* segL;    // end offset of each L level segment
+  const int32_t* segU;    // end offset of each U level segment
+  const int32_t* segLoff; // ncomp + 1 offsets into segL
+  const int32_t* segUoff; // ncomp + 1 offsets into segU
+  const int32_t* local;   // row -> position in its component's L order
+  int n;
+};
+
 #define CTX_CHECK(expr)      \
   do {                       \
     int _r = (expr);         \

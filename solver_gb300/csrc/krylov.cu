@@ -22,31 +22,34 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// partial[blk][c] (complex) = sum over the CTA's rows of conj(U[i,c0+c]) * v[i]
+// partial[c0+c][blk] (complex) = sum over the CTA's rows of conj(U[i,c0+c]) * v[i],
+// c < NC: the tile's columns are a template parameter, so loads, products and the
+// shuffle reductions are exactly the ones needed; each thread walks at least eight rows
+template <int NC>
 __global__ void __launch_bounds__(RED_TPB) k_multidot(const c64* __restrict__ U, size_t ldu,
                                                       const c64* __restrict__ v, size_t N,
-                                                      int k, c64* partial) {
-  __shared__ double red[RED_TPB / 32][2 * KB];
-  const int c0 = blockIdx.y * KB;
-  const int nc = min(KB, k - c0);
-  double ar[KB], ai[KB];
+                                                      int c0, c64* partial) {
+  __shared__ double red[RED_TPB / 32][2 * NC];
+  c0 += blockIdx.y * NC;
+  const c64* __restrict__ Uc = U + (size_t)c0 * ldu;
+  double ar[NC], ai[NC];
 #pragma unroll
-  for (int c = 0; c < KB; ++c) ar[c] = ai[c] = 0.0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
-       i += (size_t)gridDim.x * blockDim.x) {
+  for (int c = 0; c < NC; ++c) ar[c] = ai[c] = 0.0;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
+    c64 u[NC];
     const c64 x = v[i];
 #pragma unroll
-    for (int c = 0; c < KB; ++c) {
-      if (c < nc) {
-        const c64 u = U[(size_t)(c0 + c) * ldu + i];
-        ar[c] += u.x * x.x + u.y * x.y;
-        ai[c] += u.x * x.y - u.y * x.x;
-      }
+    for (int c = 0; c < NC; ++c) u[c] = Uc[(size_t)c * ldu + i];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      ar[c] += u[c].x * x.x + u[c].y * x.y;
+      ai[c] += u[c].x * x.y - u[c].y * x.x;
     }
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-  for (int c = 0; c < KB; ++c) {
+  for (int c = 0; c < NC; ++c) {
     const double sr = warp_sum(ar[c]), si = warp_sum(ai[c]);
     if (lane == 0) {
       red[wid][2 * c] = sr;
@@ -54,14 +57,12 @@ __global__ void __launch_bounds__(RED_TPB) k_multidot(const c64* __restrict__ U,
     }
   }
   __syncthreads();
-  if (threadIdx.x < 2 * KB) {
+  if (threadIdx.x < 2 * NC) {
     double s = 0.0;
     for (int w = 0; w < RED_TPB / 32; ++w) s += red[w][threadIdx.x];
     const int c = threadIdx.x >> 1;
-    if (c < nc) {
-      double* p = reinterpret_cast<double*>(partial + (size_t)(c0 + c) * gridDim.x + blockIdx.x);
-      p[threadIdx.x & 1] = s;
-    }
+    double* p = reinterpret_cast<double*>(partial + (size_t)(c0 + c) * gridDim.x + blockIdx.x);
+    p[threadIdx.x & 1] = s;
   }
 }
 
@@ -97,7 +98,16 @@ __global__ void __launch_bounds__(RED_TPB) k_multiaxpy(const c64* __restrict__ U
     c64 x;
     if (base) x = base[i];
     else x = mk<double>(i == (size_t)unit ? 1.0 : 0.0, 0.0);
-    for (int c = 0; c < k; ++c) x = x - U[(size_t)c * ldu + i] * sc[c];
+    // columns in chunks of eight: the chunk's loads are issued before its products
+    for (int c0 = 0; c0 < k; c0 += 8) {
+      c64 u[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (c0 + q < k) u[q] = U[(size_t)(c0 + q) * ldu + i];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (c0 + q < k) x = x - u[q] * sc[c0 + q];
+    }
     out[i] = x;
     if (i >= tail0) acc += x.x * x.x + x.y * x.y;
   }
@@ -185,7 +195,15 @@ __global__ void k_xupdate(const c64* __restrict__ x, const c64* __restrict__ U, 
        i += (size_t)gridDim.x * blockDim.x) {
     c64 v = x[i];
     if (i < (size_t)k) v = v + sc2[k + i];
-    for (int c = 0; c < k; ++c) v = v - U[(size_t)c * ldu + i] * sc2[c];
+    for (int c0 = 0; c0 < k; c0 += 8) {
+      c64 u[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (c0 + q < k) u[q] = U[(size_t)(c0 + q) * ldu + i];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (c0 + q < k) v = v - u[q] * sc2[c0 + q];
+    }
     out[i] = v;
   }
 }
@@ -231,21 +249,34 @@ static inline unsigned g_stream(size_t n) {
 
 int red_blocks(size_t N) { return (int)g_stream(N); }
 
-// multi-dot CTAs per column tile: at least 4 rows per thread, at most 2 CTAs per SM
+// multi-dot CTAs per column tile: at least 8 rows per thread, at most 2 CTAs per SM
 static inline unsigned md_blocks(size_t N) {
-  size_t g = (N + 4 * RED_TPB - 1) / (4 * RED_TPB);
+  size_t g = (N + 8 * RED_TPB - 1) / (8 * RED_TPB);
   if (g > MD_BLOCKS_MAX) g = MD_BLOCKS_MAX;
   if (g < 1) g = 1;
   return (unsigned)g;
 }
 
-void launch_multidot(const c64* U, size_t ldu, const c64* v, size_t N, int k, c64* partial,
-                     c64* out, cudaStream_t st) {
-  if (k <= 0) return;
+// returns the number of kernels launched
+int launch_multidot(const c64* U, size_t ldu, const c64* v, size_t N, int k, c64* partial,
+                    c64* out, cudaStream_t st) {
+  if (k <= 0) return 0;
   const unsigned nb = md_blocks(N);
-  dim3 g(nb, (k + KB - 1) / KB);
-  k_multidot<<<g, RED_TPB, 0, st>>>(U, ldu, v, N, k, partial);
+  const int full = k / KB, rem = k - full * KB;
+  if (full) k_multidot<KB><<<dim3(nb, full), RED_TPB, 0, st>>>(U, ldu, v, N, 0, partial);
+  const int c0 = full * KB;
+  switch (rem) {
+    case 1: k_multidot<1><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 2: k_multidot<2><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 3: k_multidot<3><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 4: k_multidot<4><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 5: k_multidot<5><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 6: k_multidot<6><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 7: k_multidot<7><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    default: break;
+  }
   k_reduce_cols<<<(k + 7) / 8, 256, 0, st>>>(partial, nb, k, out);
+  return (full ? 1 : 0) + (rem ? 1 : 0) + 1;
 }
 
 void launch_multiaxpy(const c64* U, size_t ldu, const c64* base, int unit, const c64* coef,

@@ -140,10 +140,64 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// ctl[0] epoch, ctl[1] claim counter, ctl[2] error flag
+// ctl[0] epoch, ctl[1] row claim counter, ctl[2] error flag, ctl[3] component claim counter
 __global__ void k_sptrsv_begin(int* ctl) {
   ctl[0] += 1;
   ctl[1] = 0;
+  ctl[3] = 0;
+}
+
+// One warp per small component (rows linked by factor entries, at most SF_COMP_MAX):
+// L levels then U levels of the component, rows of a level spread over the lanes,
+// __syncwarp between levels, the component's values in shared memory. Per row the
+// arithmetic is the same as in k_sptrsv (right-hand side, entries subtracted in row
+// order, times the inverse diagonal). The U pass works in place: a U row reads its own
+// L value and the U values of rows of earlier U levels.
+__global__ void __launch_bounds__(SFC_TPB) k_sptrsv_comp(CompPlan C, SfTri L, SfTri U,
+                                                         const c64* __restrict__ b,
+                                                         const int32_t* __restrict__ g_in,
+                                                         const double* __restrict__ rs, c64* z,
+                                                         int* ctl) {
+  __shared__ c64 xs_all[SFC_TPB / 32][SF_COMP_MAX];
+  const int lane = threadIdx.x & 31;
+  c64* xs = xs_all[threadIdx.x >> 5];
+  for (;;) {
+    int ci = 0;
+    if (lane == 0) ci = atomicAdd(ctl + 3, 1);
+    ci = __shfl_sync(0xffffffffu, ci, 0);
+    if (ci >= C.n) break;
+    const int base = C.off[ci], end = C.off[ci + 1];
+    int prev = base;
+    for (int s = C.segLoff[ci]; s < C.segLoff[ci + 1]; ++s) {
+      const int se = C.segL[s];
+      for (int q = prev + lane; q < se; q += 32) {
+        const int r = C.rowsL[q];
+        const int j = g_in[r];
+        c64 acc = rs ? cscale(b[j], rs[j]) : b[j];
+        for (int p = L.ptr[r]; p < L.ptr[r + 1]; ++p)
+          acc = acc - L.val[p] * xs[C.local[L.col[p]]];
+        xs[q - base] = acc * L.dinv[r];
+      }
+      __syncwarp();
+      prev = se;
+    }
+    prev = base;
+    for (int s = C.segUoff[ci]; s < C.segUoff[ci + 1]; ++s) {
+      const int se = C.segU[s];
+      for (int q = prev + lane; q < se; q += 32) {
+        const int r = C.rowsU[q];
+        const int lr = C.local[r];
+        c64 acc = xs[lr];
+        for (int p = U.ptr[r]; p < U.ptr[r + 1]; ++p)
+          acc = acc - U.val[p] * xs[C.local[U.col[p]]];
+        xs[lr] = acc * U.dinv[r];
+      }
+      __syncwarp();
+      prev = se;
+    }
+    for (int q = base + lane; q < end; q += 32) z[C.rowsL[q]] = xs[q - base];
+    __syncwarp();
+  }
 }
 
 __device__ __forceinline__ void sf_wait(const int* f, int epoch, int* err, int limit) {
@@ -265,10 +319,20 @@ void launch_perm_gather(const c64* b, const int32_t* perm, const double* rs, int
 void launch_perm_scatter(const c64* z, const int32_t* perm, int n, c64* out, cudaStream_t st) {
   k_perm_scatter<<<grid_for(n), 256, 0, st>>>(z, perm, n, out);
 }
-void launch_sptrsv(const int32_t* ord, int nL, int total, const SfTri& L, const SfTri& U,
-                   const c64* b, const int32_t* g_in, const double* rs, c64* y, c64* z,
-                   int* ctl, cudaStream_t st) {
+// returns the number of kernels launched
+int launch_sptrsv(const CompPlan& C, const int32_t* ord, int nL, int total, const SfTri& L,
+                  const SfTri& U, const c64* b, const int32_t* g_in, const double* rs, c64* y,
+                  c64* z, int* ctl, cudaStream_t st) {
+  int launches = 1;
   k_sptrsv_begin<<<1, 1, 0, st>>>(ctl);
+  if (C.n > 0) {
+    int cb = (C.n + SFC_TPB / 32 - 1) / (SFC_TPB / 32);
+    if (cb > 152 * 8) cb = 152 * 8;
+    k_sptrsv_comp<<<cb, SFC_TPB, 0, st>>>(C, L, U, b, g_in, rs, z, ctl);
+    ++launches;
+  }
+  if (total <= 0) return launches;
+  ++launches;
   // enough warps to cover the widest levels; later blocks simply claim later rows
   const int warps = (total + 31) / 32;
   int blocks = (warps + SF_TPB / 32 - 1) / (SF_TPB / 32);
@@ -276,6 +340,7 @@ void launch_sptrsv(const int32_t* ord, int nL, int total, const SfTri& L, const 
   if (blocks < 1) blocks = 1;
   k_sptrsv<<<blocks, SF_TPB, 0, st>>>(ord, nL, total, L, U, b, g_in, rs, y, z, ctl,
                                         1 << 20);
+  return launches;
 }
 
 }  // namespace peec

@@ -251,6 +251,11 @@ class GpuOperator:
         _lib.check(self.h, rc)
         return x, flag.value, relres.value, [it[0], it[1]], resvec[:nres.value].copy()
 
+    def set_lu_component_max(self, max_rows):
+        """Rows of LU components up to max_rows (<= 512) are solved one component per
+        warp, the rest by the global synchronisation-free scheme (0: all global)."""
+        _lib.check(self.h, self.L.peec_set_lu_component_max(self.h, int(max_rows)))
+
     def set_residual_precision(self, precision):
         """Arithmetic of the refinement residuals of solve_mixed: PREC_FF (float-float,
         default) or PREC_FP64."""
