@@ -153,10 +153,10 @@ int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout, double tol
 
 /*
  * Work split of the LU solves inside the operator: rows of connected components of
- * the factors with at most max_rows rows (0..512, default 512) are solved one
+ * the factors with at most max_rows rows (0..512, default 0) are solved one
  * component per warp; all other rows by the synchronisation-free global scheme. Both
- * give the same results; 0 routes every row through the global scheme. Takes effect
- * at once. No counterpart in the reference (UMFPACK solves, FFT_solver_QS_S_type.jl:119).
+ * give the same results to rounding; 0 routes every row through the global scheme.
+ * Takes effect at once. No counterpart in the reference (UMFPACK solves, FFT_solver_QS_S_type.jl:119).
  */
 int peec_set_lu_component_max(peec_ctx* ctx, int max_rows);
 

@@ -115,7 +115,7 @@ struct peec_ctx {
   // per-warp component solves: component offsets into the row lists, rows in L-level and
   // U-level order, level segment ends and their per-component offsets, local indices
   int cmp_n = 0;
-  int comp_max = SF_COMP_MAX;  // largest component solved per warp
+  int comp_max = 0;  // largest component solved per warp (0: global scheme only)
   int32_t *cmp_off = nullptr, *cmp_rowsL = nullptr, *cmp_rowsU = nullptr, *cmp_segL = nullptr,
           *cmp_segU = nullptr, *cmp_segLoff = nullptr, *cmp_segUoff = nullptr,
           *cmp_local = nullptr;

@@ -253,7 +253,8 @@ class GpuOperator:
 
     def set_lu_component_max(self, max_rows):
         """Rows of LU components up to max_rows (<= 512) are solved one component per
-        warp, the rest by the global synchronisation-free scheme (0: all global)."""
+        warp, the rest by the global synchronisation-free scheme (0, the default: all
+        global)."""
         _lib.check(self.h, self.L.peec_set_lu_component_max(self.h, int(max_rows)))
 
     def set_residual_precision(self, precision):

@@ -114,15 +114,15 @@ def test_lu_solve_paths(case):
     w, fs = _freq(case)
     rng = np.random.default_rng(6)
     x = rng.standard_normal(case["op"].N) + 1j * rng.standard_normal(case["op"].N)
-    y_comp = case["op"].matvec(x, 0)
-    case["op"].set_lu_component_max(0)
+    y_glob = case["op"].matvec(x, 0)
+    case["op"].set_lu_component_max(512)
     try:
-        y_glob = case["op"].matvec(x, 0)
+        y_comp = case["op"].matvec(x, 0)
     finally:
-        case["op"].set_lu_component_max(512)
+        case["op"].set_lu_component_max(0)
     y_ref = _oracle_mv(case, w, fs)(x)
     noise = _rel(_single_solve_oracle(case, w, fs)(x), y_ref)
-    assert _rel(y_comp, y_glob) < max(1e-12, noise)
+    assert _rel(y_comp, y_glob) < max(1e-11, 2 * noise)
     assert _rel(y_comp, y_ref) < max(1e-10, 20 * noise)
     assert _rel(y_glob, y_ref) < max(1e-10, 20 * noise)
 
