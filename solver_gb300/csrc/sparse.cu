@@ -333,10 +333,12 @@ int launch_sptrsv(const CompPlan& C, const int32_t* ord, int nL, int total, cons
   }
   if (total <= 0) return launches;
   ++launches;
-  // enough warps to cover the widest levels; later blocks simply claim later rows
+  // at most two CTAs (eight warps) per SM: warps that wait on earlier rows take issue
+  // slots from kernels of other streams, and more warps do not shorten the chain of
+  // levels (the widest level at 128x128x64 is about 1,400 warp batches)
   const int warps = (total + 31) / 32;
   int blocks = (warps + SF_TPB / 32 - 1) / (SF_TPB / 32);
-  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks > 152 * 2) blocks = 152 * 2;
   if (blocks < 1) blocks = 1;
   k_sptrsv<<<blocks, SF_TPB, 0, st>>>(ord, nL, total, L, U, b, g_in, rs, y, z, ctl,
                                         1 << 20);
