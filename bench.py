@@ -58,8 +58,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=7)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=7,
+                    help="timed FP64-plain points (the first of the mixed run's timed points)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="set up, time the operator applications and exit (for ncu captures)")
     ap.add_argument("--lanes", type=int, default=4,
                     help="concurrent port solves (contexts + host threads), at most the ports")
     ap.add_argument("--inner-tol", type=float, default=1e-7,
@@ -383,7 +386,7 @@ def main():
     # host states (Yle, SuperLU factors) of the next frequencies are built by spawned
     # worker processes while the GPU solves the current one
     from solver_gb300.frequency import FrequencyPool
-    order = [0] + [i % nf for i in range(args.warmup + args.steps)] + list(range(args.fp64_steps))
+    order = [0] + [i % nf for i in range(args.warmup + args.steps)]
     static = (P["esc"], P["inc"], P["diag"], P["Zs"], P["le"], P["ports"], P["z0"])
     nworkers = max(2, min(12, (os.cpu_count() or 4) - 4))
     pf = FrequencyPool(static, lambda k: 2 * np.pi * P["freqs"][k] * P["esc"]["freq"], order,
@@ -398,6 +401,15 @@ def main():
     profff = op.profile_matvec(2, max(3, args.profile_iters // 4))
     b32, b64 = conv_bytes(info, 1), conv_bytes(info, 0)
     peak, peak_kind = load_peaks()
+    if args.profile_only:
+        # operator applications only (a few hundred launches): the command ncu captures run
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "grid": list(P["grid"]), "fp32": prof32,
+                              "fp64": prof64, "ff": profff, "fp32_bytes_by_pass": b32}),
+                  flush=True)
+        pf.close()
+        op.close()
+        return
 
     # -- mixed-precision timed steps ---------------------------------------------------------
     from solver_gb300.api import PortLanes
@@ -420,7 +432,7 @@ def main():
     gpu_ms = 0.0
     h2d = d2h = 0
     work = []
-    l0 = op.launch_count()
+    l0 = sum(o.launch_count() for o in P["lanes"].ops)
     barrier(ws)
     if have_torch:
         torch.cuda.synchronize()
@@ -460,24 +472,31 @@ def main():
     t_wall = time.perf_counter() - t_wall0
     barrier(ws)
     clk = clocks.stop()
-    launches = op.launch_count() - l0
+    launches = sum(o.launch_count() for o in P["lanes"].ops) - l0
     gpu_s = barrier_max(ws, gpu_ms / 1e3)
     wall_s = barrier_max(ws, t_wall)
     value = ws * args.steps / gpu_s
     e2e_v = ws * args.steps / wall_s
 
-    # -- FP64 plain (reference algorithm) on the first frequency points ------------------------
+    # -- FP64 plain (reference algorithm) on the same frequency sequence ---------------------
+    # the warm-up points build the same warm starts untimed; then the first fp64_steps of
+    # the timed mixed points are timed
     V64 = np.zeros_like(Vrest)
     fp64_ms = 0.0
     work64 = []
     S64 = {}
-    for k in range(args.fp64_steps):
-        fs = state(k)
-        t0 = time.perf_counter()
-        S64[k], w64, _, _ = solve_point(P, fs, V64, "fp64", tol)
-        fp64_ms += (time.perf_counter() - t0) * 1e3
-        work64 += w64
-    fp64_v = args.fp64_steps / (fp64_ms / 1e3) if args.fp64_steps else None
+    n64 = min(args.fp64_steps, args.steps)
+    if n64:
+        for i in range(args.warmup):
+            solve_point(P, state(i % nf), V64, "fp64", tol)
+        for i in range(args.warmup, args.warmup + n64):
+            k = i % nf
+            fs = state(k)
+            t0 = time.perf_counter()
+            S64[k], w64, _, _ = solve_point(P, fs, V64, "fp64", tol)
+            fp64_ms += (time.perf_counter() - t0) * 1e3
+            work64 += w64
+    fp64_v = n64 / (fp64_ms / 1e3) if n64 else None
     # mixed vs FP64 port quantities (S) at the frequencies both ran
     errs = []
     for k in S64:
@@ -507,7 +526,7 @@ def main():
                 "host_ms_per_step": {k: v / args.steps for k, v in P["host_ms"].items()}},
         "gpu_launches": int(launches),
         "clocks": clk,
-        "fp64_plain": {"value": fp64_v, "unit": UNIT, "steps": args.fp64_steps,
+        "fp64_plain": {"value": fp64_v, "unit": UNIT, "steps": n64,
                        "mixed_over_fp64": (value / fp64_v) if fp64_v else None,
                        "gmres_iters": [w_["iter"][1] for w_ in work64]},
         "mixed_work": {"outer_mean": float(np.mean([w_["outer"] for w_ in work])),
