@@ -427,7 +427,17 @@ __device__ __forceinline__ void z3_fused(cx<R>* buf, size_t tsz, const AxPlan& p
   }
 }
 
-template <typename R>
+// group size QFIX when the kernel is specialised for it (plans of the common lengths),
+// else the runtime value through qswitch
+template <int QFIX, int CAP, typename F>
+__device__ __forceinline__ void qpick(int q, F&& f) {
+  if constexpr (QFIX > 0) f(qconst<QFIX>{});
+  else qswitch<CAP>(q, f);
+}
+
+// Q0 / QL > 0: instantiation for plans whose first / last groups have those sizes (only
+// that register code is compiled: smaller kernels, fewer registers); 0: any plan
+template <typename R, int Q0 = 0, int QL = 0>
 __global__ void __launch_bounds__(ZTPB, 4) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>* T2, int nz0, int nz1,
                                                 int nz2, PSpec S, int Lx, int Ly, AxPlan p,
                                                 const cx<R>* __restrict__ twm, int twmax) {
@@ -447,13 +457,15 @@ __global__ void __launch_bounds__(ZTPB, 4) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>*
   const size_t sbase = (size_t)ky * Lz * Lx + kx0;
   load_twiddles<R>(W, twm, twmax, Lz);
   __syncthreads();
-  if (p.ng == 1) {
-    qswitch<QCap<R>::Z3>(p.q[0], [&](auto QC) { z3_single<R, decltype(QC)::value>(T0, T1, T2, nz0, nz1, nz2, pl, ncols, S, sbase, (size_t)Lx); });
-    return;
+  if constexpr (Q0 == 0) {
+    if (p.ng == 1) {
+      qswitch<QCap<R>::Z3>(p.q[0], [&](auto QC) { z3_single<R, decltype(QC)::value>(T0, T1, T2, nz0, nz1, nz2, pl, ncols, S, sbase, (size_t)Lx); });
+      return;
+    }
   }
-  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(T0, pl, ncols, nz0, buf, p, W, T0); });
-  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(T1, pl, ncols, nz1, buf + tsz, p, W, T1); });
-  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(T2, pl, ncols, nz2, buf + 2 * tsz, p, W, T2); });
+  qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(T0, pl, ncols, nz0, buf, p, W, T0); });
+  qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(T1, pl, ncols, nz1, buf + tsz, p, W, T1); });
+  qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(T2, pl, ncols, nz2, buf + 2 * tsz, p, W, T2); });
   __syncthreads();
   {
     int s = p.q[0];
@@ -465,7 +477,7 @@ __global__ void __launch_bounds__(ZTPB, 4) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>*
       __syncthreads();
     }
   }
-  qswitch<QCap<R>::Z3>(p.q[p.ng - 1], [&](auto QC) { z3_fused<R, decltype(QC)::value>(buf, tsz, p, ncols, S, sbase, (size_t)Lx); });
+  qpick<QL, QCap<R>::Z3>(p.q[p.ng - 1], [&](auto QC) { z3_fused<R, decltype(QC)::value>(buf, tsz, p, ncols, S, sbase, (size_t)Lx); });
   __syncthreads();
   {
     int s = p.n - p.q[p.ng - 1];
@@ -477,9 +489,9 @@ __global__ void __launch_bounds__(ZTPB, 4) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>*
       __syncthreads();
     }
   }
-  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf, T0, pl, ncols, nz0, p, W); });
-  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf + tsz, T1, pl, ncols, nz1, p, W); });
-  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf + 2 * tsz, T2, pl, ncols, nz2, p, W); });
+  qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf, T0, pl, ncols, nz0, p, W); });
+  qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf + tsz, T1, pl, ncols, nz1, p, W); });
+  qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf + 2 * tsz, T2, pl, ncols, nz2, p, W); });
 }
 
 // one edge family with its real spectrum
@@ -527,7 +539,7 @@ __device__ __forceinline__ void z1_fused(cx<R>* buf, const AxPlan& p, int ncols,
   }
 }
 
-template <typename R>
+template <typename R, int Q0 = 0, int QL = 0>
 __global__ void __launch_bounds__(ZTPB, 4) k_zconv1(cx<R>* T0, int nz0, const void* __restrict__ s00,
                                                 int Lx, int Ly, AxPlan p,
                                                 const cx<R>* __restrict__ twm, int twmax) {
@@ -542,17 +554,19 @@ __global__ void __launch_bounds__(ZTPB, 4) k_zconv1(cx<R>* T0, int nz0, const vo
   const size_t sbase = (size_t)ky * Lz * Lx + kx0;
   load_twiddles<R>(W, twm, twmax, Lz);
   __syncthreads();
-  if (p.ng == 1) {
-    qswitch<QCap<R>::Z1>(p.q[0], [&](auto QC) { z1_single<R, decltype(QC)::value>(Tg, nz0, pl, ncols, s00, sbase, (size_t)Lx); });
-    return;
+  if constexpr (Q0 == 0) {
+    if (p.ng == 1) {
+      qswitch<QCap<R>::Z1>(p.q[0], [&](auto QC) { z1_single<R, decltype(QC)::value>(Tg, nz0, pl, ncols, s00, sbase, (size_t)Lx); });
+      return;
+    }
   }
-  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(Tg, pl, ncols, nz0, buf, p, W, Tg); });
+  qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(Tg, pl, ncols, nz0, buf, p, W, Tg); });
   __syncthreads();
   middle_groups<R, false, LTX>(buf, TX, p, W);
-  qswitch<QCap<R>::Z1>(p.q[p.ng - 1], [&](auto QC) { z1_fused<R, decltype(QC)::value>(buf, p, ncols, s00, sbase, (size_t)Lx); });
+  qpick<QL, QCap<R>::Z1>(p.q[p.ng - 1], [&](auto QC) { z1_fused<R, decltype(QC)::value>(buf, p, ncols, s00, sbase, (size_t)Lx); });
   __syncthreads();
   middle_groups<R, true, LTX>(buf, TX, p, W);
-  qswitch<QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf, Tg, pl, ncols, nz0, p, W); });
+  qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf, Tg, pl, ncols, nz0, p, W); });
 }
 
 // --------------------------------------------------------------------------- host side
@@ -631,20 +645,26 @@ struct Launch {
                     cudaStream_t st) {
     const int Lz = F[0].L[2];
     const size_t sm = sizeof(cx<R>) * (Lz + 3 * ((size_t)Lz << LTX));
-    CTX_CHECK(smem_optin(k_zconv3<R>, sm));
+    const AxPlan p = Plans<R>::z3(F[0].logL[2]);
+    constexpr int QL = QCap<R>::Z3;
+    const bool spec = p.ng >= 2 && p.q[0] == 4 && p.q[p.ng - 1] == QL;
+    auto kern = spec ? k_zconv3<R, 4, QL> : k_zconv3<R, 0, 0>;
+    CTX_CHECK(smem_optin(kern, sm));
     dim3 g((F[0].L[0] + TX - 1) / TX, F[0].L[1]);
-    k_zconv3<R><<<g, ZTPB, sm, st>>>(buf(F[0]), buf(F[1]), buf(F[2]), F[0].dims[2], F[1].dims[2],
-                                    F[2].dims[2], S, F[0].L[0], F[0].L[1],
-                                    Plans<R>::z3(F[0].logL[2]), tw, twmax);
+    kern<<<g, ZTPB, sm, st>>>(buf(F[0]), buf(F[1]), buf(F[2]), F[0].dims[2], F[1].dims[2],
+                              F[2].dims[2], S, F[0].L[0], F[0].L[1], p, tw, twmax);
     return 0;
   }
   static int zconv1(const Family& f, const void* s, const cx<R>* tw, int twmax, cudaStream_t st) {
     const int Lz = f.L[2];
     const size_t sm = sizeof(cx<R>) * (Lz + ((size_t)Lz << LTX));
-    CTX_CHECK(smem_optin(k_zconv1<R>, sm));
+    const AxPlan p = Plans<R>::z1(f.logL[2]);
+    constexpr int QL = QCap<R>::Z1;
+    const bool spec = p.ng >= 2 && p.q[0] == 4 && p.q[p.ng - 1] == QL;
+    auto kern = spec ? k_zconv1<R, 4, QL> : k_zconv1<R, 0, 0>;
+    CTX_CHECK(smem_optin(kern, sm));
     dim3 g((f.L[0] + TX - 1) / TX, f.L[1]);
-    k_zconv1<R><<<g, ZTPB, sm, st>>>(buf(f), f.dims[2], s, f.L[0],
-                                    f.L[1], Plans<R>::z1(f.logL[2]), tw, twmax);
+    kern<<<g, ZTPB, sm, st>>>(buf(f), f.dims[2], s, f.L[0], f.L[1], p, tw, twmax);
     return 0;
   }
 };
