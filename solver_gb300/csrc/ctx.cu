@@ -101,6 +101,7 @@ struct peec_ctx {
   int32_t *ne_ptr = nullptr, *ne_idx = nullptr, *nsn_ptr = nullptr, *nsn_idx = nullptr;
   Family fam[6];
   Spectrum spec[9];
+  void* ph64[3] = {nullptr, nullptr, nullptr};  // face-grid phase tables (octant spectra)
   int row_dims[9][3] = {};
   // frequency state
   double w = 0.0;
@@ -306,9 +307,13 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
     for (int p = 0; p < 2; ++p)
       if (f.T[p]) cudaFree(f.T[p]);
   }
-  for (auto& s : ctx->spec)
+  for (auto& s : ctx->spec) {
     for (int p = 0; p < 2; ++p)
       if (s.d[p]) cudaFree(s.d[p]);
+    if (s.oct) cudaFree(s.oct);
+  }
+  for (int a = 0; a < 3; ++a)
+    if (ctx->ph64[a]) cudaFree(ctx->ph64[a]);
   free_tri(ctx->Lf);
   free_tri(ctx->Uf);
   cudaFree(ctx->sf_ord);
@@ -455,13 +460,17 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
   }
   if (ctx->fam[0].L[2] * 3 * 16 * sizeof(c64) > 200 * 1024)
     return bad(ctx, PEEC_ERR_UNSUPPORTED, "z circulant too long for the z pass tile");
-  for (auto& sp : ctx->spec)
+  for (auto& sp : ctx->spec) {
     for (int p = 0; p < 2; ++p) {
       if (sp.d[p]) cudaFree(sp.d[p]);
       sp.d[p] = nullptr;
     }
+    if (sp.oct) cudaFree(sp.oct);
+    sp.oct = nullptr;
+  }
   for (int i = 0; i < 6; ++i) std::memcpy(ctx->spec[i].L, LP, sizeof(LP));
   for (int i = 6; i < 9; ++i) std::memcpy(ctx->spec[i].L, ctx->fam[i - 3].L, sizeof(LP));
+  CTX_TRY(phase_tables(LP, ctx->ph64, ctx->st));
   // work vectors
   CTX_TRY(dalloc(&ctx->LpI, m));
   CTX_TRY(dalloc(&ctx->PQ, ns));
@@ -878,7 +887,8 @@ static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool ev
   cudaStream_t st = ctx->st;
   if (events) cudaEventRecord(ctx->ev[0], st);
   const void* tw[3] = {ctx->tw64, ctx->tw32, ctx->twff};
-  CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, x, ctx->LpI, ctx->PQ, m, prec, tw, ctx->twmax, st,
+  CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, ctx->ph64, x, ctx->LpI, ctx->PQ, m, prec, tw,
+                   ctx->twmax, st,
                    ctx->prof ? ctx->pev.data() : nullptr));
   for (const auto& F : ctx->fam) ctx->launches += F.active ? (F.lp ? 5 : 4) : 0;
   ctx->launches += 1;  // the shared z pass of the face families

@@ -58,10 +58,21 @@ struct Family {
   void* T[2] = {nullptr, nullptr};  // work buffer per precision: [z < dims[2]][y < Ly][kx < Lx]
 };
 
+// A block spectrum, scaled by 1/(Lx*Ly*Lz), in two forms.
+// Full: every position, layout (ky, kz, kx), kx fastest, in the transforms' bit-reversed
+//   position order; real for symmetric kernels; FP64 and FP32 copies (coalesced reads for
+//   the FP32 and FP64 passes).
+// Octant: along each axis the kernel is even (c = 0) or even about a half-sample shift
+//   (c = +-1), so S(k) = R(|k_x|, |k_y|, |k_z|) * prod_a exp(-i*pi*c_a*k_a/L_a) with
+//   k_a in (-L_a/2, L_a/2] and R real; the (L_x/2+1)(L_y/2+1)(L_z/2+1) values of R are kept
+//   in FP64, layout (fy, fz, fx), fx fastest. The float-float passes read this form: an
+//   eighth (a sixteenth for cross blocks) of the FP64 bytes.
 struct Spectrum {
   int L[3] = {1, 1, 1};
+  int c[3] = {0, 0, 0};
   int is_complex = 0;
-  void* d[2] = {nullptr, nullptr};  // [0] fp64, [1] fp32; layout (ky, kz, kx), kx fastest
+  void* d[2] = {nullptr, nullptr};  // full: [0] fp64, [1] fp32
+  void* oct = nullptr;              // octant R, fp64
 };
 
 // Launchers (fftconv.cu). prec: 0 = fp64, 1 = fp32, 2 = float-float; tw[prec] the master
@@ -69,9 +80,11 @@ struct Spectrum {
 // 0..2 are the face families, 3..5 the edge families; spectra 0..5 = P blocks
 // (00, 11, 22, 01, 02, 12), 6..8 = Lp blocks of families 3..5.
 // ev (nullable): 6 events around the five pass classes.
-int conv_all(const Family* F, int nfam, const Spectrum* spec, const c64* x, c64* LpI, c64* PQ,
-             int64_t m, int prec, const void* const* tw, int twmax, cudaStream_t st,
-             cudaEvent_t* ev);
+int conv_all(const Family* F, int nfam, const Spectrum* spec, const void* const* ph,
+             const c64* x, c64* LpI, c64* PQ, int64_t m, int prec, const void* const* tw,
+             int twmax, cudaStream_t st, cudaEvent_t* ev);
+// phase tables exp(-i*pi*k/L) (complex FP64) per DIF position of the three face-grid axes
+int phase_tables(const int L[3], void* e64[3], cudaStream_t st);
 int spectrum_build(Spectrum& S, const double* d_row, const int M[3], const int na[3],
                    const int nb[3], const int sdim[3], const int odim[3], int symmetric,
                    const void* twiddles64, int twmax, cudaStream_t st);

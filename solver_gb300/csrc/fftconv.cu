@@ -38,12 +38,12 @@
 
 namespace peec {
 
-int conv_all_f32(const Family*, int, const Spectrum*, const c64*, c64*, c64*, int64_t,
-                 const void*, int, cudaStream_t, cudaEvent_t*);
-int conv_all_f64(const Family*, int, const Spectrum*, const c64*, c64*, c64*, int64_t,
-                 const void*, int, cudaStream_t, cudaEvent_t*);
-int conv_all_ff(const Family*, int, const Spectrum*, const c64*, c64*, c64*, int64_t,
-                const void*, int, cudaStream_t, cudaEvent_t*);
+int conv_all_f32(const Family*, int, const Spectrum*, const void* const*, const c64*, c64*,
+                 c64*, int64_t, const void*, int, cudaStream_t, cudaEvent_t*);
+int conv_all_f64(const Family*, int, const Spectrum*, const void* const*, const c64*, c64*,
+                 c64*, int64_t, const void*, int, cudaStream_t, cudaEvent_t*);
+int conv_all_ff(const Family*, int, const Spectrum*, const void* const*, const c64*, c64*,
+                c64*, int64_t, const void*, int, cudaStream_t, cudaEvent_t*);
 
 // copy W_L[e] = exp(-2 pi i e / L) for e < n from the master table of length twmax
 template <typename R>
@@ -54,12 +54,12 @@ __device__ void load_tw(cx<R>* dst, const cx<R>* __restrict__ master, int twmax,
 
 // prec: PEEC_PREC_FP64 (0), PEEC_PREC_FP32 (1), PEEC_PREC_FF (2); tw[prec] the matching
 // master twiddle table
-int conv_all(const Family* F, int nfam, const Spectrum* spec, const c64* x, c64* LpI, c64* PQ,
-             int64_t m, int prec, const void* const* tw, int twmax, cudaStream_t st,
-             cudaEvent_t* ev) {
-  if (prec == 0) return conv_all_f64(F, nfam, spec, x, LpI, PQ, m, tw[0], twmax, st, ev);
-  if (prec == 2) return conv_all_ff(F, nfam, spec, x, LpI, PQ, m, tw[2], twmax, st, ev);
-  return conv_all_f32(F, nfam, spec, x, LpI, PQ, m, tw[1], twmax, st, ev);
+int conv_all(const Family* F, int nfam, const Spectrum* spec, const void* const* ph,
+             const c64* x, c64* LpI, c64* PQ, int64_t m, int prec, const void* const* tw,
+             int twmax, cudaStream_t st, cudaEvent_t* ev) {
+  if (prec == 0) return conv_all_f64(F, nfam, spec, ph, x, LpI, PQ, m, tw[0], twmax, st, ev);
+  if (prec == 2) return conv_all_ff(F, nfam, spec, ph, x, LpI, PQ, m, tw[2], twmax, st, ev);
+  return conv_all_f32(F, nfam, spec, ph, x, LpI, PQ, m, tw[1], twmax, st, ev);
 }
 
 // --------------------------------------------------------------------------- spectra
@@ -165,6 +165,56 @@ __global__ void k_spec_store(const c64* __restrict__ full, void* d64, void* d32,
   }
 }
 
+// full (x,y,z; z fastest, DIF bit-reversed positions along each axis) -> octant R of the
+// half-sample-shift form (see Spectrum), scaled, FP64
+__global__ void k_spec_octant(const c64* __restrict__ full, double* o64, int Lx, int Ly, int Lz,
+                              int cx, int cy, int cz, double scale) {
+  const int ox = Lx / 2 + 1, oy = Ly / 2 + 1, oz = Lz / 2 + 1;
+  const int nx = ilog2(Lx), ny = ilog2(Ly), nz = ilog2(Lz);
+  const size_t n = (size_t)ox * oy * oz;
+  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n;
+       o += (size_t)gridDim.x * blockDim.x) {
+    const int fx = (int)(o % ox);
+    const size_t rr = o / ox;
+    const int fz = (int)(rr % oz), fy = (int)(rr / oz);
+    const int px = brev(fx & (Lx - 1), nx), py = brev(fy & (Ly - 1), ny),
+              pz = brev(fz & (Lz - 1), nz);
+    const c64 v = full[((size_t)px * Ly + py) * Lz + pz];
+    // R = Re(S * prod exp(+i*pi*c*f/L)); the phase angle sum is exact in double
+    double ph = 0.0;
+    if (cx) ph += (double)cx * fx / Lx;
+    if (cy) ph += (double)cy * fy / Ly;
+    if (cz) ph += (double)cz * fz / Lz;
+    double sn, cs;
+    sincospi(ph, &sn, &cs);
+    o64[o] = (v.x * cs - v.y * sn) * scale;
+  }
+}
+
+// phase tables of the shifted axes: E[p] = exp(-i*pi*k/L) for the signed frequency k of
+// DIF position p (k = brev(p) folded into (-L/2, L/2])
+__global__ void k_phase_table(int L, c64* e64) {
+  const int n = ilog2(L);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < L; p += gridDim.x * blockDim.x) {
+    int k = brev(p, n);
+    if (k > L / 2) k -= L;
+    double sn, cs;
+    sincospi(-(double)k / L, &sn, &cs);
+    e64[p] = mk<double>(cs, sn);
+  }
+}
+
+int phase_tables(const int L[3], void* e64[3], cudaStream_t st) {
+  for (int a = 0; a < 3; ++a) {
+    if (e64[a]) cudaFree(e64[a]);
+    e64[a] = nullptr;
+    PEEC_CUDA_TRY(cudaMalloc(&e64[a], sizeof(c64) * L[a]));
+    k_phase_table<<<(L[a] + 255) / 256, 256, 0, st>>>(L[a], (c64*)e64[a]);
+  }
+  PEEC_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
 int spectrum_build(Spectrum& S, const double* d_row, const int M[3], const int na[3],
                    const int nb[3], const int sdim[3], const int odim[3], int symmetric,
                    const void* tw64, int twmax, cudaStream_t st) {
@@ -189,6 +239,9 @@ int spectrum_build(Spectrum& S, const double* d_row, const int M[3], const int n
                                          (int)sm));
     k_fft_axis<TZ><<<grid, 256, sm, st>>>(full, S.L[0], S.L[1], S.L[2], axis, logL, tw, twmax);
   }
+  // half-sample shift per axis: |2e + o| is even about e = -o/2 (the embedding window is
+  // symmetric about the same point because na - nb = -o there)
+  for (int a = 0; a < 3; ++a) S.c[a] = (!symmetric && sdim[a] == 2) ? -odim[a] : 0;
   S.is_complex = symmetric ? 0 : 1;
   const size_t es64 = S.is_complex ? sizeof(c64) : sizeof(double);
   const size_t es32 = S.is_complex ? sizeof(c32) : sizeof(float);
@@ -196,6 +249,10 @@ int spectrum_build(Spectrum& S, const double* d_row, const int M[3], const int n
   if (!S.d[1]) PEEC_CUDA_TRY(cudaMalloc(&S.d[1], n * es32));
   k_spec_store<<<1184, 256, 0, st>>>(full, S.d[0], S.d[1], S.L[0], S.L[1], S.L[2], S.is_complex,
                                      1.0 / (double)n);
+  const size_t no = (size_t)(S.L[0] / 2 + 1) * (S.L[1] / 2 + 1) * (S.L[2] / 2 + 1);
+  if (!S.oct) PEEC_CUDA_TRY(cudaMalloc(&S.oct, no * sizeof(double)));
+  k_spec_octant<<<1184, 256, 0, st>>>(full, (double*)S.oct, S.L[0], S.L[1], S.L[2], S.c[0],
+                                      S.c[1], S.c[2], 1.0 / (double)n);
   PEEC_CUDA_TRY(cudaGetLastError());
   PEEC_CUDA_TRY(cudaFreeAsync(full, st));
   return 0;

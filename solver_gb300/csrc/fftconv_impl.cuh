@@ -18,6 +18,34 @@ constexpr int TPB = 256;
 // last groups 3 x 16 columns x 8 pencils, fused step 16 x 16) and four CTAs share an SM
 constexpr int ZTPB = 128;
 
+// Family buffers stream through each pass once: loads and stores carry the streaming
+// (evict-first) cache hint, so the L2 keeps the spectra and twiddles the passes reuse.
+template <typename R>
+struct StreamVec;
+template <>
+struct StreamVec<float> {
+  using T = float2;
+};
+template <>
+struct StreamVec<double> {
+  using T = double2;
+};
+template <>
+struct StreamVec<ff> {
+  using T = float4;
+};
+template <typename R>
+__device__ __forceinline__ cx<R> ld_stream(const cx<R>* p) {
+  using V = typename StreamVec<R>::T;
+  const V v = __ldcs(reinterpret_cast<const V*>(p));
+  return *reinterpret_cast<const cx<R>*>(&v);
+}
+template <typename R>
+__device__ __forceinline__ void st_stream(cx<R>* p, const cx<R>& x) {
+  using V = typename StreamVec<R>::T;
+  __stcs(reinterpret_cast<V*>(p), *reinterpret_cast<const V*>(&x));
+}
+
 // --------------------------------------------------------------------------- x passes
 // CTA: TY = 16 consecutive y rows of one z plane. Tile element (pos, yy) at
 // buf[pos*(TY+1) + yy]; the first/last group threads run along x so map reads and
@@ -101,7 +129,7 @@ __global__ void __launch_bounds__(TPB) k_xfwd(const c64* __restrict__ xin,
   for (int q = threadIdx.x; q < TY << p.n; q += blockDim.x) {
     const int yy = q >> p.n, kx = q & (Lx - 1);
     const int y = y0 + yy;
-    if (y < ny) T[((size_t)z * Ly + y) * Lx + kx] = buf[kx * XRS + yy];
+    if (y < ny) st_stream(T + ((size_t)z * Ly + y) * Lx + kx, buf[kx * XRS + yy]);
   }
 }
 
@@ -148,7 +176,7 @@ __global__ void __launch_bounds__(TPB) k_xinv(const cx<R>* __restrict__ T, c64* 
   for (int q = threadIdx.x; q < TY << p.n; q += blockDim.x) {
     const int yy = q >> p.n, kx = q & (Lx - 1);
     const int y = y0 + yy;
-    buf[kx * XRS + yy] = (y < ny) ? T[((size_t)z * Ly + y) * Lx + kx] : mk<R>(0, 0);
+    buf[kx * XRS + yy] = (y < ny) ? ld_stream(T + ((size_t)z * Ly + y) * Lx + kx) : mk<R>(0, 0);
   }
   __syncthreads();
   if (p.ng > 1) {
@@ -185,7 +213,7 @@ __device__ __forceinline__ void col_first_fwd(const cx<R>* g, size_t gstride, in
 #pragma unroll
     for (int r = 0; r < N; ++r) {
       const int row = k + (r << lh);
-      v[r] = (col < ncols && row < n_in) ? g[row * gstride + col] : mk<R>(0, 0);
+      v[r] = (col < ncols && row < n_in) ? ld_stream(g + row * gstride + col) : mk<R>(0, 0);
     }
     dft_dif<R, Q>(v);
     if (p.ng > 1) {
@@ -194,7 +222,7 @@ __device__ __forceinline__ void col_first_fwd(const cx<R>* g, size_t gstride, in
       for (int r = 0; r < N; ++r) buf[((k + (r << lh)) << LTX) + col] = v[r];
     } else if (col < ncols) {
 #pragma unroll
-      for (int r = 0; r < N; ++r) gout[r * gstride + col] = v[r];
+      for (int r = 0; r < N; ++r) st_stream(gout + r * gstride + col, v[r]);
     }
   }
 }
@@ -214,7 +242,7 @@ __device__ __forceinline__ void col_last_fwd(const cx<R>* buf, cx<R>* g, size_t 
     dft_dif<R, Q>(v);
     if (col < ncols) {
 #pragma unroll
-      for (int r = 0; r < N; ++r) g[(start + r) * gstride + col] = v[r];
+      for (int r = 0; r < N; ++r) st_stream(g + (start + r) * gstride + col, v[r]);
     }
   }
 }
@@ -233,7 +261,7 @@ __device__ __forceinline__ void col_first_inv(const cx<R>* g, size_t gstride, in
     cx<R> v[N];
 #pragma unroll
     for (int r = 0; r < N; ++r)
-      v[r] = col < ncols ? g[(start + r) * gstride + col] : mk<R>(0, 0);
+      v[r] = col < ncols ? ld_stream(g + (start + r) * gstride + col) : mk<R>(0, 0);
     dft_dit<R, Q>(v);
     if (p.ng > 1) {
 #pragma unroll
@@ -241,7 +269,7 @@ __device__ __forceinline__ void col_first_inv(const cx<R>* g, size_t gstride, in
     } else if (col < ncols) {
 #pragma unroll
       for (int r = 0; r < N; ++r)
-        if (start + r < n_out) gout[(start + r) * gstride + col] = v[r];
+        if (start + r < n_out) st_stream(gout + (start + r) * gstride + col, v[r]);
     }
   }
 }
@@ -267,7 +295,7 @@ __device__ __forceinline__ void col_last_inv(const cx<R>* buf, cx<R>* g, size_t 
 #pragma unroll
       for (int r = 0; r < N; ++r) {
         const int row = k + (r << lh);
-        if (row < n_out) g[row * gstride + col] = v[r];
+        if (row < n_out) st_stream(g + row * gstride + col, v[r]);
       }
     }
   }
@@ -321,14 +349,36 @@ __global__ void __launch_bounds__(TPB) k_ypass(cx<R>* T, int Lx, AxPlan p, int n
 
 // --------------------------------------------------------------------------- z passes
 
+// The six P spectra: full form (diagonal blocks real, cross blocks complex, in the pass's
+// storage precision) and octant form (real R, FP64) with the cross blocks' half-sample
+// shifts and the face grid's phase tables E_a[p] = exp(-i*pi*k/L_a), k the signed
+// frequency of position p. In octant form a cross spectrum is R times the product of
+// E_a (shift +1) or conj(E_a) (shift -1) over its shifted axes. The FP32 and FP64 passes
+// read the full form (coalesced); the float-float passes read the octant (an eighth of
+// the FP64 bytes, and FP32-pipe arithmetic for the phases).
 struct PSpec {
-  const void* s00;
-  const void* s11;
-  const void* s22;  // real
-  const void* s01;
-  const void* s02;
-  const void* s12;  // complex
+  const void* f00;
+  const void* f11;
+  const void* f22;
+  const void* f01;
+  const void* f02;
+  const void* f12;
+  const void* o00;
+  const void* o11;
+  const void* o22;
+  const void* o01;
+  const void* o02;
+  const void* o12;
+  const void* ex;
+  const void* ey;
+  const void* ez;
+  int c01[3], c02[3], c12[3];
 };
+
+template <typename R>
+constexpr bool octant_spectra() {
+  return std::is_same<R, ff>::value;
+}
 
 // storage type of the spectra a pass of arithmetic type R reads: the float-float
 // passes split the FP64 spectra on load
@@ -350,47 +400,120 @@ __device__ __forceinline__ cx<R> spec_cx(const void* p, size_t i) {
   return mk<R>(R(v.x), R(v.y));
 }
 
-// Y_f = sum_g S_fg X_g with S_gf = conj(S_fg), at spectrum index si
+__device__ __forceinline__ int brevn(int v, int n) {
+  return n ? (int)(__brev((unsigned)v) >> (32 - n)) : 0;
+}
+// octant index of the frequency at DIF position p of a length-2^n axis
+__device__ __forceinline__ int fold_pos(int p, int n) {
+  const int k = brevn(p, n), L = 1 << n;
+  return k <= (L >> 1) ? k : L - k;
+}
+
+// Spectrum addressing of one z-pass CTA (fixed ky, kx tile). Full form: (ky, kz, kx0+col)
+// at sbase + kz*Lx + col. Octant form: entry (fy, fz, fx) at (fy*oz + fz)*ox + fx with
+// o_a = L_a/2 + 1.
+struct OctIdx {
+  size_t rowbase;  // fy * oz * ox
+  size_t sbase;    // ky * Lz * Lx + kx0
+  int Lx, ox, nx, nz, kx0;
+  __device__ __forceinline__ size_t at(int col, int pz) const {
+    return rowbase + (size_t)fold_pos(pz, nz) * ox + fold_pos(kx0 + col, nx);
+  }
+  __device__ __forceinline__ size_t full(int col, int pz) const {
+    return sbase + (size_t)pz * Lx + col;
+  }
+};
+
+__device__ __forceinline__ OctIdx make_octidx(int Lx, int Ly, int Lz, int kx0, int ky) {
+  OctIdx o;
+  o.Lx = Lx;
+  o.nx = ilog2(Lx);
+  o.nz = ilog2(Lz);
+  o.ox = Lx / 2 + 1;
+  o.kx0 = kx0;
+  o.rowbase = (size_t)fold_pos(ky, ilog2(Ly)) * (Lz / 2 + 1) * o.ox;
+  o.sbase = (size_t)ky * Lz * Lx + kx0;
+  return o;
+}
+
 template <typename R>
-__device__ __forceinline__ void pspec_apply(const PSpec& S, size_t si, cx<R>& a0, cx<R>& a1,
-                                            cx<R>& a2) {
-  const cx<R> c01 = spec_cx<R>(S.s01, si), c02 = spec_cx<R>(S.s02, si),
-              c12 = spec_cx<R>(S.s12, si);
-  const cx<R> b0 = cscale(a0, spec_re<R>(S.s00, si)) + c01 * a1 + c02 * a2;
-  const cx<R> b1 = cmulc(a0, c01) + cscale(a1, spec_re<R>(S.s11, si)) + c12 * a2;
-  const cx<R> b2 = cmulc(a0, c02) + cmulc(a1, c12) + cscale(a2, spec_re<R>(S.s22, si));
+__device__ __forceinline__ cx<R> shift_phase(const int c[3], const cx<R>& ex, const cx<R>& ey,
+                                             const cx<R>& ez) {
+  cx<R> f = mk<R>(1, 0);
+  if (c[0]) f = c[0] > 0 ? f * ex : cmulc(f, ex);
+  if (c[1]) f = c[1] > 0 ? f * ey : cmulc(f, ey);
+  if (c[2]) f = c[2] > 0 ? f * ez : cmulc(f, ez);
+  return f;
+}
+
+// Y_f = sum_g S_fg X_g with S_gf = conj(S_fg), at the frequency of (column col, z
+// position pz) of the CTA; ex / ey the CTA's x (per column) and y phases
+template <typename R>
+__device__ __forceinline__ void pspec_apply(const PSpec& S, const OctIdx& O, int col, int pz,
+                                            const cx<R>& ex, const cx<R>& ey, cx<R>& a0,
+                                            cx<R>& a1, cx<R>& a2) {
+  cx<R> c01, c02, c12;
+  R d00, d11, d22;
+  if constexpr (octant_spectra<R>()) {
+    const size_t oi = O.at(col, pz);
+    const cx<R> ez = spec_cx<R>(S.ez, pz);
+    c01 = cscale(shift_phase<R>(S.c01, ex, ey, ez), spec_re<R>(S.o01, oi));
+    c02 = cscale(shift_phase<R>(S.c02, ex, ey, ez), spec_re<R>(S.o02, oi));
+    c12 = cscale(shift_phase<R>(S.c12, ex, ey, ez), spec_re<R>(S.o12, oi));
+    d00 = spec_re<R>(S.o00, oi);
+    d11 = spec_re<R>(S.o11, oi);
+    d22 = spec_re<R>(S.o22, oi);
+  } else {
+    const size_t si = O.full(col, pz);
+    c01 = spec_cx<R>(S.f01, si);
+    c02 = spec_cx<R>(S.f02, si);
+    c12 = spec_cx<R>(S.f12, si);
+    d00 = spec_re<R>(S.f00, si);
+    d11 = spec_re<R>(S.f11, si);
+    d22 = spec_re<R>(S.f22, si);
+  }
+  const cx<R> b0 = cscale(a0, d00) + c01 * a1 + c02 * a2;
+  const cx<R> b1 = cmulc(a0, c01) + cscale(a1, d11) + c12 * a2;
+  const cx<R> b2 = cmulc(a0, c02) + cmulc(a1, c12) + cscale(a2, d22);
   a0 = b0;
   a1 = b1;
   a2 = b2;
+}
+
+// the x and y phases of a column / the CTA (octant form only)
+template <typename R>
+__device__ __forceinline__ cx<R> phase_at(const void* table, int p) {
+  if constexpr (octant_spectra<R>()) return spec_cx<R>(table, p);
+  else return mk<R>(1, 0);
 }
 
 // single-group z transform of all three face families in registers
 template <typename R, int Q>
 __device__ __forceinline__ void z3_single(cx<R>* T0, cx<R>* T1, cx<R>* T2, int nz0, int nz1,
                                           int nz2, size_t pl, int ncols, const PSpec& S,
-                                          size_t sbase, size_t sstride) {
+                                          const OctIdx& O, const cx<R>& ey) {
   constexpr int N = 1 << Q;
   for (int col = threadIdx.x; col < TX; col += blockDim.x) {
     if (col >= ncols) continue;
+    const cx<R> ex = phase_at<R>(S.ex, O.kx0 + col);
     cx<R> v[3][N];
 #pragma unroll
     for (int r = 0; r < N; ++r) {
-      v[0][r] = r < nz0 ? T0[r * pl + col] : mk<R>(0, 0);
-      v[1][r] = r < nz1 ? T1[r * pl + col] : mk<R>(0, 0);
-      v[2][r] = r < nz2 ? T2[r * pl + col] : mk<R>(0, 0);
+      v[0][r] = r < nz0 ? ld_stream(T0 + r * pl + col) : mk<R>(0, 0);
+      v[1][r] = r < nz1 ? ld_stream(T1 + r * pl + col) : mk<R>(0, 0);
+      v[2][r] = r < nz2 ? ld_stream(T2 + r * pl + col) : mk<R>(0, 0);
     }
 #pragma unroll
     for (int f = 0; f < 3; ++f) dft_dif<R, Q>(v[f]);
 #pragma unroll
-    for (int r = 0; r < N; ++r)
-      pspec_apply<R>(S, sbase + r * sstride + col, v[0][r], v[1][r], v[2][r]);
+    for (int r = 0; r < N; ++r) pspec_apply<R>(S, O, col, r, ex, ey, v[0][r], v[1][r], v[2][r]);
 #pragma unroll
     for (int f = 0; f < 3; ++f) dft_dit<R, Q>(v[f]);
 #pragma unroll
     for (int r = 0; r < N; ++r) {
-      if (r < nz0) T0[r * pl + col] = v[0][r];
-      if (r < nz1) T1[r * pl + col] = v[1][r];
-      if (r < nz2) T2[r * pl + col] = v[2][r];
+      if (r < nz0) st_stream(T0 + r * pl + col, v[0][r]);
+      if (r < nz1) st_stream(T1 + r * pl + col, v[1][r]);
+      if (r < nz2) st_stream(T2 + r * pl + col, v[2][r]);
     }
   }
 }
@@ -400,7 +523,7 @@ __device__ __forceinline__ void z3_single(cx<R>* T0, cx<R>* T1, cx<R>* T2, int n
 // buf + f*tsz)
 template <typename R, int Q>
 __device__ __forceinline__ void z3_fused(cx<R>* buf, size_t tsz, const AxPlan& p, int ncols,
-                                         const PSpec& S, size_t sbase, size_t sstride) {
+                                         const PSpec& S, const OctIdx& O, const cx<R>& ey) {
   constexpr int N = 1 << Q;
   const int tasks = TX << (p.n - Q);
   for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
@@ -414,9 +537,10 @@ __device__ __forceinline__ void z3_fused(cx<R>* buf, size_t tsz, const AxPlan& p
       dft_dif<R, Q>(v[f]);
     }
     if (col < ncols) {
+      const cx<R> ex = phase_at<R>(S.ex, O.kx0 + col);
 #pragma unroll
       for (int r = 0; r < N; ++r)
-        pspec_apply<R>(S, sbase + (start + r) * sstride + col, v[0][r], v[1][r], v[2][r]);
+        pspec_apply<R>(S, O, col, start + r, ex, ey, v[0][r], v[1][r], v[2][r]);
     }
 #pragma unroll
     for (int f = 0; f < 3; ++f) {
@@ -453,13 +577,13 @@ __global__ void __launch_bounds__(ZTPB, 4) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>*
   T0 += off;
   T1 += off;
   T2 += off;
-  // spectrum index of (ky, kz, kx0 + col) = sbase + kz*Lx + col
-  const size_t sbase = (size_t)ky * Lz * Lx + kx0;
+  const OctIdx O = make_octidx(Lx, Ly, Lz, kx0, ky);
+  const cx<R> ey = phase_at<R>(S.ey, ky);
   load_twiddles<R>(W, twm, twmax, Lz);
   __syncthreads();
   if constexpr (Q0 == 0) {
     if (p.ng == 1) {
-      qswitch<QCap<R>::Z3>(p.q[0], [&](auto QC) { z3_single<R, decltype(QC)::value>(T0, T1, T2, nz0, nz1, nz2, pl, ncols, S, sbase, (size_t)Lx); });
+      qswitch<QCap<R>::Z3>(p.q[0], [&](auto QC) { z3_single<R, decltype(QC)::value>(T0, T1, T2, nz0, nz1, nz2, pl, ncols, S, O, ey); });
       return;
     }
   }
@@ -477,7 +601,7 @@ __global__ void __launch_bounds__(ZTPB, 4) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>*
       __syncthreads();
     }
   }
-  qpick<QL, QCap<R>::Z3>(p.q[p.ng - 1], [&](auto QC) { z3_fused<R, decltype(QC)::value>(buf, tsz, p, ncols, S, sbase, (size_t)Lx); });
+  qpick<QL, QCap<R>::Z3>(p.q[p.ng - 1], [&](auto QC) { z3_fused<R, decltype(QC)::value>(buf, tsz, p, ncols, S, O, ey); });
   __syncthreads();
   {
     int s = p.n - p.q[p.ng - 1];
@@ -497,28 +621,27 @@ __global__ void __launch_bounds__(ZTPB, 4) k_zconv3(cx<R>* T0, cx<R>* T1, cx<R>*
 // one edge family with its real spectrum
 template <typename R, int Q>
 __device__ __forceinline__ void z1_single(cx<R>* Tg, int nz, size_t pl, int ncols,
-                                          const void* __restrict__ s, size_t sbase,
-                                          size_t sstride) {
+                                          const void* __restrict__ s, const OctIdx& O) {
   constexpr int N = 1 << Q;
   for (int col = threadIdx.x; col < TX; col += blockDim.x) {
     if (col >= ncols) continue;
     cx<R> v[N];
 #pragma unroll
-    for (int r = 0; r < N; ++r) v[r] = r < nz ? Tg[r * pl + col] : mk<R>(0, 0);
+    for (int r = 0; r < N; ++r) v[r] = r < nz ? ld_stream(Tg + r * pl + col) : mk<R>(0, 0);
     dft_dif<R, Q>(v);
 #pragma unroll
-    for (int r = 0; r < N; ++r) v[r] = cscale(v[r], spec_re<R>(s, sbase + r * sstride + col));
+    for (int r = 0; r < N; ++r)
+      v[r] = cscale(v[r], spec_re<R>(s, octant_spectra<R>() ? O.at(col, r) : O.full(col, r)));
     dft_dit<R, Q>(v);
 #pragma unroll
     for (int r = 0; r < N; ++r)
-      if (r < nz) Tg[r * pl + col] = v[r];
+      if (r < nz) st_stream(Tg + r * pl + col, v[r]);
   }
 }
 
 template <typename R, int Q>
 __device__ __forceinline__ void z1_fused(cx<R>* buf, const AxPlan& p, int ncols,
-                                         const void* __restrict__ s, size_t sbase,
-                                         size_t sstride) {
+                                         const void* __restrict__ s, const OctIdx& O) {
   constexpr int N = 1 << Q;
   const int tasks = TX << (p.n - Q);
   for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
@@ -531,7 +654,8 @@ __device__ __forceinline__ void z1_fused(cx<R>* buf, const AxPlan& p, int ncols,
     if (col < ncols) {
 #pragma unroll
       for (int r = 0; r < N; ++r)
-        v[r] = cscale(v[r], spec_re<R>(s, sbase + (start + r) * sstride + col));
+        v[r] = cscale(v[r], spec_re<R>(s, octant_spectra<R>() ? O.at(col, start + r)
+                                                              : O.full(col, start + r)));
     }
     dft_dit<R, Q>(v);
 #pragma unroll
@@ -551,19 +675,19 @@ __global__ void __launch_bounds__(ZTPB, 4) k_zconv1(cx<R>* T0, int nz0, const vo
   const int ncols = min(TX, Lx - kx0);
   const size_t pl = (size_t)Ly * Lx;
   cx<R>* Tg = T0 + (size_t)ky * Lx + kx0;
-  const size_t sbase = (size_t)ky * Lz * Lx + kx0;
+  const OctIdx O = make_octidx(Lx, Ly, Lz, kx0, ky);
   load_twiddles<R>(W, twm, twmax, Lz);
   __syncthreads();
   if constexpr (Q0 == 0) {
     if (p.ng == 1) {
-      qswitch<QCap<R>::Z1>(p.q[0], [&](auto QC) { z1_single<R, decltype(QC)::value>(Tg, nz0, pl, ncols, s00, sbase, (size_t)Lx); });
+      qswitch<QCap<R>::Z1>(p.q[0], [&](auto QC) { z1_single<R, decltype(QC)::value>(Tg, nz0, pl, ncols, s00, O); });
       return;
     }
   }
   qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_first_fwd<R, decltype(QC)::value>(Tg, pl, ncols, nz0, buf, p, W, Tg); });
   __syncthreads();
   middle_groups<R, false, LTX>(buf, TX, p, W);
-  qpick<QL, QCap<R>::Z1>(p.q[p.ng - 1], [&](auto QC) { z1_fused<R, decltype(QC)::value>(buf, p, ncols, s00, sbase, (size_t)Lx); });
+  qpick<QL, QCap<R>::Z1>(p.q[p.ng - 1], [&](auto QC) { z1_fused<R, decltype(QC)::value>(buf, p, ncols, s00, O); });
   __syncthreads();
   middle_groups<R, true, LTX>(buf, TX, p, W);
   qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf, Tg, pl, ncols, nz0, p, W); });
@@ -670,10 +794,11 @@ struct Launch {
 };
 
 // ev (nullable): 6 events bracketing the five pass classes
+// ph: the face grid's phase tables (x, y, z), complex FP64
 template <typename R>
-int conv_all_t(const Family* F, int nfam, const Spectrum* spec, const c64* x, c64* LpI,
-                      c64* PQ, int64_t m, const cx<R>* tw, int twmax, cudaStream_t st,
-                      cudaEvent_t* ev) {
+int conv_all_t(const Family* F, int nfam, const Spectrum* spec, const void* const* ph,
+               const c64* x, c64* LpI, c64* PQ, int64_t m, const cx<R>* tw, int twmax,
+               cudaStream_t st, cudaEvent_t* ev) {
   using Lc = Launch<R>;
   const int p = slot_of<R>();
   if (ev) cudaEventRecord(ev[0], st);
@@ -683,10 +808,19 @@ int conv_all_t(const Family* F, int nfam, const Spectrum* spec, const c64* x, c6
   for (int f = 0; f < nfam; ++f)
     if (F[f].active) CTX_CHECK(Lc::template ypass<false>(F[f], tw, twmax, st));
   if (ev) cudaEventRecord(ev[2], st);
-  PSpec S{spec[0].d[p], spec[1].d[p], spec[2].d[p], spec[3].d[p], spec[4].d[p], spec[5].d[p]};
+  PSpec S{spec[0].d[p], spec[1].d[p], spec[2].d[p], spec[3].d[p], spec[4].d[p], spec[5].d[p],
+          spec[0].oct,  spec[1].oct,  spec[2].oct,  spec[3].oct,  spec[4].oct,  spec[5].oct,
+          ph[0],        ph[1],        ph[2],        {},           {},           {}};
+  for (int a = 0; a < 3; ++a) {
+    S.c01[a] = spec[3].c[a];
+    S.c02[a] = spec[4].c[a];
+    S.c12[a] = spec[5].c[a];
+  }
   CTX_CHECK(Lc::zconv3(F, S, tw, twmax, st));
   for (int f = 3; f < nfam; ++f)
-    if (F[f].active) CTX_CHECK(Lc::zconv1(F[f], spec[3 + f].d[p], tw, twmax, st));
+    if (F[f].active)
+      CTX_CHECK(Lc::zconv1(F[f], octant_spectra<R>() ? spec[3 + f].oct : spec[3 + f].d[p], tw,
+                           twmax, st));
   if (ev) cudaEventRecord(ev[3], st);
   for (int f = 0; f < nfam; ++f)
     if (F[f].active) CTX_CHECK(Lc::template ypass<true>(F[f], tw, twmax, st));
