@@ -279,3 +279,32 @@ def _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode, mixed_inne
                     S[c2, c1, k] = S[c1, c2, k]
     return {"S": S, "Z": s2z_fft(S, ports_scatter_value), "Y": s2y_fft(S, ports_scatter_value),
             "info": info, "Vrest": Vrest}
+
+
+def sweep_many(requests, mode="mixed", concurrency=4, device=0):
+    """Frequency sweeps of several geometries, concurrently: each geometry gets its own
+    context (CUDA stream, fill, spectra, workspaces) and host thread, so the sweeps' kernels
+    overlap on the GPU the way port lanes do. Per request: the mesher, the GPU fill, then
+    FFT_solver_QS_S_type in the given mode. Returns the results in request order."""
+    from concurrent.futures import ThreadPoolExecutor
+    from . import mesher
+    from .operator import GpuOperator
+
+    def one(req):
+        out, freqs, settings, z0, grid = mesher.parse_request(req)
+        esc, inc, cc, diag, exp, ports, le, li, Zs = out
+        op = GpuOperator(inc, exp, diag["P"], device=device)
+        try:
+            op.fill(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"])
+            exp["gpu_ctx"] = op
+            h = CirculantSpectra(op)
+            st = {"Inner_Iter": settings["Inner_Iter"],
+                  "tol": np.full(len(freqs), settings["tol"])}
+            return FFT_solver_QS_S_type(freqs, esc, inc, h, h, diag, ports, z0, le, exp, st, Zs,
+                                        mode=mode)
+        finally:
+            exp.pop("gpu_ctx", None)
+            op.close()
+
+    with ThreadPoolExecutor(max_workers=max(1, concurrency)) as pool:
+        return list(pool.map(one, requests))

@@ -14,6 +14,8 @@ synthetic stand-ins with the stated shapes, sizes and distributions.
   10 MHz - 10 GHz, tol 1e-8. Voxels without any occupied face neighbour are removed
   (drop_isolated), since the reference algorithm cannot solve a geometry that has them.
 * random_copper(a, b, c, p, seed) -- copper-only Bernoulli(p) grids.
+* batched_sweep -- 12 uneven copper grids a x a x a/2 (a = 32..96 from seed 4),
+  Bernoulli(0.25), one port each, 64 frequencies 1 MHz - 10 GHz, tol 1e-8.
 """
 from __future__ import annotations
 
@@ -125,3 +127,17 @@ def random_copper(shape, s=5e-5, p=0.3, seed=5, nports=1, freqs=(1e9,), tol=1e-8
     cu = drop_isolated(_draw(shape, p, rng))
     ports = _boundary_ports(cu, nports, rng)
     return make_request({"copper": cu}, [dict(COPPER)], (s, s, s), ports, freqs, tol, inner=inner)
+
+
+def batched_sweep(count=12, seed=4, side_range=(4, 13), nfreq=64, fmin=1e6, fmax=1e10, s=5e-5,
+                  p=0.25, tol=1e-8, inner=100):
+    """Uneven copper grids for a batched frequency sweep: side a = 8*integers(side_range)
+    drawn from the seed, grid a x a x a/2, Bernoulli(p) copper occupancy and one port per
+    geometry drawn from a per-geometry seed (1000*seed + index), nfreq log-spaced
+    frequencies from fmin to fmax on every geometry."""
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(side_range[0], side_range[1], size=count) * 8
+    freqs = list(np.logspace(np.log10(fmin), np.log10(fmax), nfreq))
+    return [random_copper((int(a), int(a), int(a) // 2), s=s, p=p, seed=1000 * seed + i,
+                          nports=1, freqs=freqs, tol=tol, inner=inner)
+            for i, a in enumerate(sides)]

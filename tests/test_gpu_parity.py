@@ -344,3 +344,23 @@ def test_mixed_crossbar_per_frequency():
         assert max(errs) <= 1e-7, dict(zip([float(f) for f in freqs], errs))
     finally:
         op.close()
+
+
+def test_batched_sweep_many_geometries():
+    """Several uneven copper geometries swept concurrently (one context and host thread
+    per geometry, mixed precision, relative residual 1e-10) against the oracle's FP64
+    sweep of each geometry: port impedances within 1e-6 at every frequency."""
+    from solver_gb300 import api
+    reqs = configs.batched_sweep(count=3, side_range=(1, 3), nfreq=4, fmin=1e8, fmax=1e10,
+                                 tol=1e-10)
+    got = api.sweep_many(reqs, mode="mixed", concurrency=3)
+    for req, res in zip(reqs, got):
+        c = _case(req)
+        nf = len(c["freqs"])
+        ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
+                                     c["diag"], c["ports"], c["z0"], c["le"], c["exp"],
+                                     {"Inner_Iter": 200, "tol": np.full(nf, 1e-10)}, c["Zs"])
+        assert all(r["flag"] == 0 for r in res["info"])
+        for k in range(nf):
+            e = np.max(np.abs(res["Z"][:, :, k] - ref["Z"][:, :, k])) / np.max(np.abs(ref["Z"][:, :, k]))
+            assert e < 1e-6, (c["grid"], k, e)
