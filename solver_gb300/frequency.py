@@ -67,7 +67,9 @@ class FrequencyState:
     UMFPACK, FFT_solver_QS_S_type.jl:119; any sparse LU of SS gives the same operator)."""
 
     def __init__(self, w, escalings, incidence_selection, diagonals, Zs_info, lumped_elements,
-                 ports, z0):
+                 ports, z0, DZ=None):
+        """DZ (optional) replaces the edge impedances built from diagonals and Zs_info
+        (per-voxel conductivities, see gradient.dz_edges)."""
         A = incidence_selection["A"]
         Gamma = incidence_selection["Gamma"]
         n = A.shape[1]
@@ -82,6 +84,8 @@ class FrequencyState:
         Zs = Zs.copy()
         Zs[se[d < 0]] = 1j * Zs[se[d < 0]].imag
         self.DZ = Zself + Zs.real + 1j * w * np.asarray(diagonals["Lp"]).ravel()
+        if DZ is not None:
+            self.DZ = np.asarray(DZ, dtype=np.complex128).ravel()
         self.invZ = sp.diags(1.0 / self.DZ)
         self.invP = sp.diags(1.0 / np.asarray(diagonals["P"]).ravel())
         SS = (self.Yle + A.T @ (self.invZ @ A) + 1j * w * ((Gamma @ self.invP) @ Gamma.T)).tocsc()

@@ -323,7 +323,9 @@ def mesher_FFT(materials, sx, sy, sz, grids, ports, lumped_elements, origin, dom
                   "N1": N1, "N2": N2, "N3": N3,
                   # compact lattice placement used by the GPU operator
                   "edge_cell": edge_cell, "surf_cell": surf_cell, "surf_fam": fam,
-                  "grid": (Nx, Ny, Nz)}
+                  "grid": (Nx, Ny, Nz),
+                  # voxel number (1-based, 0 empty) per lattice cell, x fastest
+                  "vox_map": np.asarray(raw["vox_map"])}
 
     # diagonals (compute_diagonals.jl:1-134)
     mats = raw["edge_mat"]
@@ -437,8 +439,10 @@ def _compute_zs(materials, mats, b1, b2, zs, offs, sx, sy, sz):
     Zs = par(Zsw[:, 0], Zsw[:, 1]) + par(Zsw[:, 2], Zsw[:, 3])
     internal = np.nonzero(np.abs(Zs) == 0)[0]
     surface = np.nonzero(np.abs(Zs) != 0)[0]
+    # Zsw: the four contributions per edge (columns 0, 1 lie in the edge's first voxel,
+    # 2, 3 in its second), kept for conductivity derivatives
     return {"Zs": Zs, "internal_edges": internal, "surface_edges": surface,
-            "materials": mats.copy()}
+            "materials": mats.copy(), "Zsw": Zsw}
 
 
 # ----------------------------------------------------------------------------------------

@@ -1,0 +1,117 @@
+"""CPU: known-answer checks of the oracle (oracle/peec_oracle.py, oracle/fill_ref.c).
+The reference ships no outputs for this path, so the oracle is held to what physics and
+the reference's own closed forms fix:
+
+* the fill's coincident-cell Lp integral equals the closed-form bar self inductance of
+  compute_diagonals.jl:136-155, and its P integral equals the mesher's face self terms
+  (mesher_FFT.jl:114-138);
+* far apart, Lp -> mu0 l^2 / (4 pi R) and P -> 1 / (4 pi eps0 R), with the quadrupole
+  error falling as 1/R^2;
+* the port operator is reciprocal: port 2's solution gives the same S12 as port 1's
+  (FFT_solver_QS_S_type.jl:206 fills S symmetrically by assuming it);
+* the oracle reproduces its committed regression outputs (tests/golden/oracle_*.npz,
+  written by tests/golden/make_fixtures.py)."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import peec_oracle as O
+from solver_gb300 import configs, mesher
+
+MU0 = 4 * math.pi * 1e-7
+EPS0 = 8.854187812813e-12
+CELL = (1e-4, 2e-4, 5e-5)
+
+
+def _line(n, axis, step):
+    c = np.zeros((n, 3))
+    c[:, axis] = np.arange(n) * step
+    return c
+
+
+@pytest.mark.parametrize("dc", [1, 2, 3])
+def test_lp_self_matches_closed_form(dc):
+    sx, sy, sz = CELL
+    l = CELL[dc - 1]
+    W, T = [(sy, sz), (sx, sz), (sy, sx)][dc - 1]
+    row = O.lp_row(dc, _line(2, 0, 10 * sx), sx, sy, sz)
+    assert row[0] == pytest.approx(mesher._lp_self(l, W, T), rel=1e-12)
+
+
+def test_p_self_matches_mesher_self_terms():
+    sx, sy, sz = CELL
+    want = mesher.p_self_terms(sx, sy, sz)
+    for k, caser in enumerate((1, 3, 5)):
+        row = O.p_row(caser, caser, _line(2, 2, 10 * sz), sx, sy, sz, mesher.ESCALINGS["P"])
+        assert row[0] == pytest.approx(want[k], rel=1e-12)
+
+
+# centre distances stay below 200 x the smallest cell edge, where the reference switches
+# to its lower-dimensional (suppressed) integrals
+FAR = np.array([10, 20, 40])
+
+
+@pytest.mark.parametrize("dc", [1, 2, 3])
+def test_lp_far_field(dc):
+    sx, sy, sz = CELL
+    l = CELL[dc - 1]
+    step = max(CELL)
+    row = O.lp_row(dc, _line(41, dc % 3, step), sx, sy, sz)
+    err = np.abs(row[FAR] * (FAR * step) / (MU0 / (4 * math.pi) * l * l) - 1)
+    assert np.all(err * FAR**2 < 2.0) and err[-1] < 1e-3, err
+
+
+@pytest.mark.parametrize("caser", [1, 3, 5])
+def test_p_far_field(caser):
+    sx, sy, sz = CELL
+    step = max(CELL)
+    row = O.p_row(caser, caser, _line(41, 2 if caser != 5 else 0, step), sx, sy, sz, 1.0)
+    err = np.abs(row[FAR] * (FAR * step) * 4 * math.pi * EPS0 - 1)
+    assert np.all(err * FAR**2 < 2.0) and err[-1] < 1e-3, err
+
+
+def test_port_operator_is_reciprocal():
+    req = configs.random_mixed(shape=(10, 10, 4), p=0.45, seed=3, nports=2,
+                               freqs=[1e8, 3e9], tol=1e-10)
+    out, freqs, _settings, z0, (Nx, Ny, Nz) = mesher.parse_request(req)
+    esc, inc, cc, diag, exp, ports, le, _li, Zs = out
+    FFTCP, FFTCLp = O.spectra_from_rows(O.fill_rows(cc, esc, Nx, Ny, Nz), Nx, Ny, Nz)
+    m, n = inc["A"].shape
+    ns = inc["Gamma"].shape[1]
+    pn = np.asarray(ports["port_nodes"])
+    sols = {}
+    O.FFT_solver_QS_S_type(freqs, esc, inc, FFTCP, FFTCLp, diag, ports, z0, le, exp,
+                           {"Inner_Iter": 200, "tol": np.full(len(freqs), 1e-12)}, Zs,
+                           callback=lambda k, p, V: sols.__setitem__((k, p), V.copy()))
+    for k in range(len(freqs)):
+        v = lambda p, q: 2 * (sols[(k, p)][m + ns + pn[q][0]] - sols[(k, p)][m + ns + pn[q][1]])
+        s12, s21 = v(0, 1), v(1, 0)
+        assert abs(s12 - s21) <= 1e-7 * max(abs(s12), 1e-3 * abs(v(0, 0))), (k, s12, s21)
+
+
+def _case(tag):
+    from pathlib import Path
+    g = Path(__file__).resolve().parent / "golden"
+    req = (mesher.load_request(g / "first_run_data.json") if tag == "first_run_data"
+           else configs.crossbar_20x20x4())
+    return req, np.load(g / f"oracle_{tag}.npz")
+
+
+@pytest.mark.parametrize("tag", ["first_run_data", "crossbar_20x20x4"])
+def test_oracle_matches_its_regression_pins(tag):
+    req, pin = _case(tag)
+    out, freqs, settings, z0, (Nx, Ny, Nz) = mesher.parse_request(req)
+    esc, inc, cc, diag, exp, ports, le, _li, Zs = out
+    rows = O.fill_rows(cc, esc, Nx, Ny, Nz)
+    for key, row in rows.items():
+        np.testing.assert_allclose(row, pin[f"row_{key}"], rtol=1e-13, atol=0)
+    FFTCP, FFTCLp = O.spectra_from_rows(rows, Nx, Ny, Nz)
+    w = 2 * np.pi * freqs[0] * esc["freq"]
+    fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
+    y = O.ComputeMatrixVectorFTT(pin["x"], w, inc, FFTCP, FFTCLp, fs["DZ"], fs["Yle"], exp,
+                                 fs["invZ"], fs["invP"], fs["F"])
+    np.testing.assert_allclose(y, pin["y"], rtol=0, atol=1e-9 * np.max(np.abs(pin["y"])))
+    st = {"Inner_Iter": settings["Inner_Iter"], "tol": np.full(len(freqs), settings["tol"])}
+    res = O.FFT_solver_QS_S_type(freqs, esc, inc, FFTCP, FFTCLp, diag, ports, z0, le, exp, st, Zs)
+    np.testing.assert_allclose(res["Z"], pin["Z"], rtol=1e-8)
