@@ -95,8 +95,9 @@ int peec_set_rows(peec_ctx* ctx, const double* const rows[9]);
  * compute_FFT_mutual_coupling_mats with QS_Rcc_FW == 1. origin is the mesh
  * origin (unscaled, as the reference passes it), s* the escaled cell sizes.
  * rows_out may be NULL, or hold nine host buffers (or NULL entries) that receive
- * the rows. Returns PEEC_ERR_UNSUPPORTED if an entry needs a far-field
- * (suppressed) branch of the reference integrals.
+ * the rows. Every branch of the reference's integral dispatch is evaluated,
+ * the far-field (suppressed) ones included. Returns PEEC_ERR_UNSUPPORTED if an
+ * entry comes out non-finite (degenerate cell sizes).
  */
 int peec_fill(peec_ctx* ctx, const double origin[3], double sx, double sy, double sz,
               double escal_Lp, double escal_P, double* const rows_out[9]);

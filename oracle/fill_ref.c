@@ -9,19 +9,22 @@
  *
  * Follows:
  *   src/lib/solverFFT/compute_Lp_Voxels.jl:1-63    row driver (round_ud_fft :807)
- *   src/lib/solverFFT/compute_Lp_Voxels.jl:65-306  Integ_vol_vol_fft dispatch
+ *   src/lib/solverFFT/compute_Lp_Voxels.jl:65-435  Integ_vol_vol_fft dispatch
  *   src/lib/solverFFT/compute_Lp_Voxels.jl:437-447 check_condition_fft
- *   src/lib/solverFFT/compute_Lp_Voxels.jl:766-805 integ_vol_vol_fft
+ *   src/lib/solverFFT/compute_Lp_Voxels.jl:449-805 primitives (integ_*_fft)
  *   src/lib/solverFFT/compute_row_P_sup.jl:1-104   row driver (caser/caser2)
  *   src/lib/solverFFT/compute_row_P_sup.jl:106-381 Integ_sup_sup_P dispatch
  *   src/lib/solverFFT/compute_row_P_sup.jl:383-394 check_condition_P_P
- *   src/lib/solverFFT/compute_row_P_sup.jl:557-590 integ_surf_surf_ortho_P
+ *   src/lib/solverFFT/compute_row_P_sup.jl:396-590 primitives (integ_*_P)
  *   src/lib/solverFFT/compute_Lp_Voxels_QS.jl:695-730 integ_surf_surf_para
- * Only the near-field branches (no suppression: volume-volume for Lp,
- * surface-surface for P) are restated; an entry whose suppression test fires is
- * returned as NaN and counted, so a caller can never take a far-field entry from
- * here silently. On uniform voxels the suppression tests need centre distances
- * above ~200 voxel edges, beyond every grid the tests and benchmarks use.
+ * Every branch of both dispatches is restated, including the far-field ones that
+ * replace a body by a surface, a line or a point once a dimension passes its
+ * suppression test (on uniform voxels: centre distances beyond ~200 edges of that
+ * dimension), together with their quirks: the 1e-8 nudges of integ_line_point, the
+ * origin-dependent collinear line formulas integ_line_line_sp_fft / _P, the 3-term
+ * integ_line_surf_ortho_fft and the 4-term integ_surf_surf_ortho_fft. A mode flag
+ * turns the suppression off (every entry by its full closed form), which the
+ * known-answer tests evaluate in long double as the accurate far-field value.
  *
  * Besides the value each entry also returns the sum of |terms| of its closed
  * form (times the same prefactor): the cancellation-aware scale for error bounds.
@@ -116,9 +119,285 @@ static REAL vol_vol(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REA
   return sol;
 }
 
-/* Integ_vol_vol_fft suppression tests; returns the number of suppressed dims */
-static int lp_supp(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REAL* x2v,
-                   const REAL* y2v, const REAL* z2v) {
+/* ---------------------------------------------------------------------------------
+ * Closed-form primitives of the dispatch. Each returns the signed corner sum and adds
+ * sum |term| to *acc. Corner signs: the reference's (-1)^(c1+...+cn [+1]) with 1-based
+ * corner indices; with 0-based ones that is (-1)^(sum + n [+1]).
+ * --------------------------------------------------------------------------------- */
+
+/* integ_line_point_fft / _P (compute_Lp_Voxels.jl:449-467, compute_row_P_sup.jl:396-414):
+ * line x in [x3, x4] at (y3, z3), point (x1, y1, z1) */
+static REAL line_point(const REAL* xv, REAL y3, REAL z3, REAL x1, REAL y1, REAL z1, REAL* acc) {
+  REAL x3 = xv[0], x4 = xv[1];
+  REAL chk = (REAL)1 / (x1 - x3);
+  if (isnan(chk) || isinf(chk)) x1 = x1 - (REAL)1e-8;
+  chk = (REAL)1 / (x1 - x4);
+  if (isnan(chk) || (isinf(chk) && x1 > 0)) x1 = x1 + (REAL)1e-8;
+  REAL R1 = SQRT((x1 - x3) * (x1 - x3) + (y1 - y3) * (y1 - y3) + (z1 - z3) * (z1 - z3));
+  REAL R2 = SQRT((x1 - x4) * (x1 - x4) + (y1 - y3) * (y1 - y3) + (z1 - z3) * (z1 - z3));
+  REAL l1 = LOG((x1 - x3) + R1), l2 = LOG((x1 - x4) + R2);
+  REAL Ip = l1 - l2;
+  if (!ISFIN(Ip)) {
+    l1 = (x1 - x3) / FABS(x1 - x3) * LOG(FABS(x1 - x3));
+    l2 = (x1 - x4) / FABS(x1 - x4) * LOG(FABS(x1 - x4));
+    Ip = l1 - l2;
+  }
+  *acc += FABS(l1) + FABS(l2);
+  return Ip;
+}
+
+/* integ_point_sup_fft / _P (compute_Lp_Voxels.jl:469-489): point, surface in the
+ * (x, y) plane at z2 */
+static REAL point_sup(REAL x1, REAL y1, REAL z1, const REAL* x2v, const REAL* y2v, REAL z2,
+                      REAL* acc) {
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2) {
+      REAL X = x1 - x2v[c1], Y = y1 - y2v[c2], Z = z1 - z2;
+      REAL R = SQRT(X * X + Y * Y + Z * Z);
+      REAL t1 = fin(X * lg(Y + R));
+      REAL t2 = fin(Y * lg(X + R));
+      REAL t3 = -FABS(Z) * ATAN2(X * Y, FABS(Z) * R);
+      sol += sgnp(c1 + c2) * (t1 + t2 + t3);
+      *acc += FABS(t1) + FABS(t2) + FABS(t3);
+    }
+  return sol;
+}
+
+/* integ_line_line_sp_fft (compute_Lp_Voxels.jl:514-529) and integ_line_line_sp_P
+ * (compute_row_P_sup.jl:461-476), collinear lines. As the reference writes them these
+ * take absolute coordinates, not differences; pform selects the _P variant's extra
+ * x1*log|x1-x2| term. */
+static REAL ll_sp(const REAL* x1v, const REAL* x2v, int pform, REAL* acc) {
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2) {
+      REAL x1 = x1v[c1], x2 = x2v[c2];
+      REAL R = SQRT((x1 - x2) * (x1 - x2));
+      REAL t1 = (x1 - x2) / R * (x1 - x2 * lg(x2 - x1));
+      if (pform) t1 = t1 + x1 * lg(x1 - x2);
+      t1 = fin(t1);
+      sol += sgnp(c1 + c2 + 1) * t1;
+      *acc += FABS(t1);
+    }
+  return sol;
+}
+
+/* integ_line_line_parall_fft / _P (compute_Lp_Voxels.jl:491-512, compute_row_P_sup.jl:438-459) */
+static REAL ll_parall(const REAL* x1v, REAL y1, REAL z1, const REAL* x2v, REAL y2, REAL z2,
+                      int pform, REAL* acc) {
+  REAL dy = y1 - y2, dz = z1 - z2;
+  if (FABS(dy) < (REAL)1e-10 && FABS(dz) < (REAL)1e-10) return ll_sp(x1v, x2v, pform, acc);
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2) {
+      REAL X = x1v[c1] - x2v[c2];
+      REAL R = SQRT(X * X + dy * dy + dz * dz);
+      REAL t1 = fin(X * lg(X + R));
+      sol += sgnp(c1 + c2 + 1) * (t1 - R);
+      *acc += FABS(t1) + R;
+    }
+  return sol;
+}
+
+/* integ_line_line_ortho_xy_fft / _P (compute_Lp_Voxels.jl:531-551): line along x
+ * at (y1, z1), line along y at (x2, z2) */
+static REAL ll_ortho(const REAL* x1v, REAL y1, REAL z1, REAL x2, const REAL* y2v, REAL z2,
+                     REAL* acc) {
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2) {
+      REAL X = x1v[c1] - x2, Y = y1 - y2v[c2], Z = z1 - z2;
+      REAL R = SQRT(X * X + Y * Y + Z * Z);
+      REAL t1 = fin(X * lg(Y + R));
+      REAL t2 = fin(Y * lg(X + R));
+      REAL t3 = -FABS(Z) * ATAN2(X * Y, FABS(Z) * R);
+      sol += sgnp(c1 + c2 + 1) * (t1 + t2 + t3);
+      *acc += FABS(t1) + FABS(t2) + FABS(t3);
+    }
+  return sol;
+}
+
+/* the six-term triple antiderivative shared by integ_point_vol_fft
+ * (compute_Lp_Voxels.jl:553-582) and integ_line_surf_ortho_P (compute_row_P_sup.jl:500-529) */
+static REAL f111(REAL X, REAL Y, REAL Z, REAL* acc) {
+  REAL R = SQRT(X * X + Y * Y + Z * Z);
+  REAL t1 = fin(Y * Z * lg(X + R));
+  REAL t2 = fin(X * Z * lg(Y + R));
+  REAL t3 = fin(Y * X * lg(Z + R));
+  REAL t4 = -(REAL)0.5 * FABS(Z) * Z * ATAN2(X * Y, FABS(Z) * R);
+  REAL t5 = -(REAL)0.5 * FABS(Y) * Y * ATAN2(X * Z, FABS(Y) * R);
+  REAL t6 = -(REAL)0.5 * FABS(X) * X * ATAN2(Y * Z, FABS(X) * R);
+  *acc += FABS(t1) + FABS(t2) + FABS(t3) + FABS(t4) + FABS(t5) + FABS(t6);
+  return t1 + t2 + t3 + t4 + t5 + t6;
+}
+
+/* integ_point_vol_fft: point, volume */
+static REAL point_vol(REAL x1, REAL y1, REAL z1, const REAL* x2v, const REAL* y2v,
+                      const REAL* z2v, REAL* acc) {
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2)
+      for (int c3 = 0; c3 < 2; ++c3)
+        sol += sgnp(c1 + c2 + c3) * f111(x1 - x2v[c1], y1 - y2v[c2], z1 - z2v[c3], acc);
+  return sol;
+}
+
+/* integ_line_surf_ortho_fft (compute_Lp_Voxels.jl:584-607; three terms as written there)
+ * and integ_line_surf_ortho_P (pform): line along x at (y1, z1), surface in the
+ * (y, z) plane at x2 */
+static REAL ls_ortho(const REAL* x1v, REAL y1, REAL z1, REAL x2, const REAL* y2v,
+                     const REAL* z2v, int pform, REAL* acc) {
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2)
+      for (int c3 = 0; c3 < 2; ++c3) {
+        REAL X = x1v[c1] - x2, Y = y1 - y2v[c2], Z = z1 - z2v[c3];
+        REAL v;
+        if (pform) {
+          v = f111(X, Y, Z, acc);
+        } else {
+          REAL R = SQRT(X * X + Y * Y + Z * Z);
+          REAL t1 = fin(Y * Z * lg(X + R));
+          REAL t2 = fin(X * Z * lg(Y + R));
+          REAL t3 = -FABS(Z) * ATAN2(X * Y, FABS(Z) * R);
+          *acc += FABS(t1) + FABS(t2) + FABS(t3);
+          v = t1 + t2 + t3;
+        }
+        sol += sgnp(c1 + c2 + c3 + 1) * v;
+      }
+  return sol;
+}
+
+/* integ_line_surf_para_fft / _P (compute_Lp_Voxels.jl:609-633): surface in the (x, y)
+ * plane at z1, line along x at (y2, z2) */
+static REAL ls_para(const REAL* x1v, const REAL* y1v, REAL z1, const REAL* x2v, REAL y2, REAL z2,
+                    REAL* acc) {
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2)
+      for (int c3 = 0; c3 < 2; ++c3) {
+        REAL X = x1v[c1] - x2v[c3], Y = y1v[c2] - y2, Z = z1 - z2;
+        REAL R = SQRT(X * X + Y * Y + Z * Z);
+        REAL t1 = fin(X * Y * lg(X + R));
+        REAL t2 = fin((X * X - Z * Z) / 2 * lg(Y + R));
+        REAL t3 = -X * FABS(Z) * ATAN2(X * Y, FABS(Z) * R);
+        REAL t4 = -Y / 2 * R;
+        sol += sgnp(c1 + c2 + c3 + 3 + 1) * (t1 + t2 + t3 + t4);
+        *acc += FABS(t1) + FABS(t2) + FABS(t3) + FABS(t4);
+      }
+  return sol;
+}
+
+/* integ_line_vol_fft (compute_Lp_Voxels.jl:635-668): volume, line along x at (y2, z2) */
+static REAL line_vol(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REAL* x2v, REAL y2,
+                     REAL z2, REAL* acc) {
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2)
+      for (int c3 = 0; c3 < 2; ++c3)
+        for (int c4 = 0; c4 < 2; ++c4) {
+          REAL X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2, Z = z1v[c3] - z2;
+          REAL R = SQRT(X * X + Y * Y + Z * Z);
+          REAL t1 = -(REAL)1 / 3 * Y * Z * R;
+          REAL t2 = -(REAL)0.5 * X * FABS(Z) * Z * ATAN2(X * Y, FABS(Z) * R);
+          REAL t3 = -(REAL)0.5 * X * FABS(Y) * Y * ATAN2(X * Z, FABS(Y) * R);
+          REAL t4 = -(REAL)1 / 6 * (FABS(X) * FABS(X) * FABS(X)) * ATAN2(Y * Z, FABS(X) * R);
+          REAL t5 = fin(X * Y * Z * lg(X + R));
+          REAL t6 = fin(((REAL)0.5 * (X * X) - (REAL)1 / 6 * (Z * Z)) * Z * lg(Y + R));
+          REAL t7 = fin(((REAL)0.5 * (X * X) - (REAL)1 / 6 * (Y * Y)) * Y * lg(Z + R));
+          sol += sgnp(c1 + c2 + c3 + c4 + 1) * (t1 + t2 + t3 + t4 + t5 + t6 + t7);
+          *acc += FABS(t1) + FABS(t2) + FABS(t3) + FABS(t4) + FABS(t5) + FABS(t6) + FABS(t7);
+        }
+  return sol;
+}
+
+/* integ_surf_surf_para_fft (compute_Lp_Voxels.jl:670-697) = integ_surf_surf_para
+ * (compute_Lp_Voxels_QS.jl:695-730): surfaces in (x, y) planes at z1, z2 */
+static REAL ss_para(const REAL* x1v, const REAL* y1v, REAL z1, const REAL* x2v, const REAL* y2v,
+                    REAL z2, REAL* acc) {
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2)
+      for (int c3 = 0; c3 < 2; ++c3)
+        for (int c4 = 0; c4 < 2; ++c4) {
+          REAL X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2v[c3], Z = z1 - z2;
+          REAL R = SQRT(X * X + Y * Y + Z * Z);
+          REAL t1 = -(REAL)1 / 6 * (X * X + Y * Y - 2 * Z * Z) * R;
+          REAL t2 = -X * Y * FABS(Z) * ATAN2(X * Y, FABS(Z) * R);
+          REAL t3 = fin((REAL)0.5 * (X * X - Z * Z) * Y * lg(Y + R));
+          REAL t4 = fin((REAL)0.5 * (Y * Y - Z * Z) * X * lg(X + R));
+          sol += sgnp(c1 + c2 + c3 + c4) * (t1 + t2 + t3 + t4);
+          *acc += FABS(t1) + FABS(t2) + FABS(t3) + FABS(t4);
+        }
+  return sol;
+}
+
+/* integ_surf_surf_ortho_P (compute_row_P_sup.jl:557-590, seven terms) and, with
+ * pform == 0, integ_surf_surf_ortho_fft (compute_Lp_Voxels.jl:699-726, four terms as
+ * written there): surface in the (x, y) plane at z1, surface in the (x, z) plane at y2 */
+static REAL ss_ortho(const REAL* x1v, const REAL* y1v, REAL z1, const REAL* x2v, REAL y2,
+                     const REAL* z2v, int pform, REAL* acc) {
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2)
+      for (int c3 = 0; c3 < 2; ++c3)
+        for (int c4 = 0; c4 < 2; ++c4) {
+          REAL X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2, Z = z1 - z2v[c3];
+          REAL R = SQRT(X * X + Y * Y + Z * Z);
+          REAL t1 = -(REAL)1 / 3 * Y * Z * R;
+          REAL t2 = -(REAL)0.5 * X * FABS(Z) * Z * ATAN2(X * Y, FABS(Z) * R);
+          REAL s, a;
+          if (pform) {
+            REAL t3 = -(REAL)0.5 * X * FABS(Y) * Y * ATAN2(X * Z, FABS(Y) * R);
+            REAL t4 = -(REAL)1 / 6 * FABS(X) * X * X * ATAN2(Y * Z, FABS(X) * R);
+            REAL t5 = fin(X * Y * Z * lg(X + R));
+            REAL t6 = fin(((REAL)0.5 * X * X - (REAL)1 / 6 * Z * Z) * Z * lg(Y + R));
+            REAL t7 = fin(((REAL)0.5 * X * X - (REAL)1 / 6 * Y * Y) * Y * lg(Z + R));
+            s = t1 + t2 + t3 + t4 + t5 + t6 + t7;
+            a = FABS(t1) + FABS(t2) + FABS(t3) + FABS(t4) + FABS(t5) + FABS(t6) + FABS(t7);
+          } else {
+            REAL t3 = fin((REAL)0.5 * (X * X - Z * Z) * Y * lg(Y + R));
+            REAL t4 = fin((REAL)0.5 * (X * X - Y * Y) * X * lg(X + R));
+            s = t1 + t2 + t3 + t4;
+            a = FABS(t1) + FABS(t2) + FABS(t3) + FABS(t4);
+          }
+          sol += sgnp(c1 + c2 + c3 + c4) * s;
+          *acc += a;
+        }
+  return sol;
+}
+
+/* integ_vol_surf_fft (compute_Lp_Voxels.jl:728-764): volume, surface in the (x, y)
+ * plane at z2 */
+static REAL vol_surf(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REAL* x2v,
+                     const REAL* y2v, REAL z2, REAL* acc) {
+  REAL sol = 0;
+  for (int c1 = 0; c1 < 2; ++c1)
+    for (int c2 = 0; c2 < 2; ++c2)
+      for (int c3 = 0; c3 < 2; ++c3)
+        for (int c4 = 0; c4 < 2; ++c4)
+          for (int c5 = 0; c5 < 2; ++c5) {
+            REAL X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2v[c5], Z = z1v[c3] - z2;
+            REAL X2 = X * X, Y2 = Y * Y, Z2 = Z * Z;
+            REAL R = SQRT(X2 + Y2 + Z2);
+            REAL t1 = (Z2 / 12 - (X2 + Y2) / 8) * Z * R;
+            REAL t2 = fin((Y2 / 2 - Z2 / 6) * X * lg(X + R));
+            REAL t3 = fin((X2 / 2 - Z2 / 6) * Y * lg(Y + R));
+            REAL t4 = fin((-(X2 * X2) / 24 - (Y2 * Y2) / 24 + (Y2 * X2) / 4) * lg(Z + R));
+            REAL t5 = -(FABS(X) * FABS(X) * FABS(X)) * Y / 6 * ATAN2(Y * Z, FABS(X) * R);
+            REAL t6 = -X * (FABS(Y) * FABS(Y) * FABS(Y)) / 6 * ATAN2(X * Z, FABS(Y) * R);
+            REAL t7 = -X * Y * FABS(Z) * Z / 2 * ATAN2(X * Y, FABS(Z) * R);
+            sol += sgnp(c1 + c2 + c3 + c4 + c5 + 5) * (t1 + t2 + t3 + t4 + t5 + t6 + t7);
+            *acc += FABS(t1) + FABS(t2) + FABS(t3) + FABS(t4) + FABS(t5) + FABS(t6) + FABS(t7);
+          }
+  return sol;
+}
+
+/* Integ_vol_vol_fft suppression flags (compute_Lp_Voxels.jl:86-172): s1[d] / s2[d] set
+ * when dimension d (x, y, z) of voxel 1 / 2 is suppressed */
+static void lp_supp(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REAL* x2v,
+                    const REAL* y2v, const REAL* z2v, int* s1, int* s2) {
   const REAL e1 = 5e-3, e2 = 1e-3, e3 = 1e-3, e4 = 3e-1;
   REAL a1 = FABS(x1v[1] - x1v[0]), b1 = FABS(y1v[1] - y1v[0]), c1 = FABS(z1v[1] - z1v[0]);
   REAL a2 = FABS(x2v[1] - x2v[0]), b2 = FABS(y2v[1] - y2v[0]), c2 = FABS(z2v[1] - z2v[0]);
@@ -131,40 +410,195 @@ static int lp_supp(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REAL
   REAL min_R = SQRT(mx * mx + my * my + mz * mz);
   REAL dx = maxabs4(ax[0], ax[1], ax[2], ax[3]), dy = maxabs4(ay[0], ay[1], ay[2], ay[3]),
        dz = maxabs4(az[0], az[1], az[2], az[3]);
-  int s = 0;
   for (int side = 0; side < 2; ++side) {
     REAL a = side ? a2 : a1, b = side ? b2 : b1, c = side ? c2 : c1;
-    int sx = 0, sy = 0, sz = 0;
+    int* s = side ? s2 : s1;
+    s[0] = s[1] = s[2] = 0;
     if (a <= b && a <= c) {
-      sx = check_fft(e1, e2, e3, V1, V2, dx, min_R, a, b, c);
-      if (sx && (b > c ? b : c) / (min_R + (REAL)1e-15) < e4) {
-        sy = check_fft(e1, e2, e3, V1, V2, dy, min_R, b, a, c);
-        sz = check_fft(e1, e2, e3, V1, V2, dz, min_R, c, a, b);
+      s[0] = check_fft(e1, e2, e3, V1, V2, dx, min_R, a, b, c);
+      if (s[0] && (b > c ? b : c) / (min_R + (REAL)1e-15) < e4) {
+        s[1] = check_fft(e1, e2, e3, V1, V2, dy, min_R, b, a, c);
+        s[2] = check_fft(e1, e2, e3, V1, V2, dz, min_R, c, a, b);
       }
     } else if (b <= a && b <= c) {
-      sy = check_fft(e1, e2, e3, V1, V2, dy, min_R, b, a, c);
-      if (sy && (a > c ? a : c) / (min_R + (REAL)1e-15) < e4) {
-        sx = check_fft(e1, e2, e3, V1, V2, dx, min_R, a, b, c);
-        sz = check_fft(e1, e2, e3, V1, V2, dz, min_R, c, a, b);
+      s[1] = check_fft(e1, e2, e3, V1, V2, dy, min_R, b, a, c);
+      if (s[1] && (a > c ? a : c) / (min_R + (REAL)1e-15) < e4) {
+        s[0] = check_fft(e1, e2, e3, V1, V2, dx, min_R, a, b, c);
+        s[2] = check_fft(e1, e2, e3, V1, V2, dz, min_R, c, a, b);
       }
     } else {
-      sz = check_fft(e1, e2, e3, V1, V2, dz, min_R, c, a, b);
-      if (sz && (a > b ? a : b) / (min_R + (REAL)1e-15) < e4) {
-        sx = check_fft(e1, e2, e3, V1, V2, dx, min_R, a, b, c);
-        sy = check_fft(e1, e2, e3, V1, V2, dy, min_R, b, a, c);
+      s[2] = check_fft(e1, e2, e3, V1, V2, dz, min_R, c, a, b);
+      if (s[2] && (a > b ? a : b) / (min_R + (REAL)1e-15) < e4) {
+        s[0] = check_fft(e1, e2, e3, V1, V2, dx, min_R, a, b, c);
+        s[1] = check_fft(e1, e2, e3, V1, V2, dy, min_R, b, a, c);
       }
     }
-    s += sx + sy + sz;
   }
-  return s;
+}
+
+/* The case tree shared by Integ_vol_vol_fft (compute_Lp_Voxels.jl:172-433) and
+ * Integ_sup_sup_P (compute_row_P_sup.jl:175-379): the integral of 1/R over two boxes
+ * (intervals x1v.., centres xc1.., edge lengths a1..) of which the dimensions flagged in
+ * s1 / s2 are collapsed, each collapsed length entering as a factor. The P tree has no
+ * volume cases, calls the _P primitives (pform = 1) and passes unit lengths for the
+ * face normals. */
+static REAL integ_bodies(const REAL* x1v, const REAL* y1v, const REAL* z1v, REAL xc1, REAL yc1,
+                         REAL zc1, REAL a1, REAL b1, REAL c1, const REAL* x2v, const REAL* y2v,
+                         const REAL* z2v, REAL xc2, REAL yc2, REAL zc2, REAL a2, REAL b2,
+                         REAL c2, const int* s1, const int* s2, int pform, REAL* acc) {
+  REAL V1 = a1 * b1 * c1, V2 = a2 * b2 * c2;
+  int n1 = s1[0] + s1[1] + s1[2], n2 = s2[0] + s2[1] + s2[2];
+  int sum = n1 + n2;
+  REAL w = 0;
+  *acc = 0;
+  switch (sum) {
+    case 6: { /* point-point */
+      REAL d = SQRT((xc1 - xc2) * (xc1 - xc2) + (yc1 - yc2) * (yc1 - yc2) + (zc1 - zc2) * (zc1 - zc2));
+      *acc = V1 * V2 / d;
+      return V1 * V2 / d;
+    }
+    case 5: { /* point-line */
+      REAL v;
+      if (n1 == 3) {
+        if (!s2[0]) { w = V1 * V2 / a2; v = line_point(x2v, yc2, zc2, xc1, yc1, zc1, acc); }
+        else if (!s2[1]) { w = V1 * V2 / b2; v = line_point(y2v, xc2, zc2, yc1, xc1, zc1, acc); }
+        else { w = V1 * V2 / c2; v = line_point(z2v, xc2, yc2, zc1, xc1, yc1, acc); }
+      } else {
+        if (!s1[0]) { w = V1 * V2 / a1; v = line_point(x1v, yc1, zc1, xc2, yc2, zc2, acc); }
+        else if (!s1[1]) { w = V1 * V2 / b1; v = line_point(y1v, xc1, zc1, yc2, xc2, zc2, acc); }
+        else { w = V1 * V2 / c1; v = line_point(z1v, xc1, yc1, zc2, xc2, yc2, acc); }
+      }
+      *acc *= FABS(w);
+      return w * v;
+    }
+    case 4: {
+      REAL v;
+      if (n1 == 3) { /* point-surface */
+        if (s2[0]) { w = V1 * a2; v = point_sup(zc1, yc1, xc1, z2v, y2v, xc2, acc); }
+        else if (s2[1]) { w = V1 * b2; v = point_sup(xc1, zc1, yc1, x2v, z2v, yc2, acc); }
+        else { w = V1 * c2; v = point_sup(xc1, yc1, zc1, x2v, y2v, zc2, acc); }
+      } else if (n2 == 3) {
+        if (s1[0]) { w = V2 * a1; v = point_sup(zc2, yc2, xc2, z1v, y1v, xc1, acc); }
+        else if (s1[1]) { w = V2 * b1; v = point_sup(xc2, zc2, yc2, x1v, z1v, yc1, acc); }
+        else { w = V2 * c1; v = point_sup(xc2, yc2, zc2, x1v, y1v, zc1, acc); }
+      } else if (s1[1] && s1[2]) { /* line-line, line 1 along x */
+        if (s2[1] && s2[2]) { w = b1 * c1 * b2 * c2; v = ll_parall(x1v, yc1, zc1, x2v, yc2, zc2, pform, acc); }
+        else if (s2[0] && s2[2]) { w = b1 * c1 * a2 * c2; v = ll_ortho(x1v, yc1, zc1, xc2, y2v, zc2, acc); }
+        else { w = b1 * c1 * a2 * b2; v = ll_ortho(x1v, zc1, yc1, xc2, z2v, yc2, acc); }
+      } else if (s1[0] && s1[2]) { /* line 1 along y */
+        if (s2[0] && s2[2]) { w = a1 * c1 * a2 * c2; v = ll_parall(y1v, xc1, zc1, y2v, xc2, zc2, pform, acc); }
+        else if (s2[0] && s2[1]) { w = a1 * c1 * a2 * b2; v = ll_ortho(y1v, zc1, xc1, yc2, z2v, xc2, acc); }
+        else { w = a1 * c1 * b2 * c2; v = ll_ortho(y1v, xc1, zc1, yc2, x2v, zc2, acc); }
+      } else { /* line 1 along z */
+        if (s2[0] && s2[1]) { w = a1 * b1 * a2 * b2; v = ll_parall(z1v, xc1, yc1, z2v, xc2, yc2, pform, acc); }
+        else if (s2[0] && s2[2]) { w = a1 * b1 * a2 * c2; v = ll_ortho(z1v, yc1, xc1, zc2, y2v, xc2, acc); }
+        else { w = a1 * b1 * b2 * c2; v = ll_ortho(z1v, xc1, yc1, zc2, x2v, yc2, acc); }
+      }
+      *acc *= FABS(w);
+      return w * v;
+    }
+    case 3: {
+      REAL v;
+      if (n1 == 3) { w = a1 * b1 * c1; v = point_vol(xc1, yc1, zc1, x2v, y2v, z2v, acc); }
+      else if (n2 == 3) { w = a2 * b2 * c2; v = point_vol(xc2, yc2, zc2, x1v, y1v, z1v, acc); }
+      else if (n1 == 1) { /* surface 1, line 2 */
+        if (s1[0]) {
+          if (!s2[0]) { w = a1 * b2 * c2; v = ls_ortho(x2v, yc2, zc2, xc1, y1v, z1v, pform, acc); }
+          else if (!s2[1]) { w = a1 * a2 * c2; v = ls_para(y1v, z1v, xc1, y2v, zc2, xc2, acc); }
+          else { w = a1 * a2 * b2; v = ls_para(z1v, y1v, xc1, z2v, yc2, xc2, acc); }
+        } else if (s1[1]) {
+          if (!s2[0]) { w = b1 * b2 * c2; v = ls_para(x1v, z1v, yc1, x2v, zc2, yc2, acc); }
+          else if (!s2[1]) { w = b1 * a2 * c2; v = ls_ortho(y2v, xc2, zc2, yc1, x1v, z1v, pform, acc); }
+          else { w = b1 * a2 * b2; v = ls_para(z1v, x1v, yc1, z2v, xc2, yc2, acc); }
+        } else {
+          if (!s2[0]) { w = c1 * b2 * c2; v = ls_para(x1v, y1v, zc1, x2v, yc2, zc2, acc); }
+          else if (!s2[1]) { w = c1 * a2 * c2; v = ls_para(y1v, x1v, zc1, y2v, xc2, zc2, acc); }
+          else { w = c1 * a2 * b2; v = ls_ortho(z2v, xc2, yc2, zc1, x1v, y1v, pform, acc); }
+        }
+      } else { /* surface 2, line 1 */
+        if (s2[0]) {
+          if (!s1[0]) { w = a2 * b1 * c1; v = ls_ortho(x1v, yc1, zc1, xc2, y2v, z2v, pform, acc); }
+          else if (!s1[1]) { w = a2 * a1 * c1; v = ls_para(y2v, z2v, xc2, y1v, zc1, xc1, acc); }
+          else { w = a2 * a1 * b1; v = ls_para(z2v, y2v, xc2, z1v, yc1, xc1, acc); }
+        } else if (s2[1]) {
+          if (!s1[0]) { w = b2 * b1 * c1; v = ls_para(x2v, z2v, yc2, x1v, zc1, yc1, acc); }
+          else if (!s1[1]) { w = b2 * a1 * c1; v = ls_ortho(y1v, xc1, zc1, yc2, x2v, z2v, pform, acc); }
+          else { w = b2 * a1 * b1; v = ls_para(z2v, x2v, yc2, z1v, xc1, yc1, acc); }
+        } else {
+          if (!s1[0]) { w = c2 * b1 * c1; v = ls_para(x2v, y2v, zc2, x1v, yc1, zc1, acc); }
+          else if (!s1[1]) { w = c2 * a1 * c1; v = ls_para(y2v, x2v, zc2, y1v, xc1, zc1, acc); }
+          else { w = c2 * a1 * b1; v = ls_ortho(z1v, xc1, yc1, zc2, x2v, y2v, pform, acc); }
+        }
+      }
+      *acc *= FABS(w);
+      return w * v;
+    }
+    case 2: {
+      REAL v;
+      if (n1 == 2) { /* line 1, volume 2 */
+        if (!s1[0]) { w = b1 * c1; v = line_vol(x2v, y2v, z2v, x1v, yc1, zc1, acc); }
+        else if (!s1[1]) { w = a1 * c1; v = line_vol(y2v, x2v, z2v, y1v, xc1, zc1, acc); }
+        else { w = a1 * b1; v = line_vol(z2v, x2v, y2v, z1v, xc1, yc1, acc); }
+      } else if (n2 == 2) {
+        if (!s2[0]) { w = b2 * c2; v = line_vol(x1v, y1v, z1v, x2v, yc2, zc2, acc); }
+        else if (!s2[1]) { w = a2 * c2; v = line_vol(y1v, x1v, z1v, y2v, xc2, zc2, acc); }
+        else { w = a2 * b2; v = line_vol(z1v, x1v, y1v, z2v, xc2, yc2, acc); }
+      } else if (s1[0]) { /* surface-surface, surface 1 in the yz plane */
+        if (s2[0]) { w = a1 * a2; v = ss_para(y1v, z1v, xc1, y2v, z2v, xc2, acc); }
+        else if (s2[1]) { w = a1 * b2; v = ss_ortho(z1v, y1v, xc1, z2v, yc2, x2v, pform, acc); }
+        else { w = a1 * c2; v = ss_ortho(y1v, z1v, xc1, y2v, zc2, x2v, pform, acc); }
+      } else if (s1[1]) {
+        if (s2[0]) { w = b1 * a2; v = ss_ortho(z1v, x1v, yc1, z2v, xc2, y2v, pform, acc); }
+        else if (s2[1]) { w = b1 * b2; v = ss_para(x1v, z1v, yc1, x2v, z2v, yc2, acc); }
+        else { w = b1 * c2; v = ss_ortho(x1v, z1v, yc1, x2v, zc2, y2v, pform, acc); }
+      } else {
+        if (s2[0]) { w = c1 * a2; v = ss_ortho(y1v, x1v, zc1, y2v, xc2, z2v, pform, acc); }
+        else if (s2[1]) { w = c1 * b2; v = ss_ortho(x1v, y1v, zc1, x2v, yc2, z2v, pform, acc); }
+        else { w = c1 * c2; v = ss_para(x1v, y1v, zc1, x2v, y2v, zc2, acc); }
+      }
+      *acc *= FABS(w);
+      return w * v;
+    }
+    case 1: {
+      REAL v;
+      if (s1[0]) { w = a1; v = vol_surf(y2v, z2v, x2v, y1v, z1v, xc1, acc); }
+      else if (s1[1]) { w = b1; v = vol_surf(x2v, z2v, y2v, x1v, z1v, yc1, acc); }
+      else if (s1[2]) { w = c1; v = vol_surf(x2v, y2v, z2v, x1v, y1v, zc1, acc); }
+      else if (s2[0]) { w = a2; v = vol_surf(y1v, z1v, x1v, y2v, z2v, xc2, acc); }
+      else if (s2[1]) { w = b2; v = vol_surf(x1v, z1v, y1v, x2v, z2v, yc2, acc); }
+      else { w = c2; v = vol_surf(x1v, y1v, z1v, x2v, y2v, zc2, acc); }
+      *acc *= FABS(w);
+      return w * v;
+    }
+    default:
+      return vol_vol(x1v, y1v, z1v, x2v, y2v, z2v, acc);
+  }
+}
+
+/* Integ_vol_vol_fft (compute_Lp_Voxels.jl:65-435). *far = 1 when a suppressed branch
+ * was taken; suppress == 0 skips the tests (the full volume-volume form). */
+static REAL lp_integ(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REAL* x2v,
+                     const REAL* y2v, const REAL* z2v, int suppress, REAL* acc, int* far) {
+  REAL xc1 = (REAL)0.5 * (x1v[0] + x1v[1]), yc1 = (REAL)0.5 * (y1v[0] + y1v[1]),
+       zc1 = (REAL)0.5 * (z1v[0] + z1v[1]);
+  REAL xc2 = (REAL)0.5 * (x2v[0] + x2v[1]), yc2 = (REAL)0.5 * (y2v[0] + y2v[1]),
+       zc2 = (REAL)0.5 * (z2v[0] + z2v[1]);
+  REAL a1 = FABS(x1v[1] - x1v[0]), b1 = FABS(y1v[1] - y1v[0]), c1 = FABS(z1v[1] - z1v[0]);
+  REAL a2 = FABS(x2v[1] - x2v[0]), b2 = FABS(y2v[1] - y2v[0]), c2 = FABS(z2v[1] - z2v[0]);
+  int s1[3] = {0, 0, 0}, s2[3] = {0, 0, 0};
+  if (suppress) lp_supp(x1v, y1v, z1v, x2v, y2v, z2v, s1, s2);
+  *far = s1[0] + s1[1] + s1[2] + s2[0] + s2[1] + s2[2] > 0;
+  return integ_bodies(x1v, y1v, z1v, xc1, yc1, zc1, a1, b1, c1, x2v, y2v, z2v, xc2, yc2, zc2, a2,
+                      b2, c2, s1, s2, 0, acc);
 }
 
 /* One Lp generating row: source centre src, targets centers[N][3] (row-major),
  * current direction dc = 1,2,3. out[k] = 1e-7/S * integral (compute_Lp_Voxels.jl:40-60),
  * scale[k] = the same prefactor times sum|terms|. Returns the count of entries
- * that needed a far-field branch (set to NaN). */
+ * that took a far-field (suppressed) branch. */
 int64_t FN(oracle_lp_row)(int dc, const double* src, const double* centers, int64_t N,
-                          double sx_, double sy_, double sz_, double* out, double* scale) {
+                          double sx_, double sy_, double sz_, int suppress, double* out,
+                          double* scale) {
   REAL sx = sx_, sy = sy_, sz = sz_;
   REAL S = sy * sz * sy * sz;
   if (dc == 2) S = sx * sz * sx * sz;
@@ -180,63 +614,14 @@ int64_t FN(oracle_lp_row)(int dc, const double* src, const double* centers, int6
     REAL x2v[2] = {round14(cx - sx / 2), round14(cx + sx / 2)};
     REAL y2v[2] = {round14(cy - sy / 2), round14(cy + sy / 2)};
     REAL z2v[2] = {round14(cz - sz / 2), round14(cz + sz / 2)};
-    if (lp_supp(x1v, y1v, z1v, x2v, y2v, z2v) != 0) {
-      out[k] = NAN;
-      if (scale) scale[k] = NAN;
-      bad += 1;
-      continue;
-    }
     REAL acc;
-    REAL v = vol_vol(x1v, y1v, z1v, x2v, y2v, z2v, &acc);
+    int far = 0;
+    REAL v = lp_integ(x1v, y1v, z1v, x2v, y2v, z2v, suppress, &acc, &far);
+    bad += far;
     out[k] = (double)((REAL)1e-7 / S * v);
     if (scale) scale[k] = (double)((REAL)1e-7 / S * acc);
   }
   return bad;
-}
-
-/* integ_surf_surf_para (compute_Lp_Voxels_QS.jl:695-730) */
-static REAL ss_para(const REAL* x1v, const REAL* y1v, REAL z1, const REAL* x2v, const REAL* y2v,
-                    REAL z2, REAL* abssum) {
-  REAL sol = 0, acc = 0;
-  for (int c1 = 0; c1 < 2; ++c1)
-    for (int c2 = 0; c2 < 2; ++c2)
-      for (int c3 = 0; c3 < 2; ++c3)
-        for (int c4 = 0; c4 < 2; ++c4) {
-          REAL X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2v[c3], Z = z1 - z2;
-          REAL R = SQRT(X * X + Y * Y + Z * Z);
-          REAL t1 = -(REAL)1 / 6 * (X * X + Y * Y - 2 * Z * Z) * R;
-          REAL t2 = -X * Y * FABS(Z) * ATAN2(X * Y, FABS(Z) * R);
-          REAL t3 = fin((REAL)0.5 * (X * X - Z * Z) * Y * lg(Y + R));
-          REAL t4 = fin((REAL)0.5 * (Y * Y - Z * Z) * X * lg(X + R));
-          sol += sgnp(c1 + c2 + c3 + c4) * (t1 + t2 + t3 + t4);
-          acc += FABS(t1) + FABS(t2) + FABS(t3) + FABS(t4);
-        }
-  *abssum = acc;
-  return sol;
-}
-
-/* integ_surf_surf_ortho_P (compute_row_P_sup.jl:557-590) */
-static REAL ss_ortho(const REAL* x1v, const REAL* y1v, REAL z1, const REAL* x2v, REAL y2,
-                     const REAL* z2v, REAL* abssum) {
-  REAL sol = 0, acc = 0;
-  for (int c1 = 0; c1 < 2; ++c1)
-    for (int c2 = 0; c2 < 2; ++c2)
-      for (int c3 = 0; c3 < 2; ++c3)
-        for (int c4 = 0; c4 < 2; ++c4) {
-          REAL X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2, Z = z1 - z2v[c3];
-          REAL R = SQRT(X * X + Y * Y + Z * Z);
-          REAL t1 = -(REAL)1 / 3 * Y * Z * R;
-          REAL t2 = -(REAL)0.5 * X * FABS(Z) * Z * ATAN2(X * Y, FABS(Z) * R);
-          REAL t3 = -(REAL)0.5 * X * FABS(Y) * Y * ATAN2(X * Z, FABS(Y) * R);
-          REAL t4 = -(REAL)1 / 6 * FABS(X) * X * X * ATAN2(Y * Z, FABS(X) * R);
-          REAL t5 = fin(X * Y * Z * lg(X + R));
-          REAL t6 = fin(((REAL)0.5 * X * X - (REAL)1 / 6 * Z * Z) * Z * lg(Y + R));
-          REAL t7 = fin(((REAL)0.5 * X * X - (REAL)1 / 6 * Y * Y) * Y * lg(Z + R));
-          sol += sgnp(c1 + c2 + c3 + c4) * (t1 + t2 + t3 + t4 + t5 + t6 + t7);
-          acc += FABS(t1) + FABS(t2) + FABS(t3) + FABS(t4) + FABS(t5) + FABS(t6) + FABS(t7);
-        }
-  *abssum = acc;
-  return sol;
 }
 
 static int check_pp(REAL e1, REAL e2, REAL e3, REAL e4, REAL S1, REAL S2, REAL max_d, REAL min_R,
@@ -250,16 +635,16 @@ static int check_pp(REAL e1, REAL e2, REAL e3, REAL e4, REAL S1, REAL S2, REAL m
   return (condS < e4 && (b <= e3 || f < e1) && a < e2) ? 1 : 0;
 }
 
-/* Integ_sup_sup_P restricted to the surface-surface branch; returns NaN (and
- * *unsup=1) when a suppression test fires. */
+/* Integ_sup_sup_P (compute_row_P_sup.jl:106-381): faces given by centre and extents
+ * (one extent 0: the face normal). *far = 1 when a suppressed branch was taken. */
 static REAL sup_sup(REAL xc1, REAL yc1, REAL zc1, REAL xc2, REAL yc2, REAL zc2, REAL a1, REAL b1,
-                    REAL c1, REAL a2, REAL b2, REAL c2, REAL* abssum, int* unsup) {
+                    REAL c1, REAL a2, REAL b2, REAL c2, int suppress, REAL* acc, int* far) {
   const REAL e1 = 5e-3, e2 = 1e-3, e3 = 1e-3, e4 = 3e-1;
   REAL x1v[2] = {xc1 - a1 / 2, xc1 + a1 / 2}, y1v[2] = {yc1 - b1 / 2, yc1 + b1 / 2},
        z1v[2] = {zc1 - c1 / 2, zc1 + c1 / 2};
   REAL x2v[2] = {xc2 - a2 / 2, xc2 + a2 / 2}, y2v[2] = {yc2 - b2 / 2, yc2 + b2 / 2},
        z2v[2] = {zc2 - c2 / 2, zc2 + c2 / 2};
-  int p1 = 2, p2 = 2; /* normal axis: 0 yz-plane, 1 xz-plane, 2 xy-plane */
+  int p1 = 2, p2 = 2; /* normal axis */
   if (a1 <= b1 && a1 <= c1) { p1 = 0; a1 = 1; }
   else if (b1 <= a1 && b1 <= c1) { p1 = 1; b1 = 1; }
   else { c1 = 1; }
@@ -267,42 +652,28 @@ static REAL sup_sup(REAL xc1, REAL yc1, REAL zc1, REAL xc2, REAL yc2, REAL zc2, 
   else if (b2 <= a2 && b2 <= c2) { p2 = 1; b2 = 1; }
   else { c2 = 1; }
   REAL s1 = a1 * b1 * c1, s2 = a2 * b2 * c2;
-  REAL ax[4] = {x1v[0] - x2v[0], x1v[0] - x2v[1], x1v[1] - x2v[0], x1v[1] - x2v[1]};
-  REAL ay[4] = {y1v[0] - y2v[0], y1v[0] - y2v[1], y1v[1] - y2v[0], y1v[1] - y2v[1]};
-  REAL az[4] = {z1v[0] - z2v[0], z1v[0] - z2v[1], z1v[1] - z2v[0], z1v[1] - z2v[1]};
-  REAL mx = minabs4(ax[0], ax[1], ax[2], ax[3]), my = minabs4(ay[0], ay[1], ay[2], ay[3]),
-       mz = minabs4(az[0], az[1], az[2], az[3]);
-  REAL min_R = SQRT(mx * mx + my * my + mz * mz);
-  REAL dx = maxabs4(ax[0], ax[1], ax[2], ax[3]), dy = maxabs4(ay[0], ay[1], ay[2], ay[3]),
-       dz = maxabs4(az[0], az[1], az[2], az[3]);
-  int sx1 = check_pp(e1, e2, e3, e4, s1, s2, dx, min_R, a1, b1, c1);
-  int sx2 = check_pp(e1, e2, e3, e4, s1, s2, dx, min_R, a2, b2, c2);
-  int sy1 = check_pp(e1, e2, e3, e4, s1, s2, dy, min_R, b1, a1, c1);
-  int sy2 = check_pp(e1, e2, e3, e4, s1, s2, dy, min_R, b2, a2, c2);
-  int sz1 = check_pp(e1, e2, e3, e4, s1, s2, dz, min_R, c1, a1, b1);
-  int sz2 = check_pp(e1, e2, e3, e4, s1, s2, dz, min_R, c2, a2, b2);
-  if (p1 == 0) sx1 = 1; else if (p1 == 1) sy1 = 1; else sz1 = 1;
-  if (p2 == 0) sx2 = 1; else if (p2 == 1) sy2 = 1; else sz2 = 1;
-  if (sx1 + sy1 + sz1 + sx2 + sy2 + sz2 != 2) {
-    *unsup = 1;
-    *abssum = NAN;
-    return NAN;
+  int f1[3] = {0, 0, 0}, f2[3] = {0, 0, 0};
+  if (suppress) {
+    REAL ax[4] = {x1v[0] - x2v[0], x1v[0] - x2v[1], x1v[1] - x2v[0], x1v[1] - x2v[1]};
+    REAL ay[4] = {y1v[0] - y2v[0], y1v[0] - y2v[1], y1v[1] - y2v[0], y1v[1] - y2v[1]};
+    REAL az[4] = {z1v[0] - z2v[0], z1v[0] - z2v[1], z1v[1] - z2v[0], z1v[1] - z2v[1]};
+    REAL mx = minabs4(ax[0], ax[1], ax[2], ax[3]), my = minabs4(ay[0], ay[1], ay[2], ay[3]),
+         mz = minabs4(az[0], az[1], az[2], az[3]);
+    REAL min_R = SQRT(mx * mx + my * my + mz * mz);
+    REAL dx = maxabs4(ax[0], ax[1], ax[2], ax[3]), dy = maxabs4(ay[0], ay[1], ay[2], ay[3]),
+         dz = maxabs4(az[0], az[1], az[2], az[3]);
+    f1[0] = check_pp(e1, e2, e3, e4, s1, s2, dx, min_R, a1, b1, c1);
+    f2[0] = check_pp(e1, e2, e3, e4, s1, s2, dx, min_R, a2, b2, c2);
+    f1[1] = check_pp(e1, e2, e3, e4, s1, s2, dy, min_R, b1, a1, c1);
+    f2[1] = check_pp(e1, e2, e3, e4, s1, s2, dy, min_R, b2, a2, c2);
+    f1[2] = check_pp(e1, e2, e3, e4, s1, s2, dz, min_R, c1, a1, b1);
+    f2[2] = check_pp(e1, e2, e3, e4, s1, s2, dz, min_R, c2, a2, b2);
   }
-  REAL X1[2], Y1[2], X2[2], Z2[2];
-  if (p1 == 0) {
-    if (p2 == 0) return a1 * a2 * ss_para(y1v, z1v, xc1, y2v, z2v, xc2, abssum);
-    if (p2 == 1) return a1 * b2 * ss_ortho(z1v, y1v, xc1, z2v, yc2, x2v, abssum);
-    return a1 * c2 * ss_ortho(y1v, z1v, xc1, y2v, zc2, x2v, abssum);
-  }
-  if (p1 == 1) {
-    if (p2 == 0) return b1 * a2 * ss_ortho(z1v, x1v, yc1, z2v, xc2, y2v, abssum);
-    if (p2 == 1) return b1 * b2 * ss_para(x1v, z1v, yc1, x2v, z2v, yc2, abssum);
-    return b1 * c2 * ss_ortho(x1v, z1v, yc1, x2v, zc2, y2v, abssum);
-  }
-  (void)X1; (void)Y1; (void)X2; (void)Z2;
-  if (p2 == 0) return c1 * a2 * ss_ortho(y1v, x1v, zc1, y2v, xc2, z2v, abssum);
-  if (p2 == 1) return c1 * b2 * ss_ortho(x1v, y1v, zc1, x2v, yc2, z2v, abssum);
-  return c1 * c2 * ss_para(x1v, y1v, zc1, x2v, y2v, zc2, abssum);
+  f1[p1] = 1;
+  f2[p2] = 1;
+  *far = f1[0] + f1[1] + f1[2] + f2[0] + f2[1] + f2[2] > 2;
+  return integ_bodies(x1v, y1v, z1v, xc1, yc1, zc1, a1, b1, c1, x2v, y2v, z2v, xc2, yc2, zc2, a2,
+                      b2, c2, f1, f2, 1, acc);
 }
 
 /* face centre and extents of face type caser (1..6) of a voxel centred at c
@@ -324,7 +695,7 @@ static void face(int caser, REAL cx, REAL cy, REAL cz, REAL sx, REAL sy, REAL sz
  * caser, targets centers[N][3] with face caser2. out is escaled by escal_P. */
 int64_t FN(oracle_p_row)(int caser, int caser2, const double* src, const double* centers,
                          int64_t N, double sx_, double sy_, double sz_, double escal_P,
-                         double* out, double* scale) {
+                         int suppress, double* out, double* scale) {
   const REAL eps0 = 8.854187816997944e-12L;
   const REAL pi = 3.14159265358979323846264338327950288L;
   REAL sx = sx_, sy = sy_, sz = sz_;
@@ -337,17 +708,12 @@ int64_t FN(oracle_p_row)(int caser, int caser2, const double* src, const double*
     REAL f2[3], e2[3], d2[2];
     face(caser2, centers[3 * k], centers[3 * k + 1], centers[3 * k + 2], sx, sy, sz, f2, e2, d2);
     REAL acc;
-    int unsup = 0;
+    int far = 0;
     REAL v = sup_sup(f1[0], f1[1], f1[2], f2[0], f2[1], f2[2], e1[0], e1[1], e1[2], e2[0], e2[1],
-                     e2[2], &acc, &unsup);
+                     e2[2], suppress, &acc, &far);
+    bad += far;
     /* 1/(4*pi*eps0*A1*d*d) evaluated left to right as the reference writes it */
     REAL pref = (REAL)1 / ((REAL)4 * pi * eps0 * A1 * d2[0] * d2[1]);
-    if (unsup) {
-      out[k] = NAN;
-      if (scale) scale[k] = NAN;
-      bad += 1;
-      continue;
-    }
     out[k] = (double)((REAL)escal_P * (pref * v));
     if (scale) scale[k] = (double)((REAL)escal_P * (pref * acc));
   }

@@ -58,13 +58,13 @@ def _fill_lib():
             f = getattr(lib, "oracle_lp_row" + sfx)
             f.restype = ctypes.c_int64
             f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
-                          ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
-                          ctypes.c_void_p]
+                          ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                          ctypes.c_void_p, ctypes.c_void_p]
             g = getattr(lib, "oracle_p_row" + sfx)
             g.restype = ctypes.c_int64
             g.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                           ctypes.c_int64, ctypes.c_double, ctypes.c_double, ctypes.c_double,
-                          ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+                          ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         _fill = lib
     return _fill
 
@@ -73,36 +73,38 @@ def _fill_lib():
 # fill (compute_FFT_mutual_coupling_mats.jl, compute_Lp_Voxels.jl, compute_row_P_sup.jl)
 # ----------------------------------------------------------------------------------------
 
-def lp_row(dc, centers, sx, sy, sz, precision="double", with_scale=False):
+def lp_row(dc, centers, sx, sy, sz, precision="double", with_scale=False, suppression=True,
+           count_far=False):
     """compute_Lp_Voxels(centers[0], centers, ...) for one direction dc in 1..3
-    (compute_Lp_Voxels.jl:1-63), unescaled."""
+    (compute_Lp_Voxels.jl:1-63), unescaled. suppression=False evaluates every entry by
+    the full volume-volume closed form instead of the reference's far-field branches.
+    count_far=True also returns how many entries took a far-field branch."""
     centers = np.ascontiguousarray(centers, dtype=np.float64)
     N = centers.shape[0]
     out = np.empty(N)
     scale = np.empty(N) if with_scale else None
     src = np.ascontiguousarray(centers[0])
     fn = getattr(_fill_lib(), "oracle_lp_row" + ("_ld" if precision == "long" else "_d"))
-    bad = fn(dc, src.ctypes.data, centers.ctypes.data, N, sx, sy, sz, out.ctypes.data,
-             scale.ctypes.data if with_scale else None)
-    if bad:
-        raise NotImplementedError(f"{bad} Lp entries need a far-field (suppressed) branch")
-    return (out, scale) if with_scale else out
+    far = fn(dc, src.ctypes.data, centers.ctypes.data, N, sx, sy, sz, int(bool(suppression)),
+             out.ctypes.data, scale.ctypes.data if with_scale else None)
+    res = (out, scale) if with_scale else out
+    return (res, int(far)) if count_far else res
 
 
-def p_row(caser, caser2, centers, sx, sy, sz, escal_P, precision="double", with_scale=False):
+def p_row(caser, caser2, centers, sx, sy, sz, escal_P, precision="double", with_scale=False,
+          suppression=True, count_far=False):
     """escal_P * compute_row_P_sup(centers[0], centers, ..., caser, caser2)
-    (compute_row_P_sup.jl:1-104)."""
+    (compute_row_P_sup.jl:1-104); suppression / count_far as for lp_row."""
     centers = np.ascontiguousarray(centers, dtype=np.float64)
     N = centers.shape[0]
     out = np.empty(N)
     scale = np.empty(N) if with_scale else None
     src = np.ascontiguousarray(centers[0])
     fn = getattr(_fill_lib(), "oracle_p_row" + ("_ld" if precision == "long" else "_d"))
-    bad = fn(caser, caser2, src.ctypes.data, centers.ctypes.data, N, sx, sy, sz, escal_P,
-             out.ctypes.data, scale.ctypes.data if with_scale else None)
-    if bad:
-        raise NotImplementedError(f"{bad} P entries need a far-field (suppressed) branch")
-    return (out, scale) if with_scale else out
+    far = fn(caser, caser2, src.ctypes.data, centers.ctypes.data, N, sx, sy, sz, escal_P,
+             int(bool(suppression)), out.ctypes.data, scale.ctypes.data if with_scale else None)
+    res = (out, scale) if with_scale else out
+    return (res, int(far)) if count_far else res
 
 
 # (lattice key, caser, caser2, reference dims) of the six P rows, in the order
@@ -120,16 +122,21 @@ def ref_dims(Nx, Ny, Nz):
             "p3456": (2 * (Nx + 1) - 1, Ny, 2 * (Nz + 1) - 1)}
 
 
-def fill_rows(circulant_centers, escalings, Nx, Ny, Nz, precision="double", with_scale=False):
+def fill_rows(circulant_centers, escalings, Nx, Ny, Nz, precision="double", with_scale=False,
+              far_counts=None):
     """The nine generating rows (escaled; Lp self entries zeroed as at
-    compute_FFT_mutual_coupling_mats.jl:56,68,80). Returns {key: row or (row, scale)}."""
+    compute_FFT_mutual_coupling_mats.jl:56,68,80). Returns {key: row or (row, scale)}.
+    far_counts, a dict, receives per row the number of entries that took a far-field
+    (suppressed) branch."""
     cc = circulant_centers
     sx, sy, sz = cc["sx"], cc["sy"], cc["sz"]
     out = {}
     for _, key, dc in LP_ROWS:
         if np.prod(ref_dims(Nx, Ny, Nz)[key]) == 0:
             continue
-        r = lp_row(dc, cc[key], sx, sy, sz, precision, with_scale)
+        r, far = lp_row(dc, cc[key], sx, sy, sz, precision, with_scale, count_far=True)
+        if far_counts is not None:
+            far_counts[key] = far
         if with_scale:
             row = escalings["Lp"] * r[0]
             row[0] = 0.0
@@ -139,7 +146,10 @@ def fill_rows(circulant_centers, escalings, Nx, Ny, Nz, precision="double", with
             row[0] = 0.0
             out[key] = row
     for _, key, c1, c2 in P_ROWS:
-        out[key] = p_row(c1, c2, cc[key], sx, sy, sz, escalings["P"], precision, with_scale)
+        out[key], far = p_row(c1, c2, cc[key], sx, sy, sz, escalings["P"], precision, with_scale,
+                              count_far=True)
+        if far_counts is not None:
+            far_counts[key] = far
     return out
 
 

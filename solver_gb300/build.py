@@ -30,7 +30,9 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 MESH_SOURCES = ["mesher.cpp"]
 CUDA_SOURCES = ["ctx.cu", "fftconv.cu", "fftconv_f32.cu", "fftconv_f64.cu", "fftconv_ff.cu",
                 "krylov.cu", "sparse.cu", "fill.cu"]
-CUDA_HEADERS = ["common.cuh", "fft.cuh", "fft_reg.cuh", "fftconv_impl.cuh", "integrals.cuh",
+# the fill keeps the reference's scalar rounding: no FMA contraction
+FILE_FLAGS = {"fill.cu": ["-fmad=false"]}
+CUDA_HEADERS = ["common.cuh", "fft.cuh", "fft_reg.cuh", "fftconv_impl.cuh",
                 "ctx.hpp"]
 
 
@@ -46,6 +48,7 @@ def _digest(paths) -> str:
     for p in paths:
         h.update(Path(p).read_bytes())
     h.update(" ".join(ARCH + NVCC_FLAGS).encode())
+    h.update(repr(sorted(FILE_FLAGS.items())).encode())
     return h.hexdigest()
 
 
@@ -84,7 +87,8 @@ def build_cuda(force: bool = False, verbose: bool = False) -> Path:
 
     def compile_one(src: Path) -> str:
         obj = BUILD / (src.stem + ".o")
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + ["-Xptxas", "-v", "-c", str(src), "-o", str(obj)]
+        cmd = ([nvcc] + ARCH + NVCC_FLAGS + FILE_FLAGS.get(src.name, []) +
+               ["-Xptxas", "-v", "-c", str(src), "-o", str(obj)])
         return _run(cmd)
 
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:

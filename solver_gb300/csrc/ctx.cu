@@ -587,7 +587,7 @@ extern "C" int peec_fill(peec_ctx* ctx, const double origin[3], double sx, doubl
       rc = fail_cuda(cudaGetLastError(), "fill", __FILE__, __LINE__);
     else if (hbad)
       rc = bad(ctx, PEEC_ERR_UNSUPPORTED,
-               "fill: an entry needs a far-field (suppressed) branch of the reference integrals");
+               "fill: a row entry is not finite (degenerate cell sizes?)");
   }
   if (rc == PEEC_OK && rows_out) {
     for (int i = 0; i < 9; ++i)

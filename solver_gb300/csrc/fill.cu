@@ -1,18 +1,28 @@
 // GPU fill of the nine generating rows of the voxel Lp / P circulant blocks
 // (compute_FFT_mutual_coupling_mats with QS_Rcc_FW == 1), one thread per lattice
-// entry, FP64 throughout (the closed forms cancel ~R^5 terms down to ~s^6/R).
+// entry, FP64 throughout (the near-field closed forms cancel ~R^5 terms down to ~s^6/R).
 //
-// Lp rows: compute_Lp_Voxels.jl:40-60 with round_ud_fft(.,14) coordinates
-// (:807-815) and the volume-volume closed form integ_vol_vol_fft (:766-805).
-// P rows: compute_row_P_sup.jl:1-104 with the face-face closed forms
-// integ_surf_surf_para (compute_Lp_Voxels_QS.jl:695-730) and
-// integ_surf_surf_ortho_P (compute_row_P_sup.jl:557-590).
+// Lp rows: compute_Lp_Voxels.jl:40-60 with round_ud_fft(.,14) coordinates (:807-815) and
+// the Integ_vol_vol_fft dispatch (:65-435): the volume-volume closed form
+// integ_vol_vol_fft (:766-805) in the near field, and once a dimension passes its
+// suppression test (check_condition_fft, :437-447; on uniform voxels a centre distance
+// beyond ~200 edges of that dimension) the closed form of the bodies left when that
+// dimension collapses (volume-surface ... point-point, :449-764).
+// P rows: compute_row_P_sup.jl:1-104 with the Integ_sup_sup_P dispatch (:106-381), its
+// face-face closed forms integ_surf_surf_para (compute_Lp_Voxels_QS.jl:695-730) and
+// integ_surf_surf_ortho_P (:557-590), and its far-field primitives (:396-556).
+//
+// The far-field primitives keep the reference's arithmetic exactly (expression order,
+// the zeroing of non-finite log terms, the 1e-8 nudges of integ_line_point and the
+// origin-dependent collinear-line forms integ_line_line_sp_fft / _P), and this file is
+// compiled without FMA contraction, so that degenerate corners (X + R rounding to 0)
+// fall the same way as in the reference's scalar Float64 code.
+//
+// The dispatch is written over axis-indexed boxes: for each pair of bodies the
+// collapsed dimensions select a primitive, whose arguments are the boxes' intervals and
+// centres permuted the way the reference's case tree passes them.
 // Lattice centres are recomputed from the origin with the reference's expression
 // order (build_center_P_Voxels.jl:15-80, build_centers_Lp_with_air.jl:1-60).
-// The suppression (far-field) tests of Integ_vol_vol_fft / Integ_sup_sup_P are
-// evaluated; an entry that would take a far-field branch sets *bad, because only the
-// near-field closed forms are implemented (on uniform voxels those branches need
-// centre distances beyond ~200 voxel edges).
 #include <math.h>
 #include <math_constants.h>
 
@@ -20,11 +30,18 @@
 
 namespace peec {
 
-__device__ __forceinline__ double lgc(double v) {  // real(log(complex(v))), v >= 0
+__device__ __forceinline__ double lgc(double v) {  // real(log(complex(v)))
   return v > 0 ? log(v) : (v == 0 ? -INFINITY : log(fabs(v)));
 }
 __device__ __forceinline__ double fin(double t) { return isfinite(t) ? t : 0.0; }
 __device__ __forceinline__ double round14(double v) { return rint(v * 1e14) / 1e14; }
+// (-1)^k
+__device__ __forceinline__ double sgn(int k) { return (k & 1) ? -1.0 : 1.0; }
+
+// ---------------------------------------------------------------------------------
+// closed forms; corner signs are the reference's (-1)^(c1+..+cn [+1]) with 1-based c,
+// i.e. (-1)^(sum0 + n [+1]) with the 0-based corner bits used here
+// ---------------------------------------------------------------------------------
 
 __device__ double vol_vol(const double* x1v, const double* y1v, const double* z1v,
                           const double* x2v, const double* y2v, const double* z2v) {
@@ -43,10 +60,346 @@ __device__ double vol_vol(const double* x1v, const double* y1v, const double* z1
     const double t5 = -fabs(X) * X2 * Y * Z / 6 * atan2(Y * Z, fabs(X) * R);
     const double t6 = -X * fabs(Y) * Y2 * Z / 6 * atan2(X * Z, fabs(Y) * R);
     const double t7 = -X * Y * fabs(Z) * Z2 / 6 * atan2(X * Y, fabs(Z) * R);
-    const double s = t1 + t2 + t3 + t4 + t5 + t6 + t7;
-    sol += ((c1 + c2 + c3 + c4 + c5 + c6 + 1) & 1) ? -s : s;
+    sol += sgn(c1 + c2 + c3 + c4 + c5 + c6 + 1) * (t1 + t2 + t3 + t4 + t5 + t6 + t7);
   }
   return sol;
+}
+
+// surfaces in (x, y) planes at heights z1, z2
+__device__ double ss_para(const double* x1v, const double* y1v, double z1, const double* x2v,
+                          const double* y2v, double z2) {
+  double sol = 0.0;
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    const int c1 = (c >> 3) & 1, c2 = (c >> 2) & 1, c3 = (c >> 1) & 1, c4 = c & 1;
+    const double X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2v[c3], Z = z1 - z2;
+    const double R = sqrt(X * X + Y * Y + Z * Z);
+    const double t1 = -1.0 / 6 * (X * X + Y * Y - 2 * Z * Z) * R;
+    const double t2 = -X * Y * fabs(Z) * atan2(X * Y, fabs(Z) * R);
+    const double t3 = fin(0.5 * (X * X - Z * Z) * Y * lgc(Y + R));
+    const double t4 = fin(0.5 * (Y * Y - Z * Z) * X * lgc(X + R));
+    sol += sgn(c1 + c2 + c3 + c4) * (t1 + t2 + t3 + t4);
+  }
+  return sol;
+}
+
+// surface in the (x, y) plane at z1 against one in the (x, z) plane at y2; pform selects
+// the seven-term integ_surf_surf_ortho_P over the four-term integ_surf_surf_ortho_fft
+__device__ double ss_ortho(const double* x1v, const double* y1v, double z1, const double* x2v,
+                           double y2, const double* z2v, int pform) {
+  double sol = 0.0;
+#pragma unroll 1
+  for (int c = 0; c < 16; ++c) {
+    const int c1 = (c >> 3) & 1, c2 = (c >> 2) & 1, c3 = (c >> 1) & 1, c4 = c & 1;
+    const double X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2, Z = z1 - z2v[c3];
+    const double R = sqrt(X * X + Y * Y + Z * Z);
+    const double t1 = -1.0 / 3 * Y * Z * R;
+    const double t2 = -0.5 * X * fabs(Z) * Z * atan2(X * Y, fabs(Z) * R);
+    double s;
+    if (pform) {
+      const double t3 = -0.5 * X * fabs(Y) * Y * atan2(X * Z, fabs(Y) * R);
+      const double t4 = -1.0 / 6 * fabs(X) * X * X * atan2(Y * Z, fabs(X) * R);
+      const double t5 = fin(X * Y * Z * lgc(X + R));
+      const double t6 = fin((0.5 * X * X - 1.0 / 6 * Z * Z) * Z * lgc(Y + R));
+      const double t7 = fin((0.5 * X * X - 1.0 / 6 * Y * Y) * Y * lgc(Z + R));
+      s = t1 + t2 + t3 + t4 + t5 + t6 + t7;
+    } else {
+      const double t3 = fin(0.5 * (X * X - Z * Z) * Y * lgc(Y + R));
+      const double t4 = fin(0.5 * (X * X - Y * Y) * X * lgc(X + R));
+      s = t1 + t2 + t3 + t4;
+    }
+    sol += sgn(c1 + c2 + c3 + c4) * s;
+  }
+  return sol;
+}
+
+// line [xv] at (y3, z3) against the point (x1, y1, z1)
+__device__ double line_point(const double* xv, double y3, double z3, double x1, double y1,
+                             double z1) {
+  const double x3 = xv[0], x4 = xv[1];
+  double chk = 1.0 / (x1 - x3);
+  if (isnan(chk) || isinf(chk)) x1 = x1 - 1e-8;
+  chk = 1.0 / (x1 - x4);
+  if (isnan(chk) || (isinf(chk) && x1 > 0)) x1 = x1 + 1e-8;
+  const double R1 = sqrt((x1 - x3) * (x1 - x3) + (y1 - y3) * (y1 - y3) + (z1 - z3) * (z1 - z3));
+  const double R2 = sqrt((x1 - x4) * (x1 - x4) + (y1 - y3) * (y1 - y3) + (z1 - z3) * (z1 - z3));
+  double Ip = log((x1 - x3) + R1) - log((x1 - x4) + R2);
+  if (!isfinite(Ip))
+    Ip = (x1 - x3) / fabs(x1 - x3) * log(fabs(x1 - x3)) -
+         (x1 - x4) / fabs(x1 - x4) * log(fabs(x1 - x4));
+  return Ip;
+}
+
+// point (x1, y1, z1) against the surface [x2v] x [y2v] at height z2
+__device__ double point_sup(double x1, double y1, double z1, const double* x2v, const double* y2v,
+                            double z2) {
+  double sol = 0.0;
+  for (int c = 0; c < 4; ++c) {
+    const int c1 = c >> 1, c2 = c & 1;
+    const double X = x1 - x2v[c1], Y = y1 - y2v[c2], Z = z1 - z2;
+    const double R = sqrt(X * X + Y * Y + Z * Z);
+    sol += sgn(c1 + c2) *
+           (fin(X * lgc(Y + R)) + fin(Y * lgc(X + R)) - fabs(Z) * atan2(X * Y, fabs(Z) * R));
+  }
+  return sol;
+}
+
+// collinear lines, in absolute coordinates as the reference writes them
+__device__ double ll_sp(const double* x1v, const double* x2v, int pform) {
+  double sol = 0.0;
+  for (int c = 0; c < 4; ++c) {
+    const int c1 = c >> 1, c2 = c & 1;
+    const double x1 = x1v[c1], x2 = x2v[c2];
+    const double R = sqrt((x1 - x2) * (x1 - x2));
+    double t = (x1 - x2) / R * (x1 - x2 * lgc(x2 - x1));
+    if (pform) t = t + x1 * lgc(x1 - x2);
+    sol += sgn(c1 + c2 + 1) * fin(t);
+  }
+  return sol;
+}
+
+// parallel lines along x at (y1, z1) and (y2, z2)
+__device__ double ll_parall(const double* x1v, double y1, double z1, const double* x2v, double y2,
+                            double z2, int pform) {
+  const double dy = y1 - y2, dz = z1 - z2;
+  if (fabs(dy) < 1e-10 && fabs(dz) < 1e-10) return ll_sp(x1v, x2v, pform);
+  double sol = 0.0;
+  for (int c = 0; c < 4; ++c) {
+    const int c1 = c >> 1, c2 = c & 1;
+    const double X = x1v[c1] - x2v[c2];
+    const double R = sqrt(X * X + dy * dy + dz * dz);
+    sol += sgn(c1 + c2 + 1) * (fin(X * lgc(X + R)) - R);
+  }
+  return sol;
+}
+
+// line along x at (y1, z1) against a line along y at (x2, z2)
+__device__ double ll_ortho(const double* x1v, double y1, double z1, double x2, const double* y2v,
+                           double z2) {
+  double sol = 0.0;
+  for (int c = 0; c < 4; ++c) {
+    const int c1 = c >> 1, c2 = c & 1;
+    const double X = x1v[c1] - x2, Y = y1 - y2v[c2], Z = z1 - z2;
+    const double R = sqrt(X * X + Y * Y + Z * Z);
+    sol += sgn(c1 + c2 + 1) *
+           (fin(X * lgc(Y + R)) + fin(Y * lgc(X + R)) - fabs(Z) * atan2(X * Y, fabs(Z) * R));
+  }
+  return sol;
+}
+
+// the triple antiderivative of 1/R (six terms)
+__device__ double f111(double X, double Y, double Z) {
+  const double R = sqrt(X * X + Y * Y + Z * Z);
+  const double t1 = fin(Y * Z * lgc(X + R));
+  const double t2 = fin(X * Z * lgc(Y + R));
+  const double t3 = fin(Y * X * lgc(Z + R));
+  const double t4 = -0.5 * fabs(Z) * Z * atan2(X * Y, fabs(Z) * R);
+  const double t5 = -0.5 * fabs(Y) * Y * atan2(X * Z, fabs(Y) * R);
+  const double t6 = -0.5 * fabs(X) * X * atan2(Y * Z, fabs(X) * R);
+  return t1 + t2 + t3 + t4 + t5 + t6;
+}
+
+__device__ double point_vol(double x1, double y1, double z1, const double* x2v, const double* y2v,
+                            const double* z2v) {
+  double sol = 0.0;
+  for (int c = 0; c < 8; ++c) {
+    const int c1 = c >> 2, c2 = (c >> 1) & 1, c3 = c & 1;
+    sol += sgn(c1 + c2 + c3) * f111(x1 - x2v[c1], y1 - y2v[c2], z1 - z2v[c3]);
+  }
+  return sol;
+}
+
+// line along x at (y1, z1) against the surface [y2v] x [z2v] at x2; pform selects the
+// six-term integ_line_surf_ortho_P over the three-term integ_line_surf_ortho_fft
+__device__ double ls_ortho(const double* x1v, double y1, double z1, double x2, const double* y2v,
+                           const double* z2v, int pform) {
+  double sol = 0.0;
+  for (int c = 0; c < 8; ++c) {
+    const int c1 = c >> 2, c2 = (c >> 1) & 1, c3 = c & 1;
+    const double X = x1v[c1] - x2, Y = y1 - y2v[c2], Z = z1 - z2v[c3];
+    double v;
+    if (pform) {
+      v = f111(X, Y, Z);
+    } else {
+      const double R = sqrt(X * X + Y * Y + Z * Z);
+      v = fin(Y * Z * lgc(X + R)) + fin(X * Z * lgc(Y + R)) - fabs(Z) * atan2(X * Y, fabs(Z) * R);
+    }
+    sol += sgn(c1 + c2 + c3 + 1) * v;
+  }
+  return sol;
+}
+
+// surface [x1v] x [y1v] at z1 against a line along x at (y2, z2)
+__device__ double ls_para(const double* x1v, const double* y1v, double z1, const double* x2v,
+                          double y2, double z2) {
+  double sol = 0.0;
+  for (int c = 0; c < 8; ++c) {
+    const int c1 = c >> 2, c2 = (c >> 1) & 1, c3 = c & 1;
+    const double X = x1v[c1] - x2v[c3], Y = y1v[c2] - y2, Z = z1 - z2;
+    const double R = sqrt(X * X + Y * Y + Z * Z);
+    const double t1 = fin(X * Y * lgc(X + R));
+    const double t2 = fin((X * X - Z * Z) / 2 * lgc(Y + R));
+    const double t3 = -X * fabs(Z) * atan2(X * Y, fabs(Z) * R);
+    const double t4 = -Y / 2 * R;
+    sol += sgn(c1 + c2 + c3) * (t1 + t2 + t3 + t4);
+  }
+  return sol;
+}
+
+// volume against a line along x at (y2, z2)
+__device__ double line_vol(const double* x1v, const double* y1v, const double* z1v,
+                           const double* x2v, double y2, double z2) {
+  double sol = 0.0;
+#pragma unroll 1
+  for (int c = 0; c < 16; ++c) {
+    const int c1 = c >> 3, c2 = (c >> 2) & 1, c3 = (c >> 1) & 1, c4 = c & 1;
+    const double X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2, Z = z1v[c3] - z2;
+    const double R = sqrt(X * X + Y * Y + Z * Z);
+    const double aX = fabs(X);
+    const double t1 = -1.0 / 3 * Y * Z * R;
+    const double t2 = -0.5 * X * fabs(Z) * Z * atan2(X * Y, fabs(Z) * R);
+    const double t3 = -0.5 * X * fabs(Y) * Y * atan2(X * Z, fabs(Y) * R);
+    const double t4 = -1.0 / 6 * (aX * aX * aX) * atan2(Y * Z, aX * R);
+    const double t5 = fin(X * Y * Z * lgc(X + R));
+    const double t6 = fin((0.5 * (X * X) - 1.0 / 6 * (Z * Z)) * Z * lgc(Y + R));
+    const double t7 = fin((0.5 * (X * X) - 1.0 / 6 * (Y * Y)) * Y * lgc(Z + R));
+    sol += sgn(c1 + c2 + c3 + c4 + 1) * (t1 + t2 + t3 + t4 + t5 + t6 + t7);
+  }
+  return sol;
+}
+
+// volume against the surface [x2v] x [y2v] at z2
+__device__ double vol_surf(const double* x1v, const double* y1v, const double* z1v,
+                           const double* x2v, const double* y2v, double z2) {
+  double sol = 0.0;
+#pragma unroll 1
+  for (int c = 0; c < 32; ++c) {
+    const int c1 = c >> 4, c2 = (c >> 3) & 1, c3 = (c >> 2) & 1, c4 = (c >> 1) & 1, c5 = c & 1;
+    const double X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2v[c5], Z = z1v[c3] - z2;
+    const double X2 = X * X, Y2 = Y * Y, Z2 = Z * Z;
+    const double R = sqrt(X2 + Y2 + Z2);
+    const double aX = fabs(X), aY = fabs(Y);
+    const double t1 = (Z2 / 12 - (X2 + Y2) / 8) * Z * R;
+    const double t2 = fin((Y2 / 2 - Z2 / 6) * X * lgc(X + R));
+    const double t3 = fin((X2 / 2 - Z2 / 6) * Y * lgc(Y + R));
+    const double t4 = fin((-(X2 * X2) / 24 - (Y2 * Y2) / 24 + (Y2 * X2) / 4) * lgc(Z + R));
+    const double t5 = -(aX * aX * aX) * Y / 6 * atan2(Y * Z, aX * R);
+    const double t6 = -X * (aY * aY * aY) / 6 * atan2(X * Z, aY * R);
+    const double t7 = -X * Y * fabs(Z) * Z / 2 * atan2(X * Y, fabs(Z) * R);
+    sol += sgn(c1 + c2 + c3 + c4 + c5 + 1) * (t1 + t2 + t3 + t4 + t5 + t6 + t7);
+  }
+  return sol;
+}
+
+// ---------------------------------------------------------------------------------
+// dispatch over axis-indexed boxes
+// ---------------------------------------------------------------------------------
+
+struct Box {
+  double iv[3][2];  // interval per axis
+  double c[3];      // centre per axis
+  double len[3];    // edge length per axis (1 for a face normal in the P tree)
+  int s[3];         // dimension collapsed
+  int n;            // number collapsed
+};
+
+// the two axes other than a, in increasing order
+__device__ __forceinline__ void others(int a, int& u, int& v) {
+  u = a == 0 ? 1 : 0;
+  v = a == 2 ? 1 : 2;
+}
+__device__ __forceinline__ int open_axis(const Box& b) { return !b.s[0] ? 0 : (!b.s[1] ? 1 : 2); }
+__device__ __forceinline__ int shut_axis(const Box& b) { return b.s[0] ? 0 : (b.s[1] ? 1 : 2); }
+
+// The integral of 1/R over the two boxes with their collapsed dimensions, each collapsed
+// length entering as a factor (the shared case tree of Integ_vol_vol_fft and
+// Integ_sup_sup_P; pform selects the _P primitives).
+__device__ __noinline__ double integ_boxes(const Box& A, const Box& B, int pform) {
+  const double V1 = A.len[0] * A.len[1] * A.len[2], V2 = B.len[0] * B.len[1] * B.len[2];
+  switch (A.n + B.n) {
+    case 6: {
+      const double dx = A.c[0] - B.c[0], dy = A.c[1] - B.c[1], dz = A.c[2] - B.c[2];
+      return V1 * V2 / sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    case 5: {  // point - line
+      const Box& L = A.n == 3 ? B : A;
+      const Box& P = A.n == 3 ? A : B;
+      const int i = open_axis(L);
+      int j, k;
+      others(i, j, k);
+      return V1 * V2 / L.len[i] * line_point(L.iv[i], L.c[j], L.c[k], P.c[i], P.c[j], P.c[k]);
+    }
+    case 4: {
+      if (A.n == 3 || B.n == 3) {  // point - surface
+        const Box& P = A.n == 3 ? A : B;
+        const Box& S = A.n == 3 ? B : A;
+        const int nrm = shut_axis(S);
+        const int u = nrm == 0 ? 2 : 0, v = nrm == 1 ? 2 : 1;
+        const double Vp = A.n == 3 ? V1 : V2;
+        return Vp * S.len[nrm] * point_sup(P.c[u], P.c[v], P.c[nrm], S.iv[u], S.iv[v], S.c[nrm]);
+      }
+      // line - line
+      const int i = open_axis(A), j = open_axis(B);
+      int o1, o2, q1, q2;
+      others(i, o1, o2);
+      others(j, q1, q2);
+      const double w = A.len[o1] * A.len[o2] * B.len[q1] * B.len[q2];
+      if (i == j) return w * ll_parall(A.iv[i], A.c[o1], A.c[o2], B.iv[i], B.c[o1], B.c[o2], pform);
+      const int k = 3 - i - j;
+      return w * ll_ortho(A.iv[i], A.c[j], A.c[k], B.c[i], B.iv[j], B.c[k]);
+    }
+    case 3: {
+      if (A.n == 3)
+        return A.len[0] * A.len[1] * A.len[2] * point_vol(A.c[0], A.c[1], A.c[2], B.iv[0], B.iv[1], B.iv[2]);
+      if (B.n == 3)
+        return B.len[0] * B.len[1] * B.len[2] * point_vol(B.c[0], B.c[1], B.c[2], A.iv[0], A.iv[1], A.iv[2]);
+      // surface - line
+      const Box& S = A.n == 1 ? A : B;
+      const Box& L = A.n == 1 ? B : A;
+      const int nrm = shut_axis(S), i = open_axis(L);
+      int q1, q2;
+      others(i, q1, q2);
+      const double w = S.len[nrm] * L.len[q1] * L.len[q2];
+      if (i == nrm) {
+        int u, v;
+        others(i, u, v);
+        return w * ls_ortho(L.iv[i], L.c[u], L.c[v], S.c[nrm], S.iv[u], S.iv[v], pform);
+      }
+      const int m = 3 - i - nrm;
+      return w * ls_para(S.iv[i], S.iv[m], S.c[nrm], L.iv[i], L.c[m], L.c[nrm]);
+    }
+    case 2: {
+      if (A.n == 2 || B.n == 2) {  // line - volume
+        const Box& L = A.n == 2 ? A : B;
+        const Box& V = A.n == 2 ? B : A;
+        const int i = open_axis(L);
+        int o1, o2;
+        others(i, o1, o2);
+        return L.len[o1] * L.len[o2] *
+               line_vol(V.iv[i], V.iv[o1], V.iv[o2], L.iv[i], L.c[o1], L.c[o2]);
+      }
+      // surface - surface
+      const int n1 = shut_axis(A), n2 = shut_axis(B);
+      const double w = A.len[n1] * B.len[n2];
+      if (n1 == n2) {
+        int u, v;
+        others(n1, u, v);
+        return w * ss_para(A.iv[u], A.iv[v], A.c[n1], B.iv[u], B.iv[v], B.c[n1]);
+      }
+      const int a = 3 - n1 - n2;
+      return w * ss_ortho(A.iv[a], A.iv[n2], A.c[n1], B.iv[a], B.c[n2], B.iv[n1], pform);
+    }
+    case 1: {  // surface - volume
+      const Box& S = A.n == 1 ? A : B;
+      const Box& V = A.n == 1 ? B : A;
+      const int nrm = shut_axis(S);
+      int u, v;
+      others(nrm, u, v);
+      return S.len[nrm] * vol_surf(V.iv[u], V.iv[v], V.iv[nrm], S.iv[u], S.iv[v], S.c[nrm]);
+    }
+    default:
+      return vol_vol(A.iv[0], A.iv[1], A.iv[2], B.iv[0], B.iv[1], B.iv[2]);
+  }
 }
 
 __device__ __forceinline__ void minmax4(double a, double b, double c, double d, double& mn,
@@ -56,6 +409,16 @@ __device__ __forceinline__ void minmax4(double a, double b, double c, double d, 
   mx = fmax(fmax(a, b), fmax(c, d));
 }
 
+// closest-corner distance of the two boxes and the largest corner offset per axis
+__device__ __forceinline__ double box_gaps(const Box& A, const Box& B, double mxd[3]) {
+  double mn[3];
+  for (int d = 0; d < 3; ++d)
+    minmax4(A.iv[d][0] - B.iv[d][0], A.iv[d][0] - B.iv[d][1], A.iv[d][1] - B.iv[d][0],
+            A.iv[d][1] - B.iv[d][1], mn[d], mxd[d]);
+  return sqrt(mn[0] * mn[0] + mn[1] * mn[1] + mn[2] * mn[2]);
+}
+
+// check_condition_fft (compute_Lp_Voxels.jl:437-447)
 __device__ int chk_fft(double V1, double V2, double max_d, double min_R, double size_dim, double o1,
                        double o2) {
   const double e1 = 5e-3, e2 = 1e-3, e3 = 1e-3;
@@ -67,44 +430,30 @@ __device__ int chk_fft(double V1, double V2, double max_d, double min_R, double 
   return ((b <= e3 || f < e1) && a < e2) ? 1 : 0;
 }
 
-// number of suppressed dimensions of Integ_vol_vol_fft (compute_Lp_Voxels.jl:86-172)
-__device__ int lp_suppressed(const double* x1v, const double* y1v, const double* z1v,
-                             const double* x2v, const double* y2v, const double* z2v) {
+// suppression flags of Integ_vol_vol_fft (compute_Lp_Voxels.jl:86-172): the smallest
+// edge first, the other two only when the larger of them is under 0.3 min_R
+__device__ void lp_flags(Box& A, Box& B) {
   const double e4 = 3e-1;
-  const double a1 = fabs(x1v[1] - x1v[0]), b1 = fabs(y1v[1] - y1v[0]), c1 = fabs(z1v[1] - z1v[0]);
-  const double a2 = fabs(x2v[1] - x2v[0]), b2 = fabs(y2v[1] - y2v[0]), c2 = fabs(z2v[1] - z2v[0]);
-  const double V1 = a1 * b1 * c1, V2 = a2 * b2 * c2;
-  double mnx, mxx, mny, mxy, mnz, mxz;
-  minmax4(x1v[0] - x2v[0], x1v[0] - x2v[1], x1v[1] - x2v[0], x1v[1] - x2v[1], mnx, mxx);
-  minmax4(y1v[0] - y2v[0], y1v[0] - y2v[1], y1v[1] - y2v[0], y1v[1] - y2v[1], mny, mxy);
-  minmax4(z1v[0] - z2v[0], z1v[0] - z2v[1], z1v[1] - z2v[0], z1v[1] - z2v[1], mnz, mxz);
-  const double min_R = sqrt(mnx * mnx + mny * mny + mnz * mnz);
-  int s = 0;
+  double mxd[3];
+  const double min_R = box_gaps(A, B, mxd);
+  const double V1 = A.len[0] * A.len[1] * A.len[2], V2 = B.len[0] * B.len[1] * B.len[2];
   for (int side = 0; side < 2; ++side) {
-    const double a = side ? a2 : a1, b = side ? b2 : b1, c = side ? c2 : c1;
-    int sx = 0, sy = 0, sz = 0;
-    if (a <= b && a <= c) {
-      sx = chk_fft(V1, V2, mxx, min_R, a, b, c);
-      if (sx && fmax(b, c) / (min_R + 1e-15) < e4) {
-        sy = chk_fft(V1, V2, mxy, min_R, b, a, c);
-        sz = chk_fft(V1, V2, mxz, min_R, c, a, b);
-      }
-    } else if (b <= a && b <= c) {
-      sy = chk_fft(V1, V2, mxy, min_R, b, a, c);
-      if (sy && fmax(a, c) / (min_R + 1e-15) < e4) {
-        sx = chk_fft(V1, V2, mxx, min_R, a, b, c);
-        sz = chk_fft(V1, V2, mxz, min_R, c, a, b);
-      }
-    } else {
-      sz = chk_fft(V1, V2, mxz, min_R, c, a, b);
-      if (sz && fmax(a, b) / (min_R + 1e-15) < e4) {
-        sx = chk_fft(V1, V2, mxx, min_R, a, b, c);
-        sy = chk_fft(V1, V2, mxy, min_R, b, a, c);
-      }
+    Box& X = side ? B : A;
+    const double* l = X.len;
+    const int first = (l[0] <= l[1] && l[0] <= l[2]) ? 0 : ((l[1] <= l[0] && l[1] <= l[2]) ? 1 : 2);
+    int u, v;
+    others(first, u, v);
+    X.s[0] = X.s[1] = X.s[2] = 0;
+    X.s[first] = chk_fft(V1, V2, mxd[first], min_R, l[first], l[u], l[v]);
+    if (X.s[first] && fmax(l[u], l[v]) / (min_R + 1e-15) < e4) {
+      int a, b;
+      others(u, a, b);
+      X.s[u] = chk_fft(V1, V2, mxd[u], min_R, l[u], l[a], l[b]);
+      others(v, a, b);
+      X.s[v] = chk_fft(V1, V2, mxd[v], min_R, l[v], l[a], l[b]);
     }
-    s += sx + sy + sz;
+    X.n = X.s[0] + X.s[1] + X.s[2];
   }
-  return s;
 }
 
 // lattice centre of index (i,j,k); half = ceil(i/2)-style lattice per axis
@@ -128,31 +477,39 @@ __device__ __forceinline__ double lp_center(const LpRowArgs& a, int axis, int i)
   return 0.5 * (A + B);
 }
 
+// voxel box of compute_Lp_Voxels: round_ud_fft(centre -+ s/2, 14) per axis
+__device__ __forceinline__ void lp_box(Box& b, const double c[3], const double s[3]) {
+  for (int d = 0; d < 3; ++d) {
+    b.iv[d][0] = round14(c[d] - s[d] / 2);
+    b.iv[d][1] = round14(c[d] + s[d] / 2);
+    b.c[d] = 0.5 * (b.iv[d][0] + b.iv[d][1]);
+    b.len[d] = fabs(b.iv[d][1] - b.iv[d][0]);
+  }
+}
+
 __global__ void k_fill_lp(LpRowArgs a, double* row, int64_t N, int* bad) {
   const double sx = a.s[0], sy = a.s[1], sz = a.s[2];
   double S = sy * sz * sy * sz;
   if (a.dir == 1) S = sx * sz * sx * sz;
   else if (a.dir == 2) S = sx * sy * sx * sy;
-  const double c1x = lp_center(a, 0, 0), c1y = lp_center(a, 1, 0), c1z = lp_center(a, 2, 0);
-  const double x1v[2] = {round14(c1x - sx / 2), round14(c1x + sx / 2)};
-  const double y1v[2] = {round14(c1y - sy / 2), round14(c1y + sy / 2)};
-  const double z1v[2] = {round14(c1z - sz / 2), round14(c1z + sz / 2)};
+  const double c1[3] = {lp_center(a, 0, 0), lp_center(a, 1, 0), lp_center(a, 2, 0)};
+  Box A;
+  lp_box(A, c1, a.s);
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
        p += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(p % a.M[0]);
     const int j = (int)((p / a.M[0]) % a.M[1]);
     const int k = (int)(p / ((int64_t)a.M[0] * a.M[1]));
-    const double cx = lp_center(a, 0, i), cy = lp_center(a, 1, j), cz = lp_center(a, 2, k);
-    const double x2v[2] = {round14(cx - sx / 2), round14(cx + sx / 2)};
-    const double y2v[2] = {round14(cy - sy / 2), round14(cy + sy / 2)};
-    const double z2v[2] = {round14(cz - sz / 2), round14(cz + sz / 2)};
-    if (lp_suppressed(x1v, y1v, z1v, x2v, y2v, z2v) != 0) {
-      atomicOr(bad, 1);
-      row[p] = CUDART_NAN;
-      continue;
-    }
-    const double v = vol_vol(x1v, y1v, z1v, x2v, y2v, z2v);
-    row[p] = (p == 0) ? 0.0 : a.escal * (1e-7 / S * v);
+    const double c2[3] = {lp_center(a, 0, i), lp_center(a, 1, j), lp_center(a, 2, k)};
+    Box B;
+    lp_box(B, c2, a.s);
+    lp_flags(A, B);
+    const double v = (A.n + B.n == 0)
+                         ? vol_vol(A.iv[0], A.iv[1], A.iv[2], B.iv[0], B.iv[1], B.iv[2])
+                         : integ_boxes(A, B, 0);
+    const double e = (p == 0) ? 0.0 : a.escal * (1e-7 / S * v);
+    if (!isfinite(e)) atomicOr(bad, 1);
+    row[p] = e;
   }
 }
 
@@ -160,45 +517,7 @@ __global__ void k_fill_lp(LpRowArgs a, double* row, int64_t N, int* bad) {
 // P rows
 // ---------------------------------------------------------------------------------
 
-__device__ double ss_para(const double* x1v, const double* y1v, double z1, const double* x2v,
-                          const double* y2v, double z2) {
-  double sol = 0.0;
-#pragma unroll
-  for (int c = 0; c < 16; ++c) {
-    const int c1 = (c >> 3) & 1, c2 = (c >> 2) & 1, c3 = (c >> 1) & 1, c4 = c & 1;
-    const double X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2v[c3], Z = z1 - z2;
-    const double R = sqrt(X * X + Y * Y + Z * Z);
-    const double t1 = -1.0 / 6 * (X * X + Y * Y - 2 * Z * Z) * R;
-    const double t2 = -X * Y * fabs(Z) * atan2(X * Y, fabs(Z) * R);
-    const double t3 = fin(0.5 * (X * X - Z * Z) * Y * lgc(Y + R));
-    const double t4 = fin(0.5 * (Y * Y - Z * Z) * X * lgc(X + R));
-    const double s = t1 + t2 + t3 + t4;
-    sol += ((c1 + c2 + c3 + c4) & 1) ? -s : s;
-  }
-  return sol;
-}
-
-__device__ double ss_ortho(const double* x1v, const double* y1v, double z1, const double* x2v,
-                           double y2, const double* z2v) {
-  double sol = 0.0;
-#pragma unroll
-  for (int c = 0; c < 16; ++c) {
-    const int c1 = (c >> 3) & 1, c2 = (c >> 2) & 1, c3 = (c >> 1) & 1, c4 = c & 1;
-    const double X = x1v[c1] - x2v[c4], Y = y1v[c2] - y2, Z = z1 - z2v[c3];
-    const double R = sqrt(X * X + Y * Y + Z * Z);
-    const double t1 = -1.0 / 3 * Y * Z * R;
-    const double t2 = -0.5 * X * fabs(Z) * Z * atan2(X * Y, fabs(Z) * R);
-    const double t3 = -0.5 * X * fabs(Y) * Y * atan2(X * Z, fabs(Y) * R);
-    const double t4 = -1.0 / 6 * fabs(X) * X * X * atan2(Y * Z, fabs(X) * R);
-    const double t5 = fin(X * Y * Z * lgc(X + R));
-    const double t6 = fin((0.5 * X * X - 1.0 / 6 * Z * Z) * Z * lgc(Y + R));
-    const double t7 = fin((0.5 * X * X - 1.0 / 6 * Y * Y) * Y * lgc(Z + R));
-    const double s = t1 + t2 + t3 + t4 + t5 + t6 + t7;
-    sol += ((c1 + c2 + c3 + c4) & 1) ? -s : s;
-  }
-  return sol;
-}
-
+// check_condition_P_P (compute_row_P_sup.jl:383-394)
 __device__ int chk_pp(double S1, double S2, double max_d, double min_R, double size_dim, double o1,
                       double o2) {
   const double e1 = 5e-3, e2 = 1e-3, e3 = 1e-3, e4 = 3e-1;
@@ -211,49 +530,50 @@ __device__ int chk_pp(double S1, double S2, double max_d, double min_R, double s
   return (condS < e4 && (b <= e3 || f < e1) && a < e2) ? 1 : 0;
 }
 
-// Integ_sup_sup_P restricted to its surface-surface branch
-__device__ double sup_sup(double xc1, double yc1, double zc1, double xc2, double yc2, double zc2,
-                          double a1, double b1, double c1, double a2, double b2, double c2,
-                          int* unsup) {
-  const double x1v[2] = {xc1 - a1 / 2, xc1 + a1 / 2}, y1v[2] = {yc1 - b1 / 2, yc1 + b1 / 2},
-               z1v[2] = {zc1 - c1 / 2, zc1 + c1 / 2};
-  const double x2v[2] = {xc2 - a2 / 2, xc2 + a2 / 2}, y2v[2] = {yc2 - b2 / 2, yc2 + b2 / 2},
-               z2v[2] = {zc2 - c2 / 2, zc2 + c2 / 2};
-  int p1 = 2, p2 = 2;
-  if (a1 <= b1 && a1 <= c1) { p1 = 0; a1 = 1; }
-  else if (b1 <= a1 && b1 <= c1) { p1 = 1; b1 = 1; }
-  else { c1 = 1; }
-  if (a2 <= b2 && a2 <= c2) { p2 = 0; a2 = 1; }
-  else if (b2 <= a2 && b2 <= c2) { p2 = 1; b2 = 1; }
-  else { c2 = 1; }
-  const double s1 = a1 * b1 * c1, s2 = a2 * b2 * c2;
-  double mnx, mxx, mny, mxy, mnz, mxz;
-  minmax4(x1v[0] - x2v[0], x1v[0] - x2v[1], x1v[1] - x2v[0], x1v[1] - x2v[1], mnx, mxx);
-  minmax4(y1v[0] - y2v[0], y1v[0] - y2v[1], y1v[1] - y2v[0], y1v[1] - y2v[1], mny, mxy);
-  minmax4(z1v[0] - z2v[0], z1v[0] - z2v[1], z1v[1] - z2v[0], z1v[1] - z2v[1], mnz, mxz);
-  const double min_R = sqrt(mnx * mnx + mny * mny + mnz * mnz);
-  int sx1 = chk_pp(s1, s2, mxx, min_R, a1, b1, c1), sx2 = chk_pp(s1, s2, mxx, min_R, a2, b2, c2);
-  int sy1 = chk_pp(s1, s2, mxy, min_R, b1, a1, c1), sy2 = chk_pp(s1, s2, mxy, min_R, b2, a2, c2);
-  int sz1 = chk_pp(s1, s2, mxz, min_R, c1, a1, b1), sz2 = chk_pp(s1, s2, mxz, min_R, c2, a2, b2);
-  if (p1 == 0) sx1 = 1; else if (p1 == 1) sy1 = 1; else sz1 = 1;
-  if (p2 == 0) sx2 = 1; else if (p2 == 1) sy2 = 1; else sz2 = 1;
-  if (sx1 + sy1 + sz1 + sx2 + sy2 + sz2 != 2) {
-    *unsup = 1;
-    return CUDART_NAN;
+// face box of Integ_sup_sup_P: intervals from the face centre and extents, the normal
+// (smallest extent) length replaced by 1 and always collapsed
+__device__ __forceinline__ int face_box(Box& b, const double fc[3], const double ext[3]) {
+  for (int d = 0; d < 3; ++d) {
+    b.iv[d][0] = fc[d] - ext[d] / 2;
+    b.iv[d][1] = fc[d] + ext[d] / 2;
+    b.c[d] = fc[d];
+    b.len[d] = ext[d];
   }
-  if (p1 == 0) {
-    if (p2 == 0) return a1 * a2 * ss_para(y1v, z1v, xc1, y2v, z2v, xc2);
-    if (p2 == 1) return a1 * b2 * ss_ortho(z1v, y1v, xc1, z2v, yc2, x2v);
-    return a1 * c2 * ss_ortho(y1v, z1v, xc1, y2v, zc2, x2v);
+  const double* e = ext;
+  const int nrm = (e[0] <= e[1] && e[0] <= e[2]) ? 0 : ((e[1] <= e[0] && e[1] <= e[2]) ? 1 : 2);
+  b.len[nrm] = 1.0;
+  return nrm;
+}
+
+// Integ_sup_sup_P (compute_row_P_sup.jl:106-381)
+__device__ double sup_sup(const double f1[3], const double e1[3], const double f2[3],
+                          const double e2[3]) {
+  Box A, B;
+  const int p1 = face_box(A, f1, e1), p2 = face_box(B, f2, e2);
+  const double s1 = A.len[0] * A.len[1] * A.len[2], s2 = B.len[0] * B.len[1] * B.len[2];
+  double mxd[3];
+  const double min_R = box_gaps(A, B, mxd);
+  for (int d = 0; d < 3; ++d) {
+    int u, v;
+    others(d, u, v);
+    A.s[d] = chk_pp(s1, s2, mxd[d], min_R, A.len[d], A.len[u], A.len[v]);
+    B.s[d] = chk_pp(s1, s2, mxd[d], min_R, B.len[d], B.len[u], B.len[v]);
   }
-  if (p1 == 1) {
-    if (p2 == 0) return b1 * a2 * ss_ortho(z1v, x1v, yc1, z2v, xc2, y2v);
-    if (p2 == 1) return b1 * b2 * ss_para(x1v, z1v, yc1, x2v, z2v, yc2);
-    return b1 * c2 * ss_ortho(x1v, z1v, yc1, x2v, zc2, y2v);
+  A.s[p1] = 1;
+  B.s[p2] = 1;
+  A.n = A.s[0] + A.s[1] + A.s[2];
+  B.n = B.s[0] + B.s[1] + B.s[2];
+  if (A.n + B.n == 2) {  // face - face, the near field
+    const double w = A.len[p1] * B.len[p2];
+    if (p1 == p2) {
+      int u, v;
+      others(p1, u, v);
+      return w * ss_para(A.iv[u], A.iv[v], A.c[p1], B.iv[u], B.iv[v], B.c[p1]);
+    }
+    const int a = 3 - p1 - p2;
+    return w * ss_ortho(A.iv[a], A.iv[p2], A.c[p1], B.iv[a], B.c[p2], B.iv[p1], 1);
   }
-  if (p2 == 0) return c1 * a2 * ss_ortho(y1v, x1v, zc1, y2v, xc2, z2v);
-  if (p2 == 1) return c1 * b2 * ss_ortho(x1v, y1v, zc1, x2v, yc2, z2v);
-  return c1 * c2 * ss_para(x1v, y1v, zc1, x2v, y2v, zc2);
+  return integ_boxes(A, B, 1);
 }
 
 struct PRowArgs {
@@ -293,16 +613,11 @@ __global__ void k_fill_p(PRowArgs a, double* row, int64_t N, int* bad) {
     double f2[3], e2[3], d2[2];
     face(a.caser2, ctr(a.o[0], sx, i, a.half[0]), ctr(a.o[1], sy, j, a.half[1]),
          ctr(a.o[2], sz, k, a.half[2]), sx, sy, sz, f2, e2, d2);
-    int unsup = 0;
-    const double v = sup_sup(f1[0], f1[1], f1[2], f2[0], f2[1], f2[2], e1[0], e1[1], e1[2], e2[0],
-                             e2[1], e2[2], &unsup);
-    if (unsup) {
-      atomicOr(bad, 1);
-      row[p] = CUDART_NAN;
-      continue;
-    }
+    const double v = sup_sup(f1, e1, f2, e2);
     const double pref = 1.0 / (4 * pi * eps0 * A1 * d2[0] * d2[1]);
-    row[p] = a.escal * (pref * v);
+    const double e = a.escal * (pref * v);
+    if (!isfinite(e)) atomicOr(bad, 1);
+    row[p] = e;
   }
 }
 

@@ -115,3 +115,59 @@ def test_oracle_matches_its_regression_pins(tag):
     st = {"Inner_Iter": settings["Inner_Iter"], "tol": np.full(len(freqs), settings["tol"])}
     res = O.FFT_solver_QS_S_type(freqs, esc, inc, FFTCP, FFTCLp, diag, ports, z0, le, exp, st, Zs)
     np.testing.assert_allclose(res["Z"], pin["Z"], rtol=1e-8)
+
+
+# grids whose rows reach the far-field (suppressed) branches of the reference's integral
+# dispatch: (shape, cell edges)
+FAR_GRIDS = {
+    "cubic_232x3x2": ((232, 3, 2), (5e-5, 5e-5, 5e-5)),
+    "thin_40x40x3": ((40, 40, 3), (1e-4, 1e-4, 1e-6)),
+    "needle_60x4x4": ((60, 4, 4), (1e-3, 1e-5, 1e-5)),
+    "aniso_120x48x4": ((120, 48, 4), (1e-4, 2e-4, 5e-5)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FAR_GRIDS))
+def test_far_field_branches_reach_the_point_limit(name):
+    """Every distant entry (centre distance R > 30 x the longest edge; on cubic voxels
+    R > 205 edges, past the switch, since the double near-field form itself loses
+    ~1e-3 to cancellation just before it) is within 3 (edge/R)^2 of the point-point
+    value -- except collinear pairs that reach the line-line branch: the reference's
+    integ_line_line_sp_fft / _P (compute_Lp_Voxels.jl:514-529,
+    compute_row_P_sup.jl:461-476) evaluate those in absolute coordinates, and the
+    oracle (like the GPU fill) keeps that."""
+    shape, cell = FAR_GRIDS[name]
+    cu = np.zeros(shape, dtype=bool)
+    cu[0:3, 0, 0] = True
+    req = configs.make_request({"copper": cu}, [dict(configs.COPPER)], cell,
+                               [((0, 0, 0), (2, 0, 0))], [1e9], 1e-8)
+    out, _f, _s, _z, _grid = mesher.parse_request(req)
+    cc = out[2]
+    sx, sy, sz = cc["sx"], cc["sy"], cc["sz"]
+    edge = max(sx, sy, sz)
+    cut = 205 * edge if name.startswith("cubic") else 30 * edge
+    V = sx * sy * sz
+    rows = [(dc, key, None) for dc, key in ((1, "Lpx"), (2, "Lpy"), (3, "Lpz"))]
+    rows += [(None, key, cs) for key, cs in (("p12_se", 1), ("p34_se", 3), ("p56_se", 5))]
+    collinear_seen = far_total = 0
+    for dc, key, cs in rows:
+        c = np.asarray(cc[key])
+        if dc:
+            S = [(sy * sz) ** 2, (sx * sz) ** 2, (sx * sy) ** 2][dc - 1]
+            (row, far) = O.lp_row(dc, c, sx, sy, sz, count_far=True)
+            point = lambda R: 1e-7 / S * V * V / R
+        else:
+            (row, far) = O.p_row(cs, cs, c, sx, sy, sz, 1.0, count_far=True)
+            point = lambda R: 1 / (4 * math.pi * 8.854187816997944e-12 * R)
+        d = c - c[0]
+        R = np.linalg.norm(d, axis=1)
+        sel = np.flatnonzero(R > cut)
+        far_total += far
+        collinear = np.sum(np.abs(d[sel]) < 1e-12 * edge, axis=1) >= 2
+        rel = np.abs(row[sel] - point(R[sel])) / point(R[sel])
+        ok = rel <= 3 * (edge / R[sel]) ** 2
+        assert np.all(ok | collinear), (key, float(rel[~(ok | collinear)].max()))
+        collinear_seen += int(np.sum(~ok & collinear))
+    assert far_total > 0
+    if name == "needle_60x4x4":
+        assert collinear_seen > 0
