@@ -4,7 +4,7 @@
   FFT-solver request bodies (inputs only; the reference ships no outputs for this
   path), copied verbatim from the reference checkout given as argv[1].
 * ``oracle_*.npz``: outputs of the CPU oracle (oracle/peec_oracle.py) on those inputs
-  and on the 20x20x4 crossbar configuration, kept as regression pins of the oracle
+  (the two-material one at 1 GHz and 3 GHz) and on the 20x20x4 crossbar configuration, kept as regression pins of the oracle
   itself (rows, one matvec on a seeded vector, the port solution and Z).
 
 Usage: python tests/golden/make_fixtures.py /path/to/reference
@@ -45,6 +45,11 @@ def main():
     for name in ("first_run_data.json", "first_run_data_2_materials.json"):
         shutil.copyfile(ref / name, HERE / name)
     oracle_case(mesher.load_request(HERE / "first_run_data.json"), "first_run_data")
+    # the two-material fixture at 1 GHz and 3 GHz: its face rows reach the far-field
+    # (suppressed) branches of the P integrals
+    req2 = mesher.load_request(HERE / "first_run_data_2_materials.json")
+    req2["solverInput"]["frequencies"] = [1e9, 3e9]
+    oracle_case(req2, "first_run_data_2_materials")
     oracle_case(configs.crossbar_20x20x4(), "crossbar_20x20x4")
 
 

@@ -42,6 +42,8 @@ def _at(req, freqs):
 CASES = {
     "first_run_data_1GHz": lambda: _at(mesher.load_request(GOLDEN / "first_run_data.json"),
                                        [1e9, 3e9]),
+    "first_run_data_2_materials_1GHz": lambda: _at(
+        mesher.load_request(GOLDEN / "first_run_data_2_materials.json"), [1e9, 3e9]),
     "crossbar_20x20x4": configs.crossbar_20x20x4,
     "random_24x20x12": lambda: configs.random_mixed((24, 20, 12), s=5e-5, p=0.35, seed=7,
                                                     nports=2, freqs=[1e8, 3e9], tol=1e-8),

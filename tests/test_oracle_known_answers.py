@@ -93,12 +93,17 @@ def test_port_operator_is_reciprocal():
 def _case(tag):
     from pathlib import Path
     g = Path(__file__).resolve().parent / "golden"
-    req = (mesher.load_request(g / "first_run_data.json") if tag == "first_run_data"
-           else configs.crossbar_20x20x4())
+    if tag == "crossbar_20x20x4":
+        req = configs.crossbar_20x20x4()
+    else:
+        req = mesher.load_request(g / f"{tag}.json")
+        if tag == "first_run_data_2_materials":
+            req["solverInput"]["frequencies"] = [1e9, 3e9]
     return req, np.load(g / f"oracle_{tag}.npz")
 
 
-@pytest.mark.parametrize("tag", ["first_run_data", "crossbar_20x20x4"])
+@pytest.mark.parametrize("tag", ["first_run_data", "first_run_data_2_materials",
+                                 "crossbar_20x20x4"])
 def test_oracle_matches_its_regression_pins(tag):
     req, pin = _case(tag)
     out, freqs, settings, z0, (Nx, Ny, Nz) = mesher.parse_request(req)
