@@ -58,6 +58,7 @@ void launch_scale_rnorm(c64*, size_t, const double*, cudaStream_t);
 void launch_make_reflector(const c64*, size_t, int, c64, double, c64*, cudaStream_t);
 void launch_sub(const c64*, const c64*, size_t, c64*, cudaStream_t);
 void launch_add(const c64*, const c64*, size_t, c64*, cudaStream_t);
+void launch_differs(const c64*, const c64*, size_t, int*, cudaStream_t);
 void launch_tri(c64*, int, int, const c64*, c64*, int, cudaStream_t);
 void launch_xupdate(const c64*, const c64*, size_t, const c64*, const c64*, int, size_t, c64*,
                     cudaStream_t);
@@ -121,6 +122,11 @@ struct peec_ctx {
           *cmp_segU = nullptr, *cmp_segLoff = nullptr, *cmp_segUoff = nullptr,
           *cmp_local = nullptr;
   c64 *ir_b = nullptr, *ir_x = nullptr, *ir_r = nullptr, *ir_d = nullptr;  // refinement vectors
+  // convolutions of the last converged mixed solve's final residual: x, Lp*I, P*Q and
+  // the precision they were computed in (-1: none). They do not depend on the frequency.
+  c64 *cc_x = nullptr, *cc_LpI = nullptr, *cc_PQ = nullptr;
+  int cc_prec = -1;
+  int* d_flag = nullptr;
   int sf_total = 0, sf_nL = 0;
   int* sf_ctl = nullptr;  // [epoch, claim counter, error flag]
   LevelTri Lf, Uf;
@@ -321,7 +327,9 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   for (int32_t* p : {ctx->cmp_off, ctx->cmp_rowsL, ctx->cmp_rowsU, ctx->cmp_segL, ctx->cmp_segU,
                      ctx->cmp_segLoff, ctx->cmp_segUoff, ctx->cmp_local})
     cudaFree(p);
-  for (c64* p : {ctx->ir_b, ctx->ir_x, ctx->ir_r, ctx->ir_d}) cudaFree(p);
+  for (c64* p : {ctx->ir_b, ctx->ir_x, ctx->ir_r, ctx->ir_d, ctx->cc_x, ctx->cc_LpI, ctx->cc_PQ})
+    cudaFree(p);
+  cudaFree(ctx->d_flag);
   if (ctx->hx) cudaFreeHost(ctx->hx);
   if (ctx->hy) cudaFreeHost(ctx->hy);
   if (ctx->hsmall) cudaFreeHost(ctx->hsmall);
@@ -484,7 +492,11 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
   CTX_TRY(dalloc(&ctx->lutmp2, n));
   CTX_TRY(dalloc(&ctx->dx, ctx->N));
   CTX_TRY(dalloc(&ctx->dy, ctx->N));
-  for (c64** p : {&ctx->ir_b, &ctx->ir_x, &ctx->ir_r, &ctx->ir_d}) CTX_TRY(dalloc(p, ctx->N));
+  for (c64** p : {&ctx->ir_b, &ctx->ir_x, &ctx->ir_r, &ctx->ir_d, &ctx->cc_x}) CTX_TRY(dalloc(p, ctx->N));
+  CTX_TRY(dalloc(&ctx->cc_LpI, m));
+  CTX_TRY(dalloc(&ctx->cc_PQ, ns));
+  CTX_TRY(dalloc(&ctx->d_flag, 1));
+  ctx->cc_prec = -1;
   if (ctx->hx) cudaFreeHost(ctx->hx);
   if (ctx->hy) cudaFreeHost(ctx->hy);
   PEEC_CUDA_TRY(cudaMallocHost(&ctx->hx, sizeof(c64) * ctx->N));
@@ -513,6 +525,7 @@ extern "C" int peec_set_pdiag(peec_ctx* ctx, const double* diagP) {
 // (cross: output family f, input family g), then the three Lp blocks.
 static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
   drop_graphs(ctx);
+  ctx->cc_prec = -1;
   static const int srow[9] = {3, 4, 5, 6, 7, 8, 0, 1, 2};
   static const int fout[9] = {0, 1, 2, 0, 0, 1, 3, 4, 5};
   static const int fin[9] = {0, 1, 2, 1, 2, 2, 3, 4, 5};
@@ -881,24 +894,16 @@ static int check_solve_errors(peec_ctx* ctx) {
   return PEEC_OK;
 }
 
-// enqueue one operator application y = M^-1 K x on the context stream
-static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool events) {
+// enqueue the sparse half of an operator application y = M^-1 K x (block rows, the LU
+// solve of the preconditioner), given the convolutions LpI = Lp*I and PQ = P*Q of x
+static void sparse_enqueue(peec_ctx* ctx, const c64* x, c64* y, const c64* LpI, const c64* PQ) {
   const int64_t m = ctx->m, ns = ctx->ns, n = ctx->n;
   cudaStream_t st = ctx->st;
-  if (events) cudaEventRecord(ctx->ev[0], st);
-  const void* tw[3] = {ctx->tw64, ctx->tw32, ctx->twff};
-  CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, ctx->ph64, x, ctx->LpI, ctx->PQ, m, prec, tw,
-                   ctx->twmax, st,
-                   ctx->prof ? ctx->pev.data() : nullptr));
-  for (const auto& F : ctx->fam) ctx->launches += F.active ? (F.lp ? 5 : 4) : 0;
-  ctx->launches += 1;  // the shared z pass of the face families
-  if (events) cudaEventRecord(ctx->ev[1], st);
   const c64* I = x;
   const c64* Q = x + m;
   const c64* Phi = x + m + ns;
-  launch_edge_rows(I, Phi, ctx->LpI, ctx->DZ, ctx->n1, ctx->n2, ctx->w, (int)m, ctx->Y1, ctx->U1,
-                   st);
-  launch_surf_rows(ctx->PQ, Phi, ctx->snode, ctx->invP, (int)ns, ctx->Y2, ctx->U2, st);
+  launch_edge_rows(I, Phi, LpI, ctx->DZ, ctx->n1, ctx->n2, ctx->w, (int)m, ctx->Y1, ctx->U1, st);
+  launch_surf_rows(PQ, Phi, ctx->snode, ctx->invP, (int)ns, ctx->Y2, ctx->U2, st);
   launch_node_rows(I, Q, Phi, ctx->U1, ctx->U2, ctx->ne_ptr, ctx->ne_idx, ctx->nsn_ptr,
                    ctx->nsn_idx, ctx->yle_ptr, ctx->yle_col, ctx->yle_val, ctx->w, (int)n,
                    ctx->tvec, st);
@@ -907,6 +912,20 @@ static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool ev
   launch_final_rows(ctx->Y1, ctx->Y2, ctx->Mvec, ctx->DZ, ctx->n1, ctx->n2, ctx->snode, ctx->invP,
                     (int)m, (int)ns, (int)n, y, st);
   ctx->launches++;
+}
+
+// enqueue one operator application y = M^-1 K x on the context stream
+static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool events) {
+  cudaStream_t st = ctx->st;
+  if (events) cudaEventRecord(ctx->ev[0], st);
+  const void* tw[3] = {ctx->tw64, ctx->tw32, ctx->twff};
+  CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, ctx->ph64, x, ctx->LpI, ctx->PQ, ctx->m, prec, tw,
+                   ctx->twmax, st,
+                   ctx->prof ? ctx->pev.data() : nullptr));
+  for (const auto& F : ctx->fam) ctx->launches += F.active ? (F.lp ? 5 : 4) : 0;
+  ctx->launches += 1;  // the shared z pass of the face families
+  if (events) cudaEventRecord(ctx->ev[1], st);
+  sparse_enqueue(ctx, x, y, ctx->LpI, ctx->PQ);
   if (events) cudaEventRecord(ctx->ev[2], st);
   return PEEC_OK;
 }
@@ -1530,6 +1549,21 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
   cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, ctx->st);
   cudaMemcpyAsync(dxv, x_inout, bytes, cudaMemcpyHostToDevice, ctx->st);
   Gm g{ctx, N, ctx->resid_prec, ctx->st};
+  // The convolutions Lp*I and P*Q do not depend on the frequency. When x0 is the solution
+  // this context returned last (the warm start of a frequency sweep), the first residual
+  // reuses the convolutions of that solve's final residual -- the same numbers a fresh
+  // application would produce -- and only the sparse half runs.
+  bool reuse = false;
+  if (ctx->cc_prec == ctx->resid_prec) {
+    cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->st);
+    launch_differs(dxv, ctx->cc_x, N, ctx->d_flag, ctx->st);
+    ctx->launches++;
+    cudaMemcpyAsync(ctx->hscal, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->st);
+    PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+    reuse = *(const int*)ctx->hscal == 0;
+  }
+  ctx->cc_prec = -1;  // re-armed below once this solve converges
+  bool fresh = false;  // the last residual computed its own convolutions
   const double n2b = g.norm(db);
   int outer = 0, tot_inner = 0, fl = 1;
   double rel = 0;
@@ -1544,9 +1578,17 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
       if (outer == 0 && x_zero) {
         g.copy(dr, db);
         nr = n2b;
+        fresh = false;
+      } else if (outer == 0 && reuse) {
+        sparse_enqueue(ctx, dxv, ctx->gtmp, ctx->cc_LpI, ctx->cc_PQ);
+        launch_sub(db, ctx->gtmp, N, dr, ctx->st);
+        ctx->launches++;
+        nr = g.norm(dr);
+        fresh = false;
       } else {
         g.residual(db, dxv, dr);  // FP64 or float-float operator
         nr = g.norm(dr);
+        fresh = true;
       }
       if (g.rc) { cleanup(); return g.rc; }
       rel = nr / n2b;
@@ -1566,6 +1608,17 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
       launch_add(dxv, dd, N, dxv, ctx->st);  // x += d
       ctx->launches++;
     }
+  }
+  if (fl == 0 && n2b != 0 && (fresh || reuse)) {
+    // keep the convolutions of the returned solution for the next frequency's warm start
+    if (fresh) {
+      cudaMemcpyAsync(ctx->cc_x, dxv, bytes, cudaMemcpyDeviceToDevice, ctx->st);
+      cudaMemcpyAsync(ctx->cc_LpI, ctx->LpI, sizeof(c64) * ctx->m, cudaMemcpyDeviceToDevice,
+                      ctx->st);
+      cudaMemcpyAsync(ctx->cc_PQ, ctx->PQ, sizeof(c64) * ctx->ns, cudaMemcpyDeviceToDevice,
+                      ctx->st);
+    }
+    ctx->cc_prec = ctx->resid_prec;
   }
   cudaMemcpyAsync(x_inout, dxv, bytes, cudaMemcpyDeviceToHost, ctx->st);
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));

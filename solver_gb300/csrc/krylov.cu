@@ -314,6 +314,23 @@ void launch_add(const c64* a, const c64* b, size_t N, c64* out, cudaStream_t st)
   k_add<<<g_stream(N), 256, 0, st>>>(a, b, N, out);
 }
 
+// flag |= 1 when a and b differ anywhere (bitwise on the doubles)
+__global__ void k_differs(const c64* __restrict__ a, const c64* __restrict__ b, size_t N,
+                          int* flag) {
+  int d = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const c64 u = a[i], v = b[i];
+    d |= (__double_as_longlong(u.x) != __double_as_longlong(v.x)) |
+         (__double_as_longlong(u.y) != __double_as_longlong(v.y));
+  }
+  if (__any_sync(0xffffffffu, d) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+void launch_differs(const c64* a, const c64* b, size_t N, int* flag, cudaStream_t st) {
+  k_differs<<<g_stream(N), 256, 0, st>>>(a, b, N, flag);
+}
+
 void launch_tri(c64* T, int ld, int k, const c64* in, c64* out, int mode, cudaStream_t st) {
   k_tri<<<1, 256, 0, st>>>(T, ld, k, in, out, mode);
 }

@@ -366,3 +366,34 @@ def test_batched_sweep_many_geometries():
         for k in range(nf):
             e = np.max(np.abs(res["Z"][:, :, k] - ref["Z"][:, :, k])) / np.max(np.abs(ref["Z"][:, :, k]))
             assert e < 1e-6, (c["grid"], k, e)
+
+
+def test_mixed_warm_start_reuses_convolutions(case):
+    """A warm-started mixed solve whose x0 is the solution the context returned last
+    reuses that solve's residual convolutions (they do not depend on the frequency): the
+    result is bitwise the one a context without that cache computes, with one
+    convolution pass fewer."""
+    c = case
+    if len(c["freqs"]) < 2:
+        pytest.skip("needs two frequencies")
+    n1, n2 = np.asarray(c["ports"]["port_nodes"]).reshape(-1, 2)[0]
+    other = c["op"].clone()
+    try:
+        _freq(c, 0)
+        tn0 = c["op"].port_rhs(n1, n2, c["esc"]["Is"])
+        x0, fl0, _, _, _ = c["op"].solve_mixed(tn0, None, 1e-10)
+        assert fl0 == 0
+        w, fs = _freq(c, 1)
+        other.set_frequency(w, fs["DZ"], fs["Yle"], fs["lu"])
+        tn1 = c["op"].port_rhs(n1, n2, c["esc"]["Is"])
+        l0 = c["op"].launch_count()
+        xa, fla, ra, oa, ia = c["op"].solve_mixed(tn1, x0, 1e-10)
+        la = c["op"].launch_count() - l0
+        l1 = other.launch_count()
+        xb, flb, rb, ob, ib = other.solve_mixed(tn1, x0, 1e-10)
+        lb = other.launch_count() - l1
+        assert (fla, ra, oa, ia) == (flb, rb, ob, ib)
+        assert np.array_equal(xa, xb)
+        assert la < lb, (la, lb)
+    finally:
+        other.close()
