@@ -497,47 +497,72 @@ def main():
     for i in range(args.warmup):
         k = i % nf
         S_mixed[k], _, _, _ = solve_point(P, state(k), Vrest, "mixed", tol)
-    gpu_ms = 0.0
-    h2d = d2h = 0
+    # the timed points: every lane runs its ports through the whole timed frequency
+    # sequence on its own (PortLanes.sweep), so one lane's frequency-state upload overlaps
+    # the other lanes' solves; the device span runs from an event all lane streams wait
+    # on to the last lane's end
+    from solver_gb300 import api as _api
+    import threading
+    seq = [i % nf for i in range(args.warmup, args.warmup + args.steps)]
+    m_, n_ = P["inc"]["A"].shape
+    ns_ = P["inc"]["Gamma"].shape[1]
+    pn = np.asarray(P["ports"]["port_nodes"], dtype=np.int64)
+    npt = pn.shape[0]
+    cols = {}
     work = []
+    rlock = threading.Lock()
+    wait_s = [0.0]
+
+    def record(pos, k, c1, V, flag, relres, outer, ninner):
+        col = _api._port_column(V, pn, c1, m_, ns_, P["z0"])
+        with rlock:
+            cols.setdefault(pos, {})[c1] = col
+            work.append({"flag": flag, "relres": relres, "outer": outer, "inner": ninner,
+                         "fp64_matvecs": outer + 1, "fp32_matvecs": ninner + outer})
+
+    def get_state(k, pos):
+        th = time.perf_counter()
+        st = pf.get(k, pos=1 + args.warmup + pos)
+        with rlock:
+            wait_s[0] += time.perf_counter() - th
+        return st
+
     l0 = sum(o.launch_count() for o in P["lanes"].ops)
     barrier(ws)
     if have_torch:
         torch.cuda.synchronize()
     clocks = Clocks(local)
-    host_wait = 0.0
-    P["host_ms"] = {k: 0.0 for k in P["host_ms"]}
     t_wall0 = time.perf_counter()
-    for i in range(args.warmup, args.warmup + args.steps):
-        k = i % nf
-        th = time.perf_counter()
-        fs = state(k)  # host LU, built by the worker processes while earlier points solved
-        host_wait += time.perf_counter() - th
-        if have_torch:
-            # the step spans every lane: the other lanes' streams wait on e0, and the
-            # first lane's stream waits on each lane's end before e1
-            e0, e1 = ev(), ev()
-            e0.record(ext)
-            for xs in lane_ext[1:]:
-                xs.wait_event(e0)
-        t0 = time.perf_counter()
-        S_mixed[k], w_, hb, db = solve_point(P, fs, Vrest, "mixed", tol)
-        if have_torch:
-            for xs in lane_ext[1:]:
-                ei = ev()
-                ei.record(xs)
-                ext.wait_event(ei)
-            e1.record(ext)
-            e1.synchronize()
-            gpu_ms += e0.elapsed_time(e1)
-        else:
-            gpu_ms += (time.perf_counter() - t0) * 1e3
-        work += w_
-        h2d += hb
-        d2h += db
     if have_torch:
+        e0, e1 = ev(), ev()
+        e0.record(ext)
+        for xs in lane_ext[1:]:
+            xs.wait_event(e0)
+    P["lanes"].sweep(seq, get_state, lambda k: None, pn, P["esc"]["Is"], Vrest,
+                     lambda k: tol, dict(inner_tol=P["inner_tol"],
+                                         inner_maxit=P["settings"]["Inner_Iter"]), record)
+    if have_torch:
+        for xs in lane_ext[1:]:
+            ei = ev()
+            ei.record(xs)
+            ext.wait_event(ei)
+        e1.record(ext)
+        e1.synchronize()
+        gpu_ms = e0.elapsed_time(e1)
         torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall0
+    if not have_torch:
+        gpu_ms = t_wall * 1e3
+    host_wait = wait_s[0] / max(1, nlanes)
+    h2d = d2h = 0
+    for pos, k in enumerate(seq):
+        Sk = np.zeros((npt, npt), dtype=np.complex128)
+        for c1, col in cols[pos].items():
+            for c2, v in col.items():
+                Sk[c1, c2] = Sk[c2, c1] = v
+        S_mixed[k] = Sk
+        h2d += _point_bytes(P, state(k), npt)
+        d2h += npt * 2 * (m_ + ns_ + n_) * 16
     barrier(ws)
     clk = clocks.stop()
     launches = sum(o.launch_count() for o in P["lanes"].ops) - l0
@@ -590,8 +615,7 @@ def main():
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps),
                 "host_state_wait_ms_per_step": host_wait * 1e3 / args.steps,
-                "host_state_workers": nworkers,
-                "host_ms_per_step": {k: v / args.steps for k, v in P["host_ms"].items()}},
+                "host_state_workers": nworkers},
         "gpu_launches": int(launches),
         "clocks": clk,
         "fp64_plain": {"value": fp64_v, "unit": UNIT, "steps": n64,

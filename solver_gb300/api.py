@@ -179,6 +179,52 @@ class PortLanes:
                 out[j] = r
         return out
 
+    def sweep(self, seq, get_state, release, pn, Is, Vrest, tol_of, solve_kw, record,
+              stop_flag=None):
+        """Mixed-precision solves of every port at every frequency key of seq, each lane
+        on its own through the whole sequence: port c runs on lane c % lanes; a lane sets
+        each frequency state on its context, then solves its ports warm-started from its
+        own previous solutions (columns of Vrest). No lane waits for another between
+        frequencies, so one lane's host work (setting a frequency state, its uploads)
+        overlaps the other lanes' GPU solves.
+
+        get_state(k, pos) -> state with w, DZ, Yle, lu; release(k) is called once every
+        lane has set state k. record(pos, k, c, V, flag, relres, outer, inner) is called
+        from the lane threads after each solve. Returns False if stopped."""
+        L = len(self.ops)
+        npt = len(pn)
+        left = {}
+        lock = __import__("threading").Lock()
+        stopped = []
+
+        def lane(i):
+            op = self.ops[i]
+            mine = range(i, npt, L)
+            for pos, k in enumerate(seq):
+                if stop_flag is not None and stop_flag.value:
+                    stopped.append(True)
+                    return
+                fs = get_state(k, pos)
+                op.set_frequency(fs.w, fs.DZ, fs.Yle, fs.lu)
+                with lock:
+                    left[pos] = left.get(pos, min(L, npt)) - 1
+                    if left[pos] == 0 and k not in seq[pos + 1:]:
+                        release(k)
+                for c in mine:
+                    tn = op.port_rhs(pn[c][0], pn[c][1], Is)
+                    V, flag, relres, outer, inner = op.solve_mixed(tn, Vrest[:, c], tol_of(k),
+                                                                   **solve_kw)
+                    if flag == 99:
+                        stopped.append(True)
+                        return
+                    Vrest[:, c] = V
+                    record(pos, k, c, V, flag, relres, outer, inner)
+
+        futs = [self._pool.submit(lane, i) for i in range(min(L, npt))]
+        for f in futs:
+            f.result()
+        return not stopped
+
     def close(self):
         self._pool.shutdown(wait=True)
         for o in self.ops[1:]:
@@ -194,12 +240,14 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
                          ports_scatter_value, lumped_elements, expansions, GMRES_settings,
                          Zs_info, QS_Rcc_FW=1, id=None, chan=None, commentsEnabled=False, *,
                          mode="fp64", mixed_inner_tol=1e-7, mixed_warm_start=True,
-                         stop_flag=None, on_solve=None):
+                         stop_flag=None, on_solve=None, lanes=1):
     """Frequency x port sweep with warm starts (FFT_solver_QS_S_type.jl:1-234).
 
     mode "fp64": the reference algorithm (FP64 convolutions, Householder GMRES).
     mode "mixed": FP32 convolutions inside FP64 iterative refinement to the same
-    relative residual. Returns {"S","Z","Y","f","info"}; None if stopped.
+    relative residual. lanes > 1 (mixed, warm starts): the ports are spread over that
+    many contexts (PortLanes), each sweeping its ports through every frequency on its
+    own. Returns {"S","Z","Y","f","info"}; None if stopped.
     """
     if QS_Rcc_FW != 1:
         raise NotImplementedError("only the quasi-static operator (QS_Rcc_FW == 1) is implemented")
@@ -219,25 +267,79 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
     Vrest = np.zeros((m + n + ns, npt), dtype=np.complex128)
     tol = GMRES_settings["tol"]
     info = []
+    nl = min(int(lanes), npt)
+    # lanes read each state once per lane: keep states until every lane has set them
+    keep = mode == "mixed" and mixed_warm_start and nl > 1
     if n >= POOL_MIN_NODES and w.size > 2:
         # large node systems: factorise ahead in spawned worker processes
         pf = fq.FrequencyPool((escalings, incidence_selection, diagonals, Zs_info,
                                lumped_elements, ports, ports_scatter_value),
-                              lambda k: w[k], range(w.size), workers=4, lookahead=4, keep=False)
+                              lambda k: w[k], range(w.size), workers=4, lookahead=4, keep=keep)
     else:
         pf = fq.StatePrefetcher(
             lambda k: fq.FrequencyState(w[k], escalings, incidence_selection, diagonals, Zs_info,
                                         lumped_elements, ports, ports_scatter_value),
-            range(w.size), keep=False)
+            range(w.size), keep=keep)
     try:
-        res = _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode,
-                     mixed_inner_tol, mixed_warm_start, stop_flag, on_solve, info, m, ns,
-                     ports_scatter_value)
+        if mode == "mixed" and mixed_warm_start and nl > 1:
+            res = _sweep_lanes(op, nl, pf, w, pn, S, Vrest, tol, inner, escalings,
+                               mixed_inner_tol, stop_flag, on_solve, info, m, ns,
+                               ports_scatter_value)
+        else:
+            res = _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode,
+                         mixed_inner_tol, mixed_warm_start, stop_flag, on_solve, info, m, ns,
+                         ports_scatter_value)
     finally:
         pf.close()
     if res is not None:
         res["f"] = freq / escalings["freq"]
     return res
+
+
+def _port_column(V, pn, c1, m, ns, z0):
+    """S entries (c1, c2 >= c1) from port c1's solution (FFT_solver_QS_S_type.jl:199-208)."""
+    out = {}
+    for c2 in range(c1, len(pn)):
+        n3, n4 = pn[c2]
+        val = 2 * (V[m + ns + n3] - V[m + ns + n4])
+        out[c2] = (val - z0) / z0 if c1 == c2 else val / z0
+    return out
+
+
+def _sweep_lanes(op, nl, pf, w, pn, S, Vrest, tol, inner, escalings, mixed_inner_tol,
+                 stop_flag, on_solve, info, m, ns, z0):
+    lanes = PortLanes(op, nl)
+    if stop_flag is not None:
+        for o in lanes.ops[1:]:
+            o.set_stop_flag(stop_flag)
+    recs = []
+    lock = __import__("threading").Lock()
+
+    def record(pos, k, c1, V, flag, relres, outer, ninner):
+        col = _port_column(V, pn, c1, m, ns, z0)
+        with lock:
+            recs.append(({"flag": flag, "relres": relres, "outer": outer, "niter": ninner,
+                          "freq": k, "port": c1}, col))
+            if on_solve:
+                on_solve(k, c1, V)
+
+    try:
+        ok = lanes.sweep(list(range(w.size)), pf.get, pf.release, pn, escalings["Is"], Vrest,
+                         lambda k: float(tol[k]) if np.ndim(tol) else float(tol),
+                         dict(inner_tol=mixed_inner_tol, inner_maxit=inner), record,
+                         stop_flag=stop_flag)
+    finally:
+        lanes.close()
+    if not ok:
+        return None
+    recs.sort(key=lambda r: (r[0]["freq"], r[0]["port"]))
+    for rec, col in recs:
+        k, c1 = rec["freq"], rec["port"]
+        for c2, v in col.items():
+            S[c1, c2, k] = v
+            S[c2, c1, k] = v
+        info.append(rec)
+    return {"S": S, "Z": s2z_fft(S, z0), "Y": s2y_fft(S, z0), "info": info, "Vrest": Vrest}
 
 
 def _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode, mixed_inner_tol,

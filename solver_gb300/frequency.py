@@ -10,6 +10,8 @@ from __future__ import annotations
 
 import math
 
+import threading
+
 import numpy as np
 import scipy.sparse as sp
 import scipy.sparse.linalg as spla
@@ -137,25 +139,40 @@ class StatePrefetcher:
         self._pending = {}
         self._done = {}
         self._keep = keep
+        self._lock = threading.Lock()
 
-    def get(self, k):
-        if k in self._done:
-            st = self._done[k]
-        elif k in self._pending:
-            st = self._pending.pop(k).result()
-        else:
-            st = self._make(k)
-        if self._keep:
-            self._done[k] = st
-        # start the state the sequence asks for next, if it is not built yet
-        while self._pos < len(self._order) and self._order[self._pos] != k:
-            self._pos += 1
-        self._pos += 1
-        if self._pos < len(self._order):
-            nxt = self._order[self._pos]
-            if nxt not in self._done and nxt not in self._pending:
+    def get(self, k, pos=None):
+        """The state of key k. pos, the caller's index in the sequence, sets which state
+        is started next (callers that walk the sequence concurrently pass it); without
+        it the position advances to the next occurrence of k."""
+        with self._lock:
+            if k in self._done:
+                fut, st = None, self._done[k]
+            elif k in self._pending:
+                fut = self._pending[k]
+            else:
+                fut = self._pending[k] = self._pool.submit(self._make, k)
+            if pos is None:
+                while self._pos < len(self._order) and self._order[self._pos] != k:
+                    self._pos += 1
+                pos = self._pos
+                self._pos += 1
+            nxt = self._order[pos + 1] if pos + 1 < len(self._order) else None
+            if nxt is not None and nxt not in self._done and nxt not in self._pending:
                 self._pending[nxt] = self._pool.submit(self._make, nxt)
+        if fut is not None:
+            st = fut.result()
+            with self._lock:
+                if self._pending.get(k) is fut:
+                    del self._pending[k]
+                    if self._keep:
+                        self._done[k] = st
         return st
+
+    def release(self, k):
+        """Drops a kept state."""
+        with self._lock:
+            self._done.pop(k, None)
 
     def close(self):
         self._pool.shutdown(wait=True)
@@ -206,27 +223,41 @@ class FrequencyPool:
         self._pending = {}
         self._done = {}
         self._keep = keep
+        self._lock = threading.Lock()
 
     def _submit(self, k):
         if k not in self._done and k not in self._pending:
             self._pending[k] = self._pool.submit(_worker_state, self._w_of(k))
 
-    def get(self, k):
-        while self._pos < len(self._order) and self._order[self._pos] != k:
-            self._pos += 1
-        for nxt in self._order[self._pos:self._pos + 1 + self._ahead]:
-            self._submit(nxt)
-        if k in self._done:
-            st = self._done[k]
-        else:
+    def get(self, k, pos=None):
+        """The state of key k (blocking until a worker has built it). pos, the caller's
+        index in the sequence, sets which states are started ahead (callers that walk
+        the sequence concurrently pass it); without it the position advances to the
+        next occurrence of k. Safe to call from several threads."""
+        with self._lock:
+            if pos is None:
+                while self._pos < len(self._order) and self._order[self._pos] != k:
+                    self._pos += 1
+                pos = self._pos
+                self._pos += 1
+            for nxt in self._order[pos:pos + 1 + self._ahead]:
+                self._submit(nxt)
+            if k in self._done:
+                return self._done[k]
             self._submit(k)
-            st = self._pending.pop(k).result()
-        if self._keep:
-            self._done[k] = st
-        self._pos += 1
-        for nxt in self._order[self._pos:self._pos + self._ahead]:
-            self._submit(nxt)
+            fut = self._pending[k]
+        st = fut.result()
+        with self._lock:
+            if self._pending.get(k) is fut:
+                del self._pending[k]
+                if self._keep:
+                    self._done[k] = st
         return st
+
+    def release(self, k):
+        """Drops a kept state."""
+        with self._lock:
+            self._done.pop(k, None)
 
     def close(self):
         for f in self._pending.values():

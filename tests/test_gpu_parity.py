@@ -212,20 +212,26 @@ def test_sweep_parity(case):
     assert _rel(got["Vrest"], ref["Vrest"]) < 1e-10
 
 
-def test_mixed_sweep(case):
-    """The port x frequency sweep in mixed precision (zero initial guesses, host LU of
-    the next frequency built on a worker thread) against the oracle's FP64 sweep, both
-    converged to 1e-10: every solve meets the tolerance in the FP64 residual and the
-    port impedances agree to the accuracy that residual bounds."""
+@pytest.mark.parametrize("lanes", [1, 2])
+def test_mixed_sweep(case, lanes):
+    """The port x frequency sweep in mixed precision (warm starts, host LU of the next
+    frequency built on a worker thread; with 2 lanes the ports sweep the frequencies on
+    two contexts independently) against the oracle's FP64 sweep, both converged to
+    1e-10: every solve meets the tolerance in the FP64 residual and the port impedances
+    agree to the accuracy that residual bounds."""
     from solver_gb300 import api
     c = case
+    if lanes > 1 and len(np.asarray(c["ports"]["port_nodes"]).reshape(-1, 2)) < 2:
+        pytest.skip("one port")
     st = {"Inner_Iter": c["settings"]["Inner_Iter"], "tol": np.full(len(c["freqs"]), 1e-10)}
     ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
                                  c["diag"], c["ports"], c["z0"], c["le"], c["exp"], st, c["Zs"])
     c["exp"]["gpu_ctx"] = c["op"]
     h = api.CirculantSpectra(c["op"])
     got = api.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], h, h, c["diag"], c["ports"],
-                                   c["z0"], c["le"], c["exp"], st, c["Zs"], mode="mixed")
+                                   c["z0"], c["le"], c["exp"], st, c["Zs"], mode="mixed",
+                                   lanes=lanes)
+    assert len(got["info"]) == len(ref["info"])
     assert all(r["flag"] == 0 and r["relres"] <= 1e-10 for r in got["info"]), got["info"]
     assert _rel(got["Z"], ref["Z"]) < 1e-6
 
