@@ -46,10 +46,12 @@ METRIC = "freq-point solves/s at 1e-8 residual, mixed vs FP64 plain on 1 GB300; 
 UNIT = "freq-point solves/s"
 WORKLOAD = ("random_128x128x64: 5e-5 m voxels, Bernoulli(0.3) occupancy (seed 2), Cu/dielectric "
             "50/50, 4 ports, 10 freqs 10 MHz-10 GHz, tol 1e-8")
-# average FP64 matvecs per port solve of the reference algorithm at this workload
-# (Householder GMRES iterations + true-residual checks), used only by --impl reference,
-# which has no GPU run to count them; the GPU arm measures and reports its own count
-REF_MATVECS_PER_PORT = 32
+# average FP64 operator applications per port solve of the reference algorithm on this
+# workload's warm-started frequency sequence: GMRES takes 12-23 iterations per port (mean
+# 17.3 over the 28 port solves of 7 points, measured by the FP64 leg of this script on a
+# GB300), plus the initial residual and the final true-residual check. Used only by
+# --impl reference, which has no GPU run to count them; the GPU arm counts its own.
+REF_MATVECS_PER_PORT = 19.3
 
 
 def parse():
@@ -65,6 +67,9 @@ def parse():
                     help="run the adjoint-gradient configuration instead")
     ap.add_argument("--batched-sweep", action="store_true",
                     help="run the batched multi-geometry sweep configuration instead")
+    ap.add_argument("--small-configs", action="store_true",
+                    help="the crossbar 20x20x4 configurations (FP64 plain and mixed per "
+                         "frequency), one JSON line")
     ap.add_argument("--profile-only", action="store_true",
                     help="set up, time the operator applications and exit (for ncu captures)")
     ap.add_argument("--lanes", type=int, default=4,
@@ -185,6 +190,21 @@ def reference_model_bytes(grid, c):
 def conv_gbs(b, prof):
     keys = ("xfwd", "yfwd", "z", "yinv", "xinv")
     return sum(b[k] for k in keys) / (sum(prof[k] for k in keys) * 1e-3) / 1e9
+
+
+def z_traffic(grid):
+    """DRAM bytes (read + write) of one operator application's FP32 z passes from the
+    committed ncu summary of the 128x128x64 workload; None for other grids."""
+    if tuple(grid) != (128, 128, 64):
+        return None
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                        "z_traffic_random_128x128x64.md")
+    try:
+        import re
+        m = re.search(r"traffic_bytes_per_matvec:\s*(\d+)", open(path).read())
+        return int(m.group(1)) if m else None
+    except OSError:
+        return None
 
 
 def load_peaks():
@@ -329,6 +349,75 @@ def cpu_baseline(P, mv_per_port, sample_note):
             "matvec_s": t_mv, "lu_s": t_lu}
 
 
+def run_small_configs(args):
+    """The two small configurations, as one JSON line.
+    * crossbar 20x20x4 (two copper bars, one port, 1 GHz, tol 1e-6): the reference
+      algorithm (FP64 GMRES) on the GPU, per port solve from a zero initial guess,
+      timed over repeated solves, beside the CPU oracle's solve of the same system
+      (cpu_baseline leg);
+    * the same geometry in mixed precision to 1e-8 at 1 GHz and five log-spaced
+      frequencies 100 MHz - 10 GHz: per-frequency port-impedance error against the GPU
+      FP64 sweep at 1e-12 (itself parity-tested against the oracle at 1e-10)."""
+    from oracle import peec_oracle as O
+    from solver_gb300 import api, configs, mesher
+    from solver_gb300.operator import GpuOperator
+    out, freqs, settings, z0, grid = mesher.parse_request(configs.crossbar_20x20x4())
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    op = GpuOperator(inc, exp, diag["P"])
+    op.fill(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"])
+    w = 2 * np.pi * freqs[0] * esc["freq"]
+    fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
+    op.set_frequency(w, fs["DZ"], fs["Yle"], fs["lu"])
+    n1, n2 = np.asarray(ports["port_nodes"]).reshape(-1, 2)[0]
+    tn = op.port_rhs(n1, n2, esc["Is"])
+    times = []
+    for i in range(args.warmup + 20):
+        t = time.perf_counter()
+        V, flag, relres, it, rv = op.gmres(tn, None, 1e-6, 100)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t)
+    gpu_s = float(np.median(times))
+    # the CPU oracle on the same system (reference 2N extents, SuperLU, Householder GMRES)
+    rows = O.fill_rows(cc, esc, *grid)
+    FFTCP, FFTCLp = O.spectra_from_rows(rows, *grid)
+    mv = lambda x: O.ComputeMatrixVectorFTT(x, w, inc, FFTCP, FFTCLp, fs["DZ"], fs["Yle"], exp,
+                                            fs["invZ"], fs["invP"], fs["F"])
+    tn_h = np.asarray(tn)
+    ct = []
+    for i in range(3):
+        t = time.perf_counter()
+        O.gmres_custom(tn_h, False, 1e-6, 100, np.zeros_like(tn_h), mv)
+        ct.append(time.perf_counter() - t)
+    cpu_s = float(np.median(ct))
+    # mixed precision per frequency against the GPU FP64 sweep
+    f3 = [1e9] + list(np.logspace(8, 10, 5))
+    nf = len(f3)
+    h = api.CirculantSpectra(op)
+    exp["gpu_ctx"] = op
+    ref = api.FFT_solver_QS_S_type(f3, esc, inc, h, h, diag, ports, z0, le, exp,
+                                   {"Inner_Iter": 200, "tol": np.full(nf, 1e-12)}, Zs)
+    t = time.perf_counter()
+    got = api.FFT_solver_QS_S_type(f3, esc, inc, h, h, diag, ports, z0, le, exp,
+                                   {"Inner_Iter": 100, "tol": np.full(nf, 1e-8)}, Zs,
+                                   mode="mixed")
+    mixed_s = time.perf_counter() - t
+    errs = [float(np.max(np.abs(got["Z"][:, :, k] - ref["Z"][:, :, k])) /
+                  np.max(np.abs(ref["Z"][:, :, k]))) for k in range(nf)]
+    exp.pop("gpu_ctx", None)
+    op.close()
+    print(json.dumps({
+        "metric": "small configurations: crossbar 20x20x4 FP64 plain and mixed per frequency",
+        "crossbar_fp64": {"port_solves_per_s": 1.0 / gpu_s, "solve_ms": gpu_s * 1e3,
+                          "gmres_iters": int(it[1]), "flag": int(flag), "relres": relres,
+                          "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "port solves/s",
+                                           "cores": os.cpu_count() or 1, "kind": "port",
+                                           "sample": "one oracle GMRES solve of the same system"}},
+        "crossbar_mixed": {"freqs_hz": f3, "z_rel_err_vs_fp64_1e-12": dict(
+            zip([f"{f:.4g}" for f in f3], errs)), "max_err": max(errs),
+            "freq_point_solves_per_s": nf / mixed_s,
+            "flags": sorted({int(r["flag"]) for r in got["info"]})}}), flush=True)
+
+
 def run_reference(args):
     ws, rank, local = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
     if rank != 0:
@@ -442,6 +531,9 @@ def main():
         return
     if args.batched_sweep:
         run_batched_sweep(args)
+        return
+    if args.small_configs:
+        run_small_configs(args)
         return
     ws, rank, local = dist_init()
     P = setup_problem(device=local, grid=args.grid)
@@ -640,7 +732,8 @@ def main():
                      "achieved": b32["z"] / (prof32["z"] * 1e-3) / 1e9, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": b32["z"] / (prof32["z"] * 1e-3) / 1e9 / peak,
-                     "traffic": None, "bytes_per_matvec": b32["z"], "launches_per_matvec": 4},
+                     "traffic": z_traffic(P["grid"]), "bytes_per_matvec": b32["z"],
+                     "launches_per_matvec": 4},
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(P, mv_per_port,
