@@ -922,8 +922,10 @@ static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool ev
   CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, ctx->ph64, x, ctx->LpI, ctx->PQ, ctx->m, prec, tw,
                    ctx->twmax, st,
                    ctx->prof ? ctx->pev.data() : nullptr));
-  for (const auto& F : ctx->fam) ctx->launches += F.active ? (F.lp ? 5 : 4) : 0;
-  ctx->launches += 1;  // the shared z pass of the face families
+  // one launch per x / y pass over all families, the shared z pass of the face
+  // families, one z pass per edge family
+  ctx->launches += 5;
+  for (const auto& F : ctx->fam) ctx->launches += (F.active && F.lp) ? 1 : 0;
   if (events) cudaEventRecord(ctx->ev[1], st);
   sparse_enqueue(ctx, x, y, ctx->LpI, ctx->PQ);
   if (events) cudaEventRecord(ctx->ev[2], st);

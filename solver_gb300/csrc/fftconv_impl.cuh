@@ -104,16 +104,57 @@ __device__ __forceinline__ void x_last_inplace(cx<R>* buf, const AxPlan& p) {
   }
 }
 
+// One launch runs a pass over every active family: the CTAs of family i are
+// [cta0, cta0 + gx * gy) of the 1-D grid, laid out as that family's own gx x gy grid.
+// Separate launches per family left each pass a train of partial waves (at 128x128x64 a
+// family's x pass is under one wave of CTAs) with a ramp-up and tail each.
 template <typename R>
-__global__ void __launch_bounds__(TPB) k_xfwd(const c64* __restrict__ xin,
-                                              const int32_t* __restrict__ map, cx<R>* T,
-                                              AxPlan p, int Ly, int nx, int ny,
-                                              const cx<R>* __restrict__ twm, int twmax) {
+struct FamPass {
+  cx<R>* T;             // family buffer
+  const int32_t* map;   // x passes: lattice map
+  c64* io;              // x passes: compact input (forward) / output (inverse)
+  AxPlan p;             // transform plan along the pass axis
+  int L_other;          // x passes: Ly; y passes: Lx
+  int a, b;             // x passes: lattice nx, ny; y passes: rows read, rows written
+  int gx;               // CTAs along the family grid's first axis
+  int cta0;             // first CTA of the family
+};
+constexpr int kMaxFam = 6;
+template <typename R>
+struct PassSet {
+  int nf;
+  FamPass<R> f[kMaxFam];
+};
+
+// this CTA's family, and its (x, y) block index in that family's grid
+template <typename R>
+__device__ __forceinline__ FamPass<R> pick_family(const PassSet<R>& s, int& bx, int& by) {
+  const int b = blockIdx.x;
+  FamPass<R> F = s.f[0];
+#pragma unroll
+  for (int i = 1; i < kMaxFam; ++i)
+    if (i < s.nf && b >= s.f[i].cta0) F = s.f[i];
+  const int lb = b - F.cta0;
+  bx = lb % F.gx;
+  by = lb / F.gx;
+  return F;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(TPB) k_xfwd(PassSet<R> s, const cx<R>* __restrict__ twm,
+                                              int twmax) {
   extern __shared__ unsigned char smem_raw[];
+  int bx, by;
+  const FamPass<R> F = pick_family(s, bx, by);
+  const c64* __restrict__ xin = F.io;
+  const int32_t* __restrict__ map = F.map;
+  cx<R>* T = F.T;
+  const AxPlan& p = F.p;
+  const int Ly = F.L_other, nx = F.a, ny = F.b;
   const int Lx = 1 << p.n;
   cx<R>* W = reinterpret_cast<cx<R>*>(smem_raw);
   cx<R>* buf = W + Lx;
-  const int y0 = blockIdx.x * TY, z = blockIdx.y;
+  const int y0 = bx * TY, z = by;
   load_twiddles<R>(W, twm, twmax, Lx);
   __syncthreads();
   qswitch<4>(p.q[0], [&](auto QC) {
@@ -163,15 +204,20 @@ __device__ __forceinline__ void xinv_last(const cx<R>* buf, c64* yout,
 }
 
 template <typename R>
-__global__ void __launch_bounds__(TPB) k_xinv(const cx<R>* __restrict__ T, c64* yout,
-                                              const int32_t* __restrict__ map, AxPlan p, int Ly,
-                                              int nx, int ny, const cx<R>* __restrict__ twm,
+__global__ void __launch_bounds__(TPB) k_xinv(PassSet<R> s, const cx<R>* __restrict__ twm,
                                               int twmax) {
   extern __shared__ unsigned char smem_raw[];
+  int bx, by;
+  const FamPass<R> F = pick_family(s, bx, by);
+  const cx<R>* __restrict__ T = F.T;
+  c64* yout = F.io;
+  const int32_t* __restrict__ map = F.map;
+  const AxPlan& p = F.p;
+  const int Ly = F.L_other, nx = F.a, ny = F.b;
   const int Lx = 1 << p.n;
   cx<R>* W = reinterpret_cast<cx<R>*>(smem_raw);
   cx<R>* buf = W + Lx;
-  const int y0 = blockIdx.x * TY, z = blockIdx.y;
+  const int y0 = bx * TY, z = by;
   load_twiddles<R>(W, twm, twmax, Lx);
   for (int q = threadIdx.x; q < TY << p.n; q += blockDim.x) {
     const int yy = q >> p.n, kx = q & (Lx - 1);
@@ -319,13 +365,18 @@ constexpr int slot_of() {
 // --------------------------------------------------------------------------- y pass
 // planes z < nz; rows y < n_in are read (zero padded to Ly), rows y < n_out written
 template <typename R, bool INV>
-__global__ void __launch_bounds__(TPB) k_ypass(cx<R>* T, int Lx, AxPlan p, int n_in, int n_out,
-                                               const cx<R>* __restrict__ twm, int twmax) {
+__global__ void __launch_bounds__(TPB) k_ypass(PassSet<R> s, const cx<R>* __restrict__ twm,
+                                               int twmax) {
   extern __shared__ unsigned char smem_raw[];
+  int bx, by;
+  const FamPass<R> F = pick_family(s, bx, by);
+  cx<R>* T = F.T;
+  const AxPlan& p = F.p;
+  const int Lx = F.L_other, n_in = F.a, n_out = F.b;
   const int Ly = 1 << p.n;
   cx<R>* W = reinterpret_cast<cx<R>*>(smem_raw);
   cx<R>* buf = W + Ly;
-  const int kx0 = blockIdx.x * TX, z = blockIdx.y;
+  const int kx0 = bx * TX, z = by;
   const int ncols = min(TX, Lx - kx0);
   cx<R>* col = T + (size_t)z * Ly * Lx + kx0;
   load_twiddles<R>(W, twm, twmax, Ly);
@@ -737,32 +788,61 @@ struct Plans {
 template <typename R>
 struct Launch {
   static cx<R>* buf(const Family& f) { return reinterpret_cast<cx<R>*>(f.T[slot_of<R>()]); }
-  static int xfwd(const Family& f, const c64* xin, const cx<R>* tw, int twmax, cudaStream_t st) {
-    const int Lx = f.L[0];
-    const size_t sm = sizeof(cx<R>) * (Lx + (size_t)Lx * XRS);
-    CTX_CHECK(smem_optin(k_xfwd<R>, sm));
-    dim3 g((f.dims[1] + TY - 1) / TY, f.dims[2]);
-    k_xfwd<R><<<g, TPB, sm, st>>>(xin, f.map, buf(f), Plans<R>::xy(f.logL[0]), f.L[1], f.dims[0],
-                                  f.dims[1], tw, twmax);
-    return 0;
-  }
-  static int xinv(const Family& f, c64* yout, const cx<R>* tw, int twmax, cudaStream_t st) {
-    const int Lx = f.L[0];
-    const size_t sm = sizeof(cx<R>) * (Lx + (size_t)Lx * XRS);
-    CTX_CHECK(smem_optin(k_xinv<R>, sm));
-    dim3 g((f.dims[1] + TY - 1) / TY, f.dims[2]);
-    k_xinv<R><<<g, TPB, sm, st>>>(buf(f), yout, f.map, Plans<R>::xy(f.logL[0]), f.L[1], f.dims[0],
-                                  f.dims[1], tw, twmax);
-    return 0;
-  }
-  template <bool INV>
-  static int ypass(const Family& f, const cx<R>* tw, int twmax, cudaStream_t st) {
-    const int Ly = f.L[1];
-    const size_t sm = sizeof(cx<R>) * (Ly + ((size_t)Ly << LTX));
-    CTX_CHECK(smem_optin(k_ypass<R, INV>, sm));
-    dim3 g((f.L[0] + TX - 1) / TX, f.dims[2]);
-    k_ypass<R, INV><<<g, TPB, sm, st>>>(buf(f), f.L[0], Plans<R>::xy(f.logL[1]),
-                                        INV ? Ly : f.dims[1], INV ? f.dims[1] : Ly, tw, twmax);
+  // kind 0: forward x, 1: inverse x, 2: forward y, 3: inverse y; io[f]: the compact
+  // vector of family f (x passes)
+  static int pass(int kind, const Family* F, int nfam, c64* const* io, const cx<R>* tw,
+                  int twmax, cudaStream_t st) {
+    PassSet<R> s{};
+    int ctas = 0;
+    size_t sm = 0;
+    for (int f = 0; f < nfam; ++f) {
+      if (!F[f].active) continue;
+      if (s.nf == kMaxFam) return set_error("too many families in one pass"), PEEC_ERR_UNSUPPORTED_INTERNAL;
+      const Family& fam = F[f];
+      FamPass<R>& d = s.f[s.nf++];
+      d.T = buf(fam);
+      d.map = fam.map;
+      d.io = io ? io[f] : nullptr;
+      d.cta0 = ctas;
+      int gy = fam.dims[2];
+      if (kind < 2) {
+        const int Lx = fam.L[0];
+        d.p = Plans<R>::xy(fam.logL[0]);
+        d.L_other = fam.L[1];
+        d.a = fam.dims[0];
+        d.b = fam.dims[1];
+        d.gx = (fam.dims[1] + TY - 1) / TY;
+        sm = std::max(sm, sizeof(cx<R>) * (Lx + (size_t)Lx * XRS));
+      } else {
+        const int Ly = fam.L[1];
+        d.p = Plans<R>::xy(fam.logL[1]);
+        d.L_other = fam.L[0];
+        d.a = kind == 3 ? Ly : fam.dims[1];
+        d.b = kind == 3 ? fam.dims[1] : Ly;
+        d.gx = (fam.L[0] + TX - 1) / TX;
+        sm = std::max(sm, sizeof(cx<R>) * (Ly + ((size_t)Ly << LTX)));
+      }
+      ctas += d.gx * gy;
+    }
+    if (s.nf == 0) return 0;
+    switch (kind) {
+      case 0:
+        CTX_CHECK(smem_optin(k_xfwd<R>, sm));
+        k_xfwd<R><<<ctas, TPB, sm, st>>>(s, tw, twmax);
+        break;
+      case 1:
+        CTX_CHECK(smem_optin(k_xinv<R>, sm));
+        k_xinv<R><<<ctas, TPB, sm, st>>>(s, tw, twmax);
+        break;
+      case 2:
+        CTX_CHECK(smem_optin(k_ypass<R, false>, sm));
+        k_ypass<R, false><<<ctas, TPB, sm, st>>>(s, tw, twmax);
+        break;
+      default:
+        CTX_CHECK(smem_optin(k_ypass<R, true>, sm));
+        k_ypass<R, true><<<ctas, TPB, sm, st>>>(s, tw, twmax);
+        break;
+    }
     return 0;
   }
   static int zconv3(const Family* F, const PSpec& S, const cx<R>* tw, int twmax,
@@ -801,12 +881,17 @@ int conv_all_t(const Family* F, int nfam, const Spectrum* spec, const void* cons
                cudaStream_t st, cudaEvent_t* ev) {
   using Lc = Launch<R>;
   const int p = slot_of<R>();
+  if (nfam > kMaxFam) return set_error("too many families"), PEEC_ERR_UNSUPPORTED_INTERNAL;
+  c64* in[kMaxFam];
+  c64* out[kMaxFam];
+  for (int f = 0; f < nfam; ++f) {
+    in[f] = const_cast<c64*>(F[f].lp ? x : x + m);
+    out[f] = F[f].lp ? LpI : PQ;
+  }
   if (ev) cudaEventRecord(ev[0], st);
-  for (int f = 0; f < nfam; ++f)
-    if (F[f].active) CTX_CHECK(Lc::xfwd(F[f], F[f].lp ? x : x + m, tw, twmax, st));
+  CTX_CHECK(Lc::pass(0, F, nfam, in, tw, twmax, st));
   if (ev) cudaEventRecord(ev[1], st);
-  for (int f = 0; f < nfam; ++f)
-    if (F[f].active) CTX_CHECK(Lc::template ypass<false>(F[f], tw, twmax, st));
+  CTX_CHECK(Lc::pass(2, F, nfam, nullptr, tw, twmax, st));
   if (ev) cudaEventRecord(ev[2], st);
   PSpec S{spec[0].d[p], spec[1].d[p], spec[2].d[p], spec[3].d[p], spec[4].d[p], spec[5].d[p],
           spec[0].oct,  spec[1].oct,  spec[2].oct,  spec[3].oct,  spec[4].oct,  spec[5].oct,
@@ -822,11 +907,9 @@ int conv_all_t(const Family* F, int nfam, const Spectrum* spec, const void* cons
       CTX_CHECK(Lc::zconv1(F[f], octant_spectra<R>() ? spec[3 + f].oct : spec[3 + f].d[p], tw,
                            twmax, st));
   if (ev) cudaEventRecord(ev[3], st);
-  for (int f = 0; f < nfam; ++f)
-    if (F[f].active) CTX_CHECK(Lc::template ypass<true>(F[f], tw, twmax, st));
+  CTX_CHECK(Lc::pass(3, F, nfam, nullptr, tw, twmax, st));
   if (ev) cudaEventRecord(ev[4], st);
-  for (int f = 0; f < nfam; ++f)
-    if (F[f].active) CTX_CHECK(Lc::xinv(F[f], F[f].lp ? LpI : PQ, tw, twmax, st));
+  CTX_CHECK(Lc::pass(1, F, nfam, out, tw, twmax, st));
   if (ev) cudaEventRecord(ev[5], st);
   return 0;
 }
