@@ -153,6 +153,23 @@ int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout, double tol
                      double* relres, int* outer_out, int* inner_total);
 
 /*
+ * Gradient of a port voltage in per-voxel parameters, by reciprocity. The operator's
+ * edge block is diagonal in a voxel parameter (conductivity: the resistance halves
+ * and the surface impedance, compute_diagonals.jl:10-12, compute_Zs_with_indices.jl:
+ * 27-32) and the unpreconditioned matrix satisfies K^T = D1 K D2 with diagonal D1,
+ * D2, so the port's adjoint solution is its forward solution rescaled. With I =
+ * x[0:m] the edge currents of the port solution x (N complex, host), returns per voxel
+ *   g[v] = (2/Is) * ( sum_{e: v1[e]=v} d1[e] I_e^2 + sum_{e: v2[e]=v} d2[e] I_e^2 ),
+ * the derivative of the port voltage 2(phi_n1 - phi_n2) with respect to the parameter
+ * of voxel v. d1 / d2 (m complex, host) are the derivatives of the edge impedance DZ_e
+ * with respect to the parameter of the edge's first / second voxel v1[e] / v2[e]
+ * (int32, -1: none). g: nvox complex (host). The reference has no gradient; this is
+ * the device half of the adjoint configuration (solver_gb300/gradient.py).
+ */
+int peec_adjoint(peec_ctx* ctx, const double* x, const int32_t* v1, const int32_t* v2,
+                 const double* d1, const double* d2, double Is, int64_t nvox, double* g);
+
+/*
  * Work split of the LU solves inside the operator: rows of connected components of
  * the factors with at most max_rows rows (0..512, default 0) are solved one
  * component per warp; all other rows by the synchronisation-free global scheme. Both

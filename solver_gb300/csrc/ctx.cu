@@ -65,6 +65,8 @@ void launch_xupdate(const c64*, const c64*, size_t, const c64*, const c64*, int,
 int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, double escal_Lp,
                   double escal_P, int Nx, int Ny, int Nz, double* const d_rows[9],
                   const int64_t row_len[9], int* d_bad, cudaStream_t st);
+void launch_adjoint(const c64*, const int32_t*, const int32_t*, const c64*, const c64*, double,
+                    int64_t, int64_t, double*, cudaStream_t);
 
 }  // namespace peec
 
@@ -1095,6 +1097,45 @@ extern "C" int peec_port_rhs(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, d
   PEEC_CUDA_TRY(cudaMemcpyAsync(tn, ctx->dy, sizeof(c64) * ctx->N, cudaMemcpyDeviceToHost, ctx->st));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return PEEC_OK;
+}
+
+extern "C" int peec_adjoint(peec_ctx* ctx, const double* x, const int32_t* v1,
+                            const int32_t* v2, const double* d1, const double* d2, double Is,
+                            int64_t nvox, double* g) {
+  if (!ctx || !x || !v1 || !v2 || !d1 || !d2 || !g || nvox < 0 || Is == 0) return badarg(__func__);
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  cudaSetDevice(ctx->dev);
+  const int64_t m = ctx->m;
+  int32_t *dv1 = nullptr, *dv2 = nullptr;
+  c64 *dd1 = nullptr, *dd2 = nullptr;
+  double* dg = nullptr;
+  int rc = PEEC_OK;
+  auto cleanup = [&]() {
+    cudaFree(dv1);
+    cudaFree(dv2);
+    cudaFree(dd1);
+    cudaFree(dd2);
+    cudaFree(dg);
+  };
+  if (dalloc(&dv1, m) || dalloc(&dv2, m) || dalloc(&dd1, m) || dalloc(&dd2, m) ||
+      dalloc(&dg, 2 * (size_t)std::max<int64_t>(nvox, 1))) {
+    cleanup();
+    return bad(ctx, PEEC_ERR_OOM, "peec_adjoint: device buffers");
+  }
+  cudaStream_t st = ctx->st;
+  cudaMemcpyAsync(ctx->dx, x, sizeof(c64) * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dv1, v1, sizeof(int32_t) * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dv2, v2, sizeof(int32_t) * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dd1, d1, sizeof(c64) * m, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(dd2, d2, sizeof(c64) * m, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(dg, 0, sizeof(double) * 2 * (size_t)std::max<int64_t>(nvox, 1), st);
+  launch_adjoint(ctx->dx, dv1, dv2, dd1, dd2, 2.0 / Is, m, nvox, dg, st);
+  ctx->launches++;
+  cudaMemcpyAsync(g, dg, sizeof(double) * 2 * (size_t)nvox, cudaMemcpyDeviceToHost, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) rc = fail_cuda(e, "peec_adjoint", __FILE__, __LINE__);
+  cleanup();
+  return rc;
 }
 
 // ------------------------------------------------------------------------------------

@@ -128,18 +128,23 @@ def dz_edges(w, escalings, diagonals, Zs_info, sigma_voxel, v1, v2, sigma_ref):
     return DZ, d1, d2
 
 
-def port_impedance_and_gradient(V, m, ns, port_nodes, z0, Is, d1, d2, v1, v2, nvox):
+def port_impedance_and_gradient(V, m, ns, port_nodes, z0, Is, d1, d2, v1, v2, nvox, op=None):
     """|Z| of a one-port geometry and d|Z|/d sigma_v for every voxel from the forward
-    solution V = [I; Q; phi] (edge currents first) and the DZ derivatives."""
+    solution V = [I; Q; phi] (edge currents first) and the DZ derivatives. With op (a
+    GpuOperator) the per-voxel scatter runs on the GPU (peec_adjoint); without, on the
+    host."""
     n1, n2 = (int(t) for t in port_nodes)
     val = 2.0 * (V[m + ns + n1] - V[m + ns + n2])
     Z = z0 * val / (2.0 * z0 - val)
     dZ_dval = 2.0 * z0 * z0 / (2.0 * z0 - val) ** 2
-    I2 = V[:m] ** 2
-    g = np.zeros(nvox, dtype=np.complex128)
-    ok1, ok2 = v1 >= 0, v2 >= 0
-    np.add.at(g, v1[ok1], (2.0 / Is) * d1[ok1] * I2[ok1])
-    np.add.at(g, v2[ok2], (2.0 / Is) * d2[ok2] * I2[ok2])
+    if op is not None:
+        g = op.adjoint(V, v1, v2, d1, d2, Is, nvox)
+    else:
+        I2 = V[:m] ** 2
+        g = np.zeros(nvox, dtype=np.complex128)
+        ok1, ok2 = v1 >= 0, v2 >= 0
+        np.add.at(g, v1[ok1], (2.0 / Is) * d1[ok1] * I2[ok1])
+        np.add.at(g, v2[ok2], (2.0 / Is) * d2[ok2] * I2[ok2])
     dZ = dZ_dval * g
     return abs(Z), np.real(np.conj(Z) * dZ) / abs(Z), Z
 
@@ -236,7 +241,7 @@ class PortImpedanceProblem:
         self._x[mode] = V
         absZ, g, Z = port_impedance_and_gradient(V, self.m, self.ns, (n1, n2), self.z0,
                                                  self.esc["Is"], d1, d2, self.v1, self.v2,
-                                                 self.nvox)
+                                                 self.nvox, op=self.op)
         return absZ, g, Z
 
     def finite_difference(self, k, voxels, h_rel=1e-6, tol=1e-12, maxit=600):

@@ -257,6 +257,25 @@ class GpuOperator:
         global)."""
         _lib.check(self.h, self.L.peec_set_lu_component_max(self.h, int(max_rows)))
 
+    def adjoint(self, x, v1, v2, d1, d2, Is, nvox):
+        """Per-voxel derivative of the port voltage from the port solution x by
+        reciprocity (peec_adjoint): (2/Is) * sum over each voxel's edges of
+        d1[e] I_e^2 (first voxel v1[e]) or d2[e] I_e^2 (second voxel v2[e])."""
+        x = np.ascontiguousarray(np.asarray(x, dtype=np.complex128).ravel())
+        if x.size < self.m:
+            raise ValueError("x must hold the edge currents first")
+        v1 = np.ascontiguousarray(np.asarray(v1, dtype=np.int32).ravel())
+        v2 = np.ascontiguousarray(np.asarray(v2, dtype=np.int32).ravel())
+        d1 = np.ascontiguousarray(np.asarray(d1, dtype=np.complex128).ravel())
+        d2 = np.ascontiguousarray(np.asarray(d2, dtype=np.complex128).ravel())
+        if not (v1.size == v2.size == d1.size == d2.size == self.m):
+            raise ValueError("v1, v2, d1, d2 need one entry per edge")
+        g = np.zeros(int(nvox), dtype=np.complex128)
+        _lib.check(self.h, self.L.peec_adjoint(
+            self.h, _lib.ptr(x), _lib.ptr(v1), _lib.ptr(v2), _lib.ptr(d1.view(np.float64)),
+            _lib.ptr(d2.view(np.float64)), float(Is), int(nvox), _lib.ptr(g.view(np.float64))))
+        return g
+
     def set_residual_precision(self, precision):
         """Arithmetic of the refinement residuals of solve_mixed: PREC_FF (float-float,
         default) or PREC_FP64."""

@@ -67,3 +67,19 @@ def test_autograd_function(bar):
     z.backward()
     _, g, _ = bar.solve(0, mode="fp64")
     assert np.allclose(sigma.grad.numpy(), g, rtol=1e-6, atol=1e-6 * np.max(np.abs(g)))
+
+
+def test_device_scatter_matches_host(problem):
+    """peec_adjoint (the per-voxel scatter on the GPU, double atomics) against the
+    host scatter of the same solution and derivative tables."""
+    k = 0
+    w = 2 * np.pi * problem.freqs[k] * problem.esc["freq"]
+    _fs, d1, d2 = problem._state(w, problem.sigma_ref_voxel)
+    absZ, g_dev, _ = problem.solve(k, mode="fp64", tol=1e-10, warm=False, maxit=600)
+    V = problem._x["fp64"]
+    n1, n2 = np.asarray(problem.ports["port_nodes"]).reshape(-1, 2)[0]
+    a_host, g_host, _ = G.port_impedance_and_gradient(
+        V, problem.m, problem.ns, (n1, n2), problem.z0, problem.esc["Is"], d1, d2, problem.v1,
+        problem.v2, problem.nvox)
+    assert a_host == absZ
+    assert np.max(np.abs(g_dev - g_host)) <= 1e-12 * np.max(np.abs(g_host))
