@@ -170,6 +170,15 @@ int peec_adjoint(peec_ctx* ctx, const double* x, const int32_t* v1, const int32_
                  const double* d1, const double* d2, double Is, int64_t nvox, double* g);
 
 /*
+ * Self-test of the bounded-wait failure path: runs the synchronisation-free
+ * triangular-solve kernel on a two-row system whose second row depends on a row that
+ * is never solved, so its dependency wait gives up after its poll limit (about 50 ms)
+ * and records the error word. Returns PEEC_ERR_TIMEOUT when that path works (the
+ * expected result); the context stays usable. No counterpart in the reference.
+ */
+int peec_check_wait_limit(peec_ctx* ctx);
+
+/*
  * Work split of the LU solves inside the operator: rows of connected components of
  * the factors with at most max_rows rows (0..512, default 0) are solved one
  * component per warp; all other rows by the synchronisation-free global scheme. Both

@@ -26,7 +26,7 @@ EXPORTS = ("peec_version", "peec_ctx_create", "peec_ctx_destroy", "peec_last_err
            "peec_launch_count", "peec_sizes", "peec_stream", "peec_conv_count",
            "peec_conv_info", "peec_profile_matvec", "peec_multidot",
            "peec_multidot_noalloc", "peec_set_residual_precision",
-           "peec_set_lu_component_max", "peec_adjoint")
+           "peec_set_lu_component_max", "peec_adjoint", "peec_check_wait_limit")
 
 
 PREC_FP64, PREC_FP32, PREC_FF = 0, 1, 2
@@ -64,6 +64,7 @@ def load(build_if_missing: bool = True):
     L.peec_version.restype = ctypes.c_int
     L.peec_set_residual_precision.argtypes = [P, ctypes.c_int]
     L.peec_set_lu_component_max.argtypes = [P, ctypes.c_int]
+    L.peec_check_wait_limit.argtypes = [P]
     L.peec_adjoint.argtypes = [P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
                                ctypes.c_int64, ctypes.c_void_p]

@@ -67,6 +67,7 @@ int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, doubl
                   const int64_t row_len[9], int* d_bad, cudaStream_t st);
 void launch_adjoint(const c64*, const int32_t*, const int32_t*, const c64*, const c64*, double,
                     int64_t, int64_t, double*, cudaStream_t);
+int selftest_wait_limit(int limit, cudaStream_t st, int* err_out);
 
 }  // namespace peec
 
@@ -1096,6 +1097,17 @@ extern "C" int peec_port_rhs(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, d
   ctx->launches++;
   PEEC_CUDA_TRY(cudaMemcpyAsync(tn, ctx->dy, sizeof(c64) * ctx->N, cudaMemcpyDeviceToHost, ctx->st));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return PEEC_OK;
+}
+
+extern "C" int peec_check_wait_limit(peec_ctx* ctx) {
+  if (!ctx) return badarg(__func__);
+  cudaSetDevice(ctx->dev);
+  int e = 0;
+  const int rc = selftest_wait_limit(1 << 16, ctx->st, &e);
+  if (rc) return ctx->err = g_err, rc;
+  ctx->launches += 2;
+  if (e) return bad(ctx, PEEC_ERR_TIMEOUT, "self-test: a dependency wait ran into its limit");
   return PEEC_OK;
 }
 

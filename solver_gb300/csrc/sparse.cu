@@ -345,5 +345,48 @@ int launch_sptrsv(const CompPlan& C, const int32_t* ord, int nL, int total, cons
   return launches;
 }
 
-}  // namespace peec
+// The bounded-wait failure path of k_sptrsv on a two-row lower triangle whose second row
+// depends on the first, with only the second row in the claim order: the first row's
+// flag is never set, so the dependency wait runs into `limit` polls, records the error
+// word and returns. Returns the error word (1 when the wait gave up).
+int selftest_wait_limit(int limit, cudaStream_t st, int* err_out) {
+  struct Host {
+    int32_t ptr[3] = {0, 0, 1};
+    int32_t col[1] = {0};
+    c64 val[1];
+    c64 dinv[2];
+    int32_t ord[32];
+    c64 b[2];
+    int32_t g_in[2] = {0, 1};
+    int ctl[4] = {0, 0, 0, 0};
+    int flag[2] = {0, 0};
+  } h;
+  h.val[0] = mk<double>(0.5, 0);
+  h.dinv[0] = h.dinv[1] = mk<double>(1, 0);
+  h.b[0] = h.b[1] = mk<double>(1, 0);
+  h.ord[0] = 1;
+  for (int i = 1; i < 32; ++i) h.ord[i] = -1;
+  Host* d = nullptr;
+  c64* yz = nullptr;
+  PEEC_CUDA_TRY(cudaMalloc(&d, sizeof(Host)));
+  if (cudaMalloc(&yz, 4 * sizeof(c64)) != cudaSuccess) {
+    cudaFree(d);
+    return fail_cuda(cudaErrorMemoryAllocation, "selftest buffers", __FILE__, __LINE__);
+  }
+  cudaMemcpyAsync(d, &h, sizeof(Host), cudaMemcpyHostToDevice, st);
+  SfTri L{d->ptr, d->col, d->val, d->dinv, d->flag};
+  SfTri U = L;
+  k_sptrsv_begin<<<1, 1, 0, st>>>(d->ctl);
+  k_sptrsv<<<1, SF_TPB, 0, st>>>(d->ord, 32, 32, L, U, d->b, d->g_in, nullptr, yz, yz + 2, d->ctl,
+                                  limit);
+  int e = 0;
+  cudaMemcpyAsync(&e, d->ctl + 2, sizeof(int), cudaMemcpyDeviceToHost, st);
+  const cudaError_t rc = cudaStreamSynchronize(st);
+  cudaFree(d);
+  cudaFree(yz);
+  if (rc != cudaSuccess) return fail_cuda(rc, "selftest_wait_limit", __FILE__, __LINE__);
+  *err_out = e;
+  return 0;
+}
 
+}  // namespace peec

@@ -289,8 +289,11 @@ class GpuOperator:
         relres = ctypes.c_double()
         outer = ctypes.c_int()
         inner = ctypes.c_int()
-        _lib.check(self.h, self.L.peec_solve_mixed(
+        rc = self.L.peec_solve_mixed(
             self.h, _lib.ptr(b), _lib.ptr(x), float(tol), float(inner_tol), int(inner_maxit),
             int(max_outer), ctypes.byref(flag), ctypes.byref(relres), ctypes.byref(outer),
-            ctypes.byref(inner)))
+            ctypes.byref(inner))
+        if rc == -3:  # cancelled by the stop flag: flag 99, as gmres reports it
+            return x, 99, 0.0, 0, 0
+        _lib.check(self.h, rc)
         return x, flag.value, relres.value, outer.value, inner.value
