@@ -17,6 +17,8 @@ from __future__ import annotations
 
 import math
 
+import time
+
 import numpy as np
 
 from . import frequency as fq
@@ -240,14 +242,16 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
                          ports_scatter_value, lumped_elements, expansions, GMRES_settings,
                          Zs_info, QS_Rcc_FW=1, id=None, chan=None, commentsEnabled=False, *,
                          mode="fp64", mixed_inner_tol=1e-7, mixed_warm_start=True,
-                         stop_flag=None, on_solve=None, lanes=1):
+                         stop_flag=None, on_solve=None, lanes=1, records=None):
     """Frequency x port sweep with warm starts (FFT_solver_QS_S_type.jl:1-234).
 
     mode "fp64": the reference algorithm (FP64 convolutions, Householder GMRES).
     mode "mixed": FP32 convolutions inside FP64 iterative refinement to the same
     relative residual. lanes > 1 (mixed, warm starts): the ports are spread over that
     many contexts (PortLanes), each sweeping its ports through every frequency on its
-    own. Returns {"S","Z","Y","f","info"}; None if stopped.
+    own. records: a path; one JSON line per port solve (frequency index and Hz, port,
+    mode, flag, relative residual, iterations, wall ms) is appended to it. Returns
+    {"S","Z","Y","f","info"}; None if stopped.
     """
     if QS_Rcc_FW != 1:
         raise NotImplementedError("only the quasi-static operator (QS_Rcc_FW == 1) is implemented")
@@ -293,7 +297,24 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
         pf.close()
     if res is not None:
         res["f"] = freq / escalings["freq"]
+        if records is not None:
+            _write_records(records, res["info"], res["f"], mode)
     return res
+
+
+def _write_records(path, info, f_hz, mode):
+    import json
+    with open(path, "a") as fh:
+        for r in info:
+            rec = {"freq_index": int(r["freq"]), "f_hz": float(f_hz[r["freq"]]),
+                   "port": int(r["port"]), "mode": mode, "flag": int(r["flag"]),
+                   "relres": float(r["relres"]), "ms": float(r.get("ms", 0.0))}
+            if "iter" in r:
+                rec["iterations"] = [int(t) for t in r["iter"]]
+            if "outer" in r:
+                rec["outer"] = int(r["outer"])
+                rec["inner"] = int(r["niter"])
+            fh.write(json.dumps(rec) + "\n")
 
 
 def _port_column(V, pn, c1, m, ns, z0):
@@ -353,6 +374,7 @@ def _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode, mixed_inne
         for c1 in range(npt):
             n1, n2 = pn[c1]
             tn = op.port_rhs(n1, n2, escalings["Is"])
+            t0 = time.perf_counter()
             if mode == "fp64":
                 V, flag, relres, it, resvec = op.gmres(tn, Vrest[:, c1], tk, inner)
                 rec = {"flag": flag, "relres": relres, "iter": it, "niter": len(resvec) - 1}
@@ -366,7 +388,7 @@ def _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode, mixed_inne
                 raise ValueError(mode)
             if flag == 99:
                 return None
-            rec.update(freq=k, port=c1)
+            rec.update(freq=k, port=c1, ms=(time.perf_counter() - t0) * 1e3)
             info.append(rec)
             if on_solve:
                 on_solve(k, c1, V)

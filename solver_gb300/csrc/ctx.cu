@@ -14,10 +14,21 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "ctx.hpp"
 #include "peec_gb300.h"
 
 namespace peec {
+
+// NVTX ranges around the C-ABI entry points (header-only NVTX 3: no cost unless a
+// profiler attaches), so a timeline shows fill, frequency set-up and solves per context
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 static thread_local std::string g_err;
 void set_error(const std::string& msg) { g_err = msg; }
@@ -366,6 +377,7 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
                                  int64_t mz, const int64_t* edge_cell, const int64_t* edge_n1,
                                  const int64_t* edge_n2, int64_t ns, const int32_t* surf_fam,
                                  const int64_t* surf_cell, const int64_t* surf_node, int64_t n) {
+  NvtxRange nvtx_range_("peec_set_topology");
   drop_graphs(ctx);
   if (!ctx) return badarg(__func__);
   if (Nx < 1 || Ny < 1 || Nz < 1 || mx < 0 || my < 0 || mz < 0 || ns < 0 || n < 1)
@@ -551,6 +563,7 @@ static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
 }
 
 extern "C" int peec_set_rows(peec_ctx* ctx, const double* const rows[9]) {
+  NvtxRange nvtx_range_("peec_set_rows");
   if (!ctx || !rows) return badarg(__func__);
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
@@ -574,6 +587,7 @@ extern "C" int peec_set_rows(peec_ctx* ctx, const double* const rows[9]) {
 
 extern "C" int peec_fill(peec_ctx* ctx, const double origin[3], double sx, double sy, double sz,
                          double escal_Lp, double escal_P, double* const rows_out[9]) {
+  NvtxRange nvtx_range_("peec_fill");
   if (!ctx || !origin) return badarg(__func__);
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
@@ -798,6 +812,7 @@ extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int
                                   const int64_t* U_ptr, const int64_t* U_col,
                                   const double* U_val, const int64_t* perm_r,
                                   const int64_t* perm_c, const double* row_scale) {
+  NvtxRange nvtx_range_("peec_set_frequency");
   drop_graphs(ctx);
   if (!ctx || !DZ || !L_ptr || !U_ptr || !perm_r || !perm_c) return badarg(__func__);
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
@@ -972,6 +987,7 @@ static int matvec_dev(peec_ctx* ctx, const c64* x, c64* y, int prec, bool timed)
 }
 
 extern "C" int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precision) {
+  NvtxRange nvtx_range_("peec_matvec_dev");
   if (!ctx || !x || !y) return badarg(__func__);
   if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
   cudaSetDevice(ctx->dev);
@@ -985,6 +1001,7 @@ extern "C" int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precis
 }
 
 extern "C" int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precision) {
+  NvtxRange nvtx_range_("peec_matvec");
   if (!ctx || !x || !y) return badarg(__func__);
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
@@ -1079,6 +1096,7 @@ extern "C" int peec_last_timing(peec_ctx* ctx, double* total_ms, double* conv_ms
 }
 
 extern "C" int peec_port_rhs(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, double* tn) {
+  NvtxRange nvtx_range_("peec_port_rhs");
   if (!ctx || !tn) return badarg(__func__);
   if (!ctx->have_freq || !ctx->have_pdiag) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
   if (n1 < 0 || n1 >= ctx->n || n2 < 0 || n2 >= ctx->n) return bad(ctx, PEEC_ERR_BADARG, "port node out of range");
@@ -1114,6 +1132,7 @@ extern "C" int peec_check_wait_limit(peec_ctx* ctx) {
 extern "C" int peec_adjoint(peec_ctx* ctx, const double* x, const int32_t* v1,
                             const int32_t* v2, const double* d1, const double* d2, double Is,
                             int64_t nvox, double* g) {
+  NvtxRange nvtx_range_("peec_adjoint");
   if (!ctx || !x || !v1 || !v2 || !d1 || !d2 || !g || nvox < 0 || Is == 0) return badarg(__func__);
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
@@ -1568,6 +1587,7 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
 extern "C" int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, double tol, int maxit,
                           int restarted, int restart, int precision, int* flag, double* relres,
                           int* iter, double* resvec, int resvec_cap, int* nres) {
+  NvtxRange nvtx_range_("peec_gmres");
   if (!ctx || !b || !x_inout || !flag || !relres || !iter) return badarg(__func__);
   if (maxit < 1 || (restarted && restart < 1)) return bad(ctx, PEEC_ERR_BADARG, "maxit/restart must be >= 1");
   if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
@@ -1594,6 +1614,7 @@ extern "C" int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, doubl
 extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout, double tol,
                                 double inner_tol, int inner_maxit, int max_outer, int* flag,
                                 double* relres, int* outer_out, int* inner_total) {
+  NvtxRange nvtx_range_("peec_solve_mixed");
   if (!ctx || !b || !x_inout || !flag || !relres) return badarg(__func__);
   if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
   cudaSetDevice(ctx->dev);

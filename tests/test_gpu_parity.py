@@ -196,7 +196,8 @@ def test_mixed_solve(case, resid):
     assert _rel(x, x_ref) < 1e-6
 
 
-def test_sweep_parity(case):
+def test_sweep_parity(case, tmp_path):
+    import json
     from solver_gb300 import api
     c = case
     st = {"Inner_Iter": c["settings"]["Inner_Iter"],
@@ -205,11 +206,15 @@ def test_sweep_parity(case):
                                  c["diag"], c["ports"], c["z0"], c["le"], c["exp"], st, c["Zs"])
     c["exp"]["gpu_ctx"] = c["op"]
     h = api.CirculantSpectra(c["op"])
+    rec = tmp_path / "solves.jsonl"
     got = api.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], h, h, c["diag"], c["ports"],
-                                   c["z0"], c["le"], c["exp"], st, c["Zs"])
+                                   c["z0"], c["le"], c["exp"], st, c["Zs"], records=str(rec))
     assert [r["niter"] for r in got["info"]] == [len(r["resvec"]) - 1 for r in ref["info"]]
     assert _rel(got["Z"], ref["Z"]) < 1e-10
     assert _rel(got["Vrest"], ref["Vrest"]) < 1e-10
+    lines = [json.loads(t) for t in rec.read_text().splitlines()]
+    assert len(lines) == len(got["info"])
+    assert all(r["mode"] == "fp64" and r["flag"] == r0["flag"] for r, r0 in zip(lines, got["info"]))
 
 
 @pytest.mark.parametrize("lanes", [1, 2])
