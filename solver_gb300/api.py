@@ -405,6 +405,57 @@ def _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode, mixed_inne
             "info": info, "Vrest": Vrest}
 
 
+def dump_json_data(matrix_Z, matrix_S, matrix_Y, num_ports, id, partial=False, freqIndex=None):
+    """The results dictionary of the reference (format_input_output_solver_functions.jl:
+    1-31): per port pair (i outer, j inner) a list holding the per-frequency [re, im]
+    pairs, each matrix serialised as a JSON string."""
+    import json
+
+    def enc(M):
+        M = np.asarray(M, dtype=np.complex128)
+        return json.dumps([[[[float(v.real), float(v.imag)] for v in M[i, j, :]]]
+                           for i in range(num_ports) for j in range(num_ports)])
+
+    return {"matrices": {"matrix_Z": enc(matrix_Z), "matrix_S": enc(matrix_S),
+                         "matrix_Y": enc(matrix_Y)},
+            "isStopped": False, "id": id, "partial": partial, "freqIndex": freqIndex}
+
+
+def do_solving_fft(request, id="job", mode="mixed", lanes=1, device=0, stop_flag=None,
+                   records=None):
+    """A solve request end to end, as the reference's doSolvingFFT does it
+    (do_solving_fft.jl:1-177) without its message queue and object store: the request
+    body (mesherOutput / solverInput / solverAlgoParams / solverType) through the mesher,
+    the GPU fill and the frequency x port sweep. Returns the reference's results
+    dictionary (dump_json_data) plus "S", "Z", "Y" (ports x ports x frequencies) and
+    "f"; None if stopped. mode "fp64" runs the reference algorithm, "mixed" the mixed
+    precision solves (lanes: port lanes, see FFT_solver_QS_S_type)."""
+    from . import mesher
+    solver_type = int(request.get("solverType", 1))
+    if solver_type != 1:
+        raise NotImplementedError("only the quasi-static solver (solverType 1) is implemented")
+    out, freqs, settings, z0, grid = mesher.parse_request(request)
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    op = GpuOperator(inc, exp, diag["P"], device=device)
+    try:
+        op.fill(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"])
+        exp["gpu_ctx"] = op
+        h = CirculantSpectra(op)
+        st = {"Inner_Iter": settings["Inner_Iter"],
+              "tol": np.full(len(freqs), settings["tol"])}
+        res = FFT_solver_QS_S_type(freqs, esc, inc, h, h, diag, ports, z0, le, exp, st, Zs,
+                                   mode=mode, lanes=lanes, stop_flag=stop_flag, records=records)
+    finally:
+        exp.pop("gpu_ctx", None)
+        op.close()
+    if res is None:
+        return None
+    npt = res["S"].shape[0]
+    outd = dump_json_data(res["Z"], res["S"], res["Y"], npt, id)
+    outd.update(S=res["S"], Z=res["Z"], Y=res["Y"], f=res["f"], info=res["info"])
+    return outd
+
+
 def sweep_many(requests, mode="mixed", concurrency=4, device=0):
     """Frequency sweeps of several geometries, concurrently: each geometry gets its own
     context (CUDA stream, fill, spectra, workspaces) and host thread, so the sweeps' kernels

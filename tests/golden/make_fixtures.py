@@ -1,8 +1,9 @@
 """Regenerates the committed fixtures under tests/golden/.
 
-* ``first_run_data.json`` / ``first_run_data_2_materials.json``: the reference's own
-  FFT-solver request bodies (inputs only; the reference ships no outputs for this
-  path), copied verbatim from the reference checkout given as argv[1].
+* ``first_run_data.json`` / ``first_run_data_2_materials.json`` / ``crossbar.json.gz``:
+  the reference's own FFT-solver request bodies (inputs only; the reference ships no
+  outputs for this path), copied verbatim (the crossbar gzip-compressed) from the
+  reference checkout given as argv[1].
 * ``oracle_*.npz``: outputs of the CPU oracle (oracle/peec_oracle.py) on those inputs
   (the two-material one at 1 GHz and 3 GHz) and on the 20x20x4 crossbar configuration, kept as regression pins of the oracle
   itself (rows, one matvec on a seeded vector, the port solution and Z).
@@ -44,6 +45,11 @@ def main():
     ref = Path(sys.argv[1])
     for name in ("first_run_data.json", "first_run_data_2_materials.json"):
         shutil.copyfile(ref / name, HERE / name)
+    # the 57x57x13 crossbar request (2 ports, 7 lumped elements, thin cells whose rows
+    # reach the far-field fill branches), gzip-compressed: its voxel grid is 1.4 MB of JSON
+    import gzip
+    with open(ref / "crossbar.json", "rb") as src, gzip.open(HERE / "crossbar.json.gz", "wb") as dst:
+        shutil.copyfileobj(src, dst)
     oracle_case(mesher.load_request(HERE / "first_run_data.json"), "first_run_data")
     # the two-material fixture at 1 GHz and 3 GHz: its face rows reach the far-field
     # (suppressed) branches of the P integrals

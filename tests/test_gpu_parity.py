@@ -408,3 +408,43 @@ def test_mixed_warm_start_reuses_convolutions(case):
         assert la < lb, (la, lb)
     finally:
         other.close()
+
+
+def test_do_solving_fft_end_to_end():
+    """The reference's request fixture end to end (mesher, GPU fill, sweep) in the
+    reference's results format, against the oracle's sweep on the oracle's fill, at the
+    fixture's own tolerance (1e-4) and at 1 GHz / 3 GHz."""
+    import json
+    from solver_gb300 import api
+    req = _at(mesher.load_request(GOLDEN / "first_run_data.json"), [1e9, 3e9])
+    got = api.do_solving_fft(req, id="fixture", mode="fp64")
+    c = _case(req)
+    st = {"Inner_Iter": c["settings"]["Inner_Iter"], "tol": np.full(2, c["settings"]["tol"])}
+    ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
+                                 c["diag"], c["ports"], c["z0"], c["le"], c["exp"], st, c["Zs"])
+    assert _rel(got["Z"], ref["Z"]) < 1e-8
+    mz = json.loads(got["matrices"]["matrix_Z"])
+    npt = got["Z"].shape[0]
+    assert len(mz) == npt * npt and len(mz[0][0]) == 2
+    assert mz[0][0][1] == [float(got["Z"][0, 0, 1].real), float(got["Z"][0, 0, 1].imag)]
+
+
+def test_reference_crossbar_fixture():
+    """The reference's 57x57x13 crossbar request (2 ports, 7 lumped elements, thin cells:
+    its rows take the far-field fill branches) end to end on the GPU -- mesher, GPU
+    fill, FP64 sweep at the fixture's own tolerance (1e-4, 150 inner iterations) -- at
+    its first two frequencies, against the oracle's fill and sweep: the same flags and
+    iteration counts, port impedances within 1e-8."""
+    import gzip
+    import json
+    from solver_gb300 import api
+    req = json.loads(gzip.open(GOLDEN / "crossbar.json.gz").read())
+    req["solverInput"]["frequencies"] = req["solverInput"]["frequencies"][:2]
+    got = api.do_solving_fft(req, id="crossbar", mode="fp64")
+    c = _case(req)
+    st = {"Inner_Iter": c["settings"]["Inner_Iter"], "tol": np.full(2, c["settings"]["tol"])}
+    ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
+                                 c["diag"], c["ports"], c["z0"], c["le"], c["exp"], st, c["Zs"])
+    assert [r["flag"] for r in got["info"]] == [r["flag"] for r in ref["info"]]
+    assert [r["niter"] for r in got["info"]] == [len(r["resvec"]) - 1 for r in ref["info"]]
+    assert _rel(got["Z"], ref["Z"]) < 1e-8
