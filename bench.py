@@ -224,8 +224,29 @@ def setup_problem(device=0, grid=None):
     op = GpuOperator(inc, exp, diag["P"], device=device)
     rows = op.fill(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"],
                    return_rows=True)
+    # the fill again, timed: nine generating rows on the GPU plus their spectra
+    t = time.perf_counter()
+    op.fill(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"])
+    fill_s = time.perf_counter() - t
     return dict(req=req, esc=esc, inc=inc, cc=cc, diag=diag, exp=exp, ports=ports, le=le,
-                Zs=Zs, freqs=freqs, settings=settings, z0=z0, grid=grid, op=op, rows=rows)
+                Zs=Zs, freqs=freqs, settings=settings, z0=z0, grid=grid, op=op, rows=rows,
+                fill_s=fill_s)
+
+
+def fill_report(P, with_cpu):
+    """Fill throughput: row entries per second of the GPU fill (rows and spectra), and of
+    the oracle's C fill with OpenMP on every host core (the cpu_baseline leg)."""
+    entries = int(sum(np.asarray(r).size for r in P["rows"].values()))
+    out = {"entries": entries, "gpu_ms": P["fill_s"] * 1e3,
+           "gpu_entries_per_s": entries / P["fill_s"]}
+    if with_cpu:
+        from oracle import peec_oracle as O
+        t = time.perf_counter()
+        O.fill_rows(P["cc"], P["esc"], *P["grid"])
+        cpu_s = time.perf_counter() - t
+        out.update(cpu_ms=cpu_s * 1e3, cpu_entries_per_s=entries / cpu_s,
+                   cpu_cores=os.cpu_count() or 1, cpu_kind="port")
+    return out
 
 
 def freq_state(P, k):
@@ -735,6 +756,7 @@ def main():
                      "traffic": z_traffic(P["grid"]), "bytes_per_matvec": b32["z"],
                      "launches_per_matvec": 4},
     }
+    line["fill"] = fill_report(P, rank == 0 and ws == 1 and not args.no_cpu_baseline)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(P, mv_per_port,
                                             "matvec count measured by the FP64 run above")

@@ -61,17 +61,24 @@ int launch_sptrsv(const CompPlan&, const int32_t*, int, int, const SfTri&, const
                   const c64*, const int32_t*, const double*, c64*, c64*, int*, cudaStream_t);
 int red_blocks(size_t N);
 int launch_multidot(const c64*, size_t, const c64*, size_t, int, c64*, c64*, cudaStream_t);
+int launch_multidot(const cff*, size_t, const c64*, size_t, int, c64*, c64*, cudaStream_t);
+int launch_multidot(const cff*, size_t, const cff*, size_t, int, c64*, c64*, cudaStream_t);
 void launch_multiaxpy(const c64*, size_t, const c64*, int, const c64*, int, size_t, c64*, size_t,
+                      double*, cudaStream_t);
+void launch_multiaxpy(const cff*, size_t, const c64*, int, const c64*, int, size_t, c64*, size_t,
                       double*, cudaStream_t);
 void launch_norm2(const c64*, size_t, size_t, double*, double*, cudaStream_t);
 void launch_sum_parts(const double*, int, double*, cudaStream_t);
 void launch_scale_rnorm(c64*, size_t, const double*, cudaStream_t);
 void launch_make_reflector(const c64*, size_t, int, c64, double, c64*, cudaStream_t);
+void launch_make_reflector(const c64*, size_t, int, c64, double, cff*, cudaStream_t);
 void launch_sub(const c64*, const c64*, size_t, c64*, cudaStream_t);
 void launch_add(const c64*, const c64*, size_t, c64*, cudaStream_t);
 void launch_differs(const c64*, const c64*, size_t, int*, cudaStream_t);
 void launch_tri(c64*, int, int, const c64*, c64*, int, cudaStream_t);
 void launch_xupdate(const c64*, const c64*, size_t, const c64*, const c64*, int, size_t, c64*,
+                    cudaStream_t);
+void launch_xupdate(const c64*, const cff*, size_t, const c64*, const c64*, int, size_t, c64*,
                     cudaStream_t);
 int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, double escal_Lp,
                   double escal_P, int Nx, int Ny, int Nz, double* const d_rows[9],
@@ -152,7 +159,9 @@ struct peec_ctx {
   c64 *dx = nullptr, *dy = nullptr;  // device N
   // krylov workspace
   int kcap = 0;
-  c64* U = nullptr;
+  c64* U = nullptr;     // reflector basis of the FP64 / float-float solves, N x kcap_u
+  cff* U32 = nullptr;   // reflector basis of the FP32-operator (inner) solves, float-float, N x kcap_u32
+  int kcap_u = 0, kcap_u32 = 0;
   c64 *gb = nullptr, *gx = nullptr, *gr = nullptr, *gv = nullptr, *gw = nullptr, *gxm = nullptr,
       *gxmin = nullptr, *gtmp = nullptr, *gzero = nullptr;
   c64 *dcoef = nullptr, *dcoef2 = nullptr, *dpart = nullptr, *dT = nullptr;
@@ -316,7 +325,7 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   void* ptrs[] = {ctx->tw64, ctx->tw32, ctx->twff, ctx->n1, ctx->n2, ctx->snode, ctx->invP, ctx->ne_ptr,
                   ctx->ne_idx, ctx->nsn_ptr, ctx->nsn_idx, ctx->DZ, ctx->yle_ptr, ctx->yle_col,
                   ctx->yle_val, ctx->g_in, ctx->g_out, ctx->lu_rs, ctx->LpI, ctx->PQ, ctx->Y1, ctx->U1,
-                  ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->lutmp2, ctx->dx, ctx->dy, ctx->U,
+                  ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->lutmp2, ctx->dx, ctx->dy, ctx->U, (c64*)ctx->U32,
                   ctx->gb, ctx->gx, ctx->gr, ctx->gv, ctx->gw, ctx->gxm, ctx->gxmin, ctx->gtmp,
                   ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal, ctx->dT,
                   ctx->mdpart};
@@ -1173,10 +1182,20 @@ extern "C" int peec_adjoint(peec_ctx* ctx, const double* x, const int32_t* v1,
 // Householder GMRES (gmres_custom.jl:1-331) on device vectors
 // ------------------------------------------------------------------------------------
 
-static int ensure_krylov(peec_ctx* ctx, int k) {
-  if (ctx->kcap >= k && ctx->U) return PEEC_OK;
+// work vectors for Krylov solves of up to k reflectors, and the reflector basis in the
+// storage the solve's precision uses (complex float-float for the FP32-operator solves)
+static int ensure_krylov(peec_ctx* ctx, int k, int prec) {
   const size_t N = ctx->N;
-  CTX_TRY(dalloc(&ctx->U, N * (size_t)k));
+  if (prec == PEEC_PREC_FP32) {
+    if (ctx->kcap_u32 < k) {
+      CTX_TRY(dalloc(&ctx->U32, N * (size_t)k));
+      ctx->kcap_u32 = k;
+    }
+  } else if (ctx->kcap_u < k) {
+    CTX_TRY(dalloc(&ctx->U, N * (size_t)k));
+    ctx->kcap_u = k;
+  }
+  if (ctx->kcap >= k) return PEEC_OK;
   for (c64** p : {&ctx->gb, &ctx->gx, &ctx->gr, &ctx->gv, &ctx->gw, &ctx->gxm, &ctx->gxmin,
                   &ctx->gtmp, &ctx->gzero})
     CTX_TRY(dalloc(p, N));
@@ -1284,16 +1303,24 @@ static void apply_Q(Gm& g, const std::vector<cd>& Utop, int ldt, int k, const st
   g.to_dev(ctx->dcoef2, h);
   g.to_dev(ctx->dcoef + k, yy);
   launch_tri(ctx->dT, ctx->kcap, k, ctx->dcoef2, ctx->dcoef, 0, g.st);  // c = T h
-  launch_xupdate(base ? base : ctx->gzero, ctx->U, g.N, ctx->dcoef, ctx->dcoef + k, k, g.N, out,
-                 g.st);
+  if (g.prec == PEEC_PREC_FP32)
+    launch_xupdate(base ? base : ctx->gzero, ctx->U32, g.N, ctx->dcoef, ctx->dcoef + k, k, g.N,
+                   out, g.st);
+  else
+    launch_xupdate(base ? base : ctx->gzero, ctx->U, g.N, ctx->dcoef, ctx->dcoef + k, k, g.N, out,
+                   g.st);
   ctx->launches += 2;
 }
 
 // x0_zero: the caller guarantees x_dev == 0, so the initial residual is b itself (A*0 is
-// exactly 0 in every precision) and its operator application is skipped
+// exactly 0 in every precision) and its operator application is skipped.
+// trust_recursive: convergence is decided on the recursive (least-squares) residual
+// without the confirming true-residual application -- for the inner solves of the mixed
+// solve, whose refinement loop computes the true residual of the corrected solution next.
 static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, int maxit,
                      int restarted, int restart, int prec, int* flag_out, double* relres_out,
-                     int* iter_out, std::vector<double>& resvec_out, bool x0_zero = false) {
+                     int* iter_out, std::vector<double>& resvec_out, bool x0_zero = false,
+                     bool trust_recursive = false) {
   const size_t N = ctx->N;
   int n = (int)N;
   int outer, inner;
@@ -1307,9 +1334,12 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
   }
   if (inner < 1) inner = 1;
   if (2 * (inner + 1) > Gm::kSlot) return bad(ctx, PEEC_ERR_UNSUPPORTED, "inner iterations above 2047");
-  CTX_TRY(ensure_krylov(ctx, inner + 1));
+  CTX_TRY(ensure_krylov(ctx, inner + 1, prec));
   Gm g{ctx, N, prec, ctx->st};
   const int ldT = ctx->kcap;
+  // FP32-operator solves keep their reflectors in complex float-float, with float-float
+  // arithmetic in the basis kernels; FP64 and float-float-operator solves in complex double
+  const bool f32 = prec == PEEC_PREC_FP32;
   c64 *b = ctx->gb, *x = ctx->gx, *r = ctx->gr, *v = ctx->gv, *xm = ctx->gxm,
       *xmin = ctx->gxmin, *add = ctx->gw;
   g.copy(b, b_dev);
@@ -1370,7 +1400,10 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
       const cd beta = sgn(rh[0]) * normr;
       const double nu2 = normr * normr - std::norm(rh[0]) + std::norm(rh[0] + beta);
       const double sc = 1.0 / std::sqrt(nu2);
-      launch_make_reflector(r, N, 0, mk<double>(beta.real(), beta.imag()), sc, ctx->U, ctx->st);
+      if (f32)
+        launch_make_reflector(r, N, 0, mk<double>(beta.real(), beta.imag()), sc, ctx->U32, ctx->st);
+      else
+        launch_make_reflector(r, N, 0, mk<double>(beta.real(), beta.imag()), sc, ctx->U, ctx->st);
       ctx->launches++;
       for (int i = 0; i < headlen; ++i) Utop[i] = (i == 0 ? rh[0] + beta : rh[i]) * sc;
       launch_tri(ctx->dT, ldT, 0, ctx->dcoef2, ctx->dT, 2, ctx->st);  // T(0,0) = 2
@@ -1394,7 +1427,8 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
         for (int col = 0; col < k; ++col) rb[col] = std::conj(Utop[(size_t)col * ld + j]);
         g.to_dev(ctx->dcoef2, rb);
         launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dcoef, 0, ctx->st);
-        launch_multiaxpy(ctx->U, N, nullptr, j, ctx->dcoef, k, N, v, N, nullptr, ctx->st);
+        if (f32) launch_multiaxpy(ctx->U32, N, nullptr, j, ctx->dcoef, k, N, v, N, nullptr, ctx->st);
+        else launch_multiaxpy(ctx->U, N, nullptr, j, ctx->dcoef, k, N, v, N, nullptr, ctx->st);
         launch_norm2(v, N, 0, ctx->dred, ctx->dscal, ctx->st);
         launch_scale_rnorm(v, N, ctx->dscal, ctx->st);
         ctx->launches += 5;
@@ -1405,10 +1439,15 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
       double alpha2 = 0.0;
       std::vector<cd> vh;
       {
-        ctx->launches += launch_multidot(ctx->U, N, add, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
+        ctx->launches += f32 ? launch_multidot(ctx->U32, N, add, N, k, ctx->dpart, ctx->dcoef2, ctx->st)
+                             : launch_multidot(ctx->U, N, add, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
         launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dcoef, 1, ctx->st);  // c = T^H z
-        launch_multiaxpy(ctx->U, N, add, 0, ctx->dcoef, k, N, v, (size_t)initer, ctx->dred,
-                         ctx->st);
+        if (f32)
+          launch_multiaxpy(ctx->U32, N, add, 0, ctx->dcoef, k, N, v, (size_t)initer, ctx->dred,
+                           ctx->st);
+        else
+          launch_multiaxpy(ctx->U, N, add, 0, ctx->dcoef, k, N, v, (size_t)initer, ctx->dred,
+                           ctx->st);
         launch_sum_parts(ctx->dred, red_blocks(N), ctx->dscal, ctx->st);
         ctx->launches += 3;
         cudaMemcpyAsync(ctx->hscal, ctx->dscal, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
@@ -1425,14 +1464,19 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
           const cd a = sgn(vj1) * alpha;
           const double nu2 = alpha2 - std::norm(vj1) + std::norm(vj1 + a);
           const double sc = 1.0 / std::sqrt(nu2);
-          c64* unew = ctx->U + (size_t)initer * N;
-          launch_make_reflector(v, N, initer, mk<double>(a.real(), a.imag()), sc, unew, ctx->st);
+          c64* unew = f32 ? nullptr : ctx->U + (size_t)initer * N;
+          cff* unew32 = f32 ? ctx->U32 + (size_t)initer * N : nullptr;
+          if (f32)
+            launch_make_reflector(v, N, initer, mk<double>(a.real(), a.imag()), sc, unew32, ctx->st);
+          else
+            launch_make_reflector(v, N, initer, mk<double>(a.real(), a.imag()), sc, unew, ctx->st);
           for (int i = 0; i < headlen; ++i)
             Utop[(size_t)initer * ld + i] =
                 i < initer ? cd(0) : (i == initer ? (vh[i] + a) * sc : vh[i] * sc);
           // T(0:k, k) = -2 T(0:k,0:k) (U(:,0:k)^H u_k), T(k,k) = 2 -- all on the device
           ctx->launches +=
-              launch_multidot(ctx->U, N, unew, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
+              f32 ? launch_multidot(ctx->U32, N, unew32, N, k, ctx->dpart, ctx->dcoef2, ctx->st)
+                  : launch_multidot(ctx->U, N, unew, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
           launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dT + (size_t)k * ldT, 2, ctx->st);
           ctx->launches += 2;
           for (int i = initer + 1; i <= inner; ++i) vs[i] = 0;
@@ -1487,6 +1531,14 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
           else stag = 0;
           g.copy(ctx->gtmp, xm);
           apply_Q(g, Utop, ld, initer, addvc, ctx->gtmp, xm);
+        }
+        if (trust_recursive && normr <= tolb) {
+          g.copy(x, xm);
+          normr_act = normr;
+          flag = 0;
+          it0 = outiter;
+          it1 = initer;
+          break;
         }
         g.residual(b, xm, r);
         const double nr = g.norm(r);
@@ -1621,7 +1673,7 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
   const size_t N = ctx->N, bytes = sizeof(c64) * N;
   c64 *db = ctx->ir_b, *dxv = ctx->ir_x, *dr = ctx->ir_r, *dd = ctx->ir_d;
   auto cleanup = [&]() {};
-  CTX_TRY(ensure_krylov(ctx, std::max(inner_maxit, 1) + 1));
+  CTX_TRY(ensure_krylov(ctx, std::max(inner_maxit, 1) + 1, PEEC_PREC_FP32));
   cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, ctx->st);
   cudaMemcpyAsync(dxv, x_inout, bytes, cudaMemcpyHostToDevice, ctx->st);
   Gm g{ctx, N, ctx->resid_prec, ctx->st};

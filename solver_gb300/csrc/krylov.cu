@@ -12,6 +12,27 @@
 
 namespace peec {
 
+// Basis storage: complex double (the FP64 solves) or complex float-float (the inner
+// solves of the mixed solve), and the arithmetic follows the storage. GB300 runs FP64 at
+// about 1/60 of its FP32 rate, and these kernels do eight flops per basis element and
+// column, so with FP64 arithmetic they are FP64-pipe bound at a fraction of HBM speed;
+// float-float arithmetic (FP32 error-free transformations, ~2^-48) keeps the basis at
+// FP64-like accuracy with the same 16 bytes per element and runs at HBM speed.
+template <typename T>
+struct BasisArith;
+template <>
+struct BasisArith<c64> {
+  using A = double;
+};
+template <>
+struct BasisArith<cff> {
+  using A = ff;
+};
+template <typename A, typename T>
+__device__ __forceinline__ cx<A> as(const T& v) {
+  return mk<A>((A)v.x, (A)v.y);
+}
+
 constexpr int KB = 8;        // columns per multi-dot tile
 constexpr int RED_TPB = 256;
 constexpr int MD_BLOCKS_MAX = 152 * 2;
@@ -25,32 +46,33 @@ __device__ __forceinline__ double warp_sum(double v) {
 // partial[c0+c][blk] (complex) = sum over the CTA's rows of conj(U[i,c0+c]) * v[i],
 // c < NC: the tile's columns are a template parameter, so loads, products and the
 // shuffle reductions are exactly the ones needed; each thread walks at least eight rows
-template <int NC>
-__global__ void __launch_bounds__(RED_TPB) k_multidot(const c64* __restrict__ U, size_t ldu,
-                                                      const c64* __restrict__ v, size_t N,
+template <int NC, typename UT, typename VT>
+__global__ void __launch_bounds__(RED_TPB) k_multidot(const UT* __restrict__ U, size_t ldu,
+                                                      const VT* __restrict__ v, size_t N,
                                                       int c0, c64* partial) {
+  using A = typename BasisArith<UT>::A;
   __shared__ double red[RED_TPB / 32][2 * NC];
   c0 += blockIdx.y * NC;
-  const c64* __restrict__ Uc = U + (size_t)c0 * ldu;
-  double ar[NC], ai[NC];
+  const UT* __restrict__ Uc = U + (size_t)c0 * ldu;
+  A ar[NC], ai[NC];
 #pragma unroll
-  for (int c = 0; c < NC; ++c) ar[c] = ai[c] = 0.0;
+  for (int c = 0; c < NC; ++c) ar[c] = ai[c] = 0;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += stride) {
-    c64 u[NC];
-    const c64 x = v[i];
+    cx<A> u[NC];
+    const cx<A> x = as<A>(v[i]);
 #pragma unroll
-    for (int c = 0; c < NC; ++c) u[c] = Uc[(size_t)c * ldu + i];
+    for (int c = 0; c < NC; ++c) u[c] = as<A>(Uc[(size_t)c * ldu + i]);
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      ar[c] += u[c].x * x.x + u[c].y * x.y;
-      ai[c] += u[c].x * x.y - u[c].y * x.x;
+      ar[c] = ar[c] + (u[c].x * x.x + u[c].y * x.y);
+      ai[c] = ai[c] + (u[c].x * x.y - u[c].y * x.x);
     }
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
-    const double sr = warp_sum(ar[c]), si = warp_sum(ai[c]);
+    const double sr = warp_sum((double)ar[c]), si = warp_sum((double)ai[c]);
     if (lane == 0) {
       red[wid][2 * c] = sr;
       red[wid][2 * c + 1] = si;
@@ -84,13 +106,16 @@ __global__ void k_reduce_cols(const c64* __restrict__ partial, int nblk, int k, 
 }
 
 // v[i] = base[i] (or e_unit) - sum_c U[i,c]*coef[c];  optional tail |v|^2 partials for i >= tail0
-__global__ void __launch_bounds__(RED_TPB) k_multiaxpy(const c64* __restrict__ U, size_t ldu,
+template <typename UT>
+__global__ void __launch_bounds__(RED_TPB) k_multiaxpy(const UT* __restrict__ U, size_t ldu,
                                                        const c64* __restrict__ base, int unit,
                                                        const c64* __restrict__ coef, int k,
                                                        size_t N, c64* out, size_t tail0,
                                                        double* tailpart) {
-  extern __shared__ c64 sc[];
-  for (int c = threadIdx.x; c < k; c += blockDim.x) sc[c] = coef[c];
+  using A = typename BasisArith<UT>::A;
+  extern __shared__ unsigned char sc_raw[];
+  cx<A>* sc = reinterpret_cast<cx<A>*>(sc_raw);
+  for (int c = threadIdx.x; c < k; c += blockDim.x) sc[c] = as<A>(coef[c]);
   __syncthreads();
   double acc = 0.0;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
@@ -98,16 +123,19 @@ __global__ void __launch_bounds__(RED_TPB) k_multiaxpy(const c64* __restrict__ U
     c64 x;
     if (base) x = base[i];
     else x = mk<double>(i == (size_t)unit ? 1.0 : 0.0, 0.0);
-    // columns in chunks of eight: the chunk's loads are issued before its products
+    // sum_c U[i,c] coef[c] in the basis arithmetic, columns in chunks of eight (the
+    // chunk's loads are issued before its products), then one subtraction in FP64
+    cx<A> s = mk<A>(0, 0);
     for (int c0 = 0; c0 < k; c0 += 8) {
-      c64 u[8];
+      cx<A> u[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        if (c0 + q < k) u[q] = U[(size_t)(c0 + q) * ldu + i];
+        if (c0 + q < k) u[q] = as<A>(U[(size_t)(c0 + q) * ldu + i]);
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        if (c0 + q < k) x = x - u[q] * sc[c0 + q];
+        if (c0 + q < k) s = s + u[q] * sc[c0 + q];
     }
+    x = x - as<double>(s);
     out[i] = x;
     if (i >= tail0) acc += x.x * x.x + x.y * x.y;
   }
@@ -167,13 +195,16 @@ __global__ void k_scale_by_rnorm(c64* v, size_t N, const double* __restrict__ ss
 }
 
 // new reflector column: u = (w with entries [0,j) zeroed, w[j] += add) * scale
+template <typename UT>
 __global__ void k_make_reflector(const c64* __restrict__ w, size_t N, int j, c64 add,
-                                 double scale, c64* u) {
+                                 double scale, UT* u) {
+  using A = typename BasisArith<UT>::A;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
        i += (size_t)gridDim.x * blockDim.x) {
     c64 x = (i < (size_t)j) ? mk<double>(0, 0) : w[i];
     if (i == (size_t)j) x = x + add;
-    u[i] = cscale(x, scale);
+    const c64 y = cscale(x, scale);
+    u[i] = mk<A>((A)y.x, (A)y.y);
   }
 }
 
@@ -185,26 +216,34 @@ __global__ void k_sub(const c64* __restrict__ a, const c64* __restrict__ b, size
 }
 
 // out = x + y_pad - sum_c U[i,c] coef[c] where y_pad holds ny leading entries
-__global__ void k_xupdate(const c64* __restrict__ x, const c64* __restrict__ U, size_t ldu,
+template <typename UT>
+__global__ void k_xupdate(const c64* __restrict__ x, const UT* __restrict__ U, size_t ldu,
                           const c64* __restrict__ coef, const c64* __restrict__ ypad, int k,
                           size_t N, c64* out) {
-  extern __shared__ c64 sc2[];
-  for (int c = threadIdx.x; c < 2 * k; c += blockDim.x) sc2[c] = c < k ? coef[c] : ypad[c - k];
+  using A = typename BasisArith<UT>::A;
+  extern __shared__ unsigned char sx_raw[];
+  c64* yp = reinterpret_cast<c64*>(sx_raw);                 // k entries
+  cx<A>* sc2 = reinterpret_cast<cx<A>*>(sx_raw + sizeof(c64) * k);  // k entries
+  for (int c = threadIdx.x; c < k; c += blockDim.x) {
+    yp[c] = ypad[c];
+    sc2[c] = as<A>(coef[c]);
+  }
   __syncthreads();
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
        i += (size_t)gridDim.x * blockDim.x) {
     c64 v = x[i];
-    if (i < (size_t)k) v = v + sc2[k + i];
+    if (i < (size_t)k) v = v + yp[i];
+    cx<A> s = mk<A>(0, 0);
     for (int c0 = 0; c0 < k; c0 += 8) {
-      c64 u[8];
+      cx<A> u[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        if (c0 + q < k) u[q] = U[(size_t)(c0 + q) * ldu + i];
+        if (c0 + q < k) u[q] = as<A>(U[(size_t)(c0 + q) * ldu + i]);
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        if (c0 + q < k) v = v - u[q] * sc2[c0 + q];
+        if (c0 + q < k) s = s + u[q] * sc2[c0 + q];
     }
-    out[i] = v;
+    out[i] = v - as<double>(s);
   }
 }
 
@@ -258,33 +297,58 @@ static inline unsigned md_blocks(size_t N) {
 }
 
 // returns the number of kernels launched
-int launch_multidot(const c64* U, size_t ldu, const c64* v, size_t N, int k, c64* partial,
-                    c64* out, cudaStream_t st) {
+template <typename UT, typename VT>
+static int multidot_t(const UT* U, size_t ldu, const VT* v, size_t N, int k, c64* partial,
+                      c64* out, cudaStream_t st) {
   if (k <= 0) return 0;
   const unsigned nb = md_blocks(N);
   const int full = k / KB, rem = k - full * KB;
-  if (full) k_multidot<KB><<<dim3(nb, full), RED_TPB, 0, st>>>(U, ldu, v, N, 0, partial);
+  if (full) k_multidot<KB, UT, VT><<<dim3(nb, full), RED_TPB, 0, st>>>(U, ldu, v, N, 0, partial);
   const int c0 = full * KB;
   switch (rem) {
-    case 1: k_multidot<1><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
-    case 2: k_multidot<2><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
-    case 3: k_multidot<3><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
-    case 4: k_multidot<4><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
-    case 5: k_multidot<5><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
-    case 6: k_multidot<6><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
-    case 7: k_multidot<7><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 1: k_multidot<1, UT, VT><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 2: k_multidot<2, UT, VT><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 3: k_multidot<3, UT, VT><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 4: k_multidot<4, UT, VT><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 5: k_multidot<5, UT, VT><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 6: k_multidot<6, UT, VT><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
+    case 7: k_multidot<7, UT, VT><<<nb, RED_TPB, 0, st>>>(U, ldu, v, N, c0, partial); break;
     default: break;
   }
   k_reduce_cols<<<(k + 7) / 8, 256, 0, st>>>(partial, nb, k, out);
   return (full ? 1 : 0) + (rem ? 1 : 0) + 1;
 }
+int launch_multidot(const c64* U, size_t ldu, const c64* v, size_t N, int k, c64* partial,
+                    c64* out, cudaStream_t st) {
+  return multidot_t(U, ldu, v, N, k, partial, out, st);
+}
+int launch_multidot(const cff* U, size_t ldu, const c64* v, size_t N, int k, c64* partial,
+                    c64* out, cudaStream_t st) {
+  return multidot_t(U, ldu, v, N, k, partial, out, st);
+}
+int launch_multidot(const cff* U, size_t ldu, const cff* v, size_t N, int k, c64* partial,
+                    c64* out, cudaStream_t st) {
+  return multidot_t(U, ldu, v, N, k, partial, out, st);
+}
 
+template <typename UT>
+static void multiaxpy_t(const UT* U, size_t ldu, const c64* base, int unit, const c64* coef,
+                        int k, size_t N, c64* out, size_t tail0, double* tailpart,
+                        cudaStream_t st) {
+  using A = typename BasisArith<UT>::A;
+  const unsigned nb = g_stream(N);
+  k_multiaxpy<UT><<<nb, RED_TPB, sizeof(cx<A>) * (k > 0 ? k : 1), st>>>(
+      U, ldu, base, unit, coef, k, N, out, tail0, tailpart);
+}
 void launch_multiaxpy(const c64* U, size_t ldu, const c64* base, int unit, const c64* coef,
                       int k, size_t N, c64* out, size_t tail0, double* tailpart,
                       cudaStream_t st) {
-  const unsigned nb = g_stream(N);
-  k_multiaxpy<<<nb, RED_TPB, sizeof(c64) * (k > 0 ? k : 1), st>>>(U, ldu, base, unit, coef, k, N,
-                                                                   out, tail0, tailpart);
+  multiaxpy_t(U, ldu, base, unit, coef, k, N, out, tail0, tailpart, st);
+}
+void launch_multiaxpy(const cff* U, size_t ldu, const c64* base, int unit, const c64* coef,
+                      int k, size_t N, c64* out, size_t tail0, double* tailpart,
+                      cudaStream_t st) {
+  multiaxpy_t(U, ldu, base, unit, coef, k, N, out, tail0, tailpart, st);
 }
 
 void launch_norm2(const c64* v, size_t N, size_t i0, double* part, double* out, cudaStream_t st) {
@@ -303,7 +367,11 @@ void launch_scale_rnorm(c64* v, size_t N, const double* ss, cudaStream_t st) {
 
 void launch_make_reflector(const c64* w, size_t N, int j, c64 add, double scale, c64* u,
                            cudaStream_t st) {
-  k_make_reflector<<<g_stream(N), 256, 0, st>>>(w, N, j, add, scale, u);
+  k_make_reflector<c64><<<g_stream(N), 256, 0, st>>>(w, N, j, add, scale, u);
+}
+void launch_make_reflector(const c64* w, size_t N, int j, c64 add, double scale, cff* u,
+                           cudaStream_t st) {
+  k_make_reflector<cff><<<g_stream(N), 256, 0, st>>>(w, N, j, add, scale, u);
 }
 
 void launch_sub(const c64* a, const c64* b, size_t N, c64* out, cudaStream_t st) {
@@ -337,8 +405,13 @@ void launch_tri(c64* T, int ld, int k, const c64* in, c64* out, int mode, cudaSt
 
 void launch_xupdate(const c64* x, const c64* U, size_t ldu, const c64* coef, const c64* ypad,
                     int k, size_t N, c64* out, cudaStream_t st) {
-  k_xupdate<<<g_stream(N), 256, sizeof(c64) * 2 * (k > 0 ? k : 1), st>>>(x, U, ldu, coef, ypad, k,
-                                                                        N, out);
+  k_xupdate<c64><<<g_stream(N), 256, 2 * sizeof(c64) * (k > 0 ? k : 1), st>>>(x, U, ldu, coef,
+                                                                             ypad, k, N, out);
+}
+void launch_xupdate(const c64* x, const cff* U, size_t ldu, const c64* coef, const c64* ypad,
+                    int k, size_t N, c64* out, cudaStream_t st) {
+  k_xupdate<cff><<<g_stream(N), 256, (sizeof(c64) + sizeof(cff)) * (k > 0 ? k : 1), st>>>(
+      x, U, ldu, coef, ypad, k, N, out);
 }
 
 // ------------------------------------------------------------------------------------
