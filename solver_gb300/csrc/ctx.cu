@@ -1313,14 +1313,13 @@ static void apply_Q(Gm& g, const std::vector<cd>& Utop, int ldt, int k, const st
 }
 
 // x0_zero: the caller guarantees x_dev == 0, so the initial residual is b itself (A*0 is
-// exactly 0 in every precision) and its operator application is skipped.
-// trust_recursive: convergence is decided on the recursive (least-squares) residual
-// without the confirming true-residual application -- for the inner solves of the mixed
-// solve, whose refinement loop computes the true residual of the corrected solution next.
+// exactly 0 in every precision) and its operator application is skipped. Convergence is
+// always confirmed on the true residual, as gmres_custom does: deciding on the recursive
+// estimate alone left port impedances of the mixed solve a little less accurate at
+// ill-conditioned frequencies.
 static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, int maxit,
                      int restarted, int restart, int prec, int* flag_out, double* relres_out,
-                     int* iter_out, std::vector<double>& resvec_out, bool x0_zero = false,
-                     bool trust_recursive = false) {
+                     int* iter_out, std::vector<double>& resvec_out, bool x0_zero = false) {
   const size_t N = ctx->N;
   int n = (int)N;
   int outer, inner;
@@ -1531,14 +1530,6 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
           else stag = 0;
           g.copy(ctx->gtmp, xm);
           apply_Q(g, Utop, ld, initer, addvc, ctx->gtmp, xm);
-        }
-        if (trust_recursive && normr <= tolb) {
-          g.copy(x, xm);
-          normr_act = normr;
-          flag = 0;
-          it0 = outiter;
-          it1 = initer;
-          break;
         }
         g.residual(b, xm, r);
         const double nr = g.norm(r);
