@@ -72,6 +72,9 @@ def parse():
                          "frequency), one JSON line")
     ap.add_argument("--profile-only", action="store_true",
                     help="set up, time the operator applications and exit (for ncu captures)")
+    ap.add_argument("--host-states", choices=["processes", "thread"], default="processes",
+                    help="where the per-frequency host states (SuperLU) are built: spawned "
+                         "worker processes (default) or one worker thread")
     ap.add_argument("--lanes", type=int, default=4,
                     help="concurrent port solves (contexts + host threads), at most the ports")
     ap.add_argument("--inner-tol", type=float, default=1e-7,
@@ -570,8 +573,14 @@ def main():
     order = [0] + [i % nf for i in range(args.warmup + args.steps)]
     static = (P["esc"], P["inc"], P["diag"], P["Zs"], P["le"], P["ports"], P["z0"])
     nworkers = max(2, min(12, (os.cpu_count() or 4) - 4))
-    pf = FrequencyPool(static, lambda k: 2 * np.pi * P["freqs"][k] * P["esc"]["freq"], order,
-                       workers=nworkers, lookahead=nworkers, keep=True)
+    if args.host_states == "processes":
+        pf = FrequencyPool(static, lambda k: 2 * np.pi * P["freqs"][k] * P["esc"]["freq"],
+                           order, workers=nworkers, lookahead=nworkers, keep=True)
+    else:
+        # one worker thread, no child processes (for runs under a profiler)
+        from solver_gb300.frequency import StatePrefetcher
+        nworkers = 1
+        pf = StatePrefetcher(lambda k: freq_state(P, k), order, keep=True)
     state = pf.get
 
     # -- operator profile and roofline (FP32 and FP64 convolutions) --------------------------
