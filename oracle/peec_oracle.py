@@ -20,7 +20,6 @@ from __future__ import annotations
 
 import ctypes
 import math
-import os
 
 import numpy as np
 import scipy.sparse as sp

@@ -5,7 +5,6 @@ Loading fails loudly: there is no CPU fallback anywhere in the product path.
 from __future__ import annotations
 
 import ctypes
-from pathlib import Path
 
 import numpy as np
 
