@@ -15,7 +15,6 @@ generating rows are recovered once on the host.
 """
 from __future__ import annotations
 
-
 import time
 
 import numpy as np
