@@ -1,0 +1,119 @@
+"""CPU: host-side logic of the sweep API with stand-in contexts (no GPU).
+
+* PortLanes.sweep gives every port its own lane (port c on lane c % lanes), walks each
+  lane through the whole frequency sequence in order with warm starts from that lane's
+  own previous solutions, releases a frequency state once every lane has set it (and
+  not while a later position still needs it), and stops on the stop flag.
+* dump_json_data writes the reference's results layout
+  (format_input_output_solver_functions.jl:1-31).
+* do_solving_fft refuses the solver types it does not implement."""
+import ctypes
+import json
+import threading
+
+import numpy as np
+import pytest
+
+from solver_gb300 import api
+
+
+class FakeOp:
+    """Stands in for a GpuOperator: records the calls; the 'solution' of port c at
+    frequency w is x0 + (w + c), so warm starts are visible in the results."""
+
+    def __init__(self, name, log):
+        self.name, self.log, self.w = name, log, None
+
+    def set_frequency(self, w, DZ, Yle, lu, key=None):
+        self.w = w
+        self.log.append((self.name, "set", w))
+
+    def port_rhs(self, n1, n2, Is):
+        return np.array([n1, n2, Is], dtype=np.complex128)
+
+    def solve_mixed(self, tn, x0, tol, **kw):
+        self.log.append((self.name, "solve", self.w, int(tn[0].real)))
+        return x0 + (self.w + tn[0].real), 0, tol / 2, 1, 5
+
+
+class FakeLanes(api.PortLanes):
+    def __init__(self, nlanes, log):
+        from concurrent.futures import ThreadPoolExecutor
+        self.ops = [FakeOp(i, log) for i in range(nlanes)]
+        self._pool = ThreadPoolExecutor(max_workers=nlanes)
+
+    def close(self):
+        self._pool.shutdown(wait=True)
+
+
+class State:
+    def __init__(self, w):
+        self.w, self.DZ, self.Yle, self.lu = w, None, None, None
+
+
+@pytest.mark.parametrize("nlanes,nports", [(2, 4), (3, 2), (1, 3)])
+def test_lanes_sweep_schedule_warm_starts_and_release(nlanes, nports):
+    log, released, recs = [], [], []
+    lock = threading.Lock()
+    lanes = FakeLanes(nlanes, log)
+    seq = [0, 1, 2, 1]  # a repeated key must not be released before its last use
+    pn = np.array([[10 * c, 10 * c + 1] for c in range(nports)])
+    V = np.zeros((3, nports), dtype=np.complex128)
+
+    def record(pos, k, c, Vc, flag, relres, outer, inner):
+        with lock:
+            recs.append((pos, k, c, Vc.copy()))
+
+    def rel(k):
+        with lock:
+            released.append(k)
+
+    try:
+        ok = lanes.sweep(seq, lambda k, pos: State(float(k)), rel, pn, 1.0, V,
+                         lambda k: 1e-8, {}, record)
+    finally:
+        lanes.close()
+    assert ok
+    assert len(recs) == len(seq) * nports
+    # each lane walks the sequence in order and solves only its own ports
+    for lane in range(min(nlanes, nports)):
+        mine = [e for e in log if e[0] == lane]
+        sets = [e[2] for e in mine if e[1] == "set"]
+        assert sets == [float(k) for k in seq]
+        solved = {e[3] // 10 for e in mine if e[1] == "solve"}
+        assert solved == {c for c in range(nports) if c % nlanes == lane}
+    # warm starts: port c's final solution accumulates (w + 10c) over the sequence
+    for c in range(nports):
+        assert V[0, c] == sum(float(k) + 10 * c for k in seq)
+    # every key released exactly once, after its last position
+    assert sorted(released) == sorted(set(seq))
+
+
+def test_lanes_sweep_stops_on_flag():
+    log = []
+    lanes = FakeLanes(2, log)
+    stop = ctypes.c_int(1)
+    try:
+        ok = lanes.sweep([0, 1], lambda k, pos: State(float(k)), lambda k: None,
+                         np.array([[0, 1], [2, 3]]), 1.0, np.zeros((3, 2), complex),
+                         lambda k: 1e-8, {}, lambda *a: None, stop_flag=stop)
+    finally:
+        lanes.close()
+    assert ok is False and log == []
+
+
+def test_dump_json_data_layout():
+    Z = np.arange(2 * 2 * 3).reshape(2, 2, 3) * (1 + 1j)
+    out = api.dump_json_data(Z, Z * 2, Z * 3, 2, "job7", partial=True, freqIndex=4)
+    assert (out["id"], out["partial"], out["freqIndex"], out["isStopped"]) == ("job7", True, 4, False)
+    mz = json.loads(out["matrices"]["matrix_Z"])
+    assert len(mz) == 4  # port pairs, i outer, j inner
+    for idx, (i, j) in enumerate([(0, 0), (0, 1), (1, 0), (1, 1)]):
+        assert mz[idx] == [[[float(v.real), float(v.imag)] for v in Z[i, j, :]]]
+    assert json.loads(out["matrices"]["matrix_S"])[1][0][2] == [float((Z[0, 1, 2] * 2).real),
+                                                                float((Z[0, 1, 2] * 2).imag)]
+
+
+def test_do_solving_fft_rejects_other_solver_types():
+    with pytest.raises(NotImplementedError):
+        api.do_solving_fft({"solverType": 2})
