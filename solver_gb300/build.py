@@ -1,6 +1,6 @@
 """Builds the native libraries of the package in-tree.
 
-* ``lib/libpeec_mesh.so``  -- host-only voxel mesher (g++).
+* ``lib/libpeec_mesh.so``  -- host-only voxel mesher (g++, OpenMP).
 * ``lib/libpeec_gb300.so`` -- the sm_103a CUDA kernels and the C ABI declared in
   ``include/peec_gb300.h`` (nvcc, one ``-gencode`` for compute_103a/sm_103a).
 
@@ -68,7 +68,8 @@ def build_mesh(force: bool = False) -> Path:
     if out.exists() and stamp.exists() and stamp.read_text() == dig and not force:
         return out
     cxx = shutil.which("g++") or "g++"
-    _run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-o", str(out)] + [str(s) for s in srcs])
+    _run([cxx, "-O2", "-std=c++17", "-fPIC", "-fopenmp", "-shared", "-o", str(out)] +
+         [str(s) for s in srcs])
     stamp.write_text(dig)
     return out
 

@@ -11,7 +11,11 @@
 //   src/lib/solverFFT/create_mapping_A{x,y,z}_v2.jl:1-29  edge numbering
 //   src/lib/solverFFT/create_A_mats_and_find_borders_with_map_Zs.jl:1-229
 //   src/lib/solverFFT/create_mapping_Gamma_no_rep.jl:1-421 surfaces + Gamma
-// Loop orders below are the reference's loop orders: they fix the numbering.
+// Loop orders below are the reference's loop orders: they fix the numbering. Loops run
+// in parallel (OpenMP) where that cannot change the result: per-cell predicates are
+// evaluated in parallel, and every numbered sequence is assembled from per-slab pieces
+// concatenated in the reference's slab order, so the output is the same for any number
+// of threads.
 // All indices here are 0-based; the Python wrapper converts where needed.
 
 #include <algorithm>
@@ -101,7 +105,8 @@ void build_externals(const Mesh& M, Ext& E) {
           if (Nz > 1 && !M.at(k, x, y, z - 1)) E(k, 4, M.cell(x, y, z)) = 1;
         }
       }
-  // interior faces
+  // interior faces (each cell's flags are written by its own iteration)
+#pragma omp parallel for schedule(static)
   for (int z = 0; z < Nz; ++z)
     for (int y = 0; y < Ny; ++y)
       for (int x = 0; x < Nx; ++x)
@@ -171,23 +176,32 @@ void build_nodes(Mesh& M, const Ext& E, const std::vector<uint8_t>& dominant) {
   const int Nx = M.Nx, Ny = M.Ny, Nz = M.Nz;
   M.nodes.assign(M.num_vox, 0.0);
   std::vector<double> lista;
-  // dominant (conductor) grids first, in grid order (create_nodes_ref.jl:9-226)
+  // dominant (conductor) grids first, in grid order (create_nodes_ref.jl:9-226). Within a
+  // grid every voxel is set once and lista is sorted afterwards, so the cells can be
+  // visited in any order: plane by plane, in parallel.
   for (int k = 0; k < M.G; ++k) {
     if (!dominant[k]) continue;
-    for (int x = 0; x < Nx; ++x)
-      for (int y = 0; y < Ny; ++y)
-        for (int z = 0; z < Nz; ++z) {
-          if (!M.at(k, x, y, z)) continue;
-          int64_t c1 = 2 * (x + 1), c2 = 2 * (y + 1), c3 = 2 * (z + 1);
-          int dx, dy, dz;
-          size_t v = M.vox_map[M.cell(x, y, z)] - 1;
-          if (face_offset(M, E, k, x, y, z, dx, dy, dz)) {
-            M.nodes[v] = node_id(c1 + dx, c2 + dy, c3 + dz, Nx, Ny);
-            lista.push_back(M.nodes[v]);
-          } else {
-            M.nodes[v] = node_id(c1, c2, c3, Nx, Ny);
+#pragma omp parallel
+    {
+      std::vector<double> loc;
+#pragma omp for schedule(static)
+      for (int z = 0; z < Nz; ++z)
+        for (int y = 0; y < Ny; ++y)
+          for (int x = 0; x < Nx; ++x) {
+            if (!M.at(k, x, y, z)) continue;
+            int64_t c1 = 2 * (x + 1), c2 = 2 * (y + 1), c3 = 2 * (z + 1);
+            int dx, dy, dz;
+            size_t v = M.vox_map[M.cell(x, y, z)] - 1;
+            if (face_offset(M, E, k, x, y, z, dx, dy, dz)) {
+              M.nodes[v] = node_id(c1 + dx, c2 + dy, c3 + dz, Nx, Ny);
+              loc.push_back(M.nodes[v]);
+            } else {
+              M.nodes[v] = node_id(c1, c2, c3, Nx, Ny);
+            }
           }
-        }
+#pragma omp critical
+      lista.insert(lista.end(), loc.begin(), loc.end());
+    }
   }
   std::sort(lista.begin(), lista.end());
   lista.erase(std::unique(lista.begin(), lista.end()), lista.end());
@@ -200,9 +214,10 @@ void build_nodes(Mesh& M, const Ext& E, const std::vector<uint8_t>& dominant) {
       {0, 1, 0},    {0, 1, 1},   {1, 1, -1},  {1, 1, 0},   {1, 1, 1}};
   for (int k = 0; k < M.G; ++k) {
     if (dominant[k]) continue;
-    for (int x = 0; x < Nx; ++x)
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < Nz; ++z)
       for (int y = 0; y < Ny; ++y)
-        for (int z = 0; z < Nz; ++z) {
+        for (int x = 0; x < Nx; ++x) {
           if (!M.at(k, x, y, z)) continue;
           int64_t c1 = 2 * (x + 1), c2 = 2 * (y + 1), c3 = 2 * (z + 1);
           int dx, dy, dz;
@@ -227,6 +242,7 @@ void build_nodes(Mesh& M, const Ext& E, const std::vector<uint8_t>& dominant) {
   std::sort(M.nodes_red.begin(), M.nodes_red.end());
   M.nodes_red.erase(std::unique(M.nodes_red.begin(), M.nodes_red.end()), M.nodes_red.end());
   M.vox_node.resize(M.num_vox);
+#pragma omp parallel for schedule(static)
   for (int64_t v = 0; v < M.num_vox; ++v)
     M.vox_node[v] = std::lower_bound(M.nodes_red.begin(), M.nodes_red.end(), M.nodes[v]) -
                     M.nodes_red.begin();
@@ -248,30 +264,55 @@ inline int edge_grid(const Mesh& M, int x1, int y1, int z1, int x2, int y2, int 
 void build_edges(Mesh& M, const std::vector<double>& sigma) {
   const int Nx = M.Nx, Ny = M.Ny, Nz = M.Nz;
   // --- numbering (create_mapping_A{x,y,z}_v2.jl) ---
-  // x: loops y, z, x ; y: z, x, y ; z: x, y, z (last index fastest)
-  std::vector<int64_t> numx((size_t)std::max(Nx - 1, 0) * Ny * Nz, -1);
-  std::vector<int64_t> numy((size_t)Nx * std::max(Ny - 1, 0) * Nz, -1);
-  std::vector<int64_t> numz((size_t)Nx * Ny * std::max(Nz - 1, 0), -1);
-  int64_t cnt = 0;
-  for (int y = 0; y < Ny; ++y)
-    for (int z = 0; z < Nz; ++z)
-      for (int x = 0; x + 1 < Nx; ++x)
-        if (edge_grid(M, x, y, z, x + 1, y, z) >= 0)
-          numx[((size_t)z * Ny + y) * (Nx - 1) + x] = cnt++;
-  M.m[0] = cnt;
-  cnt = 0;
+  // x: loops y, z, x ; y: z, x, y ; z: x, y, z (last index fastest). The edge grid of
+  // every lattice cell is evaluated in parallel, then edges are numbered slab by slab of
+  // the reference's outer loop: per-slab counts, their prefix sums, and each slab's
+  // numbers in its inner loop order.
+  const size_t Lx = (size_t)std::max(Nx - 1, 0) * Ny * Nz;
+  const size_t Ly = (size_t)Nx * std::max(Ny - 1, 0) * Nz;
+  const size_t Lz = (size_t)Nx * Ny * std::max(Nz - 1, 0);
+  std::vector<int32_t> kx(Lx, -1), ky(Ly, -1), kz(Lz, -1);
+#pragma omp parallel for schedule(static)
   for (int z = 0; z < Nz; ++z)
-    for (int x = 0; x < Nx; ++x)
-      for (int y = 0; y + 1 < Ny; ++y)
-        if (edge_grid(M, x, y, z, x, y + 1, z) >= 0)
-          numy[((size_t)z * (Ny - 1) + y) * Nx + x] = cnt++;
-  M.m[1] = cnt;
-  cnt = 0;
-  for (int x = 0; x < Nx; ++x)
     for (int y = 0; y < Ny; ++y)
-      for (int z = 0; z + 1 < Nz; ++z)
-        if (edge_grid(M, x, y, z, x, y, z + 1) >= 0) numz[((size_t)z * Ny + y) * Nx + x] = cnt++;
-  M.m[2] = cnt;
+      for (int x = 0; x < Nx; ++x) {
+        if (x + 1 < Nx) kx[((size_t)z * Ny + y) * (Nx - 1) + x] = edge_grid(M, x, y, z, x + 1, y, z);
+        if (y + 1 < Ny) ky[((size_t)z * (Ny - 1) + y) * Nx + x] = edge_grid(M, x, y, z, x, y + 1, z);
+        if (z + 1 < Nz) kz[((size_t)z * Ny + y) * Nx + x] = edge_grid(M, x, y, z, x, y, z + 1);
+      }
+  std::vector<int64_t> numx(Lx, -1), numy(Ly, -1), numz(Lz, -1);
+  // number the cells of nslab slabs; visit(s, f) calls f(lattice cell) for slab s in order
+  auto number = [](int nslab, const std::vector<int32_t>& kk, std::vector<int64_t>& num,
+                   auto visit) -> int64_t {
+    std::vector<int64_t> start((size_t)nslab + 1, 0);
+#pragma omp parallel for schedule(static)
+    for (int sl = 0; sl < nslab; ++sl) {
+      int64_t c = 0;
+      visit(sl, [&](size_t lc) { c += kk[lc] >= 0; });
+      start[sl + 1] = c;
+    }
+    for (int sl = 0; sl < nslab; ++sl) start[sl + 1] += start[sl];
+#pragma omp parallel for schedule(static)
+    for (int sl = 0; sl < nslab; ++sl) {
+      int64_t c = start[sl];
+      visit(sl, [&](size_t lc) {
+        if (kk[lc] >= 0) num[lc] = c++;
+      });
+    }
+    return start[nslab];
+  };
+  M.m[0] = number(Ny, kx, numx, [&](int y, auto f) {
+    for (int z = 0; z < Nz; ++z)
+      for (int x = 0; x + 1 < Nx; ++x) f(((size_t)z * Ny + y) * (Nx - 1) + x);
+  });
+  M.m[1] = number(Nz, ky, numy, [&](int z, auto f) {
+    for (int x = 0; x < Nx; ++x)
+      for (int y = 0; y + 1 < Ny; ++y) f(((size_t)z * (Ny - 1) + y) * Nx + x);
+  });
+  M.m[2] = number(Nx, kz, numz, [&](int x, auto f) {
+    for (int y = 0; y < Ny; ++y)
+      for (int z = 0; z + 1 < Nz; ++z) f(((size_t)z * Ny + y) * Nx + x);
+  });
   for (int d = 0; d < 3; ++d) {
     M.e_n1[d].assign(M.m[d], -1);
     M.e_n2[d].assign(M.m[d], -1);
@@ -284,13 +325,14 @@ void build_edges(Mesh& M, const std::vector<double>& sigma) {
   auto G = [&](int k, int x, int y, int z) { return M.at(k, x, y, z); };
   // --- incidence, borders and surface-impedance counters
   //     (create_A_mats_and_find_borders_with_map_Zs.jl) ---
-  // x edges
+  // x edges (each edge's entries are written by its own iteration)
+#pragma omp parallel for schedule(static)
   for (int z = 0; z < Nz; ++z)
     for (int y = 0; y < Ny; ++y)
       for (int x = 0; x + 1 < Nx; ++x) {
-        int k = edge_grid(M, x, y, z, x + 1, y, z);
-        if (k < 0) continue;
         size_t lc = ((size_t)z * Ny + y) * (Nx - 1) + x;
+        int k = kx[lc];
+        if (k < 0) continue;
         int64_t e = numx[lc];
         M.e_n1[0][e] = node_of(M, x, y, z);
         M.e_n2[0][e] = node_of(M, x + 1, y, z);
@@ -325,12 +367,13 @@ void build_edges(Mesh& M, const std::vector<double>& sigma) {
         else if (x + 2 <= Nx - 1 && !G(k, x + 2, y, z)) M.e_border2[0][e] = k + 1;
       }
   // y edges
+#pragma omp parallel for schedule(static)
   for (int z = 0; z < Nz; ++z)
     for (int x = 0; x < Nx; ++x)
       for (int y = 0; y + 1 < Ny; ++y) {
-        int k = edge_grid(M, x, y, z, x, y + 1, z);
-        if (k < 0) continue;
         size_t lc = ((size_t)z * (Ny - 1) + y) * Nx + x;
+        int k = ky[lc];
+        if (k < 0) continue;
         int64_t e = numy[lc];
         M.e_n1[1][e] = node_of(M, x, y, z);
         M.e_n2[1][e] = node_of(M, x, y + 1, z);
@@ -365,12 +408,13 @@ void build_edges(Mesh& M, const std::vector<double>& sigma) {
         else if (y + 2 <= Ny - 1 && !G(k, x, y + 2, z)) M.e_border2[1][e] = k + 1;
       }
   // z edges
-  for (int x = 0; x < Nx; ++x)
+#pragma omp parallel for schedule(static)
+  for (int z = 0; z < Nz - 1; ++z)
     for (int y = 0; y < Ny; ++y)
-      for (int z = 0; z + 1 < Nz; ++z) {
-        int k = edge_grid(M, x, y, z, x, y, z + 1);
-        if (k < 0) continue;
+      for (int x = 0; x < Nx; ++x) {
         size_t lc = ((size_t)z * Ny + y) * Nx + x;
+        int k = kz[lc];
+        if (k < 0) continue;
         int64_t e = numz[lc];
         M.e_n1[2][e] = node_of(M, x, y, z);
         M.e_n2[2][e] = node_of(M, x, y, z + 1);
@@ -408,6 +452,27 @@ void build_edges(Mesh& M, const std::vector<double>& sigma) {
       }
 }
 
+struct SRec {
+  int32_t fam;
+  int64_t cell, node;
+};
+
+// Runs body(a, out) for the outer-loop slabs a = 0..n-1 in parallel, then appends their
+// records in slab order: the same sequence as running the loop serially.
+template <typename F>
+void ordered_push(Mesh& M, int n, F body) {
+  std::vector<std::vector<SRec>> per((size_t)std::max(n, 0));
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int a = 0; a < n; ++a) body(a, per[a]);
+  for (const auto& v : per)
+    for (const auto& r : v) {
+      M.s_fam.push_back(r.fam);
+      M.s_cell.push_back(r.cell);
+      M.s_node.push_back(r.node);
+      M.ns_fam[r.fam] += 1;
+    }
+}
+
 void build_surfaces(Mesh& M, const Ext& E) {
   const int Nx = M.Nx, Ny = M.Ny, Nz = M.Nz;
   auto G = [&](int k, int x, int y, int z) { return M.at(k, x, y, z); };
@@ -417,144 +482,154 @@ void build_surfaces(Mesh& M, const Ext& E) {
       if (k2 != k && G(k2, x, y, z)) return true;
     return false;
   };
-  auto push = [&](int fam, size_t cell, int x, int y, int z) {
-    M.s_fam.push_back(fam);
-    M.s_cell.push_back((int64_t)cell);
-    M.s_node.push_back(node_of(M, x, y, z));
-    M.ns_fam[fam] += 1;
+  auto rec = [&](std::vector<SRec>& out, int fam, size_t cell, int x, int y, int z) {
+    out.push_back(SRec{fam, (int64_t)cell, node_of(M, x, y, z)});
   };
   // family 0 (reference "12", y-normal faces) on the Nx x (Ny+1) x Nz lattice
   auto c12 = [&](int x, int yf, int z) { return ((size_t)z * (Ny + 1) + yf) * Nx + x; };
-  for (int x = 0; x < Nx; ++x)
+  ordered_push(M, Nx, [&](int x, std::vector<SRec>& out) {
     for (int z = 0; z < Nz; ++z) {  // y = 0
       int y = 0;
       for (int k = 0; k < M.G; ++k) {
         bool om = any_other(k, y + 1 <= Ny - 1, x, y + 1, z);
         if (G(k, x, y, z) && (!E.get(k, 1, M.cell(x, y, z)) || om)) {
-          push(0, c12(x, y, z), x, y, z);
+          rec(out, 0, c12(x, y, z), x, y, z);
           break;
         }
       }
     }
-  for (int x = 0; x < Nx; ++x)
+  });
+  ordered_push(M, Nx, [&](int x, std::vector<SRec>& out) {
     for (int y = 1; y < Ny; ++y)
       for (int z = 0; z < Nz; ++z)
         for (int k = 0; k < M.G; ++k) {
           bool om = any_other(k, y + 1 <= Ny - 1, x, y + 1, z);
           if (G(k, x, y, z) && !G(k, x, y - 1, z) && (!E.get(k, 1, M.cell(x, y, z)) || om)) {
-            push(0, c12(x, y, z), x, y, z);
+            rec(out, 0, c12(x, y, z), x, y, z);
             break;
           }
         }
-  for (int x = 0; x < Nx; ++x)
+  });
+  ordered_push(M, Nx, [&](int x, std::vector<SRec>& out) {
     for (int z = 0; z < Nz; ++z) {  // y = Ny-1, face Ny
       int y = Ny - 1;
       for (int k = 0; k < M.G; ++k) {
         bool om = any_other(k, y - 1 >= 0, x, y - 1, z);
         if (G(k, x, y, z) && (!E.get(k, 0, M.cell(x, y, z)) || om)) {
-          push(0, c12(x, y + 1, z), x, y, z);
+          rec(out, 0, c12(x, y + 1, z), x, y, z);
           break;
         }
       }
     }
-  for (int x = 0; x < Nx; ++x)
+  });
+  ordered_push(M, Nx, [&](int x, std::vector<SRec>& out) {
     for (int y = 0; y + 1 < Ny; ++y)
       for (int z = 0; z < Nz; ++z)
         for (int k = 0; k < M.G; ++k) {
           bool om = any_other(k, y - 1 >= 0, x, y - 1, z);
           if (G(k, x, y, z) && !G(k, x, y + 1, z) && (!E.get(k, 0, M.cell(x, y, z)) || om)) {
-            if (!any_other(k, true, x, y + 1, z)) push(0, c12(x, y + 1, z), x, y, z);
+            if (!any_other(k, true, x, y + 1, z)) rec(out, 0, c12(x, y + 1, z), x, y, z);
             break;
           }
         }
+  });
   // family 1 (reference "34", x-normal faces) on the (Nx+1) x Ny x Nz lattice
   auto c34 = [&](int xf, int y, int z) { return ((size_t)z * Ny + y) * (Nx + 1) + xf; };
-  for (int y = 0; y < Ny; ++y)
+  ordered_push(M, Ny, [&](int y, std::vector<SRec>& out) {
     for (int z = 0; z < Nz; ++z) {  // x = 0
       int x = 0;
       for (int k = 0; k < M.G; ++k) {
         bool om = any_other(k, x + 1 <= Nx - 1, x + 1, y, z);
         if (G(k, x, y, z) && (!E.get(k, 3, M.cell(x, y, z)) || om)) {
-          push(1, c34(x, y, z), x, y, z);
+          rec(out, 1, c34(x, y, z), x, y, z);
           break;
         }
       }
     }
-  for (int x = 1; x < Nx; ++x)
+  });
+  ordered_push(M, std::max(Nx - 1, 0), [&](int a, std::vector<SRec>& out) {
+    const int x = a + 1;
     for (int y = 0; y < Ny; ++y)
       for (int z = 0; z < Nz; ++z)
         for (int k = 0; k < M.G; ++k) {
           bool om = any_other(k, x + 1 <= Nx - 1, x + 1, y, z);
           if (G(k, x, y, z) && !G(k, x - 1, y, z) && (!E.get(k, 3, M.cell(x, y, z)) || om)) {
-            push(1, c34(x, y, z), x, y, z);
+            rec(out, 1, c34(x, y, z), x, y, z);
             break;
           }
         }
-  for (int y = 0; y < Ny; ++y)
+  });
+  ordered_push(M, Ny, [&](int y, std::vector<SRec>& out) {
     for (int z = 0; z < Nz; ++z) {  // x = Nx-1, face Nx
       int x = Nx - 1;
       for (int k = 0; k < M.G; ++k) {
         bool om = any_other(k, x - 1 >= 0, x - 1, y, z);
         if (G(k, x, y, z) && (!E.get(k, 2, M.cell(x, y, z)) || om)) {
-          push(1, c34(x + 1, y, z), x, y, z);
+          rec(out, 1, c34(x + 1, y, z), x, y, z);
           break;
         }
       }
     }
-  for (int x = 0; x + 1 < Nx; ++x)
+  });
+  ordered_push(M, std::max(Nx - 1, 0), [&](int x, std::vector<SRec>& out) {
     for (int y = 0; y < Ny; ++y)
       for (int z = 0; z < Nz; ++z)
         for (int k = 0; k < M.G; ++k) {
           bool om = any_other(k, x - 1 >= 0, x - 1, y, z);
           if (G(k, x, y, z) && !G(k, x + 1, y, z) && (!E.get(k, 2, M.cell(x, y, z)) || om)) {
-            if (!any_other(k, true, x + 1, y, z)) push(1, c34(x + 1, y, z), x, y, z);
+            if (!any_other(k, true, x + 1, y, z)) rec(out, 1, c34(x + 1, y, z), x, y, z);
             break;
           }
         }
+  });
   // family 2 (reference "56", z-normal faces) on the Nx x Ny x (Nz+1) lattice
   auto c56 = [&](int x, int y, int zf) { return ((size_t)zf * Ny + y) * Nx + x; };
-  for (int x = 0; x < Nx; ++x)
+  ordered_push(M, Nx, [&](int x, std::vector<SRec>& out) {
     for (int y = 0; y < Ny; ++y) {  // z = 0
       int z = 0;
       for (int k = 0; k < M.G; ++k) {
         bool om = any_other(k, z + 1 <= Nz - 1, x, y, z + 1);
         if (G(k, x, y, z) && (!E.get(k, 5, M.cell(x, y, z)) || om)) {
-          push(2, c56(x, y, z), x, y, z);
+          rec(out, 2, c56(x, y, z), x, y, z);
           break;
         }
       }
     }
-  for (int x = 0; x < Nx; ++x)
+  });
+  ordered_push(M, Nx, [&](int x, std::vector<SRec>& out) {
     for (int y = 0; y < Ny; ++y)
       for (int z = 1; z < Nz; ++z)
         for (int k = 0; k < M.G; ++k) {
           bool om = any_other(k, z + 1 <= Nz - 1, x, y, z + 1);
           if (G(k, x, y, z) && !G(k, x, y, z - 1) && (!E.get(k, 5, M.cell(x, y, z)) || om)) {
-            push(2, c56(x, y, z), x, y, z);
+            rec(out, 2, c56(x, y, z), x, y, z);
             break;
           }
         }
-  for (int x = 0; x < Nx; ++x)
+  });
+  ordered_push(M, Nx, [&](int x, std::vector<SRec>& out) {
     for (int y = 0; y < Ny; ++y) {  // z = Nz-1, face Nz
       int z = Nz - 1;
       for (int k = 0; k < M.G; ++k) {
         bool om = any_other(k, z - 1 >= 0, x, y, z - 1);
         if (G(k, x, y, z) && (!E.get(k, 4, M.cell(x, y, z)) || om)) {
-          push(2, c56(x, y, z + 1), x, y, z);
+          rec(out, 2, c56(x, y, z + 1), x, y, z);
           break;
         }
       }
     }
-  for (int x = 0; x < Nx; ++x)
+  });
+  ordered_push(M, Nx, [&](int x, std::vector<SRec>& out) {
     for (int y = 0; y < Ny; ++y)
       for (int z = 0; z + 1 < Nz; ++z)
         for (int k = 0; k < M.G; ++k) {
           bool om = any_other(k, z - 1 >= 0, x, y, z - 1);
           if (G(k, x, y, z) && !G(k, x, y, z + 1) && (!E.get(k, 4, M.cell(x, y, z)) || om)) {
-            if (!any_other(k, true, x, y, z + 1)) push(2, c56(x, y, z + 1), x, y, z);
+            if (!any_other(k, true, x, y, z + 1)) rec(out, 2, c56(x, y, z + 1), x, y, z);
             break;
           }
         }
+  });
 }
 
 }  // namespace
