@@ -176,3 +176,47 @@ def test_far_field_branches_reach_the_point_limit(name):
     assert far_total > 0
     if name == "needle_60x4x4":
         assert collinear_seen > 0
+
+
+def test_s_to_z_and_y_follow_the_reference():
+    """s2z_fft / s2y_fft (FFT_solver_QS_S_type.jl:265-285): Z = z0 (I - S)^-1 (I + S) and
+    Y = z0 (I + S)^-1 (I - S). The reference scales Y by z0 rather than 1/z0, so Z Y =
+    z0^2 I; the restatement (oracle and solver_gb300.api) keeps that."""
+    from solver_gb300 import api
+    rng = np.random.default_rng(4)
+    S = (rng.standard_normal((3, 3, 2)) + 1j * rng.standard_normal((3, 3, 2))) * 0.2
+    S = 0.5 * (S + S.transpose(1, 0, 2))
+    z0 = 50.0
+    for f in (O.s2z, api.s2z_fft):
+        Z = f(S, z0)
+        assert np.allclose(Z[:, :, 1] @ (np.eye(3) - S[:, :, 1]) / z0, np.eye(3) + S[:, :, 1])
+    Y = api.s2y_fft(S, z0)
+    np.testing.assert_allclose(O.s2y(S, z0), Y, rtol=1e-14)
+    for k in range(2):
+        np.testing.assert_allclose(api.s2z_fft(S, z0)[:, :, k] @ Y[:, :, k], z0 ** 2 * np.eye(3),
+                                   atol=1e-9 * z0 ** 2)
+
+
+def test_oracle_gmres_matches_a_dense_solve():
+    """The oracle's Householder GMRES (gmres_custom.jl restated) on the crossbar operator
+    against a dense LU solve of the explicitly assembled operator: at relative residual
+    1e-11 the solutions agree to ~10x that (the operator's condition number is ~3e6, and
+    the recursion's residual tracks the true one)."""
+    req = configs.crossbar_20x20x4()
+    out, freqs, _settings, z0, grid = mesher.parse_request(req)
+    esc, inc, cc, diag, exp, ports, le, _li, Zs = out
+    FFTCP, FFTCLp = O.spectra_from_rows(O.fill_rows(cc, esc, *grid), *grid)
+    w = 2 * np.pi * freqs[0] * esc["freq"]
+    fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
+    mv = lambda v: O.ComputeMatrixVectorFTT(v, w, inc, FFTCP, FFTCLp, fs["DZ"], fs["Yle"], exp,
+                                            fs["invZ"], fs["invP"], fs["F"])
+    m, n = inc["A"].shape
+    ns = inc["Gamma"].shape[1]
+    n1, n2 = ports["port_nodes"][0]
+    i_s = np.zeros(n)
+    i_s[n1], i_s[n2] = esc["Is"], -esc["Is"]
+    tn = O.precond_3_3_Kt_fft(fs["F"], fs["invZ"], fs["invP"], inc["A"], inc["Gamma"], m, ns, i_s)
+    x, flag, relres, it, rv = O.gmres_custom(tn, False, 1e-11, 200, None, mv)
+    assert flag == 0 and relres <= 1e-11
+    x_dense = np.linalg.solve(O.dense_operator(mv, m + ns + n), tn)
+    assert np.max(np.abs(x - x_dense)) <= 1e-9 * np.max(np.abs(x_dense))
