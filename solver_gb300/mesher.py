@@ -57,11 +57,15 @@ def _lib():
 
 
 def _raw_mesh(grids: np.ndarray, dominant, sigma) -> dict:
-    """Runs the native mesher; grids is (G, Nx, Ny, Nz) bool."""
+    """Runs the native mesher; grids is (G, Nx, Ny, Nz) bool, dominant a length-G mask of
+    the conductor grids and sigma the G conductivities (the library reads G of each)."""
     G, Nx, Ny, Nz = grids.shape
     g = np.ascontiguousarray(np.transpose(grids.astype(np.uint8), (0, 3, 2, 1)))  # x fastest
     dom = np.ascontiguousarray(np.asarray(dominant, dtype=np.uint8))
     sig = np.ascontiguousarray(np.asarray(sigma, dtype=np.float64))
+    if dom.shape != (G,) or sig.shape != (G,):
+        raise ValueError(f"dominant and sigma need one entry per grid ({G}); "
+                         f"got {dom.shape} and {sig.shape}")
     L = _lib()
     h = L.peec_mesh_build(g.ctypes.data, G, Nx, Ny, Nz, dom.ctypes.data, sig.ctypes.data)
     if not h:

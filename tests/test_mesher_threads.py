@@ -18,7 +18,7 @@ from solver_gb300 import configs, mesher
 rng = np.random.default_rng(11)
 shape = (37, 29, 13)
 grids = np.stack([rng.random(shape) < 0.25, rng.random(shape) < 0.2, rng.random(shape) < 0.15])
-out = mesher._raw_mesh(grids, [0, 2], [5.8e7, 0.0, 1e7])
+out = mesher._raw_mesh(grids, [1, 0, 1], [5.8e7, 0.0, 1e7])
 h = hashlib.sha256()
 for k in sorted(out):
     h.update(k.encode())
@@ -38,3 +38,13 @@ def test_mesher_output_independent_of_thread_count():
     one, four = _run(1), _run(4)
     assert one["m"] > 0
     assert one == four
+
+
+def test_mesher_rejects_a_mask_of_the_wrong_length():
+    import numpy as np
+    import pytest
+    sys.path.insert(0, str(ROOT))
+    from solver_gb300 import mesher
+    grids = np.ones((3, 4, 4, 2), dtype=bool)
+    with pytest.raises(ValueError):
+        mesher._raw_mesh(grids, [0, 2], [5.8e7, 0.0, 1e7])
