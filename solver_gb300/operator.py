@@ -77,6 +77,9 @@ class GpuOperator:
             grid = expansions["grid"]
         self.grid = tuple(int(v) for v in grid)
         ecell = _edge_cells(expansions, mx, my, mz)
+        if mx + my + mz != self.m or ecell.size != self.m:
+            raise ValueError(f"edge counts mx+my+mz={mx + my + mz} and {ecell.size} edge cells "
+                             f"must both equal the {self.m} rows of A")
         # A rows hold -1 at n1 and +1 at n2
         n1 = np.empty(self.m, dtype=np.int64)
         n2 = np.empty(self.m, dtype=np.int64)
@@ -93,11 +96,15 @@ class GpuOperator:
             raise ValueError("Gamma must have one entry per surface column")
         snode = Gamma.indices.astype(np.int64)
         fam, scell = _surf_cells(expansions, self.ns)
+        if fam.size != self.ns or scell.size != self.ns:
+            raise ValueError("surf_fam and surf_cell need one entry per surface")
         Nx, Ny, Nz = self.grid
         _lib.check(self.h, self.L.peec_set_topology(
             self.h, Nx, Ny, Nz, mx, my, mz, _lib.ptr(ecell), _lib.ptr(n1), _lib.ptr(n2), self.ns,
             _lib.ptr(fam), _lib.ptr(scell), _lib.ptr(snode), self.n))
         dp = np.ascontiguousarray(np.asarray(diagP, dtype=np.float64).ravel())
+        if dp.size != self.ns:
+            raise ValueError(f"diagP has {dp.size} entries, expected {self.ns}")
         _lib.check(self.h, self.L.peec_set_pdiag(self.h, _lib.ptr(dp)))
         self._freq_key = None
         self._stop = None
@@ -167,11 +174,20 @@ class GpuOperator:
         if key is not None and key == self._freq_key:
             return
         DZ = np.ascontiguousarray(np.asarray(DZ, dtype=np.complex128).ravel())
+        if DZ.size != self.m:
+            raise ValueError(f"DZ has {DZ.size} entries, expected {self.m}")
+        if tuple(Yle.shape) != (self.n, self.n):
+            raise ValueError(f"Yle must be {self.n} x {self.n}")
         Y = sp.coo_matrix(Yle)
         yr = Y.row.astype(np.int64)
         yc = Y.col.astype(np.int64)
         yv = np.ascontiguousarray(Y.data.astype(np.complex128))
         (Lp, Lc, Lv), (Up, Uc, Uv), pr, pc = export_lu(lu)
+        for ptr, col, val in ((Lp, Lc, Lv), (Up, Uc, Uv)):
+            if ptr.size != self.n + 1 or ptr[-1] != col.size or val.size != 2 * col.size:
+                raise ValueError(f"LU factors must be {self.n} x {self.n} CSR")
+        if pr.size != self.n or pc.size != self.n:
+            raise ValueError(f"LU permutations need {self.n} entries")
         _lib.check(self.h, self.L.peec_set_frequency(
             self.h, float(w), _lib.ptr(DZ.view(np.float64)), int(yr.size), _lib.ptr(yr),
             _lib.ptr(yc), _lib.ptr(yv.view(np.float64)), _lib.ptr(Lp), _lib.ptr(Lc), _lib.ptr(Lv),
@@ -232,10 +248,16 @@ class GpuOperator:
         _lib.check(self.h, self.L.peec_set_stop_flag(
             self.h, ctypes.cast(ctypes.byref(flag), ctypes.c_void_p) if flag is not None else None))
 
-    def gmres(self, b, x0, tol, maxit, restarted=False, restart=0, precision=0):
+    def _vectors(self, b, x0):
         b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())
         x = np.zeros(self.N, dtype=np.complex128) if x0 is None or np.size(x0) == 0 else \
             np.array(np.asarray(x0, dtype=np.complex128).ravel())
+        if b.size != self.N or x.size != self.N:
+            raise ValueError(f"b and x0 have {b.size} and {x.size} entries, expected {self.N}")
+        return b, x
+
+    def gmres(self, b, x0, tol, maxit, restarted=False, restart=0, precision=0):
+        b, x = self._vectors(b, x0)
         flag = ctypes.c_int()
         relres = ctypes.c_double()
         it = (ctypes.c_int * 2)()
@@ -282,9 +304,7 @@ class GpuOperator:
         _lib.check(self.h, self.L.peec_set_residual_precision(self.h, int(precision)))
 
     def solve_mixed(self, b, x0, tol, inner_tol=1e-7, inner_maxit=100, max_outer=8):
-        b = np.ascontiguousarray(np.asarray(b, dtype=np.complex128).ravel())
-        x = np.zeros(self.N, dtype=np.complex128) if x0 is None else \
-            np.array(np.asarray(x0, dtype=np.complex128).ravel())
+        b, x = self._vectors(b, x0)
         flag = ctypes.c_int()
         relres = ctypes.c_double()
         outer = ctypes.c_int()

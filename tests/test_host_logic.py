@@ -117,3 +117,20 @@ def test_dump_json_data_layout():
 def test_do_solving_fft_rejects_other_solver_types():
     with pytest.raises(NotImplementedError):
         api.do_solving_fft({"solverType": 2})
+
+
+def test_operator_rejects_vectors_of_the_wrong_length():
+    """The C library reads N entries from every vector it is given, so the host wrapper
+    checks lengths before any call (no GPU needed: the check comes first)."""
+    import numpy as np
+    import pytest
+    from solver_gb300.operator import GpuOperator
+
+    op = GpuOperator.__new__(GpuOperator)
+    op.N = 10
+    with pytest.raises(ValueError):
+        op._vectors(np.zeros(9), None)
+    with pytest.raises(ValueError):
+        op._vectors(np.zeros(10), np.zeros(11))
+    b, x = op._vectors(np.ones(10), None)
+    assert b.dtype == np.complex128 and x.shape == (10,) and not x.any()

@@ -1,0 +1,121 @@
+"""CPU: the host half of GpuOperator (the conversion of the reference's data structures
+into the C ABI's flat arrays, and its argument checks), run against a stand-in for
+libpeec_gb300.so that records each call's arguments and returns success.
+
+* The topology arrays handed to peec_set_topology agree with the incidence matrices
+  (edge n1/n2 are the -1/+1 columns of A's rows; surface nodes are Gamma's rows).
+* Every parity geometry's genuine frequency state (Yle, SuperLU factors, DZ) passes the
+  wrapper's length checks, and the exported LU parts are CSR of size n.
+* Vectors of the wrong length, a short diagP and a wrong-sized Yle are rejected before any
+  library call."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import peec_oracle as O
+from solver_gb300 import _lib, configs, mesher
+from solver_gb300 import operator as gop
+
+
+class FakeLib:
+    """Arrays are read during the call, as the library copies them before it returns."""
+
+    def __init__(self):
+        self.calls = {}
+
+    def peec_last_error(self, ctx):
+        return b"stand-in"
+
+    def peec_set_topology(self, h, Nx, Ny, Nz, mx, my, mz, ecell, n1, n2, ns, fam, scell,
+                          snode, n):
+        m = mx + my + mz
+        self.n = n
+        self.calls.setdefault("peec_set_topology", []).append(dict(
+            grid=(Nx, Ny, Nz), m=m, ns=ns, n=n, ecell=_arr(ecell, m, np.int64),
+            n1=_arr(n1, m, np.int64), n2=_arr(n2, m, np.int64), fam=_arr(fam, ns, np.int32),
+            scell=_arr(scell, ns, np.int64), snode=_arr(snode, ns, np.int64)))
+        return 0
+
+    def peec_set_frequency(self, h, w, DZ, nnz, yr, yc, yv, Lp, Lc, Lv, Up, Uc, Uv, pr, pc,
+                           extra):
+        self.calls.setdefault("peec_set_frequency", []).append(dict(
+            Lp=_arr(Lp, self.n + 1, np.int64), Up=_arr(Up, self.n + 1, np.int64),
+            pr=_arr(pr, self.n, np.int64), pc=_arr(pc, self.n, np.int64)))
+        return 0
+
+    def __getattr__(self, name):
+        if not name.startswith("peec_"):
+            raise AttributeError(name)
+
+        def call(*args):
+            self.calls.setdefault(name, []).append(args)
+            return 0
+        return call
+
+
+def _arr(p, n, dtype):
+    """Reads n values of dtype behind a ctypes pointer argument (c_void_p)."""
+    addr = p.value if isinstance(p, ctypes.c_void_p) else p
+    return np.ctypeslib.as_array(ctypes.cast(addr, ctypes.POINTER(np.ctypeslib.as_ctypes_type(
+        dtype))), shape=(n,)).copy()
+
+
+@pytest.fixture
+def fake(monkeypatch):
+    L = FakeLib()
+    monkeypatch.setattr(_lib, "load", lambda *a, **k: L)
+    return L
+
+
+CASES = {
+    "crossbar_20x20x4": configs.crossbar_20x20x4,
+    "random_12x10x6": lambda: configs.random_mixed((12, 10, 6), s=5e-5, p=0.35, seed=7,
+                                                   nports=2, freqs=[1e8], tol=1e-8),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_topology_and_frequency_arguments(fake, name):
+    out, freqs, settings, z0, grid = mesher.parse_request(CASES[name]())
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    op = gop.GpuOperator(inc, exp, diag["P"])
+    (t,) = fake.calls["peec_set_topology"]
+    m, ns, n = t["m"], t["ns"], t["n"]
+    assert t["grid"] == tuple(grid) and (m, ns, n) == (op.m, op.ns, op.n)
+    A = inc["A"].tocsr()
+    rows = np.arange(m)
+    assert np.all(A[rows, t["n1"]].A1 == -1) and np.all(A[rows, t["n2"]].A1 == 1)
+    Gm = inc["Gamma"].tocsc()
+    assert np.array_equal(t["snode"], Gm.indices)
+    assert set(np.unique(t["fam"])) <= {0, 1, 2}
+    assert t["ecell"].min() >= 0 and t["scell"].min() >= 0
+    assert np.bincount(t["fam"], minlength=3).sum() == ns
+
+    w = 2 * np.pi * freqs[0] * esc["freq"]
+    fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
+    op.set_frequency(w, fs["DZ"], fs["Yle"], fs["lu"])
+    (f,) = fake.calls["peec_set_frequency"]
+    for ptr in (f["Lp"], f["Up"]):
+        assert ptr[0] == 0 and np.all(np.diff(ptr) >= 1)   # a diagonal entry in every row
+    assert np.array_equal(np.sort(f["pr"]), np.arange(n))
+    assert np.array_equal(np.sort(f["pc"]), np.arange(n))
+
+    x, flag, relres, it, rv = op.gmres(np.ones(op.N), None, 1e-8, 10)
+    assert x.shape == (op.N,)
+    x, flag, relres, outer, inner = op.solve_mixed(np.ones(op.N), None, 1e-8)
+    assert x.shape == (op.N,)
+
+    with pytest.raises(ValueError):
+        op.gmres(np.ones(op.N - 1), None, 1e-8, 10)
+    with pytest.raises(ValueError):
+        op.solve_mixed(np.ones(op.N), np.ones(op.N + 1), 1e-8)
+    with pytest.raises(ValueError):
+        op.matvec(np.ones(op.N + 1))
+    with pytest.raises(ValueError):
+        op.set_frequency(w, fs["DZ"][:-1], fs["Yle"], fs["lu"])
+    import scipy.sparse as sp
+    with pytest.raises(ValueError):
+        op.set_frequency(w, fs["DZ"], sp.eye(op.n + 1, format="csr"), fs["lu"])
+    with pytest.raises(ValueError):
+        gop.GpuOperator(inc, exp, np.asarray(diag["P"]).ravel()[:-1])
