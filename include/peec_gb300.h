@@ -14,6 +14,8 @@
  * indices are 0-based (a Julia caller subtracts 1). Host buffers are
  * caller-owned and only read/written during the call. Every function returns
  * PEEC_OK or a negative PEEC_ERR_* code; peec_last_error() then describes it.
+ * No C++ exception crosses this interface: an exhausted host allocation inside a
+ * call returns PEEC_ERR_OOM, any other internal exception PEEC_ERR_STATE.
  * A context holds one geometry on one GPU with its own CUDA stream; contexts are
  * independent (no global state), so concurrent jobs use separate contexts.
  */

@@ -7,6 +7,8 @@
 #include <algorithm>
 #include <array>
 #include <map>
+#include <new>
+#include <stdexcept>
 #include <tuple>
 #include <cmath>
 #include <complex>
@@ -257,8 +259,8 @@ extern "C" int peec_sizes(const peec_ctx* ctx, int64_t* m, int64_t* ns, int64_t*
   return PEEC_OK;
 }
 
-extern "C" int peec_ctx_create(peec_ctx** out, int device) {
-  if (!out) return badarg(__func__);
+static int peec_ctx_create_body(peec_ctx** out, int device) {
+  if (!out) return badarg("peec_ctx_create");
   *out = nullptr;
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -382,13 +384,13 @@ static int fft_len(int na, int nb, bool sym) {
   return pow2ceil(need < 1 ? 1 : need);
 }
 
-extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t mx, int64_t my,
+static int peec_set_topology_body(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t mx, int64_t my,
                                  int64_t mz, const int64_t* edge_cell, const int64_t* edge_n1,
                                  const int64_t* edge_n2, int64_t ns, const int32_t* surf_fam,
                                  const int64_t* surf_cell, const int64_t* surf_node, int64_t n) {
   NvtxRange nvtx_range_("peec_set_topology");
   drop_graphs(ctx);
-  if (!ctx) return badarg(__func__);
+  if (!ctx) return badarg("peec_set_topology");
   if (Nx < 1 || Ny < 1 || Nz < 1 || mx < 0 || my < 0 || mz < 0 || ns < 0 || n < 1)
     return bad(ctx, PEEC_ERR_BADARG, "peec_set_topology: invalid sizes");
   const int64_t m = mx + my + mz;
@@ -532,9 +534,9 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
   return PEEC_OK;
 }
 
-extern "C" int peec_set_pdiag(peec_ctx* ctx, const double* diagP) {
+static int peec_set_pdiag_body(peec_ctx* ctx, const double* diagP) {
   drop_graphs(ctx);
-  if (!ctx || !diagP) return badarg(__func__);
+  if (!ctx || !diagP) return badarg("peec_set_pdiag");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   std::vector<double> inv(ctx->ns);
   for (int64_t s = 0; s < ctx->ns; ++s) inv[s] = 1.0 / diagP[s];
@@ -571,9 +573,9 @@ static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
   return PEEC_OK;
 }
 
-extern "C" int peec_set_rows(peec_ctx* ctx, const double* const rows[9]) {
+static int peec_set_rows_body(peec_ctx* ctx, const double* const rows[9]) {
   NvtxRange nvtx_range_("peec_set_rows");
-  if (!ctx || !rows) return badarg(__func__);
+  if (!ctx || !rows) return badarg("peec_set_rows");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
   double* d_rows[9] = {};
@@ -594,10 +596,10 @@ extern "C" int peec_set_rows(peec_ctx* ctx, const double* const rows[9]) {
   return rc;
 }
 
-extern "C" int peec_fill(peec_ctx* ctx, const double origin[3], double sx, double sy, double sz,
+static int peec_fill_body(peec_ctx* ctx, const double origin[3], double sx, double sy, double sz,
                          double escal_Lp, double escal_P, double* const rows_out[9]) {
   NvtxRange nvtx_range_("peec_fill");
-  if (!ctx || !origin) return badarg(__func__);
+  if (!ctx || !origin) return badarg("peec_fill");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
   double* d_rows[9] = {};
@@ -814,7 +816,7 @@ static int build_solve_plan(peec_ctx* ctx, int64_t n) {
   return PEEC_OK;
 }
 
-extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,
+static int peec_set_frequency_body(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,
                                   const int64_t* yle_row, const int64_t* yle_col,
                                   const double* yle_val, const int64_t* L_ptr,
                                   const int64_t* L_col, const double* L_val,
@@ -823,7 +825,7 @@ extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int
                                   const int64_t* perm_c, const double* row_scale) {
   NvtxRange nvtx_range_("peec_set_frequency");
   drop_graphs(ctx);
-  if (!ctx || !DZ || !L_ptr || !U_ptr || !perm_r || !perm_c) return badarg(__func__);
+  if (!ctx || !DZ || !L_ptr || !U_ptr || !perm_r || !perm_c) return badarg("peec_set_frequency");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
   const int64_t n = ctx->n, m = ctx->m;
@@ -995,9 +997,9 @@ static int matvec_dev(peec_ctx* ctx, const c64* x, c64* y, int prec, bool timed)
   return PEEC_OK;
 }
 
-extern "C" int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precision) {
+static int peec_matvec_dev_body(peec_ctx* ctx, const void* x, void* y, int precision) {
   NvtxRange nvtx_range_("peec_matvec_dev");
-  if (!ctx || !x || !y) return badarg(__func__);
+  if (!ctx || !x || !y) return badarg("peec_matvec_dev");
   if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
   cudaSetDevice(ctx->dev);
   CTX_TRY(matvec_dev(ctx, (const c64*)x, (c64*)y, precision, true));
@@ -1009,9 +1011,9 @@ extern "C" int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precis
   return PEEC_OK;
 }
 
-extern "C" int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precision) {
+static int peec_matvec_body(peec_ctx* ctx, const double* x, double* y, int precision) {
   NvtxRange nvtx_range_("peec_matvec");
-  if (!ctx || !x || !y) return badarg(__func__);
+  if (!ctx || !x || !y) return badarg("peec_matvec");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
   const size_t bytes = sizeof(c64) * ctx->N;
@@ -1039,8 +1041,8 @@ extern "C" int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* dims, int
   return PEEC_OK;
 }
 
-extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, double* ms) {
-  if (!ctx || !ms || iters < 1) return badarg(__func__);
+static int peec_profile_matvec_body(peec_ctx* ctx, int precision, int iters, double* ms) {
+  if (!ctx || !ms || iters < 1) return badarg("peec_profile_matvec");
   if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
   cudaSetDevice(ctx->dev);
   if (ctx->pev.size() != 6) {
@@ -1076,7 +1078,7 @@ extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, doub
   return PEEC_OK;
 }
 
-extern "C" int peec_multidot(peec_ctx* ctx, const void* U, int64_t ldu, const void* v, int64_t N,
+static int peec_multidot_body(peec_ctx* ctx, const void* U, int64_t ldu, const void* v, int64_t N,
                              int k, void* out) {
   if (!ctx || !U || !v || !out || N < 1 || k < 1 || ldu < N)
     return PEEC_ERR_BADARG;
@@ -1104,9 +1106,9 @@ extern "C" int peec_last_timing(peec_ctx* ctx, double* total_ms, double* conv_ms
   return PEEC_OK;
 }
 
-extern "C" int peec_port_rhs(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, double* tn) {
+static int peec_port_rhs_body(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, double* tn) {
   NvtxRange nvtx_range_("peec_port_rhs");
-  if (!ctx || !tn) return badarg(__func__);
+  if (!ctx || !tn) return badarg("peec_port_rhs");
   if (!ctx->have_freq || !ctx->have_pdiag) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
   if (n1 < 0 || n1 >= ctx->n || n2 < 0 || n2 >= ctx->n) return bad(ctx, PEEC_ERR_BADARG, "port node out of range");
   cudaSetDevice(ctx->dev);
@@ -1127,8 +1129,8 @@ extern "C" int peec_port_rhs(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, d
   return PEEC_OK;
 }
 
-extern "C" int peec_check_wait_limit(peec_ctx* ctx) {
-  if (!ctx) return badarg(__func__);
+static int peec_check_wait_limit_body(peec_ctx* ctx) {
+  if (!ctx) return badarg("peec_check_wait_limit");
   cudaSetDevice(ctx->dev);
   int e = 0;
   const int rc = selftest_wait_limit(1 << 16, ctx->st, &e);
@@ -1138,11 +1140,12 @@ extern "C" int peec_check_wait_limit(peec_ctx* ctx) {
   return PEEC_OK;
 }
 
-extern "C" int peec_adjoint(peec_ctx* ctx, const double* x, const int32_t* v1,
+static int peec_adjoint_body(peec_ctx* ctx, const double* x, const int32_t* v1,
                             const int32_t* v2, const double* d1, const double* d2, double Is,
                             int64_t nvox, double* g) {
   NvtxRange nvtx_range_("peec_adjoint");
-  if (!ctx || !x || !v1 || !v2 || !d1 || !d2 || !g || nvox < 0 || Is == 0) return badarg(__func__);
+  if (!ctx || !x || !v1 || !v2 || !d1 || !d2 || !g || nvox < 0 || Is == 0)
+    return badarg("peec_adjoint");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
   cudaSetDevice(ctx->dev);
   const int64_t m = ctx->m;
@@ -1627,11 +1630,11 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
   return g.rc;
 }
 
-extern "C" int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, double tol, int maxit,
+static int peec_gmres_body(peec_ctx* ctx, const double* b, double* x_inout, double tol, int maxit,
                           int restarted, int restart, int precision, int* flag, double* relres,
                           int* iter, double* resvec, int resvec_cap, int* nres) {
   NvtxRange nvtx_range_("peec_gmres");
-  if (!ctx || !b || !x_inout || !flag || !relres || !iter) return badarg(__func__);
+  if (!ctx || !b || !x_inout || !flag || !relres || !iter) return badarg("peec_gmres");
   if (maxit < 1 || (restarted && restart < 1)) return bad(ctx, PEEC_ERR_BADARG, "maxit/restart must be >= 1");
   if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
   if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
@@ -1654,11 +1657,11 @@ extern "C" int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, doubl
   return rc;
 }
 
-extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout, double tol,
+static int peec_solve_mixed_body(peec_ctx* ctx, const double* b, double* x_inout, double tol,
                                 double inner_tol, int inner_maxit, int max_outer, int* flag,
                                 double* relres, int* outer_out, int* inner_total) {
   NvtxRange nvtx_range_("peec_solve_mixed");
-  if (!ctx || !b || !x_inout || !flag || !relres) return badarg(__func__);
+  if (!ctx || !b || !x_inout || !flag || !relres) return badarg("peec_solve_mixed");
   if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
   cudaSetDevice(ctx->dev);
   const size_t N = ctx->N, bytes = sizeof(c64) * N;
@@ -1753,16 +1756,16 @@ extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout,
   return PEEC_OK;
 }
 
-extern "C" int peec_set_residual_precision(peec_ctx* ctx, int precision) {
-  if (!ctx) return badarg(__func__);
+static int peec_set_residual_precision_body(peec_ctx* ctx, int precision) {
+  if (!ctx) return badarg("peec_set_residual_precision");
   if (precision != PEEC_PREC_FP64 && precision != PEEC_PREC_FF)
     return bad(ctx, PEEC_ERR_BADARG, "residual precision must be PEEC_PREC_FP64 or PEEC_PREC_FF");
   ctx->resid_prec = precision;
   return PEEC_OK;
 }
 
-extern "C" int peec_set_lu_component_max(peec_ctx* ctx, int max_rows) {
-  if (!ctx) return badarg(__func__);
+static int peec_set_lu_component_max_body(peec_ctx* ctx, int max_rows) {
+  if (!ctx) return badarg("peec_set_lu_component_max");
   if (max_rows < 0 || max_rows > SF_COMP_MAX)
     return bad(ctx, PEEC_ERR_BADARG, "component size limit outside 0.." + std::to_string(SF_COMP_MAX));
   cudaSetDevice(ctx->dev);
@@ -1770,4 +1773,161 @@ extern "C" int peec_set_lu_component_max(peec_ctx* ctx, int max_rows) {
   ctx->comp_max = max_rows;
   if (ctx->have_freq) CTX_TRY(build_solve_plan(ctx, ctx->n));
   return PEEC_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Exported entry points. Each runs its body under one guard, so that no C++ exception
+// reaches the caller: an exhausted host allocation returns PEEC_ERR_OOM, any other
+// exception PEEC_ERR_STATE, each with its message for peec_last_error.
+
+static void record_exception(peec_ctx* ctx, const char* fn, const char* what) noexcept {
+  try {
+    std::string msg = std::string(fn) + ": " + what;
+    g_err = msg;
+    if (ctx) ctx->err = msg;
+  } catch (...) {
+    g_err.assign("out of memory");  // fits the string's inline buffer: no allocation
+  }
+}
+
+template <typename F>
+static int guarded(peec_ctx* ctx, const char* fn, F&& body) noexcept {
+  try {
+    return body();
+  } catch (const std::bad_alloc&) {
+    record_exception(ctx, fn, "host memory allocation failed");
+    return PEEC_ERR_OOM;
+  } catch (const std::length_error& e) {
+    record_exception(ctx, fn, e.what());
+    return PEEC_ERR_OOM;
+  } catch (const std::exception& e) {
+    record_exception(ctx, fn, e.what());
+    return PEEC_ERR_STATE;
+  } catch (...) {
+    record_exception(ctx, fn, "unknown exception");
+    return PEEC_ERR_STATE;
+  }
+}
+
+extern "C" int peec_ctx_create(peec_ctx** out, int device) {
+  return guarded(nullptr, "peec_ctx_create", [&] {
+    return peec_ctx_create_body(out, device);
+  });
+}
+
+extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t mx, int64_t my,
+                                 int64_t mz, const int64_t* edge_cell, const int64_t* edge_n1,
+                                 const int64_t* edge_n2, int64_t ns, const int32_t* surf_fam,
+                                 const int64_t* surf_cell, const int64_t* surf_node, int64_t n) {
+  return guarded(ctx, "peec_set_topology", [&] {
+    return peec_set_topology_body(ctx, Nx, Ny, Nz, mx, my, mz, edge_cell, edge_n1, edge_n2, ns,
+        surf_fam, surf_cell, surf_node, n);
+  });
+}
+
+extern "C" int peec_set_pdiag(peec_ctx* ctx, const double* diagP) {
+  return guarded(ctx, "peec_set_pdiag", [&] {
+    return peec_set_pdiag_body(ctx, diagP);
+  });
+}
+
+extern "C" int peec_set_rows(peec_ctx* ctx, const double* const rows[9]) {
+  return guarded(ctx, "peec_set_rows", [&] {
+    return peec_set_rows_body(ctx, rows);
+  });
+}
+
+extern "C" int peec_fill(peec_ctx* ctx, const double origin[3], double sx, double sy, double sz,
+                         double escal_Lp, double escal_P, double* const rows_out[9]) {
+  return guarded(ctx, "peec_fill", [&] {
+    return peec_fill_body(ctx, origin, sx, sy, sz, escal_Lp, escal_P, rows_out);
+  });
+}
+
+extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,
+                                  const int64_t* yle_row, const int64_t* yle_col,
+                                  const double* yle_val, const int64_t* L_ptr,
+                                  const int64_t* L_col, const double* L_val,
+                                  const int64_t* U_ptr, const int64_t* U_col,
+                                  const double* U_val, const int64_t* perm_r,
+                                  const int64_t* perm_c, const double* row_scale) {
+  return guarded(ctx, "peec_set_frequency", [&] {
+    return peec_set_frequency_body(ctx, w, DZ, yle_nnz, yle_row, yle_col, yle_val, L_ptr, L_col,
+        L_val, U_ptr, U_col, U_val, perm_r, perm_c, row_scale);
+  });
+}
+
+extern "C" int peec_matvec_dev(peec_ctx* ctx, const void* x, void* y, int precision) {
+  return guarded(ctx, "peec_matvec_dev", [&] {
+    return peec_matvec_dev_body(ctx, x, y, precision);
+  });
+}
+
+extern "C" int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precision) {
+  return guarded(ctx, "peec_matvec", [&] {
+    return peec_matvec_body(ctx, x, y, precision);
+  });
+}
+
+extern "C" int peec_profile_matvec(peec_ctx* ctx, int precision, int iters, double* ms) {
+  return guarded(ctx, "peec_profile_matvec", [&] {
+    return peec_profile_matvec_body(ctx, precision, iters, ms);
+  });
+}
+
+extern "C" int peec_multidot(peec_ctx* ctx, const void* U, int64_t ldu, const void* v, int64_t N,
+                             int k, void* out) {
+  return guarded(ctx, "peec_multidot", [&] {
+    return peec_multidot_body(ctx, U, ldu, v, N, k, out);
+  });
+}
+
+extern "C" int peec_port_rhs(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, double* tn) {
+  return guarded(ctx, "peec_port_rhs", [&] {
+    return peec_port_rhs_body(ctx, n1, n2, Is, tn);
+  });
+}
+
+extern "C" int peec_check_wait_limit(peec_ctx* ctx) {
+  return guarded(ctx, "peec_check_wait_limit", [&] {
+    return peec_check_wait_limit_body(ctx);
+  });
+}
+
+extern "C" int peec_adjoint(peec_ctx* ctx, const double* x, const int32_t* v1,
+                            const int32_t* v2, const double* d1, const double* d2, double Is,
+                            int64_t nvox, double* g) {
+  return guarded(ctx, "peec_adjoint", [&] {
+    return peec_adjoint_body(ctx, x, v1, v2, d1, d2, Is, nvox, g);
+  });
+}
+
+extern "C" int peec_gmres(peec_ctx* ctx, const double* b, double* x_inout, double tol, int maxit,
+                          int restarted, int restart, int precision, int* flag, double* relres,
+                          int* iter, double* resvec, int resvec_cap, int* nres) {
+  return guarded(ctx, "peec_gmres", [&] {
+    return peec_gmres_body(ctx, b, x_inout, tol, maxit, restarted, restart, precision, flag,
+        relres, iter, resvec, resvec_cap, nres);
+  });
+}
+
+extern "C" int peec_solve_mixed(peec_ctx* ctx, const double* b, double* x_inout, double tol,
+                                double inner_tol, int inner_maxit, int max_outer, int* flag,
+                                double* relres, int* outer_out, int* inner_total) {
+  return guarded(ctx, "peec_solve_mixed", [&] {
+    return peec_solve_mixed_body(ctx, b, x_inout, tol, inner_tol, inner_maxit, max_outer, flag,
+        relres, outer_out, inner_total);
+  });
+}
+
+extern "C" int peec_set_lu_component_max(peec_ctx* ctx, int max_rows) {
+  return guarded(ctx, "peec_set_lu_component_max", [&] {
+    return peec_set_lu_component_max_body(ctx, max_rows);
+  });
+}
+
+extern "C" int peec_set_residual_precision(peec_ctx* ctx, int precision) {
+  return guarded(ctx, "peec_set_residual_precision", [&] {
+    return peec_set_residual_precision_body(ctx, precision);
+  });
 }
