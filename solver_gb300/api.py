@@ -67,11 +67,11 @@ def _ensure_spectra(op, FFTCP, FFTCLp):
         if FFTCP.op is not op:
             raise ValueError("spectra belong to another operator context")
         return
-    key = (id(FFTCP), id(FFTCLp))
-    if getattr(op, "_spec_key", None) == key:
+    src = getattr(op, "_spec_src", None)
+    if src is not None and src[0] is FFTCP and src[1] is FFTCLp:
         return
     op.set_rows(rows_from_reference_spectra(FFTCP, FFTCLp, op.grid))
-    op._spec_key = key
+    op._spec_src = (FFTCP, FFTCLp)  # held, so these identities stay unique while cached
 
 
 def compute_FFT_mutual_coupling_mats(circulant_centers, escalings, Nx, Ny, Nz, QS_Rcc_FW=1,
@@ -93,7 +93,7 @@ def compute_FFT_mutual_coupling_mats(circulant_centers, escalings, Nx, Ny, Nz, Q
 
 
 def _set_freq(op, w, DZ, Yle, lu):
-    op.set_frequency(w, DZ, Yle, lu, key=(float(w), id(DZ), id(Yle), id(lu)))
+    op.set_frequency(w, DZ, Yle, lu, key=(float(w), DZ, Yle, lu))
 
 
 def _lu_object(lu):
@@ -367,7 +367,7 @@ def _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode, mixed_inne
         if stop_flag is not None and stop_flag.value:
             return None
         fs = pf.get(k)
-        op.set_frequency(w[k], fs.DZ, fs.Yle, fs.lu, key=("sweep", k, float(w[k])))
+        op.set_frequency(w[k], fs.DZ, fs.Yle, fs.lu)
         tk = float(tol[k]) if np.ndim(tol) else float(tol)
         for c1 in range(npt):
             n1, n2 = pn[c1]

@@ -107,6 +107,7 @@ class GpuOperator:
             raise ValueError(f"diagP has {dp.size} entries, expected {self.ns}")
         _lib.check(self.h, self.L.peec_set_pdiag(self.h, _lib.ptr(dp)))
         self._freq_key = None
+        self._spec_src = None  # the host spectra the device rows were recovered from
         self._stop = None
 
     def close(self):
@@ -136,6 +137,7 @@ class GpuOperator:
                 raise ValueError(f"row {k} has {r.size} entries, expected {n}")
             keep.append(r)
             arr[i] = r.ctypes.data
+        self._spec_src = None
         _lib.check(self.h, self.L.peec_set_rows(self.h, arr))
         self._rows = {k: v for k, v in rows.items()}
 
@@ -152,6 +154,7 @@ class GpuOperator:
                 arr[i] = outs[k].ctypes.data
             else:
                 arr[i] = None
+        self._spec_src = None
         _lib.check(self.h, self.L.peec_fill(self.h, _lib.ptr(o), sx, sy, sz, escal_Lp, escal_P,
                                             arr))
         self._rows = outs  # kept for clone()
@@ -170,8 +173,19 @@ class GpuOperator:
         return c
 
     # -- frequency ------------------------------------------------------------------
+    @staticmethod
+    def _same_key(a, b):
+        """Keys are tuples of scalars and host objects; objects match by identity. A key
+        keeps its objects alive, so an identity cannot be reused while it is cached."""
+        if a is None or b is None or len(a) != len(b):
+            return False
+        return all(x is y or (isinstance(x, (int, float, str)) and type(x) is type(y) and x == y)
+                   for x, y in zip(a, b))
+
     def set_frequency(self, w, DZ, Yle, lu, key=None):
-        if key is not None and key == self._freq_key:
+        """Uploads one frequency's state. With a key (a tuple of scalars and the host
+        objects the state came from), a repeated call with the same key is skipped."""
+        if key is not None and self._same_key(key, self._freq_key):
             return
         DZ = np.ascontiguousarray(np.asarray(DZ, dtype=np.complex128).ravel())
         if DZ.size != self.m:
@@ -182,6 +196,7 @@ class GpuOperator:
         yr = Y.row.astype(np.int64)
         yc = Y.col.astype(np.int64)
         yv = np.ascontiguousarray(Y.data.astype(np.complex128))
+        self._freq_key = None  # a failed upload leaves no usable state behind
         (Lp, Lc, Lv), (Up, Uc, Uv), pr, pc = export_lu(lu)
         for ptr, col, val in ((Lp, Lc, Lv), (Up, Uc, Uv)):
             if ptr.size != self.n + 1 or ptr[-1] != col.size or val.size != 2 * col.size:

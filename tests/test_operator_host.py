@@ -119,3 +119,36 @@ def test_topology_and_frequency_arguments(fake, name):
         op.set_frequency(w, fs["DZ"], sp.eye(op.n + 1, format="csr"), fs["lu"])
     with pytest.raises(ValueError):
         gop.GpuOperator(inc, exp, np.asarray(diag["P"]).ravel()[:-1])
+
+
+def test_cached_state_is_keyed_by_the_objects_themselves(fake):
+    """api's frequency and spectra caches hold the host objects they were built from and
+    compare them by identity: an equal but new object uploads again, the same object does
+    not, and new device rows invalidate the spectra cache."""
+    from solver_gb300 import api
+    out, freqs, settings, z0, grid = mesher.parse_request(configs.crossbar_20x20x4())
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    op = gop.GpuOperator(inc, exp, diag["P"])
+    w = 2 * np.pi * freqs[0] * esc["freq"]
+    fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
+    n_set = lambda: len(fake.calls.get("peec_set_frequency", []))
+    api._set_freq(op, w, fs["DZ"], fs["Yle"], fs["lu"])
+    api._set_freq(op, w, fs["DZ"], fs["Yle"], fs["lu"])
+    assert n_set() == 1
+    api._set_freq(op, w, fs["DZ"].copy(), fs["Yle"], fs["lu"])
+    assert n_set() == 2
+    api._set_freq(op, w * 2, fs["DZ"], fs["Yle"], fs["lu"])
+    assert n_set() == 3
+    op.set_frequency(w, fs["DZ"], fs["Yle"], fs["lu"])          # unkeyed: always uploads
+    api._set_freq(op, w, fs["DZ"], fs["Yle"], fs["lu"])
+    assert n_set() == 5
+
+    rows = O.fill_rows(cc, esc, *grid)
+    FFTCP, FFTCLp = O.spectra_from_rows(rows, *grid)
+    n_rows = lambda: len(fake.calls.get("peec_set_rows", []))
+    api._ensure_spectra(op, FFTCP, FFTCLp)
+    api._ensure_spectra(op, FFTCP, FFTCLp)
+    assert n_rows() == 1
+    op.set_rows(rows)                                            # other rows on the device
+    api._ensure_spectra(op, FFTCP, FFTCLp)
+    assert n_rows() == 3
