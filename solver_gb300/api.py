@@ -190,18 +190,25 @@ class PortLanes:
 
         get_state(k, pos) -> state with w, DZ, Yle, lu; release(k) is called once every
         lane has set state k. record(pos, k, c, V, flag, relres, outer, inner) is called
-        from the lane threads after each solve. Returns False if stopped."""
+        from the lane threads after each solve. Returns False if stopped. An exception in
+        one lane stops the others before their next frequency or port solve, and is then
+        raised here."""
+        import threading
         L = len(self.ops)
         npt = len(pn)
         left = {}
-        lock = __import__("threading").Lock()
+        lock = threading.Lock()
         stopped = []
+        failed = threading.Event()
+
+        def halted():
+            return failed.is_set() or (stop_flag is not None and stop_flag.value)
 
         def lane(i):
             op = self.ops[i]
             mine = range(i, npt, L)
             for pos, k in enumerate(seq):
-                if stop_flag is not None and stop_flag.value:
+                if halted():
                     stopped.append(True)
                     return
                 fs = get_state(k, pos)
@@ -211,6 +218,8 @@ class PortLanes:
                     if left[pos] == 0 and k not in seq[pos + 1:]:
                         release(k)
                 for c in mine:
+                    if failed.is_set():
+                        return
                     tn = op.port_rhs(pn[c][0], pn[c][1], Is)
                     V, flag, relres, outer, inner = op.solve_mixed(tn, Vrest[:, c], tol_of(k),
                                                                    **solve_kw)
@@ -220,9 +229,18 @@ class PortLanes:
                     Vrest[:, c] = V
                     record(pos, k, c, V, flag, relres, outer, inner)
 
-        futs = [self._pool.submit(lane, i) for i in range(min(L, npt))]
-        for f in futs:
-            f.result()
+        def guarded_lane(i):
+            try:
+                lane(i)
+            except BaseException:
+                failed.set()
+                raise
+
+        futs = [self._pool.submit(guarded_lane, i) for i in range(min(L, npt))]
+        errors = [f.exception() for f in futs]
+        for e in errors:
+            if e is not None:
+                raise e
         return not stopped
 
     def close(self):

@@ -134,3 +134,24 @@ def test_operator_rejects_vectors_of_the_wrong_length():
         op._vectors(np.zeros(10), np.zeros(11))
     b, x = op._vectors(np.ones(10), None)
     assert b.dtype == np.complex128 and x.shape == (10,) and not x.any()
+
+
+def test_lanes_sweep_failure_in_one_lane_stops_the_others():
+    """A lane whose solve raises (a failed library call, say) stops the other lanes before
+    their next frequency or port, and the exception reaches the caller."""
+    log = []
+    lanes = FakeLanes(2, log)
+
+    def boom(tn, x0, tol, **kw):
+        raise RuntimeError("lane 0 failed")
+    lanes.ops[0].solve_mixed = boom
+    seq = list(range(50))
+    try:
+        with pytest.raises(RuntimeError, match="lane 0 failed"):
+            lanes.sweep(seq, lambda k, pos: State(float(k)), lambda k: None,
+                        np.array([[0, 1], [2, 3]]), 1.0, np.zeros((3, 2), complex),
+                        lambda k: 1e-8, {}, lambda *a: None)
+    finally:
+        lanes.close()
+    solves = [e for e in log if e[1] == "solve"]
+    assert len(solves) < len(seq)  # lane 1 did not run the whole sweep
