@@ -1174,8 +1174,13 @@ static int peec_adjoint_body(peec_ctx* ctx, const double* x, const int32_t* v1,
   cudaMemsetAsync(dg, 0, sizeof(double) * 2 * (size_t)std::max<int64_t>(nvox, 1), st);
   launch_adjoint(ctx->dx, dv1, dv2, dd1, dd2, 2.0 / Is, m, nvox, dg, st);
   ctx->launches++;
-  cudaMemcpyAsync(g, dg, sizeof(double) * 2 * (size_t)nvox, cudaMemcpyDeviceToHost, st);
-  const cudaError_t e = cudaStreamSynchronize(st);
+  cudaError_t e = cudaGetLastError();  // launch configuration errors are not sticky
+  if (e == cudaSuccess) {
+    cudaMemcpyAsync(g, dg, sizeof(double) * 2 * (size_t)nvox, cudaMemcpyDeviceToHost, st);
+    e = cudaStreamSynchronize(st);
+  } else {
+    cudaStreamSynchronize(st);  // the uploads above still read caller memory
+  }
   if (e != cudaSuccess) rc = fail_cuda(e, "peec_adjoint", __FILE__, __LINE__);
   cleanup();
   return rc;
