@@ -220,3 +220,53 @@ def test_oracle_gmres_matches_a_dense_solve():
     assert flag == 0 and relres <= 1e-11
     x_dense = np.linalg.solve(O.dense_operator(mv, m + ns + n), tn)
     assert np.max(np.abs(x - x_dense)) <= 1e-9 * np.max(np.abs(x_dense))
+
+
+def _dense(A):
+    A = np.asarray(A, dtype=np.complex128)
+    return lambda v: A @ v
+
+
+def test_oracle_gmres_control_flow_known_answers():
+    """The oracle GMRES on small dense systems with known answers, following the
+    MATLAB semantics of gmres_custom.jl:
+    * a zero right-hand side returns x = 0, flag 0, relres 0, iter [0, 0] (:20-28);
+    * an initial guess that already meets the tolerance returns unchanged with iter [0, 0]
+      and resvec = [|r0|] (:47-55);
+    * the identity converges in one inner step;
+    * a diagonal operator with k distinct eigenvalues converges in k inner steps (the
+      Krylov space holds the solution after k steps);
+    * maxit is clamped to the system size (:12-16): with maxit 100 a 6 x 6 system
+      converges within 6 steps;
+    * a budget too small ends with flag 1 at the smallest residual seen."""
+    rng = np.random.default_rng(3)
+    n = 6
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+
+    x, flag, relres, it, rv = O.gmres_custom(np.zeros(n), False, 1e-10, 5, None, _dense(np.eye(n)))
+    assert flag == 0 and relres == 0.0 and list(it) == [0, 0] and not np.any(x)
+    assert list(rv) == [0.0]
+
+    A = np.diag([1.0, 2.0, 3.0, 4.0, 5.0, 6.0]) + 0j
+    xs = np.linalg.solve(A, b)
+    x, flag, relres, it, rv = O.gmres_custom(b, False, 1e-8, 5, xs, _dense(A))
+    assert flag == 0 and list(it) == [0, 0] and np.array_equal(x, xs)
+    assert len(rv) == 1 and rv[0] == np.linalg.norm(b - A @ xs)
+
+    x, flag, relres, it, rv = O.gmres_custom(b, False, 1e-12, 5, None, _dense(np.eye(n)))
+    assert flag == 0 and list(it) == [1, 1] and np.allclose(x, b, rtol=0, atol=1e-14)
+
+    D = np.diag([2.0, 2.0, 5.0, 5.0, 5.0, -1.0]) + 0j    # three distinct eigenvalues
+    x, flag, relres, it, rv = O.gmres_custom(b, False, 1e-10, 6, None, _dense(D))
+    assert flag == 0 and list(it) == [1, 3]
+    assert np.allclose(x, np.linalg.solve(D, b), rtol=1e-9, atol=0)
+
+    M = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + 4 * np.eye(n)
+    x, flag, relres, it, rv = O.gmres_custom(b, False, 1e-12, 100, None, _dense(M))
+    assert flag == 0 and it[0] == 1 and it[1] <= n
+    assert np.linalg.norm(b - M @ x) <= 1e-11 * np.linalg.norm(b)
+
+    x, flag, relres, it, rv = O.gmres_custom(b, False, 1e-14, 2, None, _dense(M))
+    assert flag == 1 and list(it) == [1, 2]
+    assert np.isclose(relres, np.min(rv) / np.linalg.norm(b), rtol=1e-8)
+    assert np.isclose(np.linalg.norm(b - M @ x) / np.linalg.norm(b), relres, rtol=1e-8)
