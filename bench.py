@@ -382,16 +382,16 @@ def run_small_configs(args):
     * the same geometry in mixed precision to 1e-8 at 1 GHz and five log-spaced
       frequencies 100 MHz - 10 GHz: per-frequency port-impedance error against the GPU
       FP64 sweep at 1e-12 (itself parity-tested against the oracle at 1e-10)."""
-    from oracle import peec_oracle as O
     from solver_gb300 import api, configs, mesher
+    from solver_gb300 import frequency as fq
     from solver_gb300.operator import GpuOperator
     out, freqs, settings, z0, grid = mesher.parse_request(configs.crossbar_20x20x4())
     esc, inc, cc, diag, exp, ports, le, li, Zs = out
     op = GpuOperator(inc, exp, diag["P"])
     op.fill(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"])
     w = 2 * np.pi * freqs[0] * esc["freq"]
-    fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
-    op.set_frequency(w, fs["DZ"], fs["Yle"], fs["lu"])
+    st = fq.FrequencyState(w, esc, inc, diag, Zs, le, ports, z0)
+    op.set_frequency(w, st.DZ, st.Yle, st.lu)
     n1, n2 = np.asarray(ports["port_nodes"]).reshape(-1, 2)[0]
     tn = op.port_rhs(n1, n2, esc["Is"])
     times = []
@@ -401,7 +401,10 @@ def run_small_configs(args):
         if i >= args.warmup:
             times.append(time.perf_counter() - t)
     gpu_s = float(np.median(times))
-    # the CPU oracle on the same system (reference 2N extents, SuperLU, Householder GMRES)
+    # cpu_baseline leg: the CPU oracle on the same system (reference 2N extents, SuperLU,
+    # Householder GMRES)
+    from oracle import peec_oracle as O
+    fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
     rows = O.fill_rows(cc, esc, *grid)
     FFTCP, FFTCLp = O.spectra_from_rows(rows, *grid)
     mv = lambda x: O.ComputeMatrixVectorFTT(x, w, inc, FFTCP, FFTCLp, fs["DZ"], fs["Yle"], exp,
