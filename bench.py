@@ -98,13 +98,25 @@ def dist_init():
 
 
 def barrier_max(ws, value):
+    """The maximum of value over the ranks (a device tensor under NCCL, a host tensor
+    under gloo)."""
     if ws == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rates(ws, steps, gpu_s, wall_s):
+    """Replicas: every rank solves `steps` frequency points of its own. The whole-job rate
+    is the points of all ranks over the slowest rank's time, for the device-timed value
+    and for the end-to-end wall clock."""
+    gpu_max = barrier_max(ws, gpu_s)
+    wall_max = barrier_max(ws, wall_s)
+    return ws * steps / gpu_max, ws * steps / wall_max, gpu_max, wall_max
 
 
 def barrier(ws):
@@ -691,10 +703,7 @@ def main():
     barrier(ws)
     clk = clocks.stop()
     launches = sum(o.launch_count() for o in P["lanes"].ops) - l0
-    gpu_s = barrier_max(ws, gpu_ms / 1e3)
-    wall_s = barrier_max(ws, t_wall)
-    value = ws * args.steps / gpu_s
-    e2e_v = ws * args.steps / wall_s
+    value, e2e_v, gpu_s, wall_s = whole_job_rates(ws, args.steps, gpu_ms / 1e3, t_wall)
 
     # -- FP64 plain (reference algorithm) on the same frequency sequence ---------------------
     # the warm-up points build the same warm starts untimed; then the first fp64_steps of
