@@ -254,9 +254,10 @@ int peec_multidot(peec_ctx* ctx, const void* U, int64_t ldu, const void* v, int6
  * doubles (4.98 MB), resident on every GPU that loads the library until the
  * process exits. k > PEEC_NOALLOC_MAX_K is rejected with PEEC_ERR_BADARG; any N
  * is accepted. The first call on a device looks up the array's device address
- * (one-time set-up); make that first call before any stream capture. All calls
- * share the array: calls that overlap on the GPU (other threads, other streams)
- * race on it and must be serialised by the caller. Calls no cudaMalloc/cudaFree.
+ * (one-time set-up). The call synchronises its stream, so it cannot be captured
+ * into a CUDA graph. All calls on a device share the array and take it in turn:
+ * a per-device lock is held from launch to completion, so calls from several
+ * threads or streams are serialised. Calls no cudaMalloc/cudaFree.
  */
 #define PEEC_NOALLOC_MAX_K 256
 int peec_multidot_noalloc(const void* U, int64_t ldu, const void* v, int64_t N, int k,

@@ -433,6 +433,9 @@ static __device__ __align__(256) c64 g_noalloc_partials[(size_t)NOALLOC_BLOCKS *
 
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_addr[256] = {};  // device address of the array, per device ordinal
+// held from launch to completion: calls on one device (any thread, any stream) take
+// the shared array in turn
+static std::mutex g_noalloc_run_mu[256];
 
 }  // namespace peec
 
@@ -468,6 +471,7 @@ extern "C" int peec_multidot_noalloc(const void* U, int64_t ldu, const void* v, 
     scratch = g_noalloc_addr[dev];
   }
   cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::mutex> run(g_noalloc_run_mu[dev]);
   // every partial[c][b] the reduction reads (c < k, b < grid) is written by this call's
   // multi-dot first, so the array needs no clearing between calls
   launch_multidot((const c64*)U, (size_t)ldu, (const c64*)v, (size_t)N, k, (c64*)scratch,

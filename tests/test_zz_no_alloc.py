@@ -69,3 +69,47 @@ def test_noalloc_rejects_too_many_columns():
                                  N, k, ctypes.c_void_p(out.data_ptr()), None)
     assert rc == -5
     assert b"256" in L.peec_last_error(None)
+
+
+def test_noalloc_concurrent_threads_get_their_own_results():
+    """Four host threads, each on its own CUDA stream with its own vectors, call the entry
+    point repeatedly at the same time; the per-device lock gives each call the shared
+    scratch alone, so every thread's last result equals its own inner products."""
+    import threading
+
+    import torch
+    from solver_gb300 import _lib
+    L = _lib.load()
+    rng = np.random.default_rng(7)
+    jobs = []
+    for t in range(4):
+        N, k = 200_003 + 1_000 * t, 8 + 4 * t
+        U = rng.standard_normal((k, N)) + 1j * rng.standard_normal((k, N))
+        v = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+        got = torch.full((k,), complex("nan"), dtype=torch.complex128, device="cuda")
+        jobs.append((N, k, U, v, _dev(U), _dev(v), got, torch.cuda.Stream()))
+    torch.cuda.synchronize()
+    errors = []
+
+    def run(j):
+        N, k, U, v, dU, dv, got, s = jobs[j]
+        for _ in range(10):
+            rc = L.peec_multidot_noalloc(ctypes.c_void_p(dU.data_ptr()), N,
+                                         ctypes.c_void_p(dv.data_ptr()), N, k,
+                                         ctypes.c_void_p(got.data_ptr()),
+                                         ctypes.c_void_p(s.cuda_stream))
+            if rc != 0:
+                errors.append((j, rc, L.peec_last_error(None)))
+                return
+
+    threads = [threading.Thread(target=run, args=(j,)) for j in range(len(jobs))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors
+    torch.cuda.synchronize()
+    for N, k, U, v, dU, dv, got, s in jobs:
+        ref = np.conj(U) @ v
+        g = got.cpu().numpy()
+        assert np.max(np.abs(g - ref)) <= 1e-12 * max(np.max(np.abs(ref)), 1.0) * np.sqrt(N)
