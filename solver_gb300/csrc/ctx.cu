@@ -394,7 +394,13 @@ static int peec_set_topology_body(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t
   if (Nx < 1 || Ny < 1 || Nz < 1 || mx < 0 || my < 0 || mz < 0 || ns < 0 || n < 1)
     return bad(ctx, PEEC_ERR_BADARG, "peec_set_topology: invalid sizes");
   const int64_t m = mx + my + mz;
-  if (m + ns + n > INT32_MAX) return bad(ctx, PEEC_ERR_UNSUPPORTED, "problem too large for int32 indexing");
+  // device index lists are int32: unknowns, and the signed edge references 2e, 2e+1 of
+  // the node-edge lists. The axis bound keeps the int lattice arithmetic (2N + 1) exact;
+  // the circulant lengths are limited further by the twiddle table (below).
+  if (m + ns + n > INT32_MAX || 2 * m + 1 > INT32_MAX)
+    return bad(ctx, PEEC_ERR_UNSUPPORTED, "problem too large for int32 indexing");
+  if (Nx > (1 << 20) || Ny > (1 << 20) || Nz > (1 << 20))
+    return bad(ctx, PEEC_ERR_UNSUPPORTED, "grid axis longer than 2^20 cells");
   cudaSetDevice(ctx->dev);
   ctx->Nx = Nx; ctx->Ny = Ny; ctx->Nz = Nz;
   ctx->mx = mx; ctx->my = my; ctx->mz = mz; ctx->m = m; ctx->ns = ns; ctx->n = n;
