@@ -74,7 +74,8 @@ const char* peec_last_error(const peec_ctx* ctx);
  * The cross-family exp_P blocks are implied by this placement (their lattice rows
  * are fixed functions of the family cells), so they are not passed.
  * Limits (PEEC_ERR_UNSUPPORTED beyond them): m + ns + n and 2m + 1 fit in int32;
- * every circulant length (a power of two >= 2N + 1 on the face grid) is at most 8192.
+ * every circulant length (the power of two at or above about twice the lattice
+ * extent along its axis) is at most 8192, so no axis is longer than 4096 cells.
  */
 int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t mx, int64_t my, int64_t mz,
                       const int64_t* edge_cell, const int64_t* edge_n1, const int64_t* edge_n2,
