@@ -468,8 +468,24 @@ def parse_request(req: dict):
     origin = (o["origin_x"], o["origin_y"], o["origin_z"])
     MATERIALS = [material(el) for el in si["materials"]]
     names = list(mo["mesher_matrices"].keys())
-    grids = np.stack([np.asarray(mo["mesher_matrices"][k], dtype=bool) for k in names])
+    if not names:
+        raise ValueError("mesher_matrices holds no material grid")
+    arrs = [np.asarray(mo["mesher_matrices"][k], dtype=bool) for k in names]
+    shapes = {a.shape for a in arrs}
+    if len(shapes) != 1 or len(arrs[0].shape) != 3:
+        raise ValueError(f"material grids must share one 3-D shape, got {sorted(shapes)}")
+    grids = np.stack(arrs)
+    nc = mo.get("n_cells")
+    if nc is not None:
+        want = (int(nc["n_cells_x"]), int(nc["n_cells_y"]), int(nc["n_cells_z"]))
+        if grids.shape[1:] != want:
+            raise ValueError(f"material grids are {grids.shape[1:]}, n_cells says {want}")
+    if not grids.any():
+        raise ValueError("the material grids hold no occupied voxel")
     by_name = {mt["name"]: mt for mt in MATERIALS}
+    missing = [nm for nm in names if nm not in by_name]
+    if missing:
+        raise ValueError(f"mesher_matrices names {missing} that solverInput.materials lacks")
     dominant = [i for i, nm in enumerate(names) if by_name[nm]["sigmar"] > 0]
     ports = {"port_start": np.array([[v * escal for v in p["inputElement"]] for p in si["ports"]]).reshape(-1, 3),
              "port_end": np.array([[v * escal for v in p["outputElement"]] for p in si["ports"]]).reshape(-1, 3)}

@@ -155,3 +155,36 @@ def test_lanes_sweep_failure_in_one_lane_stops_the_others():
         lanes.close()
     solves = [e for e in log if e[1] == "solve"]
     assert len(solves) < len(seq)  # lane 1 did not run the whole sweep
+
+
+def test_request_parser_rejects_inconsistent_grids():
+    """Malformed solve requests fail with a message before the mesher runs: material grids
+    of different shapes, grids that disagree with n_cells, an empty geometry, and a grid
+    whose material is not listed."""
+    import copy
+
+    from solver_gb300 import configs, mesher
+    base = configs.crossbar_20x20x4()
+    mesher.parse_request(copy.deepcopy(base))  # the well-formed request parses
+
+    r = copy.deepcopy(base)
+    r["mesherOutput"]["n_cells"]["n_cells_x"] = 21
+    with pytest.raises(ValueError, match="n_cells"):
+        mesher.parse_request(r)
+
+    r = copy.deepcopy(base)
+    r["mesherOutput"]["mesher_matrices"]["copper"] = [
+        [[False] * 4 for _ in range(20)] for _ in range(20)]
+    with pytest.raises(ValueError, match="no occupied voxel"):
+        mesher.parse_request(r)
+
+    r = copy.deepcopy(base)
+    r["mesherOutput"]["mesher_matrices"]["air"] = [[[False] * 3 for _ in range(20)]
+                                                   for _ in range(20)]
+    with pytest.raises(ValueError, match="one 3-D shape"):
+        mesher.parse_request(r)
+
+    r = copy.deepcopy(base)
+    r["solverInput"]["materials"][0]["name"] = "gold"
+    with pytest.raises(ValueError, match="lacks"):
+        mesher.parse_request(r)
