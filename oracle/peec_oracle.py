@@ -485,23 +485,72 @@ def gmres_custom(b, restarted, tol, maxit, x, matvec, restart=None, stop=None):
 # ----------------------------------------------------------------------------------------
 
 def lumped_admittance(typ, R, L, C, w):
-    """get_lumped_elements_admittance_fft (build_Yle_FFT.jl:128-209)."""
+    """get_lumped_elements_admittance_fft (build_Yle_FFT.jl:128-209), statement by
+    statement; numpy scalars give Julia's IEEE results for divisions by zero."""
+    R, L, C = np.float64(R), np.float64(L), np.float64(C)
+    jw = np.complex128(1j * w)
+
+    def bad(v):
+        return np.isnan(v) or np.isinf(v) or abs(v) < 1e-16
+
     with np.errstate(all="ignore"):
-        def bad(y):
-            return (not np.isfinite(y)) or abs(y) < 1e-16
-        jw = 1j * w
-        c = complex
+        y = np.complex128(0.0)
         if typ == 1:
-            z = c(R + jw * L + (1 / (jw * C) if C != 0 else complex(np.inf)))
-            if (not np.isfinite(z)) or abs(z) < 1e-16:
-                z = c(R + jw * L)
-            y = 1 / z if z != 0 else complex(np.inf)
-        else:
-            # the remaining element types are not used by the configurations exercised here
-            raise NotImplementedError(f"lumped element type {typ}")
-        if not np.isfinite(y):
+            z = R + jw * L + 1 / (jw * C)
+            if np.isnan(z) or np.isinf(z) or abs(z) < 1e-16:
+                z = R + jw * L
+            y = 1 / z
+        elif typ == 2:
+            y = 1 / (R + jw * L) + jw * C
+            if bad(y):
+                y = 1 / R + jw * C
+            if bad(y):
+                y = 1 / (R + jw * L)
+            if bad(y):
+                y = 1 / R
+            if bad(y):
+                y = 1 / (jw * L) + jw * C
+            if bad(y):
+                y = jw * C
+        elif typ == 3:
+            y = 1 / (R + 1 / (jw * C)) + 1 / (jw * L)
+            if bad(y):
+                y = 1 / (R + 1 / (jw * C))
+            if bad(y):
+                y = 1 / R + 1 / (jw * L)
+            if bad(y):
+                y = 1 / R
+            if bad(y):
+                y = 1 / (1 / (jw * C)) + 1 / (jw * L)
+            if bad(y):
+                y = 1 / (jw * L)
+            if bad(y):
+                y = 1 / (1 / (jw * C))
+        elif typ == 4:
+            y = 1 / R + jw * C + 1 / (jw * L)
+            if bad(y):
+                y = 1 / R + jw * C
+            if bad(y):
+                y = jw * C + 1 / (jw * L)
+            if bad(y):
+                y = jw * C
+        elif typ == 5:
+            y = 1 / R + 1 / (jw * L + 1 / (jw * C))
+            if bad(y):
+                y = 1 / R + 1 / (1 / (jw * C))
+            if bad(y):
+                y = 1 / R + 1 / (jw * L)
+            if bad(y):
+                y = 1 / R
+            if bad(y):
+                y = 1 / (jw * L + 1 / (jw * C))
+            if bad(y):
+                y = 1 / (jw * L)
+            if bad(y):
+                y = 1 / (1 / (jw * C))
+        if np.isnan(y) or np.isinf(y):
             y = 0.0
-        return y
+        return complex(y)
 
 
 def build_Yle(lumped_elements, ports, escalings, n, w, z0):

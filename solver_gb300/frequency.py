@@ -31,16 +31,64 @@ def z_self(R, Cd, w):
     return Z
 
 
+def _bad(y):
+    return not np.isfinite(y) or abs(y) < 1e-16
+
+
+# Admittance of each lumped element type as a cascade of networks: the first is the
+# element itself; while the value is not finite or below 1e-16 in magnitude, the next
+# (a network with a vanishing R, L or C dropped) is taken (build_Yle_FFT.jl:128-209).
+# Types: 1 series R-L-C, 2 (R + L) parallel C, 3 (R + C) parallel L, 4 R | C | L in
+# parallel, 5 R parallel (L + C). Divisions by zero follow IEEE arithmetic, as in Julia.
+_CASCADES = {
+    2: (lambda R, L, C, jw: 1 / (R + jw * L) + jw * C,
+        lambda R, L, C, jw: 1 / R + jw * C,
+        lambda R, L, C, jw: 1 / (R + jw * L),
+        lambda R, L, C, jw: 1 / R,
+        lambda R, L, C, jw: 1 / (jw * L) + jw * C,
+        lambda R, L, C, jw: jw * C),
+    3: (lambda R, L, C, jw: 1 / (R + 1 / (jw * C)) + 1 / (jw * L),
+        lambda R, L, C, jw: 1 / (R + 1 / (jw * C)),
+        lambda R, L, C, jw: 1 / R + 1 / (jw * L),
+        lambda R, L, C, jw: 1 / R,
+        lambda R, L, C, jw: 1 / (1 / (jw * C)) + 1 / (jw * L),
+        lambda R, L, C, jw: 1 / (jw * L),
+        lambda R, L, C, jw: 1 / (1 / (jw * C))),
+    4: (lambda R, L, C, jw: 1 / R + jw * C + 1 / (jw * L),
+        lambda R, L, C, jw: 1 / R + jw * C,
+        lambda R, L, C, jw: jw * C + 1 / (jw * L),
+        lambda R, L, C, jw: jw * C),
+    5: (lambda R, L, C, jw: 1 / R + 1 / (jw * L + 1 / (jw * C)),
+        lambda R, L, C, jw: 1 / R + 1 / (1 / (jw * C)),
+        lambda R, L, C, jw: 1 / R + 1 / (jw * L),
+        lambda R, L, C, jw: 1 / R,
+        lambda R, L, C, jw: 1 / (jw * L + 1 / (jw * C)),
+        lambda R, L, C, jw: 1 / (jw * L),
+        lambda R, L, C, jw: 1 / (1 / (jw * C))),
+}
+
+
 def lumped_admittance(typ, R, L, C, w):
-    """Type-1 (series RLC) element admittance (build_Yle_FFT.jl:128-136)."""
-    if typ != 1:
-        raise NotImplementedError(f"lumped element type {typ} is not supported")
+    """Admittance of a lumped element of type 1..5 at angular frequency w
+    (build_Yle_FFT.jl:128-209); 0 where no network of the type is finite."""
+    R, L, C = np.float64(R), np.float64(L), np.float64(C)
+    jw = np.complex128(1j * w)
     with np.errstate(all="ignore"):
-        z = complex(R + 1j * w * L) + (1 / (1j * w * C) if C != 0 else complex("inf"))
-        if not np.isfinite(z) or abs(z) < 1e-16:
-            z = complex(R + 1j * w * L)
-        y = 1 / z if z != 0 else complex("inf")
-    return y if np.isfinite(y) else 0.0
+        if typ == 1:
+            z = R + jw * L + 1 / (jw * C)
+            if _bad(z):
+                z = R + jw * L
+            y = 1 / z
+        elif typ in _CASCADES:
+            steps = _CASCADES[typ]
+            y = steps[0](R, L, C, jw)
+            for step in steps[1:]:
+                if not _bad(y):
+                    break
+                y = step(R, L, C, jw)
+        else:
+            raise ValueError(f"lumped element type {typ} is not one of 1..5")
+    return complex(y) if np.isfinite(y) else 0.0
 
 
 def yle_matrix(lumped_elements, ports, n, w_real, z0, escal_yle):

@@ -270,3 +270,63 @@ def test_oracle_gmres_control_flow_known_answers():
     assert flag == 1 and list(it) == [1, 2]
     assert np.isclose(relres, np.min(rv) / np.linalg.norm(b), rtol=1e-8)
     assert np.isclose(np.linalg.norm(b - M @ x) / np.linalg.norm(b), relres, rtol=1e-8)
+
+
+def test_lumped_element_admittances():
+    """Lumped element types 1..5 (build_Yle_FFT.jl:128-209): the element network for
+    generic values, the reference's fallbacks when an element vanishes, and the product's
+    table-driven form against the oracle's statement-by-statement one on random corners."""
+    from solver_gb300.frequency import lumped_admittance as product
+    w = 2 * np.pi * 1.3e9
+    jw = 1j * w
+    R, L, C = 37.0, 2.2e-9, 0.8e-12
+    par = lambda *ys: sum(ys)   # admittances of parallel branches add
+    ser = lambda *zs: sum(zs)   # impedances of series elements add
+    want = {1: 1 / ser(R, jw * L, 1 / (jw * C)),
+            2: par(1 / ser(R, jw * L), jw * C),
+            3: par(1 / ser(R, 1 / (jw * C)), 1 / (jw * L)),
+            4: par(1 / R, jw * C, 1 / (jw * L)),
+            5: par(1 / R, 1 / ser(jw * L, 1 / (jw * C)))}
+    for t, y in want.items():
+        assert abs(O.lumped_admittance(t, R, L, C, w) - y) <= 1e-14 * abs(y), t
+    # a vanishing element is dropped from the network
+    assert O.lumped_admittance(1, R, L, 0.0, w) == pytest.approx(1 / (R + jw * L), rel=1e-14)
+    assert O.lumped_admittance(2, 0.0, 0.0, C, w) == pytest.approx(jw * C, rel=1e-14)
+    assert O.lumped_admittance(3, R, 0.0, C, w) == pytest.approx(1 / (R + 1 / (jw * C)), rel=1e-14)
+    assert O.lumped_admittance(4, R, 0.0, C, w) == pytest.approx(1 / R + jw * C, rel=1e-14)
+    assert O.lumped_admittance(4, 0.0, L, C, w) == pytest.approx(jw * C + 1 / (jw * L), rel=1e-14)
+    assert O.lumped_admittance(5, R, L, 0.0, w) == pytest.approx(1 / R + 1 / (jw * L), rel=1e-14)
+    assert O.lumped_admittance(5, 0.0, L, C, w) == pytest.approx(1 / (jw * L + 1 / (jw * C)), rel=1e-14)
+    # nothing finite left: 0
+    assert O.lumped_admittance(1, 0.0, 0.0, 0.0, w) == 0.0
+    assert O.lumped_admittance(4, 0.0, 0.0, 0.0, w) == 0.0
+    rng = np.random.default_rng(12)
+    for _ in range(400):
+        t = int(rng.integers(1, 6))
+        vals = [v if rng.random() < 0.7 else 0.0 for v in (rng.uniform(1e-3, 1e3),
+                                                            rng.uniform(1e-12, 1e-8),
+                                                            rng.uniform(1e-15, 1e-11))]
+        ww = 2 * np.pi * 10 ** rng.uniform(6, 10)
+        a, b = product(t, *vals, ww), O.lumped_admittance(t, *vals, ww)
+        assert a == b or abs(a - b) <= 1e-15 * abs(b), (t, vals, ww, a, b)
+    with pytest.raises(ValueError):
+        product(6, R, L, C, w)
+
+
+def test_yle_stamps_lumped_elements_and_ports():
+    """Yle (build_Yle_FFT.jl:1-126): each element's admittance y between its two nodes as
+    [[y, -y], [-y, y]], each port's 1/z0 the same way, all times the Yle scaling."""
+    from solver_gb300.frequency import lumped_admittance, yle_matrix
+    w = 2 * np.pi * 5e8
+    le = {"le_nodes": [[0, 3], [2, 3]], "type": [2, 5], "R_value": [10.0, 75.0],
+          "L_value": [1e-9, 3e-9], "C_value": [1e-12, 0.0]}
+    ports = {"port_nodes": [[1, 4]]}
+    Y = yle_matrix(le, ports, 5, w, 50.0, 2.5).toarray()
+    want = np.zeros((5, 5), complex)
+    for (a, b), y in (((0, 3), lumped_admittance(2, 10.0, 1e-9, 1e-12, w)),
+                      ((2, 3), lumped_admittance(5, 75.0, 3e-9, 0.0, w)), ((1, 4), 1 / 50.0)):
+        want[a, a] += y
+        want[b, b] += y
+        want[a, b] -= y
+        want[b, a] -= y
+    assert np.allclose(Y, 2.5 * want, rtol=1e-15, atol=0)
