@@ -20,6 +20,7 @@ import time
 import numpy as np
 
 from . import frequency as fq
+from .fill_cache import fill_operator
 from .operator import GpuOperator, row_dims
 
 _P_KEYS = {(0, 0): "p12_se", (1, 1): "p34_se", (2, 2): "p56_se", (0, 1): "p1234",
@@ -438,14 +439,15 @@ def dump_json_data(matrix_Z, matrix_S, matrix_Y, num_ports, id, partial=False, f
 
 
 def do_solving_fft(request, id="job", mode="mixed", lanes=1, device=0, stop_flag=None,
-                   records=None):
+                   records=None, row_cache=None):
     """A solve request end to end, as the reference's doSolvingFFT does it
     (do_solving_fft.jl:1-177) without its message queue and object store: the request
     body (mesherOutput / solverInput / solverAlgoParams / solverType) through the mesher,
     the GPU fill and the frequency x port sweep. Returns the reference's results
     dictionary (dump_json_data) plus "S", "Z", "Y" (ports x ports x frequencies) and
     "f"; None if stopped. mode "fp64" runs the reference algorithm, "mixed" the mixed
-    precision solves (lanes: port lanes, see FFT_solver_QS_S_type)."""
+    precision solves (lanes: port lanes, see FFT_solver_QS_S_type). row_cache: a
+    fill_cache.RowCache, to reuse the rows of an earlier fill of the same lattice."""
     from . import mesher
     solver_type = int(request.get("solverType", 1))
     if solver_type != 1:
@@ -454,7 +456,7 @@ def do_solving_fft(request, id="job", mode="mixed", lanes=1, device=0, stop_flag
     esc, inc, cc, diag, exp, ports, le, li, Zs = out
     op = GpuOperator(inc, exp, diag["P"], device=device)
     try:
-        op.fill(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"])
+        fill_operator(op, cc, esc, row_cache)
         exp["gpu_ctx"] = op
         h = CirculantSpectra(op)
         st = {"Inner_Iter": settings["Inner_Iter"],
@@ -472,11 +474,12 @@ def do_solving_fft(request, id="job", mode="mixed", lanes=1, device=0, stop_flag
     return outd
 
 
-def sweep_many(requests, mode="mixed", concurrency=4, device=0):
+def sweep_many(requests, mode="mixed", concurrency=4, device=0, row_cache=None):
     """Frequency sweeps of several geometries, concurrently: each geometry gets its own
     context (CUDA stream, fill, spectra, workspaces) and host thread, so the sweeps' kernels
     overlap on the GPU the way port lanes do. Per request: the mesher, the GPU fill, then
-    FFT_solver_QS_S_type in the given mode. Returns the results in request order."""
+    FFT_solver_QS_S_type in the given mode. Returns the results in request order.
+    row_cache: a fill_cache.RowCache; geometries on the same lattice then fill once."""
     from concurrent.futures import ThreadPoolExecutor
     from . import mesher
     from .operator import GpuOperator
@@ -486,7 +489,7 @@ def sweep_many(requests, mode="mixed", concurrency=4, device=0):
         esc, inc, cc, diag, exp, ports, le, li, Zs = out
         op = GpuOperator(inc, exp, diag["P"], device=device)
         try:
-            op.fill(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"])
+            fill_operator(op, cc, esc, row_cache)
             exp["gpu_ctx"] = op
             h = CirculantSpectra(op)
             st = {"Inner_Iter": settings["Inner_Iter"],
