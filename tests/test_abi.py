@@ -59,3 +59,38 @@ def test_entry_points_reject_a_null_context_with_their_own_name(cuda_lib):
         assert msg.startswith(name + ":"), (name, msg)
     assert L.peec_ctx_create(None, 0) == -5
     assert L.peec_last_error(None).decode().startswith("peec_ctx_create:")
+
+
+def test_header_is_plain_c_and_cpp(cuda_lib, tmp_path):
+    """include/peec_gb300.h compiles as strict C99 and C++17 with every warning an error,
+    and a C program resolves each declared function from the built library by name
+    (what a cgo, JNI or ccall binding does) and calls peec_version."""
+    import shutil
+    import subprocess
+    names = declared_symbols()
+    src = tmp_path / "use_abi.c"
+    lines = ['#include <dlfcn.h>', '#include <stdio.h>', '#include "peec_gb300.h"',
+             'int main(int argc, char** argv) {',
+             '  void* h = dlopen(argv[1], RTLD_NOW | RTLD_LOCAL);',
+             '  if (!h) { fprintf(stderr, "%s\\n", dlerror()); return 2; }']
+    for nm in names:
+        lines.append(f'  if (!dlsym(h, "{nm}")) {{ fprintf(stderr, "missing {nm}\\n"); return 3; }}')
+    lines += ['  int (*ver)(void);',
+              '  *(void**)(&ver) = dlsym(h, "peec_version");  /* the POSIX form */',
+              '  printf("%d\\n", ver());',
+              '  (void)argc; return 0;', '}']
+    src.write_text("\n".join(lines) + "\n")
+    inc = str(ROOT / "include")
+    gcc, gxx = shutil.which("gcc"), shutil.which("g++")
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", inc,
+                    "-D_DEFAULT_SOURCE", "-o", str(tmp_path / "use_abi"), str(src), "-ldl"],
+                   check=True)
+    hdr = tmp_path / "hdr.cpp"
+    hdr.write_text('#include "peec_gb300.h"\n'
+                   'int main() { int (*f)(void) = &peec_version; (void)f; return 0; }\n')
+    subprocess.run([gxx, "-std=c++17", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", inc,
+                    "-fsyntax-only", str(hdr)], check=True)
+    r = subprocess.run([str(tmp_path / "use_abi"), str(cuda_lib)], capture_output=True,
+                       text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    assert int(r.stdout.strip()) >= 100
