@@ -755,7 +755,7 @@ static int smem_optin(K kernel, size_t bytes) {
   static std::mutex mu;
   static std::set<std::pair<const void*, int>> done;
   if (bytes > 227 * 1024) {
-    set_error("shared memory tile exceeds 227 KB: grid too large for this build");
+    set_error("shared memory tile exceeds 227 KB: z extent too large for the z-pass tiles");
     return PEEC_ERR_UNSUPPORTED_INTERNAL;
   }
   int dev = 0;

@@ -1,7 +1,7 @@
 """CPU: the multi-rank path of the bench (replicas, one process per GPU) with two gloo
 ranks on the host. Each rank reports its own timed region; every rank gets the maximum
 over ranks, and the whole-job rate is the frequency points of all ranks over the slowest
-rank's time (the driver launches the same code with NCCL, one rank per GPU)."""
+rank's time (a multi-GPU launch runs the same code with NCCL, one rank per GPU)."""
 import json
 import os
 import socket
