@@ -152,3 +152,40 @@ def test_cached_state_is_keyed_by_the_objects_themselves(fake):
     op.set_rows(rows)                                            # other rows on the device
     api._ensure_spectra(op, FFTCP, FFTCLp)
     assert n_rows() == 3
+
+
+def test_library_error_codes_reach_the_caller(monkeypatch):
+    """A failing library call raises PeecError carrying the code and the library's message
+    (here a host allocation failure, PEEC_ERR_OOM, as the exception guard returns it); a
+    cancelled solve (PEEC_ERR_CANCELLED) comes back as the reference's flag 99."""
+    class Failing(FakeLib):
+        def __init__(self, codes):
+            super().__init__()
+            self.codes = codes
+
+        def peec_last_error(self, ctx):
+            return b"peec_set_topology: host memory allocation failed"
+
+        def peec_set_topology(self, *args):
+            return self.codes.get("peec_set_topology", 0)
+
+        def __getattr__(self, name):
+            if not name.startswith("peec_"):
+                raise AttributeError(name)
+            return lambda *a: self.codes.get(name, 0)
+
+    out, freqs, settings, z0, grid = mesher.parse_request(configs.crossbar_20x20x4())
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    L = Failing({"peec_set_topology": -2})
+    monkeypatch.setattr(_lib, "load", lambda *a, **k: L)
+    with pytest.raises(_lib.PeecError) as ei:
+        gop.GpuOperator(inc, exp, diag["P"])
+    assert ei.value.code == -2 and "allocation failed" in str(ei.value)
+    assert "PEEC_ERR_OOM" in str(ei.value)
+
+    L = Failing({"peec_gmres": -3, "peec_solve_mixed": -3})
+    monkeypatch.setattr(_lib, "load", lambda *a, **k: L)
+    op = gop.GpuOperator(inc, exp, diag["P"])
+    b = np.ones(op.N)
+    assert op.gmres(b, None, 1e-8, 10)[1] == 99
+    assert op.solve_mixed(b, None, 1e-8)[1] == 99
