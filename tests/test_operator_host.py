@@ -189,3 +189,26 @@ def test_library_error_codes_reach_the_caller(monkeypatch):
     b = np.ones(op.N)
     assert op.gmres(b, None, 1e-8, 10)[1] == 99
     assert op.solve_mixed(b, None, 1e-8)[1] == 99
+
+
+def test_single_layer_grid(fake):
+    """A planar trace (Nz = 1): the z edge family is empty (mz = 0, no Lpz row), the host
+    wrapper passes a consistent topology, and the oracle solves the port to flag 0 with an
+    inductive impedance (a copper strip at 1 GHz)."""
+    cu = np.zeros((16, 8, 1), bool)
+    cu[1:15, 3:5, 0] = True
+    req = configs.make_request({"copper": cu}, [dict(configs.COPPER)], (1e-4,) * 3,
+                               [((1, 3, 0), (14, 4, 0))], [1e9], 1e-8)
+    out, freqs, settings, z0, grid = mesher.parse_request(req)
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    assert grid == (16, 8, 1) and int(inc["mz"]) == 0
+    op = gop.GpuOperator(inc, exp, diag["P"])
+    (t,) = fake.calls["peec_set_topology"]
+    assert t["grid"] == (16, 8, 1) and t["m"] == int(inc["mx"]) + int(inc["my"])
+    rows = O.fill_rows(cc, esc, *grid)
+    assert "Lpz" not in rows or np.asarray(rows["Lpz"]).size == 0
+    FFTCP, FFTCLp = O.spectra_from_rows(rows, *grid)
+    res = O.FFT_solver_QS_S_type(freqs, esc, inc, FFTCP, FFTCLp, diag, ports, z0, le, exp,
+                                 {"Inner_Iter": 100, "tol": np.full(1, 1e-8)}, Zs)
+    Z = res["Z"][0, 0, 0]
+    assert np.isfinite(Z) and Z.real > 0 and Z.imag > 0
