@@ -3,6 +3,10 @@
  * Lp / P generating-row fill, used by tests/ and bench.py's cpu_baseline leg as
  * the checker; never linked into the product.
  *
+ * Parity unpinned: the reference (Julia) cannot run here and ships no outputs for
+ * this path; the rows are held to closed forms (coincident-cell self terms, the
+ * far-field point limit) by tests/test_oracle_known_answers.py.
+ *
  * Built twice by oracle/build.py: REAL=double (suffix _d) and REAL=long double
  * (suffix _ld); the long double build is the high-precision evaluation of the
  * same formulas the fill parity tests measure both CPU and GPU rows against.

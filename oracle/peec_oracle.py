@@ -11,10 +11,12 @@ Third-party arithmetic the reference relies on is replaced by: numpy.fft (pocket
 for FFTW, scipy.sparse.linalg.splu (SuperLU) for UMFPACK. Both return the same
 mathematical quantities; only rounding differs.
 
-Parity status: the reference ships no tests or golden vectors for this path and no
-Julia runtime is available, so this restatement is unpinned against the reference's
-own outputs; it is pinned against analytic checks (dense-operator products, closed
-forms) in tests/test_oracle.py.
+Parity status: parity unpinned. The reference ships no tests or golden vectors for this
+path and no Julia runtime is available, so this restatement cannot be checked against the
+reference's own outputs. It is held to known answers instead (closed-form self and
+far-field integrals, reciprocity, GMRES on known systems, a dense solve of the assembled
+operator, the lumped element networks) in tests/test_oracle_known_answers.py, and to its
+committed regression fixtures on the reference's own request files (tests/golden/).
 """
 from __future__ import annotations
 
