@@ -47,8 +47,10 @@ def main():
         shutil.copyfile(ref / name, HERE / name)
     # the 57x57x13 crossbar request (2 ports, 7 lumped elements, thin cells whose rows
     # reach the far-field fill branches), gzip-compressed: its voxel grid is 1.4 MB of JSON
+    # (no name and mtime 0 in the gzip header, so regenerating gives the same bytes)
     import gzip
-    with open(ref / "crossbar.json", "rb") as src, gzip.open(HERE / "crossbar.json.gz", "wb") as dst:
+    with open(ref / "crossbar.json", "rb") as src, open(HERE / "crossbar.json.gz", "wb") as raw, \
+            gzip.GzipFile(filename="", mode="wb", fileobj=raw, mtime=0) as dst:
         shutil.copyfileobj(src, dst)
     oracle_case(mesher.load_request(HERE / "first_run_data.json"), "first_run_data")
     # the two-material fixture at 1 GHz and 3 GHz: its face rows reach the far-field
