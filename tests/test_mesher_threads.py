@@ -1,7 +1,6 @@
 """CPU: the native mesher's output does not depend on its thread count. Its loops run
 in parallel (OpenMP), and every numbered sequence (edges, surfaces, nodes) is assembled in
 the reference's loop order, so one thread and several threads give the same arrays."""
-import hashlib
 import json
 import os
 import subprocess
