@@ -67,6 +67,9 @@ def parse():
                     help="run the adjoint-gradient configuration instead")
     ap.add_argument("--batched-sweep", action="store_true",
                     help="run the batched multi-geometry sweep configuration instead")
+    ap.add_argument("--reuse-fills", action="store_true",
+                    help="batched sweep: geometries on the same lattice share one fill "
+                         "(fill_cache.RowCache)")
     ap.add_argument("--small-configs", action="store_true",
                     help="the crossbar 20x20x4 configurations (FP64 plain and mixed per "
                          "frequency), one JSON line")
@@ -507,14 +510,18 @@ def run_batched_sweep(args):
     64 frequencies each, one port, mixed precision to 1e-8, geometries swept concurrently
     (one context and host thread each). Prints one JSON line with the throughput."""
     from solver_gb300 import api, configs
+    from solver_gb300.fill_cache import RowCache
     reqs = configs.batched_sweep()
+    cache = RowCache() if args.reuse_fills else None
     t = time.perf_counter()
-    res = api.sweep_many(reqs, mode="mixed", concurrency=args.lanes)
+    res = api.sweep_many(reqs, mode="mixed", concurrency=args.lanes, row_cache=cache)
     dt = time.perf_counter() - t
     systems = sum(len(r["info"]) for r in res)
     print(json.dumps({"metric": "batched sweep: port solves/s (12 grids x 64 frequencies, 1e-8)",
                       "value": systems / dt, "unit": "port solves/s", "systems": systems,
                       "wall_s": dt, "concurrency": args.lanes,
+                      "fills": None if cache is None else {"filled": cache.misses,
+                                                           "reused": cache.hits},
                       "flags": sorted({r["flag"] for x in res for r in x["info"]}),
                       "max_relres": max(r["relres"] for x in res for r in x["info"]),
                       "inner_iters_mean": float(np.mean([r["niter"] for x in res
