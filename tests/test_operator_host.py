@@ -212,3 +212,22 @@ def test_single_layer_grid(fake):
                                  {"Inner_Iter": 100, "tol": np.full(1, 1e-8)}, Zs)
     Z = res["Z"][0, 0, 0]
     assert np.isfinite(Z) and Z.real > 0 and Z.imag > 0
+
+
+@pytest.mark.parametrize("shape,seed", [((9, 7, 5), 3), ((6, 2, 5), 4), ((8, 6, 1), 5)])
+def test_rows_recovered_from_reference_spectra(shape, seed):
+    """The drop-in API accepts the reference's own spectra (FFTCP / FFTCLp at the 2N
+    extents, store_circulant_fft) and recovers the generating rows on the host; the
+    recovered rows equal the rows the spectra were built from."""
+    from solver_gb300 import api
+    out, freqs, settings, z0, grid = mesher.parse_request(
+        configs.random_copper(shape, p=0.5, seed=seed))
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    rows = O.fill_rows(cc, esc, *grid)
+    FFTCP, FFTCLp = O.spectra_from_rows(rows, *grid)
+    got = api.rows_from_reference_spectra(FFTCP, FFTCLp, grid)
+    for k, v in rows.items():
+        v = np.asarray(v).ravel()
+        if v.size == 0:
+            continue
+        assert np.max(np.abs(got[k] - v)) <= 1e-12 * np.max(np.abs(v)), k
