@@ -231,3 +231,43 @@ def test_rows_recovered_from_reference_spectra(shape, seed):
         if v.size == 0:
             continue
         assert np.max(np.abs(got[k] - v)) <= 1e-12 * np.max(np.abs(v)), k
+
+
+def _fixture_requests():
+    import gzip
+    import json
+    from pathlib import Path
+    G = Path(__file__).resolve().parent / "golden"
+    r2 = mesher.load_request(G / "first_run_data_2_materials.json")
+    r2["solverInput"]["frequencies"] = [1e9, 3e9]
+    return {"first_run_data": mesher.load_request(G / "first_run_data.json"),
+            "first_run_data_2_materials": r2,
+            "crossbar_57x57x13": json.loads(gzip.open(G / "crossbar.json.gz").read()),
+            "crossbar_20x20x4": configs.crossbar_20x20x4()}
+
+
+@pytest.mark.parametrize("name", ["first_run_data", "first_run_data_2_materials",
+                                  "crossbar_57x57x13", "crossbar_20x20x4"])
+def test_product_frequency_state_matches_the_oracle(name):
+    """The product's per-frequency host state (frequency.FrequencyState: edge impedances
+    with the surface-impedance switch, lumped and port admittances, SS) equals the
+    oracle's restatement of FFT_solver_QS_S_type.jl:102-119 at every frequency of the
+    reference's fixtures, and the product's S-to-Z/Y conversions equal the oracle's."""
+    from solver_gb300 import api
+    from solver_gb300 import frequency as fq
+    out, freqs, settings, z0, grid = mesher.parse_request(_fixture_requests()[name])
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    for f in freqs:
+        w = 2 * np.pi * f * esc["freq"]
+        st = fq.FrequencyState(w, esc, inc, diag, Zs, le, ports, z0)
+        fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
+        assert np.max(np.abs(st.DZ - fs["DZ"])) <= 1e-15 * np.max(np.abs(fs["DZ"]))
+        assert abs(st.Yle - fs["Yle"]).max() <= 1e-15 * max(abs(fs["Yle"]).max(), 1e-300)
+        SSo = (fs["Yle"] + inc["A"].T @ (fs["invZ"] @ inc["A"])
+               + 1j * w * ((inc["Gamma"] @ fs["invP"]) @ inc["Gamma"].T))
+        assert abs(st.SS - SSo).max() <= 1e-14 * abs(SSo).max()
+    rng = np.random.default_rng(8)
+    S = 0.3 * (rng.standard_normal((3, 3, 4)) + 1j * rng.standard_normal((3, 3, 4)))
+    S = 0.5 * (S + S.transpose(1, 0, 2))
+    assert np.allclose(api.s2z_fft(S, 50.0), O.s2z(S, 50.0), rtol=1e-13, atol=0)
+    assert np.allclose(api.s2y_fft(S, 50.0), O.s2y(S, 50.0), rtol=1e-13, atol=0)
