@@ -253,14 +253,21 @@ int peec_multidot(peec_ctx* ctx, const void* U, int64_t ldu, const void* v, int6
  * No context; U, v, out are device pointers to complex doubles on the current
  * device; `stream` is a cudaStream_t (NULL = legacy default stream); returns after
  * `out` holds the result.
- * Scratch: a fixed file-scope device array of PEEC_NOALLOC_MAX_K x 1216 complex
- * doubles (4.98 MB), resident on every GPU that loads the library until the
+ * Scratch: a fixed file-scope device array of PEEC_NOALLOC_MAX_K x 304 complex
+ * doubles (1.25 MB), resident on every GPU that loads the library until the
  * process exits. k > PEEC_NOALLOC_MAX_K is rejected with PEEC_ERR_BADARG; any N
- * is accepted. The first call on a device looks up the array's device address
- * (one-time set-up). The call synchronises its stream, so it cannot be captured
- * into a CUDA graph. All calls on a device share the array and take it in turn:
- * a per-device lock is held from launch to completion, so calls from several
- * threads or streams are serialised. Calls no cudaMalloc/cudaFree.
+ * is accepted. Set-up: the first call in each CUDA context of a device looks up
+ * the array's device address; under lazy module loading that first call also
+ * loads the library's device code onto the device, which is when the runtime
+ * places the array (1.25 MB, possibly with a synchronisation). A caller whose
+ * pool later takes all device memory should make one small call first, and that
+ * first call should come before any stream capture. A failure there returns
+ * PEEC_ERR_OOM or PEEC_ERR_CUDA with a message. After a device reset the next
+ * call looks the address up again. The call synchronises its stream before it
+ * returns. All calls on a device share the array and take it in turn: a
+ * per-device lock is held from launch to completion, so calls from several
+ * threads or streams are serialised rather than racing on the array. Calls no
+ * cudaMalloc/cudaFree and no allocating library routine.
  */
 #define PEEC_NOALLOC_MAX_K 256
 int peec_multidot_noalloc(const void* U, int64_t ldu, const void* v, int64_t N, int k,

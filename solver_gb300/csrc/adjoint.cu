@@ -1,7 +1,8 @@
 // Reciprocity gradient of a port voltage in per-voxel parameters (peec_adjoint): a
 // scatter of the edge-current squares weighted by the edge-impedance derivatives onto
 // the voxels of each edge. One thread per edge, double atomics per voxel (an edge joins
-// two voxels; a voxel has at most six edges per direction pair).
+// two voxels; a voxel has at most six edges per direction pair). The atomics make the
+// order of each voxel's sum vary between runs: results agree to a few ulps, not bitwise.
 #include "ctx.hpp"
 
 namespace peec {

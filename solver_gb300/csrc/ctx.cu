@@ -198,6 +198,22 @@ static void drop_graphs(peec_ctx* ctx) {
   ctx->graphs.clear();
 }
 
+// Entry points make the context's device current for their work; this puts the
+// caller's current device back on return, so a caller mixing contexts of several
+// devices with its own device-current work is not switched underneath.
+struct DeviceRestore {
+  int dev = -1;
+  DeviceRestore() noexcept {
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+      dev = -1;
+      cudaGetLastError();
+    }
+  }
+  ~DeviceRestore() {
+    if (dev >= 0) cudaSetDevice(dev);
+  }
+};
+
 #define CTX_TRY(expr)                 \
   do {                                \
     int _rc = (expr);                 \
@@ -321,6 +337,7 @@ static void free_tri(LevelTri& t) {
 
 extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   if (!ctx) return;
+  DeviceRestore restore_device_;
   cudaSetDevice(ctx->dev);
   if (ctx->st) cudaStreamSynchronize(ctx->st);
   drop_graphs(ctx);
@@ -401,7 +418,7 @@ static int peec_set_topology_body(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t
     return bad(ctx, PEEC_ERR_UNSUPPORTED, "problem too large for int32 indexing");
   if (Nx > (1 << 20) || Ny > (1 << 20) || Nz > (1 << 20))
     return bad(ctx, PEEC_ERR_UNSUPPORTED, "grid axis longer than 2^20 cells");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   ctx->Nx = Nx; ctx->Ny = Ny; ctx->Nz = Nz;
   ctx->mx = mx; ctx->my = my; ctx->mz = mz; ctx->m = m; ctx->ns = ns; ctx->n = n;
   ctx->N = m + ns + n;
@@ -583,7 +600,7 @@ static int peec_set_rows_body(peec_ctx* ctx, const double* const rows[9]) {
   NvtxRange nvtx_range_("peec_set_rows");
   if (!ctx || !rows) return badarg("peec_set_rows");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   double* d_rows[9] = {};
   int rc = PEEC_OK;
   for (int i = 0; i < 9 && rc == PEEC_OK; ++i) {
@@ -607,7 +624,7 @@ static int peec_fill_body(peec_ctx* ctx, const double origin[3], double sx, doub
   NvtxRange nvtx_range_("peec_fill");
   if (!ctx || !origin) return badarg("peec_fill");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   double* d_rows[9] = {};
   int64_t len[9];
   int rc = PEEC_OK;
@@ -833,7 +850,7 @@ static int peec_set_frequency_body(peec_ctx* ctx, double w, const double* DZ, in
   drop_graphs(ctx);
   if (!ctx || !DZ || !L_ptr || !U_ptr || !perm_r || !perm_c) return badarg("peec_set_frequency");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   const int64_t n = ctx->n, m = ctx->m;
   ctx->w = w;
   std::vector<c64> dz(m);
@@ -1007,7 +1024,7 @@ static int peec_matvec_dev_body(peec_ctx* ctx, const void* x, void* y, int preci
   NvtxRange nvtx_range_("peec_matvec_dev");
   if (!ctx || !x || !y) return badarg("peec_matvec_dev");
   if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   CTX_TRY(matvec_dev(ctx, (const c64*)x, (c64*)y, precision, true));
   PEEC_CUDA_TRY(cudaEventSynchronize(ctx->ev[2]));
   cudaEventElapsedTime(&ctx->t_total, ctx->ev[0], ctx->ev[2]);
@@ -1021,7 +1038,7 @@ static int peec_matvec_body(peec_ctx* ctx, const double* x, double* y, int preci
   NvtxRange nvtx_range_("peec_matvec");
   if (!ctx || !x || !y) return badarg("peec_matvec");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   const size_t bytes = sizeof(c64) * ctx->N;
   PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->dx, x, bytes, cudaMemcpyHostToDevice, ctx->st));
   CTX_TRY(peec_matvec_dev(ctx, ctx->dx, ctx->dy, precision));
@@ -1050,7 +1067,7 @@ extern "C" int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* dims, int
 static int peec_profile_matvec_body(peec_ctx* ctx, int precision, int iters, double* ms) {
   if (!ctx || !ms || iters < 1) return badarg("peec_profile_matvec");
   if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   if (ctx->pev.size() != 6) {
     for (auto e : ctx->pev) cudaEventDestroy(e);
     ctx->pev.assign(6, nullptr);
@@ -1088,7 +1105,7 @@ static int peec_multidot_body(peec_ctx* ctx, const void* U, int64_t ldu, const v
                              int k, void* out) {
   if (!ctx || !U || !v || !out || N < 1 || k < 1 || ldu < N)
     return PEEC_ERR_BADARG;
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   const size_t need = (size_t)red_blocks((size_t)N) * (size_t)k;
   if (ctx->mdcap < need) {
     if (ctx->mdpart) cudaFree(ctx->mdpart);
@@ -1117,7 +1134,7 @@ static int peec_port_rhs_body(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, 
   if (!ctx || !tn) return badarg("peec_port_rhs");
   if (!ctx->have_freq || !ctx->have_pdiag) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
   if (n1 < 0 || n1 >= ctx->n || n2 < 0 || n2 >= ctx->n) return bad(ctx, PEEC_ERR_BADARG, "port node out of range");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   const int64_t m = ctx->m, ns = ctx->ns, n = ctx->n;
   std::vector<c64> is(n, mk<double>(0, 0));
   is[n1] = mk<double>(Is, 0);
@@ -1137,7 +1154,7 @@ static int peec_port_rhs_body(peec_ctx* ctx, int64_t n1, int64_t n2, double Is, 
 
 static int peec_check_wait_limit_body(peec_ctx* ctx) {
   if (!ctx) return badarg("peec_check_wait_limit");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   int e = 0;
   const int rc = selftest_wait_limit(1 << 16, ctx->st, &e);
   if (rc) return ctx->err = g_err, rc;
@@ -1153,7 +1170,7 @@ static int peec_adjoint_body(peec_ctx* ctx, const double* x, const int32_t* v1,
   if (!ctx || !x || !v1 || !v2 || !d1 || !d2 || !g || nvox < 0 || Is == 0)
     return badarg("peec_adjoint");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   const int64_t m = ctx->m;
   int32_t *dv1 = nullptr, *dv2 = nullptr;
   c64 *dd1 = nullptr, *dd2 = nullptr;
@@ -1649,7 +1666,7 @@ static int peec_gmres_body(peec_ctx* ctx, const double* b, double* x_inout, doub
   if (maxit < 1 || (restarted && restart < 1)) return bad(ctx, PEEC_ERR_BADARG, "maxit/restart must be >= 1");
   if (precision < 0 || precision > 2) return bad(ctx, PEEC_ERR_BADARG, "precision must be 0, 1 or 2");
   if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   const size_t bytes = sizeof(c64) * ctx->N;
   PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->dx, b, bytes, cudaMemcpyHostToDevice, ctx->st));
   PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->dy, x_inout, bytes, cudaMemcpyHostToDevice, ctx->st));
@@ -1674,7 +1691,7 @@ static int peec_solve_mixed_body(peec_ctx* ctx, const double* b, double* x_inout
   NvtxRange nvtx_range_("peec_solve_mixed");
   if (!ctx || !b || !x_inout || !flag || !relres) return badarg("peec_solve_mixed");
   if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "frequency state not set");
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   const size_t N = ctx->N, bytes = sizeof(c64) * N;
   c64 *db = ctx->ir_b, *dxv = ctx->ir_x, *dr = ctx->ir_r, *dd = ctx->ir_d;
   auto cleanup = [&]() {};
@@ -1779,7 +1796,7 @@ static int peec_set_lu_component_max_body(peec_ctx* ctx, int max_rows) {
   if (!ctx) return badarg("peec_set_lu_component_max");
   if (max_rows < 0 || max_rows > SF_COMP_MAX)
     return bad(ctx, PEEC_ERR_BADARG, "component size limit outside 0.." + std::to_string(SF_COMP_MAX));
-  cudaSetDevice(ctx->dev);
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   drop_graphs(ctx);
   ctx->comp_max = max_rows;
   if (ctx->have_freq) CTX_TRY(build_solve_plan(ctx, ctx->n));
@@ -1803,6 +1820,7 @@ static void record_exception(peec_ctx* ctx, const char* fn, const char* what) no
 
 template <typename F>
 static int guarded(peec_ctx* ctx, const char* fn, F&& body) noexcept {
+  DeviceRestore restore_device_;
   try {
     return body();
   } catch (const std::bad_alloc&) {

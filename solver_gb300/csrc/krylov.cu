@@ -423,19 +423,59 @@ void launch_xupdate(const c64* x, const cff* U, size_t ldu, const c64* coef, con
 // synchronisation of cudaMalloc/cudaFree is not acceptable. For them the partial
 // sums live in a fixed file-scope device array instead of caller- or
 // context-owned scratch. It holds NOALLOC_BLOCKS x PEEC_NOALLOC_MAX_K complex
-// doubles (4.98 MB) and stays resident on every GPU that loads this library until
+// doubles (1.25 MB) and stays resident on every GPU that loads this library until
 // the process exits.
 // ------------------------------------------------------------------------------------
 
-constexpr int NOALLOC_BLOCKS = 152 * 8;  // >= the grid cap of the multi-dot launcher
+constexpr int NOALLOC_BLOCKS = MD_BLOCKS_MAX;  // the multi-dot launcher's grid cap
 static_assert(NOALLOC_BLOCKS >= MD_BLOCKS_MAX, "scratch smaller than the multi-dot grid");
 static __device__ __align__(256) c64 g_noalloc_partials[(size_t)NOALLOC_BLOCKS * PEEC_NOALLOC_MAX_K];
 
+// The array's device address belongs to the CUDA context that loaded this module. A
+// cudaDeviceReset or a re-created primary context reloads the module and may move the
+// array, so the looked-up address is cached per device together with the unique id of
+// the context it was looked up in, and looked up again when the current context differs.
+// The two driver calls are reached through the runtime, so the library needs no link
+// against libcuda.
+struct NoallocSlot {
+  unsigned long long ctx_id = 0;
+  void* addr = nullptr;
+};
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_addr[256] = {};  // device address of the array, per device ordinal
+static NoallocSlot g_noalloc_slot[256];
 // held from launch to completion: calls on one device (any thread, any stream) take
 // the shared array in turn
 static std::mutex g_noalloc_run_mu[256];
+
+typedef int (*drv_ctx_get_current_t)(void** ctx);
+typedef int (*drv_ctx_get_id_t)(void* ctx, unsigned long long* id);
+static std::once_flag g_drv_once;
+static drv_ctx_get_current_t g_ctx_get_current = nullptr;
+static drv_ctx_get_id_t g_ctx_get_id = nullptr;
+
+static void resolve_driver_calls() {
+  void* f = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess && q == cudaDriverEntryPointSuccess)
+    g_ctx_get_current = (drv_ctx_get_current_t)f;
+  f = nullptr;
+  if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess && q == cudaDriverEntryPointSuccess)
+    g_ctx_get_id = (drv_ctx_get_id_t)f;
+  cudaGetLastError();
+}
+
+// the unique id of the calling thread's current context; 0 when it cannot be told
+static unsigned long long current_context_id() {
+  std::call_once(g_drv_once, resolve_driver_calls);
+  if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+  void* c = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&c) != 0 || !c) return 0;
+  if (g_ctx_get_id(c, &id) != 0) return 0;
+  return id;
+}
 
 }  // namespace peec
 
@@ -460,15 +500,27 @@ extern "C" int peec_multidot_noalloc(const void* U, int64_t ldu, const void* v, 
   }
   void* scratch = nullptr;
   {
-    // one-time set-up per device, with that device current: the host-side name of
-    // the array is not a device address, so ask the runtime for it
+    // set-up once per device and context, with that device current: the host-side
+    // name of the array is not a device address, so ask the runtime for it. The first
+    // lookup in a context loads this module there, which places the array.
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
+    NoallocSlot& slot = g_noalloc_slot[dev];
+    unsigned long long id = current_context_id();
+    if (!slot.addr || id == 0 || slot.ctx_id != id) {
       void* p = nullptr;
-      PEEC_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_partials));
-      g_noalloc_addr[dev] = p;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error(std::string("peec_multidot_noalloc: could not place the fixed scratch on "
+                              "device ") + std::to_string(dev) + " (" + cudaGetErrorString(e) +
+                  "); the first call on a device loads the library's device code there");
+        return e == cudaErrorMemoryAllocation ? PEEC_ERR_OOM : PEEC_ERR_CUDA;
+      }
+      if (id == 0) id = current_context_id();  // the lookup made the primary context current
+      slot.addr = p;
+      slot.ctx_id = id;
     }
-    scratch = g_noalloc_addr[dev];
+    scratch = slot.addr;
   }
   cudaStream_t st = (cudaStream_t)stream;
   std::lock_guard<std::mutex> run(g_noalloc_run_mu[dev]);
