@@ -46,12 +46,6 @@ METRIC = "freq-point solves/s at 1e-8 residual, mixed vs FP64 plain on 1 GB300; 
 UNIT = "freq-point solves/s"
 WORKLOAD = ("random_128x128x64: 5e-5 m voxels, Bernoulli(0.3) occupancy (seed 2), Cu/dielectric "
             "50/50, 4 ports, 10 freqs 10 MHz-10 GHz, tol 1e-8")
-# average FP64 operator applications per port solve of the reference algorithm on this
-# workload's warm-started frequency sequence: GMRES takes 12-23 iterations per port (mean
-# 17.3 over the 28 port solves of 7 points, measured by the FP64 leg of this script on a
-# GB300), plus the initial residual and the final true-residual check. Used only by
-# --impl reference, which has no GPU run to count them; the GPU arm counts its own.
-REF_MATVECS_PER_PORT = 19.3
 
 
 def parse():
@@ -83,8 +77,10 @@ def parse():
     ap.add_argument("--inner-tol", type=float, default=1e-7,
                     help="floor of the inner FP32 GMRES relative tolerance")
     ap.add_argument("--profile-iters", type=int, default=20)
+    ap.add_argument("--ref-budget", type=float, default=150.0,
+                    help="reference arm: seconds of port solves after which no new solve starts")
     ap.add_argument("--grid", type=int, nargs=3, default=None,
-                    help="smaller random Cu/dielectric grid (profiling captures only)")
+                    help="smaller random Cu/dielectric grid (profiling captures and tests only)")
     return ap.parse_args()
 
 
@@ -211,17 +207,13 @@ def conv_gbs(b, prof):
 
 
 def z_traffic(grid):
-    """DRAM bytes (read + write) of one operator application's FP32 z passes from the
-    committed ncu summary of the 128x128x64 workload; None for other grids."""
-    if tuple(grid) != (128, 128, 64):
-        return None
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
-                        "z_traffic_random_128x128x64.md")
+    """DRAM bytes (read + write) of one operator application's FP32 z passes, as captured
+    by ncu on this grid and recorded in profiles/dram_traffic.json; None when no capture
+    of this grid is recorded."""
     try:
-        import re
-        m = re.search(r"traffic_bytes_per_matvec:\s*(\d+)", open(path).read())
-        return int(m.group(1)) if m else None
-    except OSError:
+        d = json.loads((ROOT / "profiles" / "dram_traffic.json").read_text())
+        return d["z_passes_fp32"].get("x".join(str(int(g)) for g in grid))
+    except (OSError, ValueError, KeyError):
         return None
 
 
@@ -253,14 +245,20 @@ def setup_problem(device=0, grid=None):
 
 def fill_report(P, with_cpu):
     """Fill throughput: row entries per second of the GPU fill (rows and spectra), and of
-    the oracle's C fill with OpenMP on every host core (the cpu_baseline leg)."""
+    the oracle's C fill with OpenMP on every host core (the cpu_baseline leg, on the
+    oracle mesher's lattice centres; its rows are kept for the CPU solve sample)."""
     entries = int(sum(np.asarray(r).size for r in P["rows"].values()))
     out = {"entries": entries, "gpu_ms": P["fill_s"] * 1e3,
            "gpu_entries_per_s": entries / P["fill_s"]}
     if with_cpu:
+        from oracle import mesher_ref as OM
         from oracle import peec_oracle as O
         t = time.perf_counter()
-        O.fill_rows(P["cc"], P["esc"], *P["grid"])
+        P["oracle"] = OM.parse_request(P["req"])
+        out["cpu_mesh_ms"] = (time.perf_counter() - t) * 1e3
+        (esc, inc, cc, *_r), _f, _s, _z, grid = P["oracle"]
+        t = time.perf_counter()
+        P["oracle_rows"] = O.fill_rows(cc, esc, *grid)
         cpu_s = time.perf_counter() - t
         out.update(cpu_ms=cpu_s * 1e3, cpu_entries_per_s=entries / cpu_s,
                    cpu_cores=os.cpu_count() or 1, cpu_kind="port")
@@ -361,31 +359,71 @@ def solve_point(P, fs, Vrest, mode, tol):
     return S, work, _point_bytes(P, fs, npt), npt * 2 * N * 16
 
 
-def cpu_baseline(P, mv_per_port, sample_note):
-    """The CPU oracle on the host cores: one operator application at the reference's
-    2N extents (scipy.fft with all cores) and one SuperLU factorisation."""
+def oracle_port_solves(O, problem, rows, grid, freqs, budget_s, max_solves, tol):
+    """Complete port solves of the CPU oracle in the reference's order
+    (FFT_solver_QS_S_type.jl:102-208): frequency by frequency, per frequency the SuperLU
+    factorisation of SS, then per port its right-hand side (precond_3_3_Kt_fft!) and a
+    Householder GMRES solve with its reflectors, warm started from the previous
+    frequency's solution of that port. Every operator application runs at the
+    reference's 2N extents. Stops after max_solves port solves or once budget_s has
+    passed at the end of a solve. Returns the per-solve records and the elapsed time,
+    which covers everything from the first factorisation to the last solve."""
+    esc, inc, cc, diag, exp, ports, le, Zs, z0, settings = problem
+    FFTCP, FFTCLp = O.spectra_from_rows(rows, *grid)
+    A, Gamma = inc["A"], inc["Gamma"]
+    m, n = A.shape
+    ns = Gamma.shape[1]
+    pn = np.asarray(ports["port_nodes"], dtype=np.int64)
+    npt = pn.shape[0]
+    Vrest = np.zeros((m + ns + n, npt), dtype=np.complex128)
+    recs = []
+    t0 = time.perf_counter()
+    for f in freqs:
+        w = 2 * np.pi * f * esc["freq"]
+        tf = time.perf_counter()
+        fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
+        t_lu = time.perf_counter() - tf
+        mv = lambda x, fs=fs, w=w: O.ComputeMatrixVectorFTT(
+            x, w, inc, FFTCP, FFTCLp, fs["DZ"], fs["Yle"], exp, fs["invZ"], fs["invP"], fs["F"])
+        for c1 in range(npt):
+            tp = time.perf_counter()
+            is_ = np.zeros(n)
+            is_[pn[c1, 0]] = esc["Is"]
+            is_[pn[c1, 1]] = -esc["Is"]
+            tn = O.precond_3_3_Kt_fft(fs["F"], fs["invZ"], fs["invP"], A, Gamma, m, ns, is_)
+            V, flag, relres, it, rv = O.gmres_custom(tn, False, tol, int(settings["Inner_Iter"]),
+                                                     Vrest[:, c1], mv)
+            Vrest[:, c1] = V
+            recs.append({"f_hz": float(f), "port": c1, "flag": int(flag), "relres": float(relres),
+                         "iters": int(it[1]), "port_s": time.perf_counter() - tp,
+                         "lu_s": t_lu if c1 == 0 else 0.0})
+            if len(recs) >= max_solves or time.perf_counter() - t0 >= budget_s:
+                return recs, time.perf_counter() - t0, npt
+    return recs, time.perf_counter() - t0, npt
+
+
+def cpu_baseline(P):
+    """The CPU oracle on the host cores, a bounded sample of the same workload: the
+    first frequency's SuperLU factorisation and one complete port solve from a zero
+    initial guess (right-hand side, Householder GMRES with reflectors, operator
+    applications at the reference's 2N extents with scipy.fft on all cores). A
+    frequency point is that factorisation plus one such solve per port."""
     from oracle import peec_oracle as O
     cores = os.cpu_count() or 1
     O.FFT_WORKERS = cores
-    Nx, Ny, Nz = P["grid"]
-    FFTCP, FFTCLp = O.spectra_from_rows(P["rows"], Nx, Ny, Nz)
-    w = 2 * np.pi * P["freqs"][0] * P["esc"]["freq"]
-    t = time.perf_counter()
-    fs = O.frequency_setup(w, P["esc"], P["inc"], P["diag"], P["Zs"], P["le"], P["ports"], P["z0"])
-    t_lu = time.perf_counter() - t
-    x = np.random.default_rng(0).standard_normal(P["op"].N) + 0j
-    t = time.perf_counter()
-    O.ComputeMatrixVectorFTT(x, w, P["inc"], FFTCP, FFTCLp, fs["DZ"], fs["Yle"], P["exp"],
-                             fs["invZ"], fs["invP"], fs["F"])
-    t_mv = time.perf_counter() - t
-    npt = len(P["ports"]["port_nodes"])
-    t_point = t_lu + npt * mv_per_port * t_mv
+    (esc, inc, cc, diag, exp, ports, le, li, Zs), freqs, settings, z0, grid = P["oracle"]
+    problem = (esc, inc, cc, diag, exp, ports, le, Zs, z0, settings)
+    recs, el, npt = oracle_port_solves(O, problem, P["oracle_rows"], grid, freqs[:1], 0.0, 1,
+                                       float(settings["tol"]))
+    r = recs[0]
+    t_point = r["lu_s"] + npt * r["port_s"]
     return {"value": 1.0 / t_point, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": (f"one oracle operator application ({t_mv:.2f} s, reference 2N extents, "
-                       f"scipy.fft x{cores} threads, 3 SuperLU solves) + one SuperLU factorisation "
-                       f"({t_lu:.2f} s); freq point = LU + {npt} ports x {mv_per_port:.1f} matvecs "
-                       f"({sample_note})"),
-            "matvec_s": t_mv, "lu_s": t_lu}
+            "sample": (f"the oracle's SuperLU factorisation at {r['f_hz']:.3g} Hz ({r['lu_s']:.2f} s) "
+                       f"and one complete port solve from a zero initial guess ({r['port_s']:.1f} s, "
+                       f"{r['iters']} Householder GMRES iterations to {r['relres']:.2e}, operator at "
+                       f"the reference 2N extents, scipy.fft x{cores}); a frequency point = the "
+                       f"factorisation + {npt} such port solves"),
+            "lu_s": r["lu_s"], "port_solve_s": r["port_s"], "gmres_iters": r["iters"]}
 
 
 def run_small_configs(args):
@@ -461,48 +499,79 @@ def run_small_configs(args):
 
 
 def run_reference(args):
-    ws, rank, local = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    """The reference arm: the CPU oracle restatement of the reference path on the host
+    cores (the reference itself is Julia, absent on both machines), built from its own
+    mesher restatement and C fill. Each timed step is one complete port solve in the
+    reference's frequency x port order, the SuperLU factorisation of a frequency charged
+    to its first port. The metric is the completed port solves / ports per elapsed
+    second. At most --steps solves run, and no more once the time budget is spent; the
+    line reports the solves actually timed. Warm-up steps are one operator application
+    each. Rank 0 alone runs; other ranks exit."""
+    rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    from oracle import mesher_ref as OM
     from oracle import peec_oracle as O
-    from solver_gb300 import configs, mesher
+    from solver_gb300 import configs
     cores = os.cpu_count() or 1
     O.FFT_WORKERS = cores
-    req = configs.random_128x128x64()
-    out, freqs, settings, z0, grid = mesher.parse_request(req)
+    req = configs.random_128x128x64() if args.grid is None else configs.random_mixed(tuple(args.grid))
+    t = time.perf_counter()
+    out, freqs, settings, z0, grid = OM.parse_request(req)
+    mesh_s = time.perf_counter() - t
     esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    t = time.perf_counter()
     rows = O.fill_rows(cc, esc, *grid)
+    fill_s = time.perf_counter() - t
     FFTCP, FFTCLp = O.spectra_from_rows(rows, *grid)
-    npt = len(ports["port_nodes"])
-    x = np.random.default_rng(0).standard_normal(inc["A"].shape[0] + inc["A"].shape[1] +
-                                                   inc["Gamma"].shape[1]) + 0j
-    times = []
-    for i in range(args.warmup + args.steps):
-        k = i % len(freqs)
-        w = 2 * np.pi * freqs[k] * esc["freq"]
-        t = time.perf_counter()
-        fs = O.frequency_setup(w, esc, inc, diag, Zs, le, ports, z0)
-        t_lu = time.perf_counter() - t
-        t = time.perf_counter()
-        O.ComputeMatrixVectorFTT(x, w, inc, FFTCP, FFTCLp, fs["DZ"], fs["Yle"], exp, fs["invZ"],
-                                 fs["invP"], fs["F"])
-        t_mv = time.perf_counter() - t
-        if i >= args.warmup:
-            times.append(t_lu + npt * REF_MATVECS_PER_PORT * t_mv)
-    t_point = float(np.mean(times))
-    v = 1.0 / t_point
-    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_point * 1e3, "higher_is_better": True,
+    tol = float(settings["tol"])
+    w0 = 2 * np.pi * freqs[0] * esc["freq"]
+    fs0 = O.frequency_setup(w0, esc, inc, diag, Zs, le, ports, z0)
+    N = inc["A"].shape[0] + inc["A"].shape[1] + inc["Gamma"].shape[1]
+    x = np.random.default_rng(0).standard_normal(N) + 0j
+    for _ in range(args.warmup):
+        O.ComputeMatrixVectorFTT(x, w0, inc, FFTCP, FFTCLp, fs0["DZ"], fs0["Yle"], exp,
+                                 fs0["invZ"], fs0["invP"], fs0["F"])
+    del fs0
+    problem = (esc, inc, cc, diag, exp, ports, le, Zs, z0, settings)
+    recs, elapsed, npt = oracle_port_solves(O, problem, rows, grid, freqs, args.ref_budget,
+                                            args.steps, tol)
+    done = len(recs)
+    v = (done / npt) / elapsed
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": done,
+            "steps_requested": args.steps, "warmup": args.warmup,
+            "ms_per_step": elapsed * 1e3 / done, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": WORKLOAD},
+            "config": {"workload": WORKLOAD if args.grid is None else f"random {args.grid}",
+                       "grid": list(grid), "N": int(N),
+                       "step": "one complete port solve (the frequency's SuperLU factorisation "
+                               "charged to its first port); value = port solves / ports / s"},
+            "timed": {"elapsed_s": elapsed, "port_solves": done, "budget_s": args.ref_budget,
+                      "solves": recs, "mesh_s": mesh_s, "fill_s": fill_s,
+                      "note": "only the solves listed ran inside the timed region; nothing "
+                              "is extrapolated"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": (f"per step: one SuperLU factorisation + one oracle "
-                                        f"operator application (reference 2N extents, scipy.fft x"
-                                        f"{cores}), freq point = LU + {npt} ports x "
-                                        f"{REF_MATVECS_PER_PORT} matvecs")},
+                             "sample": (f"{done} complete oracle port solves in the reference's "
+                                        f"frequency x port order from {freqs[0]:.3g} Hz, warm "
+                                        f"started, SuperLU per frequency, operator at the "
+                                        f"reference 2N extents with scipy.fft x{cores}, mesher "
+                                        f"and fill from the oracle")},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line["native_so_loaded"] = loaded_native_libs()
     print(json.dumps(line), flush=True)
+
+
+def loaded_native_libs():
+    """The shared objects of this repository mapped into this process (Linux)."""
+    try:
+        maps = Path("/proc/self/maps").read_text().splitlines()
+    except OSError:
+        return None
+    root = str(ROOT)
+    libs = sorted({ln.split()[-1] for ln in maps
+                   if ln.split() and ln.split()[-1].startswith(root) and ".so" in ln})
+    return [os.path.relpath(p_, root) for p_ in libs]
 
 
 def run_batched_sweep(args):
@@ -567,6 +636,92 @@ def run_adjoint(args):
     P.close()
 
 
+def s_matrix(cols, npt):
+    S = np.zeros((npt, npt), dtype=np.complex128)
+    for c1, col in cols.items():
+        for c2, v in col.items():
+            S[c1, c2] = S[c2, c1] = v
+    return S
+
+
+def z_of_s(S, z0):
+    """s2z_fft (FFT_solver_QS_S_type.jl:265-274): Z = z0 (I - S)^-1 (I + S)."""
+    I = np.eye(len(S))
+    return z0 * np.linalg.solve(I - S, I + S)
+
+
+class LaneTimer:
+    """Device span of a lane sweep: an event on the first lane's stream that every other
+    lane stream waits on, and the last lane's end joined back into the first stream."""
+
+    def __init__(self, lanes, local):
+        import torch
+        self.torch = torch
+        streams = [o.stream() for o in lanes.ops]
+        self.ext = [torch.cuda.ExternalStream(h, device=f"cuda:{local}") for h in streams]
+
+    def start(self):
+        ev = self.torch.cuda.Event(enable_timing=True)
+        ev.record(self.ext[0])
+        for xs in self.ext[1:]:
+            xs.wait_event(ev)
+        self.e0 = ev
+
+    def stop(self):
+        for xs in self.ext[1:]:
+            ei = self.torch.cuda.Event()
+            ei.record(xs)
+            self.ext[0].wait_event(ei)
+        e1 = self.torch.cuda.Event(enable_timing=True)
+        e1.record(self.ext[0])
+        e1.synchronize()
+        return self.e0.elapsed_time(e1)
+
+
+def lane_sweep(P, lanes, seq, get_state, Vrest, tol, mode, solve_kw, timer):
+    """Every port at every frequency key of seq on the port lanes, warm started along
+    the sequence (PortLanes.sweep). Returns the device span (CUDA events, ms), the wall
+    time (s), the S columns per position, the work records and the kernel launches."""
+    import threading
+    m_, n_ = P["inc"]["A"].shape
+    ns_ = P["inc"]["Gamma"].shape[1]
+    pn = np.asarray(P["ports"]["port_nodes"], dtype=np.int64)
+    cols, work = {}, []
+    lock = threading.Lock()
+    from solver_gb300 import api as _api
+
+    def record(pos, k, c1, V, flag, relres, outer, ninner):
+        col = _api._port_column(V, pn, c1, m_, ns_, P["z0"])
+        with lock:
+            cols.setdefault(pos, {})[c1] = col
+            work.append({"pos": pos, "port": c1, "flag": flag, "relres": relres,
+                         "outer": outer, "inner": ninner})
+
+    l0 = sum(o.launch_count() for o in lanes.ops)
+    t0 = time.perf_counter()
+    if timer is not None:
+        timer.start()
+    lanes.sweep(seq, get_state, lambda k: None, pn, P["esc"]["Is"], Vrest, lambda k: tol,
+                solve_kw, record, mode=mode)
+    gpu_ms = timer.stop() if timer is not None else None
+    wall = time.perf_counter() - t0
+    if gpu_ms is None:
+        gpu_ms = wall * 1e3
+    launches = sum(o.launch_count() for o in lanes.ops) - l0
+    return gpu_ms, wall, cols, work, launches
+
+
+def z_errors(seq, cols, Zref, npt, z0):
+    """Per frequency key: max |Z - Zref| / max |Zref| at the first visit of the key in seq."""
+    out = {}
+    for pos, k in enumerate(seq):
+        if k in out or pos not in cols or k not in Zref:
+            continue
+        Z = z_of_s(s_matrix(cols[pos], npt), z0)
+        out[k] = float(np.max(np.abs(Z - Zref[k])) / np.max(np.abs(Zref[k])))
+    return out
+
+
 def main():
     args = parse()
     if getattr(args, "adjoint", False):
@@ -584,26 +739,36 @@ def main():
     ws, rank, local = dist_init()
     P = setup_problem(device=local, grid=args.grid)
     P["inner_tol"] = args.inner_tol
-    P["host_ms"] = {"set_frequency": 0.0, "port_rhs": 0.0, "solve_mixed": 0.0}
     op = P["op"]
     nf = len(P["freqs"])
     tol = float(P["settings"]["tol"])
-    Vrest = np.zeros((op.N, len(P["ports"]["port_nodes"])), dtype=np.complex128)
-    # host states (Yle, SuperLU factors) of the next frequencies are built by spawned
-    # worker processes while the GPU solves the current one
+    npt = len(P["ports"]["port_nodes"])
+    Vrest = np.zeros((op.N, npt), dtype=np.complex128)
+    w_of = lambda k: 2 * np.pi * P["freqs"][k] * P["esc"]["freq"]
+    # host states (Yle, SuperLU factors) are built by spawned worker processes; the
+    # executor is shared by the pools below, so the workers start only once
     from solver_gb300.frequency import FrequencyPool
-    order = [0] + [i % nf for i in range(args.warmup + args.steps)]
     static = (P["esc"], P["inc"], P["diag"], P["Zs"], P["le"], P["ports"], P["z0"])
     nworkers = max(2, min(12, (os.cpu_count() or 4) - 4))
+    # make_pool(order, key_of): a pool over the keys of `order`, key q building the state
+    # of frequency key_of(q), each state kept once built (lanes share it)
     if args.host_states == "processes":
-        pf = FrequencyPool(static, lambda k: 2 * np.pi * P["freqs"][k] * P["esc"]["freq"],
-                           order, workers=nworkers, lookahead=nworkers, keep=True)
+        ex = FrequencyPool.executor(static, nworkers)
+        make_pool = lambda order, key_of: FrequencyPool(
+            static, lambda q: w_of(key_of(q)), order, workers=nworkers, lookahead=nworkers,
+            keep=True, executor=ex)
     else:
         # one worker thread, no child processes (for runs under a profiler)
         from solver_gb300.frequency import StatePrefetcher
+        ex = None
         nworkers = 1
-        pf = StatePrefetcher(lambda k: freq_state(P, k), order, keep=True)
-    state = pf.get
+        make_pool = lambda order, key_of: StatePrefetcher(lambda q: freq_state(P, key_of(q)),
+                                                          order, keep=True)
+    warm_seq = [i % nf for i in range(args.warmup)]
+    seq = [i % nf for i in range(args.warmup, args.warmup + args.steps)]
+    # cached states for the device-timed passes (inputs prepared before the timed region)
+    cache = make_pool([0] + warm_seq + seq, lambda k: k)
+    state = cache.get
 
     # -- operator profile and roofline (FP32 and FP64 convolutions) --------------------------
     op.set_frequency(state(0).w, state(0).DZ, state(0).Yle, state(0).lu)
@@ -619,128 +784,129 @@ def main():
             print(json.dumps({"profile_only": True, "grid": list(P["grid"]), "fp32": prof32,
                               "fp64": prof64, "ff": profff, "fp32_bytes_by_pass": b32}),
                   flush=True)
-        pf.close()
+        cache.close()
+        if ex is not None:
+            ex.shutdown()
         op.close()
         return
 
-    # -- mixed-precision timed steps ---------------------------------------------------------
     from solver_gb300.api import PortLanes
-    nlanes = max(1, min(args.lanes, len(P["ports"]["port_nodes"])))
-    P["lanes"] = PortLanes(op, nlanes)
-    lane_streams = [op.stream()] + [o.stream() for o in P["lanes"].ops[1:]]
+    nlanes = max(1, min(args.lanes, npt))
+    lanes = PortLanes(op, nlanes)
     try:
-        import torch
-        ext = torch.cuda.ExternalStream(op.stream(), device=f"cuda:{local}")
-        lane_ext = [ext] + [torch.cuda.ExternalStream(h, device=f"cuda:{local}")
-                            for h in lane_streams[1:]]
-        ev = lambda: torch.cuda.Event(enable_timing=True)
-        have_torch = True
+        timer = LaneTimer(lanes, local)
     except Exception:
-        have_torch = False
-    S_mixed = {}
-    for i in range(args.warmup):
-        k = i % nf
-        S_mixed[k], _, _, _ = solve_point(P, state(k), Vrest, "mixed", tol)
-    # the timed points: every lane runs its ports through the whole timed frequency
-    # sequence on its own (PortLanes.sweep), so one lane's frequency-state upload overlaps
-    # the other lanes' solves; the device span runs from an event all lane streams wait
-    # on to the last lane's end
-    from solver_gb300 import api as _api
-    import threading
-    seq = [i % nf for i in range(args.warmup, args.warmup + args.steps)]
-    m_, n_ = P["inc"]["A"].shape
-    ns_ = P["inc"]["Gamma"].shape[1]
-    pn = np.asarray(P["ports"]["port_nodes"], dtype=np.int64)
-    npt = pn.shape[0]
-    cols = {}
-    work = []
-    rlock = threading.Lock()
-    wait_s = [0.0]
+        timer = None
+    mixed_kw = dict(inner_tol=P["inner_tol"], inner_maxit=P["settings"]["Inner_Iter"])
+    fp64_kw = dict(maxit=P["settings"]["Inner_Iter"])
+    cached = lambda k, pos: state(k)
+    # warm-up: the first points of the sequence, untimed; they also build the warm starts
+    if warm_seq:
+        lane_sweep(P, lanes, warm_seq, cached, Vrest, tol, "mixed", mixed_kw, None)
 
-    def record(pos, k, c1, V, flag, relres, outer, ninner):
-        col = _api._port_column(V, pn, c1, m_, ns_, P["z0"])
-        with rlock:
-            cols.setdefault(pos, {})[c1] = col
-            work.append({"flag": flag, "relres": relres, "outer": outer, "inner": ninner,
-                         "fp64_matvecs": outer + 1, "fp32_matvecs": ninner + outer})
-
-    def get_state(k, pos):
-        th = time.perf_counter()
-        st = pf.get(k, pos=1 + args.warmup + pos)
-        with rlock:
-            wait_s[0] += time.perf_counter() - th
-        return st
-
-    l0 = sum(o.launch_count() for o in P["lanes"].ops)
+    # -- value: device span of the mixed sweep over the timed points (states built) -------
+    for k in sorted(set(seq)):
+        state(k)
     barrier(ws)
-    if have_torch:
-        torch.cuda.synchronize()
+    sync = (lambda: __import__("torch").cuda.synchronize()) if timer is not None else (lambda: None)
+    sync()
     clocks = Clocks(local)
-    t_wall0 = time.perf_counter()
-    if have_torch:
-        e0, e1 = ev(), ev()
-        e0.record(ext)
-        for xs in lane_ext[1:]:
-            xs.wait_event(e0)
-    P["lanes"].sweep(seq, get_state, lambda k: None, pn, P["esc"]["Is"], Vrest,
-                     lambda k: tol, dict(inner_tol=P["inner_tol"],
-                                         inner_maxit=P["settings"]["Inner_Iter"]), record)
-    if have_torch:
-        for xs in lane_ext[1:]:
-            ei = ev()
-            ei.record(xs)
-            ext.wait_event(ei)
-        e1.record(ext)
-        e1.synchronize()
-        gpu_ms = e0.elapsed_time(e1)
-        torch.cuda.synchronize()
-    t_wall = time.perf_counter() - t_wall0
-    if not have_torch:
-        gpu_ms = t_wall * 1e3
-    host_wait = wait_s[0] / max(1, nlanes)
-    h2d = d2h = 0
-    for pos, k in enumerate(seq):
-        Sk = np.zeros((npt, npt), dtype=np.complex128)
-        for c1, col in cols[pos].items():
-            for c2, v in col.items():
-                Sk[c1, c2] = Sk[c2, c1] = v
-        S_mixed[k] = Sk
-        h2d += _point_bytes(P, state(k), npt)
-        d2h += npt * 2 * (m_ + ns_ + n_) * 16
+    V_e2e = Vrest.copy()  # the e2e pass starts from the same warm starts
+    gpu_ms, wall_v, cols_mx, work, launches = lane_sweep(P, lanes, seq, cached, Vrest, tol,
+                                                        "mixed", mixed_kw, timer)
+    sync()
+    # -- e2e: the same points again through the public calls with host buffers; each
+    # point's host state (Yle, SuperLU factorisation, exported factors) is built inside the
+    # timed region by worker processes that start on it only now, overlapped with the
+    # GPU solves of the points before it
+    barrier(ws)
+    sync()
+    t_e0 = time.perf_counter()
+    # keyed by position in the timed sequence: a frequency visited twice is built twice
+    fresh = make_pool(list(range(len(seq))), lambda pos: seq[pos])
+    waits = [0.0]
+
+    def fresh_state(k, pos):
+        th = time.perf_counter()
+        st = fresh.get(pos, pos=pos)
+        waits[0] += time.perf_counter() - th
+        return st
+    _, wall_e2e, cols_e2e, _, _ = lane_sweep(P, lanes, seq, fresh_state, V_e2e, tol, "mixed",
+                                             mixed_kw, None)
+    sync()
+    wall_e2e = time.perf_counter() - t_e0
+    fresh.close()
     barrier(ws)
     clk = clocks.stop()
-    launches = sum(o.launch_count() for o in P["lanes"].ops) - l0
-    value, e2e_v, gpu_s, wall_s = whole_job_rates(ws, args.steps, gpu_ms / 1e3, t_wall)
+    m_, n_ = P["inc"]["A"].shape
+    ns_ = P["inc"]["Gamma"].shape[1]
+    h2d = sum(_point_bytes(P, state(k), npt) for k in seq)
+    d2h = len(seq) * npt * 2 * (m_ + ns_ + n_) * 16
+    value, e2e_v, gpu_s, wall_s = whole_job_rates(ws, args.steps, gpu_ms / 1e3, wall_e2e)
 
-    # -- FP64 plain (reference algorithm) on the same frequency sequence ---------------------
-    # the warm-up points build the same warm starts untimed; then the first fp64_steps of
-    # the timed mixed points are timed
-    V64 = np.zeros_like(Vrest)
-    fp64_ms = 0.0
-    work64 = []
-    S64 = {}
+    # -- FP64 plain (reference algorithm) and the FP64-residual mixed variant, on the same
+    # lanes and the same points; each warm-started from the warm-up points' solutions
     n64 = min(args.fp64_steps, args.steps)
+    seq64 = seq[:n64]
+    V64 = np.zeros_like(Vrest)
+    fp64 = vres = None
+    cols64 = colsr = {}
     if n64:
-        for i in range(args.warmup):
-            solve_point(P, state(i % nf), V64, "fp64", tol)
-        for i in range(args.warmup, args.warmup + n64):
-            k = i % nf
-            fs = state(k)
-            t0 = time.perf_counter()
-            S64[k], w64, _, _ = solve_point(P, fs, V64, "fp64", tol)
-            fp64_ms += (time.perf_counter() - t0) * 1e3
-            work64 += w64
-    fp64_v = n64 / (fp64_ms / 1e3) if n64 else None
-    # mixed vs FP64 port quantities (S) at the frequencies both ran
-    errs = []
-    for k in S64:
-        if k in S_mixed:
-            a, b = S_mixed[k], S64[k]
-            Za = 50 * np.linalg.solve(np.eye(len(a)) - a, np.eye(len(a)) + a)
-            Zb = 50 * np.linalg.solve(np.eye(len(b)) - b, np.eye(len(b)) + b)
-            errs.append(float(np.max(np.abs(Za - Zb)) / np.max(np.abs(Zb))))
-    mv_per_port = float(np.mean([w_["fp64_matvecs"] for w_ in work64])) if work64 else \
-        float(REF_MATVECS_PER_PORT)
+        if warm_seq:
+            lane_sweep(P, lanes, warm_seq, cached, V64, tol, "fp64", fp64_kw, None)
+        sync()
+        ms64, _, cols64, work64, _ = lane_sweep(P, lanes, seq64, cached, V64, tol, "fp64",
+                                                fp64_kw, timer)
+        fp64 = {"value": n64 / (ms64 / 1e3), "unit": UNIT, "steps": n64, "lanes": nlanes,
+                "timing": "CUDA events spanning the lane streams, host states built beforehand "
+                          "(as value)",
+                "gmres_iters": [w_["inner"] for w_ in sorted(work64, key=lambda r: (r["pos"], r["port"]))]}
+        fp64["mixed_over_fp64"] = value / fp64["value"]
+        # mixed with FP64 (not float-float) refinement residuals
+        for o in lanes.ops:
+            o.set_residual_precision(0)
+        Vr = np.zeros_like(Vrest)
+        if warm_seq:
+            lane_sweep(P, lanes, warm_seq, cached, Vr, tol, "mixed", mixed_kw, None)
+        sync()
+        msr, _, colsr, workr, _ = lane_sweep(P, lanes, seq64, cached, Vr, tol, "mixed",
+                                             mixed_kw, timer)
+        for o in lanes.ops:
+            o.set_residual_precision(2)
+        vres = {"value": n64 / (msr / 1e3), "unit": UNIT, "steps": n64, "lanes": nlanes,
+                "dtype": "complex64 convolutions in the inner solves; complex128 refinement "
+                         "residuals (FP64 convolutions)",
+                "outer_mean": float(np.mean([w_["outer"] for w_ in workr])),
+                "inner_mean": float(np.mean([w_["inner"] for w_ in workr])),
+                "max_relres": float(max(w_["relres"] for w_ in workr))}
+
+    # -- accuracy: every timed arm's port impedances against FP64 GMRES at 1e-12 on the same
+    # frequencies (first visit of each in the timed sequence)
+    first = []
+    for k in seq:
+        if k not in first:
+            first.append(k)
+    Vref = np.zeros_like(Vrest)
+    _, _, cols_ref, work_ref, _ = lane_sweep(P, lanes, first, cached, Vref, 1e-12, "fp64",
+                                             dict(maxit=400), None)
+    Zref = {k: z_of_s(s_matrix(cols_ref[pos], npt), P["z0"]) for pos, k in enumerate(first)}
+    fkey = lambda k: f"{P['freqs'][k]:.4g}"
+    err_mx = z_errors(seq, cols_mx, Zref, npt, P["z0"])
+    err_e2e = z_errors(seq, cols_e2e, Zref, npt, P["z0"])
+    err_64 = z_errors(seq64, cols64, Zref, npt, P["z0"])
+    err_r = z_errors(seq64, colsr, Zref, npt, P["z0"])
+    accuracy = {
+        "reference": "FP64 GMRES at relative residual 1e-12 on the GPU (itself parity-tested "
+                     "against the oracle at 1e-10), per frequency; max |Z - Z_ref| / max |Z_ref|",
+        "ref_flags": sorted({w_["flag"] for w_ in work_ref}),
+        "mixed": {fkey(k): v for k, v in err_mx.items()},
+        "mixed_e2e": {fkey(k): v for k, v in err_e2e.items()},
+        "fp64_plain": {fkey(k): v for k, v in err_64.items()},
+        "mixed_fp64_residual": {fkey(k): v for k, v in err_r.items()},
+        "max": {"mixed": max(err_mx.values()) if err_mx else None,
+                "fp64_plain": max(err_64.values()) if err_64 else None,
+                "mixed_fp64_residual": max(err_r.values()) if err_r else None},
+        "target": 1e-7}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -752,25 +918,29 @@ def main():
                    "grid": list(P["grid"]), "N": int(op.N),
                    "m_edges": int(op.m), "ns_surfaces": int(op.ns), "n_nodes": int(op.n),
                    "l2": "inputs larger than L2 (Krylov basis and spectra > 129 MB)",
-                   "parallelism": f"replicas x{ws}", "port_lanes": nlanes},
+                   "parallelism": f"replicas x{ws}", "port_lanes": nlanes,
+                   "timed_points": [fkey(k) for k in seq]},
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps),
-                "host_state_wait_ms_per_step": host_wait * 1e3 / args.steps,
+                "host_states": "built inside the timed region by worker processes started on "
+                               "them only then (no state of a timed point exists before it)",
+                "host_state_wait_ms_per_step": waits[0] / max(1, nlanes) * 1e3 / args.steps,
                 "host_state_workers": nworkers},
         "gpu_launches": int(launches),
         "clocks": clk,
-        "fp64_plain": {"value": fp64_v, "unit": UNIT, "steps": n64,
-                       "mixed_over_fp64": (value / fp64_v) if fp64_v else None,
-                       "gmres_iters": [w_["iter"][1] for w_ in work64]},
+        "fp64_plain": fp64,
+        "mixed_fp64_residual": vres,
         "mixed_work": {"outer_mean": float(np.mean([w_["outer"] for w_ in work])),
                        "inner_mean": float(np.mean([w_["inner"] for w_ in work])),
                        "max_relres": float(max(w_["relres"] for w_ in work)),
-                       "z_rel_err_vs_fp64": max(errs) if errs else None},
+                       "flags": sorted({w_["flag"] for w_ in work})},
+        "accuracy": accuracy,
         "matvec": {"fp32_ms": prof32["total"], "fp64_ms": prof64["total"],
                    "ff_ms": profff["total"], "ff_ms_by_pass": profff,
                    "fp32_conv_gbs": conv_gbs(b32, prof32), "fp64_conv_gbs": conv_gbs(b64, prof64),
                    "fp32_ms_by_pass": prof32, "fp64_ms_by_pass": prof64,
-                   "fp32_bytes_by_pass": b32},
+                   "fp32_bytes_by_pass": b32,
+                   "fp32_operator_frac": sum(b32.values()) / (prof32["total"] * 1e-3) / 1e9 / peak},
         "reference_model": {
             "bytes_fp32": reference_model_bytes(P["grid"], 8),
             "effective_gbs_fp32": reference_model_bytes(P["grid"], 8) / (prof32["total"] * 1e-3) / 1e9,
@@ -786,12 +956,13 @@ def main():
     }
     line["fill"] = fill_report(P, rank == 0 and ws == 1 and not args.no_cpu_baseline)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(P, mv_per_port,
-                                            "matvec count measured by the FP64 run above")
+        line["cpu_baseline"] = cpu_baseline(P)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    pf.close()
-    P["lanes"].close()
+    cache.close()
+    if ex is not None:
+        ex.shutdown()
+    lanes.close()
     op.close()
     if ws > 1:
         import torch.distributed as dist

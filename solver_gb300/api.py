@@ -181,19 +181,23 @@ class PortLanes:
         return out
 
     def sweep(self, seq, get_state, release, pn, Is, Vrest, tol_of, solve_kw, record,
-              stop_flag=None):
-        """Mixed-precision solves of every port at every frequency key of seq, each lane
-        on its own through the whole sequence: port c runs on lane c % lanes; a lane sets
-        each frequency state on its context, then solves its ports warm-started from its
-        own previous solutions (columns of Vrest). No lane waits for another between
+              stop_flag=None, mode="mixed"):
+        """Solves of every port at every frequency key of seq, each lane on its own
+        through the whole sequence: port c runs on lane c % lanes; a lane sets each
+        frequency state on its context, then solves its ports warm-started from its own
+        previous solutions (columns of Vrest). No lane waits for another between
         frequencies, so one lane's host work (setting a frequency state, its uploads)
         overlaps the other lanes' GPU solves.
 
+        mode "mixed": peec_solve_mixed with solve_kw (inner_tol, inner_maxit); mode
+        "fp64": the reference algorithm, peec_gmres with solve_kw["maxit"].
         get_state(k, pos) -> state with w, DZ, Yle, lu; release(k) is called once every
         lane has set state k. record(pos, k, c, V, flag, relres, outer, inner) is called
-        from the lane threads after each solve. Returns False if stopped. An exception in
-        one lane stops the others before their next frequency or port solve, and is then
-        raised here."""
+        from the lane threads after each solve (fp64: outer = 1, inner = the GMRES
+        iterations). Returns False if stopped. An exception in one lane stops the others
+        before their next frequency or port solve, and is then raised here."""
+        if mode not in ("mixed", "fp64"):
+            raise ValueError(f"mode must be 'mixed' or 'fp64', not {mode!r}")
         import threading
         L = len(self.ops)
         npt = len(pn)
@@ -222,8 +226,13 @@ class PortLanes:
                     if failed.is_set():
                         return
                     tn = op.port_rhs(pn[c][0], pn[c][1], Is)
-                    V, flag, relres, outer, inner = op.solve_mixed(tn, Vrest[:, c], tol_of(k),
-                                                                   **solve_kw)
+                    if mode == "mixed":
+                        V, flag, relres, outer, inner = op.solve_mixed(tn, Vrest[:, c],
+                                                                       tol_of(k), **solve_kw)
+                    else:
+                        V, flag, relres, it, _ = op.gmres(tn, Vrest[:, c], tol_of(k),
+                                                          solve_kw["maxit"])
+                        outer, inner = 1, int(it[1])
                     if flag == 99:
                         stopped.append(True)
                         return

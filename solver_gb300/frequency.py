@@ -258,12 +258,9 @@ class FrequencyPool:
     static: (escalings, incidence_selection, diagonals, Zs_info, lumped_elements,
     ports, z0), sent to each worker once; w_of(k) the angular frequency of key k."""
 
-    def __init__(self, static, w_of, order, workers=4, lookahead=4, keep=True):
-        import multiprocessing
-        from concurrent.futures import ProcessPoolExecutor
-        self._pool = ProcessPoolExecutor(max_workers=workers,
-                                         mp_context=multiprocessing.get_context("spawn"),
-                                         initializer=_worker_init, initargs=(static,))
+    def __init__(self, static, w_of, order, workers=4, lookahead=4, keep=True, executor=None):
+        self._own = executor is None
+        self._pool = FrequencyPool.executor(static, workers) if executor is None else executor
         self._w_of = w_of
         self._order = list(order)
         self._pos = 0
@@ -272,6 +269,17 @@ class FrequencyPool:
         self._done = {}
         self._keep = keep
         self._lock = threading.Lock()
+
+    @staticmethod
+    def executor(static, workers):
+        """The spawned worker processes, each holding `static`. Several pools (for
+        example one per walk of a frequency sequence) can share one executor, so that
+        the workers are started and their imports paid only once."""
+        import multiprocessing
+        from concurrent.futures import ProcessPoolExecutor
+        return ProcessPoolExecutor(max_workers=workers,
+                                   mp_context=multiprocessing.get_context("spawn"),
+                                   initializer=_worker_init, initargs=(static,))
 
     def _submit(self, k):
         if k not in self._done and k not in self._pending:
@@ -308,6 +316,9 @@ class FrequencyPool:
             self._done.pop(k, None)
 
     def close(self):
+        """Cancels what was not started; shuts the workers down if this pool started
+        them (a shared executor stays up for its owner)."""
         for f in self._pending.values():
             f.cancel()
-        self._pool.shutdown(wait=True)
+        if self._own:
+            self._pool.shutdown(wait=True)

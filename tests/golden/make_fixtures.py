@@ -4,12 +4,14 @@
   the reference's own FFT-solver request bodies (inputs only; the reference ships no
   outputs for this path), copied verbatim (the crossbar gzip-compressed) from the
   reference checkout given as argv[1].
-* ``oracle_*.npz``: outputs of the CPU oracle (oracle/peec_oracle.py) on those inputs
-  (the two-material one at 1 GHz and 3 GHz) and on the 20x20x4 crossbar configuration, kept as regression pins of the oracle
-  itself (rows, one matvec on a seeded vector, the port solution and Z).
+* ``oracle_*.npz``: outputs of the CPU oracle (topology from oracle/mesher_ref.py, fill,
+  operator and sweep from oracle/peec_oracle.py) on those inputs (the two-material one at
+  1 GHz and 3 GHz) and on the 20x20x4 crossbar configuration, kept as regression pins of
+  the oracle itself (rows, one matvec on a seeded vector, the port solution and Z).
 
 Usage: python tests/golden/make_fixtures.py /path/to/reference
 """
+import json
 import shutil
 import sys
 from pathlib import Path
@@ -20,12 +22,13 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
 
+from oracle import mesher_ref as OM  # noqa: E402
 from oracle import peec_oracle as O  # noqa: E402
-from solver_gb300 import configs, mesher  # noqa: E402
+from solver_gb300 import configs  # noqa: E402
 
 
 def oracle_case(req, tag):
-    out, freqs, settings, z0, (Nx, Ny, Nz) = mesher.parse_request(req)
+    out, freqs, settings, z0, (Nx, Ny, Nz) = OM.parse_request(req)
     esc, inc, cc, diag, exp, ports, le, li, Zs = out
     rows = O.fill_rows(cc, esc, Nx, Ny, Nz)
     FFTCP, FFTCLp = O.spectra_from_rows(rows, Nx, Ny, Nz)
@@ -52,10 +55,10 @@ def main():
     with open(ref / "crossbar.json", "rb") as src, open(HERE / "crossbar.json.gz", "wb") as raw, \
             gzip.GzipFile(filename="", mode="wb", fileobj=raw, mtime=0) as dst:
         shutil.copyfileobj(src, dst)
-    oracle_case(mesher.load_request(HERE / "first_run_data.json"), "first_run_data")
+    oracle_case(json.loads((HERE / "first_run_data.json").read_text()), "first_run_data")
     # the two-material fixture at 1 GHz and 3 GHz: its face rows reach the far-field
     # (suppressed) branches of the P integrals
-    req2 = mesher.load_request(HERE / "first_run_data_2_materials.json")
+    req2 = json.loads((HERE / "first_run_data_2_materials.json").read_text())
     req2["solverInput"]["frequencies"] = [1e9, 3e9]
     oracle_case(req2, "first_run_data_2_materials")
     oracle_case(configs.crossbar_20x20x4(), "crossbar_20x20x4")

@@ -3,6 +3,8 @@ JSON line with the keys the benchmark contract asks of it, and ranks other than 
 multi-rank launch exit without work or output."""
 import json
 import os
+
+import pytest
 import subprocess
 import sys
 from pathlib import Path
@@ -17,7 +19,9 @@ def _bench(*args, env=None):
 
 
 def test_reference_arm_line():
-    r = _bench("--impl", "reference", "--steps", "1", "--warmup", "0")
+    """A small grid keeps the CPU suite short; the arm's code path is the one the
+    default 128x128x64 run takes."""
+    r = _bench("--impl", "reference", "--steps", "2", "--warmup", "1", "--grid", "10", "10", "6")
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
@@ -26,7 +30,13 @@ def test_reference_arm_line():
                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
                 "impl", "cpu_baseline", "e2e"):
         assert key in d, key
-    assert d["impl"] == "reference" and d["steps"] == 1 and d["warmup"] == 0
+    assert d["impl"] == "reference" and d["steps"] == 2 and d["warmup"] == 1
+    # complete port solves were timed, nothing extrapolated, and the reference arm built
+    # its inputs without the product's native mesher
+    solves = d["timed"]["solves"]
+    assert len(solves) == 2 and all(s["iters"] >= 1 for s in solves)
+    assert d["ms_per_step"] == pytest.approx(d["timed"]["elapsed_s"] * 1e3 / 2)
+    assert not any("libpeec" in so for so in (d["native_so_loaded"] or []))
     assert d["value"] > 0 and d["higher_is_better"] is True
     assert "workload" in d["config"]
     cb = d["cpu_baseline"]
@@ -37,7 +47,7 @@ def test_reference_arm_line():
 
 
 def test_reference_arm_other_ranks_exit_quietly():
-    r = _bench("--impl", "reference", "--steps", "1", "--warmup", "0",
+    r = _bench("--impl", "reference", "--steps", "1", "--warmup", "0", "--grid", "10", "10", "6",
                env={"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.strip() == ""

@@ -8,9 +8,12 @@ Tolerances: FP64 operator 1e-10 relative (max-norm; the preconditioned rows subt
 nearly equal terms, which lifts FFT rounding from ~1e-15 to ~1e-12), solutions and
 port impedances 1e-10 relative, FP32 operator 2e-5 relative.
 """
+import copy
+
 import numpy as np
 import pytest
 
+from oracle import mesher_ref as OM
 from oracle import peec_oracle as O
 from solver_gb300 import configs, mesher
 from solver_gb300.operator import GpuOperator
@@ -21,13 +24,23 @@ GOLDEN = __import__("pathlib").Path(__file__).resolve().parent / "golden"
 
 
 def _case(req):
-    out, freqs, settings, z0, grid = mesher.parse_request(req)
+    """The oracle side from the oracle's own mesher restatement; the GPU side (prod) from
+    the product mesher (the two are equal index for index, tests/test_oracle_mesher.py)."""
+    out, freqs, settings, z0, grid = OM.parse_request(copy.deepcopy(req))
     esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    pe = mesher.parse_request(copy.deepcopy(req))[0]
+    prod = dict(esc=pe[0], inc=pe[1], cc=pe[2], diag=pe[3], exp=pe[4], ports=pe[5], le=pe[6],
+                Zs=pe[8])
     rows = O.fill_rows(cc, esc, *grid)
     FFTCP, FFTCLp = O.spectra_from_rows(rows, *grid)
     return dict(esc=esc, inc=inc, cc=cc, diag=diag, exp=exp, ports=ports, le=le, Zs=Zs,
                 rows=rows, FFTCP=FFTCP, FFTCLp=FFTCLp, freqs=freqs, settings=settings, z0=z0,
-                grid=grid)
+                grid=grid, prod=prod)
+
+
+def _gpu_operator(c):
+    p = c["prod"]
+    return GpuOperator(p["inc"], p["exp"], p["diag"]["P"])
 
 
 def _at(req, freqs):
@@ -53,7 +66,7 @@ CASES = {
 @pytest.fixture(scope="module", params=sorted(CASES))
 def case(request):
     c = _case(CASES[request.param]())
-    op = GpuOperator(c["inc"], c["exp"], c["diag"]["P"])
+    op = _gpu_operator(c)
     op.set_rows(c["rows"])
     c["op"] = op
     c["name"] = request.param
@@ -204,11 +217,12 @@ def test_sweep_parity(case, tmp_path):
           "tol": np.full(len(c["freqs"]), c["settings"]["tol"])}
     ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
                                  c["diag"], c["ports"], c["z0"], c["le"], c["exp"], st, c["Zs"])
-    c["exp"]["gpu_ctx"] = c["op"]
+    c["prod"]["exp"]["gpu_ctx"] = c["op"]
     h = api.CirculantSpectra(c["op"])
     rec = tmp_path / "solves.jsonl"
-    got = api.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], h, h, c["diag"], c["ports"],
-                                   c["z0"], c["le"], c["exp"], st, c["Zs"], records=str(rec))
+    p = c["prod"]
+    got = api.FFT_solver_QS_S_type(c["freqs"], p["esc"], p["inc"], h, h, p["diag"], p["ports"],
+                                   c["z0"], p["le"], p["exp"], st, p["Zs"], records=str(rec))
     assert [r["niter"] for r in got["info"]] == [len(r["resvec"]) - 1 for r in ref["info"]]
     assert _rel(got["Z"], ref["Z"]) < 1e-10
     assert _rel(got["Vrest"], ref["Vrest"]) < 1e-10
@@ -231,10 +245,11 @@ def test_mixed_sweep(case, lanes):
     st = {"Inner_Iter": c["settings"]["Inner_Iter"], "tol": np.full(len(c["freqs"]), 1e-10)}
     ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
                                  c["diag"], c["ports"], c["z0"], c["le"], c["exp"], st, c["Zs"])
-    c["exp"]["gpu_ctx"] = c["op"]
+    c["prod"]["exp"]["gpu_ctx"] = c["op"]
     h = api.CirculantSpectra(c["op"])
-    got = api.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], h, h, c["diag"], c["ports"],
-                                   c["z0"], c["le"], c["exp"], st, c["Zs"], mode="mixed",
+    p = c["prod"]
+    got = api.FFT_solver_QS_S_type(c["freqs"], p["esc"], p["inc"], h, h, p["diag"], p["ports"],
+                                   c["z0"], p["le"], p["exp"], st, p["Zs"], mode="mixed",
                                    lanes=lanes)
     assert len(got["info"]) == len(ref["info"])
     assert all(r["flag"] == 0 and r["relres"] <= 1e-10 for r in got["info"]), got["info"]
@@ -294,12 +309,13 @@ def test_native_frequency_sweep():
           "tol": np.full(len(c["freqs"]), c["settings"]["tol"])}
     ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
                                  c["diag"], c["ports"], c["z0"], c["le"], c["exp"], st, c["Zs"])
-    op = GpuOperator(c["inc"], c["exp"], c["diag"]["P"])
+    op = _gpu_operator(c)
     op.set_rows(c["rows"])
-    c["exp"]["gpu_ctx"] = op
+    c["prod"]["exp"]["gpu_ctx"] = op
     h = api.CirculantSpectra(op)
-    got = api.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], h, h, c["diag"], c["ports"],
-                                   c["z0"], c["le"], c["exp"], st, c["Zs"])
+    p = c["prod"]
+    got = api.FFT_solver_QS_S_type(c["freqs"], p["esc"], p["inc"], h, h, p["diag"], p["ports"],
+                                   c["z0"], p["le"], p["exp"], st, p["Zs"])
     assert [r["niter"] for r in got["info"]] == [len(r["resvec"]) - 1 for r in ref["info"]]
     e = _rel(got["Z"], ref["Z"])
     assert e < 1e-8, e
@@ -312,7 +328,7 @@ def test_matvec_large_tiles():
     and inverse y passes, the combined and single z passes, in FP64 and FP32."""
     c = _case(configs.random_mixed((12, 72, 40), s=5e-5, p=0.3, seed=11, nports=1,
                                    freqs=[1e9], tol=1e-8))
-    op = GpuOperator(c["inc"], c["exp"], c["diag"]["P"])
+    op = _gpu_operator(c)
     try:
         op.set_rows(c["rows"])
         c["op"] = op
@@ -338,18 +354,19 @@ def test_mixed_crossbar_per_frequency():
     from solver_gb300 import api
     freqs = [1e9] + list(np.logspace(8, 10, 5))
     c = _case(_at(configs.crossbar_20x20x4(), freqs))
-    op = GpuOperator(c["inc"], c["exp"], c["diag"]["P"])
+    op = _gpu_operator(c)
     try:
         op.set_rows(c["rows"])
-        c["exp"]["gpu_ctx"] = op
+        c["prod"]["exp"]["gpu_ctx"] = op
         nf = len(c["freqs"])
         ref = O.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], c["FFTCP"], c["FFTCLp"],
                                      c["diag"], c["ports"], c["z0"], c["le"], c["exp"],
                                      {"Inner_Iter": 200, "tol": np.full(nf, 1e-12)}, c["Zs"])
         h = api.CirculantSpectra(op)
-        got = api.FFT_solver_QS_S_type(c["freqs"], c["esc"], c["inc"], h, h, c["diag"],
-                                       c["ports"], c["z0"], c["le"], c["exp"],
-                                       {"Inner_Iter": 100, "tol": np.full(nf, 1e-8)}, c["Zs"],
+        p = c["prod"]
+        got = api.FFT_solver_QS_S_type(c["freqs"], p["esc"], p["inc"], h, h, p["diag"],
+                                       p["ports"], c["z0"], p["le"], p["exp"],
+                                       {"Inner_Iter": 100, "tol": np.full(nf, 1e-8)}, p["Zs"],
                                        mode="mixed")
         assert all(r["flag"] == 0 and r["relres"] <= 1e-8 for r in got["info"])
         errs = [float(np.max(np.abs(got["Z"][:, :, k] - ref["Z"][:, :, k])) /

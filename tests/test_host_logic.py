@@ -36,6 +36,11 @@ class FakeOp:
         return x0 + (self.w + tn[0].real), 0, tol / 2, 1, 5
 
 
+    def gmres(self, tn, x0, tol, maxit):
+        self.log.append((self.name, "gmres", self.w, int(tn[0].real), maxit))
+        return x0 + (self.w + tn[0].real), 0, tol / 2, [1, 7], np.zeros(8)
+
+
 class FakeLanes(api.PortLanes):
     def __init__(self, nlanes, log):
         from concurrent.futures import ThreadPoolExecutor
@@ -188,3 +193,26 @@ def test_request_parser_rejects_inconsistent_grids():
     r["solverInput"]["materials"][0]["name"] = "gold"
     with pytest.raises(ValueError, match="lacks"):
         mesher.parse_request(r)
+
+
+def test_lanes_sweep_fp64_mode_runs_the_reference_gmres():
+    """mode="fp64": every port solve is the FP64 GMRES (peec_gmres) with the given maxit,
+    warm started along the sequence like the mixed sweep; record gets its iterations."""
+    log, recs = [], []
+    lanes = FakeLanes(2, log)
+    pn = np.array([[0, 1], [10, 11], [20, 21]])
+    V = np.zeros((1, 3), dtype=np.complex128)
+    ok = lanes.sweep([0, 1], lambda k, pos: State(float(k + 1)), lambda k: None, pn, 1.0, V,
+                     lambda k: 1e-8, {"maxit": 37},
+                     lambda pos, k, c, V_, flag, relres, outer, inner: recs.append((pos, c, inner)),
+                     mode="fp64")
+    lanes.close()
+    assert ok
+    assert sorted(recs) == [(0, 0, 7), (0, 1, 7), (0, 2, 7), (1, 0, 7), (1, 1, 7), (1, 2, 7)]
+    assert all(e[1] in ("set", "gmres") for e in log)
+    assert all(e[4] == 37 for e in log if e[1] == "gmres")
+    # warm starts: port c's final value is the sum of its two solves' increments
+    assert np.allclose(V[0], [(1 + 0) + (2 + 0), (1 + 10) + (2 + 10), (1 + 20) + (2 + 20)])
+    with pytest.raises(ValueError):
+        lanes.sweep([0], lambda k, pos: State(1.0), lambda k: None, pn, 1.0, V, lambda k: 1e-8,
+                    {}, lambda *a: None, mode="fp32")

@@ -16,6 +16,7 @@ import math
 import numpy as np
 import pytest
 
+from oracle import mesher_ref as OM
 from oracle import peec_oracle as O
 from solver_gb300 import configs, mesher
 
@@ -74,7 +75,7 @@ def test_p_far_field(caser):
 def test_port_operator_is_reciprocal():
     req = configs.random_mixed(shape=(10, 10, 4), p=0.45, seed=3, nports=2,
                                freqs=[1e8, 3e9], tol=1e-10)
-    out, freqs, _settings, z0, (Nx, Ny, Nz) = mesher.parse_request(req)
+    out, freqs, _settings, z0, (Nx, Ny, Nz) = OM.parse_request(req)
     esc, inc, cc, diag, exp, ports, le, _li, Zs = out
     FFTCP, FFTCLp = O.spectra_from_rows(O.fill_rows(cc, esc, Nx, Ny, Nz), Nx, Ny, Nz)
     m, n = inc["A"].shape
@@ -106,7 +107,7 @@ def _case(tag):
                                  "crossbar_20x20x4"])
 def test_oracle_matches_its_regression_pins(tag):
     req, pin = _case(tag)
-    out, freqs, settings, z0, (Nx, Ny, Nz) = mesher.parse_request(req)
+    out, freqs, settings, z0, (Nx, Ny, Nz) = OM.parse_request(req)
     esc, inc, cc, diag, exp, ports, le, _li, Zs = out
     rows = O.fill_rows(cc, esc, Nx, Ny, Nz)
     for key, row in rows.items():
@@ -146,7 +147,7 @@ def test_far_field_branches_reach_the_point_limit(name):
     cu[0:3, 0, 0] = True
     req = configs.make_request({"copper": cu}, [dict(configs.COPPER)], cell,
                                [((0, 0, 0), (2, 0, 0))], [1e9], 1e-8)
-    out, _f, _s, _z, _grid = mesher.parse_request(req)
+    out, _f, _s, _z, _grid = OM.parse_request(req)
     cc = out[2]
     sx, sy, sz = cc["sx"], cc["sy"], cc["sz"]
     edge = max(sx, sy, sz)
@@ -203,7 +204,7 @@ def test_oracle_gmres_matches_a_dense_solve():
     1e-11 the solutions agree to ~10x that (the operator's condition number is ~3e6, and
     the recursion's residual tracks the true one)."""
     req = configs.crossbar_20x20x4()
-    out, freqs, _settings, z0, grid = mesher.parse_request(req)
+    out, freqs, _settings, z0, grid = OM.parse_request(req)
     esc, inc, cc, diag, exp, ports, le, _li, Zs = out
     FFTCP, FFTCLp = O.spectra_from_rows(O.fill_rows(cc, esc, *grid), *grid)
     w = 2 * np.pi * freqs[0] * esc["freq"]
