@@ -162,13 +162,16 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def conv_bytes(info, prec):
+def conv_bytes(info, prec, staged=None):
     """Algorithmic bytes of the convolution passes per operator application: every
     per-family intermediate written once and read once by the next pass, each
-    spectrum read once (face families: 3 real + 3 complex spectra on the shared grid;
-    edge families: one real spectrum each), lattice maps (int32) once, compact vectors
-    (complex128) read once by the gather and written once by the scatter."""
+    spectrum read once, lattice maps (int32) once, compact vectors (complex128) read
+    once by the gather and written once by the scatter. Spectra: full form (face
+    families: 3 real + 3 complex on the shared grid; edge families: one real each), or
+    for the staged FP32 z passes (staged = {"faces", "edges"}) the y/z-folded real
+    tables of Lx(Ly/2+1)(Lz/2+1) floats (six for the faces, one per edge family)."""
     c = 16 if prec == 0 else 8
+    staged = staged or {"faces": False, "edges": False}
     b = {"xfwd": 0, "yfwd": 0, "z": 0, "yinv": 0, "xinv": 0}
     for f in info:
         if not f["active"]:
@@ -184,7 +187,11 @@ def conv_bytes(info, prec):
         b["yinv"] += t_y + t_x
         b["xinv"] += t_x + cells * 4 + cells * 16
         G = Lx * Ly * Lz
-        b["z"] += (G * c // 2) if f["edge"] else (G * c // 2 + G * c)  # per face family: 1 real + 1 complex
+        folded = Lx * (Ly // 2 + 1) * (Lz // 2 + 1) * 4
+        if prec == 1 and staged["edges" if f["edge"] else "faces"]:
+            b["z"] += folded if f["edge"] else 2 * folded  # per face family: 2 of the 6 tables
+        else:
+            b["z"] += (G * c // 2) if f["edge"] else (G * c // 2 + G * c)  # per face family: 1 real + 1 complex
     return b
 def reference_model_bytes(grid, c):
     """Bytes per operator application under the pruned three-pass pencil model counted at
@@ -206,13 +213,21 @@ def conv_gbs(b, prof):
     return sum(b[k] for k in keys) / (sum(prof[k] for k in keys) * 1e-3) / 1e9
 
 
-def z_traffic(grid):
+# the FP32 z-pass kernels of each tuner form
+ZKERNEL = {"face": {"direct": "k_zconv3<float>", "direct_yz": "k_zconv3_yz",
+                    "staged": "k_zconv3_staged"},
+           "edge": {"direct": "k_zconv1<float> x3", "direct_yz": "k_zconv1_yz x3",
+                    "staged": "k_zedge_staged"}}
+
+
+def z_traffic(grid, tuning):
     """DRAM bytes (read + write) of one operator application's FP32 z passes, as captured
-    by ncu on this grid and recorded in profiles/dram_traffic.json; None when no capture
-    of this grid is recorded."""
+    by ncu for these kernel forms on this grid and recorded in profiles/dram_traffic.json
+    (keyed "<face form>+<edge form>"); None when no such capture is recorded."""
+    form = f"{tuning['face']}+{tuning['edge']}"
     try:
         d = json.loads((ROOT / "profiles" / "dram_traffic.json").read_text())
-        return d["z_passes_fp32"].get("x".join(str(int(g)) for g in grid))
+        return d["z_passes_fp32"][form].get("x".join(str(int(g)) for g in grid))
     except (OSError, ValueError, KeyError):
         return None
 
@@ -776,13 +791,16 @@ def main():
     prof32 = op.profile_matvec(1, args.profile_iters)
     prof64 = op.profile_matvec(0, max(3, args.profile_iters // 4))
     profff = op.profile_matvec(2, max(3, args.profile_iters // 4))
-    b32, b64 = conv_bytes(info, 1), conv_bytes(info, 0)
+    tuning = op.zpass_tuning()
+    staged = {"faces": tuning["face"] != "direct", "edges": tuning["edge"] != "direct"}
+    b32, b64 = conv_bytes(info, 1, staged), conv_bytes(info, 0)
     peak, peak_kind = load_peaks()
     if args.profile_only:
         # operator applications only (a few hundred launches): the command ncu captures run
         if rank == 0:
             print(json.dumps({"profile_only": True, "grid": list(P["grid"]), "fp32": prof32,
-                              "fp64": prof64, "ff": profff, "fp32_bytes_by_pass": b32}),
+                              "fp64": prof64, "ff": profff, "fp32_bytes_by_pass": b32,
+                              "z_tuning": tuning}),
                   flush=True)
         cache.close()
         if ex is not None:
@@ -896,9 +914,12 @@ def main():
     err_64 = z_errors(seq64, cols64, Zref, npt, P["z0"])
     err_r = z_errors(seq64, colsr, Zref, npt, P["z0"])
     accuracy = {
-        "reference": "FP64 GMRES at relative residual 1e-12 on the GPU (itself parity-tested "
-                     "against the oracle at 1e-10), per frequency; max |Z - Z_ref| / max |Z_ref|",
+        "reference": "FP64 GMRES to relative residual 1e-12 on the GPU (itself parity-tested "
+                     "against the oracle at 1e-10; flag 3 marks a solve that stagnated at its "
+                     "smallest residual, ref_max_relres), per frequency; max |Z - Z_ref| / "
+                     "max |Z_ref|",
         "ref_flags": sorted({w_["flag"] for w_ in work_ref}),
+        "ref_max_relres": float(max(w_["relres"] for w_ in work_ref)),
         "mixed": {fkey(k): v for k, v in err_mx.items()},
         "mixed_e2e": {fkey(k): v for k, v in err_e2e.items()},
         "fp64_plain": {fkey(k): v for k, v in err_64.items()},
@@ -946,13 +967,16 @@ def main():
             "effective_gbs_fp32": reference_model_bytes(P["grid"], 8) / (prof32["total"] * 1e-3) / 1e9,
             "note": "pruned 3-pass pencil bytes at the reference's 2N extents over the whole "
                     "FP32 operator application (sparse part included in the time)"},
-        "roofline": {"bound": "hbm", "kernel": "k_zconv3<float> + k_zconv1<float> (z passes: "
-                     "FFT, spectral product, inverse FFT)",
+        "roofline": {"bound": "hbm",
+                     "kernel": (f"FP32 z passes (forward z FFT, spectral product, inverse z "
+                                f"FFT): faces {ZKERNEL['face'][tuning['face']]}, edges "
+                                f"{ZKERNEL['edge'][tuning['edge']]}"),
+                     "z_tuning": tuning,
                      "achieved": b32["z"] / (prof32["z"] * 1e-3) / 1e9, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": b32["z"] / (prof32["z"] * 1e-3) / 1e9 / peak,
-                     "traffic": z_traffic(P["grid"]), "bytes_per_matvec": b32["z"],
-                     "launches_per_matvec": 4},
+                     "traffic": z_traffic(P["grid"], tuning), "bytes_per_matvec": b32["z"],
+                     "launches_per_matvec": 2 if tuning["edge"] == "staged" else 4},
     }
     line["fill"] = fill_report(P, rank == 0 and ws == 1 and not args.no_cpu_baseline)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

@@ -224,6 +224,27 @@ int peec_conv_count(const peec_ctx* ctx);
  * each edge family has one real spectrum on its own grid.
  */
 int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* dims, int* active, int* kind);
+/*
+ * Profiling: the FP32 z-pass forms the autotuner picked for this context's grids, and the
+ * times it measured (ms per z pass, mean of three after a warm-up; -1 where a form was not
+ * a candidate). Forms: 0 register-direct kernels on the full-form spectra, 1 register-direct
+ * on the y/z-folded FP32 spectra (Lx(Ly/2+1)(Lz/2+1) values per block), 2 staged
+ * (persistent CTAs, each tile's pencils brought into shared memory by bulk asynchronous
+ * copies while the previous tile computes, y/z-folded spectra; the edge families in one
+ * launch). choice = {face form, edge form, edge radix plan}; face_ms[form];
+ * edge_ms[plan * 3 + form]. The tuner runs when the spectra are built (peec_fill,
+ * peec_set_rows) and caches its choice per device and grids. No counterpart in the
+ * reference (it plans FFTW with MEASURE, FFT_solver_QS_S_type.jl:17-53).
+ */
+int peec_zpass_tuning(const peec_ctx* ctx, int choice[3], double face_ms[3], double edge_ms[6]);
+/*
+ * Pins the FP32 z-pass forms (face, edge: 0..2 as above; edge_plan 0..1) in place of the
+ * tuner's choice, until the next peec_fill / peec_set_rows. A form a grid cannot take
+ * (partial 16-column tiles, too few z points) runs as form 0; peec_zpass_tuning reports
+ * the form that runs. For tests and for callers who fix the kernels. No counterpart in the
+ * reference.
+ */
+int peec_set_zpass_forms(peec_ctx* ctx, int face, int edge, int edge_plan);
 
 /*
  * Runs `iters` operator applications on an internal vector and reports the mean

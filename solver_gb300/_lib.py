@@ -23,7 +23,7 @@ EXPORTS = ("peec_version", "peec_ctx_create", "peec_ctx_destroy", "peec_last_err
            "peec_set_frequency", "peec_matvec", "peec_matvec_dev", "peec_port_rhs",
            "peec_gmres", "peec_solve_mixed", "peec_set_stop_flag", "peec_last_timing",
            "peec_launch_count", "peec_sizes", "peec_stream", "peec_conv_count",
-           "peec_conv_info", "peec_profile_matvec", "peec_multidot",
+           "peec_conv_info", "peec_zpass_tuning", "peec_set_zpass_forms", "peec_profile_matvec", "peec_multidot",
            "peec_multidot_noalloc", "peec_set_residual_precision",
            "peec_set_lu_component_max", "peec_adjoint", "peec_check_wait_limit")
 
@@ -101,6 +101,8 @@ def load(build_if_missing: bool = True):
     L.peec_conv_count.argtypes = [P]
     IP = ctypes.POINTER(ctypes.c_int)
     L.peec_conv_info.argtypes = [P, ctypes.c_int, IP, IP, IP, IP]
+    L.peec_zpass_tuning.argtypes = [P, IP, DP, DP]
+    L.peec_set_zpass_forms.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.peec_profile_matvec.argtypes = [P, ctypes.c_int, ctypes.c_int, DP]
     L.peec_multidot.argtypes = [P, P, ctypes.c_int64, P, ctypes.c_int64, ctypes.c_int, P]
     L.peec_multidot_noalloc.argtypes = [P, ctypes.c_int64, P, ctypes.c_int64, ctypes.c_int, P, P]

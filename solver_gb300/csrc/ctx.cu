@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <array>
 #include <map>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <tuple>
@@ -126,6 +127,12 @@ struct peec_ctx {
   Family fam[6];
   Spectrum spec[9];
   void* ph64[3] = {nullptr, nullptr, nullptr};  // face-grid phase tables (octant spectra)
+  void* ph32[3] = {nullptr, nullptr, nullptr};  // their FP32 rounding (FP32 z passes)
+  int* zerr = nullptr;  // set by a staged z pass whose copy wait ran into its limit
+  int nsm = 0;          // SM count of the device
+  ZTune zt;             // FP32 z-pass forms chosen by the tuner for this context's grids
+  double zface_ms[3] = {-1, -1, -1};          // tuner times per face form (-1: not a candidate)
+  double zedge_ms[6] = {-1, -1, -1, -1, -1, -1};  // per edge plan x form
   int row_dims[9][3] = {};
   // frequency state
   double w = 0.0;
@@ -323,6 +330,11 @@ static int peec_ctx_create_body(peec_ctx** out, int device) {
   cudaMemcpy(ctx->tw64, t64.data(), sizeof(c64) * ctx->twmax, cudaMemcpyHostToDevice);
   cudaMemcpy(ctx->tw32, t32.data(), sizeof(c32) * ctx->twmax, cudaMemcpyHostToDevice);
   cudaMemcpy(ctx->twff, tff.data(), sizeof(cff) * ctx->twmax, cudaMemcpyHostToDevice);
+  if (cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return fail(fail_cuda(cudaGetLastError(), "cudaDeviceGetAttribute", __FILE__, __LINE__));
+  if (cudaMalloc(&ctx->zerr, sizeof(int)) != cudaSuccess ||
+      cudaMemset(ctx->zerr, 0, sizeof(int)) != cudaSuccess)
+    return fail(fail_cuda(cudaErrorMemoryAllocation, "cudaMalloc error word", __FILE__, __LINE__));
   cudaMallocHost(&ctx->hsmall, sizeof(c64) * 16 * 4096);
   cudaMallocHost(&ctx->hread, sizeof(c64) * 4096);
   cudaMallocHost(&ctx->hscal, sizeof(double) * 64);
@@ -359,9 +371,13 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
     for (int p = 0; p < 2; ++p)
       if (s.d[p]) cudaFree(s.d[p]);
     if (s.oct) cudaFree(s.oct);
+    if (s.yz32) cudaFree(s.yz32);
   }
-  for (int a = 0; a < 3; ++a)
+  for (int a = 0; a < 3; ++a) {
     if (ctx->ph64[a]) cudaFree(ctx->ph64[a]);
+    if (ctx->ph32[a]) cudaFree(ctx->ph32[a]);
+  }
+  cudaFree(ctx->zerr);
   free_tri(ctx->Lf);
   free_tri(ctx->Uf);
   cudaFree(ctx->sf_ord);
@@ -524,10 +540,12 @@ static int peec_set_topology_body(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t
     }
     if (sp.oct) cudaFree(sp.oct);
     sp.oct = nullptr;
+    if (sp.yz32) cudaFree(sp.yz32);
+    sp.yz32 = nullptr;
   }
   for (int i = 0; i < 6; ++i) std::memcpy(ctx->spec[i].L, LP, sizeof(LP));
   for (int i = 6; i < 9; ++i) std::memcpy(ctx->spec[i].L, ctx->fam[i - 3].L, sizeof(LP));
-  CTX_TRY(phase_tables(LP, ctx->ph64, ctx->st));
+  CTX_TRY(phase_tables(LP, ctx->ph64, ctx->ph32, ctx->st));
   // work vectors
   CTX_TRY(dalloc(&ctx->LpI, m));
   CTX_TRY(dalloc(&ctx->PQ, ns));
@@ -569,6 +587,99 @@ static int peec_set_pdiag_body(peec_ctx* ctx, const double* diagP) {
   return PEEC_OK;
 }
 
+// The FP32 z-pass autotuner. For this context's grids it times every eligible form of the
+// face families' z pass and every form x radix plan of the edge families' z pass (one
+// warm-up launch, then the mean of three, CUDA events on the context stream) and keeps the
+// fastest; choices are cached process-wide by device and grids, so clones and later
+// contexts of the same lattice reuse them. The candidates run on the context's FP32 family
+// buffers, which every operator application rewrites from its input before the z passes.
+struct ZChoice {
+  int face = 0, edge = 0, plan = 0;
+  double fms[3] = {-1, -1, -1};
+  double ems[6] = {-1, -1, -1, -1, -1, -1};
+};
+static std::mutex g_tune_mu;
+static std::map<std::vector<int>, ZChoice> g_tune;
+static int check_solve_errors(peec_ctx* ctx);
+
+static int tune_zpass(peec_ctx* ctx) {
+  ctx->zt.err = ctx->zerr;
+  ctx->zt.nsm = ctx->nsm;
+  std::vector<int> key{ctx->dev};
+  for (const auto& F : ctx->fam) {
+    key.push_back(F.active ? 1 : 0);
+    for (int k = 0; k < 3; ++k) key.push_back(F.L[k]);
+    key.push_back(F.dims[2]);
+  }
+  auto apply = [&](const ZChoice& c) {
+    ctx->zt.face = c.face;
+    ctx->zt.edge = c.edge;
+    ctx->zt.edge_plan = c.plan;
+    std::memcpy(ctx->zface_ms, c.fms, sizeof(c.fms));
+    std::memcpy(ctx->zedge_ms, c.ems, sizeof(c.ems));
+  };
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return apply(it->second), PEEC_OK;
+  }
+  for (const auto& F : ctx->fam)
+    if (F.active && F.T[1])
+      PEEC_CUDA_TRY(cudaMemsetAsync(F.T[1], 0, (size_t)F.L[0] * F.L[1] * F.dims[2] * sizeof(c32),
+                                    ctx->st));
+  const void* ph[6] = {ctx->ph64[0], ctx->ph64[1], ctx->ph64[2],
+                       ctx->ph32[0], ctx->ph32[1], ctx->ph32[2]};
+  auto timed = [&](const ZTune& z, int which, double* ms) -> int {
+    CTX_TRY(zpass_f32(ctx->fam, 6, ctx->spec, ph, ctx->tw32, ctx->twmax, z, which, ctx->st));
+    PEEC_CUDA_TRY(cudaEventRecord(ctx->ev[0], ctx->st));
+    for (int i = 0; i < 3; ++i)
+      CTX_TRY(zpass_f32(ctx->fam, 6, ctx->spec, ph, ctx->tw32, ctx->twmax, z, which, ctx->st));
+    PEEC_CUDA_TRY(cudaEventRecord(ctx->ev[1], ctx->st));
+    PEEC_CUDA_TRY(cudaEventSynchronize(ctx->ev[1]));
+    float t = 0;
+    PEEC_CUDA_TRY(cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]));
+    *ms = t / 3.0;
+    return PEEC_OK;
+  };
+  ZChoice c;
+  const bool faces = ctx->fam[0].active && ctx->fam[1].active && ctx->fam[2].active;
+  bool edges = false;
+  for (int f = 3; f < 6; ++f) edges |= ctx->fam[f].active;
+  ZTune z = ctx->zt;
+  if (faces) {
+    const int nform = zpass_yz_faces(ctx->fam, 6) ? 3 : 1;
+    for (int form = 0; form < nform; ++form) {
+      z.face = form;
+      CTX_TRY(timed(z, 0, &c.fms[form]));
+      if (c.fms[form] < c.fms[c.face]) c.face = form;
+    }
+  }
+  if (edges) {
+    const int nform = zpass_yz_edges(ctx->fam, 6) ? 3 : 1;
+    double best = -1;
+    for (int plan = 0; plan < 2; ++plan) {
+      for (int form = 0; form < nform; ++form) {
+        z.edge = form;
+        z.edge_plan = plan;
+        double& ms = c.ems[plan * 3 + form];
+        CTX_TRY(timed(z, 1, &ms));
+        if (best < 0 || ms < best) {
+          best = ms;
+          c.edge = form;
+          c.plan = plan;
+        }
+      }
+    }
+  }
+  CTX_TRY(check_solve_errors(ctx));
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune[key] = c;
+  }
+  apply(c);
+  return PEEC_OK;
+}
+
 // spectra from device rows (rows in the order Lpx, Lpy, Lpz, p12, p34, p56, p1234,
 // p1256, p3456). Spectrum i uses row srow[i]: P blocks 00, 11, 22 (symmetric), 01, 02, 12
 // (cross: output family f, input family g), then the three Lp blocks.
@@ -593,6 +704,7 @@ static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
   }
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->have_spec = true;
+  CTX_TRY(tune_zpass(ctx));
   return PEEC_OK;
 }
 
@@ -935,13 +1047,19 @@ static void lu_solve(peec_ctx* ctx, const c64* b, c64* x) {
 // A triangular-solve wait that ran into its limit leaves an error word on the device;
 // entry points read it once their work is complete.
 static int check_solve_errors(peec_ctx* ctx) {
-  if (!ctx->sf_ctl) return PEEC_OK;
-  int e = 0;
-  PEEC_CUDA_TRY(cudaMemcpyAsync(&e, ctx->sf_ctl + 2, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  int e = 0, ez = 0;
+  if (ctx->sf_ctl)
+    PEEC_CUDA_TRY(cudaMemcpyAsync(&e, ctx->sf_ctl + 2, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+  if (ctx->zerr)
+    PEEC_CUDA_TRY(cudaMemcpyAsync(&ez, ctx->zerr, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   if (e) {
     cudaMemsetAsync(ctx->sf_ctl + 2, 0, sizeof(int), ctx->st);
     return bad(ctx, PEEC_ERR_TIMEOUT, "LU solve: a row dependency wait ran into its limit");
+  }
+  if (ez) {
+    cudaMemsetAsync(ctx->zerr, 0, sizeof(int), ctx->st);
+    return bad(ctx, PEEC_ERR_TIMEOUT, "z pass: a staged tile copy wait ran into its limit");
   }
   return PEEC_OK;
 }
@@ -971,13 +1089,18 @@ static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool ev
   cudaStream_t st = ctx->st;
   if (events) cudaEventRecord(ctx->ev[0], st);
   const void* tw[3] = {ctx->tw64, ctx->tw32, ctx->twff};
-  CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, ctx->ph64, x, ctx->LpI, ctx->PQ, ctx->m, prec, tw,
-                   ctx->twmax, st,
-                   ctx->prof ? ctx->pev.data() : nullptr));
+  const void* ph[6] = {ctx->ph64[0], ctx->ph64[1], ctx->ph64[2],
+                       ctx->ph32[0], ctx->ph32[1], ctx->ph32[2]};
+  CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, ph, x, ctx->LpI, ctx->PQ, ctx->m, prec, tw,
+                   ctx->twmax, st, ctx->prof ? ctx->pev.data() : nullptr, &ctx->zt));
   // one launch per x / y pass over all families, the shared z pass of the face
-  // families, one z pass per edge family
+  // families, and the edge families' z passes: one launch over all of them in the staged
+  // FP32 form (ZTune form 2), else one per family
   ctx->launches += 5;
-  for (const auto& F : ctx->fam) ctx->launches += (F.active && F.lp) ? 1 : 0;
+  int nedge = 0;
+  for (const auto& F : ctx->fam) nedge += (F.active && F.lp) ? 1 : 0;
+  const bool edge_one = prec == PEEC_PREC_FP32 && ctx->zt.edge == 2 && zpass_yz_edges(ctx->fam, 6);
+  ctx->launches += edge_one ? (nedge > 0) : nedge;
   if (events) cudaEventRecord(ctx->ev[1], st);
   sparse_enqueue(ctx, x, y, ctx->LpI, ctx->PQ);
   if (events) cudaEventRecord(ctx->ev[2], st);
@@ -1050,6 +1173,30 @@ static int peec_matvec_body(peec_ctx* ctx, const double* x, double* y, int preci
 extern "C" void* peec_stream(const peec_ctx* ctx) { return ctx ? (void*)ctx->st : nullptr; }
 
 extern "C" int peec_conv_count(const peec_ctx* ctx) { return ctx ? 6 : 0; }
+
+extern "C" int peec_set_zpass_forms(peec_ctx* ctx, int face, int edge, int edge_plan) {
+  if (!ctx) return badarg(__func__);
+  if (face < 0 || face > 2 || edge < 0 || edge > 2 || edge_plan < 0 || edge_plan > 1)
+    return bad(ctx, PEEC_ERR_BADARG, "z-pass forms are 0..2 and edge plans 0..1");
+  drop_graphs(ctx);
+  ctx->zt.face = face;
+  ctx->zt.edge = edge;
+  ctx->zt.edge_plan = edge_plan;
+  return PEEC_OK;
+}
+
+extern "C" int peec_zpass_tuning(const peec_ctx* ctx, int choice[3], double face_ms[3],
+                                 double edge_ms[6]) {
+  if (!ctx) return badarg(__func__);
+  if (choice) {
+    choice[0] = zpass_yz_faces(ctx->fam, 6) ? ctx->zt.face : 0;
+    choice[1] = zpass_yz_edges(ctx->fam, 6) ? ctx->zt.edge : 0;
+    choice[2] = ctx->zt.edge_plan;
+  }
+  if (face_ms) std::memcpy(face_ms, ctx->zface_ms, sizeof(ctx->zface_ms));
+  if (edge_ms) std::memcpy(edge_ms, ctx->zedge_ms, sizeof(ctx->zedge_ms));
+  return PEEC_OK;
+}
 
 extern "C" int peec_conv_info(const peec_ctx* ctx, int i, int* L, int* dims, int* active,
                               int* kind) {

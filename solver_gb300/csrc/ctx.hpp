@@ -67,24 +67,50 @@ struct Family {
 //   k_a in (-L_a/2, L_a/2] and R real; the (L_x/2+1)(L_y/2+1)(L_z/2+1) values of R are kept
 //   in FP64, layout (fy, fz, fx), fx fastest. The float-float passes read this form: an
 //   eighth (a sixteenth for cross blocks) of the FP64 bytes.
+// y/z-folded FP32 form (the FP32 z passes): R at the folded y and z frequencies but at
+//   every x position, layout (fy, fz, px), px the DIF position, so a z-pass tile's 16
+//   consecutive columns read 64 contiguous bytes; Lx(Ly/2+1)(Lz/2+1) floats, about a
+//   quarter of the full FP32 form. Cross blocks take their half-sample phases at run time
+//   from the FP32 phase tables.
 struct Spectrum {
   int L[3] = {1, 1, 1};
   int c[3] = {0, 0, 0};
   int is_complex = 0;
   void* d[2] = {nullptr, nullptr};  // full: [0] fp64, [1] fp32
   void* oct = nullptr;              // octant R, fp64
+  void* yz32 = nullptr;             // y/z-folded R, fp32
 };
 
 // Launchers (fftconv.cu). prec: 0 = fp64, 1 = fp32, 2 = float-float; tw[prec] the master
 // twiddle table of that arithmetic. x (input) / LpI / PQ are complex double; families
 // 0..2 are the face families, 3..5 the edge families; spectra 0..5 = P blocks
 // (00, 11, 22, 01, 02, 12), 6..8 = Lp blocks of families 3..5.
-// ev (nullable): 6 events around the five pass classes.
+// FP32 z-pass forms, chosen per grid by measurement (tune_zpass in ctx.cu). Face / edge
+// form 0: register-direct kernels on the full-form spectra; 1: register-direct kernels on
+// the y/z-folded spectra; 2: staged kernels (persistent CTAs, bulk-copied tiles, y/z-folded
+// spectra; the edge families in one launch). edge_plan: the edge families' z radix plan
+// (0: make_plan(n, 4, 4, 4), 1: make_plan(n, 4, 4, 3); 8 x 16 and 16 x 8 at Lz = 128).
+struct ZTune {
+  int* err = nullptr;  // error word set by a staged kernel whose copy wait ran into its limit
+  int nsm = 0;         // SM count of the device
+  int face = 0, edge = 0, edge_plan = 0;
+};
+// ev (nullable): 6 events around the five pass classes. ph: the face grid's phase tables,
+// FP64 (x, y, z) then FP32 (x, y, z). zt (nullable: form 0): the FP32 z-pass choice.
 int conv_all(const Family* F, int nfam, const Spectrum* spec, const void* const* ph,
              const c64* x, c64* LpI, c64* PQ, int64_t m, int prec, const void* const* tw,
-             int twmax, cudaStream_t st, cudaEvent_t* ev);
-// phase tables exp(-i*pi*k/L) (complex FP64) per DIF position of the three face-grid axes
-int phase_tables(const int L[3], void* e64[3], cudaStream_t st);
+             int twmax, cudaStream_t st, cudaEvent_t* ev, const ZTune* zt);
+// one FP32 z pass alone, in the forms of zt (which 0: the face families, 1: the edge
+// families), on the current family buffers; the tuner times it
+int zpass_f32(const Family* F, int nfam, const Spectrum* spec, const void* const* ph,
+              const void* tw, int twmax, const ZTune& zt, int which, cudaStream_t st);
+// phase tables exp(-i*pi*k/L) per DIF position of the three face-grid axes, complex FP64
+// (e64) and FP32 (e32)
+int phase_tables(const int L[3], void* e64[3], void* e32[3], cudaStream_t st);
+// whether the face / edge families' FP32 z passes can take forms 1 and 2 (whole 16-column
+// tiles, enough z points; the edge families on one shared grid)
+bool zpass_yz_faces(const Family* F, int nfam);
+bool zpass_yz_edges(const Family* F, int nfam);
 int spectrum_build(Spectrum& S, const double* d_row, const int M[3], const int na[3],
                    const int nb[3], const int sdim[3], const int odim[3], int symmetric,
                    const void* twiddles64, int twmax, cudaStream_t st);

@@ -39,11 +39,11 @@
 namespace peec {
 
 int conv_all_f32(const Family*, int, const Spectrum*, const void* const*, const c64*, c64*,
-                 c64*, int64_t, const void*, int, cudaStream_t, cudaEvent_t*);
+                 c64*, int64_t, const void*, int, cudaStream_t, cudaEvent_t*, const ZTune*);
 int conv_all_f64(const Family*, int, const Spectrum*, const void* const*, const c64*, c64*,
-                 c64*, int64_t, const void*, int, cudaStream_t, cudaEvent_t*);
+                 c64*, int64_t, const void*, int, cudaStream_t, cudaEvent_t*, const ZTune*);
 int conv_all_ff(const Family*, int, const Spectrum*, const void* const*, const c64*, c64*,
-                c64*, int64_t, const void*, int, cudaStream_t, cudaEvent_t*);
+                c64*, int64_t, const void*, int, cudaStream_t, cudaEvent_t*, const ZTune*);
 
 // copy W_L[e] = exp(-2 pi i e / L) for e < n from the master table of length twmax
 template <typename R>
@@ -56,10 +56,38 @@ __device__ void load_tw(cx<R>* dst, const cx<R>* __restrict__ master, int twmax,
 // master twiddle table
 int conv_all(const Family* F, int nfam, const Spectrum* spec, const void* const* ph,
              const c64* x, c64* LpI, c64* PQ, int64_t m, int prec, const void* const* tw,
-             int twmax, cudaStream_t st, cudaEvent_t* ev) {
-  if (prec == 0) return conv_all_f64(F, nfam, spec, ph, x, LpI, PQ, m, tw[0], twmax, st, ev);
-  if (prec == 2) return conv_all_ff(F, nfam, spec, ph, x, LpI, PQ, m, tw[2], twmax, st, ev);
-  return conv_all_f32(F, nfam, spec, ph, x, LpI, PQ, m, tw[1], twmax, st, ev);
+             int twmax, cudaStream_t st, cudaEvent_t* ev, const ZTune* zt) {
+  if (prec == 0) return conv_all_f64(F, nfam, spec, ph, x, LpI, PQ, m, tw[0], twmax, st, ev, zt);
+  if (prec == 2) return conv_all_ff(F, nfam, spec, ph, x, LpI, PQ, m, tw[2], twmax, st, ev, zt);
+  return conv_all_f32(F, nfam, spec, ph, x, LpI, PQ, m, tw[1], twmax, st, ev, zt);
+}
+
+// The y/z-folded and staged FP32 z passes need whole 16-column tiles (Lx a multiple of 16, so every
+// staged row is 128 bytes at a 128-byte offset), at least two radix groups along z, and
+// tiles that fit three (faces) / one (edges) per shared-memory budget; the edge families
+// must share one circulant grid to share a launch.
+static bool staged_grid(const Family& f, int zmin) {
+  return f.L[0] >= 16 && f.L[0] % 16 == 0 && f.L[2] >= zmin && f.L[2] <= 128 &&
+         f.dims[2] >= 1 && f.dims[2] <= f.L[2];
+}
+
+bool zpass_yz_faces(const Family* F, int nfam) {
+  if (nfam < 3) return false;
+  for (int f = 0; f < 3; ++f)
+    if (!F[f].active || !staged_grid(F[f], 16)) return false;
+  return true;
+}
+
+bool zpass_yz_edges(const Family* F, int nfam) {
+  const Family* f0 = nullptr;
+  for (int f = 3; f < nfam; ++f) {
+    if (!F[f].active) continue;
+    if (!staged_grid(F[f], 32)) return false;
+    if (!f0) f0 = &F[f];
+    else if (F[f].L[0] != f0->L[0] || F[f].L[1] != f0->L[1] || F[f].L[2] != f0->L[2])
+      return false;
+  }
+  return f0 != nullptr;
 }
 
 // --------------------------------------------------------------------------- spectra
@@ -191,9 +219,25 @@ __global__ void k_spec_octant(const c64* __restrict__ full, double* o64, int Lx,
   }
 }
 
+// octant R (FP64, (fy, fz, fx)) -> y/z-folded FP32 R ((fy, fz, px), px every DIF x position)
+__global__ void k_spec_yzfold(const double* __restrict__ o64, float* y32, int Lx, int Ly,
+                              int Lz) {
+  const int ox = Lx / 2 + 1, oy = Ly / 2 + 1, oz = Lz / 2 + 1;
+  const int nx = ilog2(Lx);
+  const size_t n = (size_t)Lx * oy * oz;
+  for (size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x; o < n;
+       o += (size_t)gridDim.x * blockDim.x) {
+    const int px = (int)(o % Lx);
+    const size_t rr = o / Lx;  // fy * oz + fz
+    int k = brev(px, nx);
+    const int fx = k <= Lx / 2 ? k : Lx - k;
+    y32[o] = (float)o64[rr * ox + fx];
+  }
+}
+
 // phase tables of the shifted axes: E[p] = exp(-i*pi*k/L) for the signed frequency k of
-// DIF position p (k = brev(p) folded into (-L/2, L/2])
-__global__ void k_phase_table(int L, c64* e64) {
+// DIF position p (k = brev(p) folded into (-L/2, L/2]), FP64 and its FP32 rounding
+__global__ void k_phase_table(int L, c64* e64, c32* e32) {
   const int n = ilog2(L);
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < L; p += gridDim.x * blockDim.x) {
     int k = brev(p, n);
@@ -201,15 +245,18 @@ __global__ void k_phase_table(int L, c64* e64) {
     double sn, cs;
     sincospi(-(double)k / L, &sn, &cs);
     e64[p] = mk<double>(cs, sn);
+    e32[p] = mk<float>((float)cs, (float)sn);
   }
 }
 
-int phase_tables(const int L[3], void* e64[3], cudaStream_t st) {
+int phase_tables(const int L[3], void* e64[3], void* e32[3], cudaStream_t st) {
   for (int a = 0; a < 3; ++a) {
     if (e64[a]) cudaFree(e64[a]);
-    e64[a] = nullptr;
+    if (e32[a]) cudaFree(e32[a]);
+    e64[a] = e32[a] = nullptr;
     PEEC_CUDA_TRY(cudaMalloc(&e64[a], sizeof(c64) * L[a]));
-    k_phase_table<<<(L[a] + 255) / 256, 256, 0, st>>>(L[a], (c64*)e64[a]);
+    PEEC_CUDA_TRY(cudaMalloc(&e32[a], sizeof(c32) * L[a]));
+    k_phase_table<<<(L[a] + 255) / 256, 256, 0, st>>>(L[a], (c64*)e64[a], (c32*)e32[a]);
   }
   PEEC_CUDA_TRY(cudaGetLastError());
   return 0;
@@ -253,6 +300,10 @@ int spectrum_build(Spectrum& S, const double* d_row, const int M[3], const int n
   if (!S.oct) PEEC_CUDA_TRY(cudaMalloc(&S.oct, no * sizeof(double)));
   k_spec_octant<<<1184, 256, 0, st>>>(full, (double*)S.oct, S.L[0], S.L[1], S.L[2], S.c[0],
                                       S.c[1], S.c[2], 1.0 / (double)n);
+  const size_t ny32 = (size_t)S.L[0] * (S.L[1] / 2 + 1) * (S.L[2] / 2 + 1);
+  if (!S.yz32) PEEC_CUDA_TRY(cudaMalloc(&S.yz32, ny32 * sizeof(float)));
+  k_spec_yzfold<<<1184, 256, 0, st>>>((const double*)S.oct, (float*)S.yz32, S.L[0], S.L[1],
+                                      S.L[2]);
   PEEC_CUDA_TRY(cudaGetLastError());
   PEEC_CUDA_TRY(cudaFreeAsync(full, st));
   return 0;

@@ -10,6 +10,7 @@
 
 #include "ctx.hpp"
 #include "fft_reg.cuh"
+#include "tma.cuh"
 
 namespace peec {
 
@@ -424,6 +425,11 @@ struct PSpec {
   const void* ey;
   const void* ez;
   int c01[3], c02[3], c12[3];
+  // staged FP32 z pass: y/z-folded R (00, 11, 22, 01, 02, 12) and FP32 phase tables
+  const float* y[6];
+  const c32* ex32;
+  const c32* ey32;
+  const c32* ez32;
 };
 
 template <typename R>
@@ -744,6 +750,406 @@ __global__ void __launch_bounds__(ZTPB, 4) k_zconv1(cx<R>* T0, int nz0, const vo
   qpick<Q0, QCap<R>::XY>(p.q[0], [&](auto QC) { col_last_inv<R, decltype(QC)::value>(buf, Tg, pl, ncols, nz0, p, W); });
 }
 
+// --------------------------------------------------------------------------- staged z passes
+// FP32 z passes over persistent CTAs that walk the tiles (one ky row, 16 kx columns) in a
+// grid-stride loop. One warp stages the next tile's occupied z rows of every family into a
+// shared-memory buffer with bulk asynchronous copies (cp.async.bulk, 128-byte rows,
+// mbarrier completion) while the CTA computes the current tile, so HBM reads overlap the
+// FFT arithmetic instead of stalling it. The first group reads the staged rows; the
+// middle, fused and last groups are those of k_zconv3 / k_zconv1. Spectra come from the
+// y/z-folded FP32 tables (Spectrum::yz32), which stay largely resident in L2.
+// Bounded waits: a copy wait that runs out sets *err, waits once more (bounded) for the
+// copies in flight and ends the CTA.
+
+constexpr int ZWAIT_LIMIT = 1 << 20;
+
+// spectrum index of the tile's column col at z position pz in the y/z-folded tables
+struct YzIdx {
+  size_t rowbase;  // fold(ky) * (Lz/2 + 1) * Lx + kx0
+  int Lx, nz;
+  __device__ __forceinline__ size_t at(int col, int pz) const {
+    return rowbase + (size_t)fold_pos(pz, nz) * Lx + col;
+  }
+};
+
+__device__ __forceinline__ YzIdx make_yzidx(int Lx, int Ly, int Lz, int kx0, int ky) {
+  YzIdx y;
+  y.Lx = Lx;
+  y.nz = ilog2(Lz);
+  y.rowbase = (size_t)fold_pos(ky, ilog2(Ly)) * (Lz / 2 + 1) * Lx + kx0;
+  return y;
+}
+
+__device__ __forceinline__ void pspec_apply_yz(const PSpec& S, const YzIdx& Y, int col, int pz,
+                                               const c32& ex, const c32& ey, c32& a0, c32& a1,
+                                               c32& a2) {
+  const size_t i = Y.at(col, pz);
+  const c32 ez = S.ez32[pz];
+  const c32 c01 = cscale(shift_phase<float>(S.c01, ex, ey, ez), __ldg(S.y[3] + i));
+  const c32 c02 = cscale(shift_phase<float>(S.c02, ex, ey, ez), __ldg(S.y[4] + i));
+  const c32 c12 = cscale(shift_phase<float>(S.c12, ex, ey, ez), __ldg(S.y[5] + i));
+  const float d00 = __ldg(S.y[0] + i), d11 = __ldg(S.y[1] + i), d22 = __ldg(S.y[2] + i);
+  const c32 b0 = cscale(a0, d00) + c01 * a1 + c02 * a2;
+  const c32 b1 = cmulc(a0, c01) + cscale(a1, d11) + c12 * a2;
+  const c32 b2 = cmulc(a0, c02) + cmulc(a1, c12) + cscale(a2, d22);
+  a0 = b0;
+  a1 = b1;
+  a2 = b2;
+}
+
+// forward first group from the staged rows (row < nz; zero beyond) into the tile
+template <int Q>
+__device__ __forceinline__ void stg_first_fwd(const c32* stg, int nz, c32* buf, const AxPlan& p,
+                                              const c32* W) {
+  constexpr int N = 1 << Q;
+  const int lh = p.n - Q;
+  const int tasks = TX << lh;
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int col = t & (TX - 1);
+    const int k = t >> LTX;
+    c32 v[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+      const int row = k + (r << lh);
+      v[r] = row < nz ? stg[(row << LTX) + col] : mk<float>(0, 0);
+    }
+    dft_dif<float, Q>(v);
+    group_twiddle<float, Q, false>(v, k, 0, W);
+#pragma unroll
+    for (int r = 0; r < N; ++r) buf[((k + (r << lh)) << LTX) + col] = v[r];
+  }
+}
+
+// fused middle step of the three face families with the y/z-folded spectra
+template <int Q>
+__device__ __forceinline__ void z3_fused_yz(c32* buf, size_t tsz, const AxPlan& p,
+                                            const PSpec& S, const YzIdx& Y, int kx0,
+                                            const c32& ey) {
+  constexpr int N = 1 << Q;
+  const int tasks = TX << (p.n - Q);
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int col = t & (TX - 1);
+    const int start = (t >> LTX) << Q;
+    c32 v[3][N];
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+#pragma unroll
+      for (int r = 0; r < N; ++r) v[f][r] = buf[f * tsz + ((start + r) << LTX) + col];
+      dft_dif<float, Q>(v[f]);
+    }
+    const c32 ex = S.ex32[kx0 + col];
+#pragma unroll
+    for (int r = 0; r < N; ++r) pspec_apply_yz(S, Y, col, start + r, ex, ey, v[0][r], v[1][r], v[2][r]);
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      dft_dit<float, Q>(v[f]);
+#pragma unroll
+      for (int r = 0; r < N; ++r) buf[f * tsz + ((start + r) << LTX) + col] = v[f][r];
+    }
+  }
+}
+
+// fused middle step of one edge family (real y/z-folded spectrum)
+template <int Q>
+__device__ __forceinline__ void z1_fused_yz(c32* buf, const AxPlan& p, const float* __restrict__ sy,
+                                            const YzIdx& Y) {
+  constexpr int N = 1 << Q;
+  const int tasks = TX << (p.n - Q);
+  for (int t = threadIdx.x; t < tasks; t += blockDim.x) {
+    const int col = t & (TX - 1);
+    const int start = (t >> LTX) << Q;
+    c32 v[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) v[r] = buf[((start + r) << LTX) + col];
+    dft_dif<float, Q>(v);
+#pragma unroll
+    for (int r = 0; r < N; ++r) v[r] = cscale(v[r], __ldg(sy + Y.at(col, start + r)));
+    dft_dit<float, Q>(v);
+#pragma unroll
+    for (int r = 0; r < N; ++r) buf[((start + r) << LTX) + col] = v[r];
+  }
+}
+
+// One family's pencil rows of a tile, for the staging warp.
+struct StageSrc {
+  const c32* T;  // family buffer at the tile's (ky, kx0)
+  int nz;        // occupied z rows
+};
+
+// the staging warp (warp 0): arm the barrier with the tile's bytes, then one bulk copy
+// per staged row, lanes striding over the rows
+__device__ __forceinline__ void stage_tile(uint64_t* bar, c32* stg, int nzs, const StageSrc* src,
+                                           int nfam, size_t pl) {
+  const int lane = threadIdx.x & 31;
+  uint32_t bytes = 0;
+  for (int f = 0; f < nfam; ++f) bytes += (uint32_t)src[f].nz * (TX * sizeof(c32));
+  if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
+  __syncwarp();
+  for (int f = 0; f < nfam; ++f)
+    for (int z = lane; z < src[f].nz; z += 32)
+      bulk_g2s(stg + ((size_t)f * nzs + z) * TX, src[f].T + (size_t)z * pl, TX * sizeof(c32), bar);
+}
+
+// every thread waits for the staged tile; false (for all threads alike) if any wait ran
+// into its limit, after the copies in flight were waited for once more
+__device__ __forceinline__ bool stage_wait(uint64_t* bar, uint32_t parity, int* err) {
+  const bool ok = mbar_wait_bounded(bar, parity, ZWAIT_LIMIT);
+  if (__syncthreads_and(ok)) return true;
+  if (threadIdx.x == 0) atomicExch(err, 1);
+  mbar_wait_bounded(bar, parity, ZWAIT_LIMIT);
+  return false;
+}
+
+template <int Q0, int QL>
+__global__ void __launch_bounds__(ZTPB, 3) k_zconv3_staged(c32* T0, c32* T1, c32* T2, int nz0,
+                                                           int nz1, int nz2, int nzs, PSpec S,
+                                                           int Lx, int Ly, AxPlan p,
+                                                           const c32* __restrict__ twm,
+                                                           int twmax, int ntiles, int* err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int Lz = 1 << p.n;
+  const size_t tsz = (size_t)Lz << LTX;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  c32* W = reinterpret_cast<c32*>(smem_raw + 128);
+  c32* buf = W + Lz;             // three work tiles, family f at buf + f*tsz
+  c32* stg = buf + 3 * tsz;      // staged rows, family f at stg + f*nzs*TX
+  const int ntx = Lx >> LTX;
+  const size_t pl = (size_t)Ly * Lx;
+  c32* Tf[3] = {T0, T1, T2};
+  const int nzf[3] = {nz0, nz1, nz2};
+  auto sources = [&](int tile, StageSrc* src) {
+    const size_t off = (size_t)(tile / ntx) * Lx + ((tile % ntx) << LTX);
+    for (int f = 0; f < 3; ++f) src[f] = StageSrc{Tf[f] + off, nzf[f]};
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  int tile = blockIdx.x;
+  if (threadIdx.x < 32 && tile < ntiles) {
+    StageSrc src[3];
+    sources(tile, src);
+    stage_tile(bar, stg, nzs, src, 3, pl);
+  }
+  load_twiddles<float>(W, twm, twmax, Lz);
+  __syncthreads();
+  uint32_t parity = 0;
+  for (; tile < ntiles; tile += gridDim.x) {
+    const int ky = tile / ntx, kx0 = (tile % ntx) << LTX;
+    if (!stage_wait(bar, parity, err)) return;
+    parity ^= 1u;
+    qpick<Q0, QCap<float>::XY>(p.q[0], [&](auto QC) {
+      stg_first_fwd<decltype(QC)::value>(stg, nz0, buf, p, W);
+      stg_first_fwd<decltype(QC)::value>(stg + (size_t)nzs * TX, nz1, buf + tsz, p, W);
+      stg_first_fwd<decltype(QC)::value>(stg + 2 * (size_t)nzs * TX, nz2, buf + 2 * tsz, p, W);
+    });
+    __syncthreads();
+    // the stage is free: fetch the next tile while this one computes
+    const int next = tile + gridDim.x;
+    if (threadIdx.x < 32 && next < ntiles) {
+      fence_proxy_async_smem();
+      StageSrc src[3];
+      sources(next, src);
+      stage_tile(bar, stg, nzs, src, 3, pl);
+    }
+    {
+      int s = p.q[0];
+      for (int g = 1; g + 1 < p.ng; ++g) {
+        smem_group_q<float, false, LTX>(buf, TX, p.q[g], p.n, s, W);
+        smem_group_q<float, false, LTX>(buf + tsz, TX, p.q[g], p.n, s, W);
+        smem_group_q<float, false, LTX>(buf + 2 * tsz, TX, p.q[g], p.n, s, W);
+        s += p.q[g];
+        __syncthreads();
+      }
+    }
+    const YzIdx Y = make_yzidx(Lx, Ly, Lz, kx0, ky);
+    const c32 ey = S.ey32[ky];
+    qpick<QL, QCap<float>::Z3>(p.q[p.ng - 1], [&](auto QC) {
+      z3_fused_yz<decltype(QC)::value>(buf, tsz, p, S, Y, kx0, ey);
+    });
+    __syncthreads();
+    {
+      int s = p.n - p.q[p.ng - 1];
+      for (int g = p.ng - 2; g >= 1; --g) {
+        s -= p.q[g];
+        smem_group_q<float, true, LTX>(buf, TX, p.q[g], p.n, s, W);
+        smem_group_q<float, true, LTX>(buf + tsz, TX, p.q[g], p.n, s, W);
+        smem_group_q<float, true, LTX>(buf + 2 * tsz, TX, p.q[g], p.n, s, W);
+        __syncthreads();
+      }
+    }
+    const size_t off = (size_t)ky * Lx + kx0;
+    qpick<Q0, QCap<float>::XY>(p.q[0], [&](auto QC) {
+      col_last_inv<float, decltype(QC)::value>(buf, T0 + off, pl, TX, nz0, p, W);
+      col_last_inv<float, decltype(QC)::value>(buf + tsz, T1 + off, pl, TX, nz1, p, W);
+      col_last_inv<float, decltype(QC)::value>(buf + 2 * tsz, T2 + off, pl, TX, nz2, p, W);
+    });
+    __syncthreads();  // the work tiles are rewritten by the next tile's first group
+  }
+}
+
+// the edge families' z passes in one launch; all share one circulant grid (Lx, Ly, Lz)
+struct EdgeSet {
+  c32* T[3];
+  int nz[3];
+  const float* sy[3];
+  int nf;
+};
+
+template <int Q0, int QL>
+__global__ void __launch_bounds__(ZTPB, 4) k_zedge_staged(EdgeSet E, int nzs, int Lx, int Ly,
+                                                          AxPlan p, const c32* __restrict__ twm,
+                                                          int twmax, int tiles_per_fam,
+                                                          int* err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int Lz = 1 << p.n;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  c32* W = reinterpret_cast<c32*>(smem_raw + 128);
+  c32* buf = W + Lz;
+  c32* stg = buf + ((size_t)Lz << LTX);
+  const int ntx = Lx >> LTX;
+  const size_t pl = (size_t)Ly * Lx;
+  const int ntiles = tiles_per_fam * E.nf;
+  auto source = [&](int tile, StageSrc* src) {
+    const int f = tile / tiles_per_fam, t = tile - f * tiles_per_fam;
+    const size_t off = (size_t)(t / ntx) * Lx + ((t % ntx) << LTX);
+    src[0] = StageSrc{E.T[f] + off, E.nz[f]};
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  int tile = blockIdx.x;
+  if (threadIdx.x < 32 && tile < ntiles) {
+    StageSrc src[1];
+    source(tile, src);
+    stage_tile(bar, stg, nzs, src, 1, pl);
+  }
+  load_twiddles<float>(W, twm, twmax, Lz);
+  __syncthreads();
+  uint32_t parity = 0;
+  for (; tile < ntiles; tile += gridDim.x) {
+    const int f = tile / tiles_per_fam, t = tile - f * tiles_per_fam;
+    const int ky = t / ntx, kx0 = (t % ntx) << LTX;
+    const int nz = E.nz[f];
+    if (!stage_wait(bar, parity, err)) return;
+    parity ^= 1u;
+    qpick<Q0, QCap<float>::XY>(p.q[0], [&](auto QC) {
+      stg_first_fwd<decltype(QC)::value>(stg, nz, buf, p, W);
+    });
+    __syncthreads();
+    const int next = tile + gridDim.x;
+    if (threadIdx.x < 32 && next < ntiles) {
+      fence_proxy_async_smem();
+      StageSrc src[1];
+      source(next, src);
+      stage_tile(bar, stg, nzs, src, 1, pl);
+    }
+    middle_groups<float, false, LTX>(buf, TX, p, W);
+    const YzIdx Y = make_yzidx(Lx, Ly, Lz, kx0, ky);
+    qpick<QL, QCap<float>::Z1>(p.q[p.ng - 1], [&](auto QC) {
+      z1_fused_yz<decltype(QC)::value>(buf, p, E.sy[f], Y);
+    });
+    __syncthreads();
+    middle_groups<float, true, LTX>(buf, TX, p, W);
+    const size_t off = (size_t)ky * Lx + kx0;
+    qpick<Q0, QCap<float>::XY>(p.q[0], [&](auto QC) {
+      col_last_inv<float, decltype(QC)::value>(buf, E.T[f] + off, pl, TX, nz, p, W);
+    });
+    __syncthreads();
+  }
+}
+
+// Register-direct FP32 z passes on the y/z-folded spectra (ZTune form 1): k_zconv3 /
+// k_zconv1 with the spectral step of the staged kernels; whole 16-column tiles.
+template <int Q0, int QL>
+__global__ void __launch_bounds__(ZTPB, 4) k_zconv3_yz(c32* T0, c32* T1, c32* T2, int nz0,
+                                                       int nz1, int nz2, PSpec S, int Lx, int Ly,
+                                                       AxPlan p, const c32* __restrict__ twm,
+                                                       int twmax) {
+  extern __shared__ unsigned char smem_raw[];
+  const int Lz = 1 << p.n;
+  const size_t tsz = (size_t)Lz << LTX;
+  c32* W = reinterpret_cast<c32*>(smem_raw);
+  c32* buf = W + Lz;
+  const int kx0 = blockIdx.x * TX, ky = blockIdx.y;
+  const size_t pl = (size_t)Ly * Lx;
+  const size_t off = (size_t)ky * Lx + kx0;
+  T0 += off;
+  T1 += off;
+  T2 += off;
+  load_twiddles<float>(W, twm, twmax, Lz);
+  __syncthreads();
+  qpick<Q0, QCap<float>::XY>(p.q[0], [&](auto QC) {
+    col_first_fwd<float, decltype(QC)::value>(T0, pl, TX, nz0, buf, p, W, T0);
+    col_first_fwd<float, decltype(QC)::value>(T1, pl, TX, nz1, buf + tsz, p, W, T1);
+    col_first_fwd<float, decltype(QC)::value>(T2, pl, TX, nz2, buf + 2 * tsz, p, W, T2);
+  });
+  __syncthreads();
+  {
+    int s = p.q[0];
+    for (int g = 1; g + 1 < p.ng; ++g) {
+      smem_group_q<float, false, LTX>(buf, TX, p.q[g], p.n, s, W);
+      smem_group_q<float, false, LTX>(buf + tsz, TX, p.q[g], p.n, s, W);
+      smem_group_q<float, false, LTX>(buf + 2 * tsz, TX, p.q[g], p.n, s, W);
+      s += p.q[g];
+      __syncthreads();
+    }
+  }
+  const YzIdx Y = make_yzidx(Lx, Ly, Lz, kx0, ky);
+  const c32 ey = S.ey32[ky];
+  qpick<QL, QCap<float>::Z3>(p.q[p.ng - 1], [&](auto QC) {
+    z3_fused_yz<decltype(QC)::value>(buf, tsz, p, S, Y, kx0, ey);
+  });
+  __syncthreads();
+  {
+    int s = p.n - p.q[p.ng - 1];
+    for (int g = p.ng - 2; g >= 1; --g) {
+      s -= p.q[g];
+      smem_group_q<float, true, LTX>(buf, TX, p.q[g], p.n, s, W);
+      smem_group_q<float, true, LTX>(buf + tsz, TX, p.q[g], p.n, s, W);
+      smem_group_q<float, true, LTX>(buf + 2 * tsz, TX, p.q[g], p.n, s, W);
+      __syncthreads();
+    }
+  }
+  qpick<Q0, QCap<float>::XY>(p.q[0], [&](auto QC) {
+    col_last_inv<float, decltype(QC)::value>(buf, T0, pl, TX, nz0, p, W);
+    col_last_inv<float, decltype(QC)::value>(buf + tsz, T1, pl, TX, nz1, p, W);
+    col_last_inv<float, decltype(QC)::value>(buf + 2 * tsz, T2, pl, TX, nz2, p, W);
+  });
+}
+
+template <int Q0, int QL>
+__global__ void __launch_bounds__(ZTPB, 4) k_zconv1_yz(c32* T0, int nz0, const float* __restrict__ sy,
+                                                       int Lx, int Ly, AxPlan p,
+                                                       const c32* __restrict__ twm, int twmax) {
+  extern __shared__ unsigned char smem_raw[];
+  const int Lz = 1 << p.n;
+  c32* W = reinterpret_cast<c32*>(smem_raw);
+  c32* buf = W + Lz;
+  const int kx0 = blockIdx.x * TX, ky = blockIdx.y;
+  const size_t pl = (size_t)Ly * Lx;
+  c32* Tg = T0 + (size_t)ky * Lx + kx0;
+  load_twiddles<float>(W, twm, twmax, Lz);
+  __syncthreads();
+  qpick<Q0, QCap<float>::XY>(p.q[0], [&](auto QC) {
+    col_first_fwd<float, decltype(QC)::value>(Tg, pl, TX, nz0, buf, p, W, Tg);
+  });
+  __syncthreads();
+  middle_groups<float, false, LTX>(buf, TX, p, W);
+  const YzIdx Y = make_yzidx(Lx, Ly, Lz, kx0, ky);
+  qpick<QL, QCap<float>::Z1>(p.q[p.ng - 1], [&](auto QC) {
+    z1_fused_yz<decltype(QC)::value>(buf, p, sy, Y);
+  });
+  __syncthreads();
+  middle_groups<float, true, LTX>(buf, TX, p, W);
+  qpick<Q0, QCap<float>::XY>(p.q[0], [&](auto QC) {
+    col_last_inv<float, decltype(QC)::value>(buf, Tg, pl, TX, nz0, p, W);
+  });
+}
+
 // --------------------------------------------------------------------------- host side
 
 // Dynamic shared memory above 48 KB needs a per-kernel opt-in. It is set once per
@@ -780,8 +1186,10 @@ struct Plans {
   static AxPlan z3(int n) {
     return QCap<R>::wide ? make_plan(n, 2, 4, 2) : make_plan(n, 3, 4, 3);
   }
-  static AxPlan z1(int n) {
-    return QCap<R>::wide ? make_plan(n, 3, 4, 3) : make_plan(n, 4, 4, 4);
+  // alt (FP32 only): the alternative edge plan the tuner may pick (first group 16 points)
+  static AxPlan z1(int n, int alt = 0) {
+    if (QCap<R>::wide) return make_plan(n, 3, 4, 3);
+    return alt ? make_plan(n, 4, 4, 3) : make_plan(n, 4, 4, 4);
   }
 };
 
@@ -859,13 +1267,17 @@ struct Launch {
                               F[2].dims[2], S, F[0].L[0], F[0].L[1], p, tw, twmax);
     return 0;
   }
-  static int zconv1(const Family& f, const void* s, const cx<R>* tw, int twmax, cudaStream_t st) {
+  static int zconv1(const Family& f, const void* s, const cx<R>* tw, int twmax, cudaStream_t st,
+                    int alt = 0) {
     const int Lz = f.L[2];
     const size_t sm = sizeof(cx<R>) * (Lz + ((size_t)Lz << LTX));
-    const AxPlan p = Plans<R>::z1(f.logL[2]);
+    const AxPlan p = Plans<R>::z1(f.logL[2], alt);
     constexpr int QL = QCap<R>::Z1;
-    const bool spec = p.ng >= 2 && p.q[0] == 4 && p.q[p.ng - 1] == QL;
-    auto kern = spec ? k_zconv1<R, 4, QL> : k_zconv1<R, 0, 0>;
+    const int q0 = p.q[0], ql = p.q[p.ng - 1];
+    auto kern = (p.ng >= 2 && q0 == 4 && ql == QL) ? k_zconv1<R, 4, QL>
+                : (p.ng >= 2 && q0 == 4 && ql == 3)  ? k_zconv1<R, 4, 3>
+                : (p.ng >= 2 && q0 == 3 && ql == QL) ? k_zconv1<R, 3, QL>
+                                                     : k_zconv1<R, 0, 0>;
     CTX_CHECK(smem_optin(kern, sm));
     dim3 g((f.L[0] + TX - 1) / TX, f.L[1]);
     kern<<<g, ZTPB, sm, st>>>(buf(f), f.dims[2], s, f.L[0], f.L[1], p, tw, twmax);
@@ -873,12 +1285,123 @@ struct Launch {
   }
 };
 
+// The FP32 z-pass forms (ZTune): direct on full-form spectra, direct on y/z-folded
+// spectra, staged. Templates, so that only the float instantiation compiles their kernels.
+template <typename R>
+static PSpec pspec_of(const Spectrum* spec, const void* const* ph) {
+  const int p = slot_of<R>();
+  PSpec S{spec[0].d[p], spec[1].d[p], spec[2].d[p], spec[3].d[p], spec[4].d[p], spec[5].d[p],
+          spec[0].oct,  spec[1].oct,  spec[2].oct,  spec[3].oct,  spec[4].oct,  spec[5].oct,
+          ph[0],        ph[1],        ph[2],        {},           {},           {}};
+  for (int a = 0; a < 3; ++a) {
+    S.c01[a] = spec[3].c[a];
+    S.c02[a] = spec[4].c[a];
+    S.c12[a] = spec[5].c[a];
+  }
+  if (std::is_same<R, float>::value) {
+    for (int i = 0; i < 6; ++i) S.y[i] = (const float*)spec[i].yz32;
+    S.ex32 = (const c32*)ph[3];
+    S.ey32 = (const c32*)ph[4];
+    S.ez32 = (const c32*)ph[5];
+  }
+  return S;
+}
+
+template <int UNUSED = 0>
+static int zface_f32(const Family* F, int nfam, const PSpec& S, const c32* tw, int twmax,
+                     const ZTune& zt, cudaStream_t st) {
+  const int form = zpass_yz_faces(F, nfam) ? zt.face : 0;
+  if (form == 0) return Launch<float>::zconv3(F, S, tw, twmax, st);
+  const int Lz = F[0].L[2], Lx = F[0].L[0], Ly = F[0].L[1];
+  const AxPlan p = Plans<float>::z3(F[0].logL[2]);
+  constexpr int QL = QCap<float>::Z3;
+  const bool spec = p.q[0] == 4 && p.q[p.ng - 1] == QL;
+  c32* T0 = Launch<float>::buf(F[0]);
+  c32* T1 = Launch<float>::buf(F[1]);
+  c32* T2 = Launch<float>::buf(F[2]);
+  if (form == 1) {
+    const size_t sm = sizeof(c32) * (Lz + 3 * ((size_t)Lz << LTX));
+    auto kern = spec ? k_zconv3_yz<4, QL> : k_zconv3_yz<0, 0>;
+    CTX_CHECK(smem_optin(kern, sm));
+    dim3 g(Lx >> LTX, Ly);
+    kern<<<g, ZTPB, sm, st>>>(T0, T1, T2, F[0].dims[2], F[1].dims[2], F[2].dims[2], S, Lx, Ly,
+                              p, tw, twmax);
+    return 0;
+  }
+  const int nzs = std::max(F[0].dims[2], std::max(F[1].dims[2], F[2].dims[2]));
+  const size_t sm = 128 + sizeof(c32) * (Lz + 3 * ((size_t)Lz << LTX) + 3 * (size_t)nzs * TX);
+  auto kern = spec ? k_zconv3_staged<4, QL> : k_zconv3_staged<0, 0>;
+  CTX_CHECK(smem_optin(kern, sm));
+  const int ntiles = (Lx >> LTX) * Ly;
+  const int per_sm = std::max(1, std::min(3, (int)((227 * 1024) / (sm + 1024))));
+  const int grid = std::min(ntiles, zt.nsm * per_sm);
+  kern<<<grid, ZTPB, sm, st>>>(T0, T1, T2, F[0].dims[2], F[1].dims[2], F[2].dims[2], nzs, S,
+                               Lx, Ly, p, tw, twmax, ntiles, zt.err);
+  return 0;
+}
+
+template <int UNUSED = 0>
+static int zedge_f32(const Family* F, int nfam, const Spectrum* spec, const c32* tw, int twmax,
+                     const ZTune& zt, cudaStream_t st) {
+  const int form = zpass_yz_edges(F, nfam) ? zt.edge : 0;
+  if (form < 2) {
+    for (int f = 3; f < nfam; ++f) {
+      if (!F[f].active) continue;
+      if (form == 0) {
+        CTX_CHECK(Launch<float>::zconv1(F[f], spec[3 + f].d[1], tw, twmax, st, zt.edge_plan));
+        continue;
+      }
+      const Family& fam = F[f];
+      const int Lz = fam.L[2];
+      const AxPlan p = Plans<float>::z1(fam.logL[2], zt.edge_plan);
+      const int q0 = p.q[0], ql = p.q[p.ng - 1];
+      auto kern = (q0 == 4 && ql == 3) ? k_zconv1_yz<4, 3>
+                  : (q0 == 3 && ql == 4) ? k_zconv1_yz<3, 4>
+                                         : k_zconv1_yz<0, 0>;
+      const size_t sm = sizeof(c32) * (Lz + ((size_t)Lz << LTX));
+      CTX_CHECK(smem_optin(kern, sm));
+      dim3 g(fam.L[0] >> LTX, fam.L[1]);
+      kern<<<g, ZTPB, sm, st>>>(Launch<float>::buf(fam), fam.dims[2],
+                                (const float*)spec[3 + f].yz32, fam.L[0], fam.L[1], p, tw,
+                                twmax);
+    }
+    return 0;
+  }
+  EdgeSet E{};
+  const Family* f0 = nullptr;
+  int nzs = 0;
+  for (int f = 3; f < nfam; ++f) {
+    if (!F[f].active) continue;
+    if (!f0) f0 = &F[f];
+    E.T[E.nf] = Launch<float>::buf(F[f]);
+    E.nz[E.nf] = F[f].dims[2];
+    E.sy[E.nf] = (const float*)spec[3 + f].yz32;
+    nzs = std::max(nzs, F[f].dims[2]);
+    ++E.nf;
+  }
+  if (!f0) return 0;
+  const int Lz = f0->L[2], Lx = f0->L[0], Ly = f0->L[1];
+  const AxPlan p = Plans<float>::z1(f0->logL[2], zt.edge_plan);
+  const size_t sm = 128 + sizeof(c32) * (Lz + ((size_t)Lz << LTX) + (size_t)nzs * TX);
+  const int q0 = p.q[0], ql = p.q[p.ng - 1];
+  auto kern = (q0 == 4 && ql == 3) ? k_zedge_staged<4, 3>
+              : (q0 == 3 && ql == 4) ? k_zedge_staged<3, 4>
+                                     : k_zedge_staged<0, 0>;
+  CTX_CHECK(smem_optin(kern, sm));
+  const int per_fam = (Lx >> LTX) * Ly;
+  const int per_sm = std::max(1, std::min(4, (int)((227 * 1024) / (sm + 1024))));
+  const int grid = std::min(per_fam * E.nf, zt.nsm * per_sm);
+  kern<<<grid, ZTPB, sm, st>>>(E, nzs, Lx, Ly, p, tw, twmax, per_fam, zt.err);
+  return 0;
+}
+
 // ev (nullable): 6 events bracketing the five pass classes
-// ph: the face grid's phase tables (x, y, z), complex FP64
+// ph: the face grid's phase tables (x, y, z), complex FP64, then complex FP32
+// zt (nullable): the FP32 z-pass forms (form 0 when null)
 template <typename R>
 int conv_all_t(const Family* F, int nfam, const Spectrum* spec, const void* const* ph,
                const c64* x, c64* LpI, c64* PQ, int64_t m, const cx<R>* tw, int twmax,
-               cudaStream_t st, cudaEvent_t* ev) {
+               cudaStream_t st, cudaEvent_t* ev, const ZTune* zt) {
   using Lc = Launch<R>;
   const int p = slot_of<R>();
   if (nfam > kMaxFam) return set_error("too many families"), PEEC_ERR_UNSUPPORTED_INTERNAL;
@@ -893,19 +1416,19 @@ int conv_all_t(const Family* F, int nfam, const Spectrum* spec, const void* cons
   if (ev) cudaEventRecord(ev[1], st);
   CTX_CHECK(Lc::pass(2, F, nfam, nullptr, tw, twmax, st));
   if (ev) cudaEventRecord(ev[2], st);
-  PSpec S{spec[0].d[p], spec[1].d[p], spec[2].d[p], spec[3].d[p], spec[4].d[p], spec[5].d[p],
-          spec[0].oct,  spec[1].oct,  spec[2].oct,  spec[3].oct,  spec[4].oct,  spec[5].oct,
-          ph[0],        ph[1],        ph[2],        {},           {},           {}};
-  for (int a = 0; a < 3; ++a) {
-    S.c01[a] = spec[3].c[a];
-    S.c02[a] = spec[4].c[a];
-    S.c12[a] = spec[5].c[a];
+  const PSpec S = pspec_of<R>(spec, ph);
+  if constexpr (std::is_same<R, float>::value) {
+    const ZTune z0{};
+    const ZTune& z = zt ? *zt : z0;
+    CTX_CHECK(zface_f32(F, nfam, S, tw, twmax, z, st));
+    CTX_CHECK(zedge_f32(F, nfam, spec, tw, twmax, z, st));
+  } else {
+    CTX_CHECK(Lc::zconv3(F, S, tw, twmax, st));
+    for (int f = 3; f < nfam; ++f)
+      if (F[f].active)
+        CTX_CHECK(Lc::zconv1(F[f], octant_spectra<R>() ? spec[3 + f].oct : spec[3 + f].d[p], tw,
+                             twmax, st));
   }
-  CTX_CHECK(Lc::zconv3(F, S, tw, twmax, st));
-  for (int f = 3; f < nfam; ++f)
-    if (F[f].active)
-      CTX_CHECK(Lc::zconv1(F[f], octant_spectra<R>() ? spec[3 + f].oct : spec[3 + f].d[p], tw,
-                           twmax, st));
   if (ev) cudaEventRecord(ev[3], st);
   CTX_CHECK(Lc::pass(3, F, nfam, nullptr, tw, twmax, st));
   if (ev) cudaEventRecord(ev[4], st);

@@ -244,6 +244,29 @@ class GpuOperator:
                         "edge": bool(kind.value)})
         return out
 
+    FORMS = ("direct", "direct_yz", "staged")
+
+    def zpass_tuning(self):
+        """The FP32 z-pass forms the autotuner picked (face, edge, edge radix plan) and the
+        ms it measured per candidate (None where a form was not a candidate)."""
+        ch = (ctypes.c_int * 3)()
+        fms = np.zeros(3)
+        ems = np.zeros(6)
+        _lib.check(self.h, self.L.peec_zpass_tuning(self.h, ch, fms.ctypes.data_as(_lib.DP),
+                                                    ems.ctypes.data_as(_lib.DP)))
+        opt = lambda v: None if v < 0 else float(v)
+        return {"face": self.FORMS[ch[0]], "edge": self.FORMS[ch[1]], "edge_plan": int(ch[2]),
+                "face_ms": {self.FORMS[i]: opt(fms[i]) for i in range(3)},
+                "edge_ms": {f"plan{p_}_{self.FORMS[i]}": opt(ems[3 * p_ + i])
+                            for p_ in range(2) for i in range(3)}}
+
+    def set_zpass_forms(self, face, edge, edge_plan=0):
+        """Pins the FP32 z-pass forms ("direct", "direct_yz", "staged" or 0..2) in place of
+        the tuner's choice until the next fill / set_rows."""
+        f = self.FORMS.index(face) if isinstance(face, str) else int(face)
+        e = self.FORMS.index(edge) if isinstance(edge, str) else int(edge)
+        _lib.check(self.h, self.L.peec_set_zpass_forms(self.h, f, e, int(edge_plan)))
+
     def profile_matvec(self, precision, iters=10):
         ms = (ctypes.c_double * 7)()
         _lib.check(self.h, self.L.peec_profile_matvec(self.h, int(precision), int(iters), ms))
