@@ -108,6 +108,34 @@ int peec_fill(peec_ctx* ctx, const double origin[3], double sx, double sy, doubl
               double escal_Lp, double escal_P, double* const rows_out[9]);
 
 /*
+ * Retarded operator (QS_Rcc_FW == 2, "Rcc"). Replaces compute_rows_Rcc_Lp /
+ * compute_rows_Rcc_P (compute_FFT_mutual_coupling_mats.jl:17-27) and the per-frequency
+ * compute_Circulant_Lp_Rcc / compute_Circulant_P_sup_Rcc calls of
+ * FFT_solver_QS_S_type.jl:61-93.
+ *
+ * peec_fill_rcc: GPU fill of the quasi-static parts of the nine Rcc rows, escaled, in
+ * the peec_set_rows order: the Lp rows through the Rcc path's own integral dispatch
+ * (compute_Lp_Voxels_QS.jl:8-397, Lp self entries zeroed), the P rows with the face
+ * types that path passes (the block indices, compute_rows_Rcc_P.jl:47-52). The rows stay
+ * on the device; rows_out as for peec_fill. An Lp entry in that dispatch's orthogonal
+ * surface-surface case, which the reference cannot evaluate (its call passes an
+ * interval where the integral takes a coordinate, compute_Lp_Voxels_QS.jl:330-352),
+ * returns PEEC_ERR_UNSUPPORTED.
+ * peec_set_rows_rcc: the same rows from the host (shared-fill parity runs), with the
+ * mesh geometry the centre distances need.
+ * peec_set_rcc_frequency: the spectra at freq_hz (Hz, unscaled): each row times
+ * exp(-i beta R), beta = 2 pi f sqrt(eps0 mu0), R the distance between centres (voxel
+ * centres for Lp, QS face centres for P; compute_Voxels_Rcc.jl, compute_P_vox_Rcc.jl).
+ * From then on operator applications, solves and port right-hand sides use the Rcc
+ * operator, until peec_set_rows / peec_fill install QS spectra again.
+ */
+int peec_fill_rcc(peec_ctx* ctx, const double origin[3], double sx, double sy, double sz,
+                  double escal_Lp, double escal_P, double* const rows_out[9]);
+int peec_set_rows_rcc(peec_ctx* ctx, const double* const rows[9], const double origin[3],
+                      double sx, double sy, double sz);
+int peec_set_rcc_frequency(peec_ctx* ctx, double freq_hz);
+
+/*
  * Per-frequency state (FFT_solver_QS_S_type.jl:105-119): scaled angular
  * frequency w, DZ[m] (complex), Yle as COO (complex values), and the sparse LU
  * factors of SS with Pr*diag(row_scale)*SS*Pc = L*U in CSR form (L lower, U upper;

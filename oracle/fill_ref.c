@@ -21,6 +21,9 @@
  *   src/lib/solverFFT/compute_row_P_sup.jl:383-394 check_condition_P_P
  *   src/lib/solverFFT/compute_row_P_sup.jl:396-590 primitives (integ_*_P)
  *   src/lib/solverFFT/compute_Lp_Voxels_QS.jl:695-730 integ_surf_surf_para
+ *   src/lib/solverFFT/compute_Lp_Voxels_QS.jl:8-397 compute_Lp_Voxels_QS and its
+ *     Integ_vol_vol dispatch, the Lp rows of the Rcc path (compute_rows_Rcc_Lp.jl:20-35),
+ *     with that file's integ_line_line_sp (:501-520) and integ_vol_surf (:777-824)
  * Every branch of both dispatches is restated, including the far-field ones that
  * replace a body by a surface, a line or a point once a dimension passes its
  * suppression test (on uniform voxels: centre distances beyond ~200 edges of that
@@ -178,8 +181,14 @@ static REAL ll_sp(const REAL* x1v, const REAL* x2v, int pform, REAL* acc) {
     for (int c2 = 0; c2 < 2; ++c2) {
       REAL x1 = x1v[c1], x2 = x2v[c2];
       REAL R = SQRT((x1 - x2) * (x1 - x2));
-      REAL t1 = (x1 - x2) / R * (x1 - x2 * lg(x2 - x1));
-      if (pform) t1 = t1 + x1 * lg(x1 - x2);
+      REAL t1;
+      if (pform == 2) /* integ_line_line_sp (compute_Lp_Voxels_QS.jl:501-520): the
+                         x1*log|x1-x2| term inside the (x1-x2)/R factor */
+        t1 = (x1 - x2) / R * (x1 - x2 * lg(x2 - x1) + x1 * lg(x1 - x2));
+      else {
+        t1 = (x1 - x2) / R * (x1 - x2 * lg(x2 - x1));
+        if (pform) t1 = t1 + x1 * lg(x1 - x2);
+      }
       t1 = fin(t1);
       sol += sgnp(c1 + c2 + 1) * t1;
       *acc += FABS(t1);
@@ -372,10 +381,11 @@ static REAL ss_ortho(const REAL* x1v, const REAL* y1v, REAL z1, const REAL* x2v,
   return sol;
 }
 
-/* integ_vol_surf_fft (compute_Lp_Voxels.jl:728-764): volume, surface in the (x, y)
- * plane at z2 */
+/* integ_vol_surf_fft (compute_Lp_Voxels.jl:728-764) and, with pform == 2,
+ * integ_vol_surf (compute_Lp_Voxels_QS.jl:777-824, whose second and third terms carry an
+ * extra factor (z1 - z2)): volume, surface in the (x, y) plane at z2 */
 static REAL vol_surf(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REAL* x2v,
-                     const REAL* y2v, REAL z2, REAL* acc) {
+                     const REAL* y2v, REAL z2, int pform, REAL* acc) {
   REAL sol = 0;
   for (int c1 = 0; c1 < 2; ++c1)
     for (int c2 = 0; c2 < 2; ++c2)
@@ -386,8 +396,10 @@ static REAL vol_surf(const REAL* x1v, const REAL* y1v, const REAL* z1v, const RE
             REAL X2 = X * X, Y2 = Y * Y, Z2 = Z * Z;
             REAL R = SQRT(X2 + Y2 + Z2);
             REAL t1 = (Z2 / 12 - (X2 + Y2) / 8) * Z * R;
-            REAL t2 = fin((Y2 / 2 - Z2 / 6) * X * lg(X + R));
-            REAL t3 = fin((X2 / 2 - Z2 / 6) * Y * lg(Y + R));
+            REAL t2 = pform == 2 ? fin((Y2 / 2 - Z2 / 6) * X * Z * lg(X + R))
+                                 : fin((Y2 / 2 - Z2 / 6) * X * lg(X + R));
+            REAL t3 = pform == 2 ? fin((X2 / 2 - Z2 / 6) * Y * Z * lg(Y + R))
+                                 : fin((X2 / 2 - Z2 / 6) * Y * lg(Y + R));
             REAL t4 = fin((-(X2 * X2) / 24 - (Y2 * Y2) / 24 + (Y2 * X2) / 4) * lg(Z + R));
             REAL t5 = -(FABS(X) * FABS(X) * FABS(X)) * Y / 6 * ATAN2(Y * Z, FABS(X) * R);
             REAL t6 = -X * (FABS(Y) * FABS(Y) * FABS(Y)) / 6 * ATAN2(X * Z, FABS(Y) * R);
@@ -440,12 +452,17 @@ static void lp_supp(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REA
   }
 }
 
-/* The case tree shared by Integ_vol_vol_fft (compute_Lp_Voxels.jl:172-433) and
- * Integ_sup_sup_P (compute_row_P_sup.jl:175-379): the integral of 1/R over two boxes
- * (intervals x1v.., centres xc1.., edge lengths a1..) of which the dimensions flagged in
- * s1 / s2 are collapsed, each collapsed length entering as a factor. The P tree has no
- * volume cases, calls the _P primitives (pform = 1) and passes unit lengths for the
- * face normals. */
+/* The case tree shared by Integ_vol_vol_fft (compute_Lp_Voxels.jl:172-433),
+ * Integ_sup_sup_P (compute_row_P_sup.jl:175-379) and Integ_vol_vol
+ * (compute_Lp_Voxels_QS.jl:167-393, the Rcc path's Lp dispatcher): the integral of 1/R
+ * over two boxes (intervals x1v.., centres xc1.., edge lengths a1..) of which the
+ * dimensions flagged in s1 / s2 are collapsed, each collapsed length entering as a
+ * factor. The P tree has no volume cases, calls the _P primitives (pform = 1) and passes
+ * unit lengths for the face normals. pform = 2 is the Rcc tree: the six-term
+ * integ_line_surf_ortho, its own integ_line_line_sp and integ_vol_surf, and in the
+ * orthogonal surface-surface case a call whose arguments Julia cannot apply (an
+ * interval where the primitive takes a coordinate, compute_Lp_Voxels_QS.jl:330-352):
+ * that entry returns NaN and the row driver counts it. */
 static REAL integ_bodies(const REAL* x1v, const REAL* y1v, const REAL* z1v, REAL xc1, REAL yc1,
                          REAL zc1, REAL a1, REAL b1, REAL c1, const REAL* x2v, const REAL* y2v,
                          const REAL* z2v, REAL xc2, REAL yc2, REAL zc2, REAL a2, REAL b2,
@@ -539,6 +556,7 @@ static REAL integ_bodies(const REAL* x1v, const REAL* y1v, const REAL* z1v, REAL
     }
     case 2: {
       REAL v;
+#define SSO(a, b, c, d, e, f) (pform == 2 ? (REAL)NAN : ss_ortho(a, b, c, d, e, f, pform, acc))
       if (n1 == 2) { /* line 1, volume 2 */
         if (!s1[0]) { w = b1 * c1; v = line_vol(x2v, y2v, z2v, x1v, yc1, zc1, acc); }
         else if (!s1[1]) { w = a1 * c1; v = line_vol(y2v, x2v, z2v, y1v, xc1, zc1, acc); }
@@ -549,28 +567,29 @@ static REAL integ_bodies(const REAL* x1v, const REAL* y1v, const REAL* z1v, REAL
         else { w = a2 * b2; v = line_vol(z1v, x1v, y1v, z2v, xc2, yc2, acc); }
       } else if (s1[0]) { /* surface-surface, surface 1 in the yz plane */
         if (s2[0]) { w = a1 * a2; v = ss_para(y1v, z1v, xc1, y2v, z2v, xc2, acc); }
-        else if (s2[1]) { w = a1 * b2; v = ss_ortho(z1v, y1v, xc1, z2v, yc2, x2v, pform, acc); }
-        else { w = a1 * c2; v = ss_ortho(y1v, z1v, xc1, y2v, zc2, x2v, pform, acc); }
+        else if (s2[1]) { w = a1 * b2; v = SSO(z1v, y1v, xc1, z2v, yc2, x2v); }
+        else { w = a1 * c2; v = SSO(y1v, z1v, xc1, y2v, zc2, x2v); }
       } else if (s1[1]) {
-        if (s2[0]) { w = b1 * a2; v = ss_ortho(z1v, x1v, yc1, z2v, xc2, y2v, pform, acc); }
+        if (s2[0]) { w = b1 * a2; v = SSO(z1v, x1v, yc1, z2v, xc2, y2v); }
         else if (s2[1]) { w = b1 * b2; v = ss_para(x1v, z1v, yc1, x2v, z2v, yc2, acc); }
-        else { w = b1 * c2; v = ss_ortho(x1v, z1v, yc1, x2v, zc2, y2v, pform, acc); }
+        else { w = b1 * c2; v = SSO(x1v, z1v, yc1, x2v, zc2, y2v); }
       } else {
-        if (s2[0]) { w = c1 * a2; v = ss_ortho(y1v, x1v, zc1, y2v, xc2, z2v, pform, acc); }
-        else if (s2[1]) { w = c1 * b2; v = ss_ortho(x1v, y1v, zc1, x2v, yc2, z2v, pform, acc); }
+        if (s2[0]) { w = c1 * a2; v = SSO(y1v, x1v, zc1, y2v, xc2, z2v); }
+        else if (s2[1]) { w = c1 * b2; v = SSO(x1v, y1v, zc1, x2v, yc2, z2v); }
         else { w = c1 * c2; v = ss_para(x1v, y1v, zc1, x2v, y2v, zc2, acc); }
       }
+#undef SSO
       *acc *= FABS(w);
       return w * v;
     }
     case 1: {
       REAL v;
-      if (s1[0]) { w = a1; v = vol_surf(y2v, z2v, x2v, y1v, z1v, xc1, acc); }
-      else if (s1[1]) { w = b1; v = vol_surf(x2v, z2v, y2v, x1v, z1v, yc1, acc); }
-      else if (s1[2]) { w = c1; v = vol_surf(x2v, y2v, z2v, x1v, y1v, zc1, acc); }
-      else if (s2[0]) { w = a2; v = vol_surf(y1v, z1v, x1v, y2v, z2v, xc2, acc); }
-      else if (s2[1]) { w = b2; v = vol_surf(x1v, z1v, y1v, x2v, z2v, yc2, acc); }
-      else { w = c2; v = vol_surf(x1v, y1v, z1v, x2v, y2v, zc2, acc); }
+      if (s1[0]) { w = a1; v = vol_surf(y2v, z2v, x2v, y1v, z1v, xc1, pform, acc); }
+      else if (s1[1]) { w = b1; v = vol_surf(x2v, z2v, y2v, x1v, z1v, yc1, pform, acc); }
+      else if (s1[2]) { w = c1; v = vol_surf(x2v, y2v, z2v, x1v, y1v, zc1, pform, acc); }
+      else if (s2[0]) { w = a2; v = vol_surf(y1v, z1v, x1v, y2v, z2v, xc2, pform, acc); }
+      else if (s2[1]) { w = b2; v = vol_surf(x1v, z1v, y1v, x2v, z2v, yc2, pform, acc); }
+      else { w = c2; v = vol_surf(x1v, y1v, z1v, x2v, y2v, zc2, pform, acc); }
       *acc *= FABS(w);
       return w * v;
     }
@@ -582,7 +601,8 @@ static REAL integ_bodies(const REAL* x1v, const REAL* y1v, const REAL* z1v, REAL
 /* Integ_vol_vol_fft (compute_Lp_Voxels.jl:65-435). *far = 1 when a suppressed branch
  * was taken; suppress == 0 skips the tests (the full volume-volume form). */
 static REAL lp_integ(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REAL* x2v,
-                     const REAL* y2v, const REAL* z2v, int suppress, REAL* acc, int* far) {
+                     const REAL* y2v, const REAL* z2v, int suppress, int form, REAL* acc,
+                     int* far) {
   REAL xc1 = (REAL)0.5 * (x1v[0] + x1v[1]), yc1 = (REAL)0.5 * (y1v[0] + y1v[1]),
        zc1 = (REAL)0.5 * (z1v[0] + z1v[1]);
   REAL xc2 = (REAL)0.5 * (x2v[0] + x2v[1]), yc2 = (REAL)0.5 * (y2v[0] + y2v[1]),
@@ -592,17 +612,19 @@ static REAL lp_integ(const REAL* x1v, const REAL* y1v, const REAL* z1v, const RE
   int s1[3] = {0, 0, 0}, s2[3] = {0, 0, 0};
   if (suppress) lp_supp(x1v, y1v, z1v, x2v, y2v, z2v, s1, s2);
   *far = s1[0] + s1[1] + s1[2] + s2[0] + s2[1] + s2[2] > 0;
+  /* the Rcc dispatcher's volume-volume case calls Integ_vol_vol_fft, whose identical
+     suppression tests again find nothing collapsed: the same volume-volume closed form */
   return integ_bodies(x1v, y1v, z1v, xc1, yc1, zc1, a1, b1, c1, x2v, y2v, z2v, xc2, yc2, zc2, a2,
-                      b2, c2, s1, s2, 0, acc);
+                      b2, c2, s1, s2, form, acc);
 }
 
 /* One Lp generating row: source centre src, targets centers[N][3] (row-major),
  * current direction dc = 1,2,3. out[k] = 1e-7/S * integral (compute_Lp_Voxels.jl:40-60),
  * scale[k] = the same prefactor times sum|terms|. Returns the count of entries
  * that took a far-field (suppressed) branch. */
-int64_t FN(oracle_lp_row)(int dc, const double* src, const double* centers, int64_t N,
-                          double sx_, double sy_, double sz_, int suppress, double* out,
-                          double* scale) {
+static int64_t lp_row_form(int dc, const double* src, const double* centers, int64_t N,
+                           double sx_, double sy_, double sz_, int suppress, int form, double* out,
+                           double* scale) {
   REAL sx = sx_, sy = sy_, sz = sz_;
   REAL S = sy * sz * sy * sz;
   if (dc == 2) S = sx * sz * sx * sz;
@@ -620,12 +642,26 @@ int64_t FN(oracle_lp_row)(int dc, const double* src, const double* centers, int6
     REAL z2v[2] = {round14(cz - sz / 2), round14(cz + sz / 2)};
     REAL acc;
     int far = 0;
-    REAL v = lp_integ(x1v, y1v, z1v, x2v, y2v, z2v, suppress, &acc, &far);
+    REAL v = lp_integ(x1v, y1v, z1v, x2v, y2v, z2v, suppress, form, &acc, &far);
     bad += far;
     out[k] = (double)((REAL)1e-7 / S * v);
     if (scale) scale[k] = (double)((REAL)1e-7 / S * acc);
   }
   return bad;
+}
+
+int64_t FN(oracle_lp_row)(int dc, const double* src, const double* centers, int64_t N,
+                          double sx_, double sy_, double sz_, int suppress, double* out,
+                          double* scale) {
+  return lp_row_form(dc, src, centers, N, sx_, sy_, sz_, suppress, 0, out, scale);
+}
+
+/* compute_Lp_Voxels_QS (compute_Lp_Voxels_QS.jl:8-42), the Rcc path's Lp row: the same
+ * driver over the Integ_vol_vol dispatcher (pform 2). Entries in its orthogonal
+ * surface-surface case, where the reference raises, come back NaN. */
+int64_t FN(oracle_lp_row_qs)(int dc, const double* src, const double* centers, int64_t N,
+                             double sx_, double sy_, double sz_, double* out, double* scale) {
+  return lp_row_form(dc, src, centers, N, sx_, sy_, sz_, 1, 2, out, scale);
 }
 
 static int check_pp(REAL e1, REAL e2, REAL e3, REAL e4, REAL S1, REAL S2, REAL max_d, REAL min_R,

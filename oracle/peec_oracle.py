@@ -61,6 +61,11 @@ def _fill_lib():
             f.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                           ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                           ctypes.c_void_p, ctypes.c_void_p]
+            q = getattr(lib, "oracle_lp_row_qs" + sfx)
+            q.restype = ctypes.c_int64
+            q.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                          ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p,
+                          ctypes.c_void_p]
             g = getattr(lib, "oracle_p_row" + sfx)
             g.restype = ctypes.c_int64
             g.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,

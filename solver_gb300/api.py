@@ -36,6 +36,13 @@ class CirculantSpectra:
         self.rows = rows
 
 
+class RccRows(CirculantSpectra):
+    """Device-resident quasi-static parts of the nine Rcc rows with their centre distances
+    (the handle returned as FFTCP and FFTCLp for QS_Rcc_FW == 2; the reference returns
+    the rows_P / rows_Lp dictionaries, compute_FFT_mutual_coupling_mats.jl:17-27). The
+    sweep builds the spectra of every frequency from them on the GPU."""
+
+
 def get_operator(incidence_selection, expansions, diagonals, device=0) -> GpuOperator:
     op = expansions.get("gpu_ctx")
     if op is None or op.h is None:
@@ -64,6 +71,9 @@ def rows_from_reference_spectra(FFTCP, FFTCLp, grid):
 
 
 def _ensure_spectra(op, FFTCP, FFTCLp):
+    if isinstance(FFTCP, RccRows):
+        raise ValueError("Rcc rows hold no spectra of their own: the sweep builds them per "
+                         "frequency (FFT_solver_QS_S_type with QS_Rcc_FW=2)")
     if isinstance(FFTCP, CirculantSpectra):
         if FFTCP.op is not op:
             raise ValueError("spectra belong to another operator context")
@@ -80,12 +90,21 @@ def compute_FFT_mutual_coupling_mats(circulant_centers, escalings, Nx, Ny, Nz, Q
                                      expansions=None, diagonals=None, return_rows=False):
     """GPU fill of the Lp/P generating rows and their spectra. Returns
     (FFTCP, FFTCLp) as one device handle (the reference returns host spectra).
-    The operator context is taken from / stored in ``expansions``."""
-    if QS_Rcc_FW != 1:
-        raise NotImplementedError("only the quasi-static fill (QS_Rcc_FW == 1) is implemented")
+    The operator context is taken from / stored in ``expansions``.
+    QS_Rcc_FW == 2: the quasi-static parts of the retarded operator's rows
+    (compute_rows_Rcc_P, compute_rows_Rcc_Lp), kept on the device as an RccRows handle."""
+    if QS_Rcc_FW not in (1, 2):
+        raise NotImplementedError("QS_Rcc_FW must be 1 (quasi-static) or 2 (Rcc); the "
+                                  "reference's Taylor variant (3) is commented out")
     op = get_operator(incidence_selection, expansions, diagonals)
     if tuple(op.grid) != (Nx, Ny, Nz):
         raise ValueError("grid does not match the operator's topology")
+    if QS_Rcc_FW == 2:
+        rows = op.fill_rcc(circulant_centers["origin"], circulant_centers["sx"],
+                           circulant_centers["sy"], circulant_centers["sz"], escalings["Lp"],
+                           escalings["P"])
+        h = RccRows(op, rows if return_rows else None)
+        return h, h
     rows = op.fill(circulant_centers["origin"], circulant_centers["sx"], circulant_centers["sy"],
                    circulant_centers["sz"], escalings["Lp"], escalings["P"],
                    return_rows=return_rows)
@@ -181,7 +200,7 @@ class PortLanes:
         return out
 
     def sweep(self, seq, get_state, release, pn, Is, Vrest, tol_of, solve_kw, record,
-              stop_flag=None, mode="mixed"):
+              stop_flag=None, mode="mixed", rcc_hz=None):
         """Solves of every port at every frequency key of seq, each lane on its own
         through the whole sequence: port c runs on lane c % lanes; a lane sets each
         frequency state on its context, then solves its ports warm-started from its own
@@ -192,7 +211,8 @@ class PortLanes:
         mode "mixed": peec_solve_mixed with solve_kw (inner_tol, inner_maxit); mode
         "fp64": the reference algorithm, peec_gmres with solve_kw["maxit"].
         get_state(k, pos) -> state with w, DZ, Yle, lu; release(k) is called once every
-        lane has set state k. record(pos, k, c, V, flag, relres, outer, inner) is called
+        lane has set state k. rcc_hz (Rcc operator): k -> Hz; each lane builds that
+        frequency's spectra on its own context. record(pos, k, c, V, flag, relres, outer, inner) is called
         from the lane threads after each solve (fp64: outer = 1, inner = the GMRES
         iterations). Returns False if stopped. An exception in one lane stops the others
         before their next frequency or port solve, and is then raised here."""
@@ -218,6 +238,8 @@ class PortLanes:
                     return
                 fs = get_state(k, pos)
                 op.set_frequency(fs.w, fs.DZ, fs.Yle, fs.lu)
+                if rcc_hz is not None:
+                    op.set_rcc_frequency(rcc_hz(k))
                 with lock:
                     left[pos] = left.get(pos, min(L, npt)) - 1
                     if left[pos] == 0 and k not in seq[pos + 1:]:
@@ -278,16 +300,26 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
     own. records: a path; one JSON line per port solve (frequency index and Hz, port,
     mode, flag, relative residual, iterations, wall ms) is appended to it. Returns
     {"S","Z","Y","f","info"}; None if stopped.
+    QS_Rcc_FW == 2 (FFTCP / FFTCLp an RccRows handle): the retarded operator, its spectra
+    rebuilt on the GPU at every frequency (FFT_solver_QS_S_type.jl:61-93).
     """
-    if QS_Rcc_FW != 1:
-        raise NotImplementedError("only the quasi-static operator (QS_Rcc_FW == 1) is implemented")
+    if QS_Rcc_FW not in (1, 2):
+        raise NotImplementedError("QS_Rcc_FW must be 1 (quasi-static) or 2 (Rcc)")
     freq = np.asarray(freq, dtype=np.float64).ravel() * escalings["freq"]
     inner = int(GMRES_settings["Inner_Iter"])
     A = incidence_selection["A"]
     m, n = A.shape
     ns = incidence_selection["Gamma"].shape[1]
     op = get_operator(incidence_selection, expansions, diagonals)
-    _ensure_spectra(op, FFTCP, FFTCLp)
+    rcc_hz = None
+    if QS_Rcc_FW == 2:
+        if not isinstance(FFTCP, RccRows) or FFTCP.op is not op:
+            raise ValueError("QS_Rcc_FW == 2 needs the RccRows handle of this operator "
+                             "(compute_FFT_mutual_coupling_mats with QS_Rcc_FW=2)")
+        # the reference rebuilds at freq[k] / escalings["freq"], the frequency in Hz
+        rcc_hz = lambda k: float(freq[k] / escalings["freq"])
+    else:
+        _ensure_spectra(op, FFTCP, FFTCLp)
     if stop_flag is not None:
         op.set_stop_flag(stop_flag)
     w = 2 * np.pi * freq
@@ -314,11 +346,11 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
         if mode == "mixed" and mixed_warm_start and nl > 1:
             res = _sweep_lanes(op, nl, pf, w, pn, S, Vrest, tol, inner, escalings,
                                mixed_inner_tol, stop_flag, on_solve, info, m, ns,
-                               ports_scatter_value)
+                               ports_scatter_value, rcc_hz)
         else:
             res = _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode,
                          mixed_inner_tol, mixed_warm_start, stop_flag, on_solve, info, m, ns,
-                         ports_scatter_value)
+                         ports_scatter_value, rcc_hz)
     finally:
         pf.close()
     if res is not None:
@@ -354,7 +386,7 @@ def _port_column(V, pn, c1, m, ns, z0):
 
 
 def _sweep_lanes(op, nl, pf, w, pn, S, Vrest, tol, inner, escalings, mixed_inner_tol,
-                 stop_flag, on_solve, info, m, ns, z0):
+                 stop_flag, on_solve, info, m, ns, z0, rcc_hz=None):
     lanes = PortLanes(op, nl)
     if stop_flag is not None:
         for o in lanes.ops[1:]:
@@ -374,7 +406,7 @@ def _sweep_lanes(op, nl, pf, w, pn, S, Vrest, tol, inner, escalings, mixed_inner
         ok = lanes.sweep(list(range(w.size)), pf.get, pf.release, pn, escalings["Is"], Vrest,
                          lambda k: float(tol[k]) if np.ndim(tol) else float(tol),
                          dict(inner_tol=mixed_inner_tol, inner_maxit=inner), record,
-                         stop_flag=stop_flag)
+                         stop_flag=stop_flag, rcc_hz=rcc_hz)
     finally:
         lanes.close()
     if not ok:
@@ -390,12 +422,15 @@ def _sweep_lanes(op, nl, pf, w, pn, S, Vrest, tol, inner, escalings, mixed_inner
 
 
 def _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode, mixed_inner_tol,
-           mixed_warm_start, stop_flag, on_solve, info, m, ns, ports_scatter_value):
+           mixed_warm_start, stop_flag, on_solve, info, m, ns, ports_scatter_value,
+           rcc_hz=None):
     for k in range(w.size):
         if stop_flag is not None and stop_flag.value:
             return None
         fs = pf.get(k)
         op.set_frequency(w[k], fs.DZ, fs.Yle, fs.lu)
+        if rcc_hz is not None:
+            op.set_rcc_frequency(rcc_hz(k))
         tk = float(tol[k]) if np.ndim(tol) else float(tol)
         for c1 in range(npt):
             n1, n2 = pn[c1]
@@ -459,19 +494,25 @@ def do_solving_fft(request, id="job", mode="mixed", lanes=1, device=0, stop_flag
     fill_cache.RowCache, to reuse the rows of an earlier fill of the same lattice."""
     from . import mesher
     solver_type = int(request.get("solverType", 1))
-    if solver_type != 1:
-        raise NotImplementedError("only the quasi-static solver (solverType 1) is implemented")
+    if solver_type not in (1, 2):
+        raise NotImplementedError("solverType must be 1 (quasi-static) or 2 (Rcc); the "
+                                  "reference's Taylor variant (3) is commented out")
     out, freqs, settings, z0, grid = mesher.parse_request(request)
     esc, inc, cc, diag, exp, ports, le, li, Zs = out
     op = GpuOperator(inc, exp, diag["P"], device=device)
     try:
-        fill_operator(op, cc, esc, row_cache)
+        if solver_type == 2:
+            op.fill_rcc(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"])
+            h = RccRows(op)
+        else:
+            fill_operator(op, cc, esc, row_cache)
+            h = CirculantSpectra(op)
         exp["gpu_ctx"] = op
-        h = CirculantSpectra(op)
         st = {"Inner_Iter": settings["Inner_Iter"],
               "tol": np.full(len(freqs), settings["tol"])}
         res = FFT_solver_QS_S_type(freqs, esc, inc, h, h, diag, ports, z0, le, exp, st, Zs,
-                                   mode=mode, lanes=lanes, stop_flag=stop_flag, records=records)
+                                   QS_Rcc_FW=solver_type, mode=mode, lanes=lanes,
+                                   stop_flag=stop_flag, records=records)
     finally:
         exp.pop("gpu_ctx", None)
         op.close()

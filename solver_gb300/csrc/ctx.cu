@@ -77,12 +77,19 @@ void launch_make_reflector(const c64*, size_t, int, c64, double, c64*, cudaStrea
 void launch_make_reflector(const c64*, size_t, int, c64, double, cff*, cudaStream_t);
 void launch_sub(const c64*, const c64*, size_t, c64*, cudaStream_t);
 void launch_add(const c64*, const c64*, size_t, c64*, cudaStream_t);
+void launch_add_i(const c64*, size_t, c64*, cudaStream_t);
 void launch_differs(const c64*, const c64*, size_t, int*, cudaStream_t);
 void launch_tri(c64*, int, int, const c64*, c64*, int, cudaStream_t);
 void launch_xupdate(const c64*, const c64*, size_t, const c64*, const c64*, int, size_t, c64*,
                     cudaStream_t);
 void launch_xupdate(const c64*, const cff*, size_t, const c64*, const c64*, int, size_t, c64*,
                     cudaStream_t);
+int fill_rows_rcc_gpu(const double origin[3], double sx, double sy, double sz, double escal_Lp,
+                      double escal_P, int Nx, int Ny, int Nz, double* const d_rows[9],
+                      const int64_t row_len[9], int* d_bad, cudaStream_t st);
+int rcc_rows_gpu(const double origin[3], double sx, double sy, double sz, int Nx, int Ny, int Nz,
+                 double beta, const double* const d_qs[9], double* const d_re[9],
+                 double* const d_im[9], const int64_t row_len[9], cudaStream_t st);
 int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, double escal_Lp,
                   double escal_P, int Nx, int Ny, int Nz, double* const d_rows[9],
                   const int64_t row_len[9], int* d_bad, cudaStream_t st);
@@ -134,6 +141,16 @@ struct peec_ctx {
   double zface_ms[3] = {-1, -1, -1};          // tuner times per face form (-1: not a candidate)
   double zedge_ms[6] = {-1, -1, -1, -1, -1, -1};  // per edge plan x form
   int row_dims[9][3] = {};
+  // retarded (Rcc, solverType 2) operator: the QS parts of its nine rows (escaled), the
+  // lattice geometry of the centre distances, and at the current frequency the spectra of
+  // the rows' imaginary parts (spec then holds those of the real parts); operator
+  // applications run both convolutions and join them (rcc set)
+  double* rcc_qs[9] = {};
+  double rcc_origin[3] = {0, 0, 0}, rcc_s[3] = {0, 0, 0};
+  bool have_rcc_rows = false, rcc = false;
+  double rcc_freq = -1.0;
+  Spectrum spec_im[9];
+  c64 *LpI2 = nullptr, *PQ2 = nullptr;
   // frequency state
   double w = 0.0;
   c64* DZ = nullptr;
@@ -359,20 +376,24 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
                   ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->lutmp2, ctx->dx, ctx->dy, ctx->U, (c64*)ctx->U32,
                   ctx->gb, ctx->gx, ctx->gr, ctx->gv, ctx->gw, ctx->gxm, ctx->gxmin, ctx->gtmp,
                   ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal, ctx->dT,
-                  ctx->mdpart};
+                  ctx->mdpart, ctx->LpI2, ctx->PQ2};
   for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (double* p : ctx->rcc_qs)
     if (p) cudaFree(p);
   for (auto& f : ctx->fam) {
     if (f.map) cudaFree(f.map);
     for (int p = 0; p < 2; ++p)
       if (f.T[p]) cudaFree(f.T[p]);
   }
-  for (auto& s : ctx->spec) {
-    for (int p = 0; p < 2; ++p)
-      if (s.d[p]) cudaFree(s.d[p]);
-    if (s.oct) cudaFree(s.oct);
-    if (s.yz32) cudaFree(s.yz32);
-  }
+  for (Spectrum* set : {ctx->spec, ctx->spec_im})
+    for (int i = 0; i < 9; ++i) {
+      Spectrum& s = set[i];
+      for (int p = 0; p < 2; ++p)
+        if (s.d[p]) cudaFree(s.d[p]);
+      if (s.oct) cudaFree(s.oct);
+      if (s.yz32) cudaFree(s.yz32);
+    }
   for (int a = 0; a < 3; ++a) {
     if (ctx->ph64[a]) cudaFree(ctx->ph64[a]);
     if (ctx->ph32[a]) cudaFree(ctx->ph32[a]);
@@ -533,22 +554,31 @@ static int peec_set_topology_body(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t
   }
   if (ctx->fam[0].L[2] * 3 * 16 * sizeof(c64) > 200 * 1024)
     return bad(ctx, PEEC_ERR_UNSUPPORTED, "z circulant too long for the z pass tile");
-  for (auto& sp : ctx->spec) {
-    for (int p = 0; p < 2; ++p) {
-      if (sp.d[p]) cudaFree(sp.d[p]);
-      sp.d[p] = nullptr;
+  for (Spectrum* set : {ctx->spec, ctx->spec_im})
+    for (int i = 0; i < 9; ++i) {
+      Spectrum& sp = set[i];
+      for (int p = 0; p < 2; ++p) {
+        if (sp.d[p]) cudaFree(sp.d[p]);
+        sp.d[p] = nullptr;
+      }
+      if (sp.oct) cudaFree(sp.oct);
+      sp.oct = nullptr;
+      if (sp.yz32) cudaFree(sp.yz32);
+      sp.yz32 = nullptr;
+      std::memcpy(sp.L, i < 6 ? LP : ctx->fam[i - 3].L, sizeof(LP));
     }
-    if (sp.oct) cudaFree(sp.oct);
-    sp.oct = nullptr;
-    if (sp.yz32) cudaFree(sp.yz32);
-    sp.yz32 = nullptr;
+  for (double*& p : ctx->rcc_qs) {
+    if (p) cudaFree(p);
+    p = nullptr;
   }
-  for (int i = 0; i < 6; ++i) std::memcpy(ctx->spec[i].L, LP, sizeof(LP));
-  for (int i = 6; i < 9; ++i) std::memcpy(ctx->spec[i].L, ctx->fam[i - 3].L, sizeof(LP));
+  ctx->have_rcc_rows = ctx->rcc = false;
+  ctx->rcc_freq = -1.0;
   CTX_TRY(phase_tables(LP, ctx->ph64, ctx->ph32, ctx->st));
   // work vectors
   CTX_TRY(dalloc(&ctx->LpI, m));
   CTX_TRY(dalloc(&ctx->PQ, ns));
+  CTX_TRY(dalloc(&ctx->LpI2, m));
+  CTX_TRY(dalloc(&ctx->PQ2, ns));
   CTX_TRY(dalloc(&ctx->Y1, m));
   CTX_TRY(dalloc(&ctx->U1, m));
   CTX_TRY(dalloc(&ctx->Y2, ns));
@@ -683,9 +713,7 @@ static int tune_zpass(peec_ctx* ctx) {
 // spectra from device rows (rows in the order Lpx, Lpy, Lpz, p12, p34, p56, p1234,
 // p1256, p3456). Spectrum i uses row srow[i]: P blocks 00, 11, 22 (symmetric), 01, 02, 12
 // (cross: output family f, input family g), then the three Lp blocks.
-static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
-  drop_graphs(ctx);
-  ctx->cc_prec = -1;
+static int build_spectrum_set(peec_ctx* ctx, Spectrum* dst, double* const d_rows[9]) {
   static const int srow[9] = {3, 4, 5, 6, 7, 8, 0, 1, 2};
   static const int fout[9] = {0, 1, 2, 0, 0, 1, 3, 4, 5};
   static const int fin[9] = {0, 1, 2, 1, 2, 2, 3, 4, 5};
@@ -697,11 +725,19 @@ static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
     if (!ctx->fam[fout[i]].active || !ctx->fam[fin[i]].active) continue;
     if (!d_rows[srow[i]]) return bad(ctx, PEEC_ERR_BADARG, "missing generating row");
     const bool sym = i < 3 || i >= 6;
-    CTX_TRY(spectrum_build(ctx->spec[i], d_rows[srow[i]], ctx->row_dims[srow[i]],
+    CTX_TRY(spectrum_build(dst[i], d_rows[srow[i]], ctx->row_dims[srow[i]],
                            ctx->fam[fout[i]].dims, ctx->fam[fin[i]].dims, sdim[i], odim[i],
                            sym ? 1 : 0, ctx->tw64, ctx->twmax, ctx->st));
     ctx->launches += 6;
   }
+  return PEEC_OK;
+}
+
+static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
+  drop_graphs(ctx);
+  ctx->cc_prec = -1;
+  ctx->rcc = false;
+  CTX_TRY(build_spectrum_set(ctx, ctx->spec, d_rows));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->have_spec = true;
   CTX_TRY(tune_zpass(ctx));
@@ -777,6 +813,145 @@ static int peec_fill_body(peec_ctx* ctx, const double origin[3], double sx, doub
     if (p) cudaFree(p);
   cudaFree(d_bad);
   return rc;
+}
+
+// ------------------------------------------------------------------------------------
+// retarded (Rcc) operator
+// ------------------------------------------------------------------------------------
+
+static int rcc_alloc_rows(peec_ctx* ctx, int64_t len[9]) {
+  for (int i = 0; i < 9; ++i) {
+    len[i] = (int64_t)ctx->row_dims[i][0] * ctx->row_dims[i][1] * ctx->row_dims[i][2];
+    if (len[i] > 0 && !ctx->rcc_qs[i])
+      if (cudaMalloc(&ctx->rcc_qs[i], len[i] * sizeof(double)) != cudaSuccess)
+        return bad(ctx, PEEC_ERR_OOM, "Rcc row allocation");
+  }
+  return PEEC_OK;
+}
+
+static void rcc_geometry(peec_ctx* ctx, const double origin[3], double sx, double sy, double sz) {
+  for (int q = 0; q < 3; ++q) ctx->rcc_origin[q] = origin[q];
+  ctx->rcc_s[0] = sx;
+  ctx->rcc_s[1] = sy;
+  ctx->rcc_s[2] = sz;
+  ctx->have_rcc_rows = true;
+  ctx->rcc_freq = -1.0;
+}
+
+static int peec_fill_rcc_body(peec_ctx* ctx, const double origin[3], double sx, double sy,
+                              double sz, double escal_Lp, double escal_P,
+                              double* const rows_out[9]) {
+  NvtxRange nvtx_range_("peec_fill_rcc");
+  if (!ctx || !origin) return badarg("peec_fill_rcc");
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  int64_t len[9];
+  ctx->have_rcc_rows = false;
+  CTX_TRY(rcc_alloc_rows(ctx, len));
+  int* d_bad = nullptr;
+  PEEC_CUDA_TRY(cudaMalloc(&d_bad, sizeof(int)));
+  cudaMemsetAsync(d_bad, 0, sizeof(int), ctx->st);
+  int rc = fill_rows_rcc_gpu(origin, sx, sy, sz, escal_Lp, escal_P, ctx->Nx, ctx->Ny, ctx->Nz,
+                             ctx->rcc_qs, len, d_bad, ctx->st);
+  ctx->launches += 9;
+  if (rc) ctx->err = g_err;
+  int hbad = 0;
+  if (rc == PEEC_OK) {
+    cudaMemcpyAsync(&hbad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->st);
+    if (cudaStreamSynchronize(ctx->st) != cudaSuccess)
+      rc = fail_cuda(cudaGetLastError(), "fill_rcc", __FILE__, __LINE__);
+    else if (hbad & 2)
+      rc = bad(ctx, PEEC_ERR_UNSUPPORTED,
+               "fill_rcc: an Lp entry falls in the orthogonal surface-surface case of the Rcc "
+               "dispatcher, which the reference cannot evaluate (compute_Lp_Voxels_QS.jl:330-352)");
+    else if (hbad)
+      rc = bad(ctx, PEEC_ERR_UNSUPPORTED,
+               "fill_rcc: a row entry is not finite (degenerate cell sizes?)");
+  }
+  cudaFree(d_bad);
+  if (rc != PEEC_OK) return rc;
+  if (rows_out)
+    for (int i = 0; i < 9; ++i)
+      if (rows_out[i] && len[i] > 0)
+        cudaMemcpyAsync(rows_out[i], ctx->rcc_qs[i], len[i] * sizeof(double),
+                        cudaMemcpyDeviceToHost, ctx->st);
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  rcc_geometry(ctx, origin, sx, sy, sz);
+  return PEEC_OK;
+}
+
+static int peec_set_rows_rcc_body(peec_ctx* ctx, const double* const rows[9],
+                                  const double origin[3], double sx, double sy, double sz) {
+  NvtxRange nvtx_range_("peec_set_rows_rcc");
+  if (!ctx || !rows || !origin) return badarg("peec_set_rows_rcc");
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  int64_t len[9];
+  ctx->have_rcc_rows = false;
+  CTX_TRY(rcc_alloc_rows(ctx, len));
+  for (int i = 0; i < 9; ++i) {
+    if (len[i] == 0) continue;
+    if (!rows[i]) return bad(ctx, PEEC_ERR_BADARG, "missing Rcc generating row");
+    cudaMemcpyAsync(ctx->rcc_qs[i], rows[i], len[i] * sizeof(double), cudaMemcpyHostToDevice,
+                    ctx->st);
+  }
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  rcc_geometry(ctx, origin, sx, sy, sz);
+  return PEEC_OK;
+}
+
+// The spectra of the Rcc rows at freq_hz: row * exp(-i beta R) with
+// beta = 2 pi f sqrt(eps0 mu0) (build_row_vox_Rcc.jl:1-11), split into real and
+// imaginary rows, each embedded and transformed like a QS row
+// (compute_Circulant_Lp_Rcc.jl, compute_Circulant_P_sup_Rcc.jl). The operator is linear
+// in its rows, so K x = K_re x + i K_im x with both halves real-row circulant operators.
+static int peec_set_rcc_frequency_body(peec_ctx* ctx, double freq_hz) {
+  NvtxRange nvtx_range_("peec_set_rcc_frequency");
+  if (!ctx) return badarg("peec_set_rcc_frequency");
+  if (!ctx->have_rcc_rows) return bad(ctx, PEEC_ERR_STATE, "Rcc rows not set");
+  if (!(freq_hz >= 0.0) || !std::isfinite(freq_hz))
+    return bad(ctx, PEEC_ERR_BADARG, "frequency must be finite and >= 0");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  if (ctx->rcc && ctx->rcc_freq == freq_hz) return PEEC_OK;
+  const double pi = 3.141592653589793;
+  const double mu0 = 4 * pi * 1e-7;
+  const double eps0 = 8.854187816997944e-12;
+  const double beta = 2 * pi * freq_hz * std::sqrt(eps0 * mu0);
+  int64_t len[9];
+  double* re[9] = {};
+  double* im[9] = {};
+  int rc = PEEC_OK;
+  for (int i = 0; i < 9 && rc == PEEC_OK; ++i) {
+    len[i] = (int64_t)ctx->row_dims[i][0] * ctx->row_dims[i][1] * ctx->row_dims[i][2];
+    if (len[i] == 0) continue;
+    if (cudaMallocAsync(&re[i], len[i] * sizeof(double), ctx->st) != cudaSuccess ||
+        cudaMallocAsync(&im[i], len[i] * sizeof(double), ctx->st) != cudaSuccess)
+      rc = bad(ctx, PEEC_ERR_OOM, "Rcc phased rows");
+  }
+  drop_graphs(ctx);
+  ctx->cc_prec = -1;
+  ctx->rcc = false;
+  if (rc == PEEC_OK) {
+    rc = rcc_rows_gpu(ctx->rcc_origin, ctx->rcc_s[0], ctx->rcc_s[1], ctx->rcc_s[2], ctx->Nx,
+                      ctx->Ny, ctx->Nz, beta, ctx->rcc_qs, re, im, len, ctx->st);
+    ctx->launches += 9;
+    if (rc) ctx->err = g_err;
+  }
+  if (rc == PEEC_OK) rc = build_spectrum_set(ctx, ctx->spec, re);
+  if (rc == PEEC_OK) rc = build_spectrum_set(ctx, ctx->spec_im, im);
+  for (int i = 0; i < 9; ++i) {
+    if (re[i]) cudaFreeAsync(re[i], ctx->st);
+    if (im[i]) cudaFreeAsync(im[i], ctx->st);
+  }
+  const cudaError_t e = cudaStreamSynchronize(ctx->st);
+  if (rc != PEEC_OK) return rc;
+  if (e != cudaSuccess) return fail_cuda(e, "Rcc spectra", __FILE__, __LINE__);
+  const bool tuned = ctx->have_spec;
+  ctx->have_spec = true;
+  ctx->rcc = true;
+  ctx->rcc_freq = freq_hz;
+  if (!tuned) CTX_TRY(tune_zpass(ctx));
+  return PEEC_OK;
 }
 
 // ------------------------------------------------------------------------------------
@@ -1093,14 +1268,21 @@ static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool ev
                        ctx->ph32[0], ctx->ph32[1], ctx->ph32[2]};
   CTX_TRY(conv_all(ctx->fam, 6, ctx->spec, ph, x, ctx->LpI, ctx->PQ, ctx->m, prec, tw,
                    ctx->twmax, st, ctx->prof ? ctx->pev.data() : nullptr, &ctx->zt));
+  if (ctx->rcc) {
+    // the imaginary-part rows' convolutions, joined as LpI += i LpI2, PQ += i PQ2
+    CTX_TRY(conv_all(ctx->fam, 6, ctx->spec_im, ph, x, ctx->LpI2, ctx->PQ2, ctx->m, prec, tw,
+                     ctx->twmax, st, nullptr, &ctx->zt));
+    launch_add_i(ctx->LpI2, ctx->m, ctx->LpI, st);
+    launch_add_i(ctx->PQ2, ctx->ns, ctx->PQ, st);
+    ctx->launches += 2;
+  }
   // one launch per x / y pass over all families, the shared z pass of the face
   // families, and the edge families' z passes: one launch over all of them in the staged
   // FP32 form (ZTune form 2), else one per family
-  ctx->launches += 5;
   int nedge = 0;
   for (const auto& F : ctx->fam) nedge += (F.active && F.lp) ? 1 : 0;
   const bool edge_one = prec == PEEC_PREC_FP32 && ctx->zt.edge == 2 && zpass_yz_edges(ctx->fam, 6);
-  ctx->launches += edge_one ? (nedge > 0) : nedge;
+  ctx->launches += (5 + (edge_one ? (nedge > 0) : nedge)) * (ctx->rcc ? 2 : 1);
   if (events) cudaEventRecord(ctx->ev[1], st);
   sparse_enqueue(ctx, x, y, ctx->LpI, ctx->PQ);
   if (events) cudaEventRecord(ctx->ev[2], st);
@@ -2018,6 +2200,23 @@ extern "C" int peec_fill(peec_ctx* ctx, const double origin[3], double sx, doubl
   return guarded(ctx, "peec_fill", [&] {
     return peec_fill_body(ctx, origin, sx, sy, sz, escal_Lp, escal_P, rows_out);
   });
+}
+
+extern "C" int peec_fill_rcc(peec_ctx* ctx, const double origin[3], double sx, double sy,
+                             double sz, double escal_Lp, double escal_P, double* const rows_out[9]) {
+  return guarded(ctx, __func__, [&] {
+    return peec_fill_rcc_body(ctx, origin, sx, sy, sz, escal_Lp, escal_P, rows_out);
+  });
+}
+
+extern "C" int peec_set_rows_rcc(peec_ctx* ctx, const double* const rows[9],
+                                 const double origin[3], double sx, double sy, double sz) {
+  return guarded(ctx, __func__,
+                 [&] { return peec_set_rows_rcc_body(ctx, rows, origin, sx, sy, sz); });
+}
+
+extern "C" int peec_set_rcc_frequency(peec_ctx* ctx, double freq_hz) {
+  return guarded(ctx, __func__, [&] { return peec_set_rcc_frequency_body(ctx, freq_hz); });
 }
 
 extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,

@@ -151,8 +151,13 @@ __device__ double ll_sp(const double* x1v, const double* x2v, int pform) {
     const int c1 = c >> 1, c2 = c & 1;
     const double x1 = x1v[c1], x2 = x2v[c2];
     const double R = sqrt((x1 - x2) * (x1 - x2));
-    double t = (x1 - x2) / R * (x1 - x2 * lgc(x2 - x1));
-    if (pform) t = t + x1 * lgc(x1 - x2);
+    double t;
+    if (pform == 2)  // integ_line_line_sp of compute_Lp_Voxels_QS.jl:501-520
+      t = (x1 - x2) / R * (x1 - x2 * lgc(x2 - x1) + x1 * lgc(x1 - x2));
+    else {
+      t = (x1 - x2) / R * (x1 - x2 * lgc(x2 - x1));
+      if (pform) t = t + x1 * lgc(x1 - x2);
+    }
     sol += sgn(c1 + c2 + 1) * fin(t);
   }
   return sol;
@@ -268,9 +273,10 @@ __device__ double line_vol(const double* x1v, const double* y1v, const double* z
   return sol;
 }
 
-// volume against the surface [x2v] x [y2v] at z2
+// volume against the surface [x2v] x [y2v] at z2; pform 2: integ_vol_surf of
+// compute_Lp_Voxels_QS.jl:777-824, whose second and third terms carry a factor (z1 - z2)
 __device__ double vol_surf(const double* x1v, const double* y1v, const double* z1v,
-                           const double* x2v, const double* y2v, double z2) {
+                           const double* x2v, const double* y2v, double z2, int pform) {
   double sol = 0.0;
 #pragma unroll 1
   for (int c = 0; c < 32; ++c) {
@@ -280,8 +286,10 @@ __device__ double vol_surf(const double* x1v, const double* y1v, const double* z
     const double R = sqrt(X2 + Y2 + Z2);
     const double aX = fabs(X), aY = fabs(Y);
     const double t1 = (Z2 / 12 - (X2 + Y2) / 8) * Z * R;
-    const double t2 = fin((Y2 / 2 - Z2 / 6) * X * lgc(X + R));
-    const double t3 = fin((X2 / 2 - Z2 / 6) * Y * lgc(Y + R));
+    const double t2 = pform == 2 ? fin((Y2 / 2 - Z2 / 6) * X * Z * lgc(X + R))
+                                 : fin((Y2 / 2 - Z2 / 6) * X * lgc(X + R));
+    const double t3 = pform == 2 ? fin((X2 / 2 - Z2 / 6) * Y * Z * lgc(Y + R))
+                                 : fin((X2 / 2 - Z2 / 6) * Y * lgc(Y + R));
     const double t4 = fin((-(X2 * X2) / 24 - (Y2 * Y2) / 24 + (Y2 * X2) / 4) * lgc(Z + R));
     const double t5 = -(aX * aX * aX) * Y / 6 * atan2(Y * Z, aX * R);
     const double t6 = -X * (aY * aY * aY) / 6 * atan2(X * Z, aY * R);
@@ -312,8 +320,12 @@ __device__ __forceinline__ int open_axis(const Box& b) { return !b.s[0] ? 0 : (!
 __device__ __forceinline__ int shut_axis(const Box& b) { return b.s[0] ? 0 : (b.s[1] ? 1 : 2); }
 
 // The integral of 1/R over the two boxes with their collapsed dimensions, each collapsed
-// length entering as a factor (the shared case tree of Integ_vol_vol_fft and
-// Integ_sup_sup_P; pform selects the _P primitives).
+// length entering as a factor (the shared case tree of Integ_vol_vol_fft,
+// Integ_sup_sup_P and the Rcc path's Integ_vol_vol; pform 1 selects the _P primitives,
+// pform 2 those of compute_Lp_Voxels_QS.jl). In the Rcc tree's orthogonal surface-surface
+// case the reference calls integ_surf_surf_ortho with an interval where it takes a
+// coordinate (compute_Lp_Voxels_QS.jl:330-352), which Julia cannot apply: NaN here, which
+// the row kernel reports.
 __device__ __noinline__ double integ_boxes(const Box& A, const Box& B, int pform) {
   const double V1 = A.len[0] * A.len[1] * A.len[2], V2 = B.len[0] * B.len[1] * B.len[2];
   switch (A.n + B.n) {
@@ -386,6 +398,7 @@ __device__ __noinline__ double integ_boxes(const Box& A, const Box& B, int pform
         others(n1, u, v);
         return w * ss_para(A.iv[u], A.iv[v], A.c[n1], B.iv[u], B.iv[v], B.c[n1]);
       }
+      if (pform == 2) return nan("");
       const int a = 3 - n1 - n2;
       return w * ss_ortho(A.iv[a], A.iv[n2], A.c[n1], B.iv[a], B.c[n2], B.iv[n1], pform);
     }
@@ -395,7 +408,7 @@ __device__ __noinline__ double integ_boxes(const Box& A, const Box& B, int pform
       const int nrm = shut_axis(S);
       int u, v;
       others(nrm, u, v);
-      return S.len[nrm] * vol_surf(V.iv[u], V.iv[v], V.iv[nrm], S.iv[u], S.iv[v], S.c[nrm]);
+      return S.len[nrm] * vol_surf(V.iv[u], V.iv[v], V.iv[nrm], S.iv[u], S.iv[v], S.c[nrm], pform);
     }
     default:
       return vol_vol(A.iv[0], A.iv[1], A.iv[2], B.iv[0], B.iv[1], B.iv[2]);
@@ -467,6 +480,7 @@ struct LpRowArgs {
   int M[3];          // lattice extents
   double o[3], s[3];
   double escal;
+  int form;          // 0: Integ_vol_vol_fft (QS fill); 2: Integ_vol_vol (Rcc rows)
 };
 
 __device__ __forceinline__ double lp_center(const LpRowArgs& a, int axis, int i) {
@@ -506,9 +520,9 @@ __global__ void k_fill_lp(LpRowArgs a, double* row, int64_t N, int* bad) {
     lp_flags(A, B);
     const double v = (A.n + B.n == 0)
                          ? vol_vol(A.iv[0], A.iv[1], A.iv[2], B.iv[0], B.iv[1], B.iv[2])
-                         : integ_boxes(A, B, 0);
+                         : integ_boxes(A, B, a.form);
     const double e = (p == 0) ? 0.0 : a.escal * (1e-7 / S * v);
-    if (!isfinite(e)) atomicOr(bad, 1);
+    if (!isfinite(e)) atomicOr(bad, a.form == 2 ? 2 : 1);
     row[p] = e;
   }
 }
@@ -621,9 +635,28 @@ __global__ void k_fill_p(PRowArgs a, double* row, int64_t N, int* bad) {
   }
 }
 
-int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, double escal_Lp,
-                  double escal_P, int Nx, int Ny, int Nz, double* const d_rows[9],
-                  const int64_t row_len[9], int* d_bad, cudaStream_t st) {
+// (lattice extents, interleaved axes, caser, caser2) of the six P rows: the QS fill's face
+// types (compute_FFT_mutual_coupling_mats.jl:96-125) and those of the Rcc path
+// (compute_rows_Rcc_P.jl:47-52), which pass the block indices as face types; the Rcc
+// centre distances take the QS face types (compute_rows_Rcc_P.jl:55-60)
+struct PDef { int M[3]; int half[3]; int c1, c2, r1, r2; };
+static void p_defs(int Nx, int Ny, int Nz, PDef pd[6]) {
+  const PDef d[6] = {{{Nx, Ny + 1, Nz}, {0, 0, 0}, 1, 1, 1, 1},
+                     {{Nx + 1, Ny, Nz}, {0, 0, 0}, 3, 3, 2, 2},
+                     {{Nx, Ny, Nz + 1}, {0, 0, 0}, 5, 5, 3, 3},
+                     {{2 * Nx + 1, 2 * Ny + 1, Nz}, {1, 1, 0}, 3, 2, 1, 2},
+                     {{Nx, 2 * Ny + 1, 2 * Nz + 1}, {0, 1, 1}, 5, 2, 1, 3},
+                     {{2 * Nx + 1, Ny, 2 * Nz + 1}, {1, 0, 1}, 5, 4, 2, 3}};
+  for (int r = 0; r < 6; ++r) pd[r] = d[r];
+}
+
+// rcc = 0: the QS rows (compute_FFT_mutual_coupling_mats.jl:36-128); rcc = 1: the QS parts
+// of the Rcc rows (compute_rows_Rcc_Lp.jl:20-35 over compute_Lp_Voxels_QS,
+// compute_rows_Rcc_P.jl:47-52), escaled, Lp self entries zero
+static int fill_rows_any(const double origin[3], double sx, double sy, double sz,
+                         double escal_Lp, double escal_P, int Nx, int Ny, int Nz,
+                         double* const d_rows[9], const int64_t row_len[9], int* d_bad,
+                         cudaStream_t st, int rcc) {
   const int grid = 152 * 8, tpb = 128;
   const int lpM[3][3] = {{Nx - 1, Ny, Nz}, {Nx, Ny - 1, Nz}, {Nx, Ny, Nz - 1}};
   for (int d = 0; d < 3; ++d) {
@@ -636,21 +669,16 @@ int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, doubl
     }
     a.s[0] = sx; a.s[1] = sy; a.s[2] = sz;
     a.escal = escal_Lp;
+    a.form = rcc ? 2 : 0;
     k_fill_lp<<<grid, tpb, 0, st>>>(a, d_rows[d], row_len[d], d_bad);
   }
-  // (lattice extents, interleaved axes, caser, caser2) of the six P rows
-  struct PDef { int M[3]; int half[3]; int c1, c2; };
-  const PDef pd[6] = {{{Nx, Ny + 1, Nz}, {0, 0, 0}, 1, 1},
-                      {{Nx + 1, Ny, Nz}, {0, 0, 0}, 3, 3},
-                      {{Nx, Ny, Nz + 1}, {0, 0, 0}, 5, 5},
-                      {{2 * Nx + 1, 2 * Ny + 1, Nz}, {1, 1, 0}, 3, 2},
-                      {{Nx, 2 * Ny + 1, 2 * Nz + 1}, {0, 1, 1}, 5, 2},
-                      {{2 * Nx + 1, Ny, 2 * Nz + 1}, {1, 0, 1}, 5, 4}};
+  PDef pd[6];
+  p_defs(Nx, Ny, Nz, pd);
   for (int r = 0; r < 6; ++r) {
     if (!d_rows[3 + r] || row_len[3 + r] == 0) continue;
     PRowArgs a;
-    a.caser = pd[r].c1;
-    a.caser2 = pd[r].c2;
+    a.caser = rcc ? pd[r].r1 : pd[r].c1;
+    a.caser2 = rcc ? pd[r].r2 : pd[r].c2;
     for (int q = 0; q < 3; ++q) {
       a.M[q] = pd[r].M[q];
       a.half[q] = pd[r].half[q];
@@ -659,6 +687,109 @@ int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, doubl
     a.s[0] = sx; a.s[1] = sy; a.s[2] = sz;
     a.escal = escal_P;
     k_fill_p<<<grid, tpb, 0, st>>>(a, d_rows[3 + r], row_len[3 + r], d_bad);
+  }
+  PEEC_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, double escal_Lp,
+                  double escal_P, int Nx, int Ny, int Nz, double* const d_rows[9],
+                  const int64_t row_len[9], int* d_bad, cudaStream_t st) {
+  return fill_rows_any(origin, sx, sy, sz, escal_Lp, escal_P, Nx, Ny, Nz, d_rows, row_len, d_bad,
+                       st, 0);
+}
+
+int fill_rows_rcc_gpu(const double origin[3], double sx, double sy, double sz, double escal_Lp,
+                      double escal_P, int Nx, int Ny, int Nz, double* const d_rows[9],
+                      const int64_t row_len[9], int* d_bad, cudaStream_t st) {
+  return fill_rows_any(origin, sx, sy, sz, escal_Lp, escal_P, Nx, Ny, Nz, d_rows, row_len, d_bad,
+                       st, 1);
+}
+
+// ---------------------------------------------------------------------------------
+// Rcc rows at one frequency: row * exp(-i beta R) (build_row_vox_Rcc.jl:1-11), R the
+// distance between the generating cell and each lattice cell: voxel centres for the Lp
+// rows (compute_Voxels_Rcc.jl:1-13), face centres of the QS face types for the P rows
+// (compute_P_vox_Rcc.jl:1-84). The real and imaginary parts go to separate rows.
+// ---------------------------------------------------------------------------------
+
+struct RccRowArgs {
+  int lp;            // Lp row (dir) or P row (casers, half)
+  int dir;
+  int caser, caser2;
+  int M[3];
+  int half[3];
+  double o[3], s[3];
+  double beta;
+};
+
+__device__ __forceinline__ double norm3(double dx, double dy, double dz) {
+  return sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+__global__ void k_rcc_phase(RccRowArgs a, const double* __restrict__ qs, double* re, double* im,
+                            int64_t N) {
+  double c0[3];
+  if (a.lp) {
+    LpRowArgs l;
+    l.dir = a.dir;
+    for (int q = 0; q < 3; ++q) { l.o[q] = a.o[q]; l.s[q] = a.s[q]; }
+    for (int q = 0; q < 3; ++q) c0[q] = lp_center(l, q, 0);
+  } else {
+    double e[3], d[2];
+    face(a.caser, ctr(a.o[0], a.s[0], 0, a.half[0]), ctr(a.o[1], a.s[1], 0, a.half[1]),
+         ctr(a.o[2], a.s[2], 0, a.half[2]), a.s[0], a.s[1], a.s[2], c0, e, d);
+  }
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < N;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(p % a.M[0]);
+    const int j = (int)((p / a.M[0]) % a.M[1]);
+    const int k = (int)(p / ((int64_t)a.M[0] * a.M[1]));
+    double c[3];
+    if (a.lp) {
+      LpRowArgs l;
+      l.dir = a.dir;
+      for (int q = 0; q < 3; ++q) { l.o[q] = a.o[q]; l.s[q] = a.s[q]; }
+      c[0] = lp_center(l, 0, i);
+      c[1] = lp_center(l, 1, j);
+      c[2] = lp_center(l, 2, k);
+    } else {
+      double e[3], d[2];
+      face(a.caser2, ctr(a.o[0], a.s[0], i, a.half[0]), ctr(a.o[1], a.s[1], j, a.half[1]),
+           ctr(a.o[2], a.s[2], k, a.half[2]), a.s[0], a.s[1], a.s[2], c, e, d);
+    }
+    const double R = norm3(c0[0] - c[0], c0[1] - c[1], c0[2] - c[2]);
+    double sn, cs;
+    sincos(a.beta * R, &sn, &cs);
+    const double v = qs[p];
+    re[p] = v * cs;
+    im[p] = -(v * sn);
+  }
+}
+
+// the real and imaginary parts of the nine Rcc rows at propagation constant beta (rad/m)
+int rcc_rows_gpu(const double origin[3], double sx, double sy, double sz, int Nx, int Ny, int Nz,
+                 double beta, const double* const d_qs[9], double* const d_re[9],
+                 double* const d_im[9], const int64_t row_len[9], cudaStream_t st) {
+  const int grid = 152 * 8, tpb = 256;
+  const int lpM[3][3] = {{Nx - 1, Ny, Nz}, {Nx, Ny - 1, Nz}, {Nx, Ny, Nz - 1}};
+  PDef pd[6];
+  p_defs(Nx, Ny, Nz, pd);
+  for (int r = 0; r < 9; ++r) {
+    if (!d_qs[r] || row_len[r] == 0) continue;
+    RccRowArgs a;
+    a.lp = r < 3;
+    a.dir = r < 3 ? r : 0;
+    a.caser = r < 3 ? 0 : pd[r - 3].c1;
+    a.caser2 = r < 3 ? 0 : pd[r - 3].c2;
+    for (int q = 0; q < 3; ++q) {
+      a.M[q] = r < 3 ? lpM[r][q] : pd[r - 3].M[q];
+      a.half[q] = r < 3 ? 0 : pd[r - 3].half[q];
+      a.o[q] = origin[q];
+    }
+    a.s[0] = sx; a.s[1] = sy; a.s[2] = sz;
+    a.beta = beta;
+    k_rcc_phase<<<grid, tpb, 0, st>>>(a, d_qs[r], d_re[r], d_im[r], row_len[r]);
   }
   PEEC_CUDA_TRY(cudaGetLastError());
   return 0;

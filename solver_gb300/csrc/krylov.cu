@@ -382,6 +382,19 @@ void launch_add(const c64* a, const c64* b, size_t N, c64* out, cudaStream_t st)
   k_add<<<g_stream(N), 256, 0, st>>>(a, b, N, out);
 }
 
+// out += i * b (the imaginary-part convolutions of the Rcc operator joined to the real ones)
+__global__ void k_add_i(const c64* __restrict__ b, size_t N, c64* out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const c64 u = out[i], v = b[i];
+    out[i] = mk<double>(u.x - v.y, u.y + v.x);
+  }
+}
+
+void launch_add_i(const c64* b, size_t N, c64* out, cudaStream_t st) {
+  k_add_i<<<g_stream(N), 256, 0, st>>>(b, N, out);
+}
+
 // flag |= 1 when a and b differ anywhere (bitwise on the doubles)
 __global__ void k_differs(const c64* __restrict__ a, const c64* __restrict__ b, size_t N,
                           int* flag) {

@@ -109,6 +109,8 @@ class GpuOperator:
         self._freq_key = None
         self._spec_src = None  # the host spectra the device rows were recovered from
         self._stop = None
+        self._rcc = None  # (rows, origin, (sx, sy, sz)) of the retarded operator, for clone()
+        self._rcc_freq = None
 
     def close(self):
         if getattr(self, "h", None):
@@ -138,6 +140,7 @@ class GpuOperator:
             keep.append(r)
             arr[i] = r.ctypes.data
         self._spec_src = None
+        self._rcc_freq = None
         _lib.check(self.h, self.L.peec_set_rows(self.h, arr))
         self._rows = {k: v for k, v in rows.items()}
 
@@ -155,21 +158,77 @@ class GpuOperator:
             else:
                 arr[i] = None
         self._spec_src = None
+        self._rcc_freq = None
         _lib.check(self.h, self.L.peec_fill(self.h, _lib.ptr(o), sx, sy, sz, escal_Lp, escal_P,
                                             arr))
         self._rows = outs  # kept for clone()
         return outs if return_rows else None
 
+    # -- retarded (Rcc) operator ------------------------------------------------------
+    def _row_buffers(self, rows=None):
+        dims = row_dims(*self.grid)
+        arr = (ctypes.c_void_p * 9)()
+        keep = {}
+        for i, k in enumerate(ROW_KEYS):
+            n = int(np.prod(dims[k]))
+            if n == 0:
+                arr[i] = None
+                continue
+            if rows is None:
+                keep[k] = np.empty(n)
+            else:
+                if k not in rows:
+                    raise ValueError(f"missing Rcc row {k}")
+                keep[k] = np.ascontiguousarray(np.asarray(rows[k], dtype=np.float64).ravel())
+                if keep[k].size != n:
+                    raise ValueError(f"row {k} has {keep[k].size} entries, expected {n}")
+            arr[i] = keep[k].ctypes.data
+        return arr, keep
+
+    def fill_rcc(self, origin, sx, sy, sz, escal_Lp, escal_P):
+        """GPU fill of the quasi-static parts of the nine Rcc rows (compute_rows_Rcc_Lp,
+        compute_rows_Rcc_P; escaled, Lp self entries zero). Returns the rows."""
+        o = np.ascontiguousarray(np.asarray(origin, dtype=np.float64))
+        arr, outs = self._row_buffers()
+        _lib.check(self.h, self.L.peec_fill_rcc(self.h, _lib.ptr(o), sx, sy, sz, escal_Lp,
+                                                escal_P, arr))
+        self._rcc = (outs, o.copy(), (float(sx), float(sy), float(sz)))
+        self._rcc_freq = None
+        return outs
+
+    def set_rows_rcc(self, rows, origin, sx, sy, sz):
+        """Uploads the quasi-static parts of the nine Rcc rows (escaled) and the mesh
+        geometry their centre distances come from."""
+        o = np.ascontiguousarray(np.asarray(origin, dtype=np.float64))
+        arr, keep = self._row_buffers(rows)
+        _lib.check(self.h, self.L.peec_set_rows_rcc(self.h, arr, _lib.ptr(o), float(sx),
+                                                    float(sy), float(sz)))
+        self._rcc = (keep, o.copy(), (float(sx), float(sy), float(sz)))
+        self._rcc_freq = None
+
+    def set_rcc_frequency(self, freq_hz):
+        """The Rcc spectra at freq_hz (Hz); later operator applications use them."""
+        if self._rcc_freq is not None and self._rcc_freq == float(freq_hz):
+            return
+        self._rcc_freq = None
+        _lib.check(self.h, self.L.peec_set_rcc_frequency(self.h, float(freq_hz)))
+        self._rcc_freq = float(freq_hz)
+
     def clone(self):
         """A second context on the same device with the same topology and circulant
         rows: its own CUDA stream and workspaces, so several port solves of one
         frequency run concurrently (one context per port, each driven from its own
-        host thread). The frequency state is set per context."""
-        if self._rows is None:
-            raise RuntimeError("clone() needs the generating rows: call fill or set_rows first")
+        host thread). The frequency state (and the Rcc frequency) is set per context."""
+        if self._rows is None and self._rcc is None:
+            raise RuntimeError("clone() needs the generating rows: call fill, set_rows, "
+                               "fill_rcc or set_rows_rcc first")
         inc, exp, dP, grid, dev = self._init_args
         c = GpuOperator(inc, exp, dP, grid=grid, device=dev)
-        c.set_rows(self._rows)
+        if self._rows is not None:
+            c.set_rows(self._rows)
+        if self._rcc is not None:
+            rows, o, (sx, sy, sz) = self._rcc
+            c.set_rows_rcc(rows, o, sx, sy, sz)
         return c
 
     # -- frequency ------------------------------------------------------------------

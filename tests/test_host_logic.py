@@ -120,8 +120,10 @@ def test_dump_json_data_layout():
 
 
 def test_do_solving_fft_rejects_other_solver_types():
-    with pytest.raises(NotImplementedError):
-        api.do_solving_fft({"solverType": 2})
+    # 1 (quasi-static) and 2 (Rcc) are built; the reference comments out Taylor (3)
+    for t in (0, 3):
+        with pytest.raises(NotImplementedError):
+            api.do_solving_fft({"solverType": t})
 
 
 def test_operator_rejects_vectors_of_the_wrong_length():
