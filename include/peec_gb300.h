@@ -149,6 +149,24 @@ int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nn
                        const int64_t* U_ptr, const int64_t* U_col, const double* U_val,
                        const int64_t* perm_r, const int64_t* perm_c, const double* row_scale);
 
+/*
+ * Device factorisation of SS at later frequencies (replaces the per-frequency lu(SS) of
+ * FFT_solver_QS_S_type.jl:118-119 after the first frequency). SS's structure does not
+ * depend on the frequency, so the factors of one host factorisation (installed by
+ * peec_set_frequency) fix the pattern and the pivot order:
+ * peec_lu_refactor_setup: builds the plan from the installed factors and the Yle pattern
+ * (COO, values not read).
+ * peec_set_frequency_refactor: DZ and Yle as for peec_set_frequency (Yle with the same
+ * pattern), then SS assembled and factorised on the device (one launch per level of L),
+ * no host factors. A zero or non-finite pivot returns PEEC_ERR_UNSUPPORTED (factorise that
+ * frequency on the host); a later peec_set_frequency drops the plan.
+ */
+int peec_lu_refactor_setup(peec_ctx* ctx, int64_t yle_nnz, const int64_t* yle_row,
+                           const int64_t* yle_col);
+int peec_set_frequency_refactor(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,
+                                const int64_t* yle_row, const int64_t* yle_col,
+                                const double* yle_val);
+
 /* y = M^-1 K x (ComputeMatrixVectorFTT); x, y host, length N = m + ns + n complex. */
 int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precision);
 /* same on device pointers (complex double) */

@@ -26,7 +26,8 @@ EXPORTS = ("peec_version", "peec_ctx_create", "peec_ctx_destroy", "peec_last_err
            "peec_conv_info", "peec_zpass_tuning", "peec_set_zpass_forms", "peec_profile_matvec", "peec_multidot",
            "peec_multidot_noalloc", "peec_set_residual_precision",
            "peec_set_lu_component_max", "peec_adjoint", "peec_check_wait_limit",
-           "peec_fill_rcc", "peec_set_rows_rcc", "peec_set_rcc_frequency")
+           "peec_fill_rcc", "peec_set_rows_rcc", "peec_set_rcc_frequency",
+           "peec_lu_refactor_setup", "peec_set_frequency_refactor")
 
 
 PREC_FP64, PREC_FP32, PREC_FF = 0, 1, 2
@@ -85,6 +86,8 @@ def load(build_if_missing: bool = True):
     L.peec_set_rows_rcc.argtypes = [P, ctypes.POINTER(P), P, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double]
     L.peec_set_rcc_frequency.argtypes = [P, ctypes.c_double]
+    L.peec_lu_refactor_setup.argtypes = [P, ctypes.c_int64, P, P]
+    L.peec_set_frequency_refactor.argtypes = [P, ctypes.c_double, P, ctypes.c_int64, P, P, P]
     L.peec_set_frequency.argtypes = [P, ctypes.c_double, P, ctypes.c_int64, P, P, P, P, P, P, P,
                                      P, P, P, P, P]
     L.peec_matvec.argtypes = [P, P, P, ctypes.c_int]

@@ -167,6 +167,18 @@ def s2y_fft(S, Zo):
     return np.stack([Zo * np.linalg.solve(I + S[:, :, k], I - S[:, :, k]) for k in range(nf)], 2)
 
 
+def install_state(op, fs, device_lu=False):
+    """Sets a frequency state on a context: with host factors (fs.lu) through
+    peec_set_frequency, and with device_lu the later states factorised on the device in
+    their pattern (fs.lu None: peec_set_frequency_refactor)."""
+    if device_lu and fs.lu is None:
+        op.set_frequency_refactor(fs.w, fs.DZ, fs.Yle)
+    else:
+        op.set_frequency(fs.w, fs.DZ, fs.Yle, fs.lu)
+        if device_lu:
+            op.enable_refactor(fs.Yle)
+
+
 class PortLanes:
     """Concurrent port solves of one frequency: one context per lane (its own CUDA
     stream, FFT buffers, Krylov workspace and LU-solve control words; same topology
@@ -200,7 +212,7 @@ class PortLanes:
         return out
 
     def sweep(self, seq, get_state, release, pn, Is, Vrest, tol_of, solve_kw, record,
-              stop_flag=None, mode="mixed", rcc_hz=None):
+              stop_flag=None, mode="mixed", rcc_hz=None, device_lu=False):
         """Solves of every port at every frequency key of seq, each lane on its own
         through the whole sequence: port c runs on lane c % lanes; a lane sets each
         frequency state on its context, then solves its ports warm-started from its own
@@ -212,7 +224,9 @@ class PortLanes:
         "fp64": the reference algorithm, peec_gmres with solve_kw["maxit"].
         get_state(k, pos) -> state with w, DZ, Yle, lu; release(k) is called once every
         lane has set state k. rcc_hz (Rcc operator): k -> Hz; each lane builds that
-        frequency's spectra on its own context. record(pos, k, c, V, flag, relres, outer, inner) is called
+        frequency's spectra on its own context. device_lu: states without host factors
+        (lu None) are factorised on each lane's device in the pattern of the first
+        factored state the lane set. record(pos, k, c, V, flag, relres, outer, inner) is called
         from the lane threads after each solve (fp64: outer = 1, inner = the GMRES
         iterations). Returns False if stopped. An exception in one lane stops the others
         before their next frequency or port solve, and is then raised here."""
@@ -237,7 +251,7 @@ class PortLanes:
                     stopped.append(True)
                     return
                 fs = get_state(k, pos)
-                op.set_frequency(fs.w, fs.DZ, fs.Yle, fs.lu)
+                install_state(op, fs, device_lu)
                 if rcc_hz is not None:
                     op.set_rcc_frequency(rcc_hz(k))
                 with lock:
@@ -290,7 +304,7 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
                          ports_scatter_value, lumped_elements, expansions, GMRES_settings,
                          Zs_info, QS_Rcc_FW=1, id=None, chan=None, commentsEnabled=False, *,
                          mode="fp64", mixed_inner_tol=1e-7, mixed_warm_start=True,
-                         stop_flag=None, on_solve=None, lanes=1, records=None):
+                         stop_flag=None, on_solve=None, lanes=1, records=None, lu="host"):
     """Frequency x port sweep with warm starts (FFT_solver_QS_S_type.jl:1-234).
 
     mode "fp64": the reference algorithm (FP64 convolutions, Householder GMRES).
@@ -302,7 +316,14 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
     {"S","Z","Y","f","info"}; None if stopped.
     QS_Rcc_FW == 2 (FFTCP / FFTCLp an RccRows handle): the retarded operator, its spectra
     rebuilt on the GPU at every frequency (FFT_solver_QS_S_type.jl:61-93).
+    lu "host": SS factorised on the host at every frequency (as the reference does);
+    "device": on the host at the first frequency only, then assembled and factorised on
+    the GPU in that pattern and pivot order (GpuOperator.set_frequency_refactor).
     """
+    if lu not in ("host", "device"):
+        raise ValueError(f"lu must be 'host' or 'device', not {lu!r}")
+    device_lu = lu == "device"
+    factor_of = (lambda k: k == 0) if device_lu else (lambda k: True)
     if QS_Rcc_FW not in (1, 2):
         raise NotImplementedError("QS_Rcc_FW must be 1 (quasi-static) or 2 (Rcc)")
     freq = np.asarray(freq, dtype=np.float64).ravel() * escalings["freq"]
@@ -336,21 +357,23 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
         # large node systems: factorise ahead in spawned worker processes
         pf = fq.FrequencyPool((escalings, incidence_selection, diagonals, Zs_info,
                                lumped_elements, ports, ports_scatter_value),
-                              lambda k: w[k], range(w.size), workers=4, lookahead=4, keep=keep)
+                              lambda k: w[k], range(w.size), workers=4, lookahead=4, keep=keep,
+                              factor_of=factor_of)
     else:
         pf = fq.StatePrefetcher(
             lambda k: fq.FrequencyState(w[k], escalings, incidence_selection, diagonals, Zs_info,
-                                        lumped_elements, ports, ports_scatter_value),
+                                        lumped_elements, ports, ports_scatter_value,
+                                        factor=factor_of(k)),
             range(w.size), keep=keep)
     try:
         if mode == "mixed" and mixed_warm_start and nl > 1:
             res = _sweep_lanes(op, nl, pf, w, pn, S, Vrest, tol, inner, escalings,
                                mixed_inner_tol, stop_flag, on_solve, info, m, ns,
-                               ports_scatter_value, rcc_hz)
+                               ports_scatter_value, rcc_hz, device_lu)
         else:
             res = _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode,
                          mixed_inner_tol, mixed_warm_start, stop_flag, on_solve, info, m, ns,
-                         ports_scatter_value, rcc_hz)
+                         ports_scatter_value, rcc_hz, device_lu)
     finally:
         pf.close()
     if res is not None:
@@ -386,7 +409,7 @@ def _port_column(V, pn, c1, m, ns, z0):
 
 
 def _sweep_lanes(op, nl, pf, w, pn, S, Vrest, tol, inner, escalings, mixed_inner_tol,
-                 stop_flag, on_solve, info, m, ns, z0, rcc_hz=None):
+                 stop_flag, on_solve, info, m, ns, z0, rcc_hz=None, device_lu=False):
     lanes = PortLanes(op, nl)
     if stop_flag is not None:
         for o in lanes.ops[1:]:
@@ -406,7 +429,7 @@ def _sweep_lanes(op, nl, pf, w, pn, S, Vrest, tol, inner, escalings, mixed_inner
         ok = lanes.sweep(list(range(w.size)), pf.get, pf.release, pn, escalings["Is"], Vrest,
                          lambda k: float(tol[k]) if np.ndim(tol) else float(tol),
                          dict(inner_tol=mixed_inner_tol, inner_maxit=inner), record,
-                         stop_flag=stop_flag, rcc_hz=rcc_hz)
+                         stop_flag=stop_flag, rcc_hz=rcc_hz, device_lu=device_lu)
     finally:
         lanes.close()
     if not ok:
@@ -423,12 +446,12 @@ def _sweep_lanes(op, nl, pf, w, pn, S, Vrest, tol, inner, escalings, mixed_inner
 
 def _sweep(op, pf, w, pn, npt, S, Vrest, tol, inner, escalings, mode, mixed_inner_tol,
            mixed_warm_start, stop_flag, on_solve, info, m, ns, ports_scatter_value,
-           rcc_hz=None):
+           rcc_hz=None, device_lu=False):
     for k in range(w.size):
         if stop_flag is not None and stop_flag.value:
             return None
         fs = pf.get(k)
-        op.set_frequency(w[k], fs.DZ, fs.Yle, fs.lu)
+        install_state(op, fs, device_lu)
         if rcc_hz is not None:
             op.set_rcc_frequency(rcc_hz(k))
         tk = float(tol[k]) if np.ndim(tol) else float(tol)
@@ -483,7 +506,7 @@ def dump_json_data(matrix_Z, matrix_S, matrix_Y, num_ports, id, partial=False, f
 
 
 def do_solving_fft(request, id="job", mode="mixed", lanes=1, device=0, stop_flag=None,
-                   records=None, row_cache=None):
+                   records=None, row_cache=None, lu="host"):
     """A solve request end to end, as the reference's doSolvingFFT does it
     (do_solving_fft.jl:1-177) without its message queue and object store: the request
     body (mesherOutput / solverInput / solverAlgoParams / solverType) through the mesher,
@@ -491,7 +514,8 @@ def do_solving_fft(request, id="job", mode="mixed", lanes=1, device=0, stop_flag
     dictionary (dump_json_data) plus "S", "Z", "Y" (ports x ports x frequencies) and
     "f"; None if stopped. mode "fp64" runs the reference algorithm, "mixed" the mixed
     precision solves (lanes: port lanes, see FFT_solver_QS_S_type). row_cache: a
-    fill_cache.RowCache, to reuse the rows of an earlier fill of the same lattice."""
+    fill_cache.RowCache, to reuse the rows of an earlier fill of the same lattice. lu: where
+    SS is factorised after the first frequency (see FFT_solver_QS_S_type)."""
     from . import mesher
     solver_type = int(request.get("solverType", 1))
     if solver_type not in (1, 2):
@@ -512,7 +536,7 @@ def do_solving_fft(request, id="job", mode="mixed", lanes=1, device=0, stop_flag
               "tol": np.full(len(freqs), settings["tol"])}
         res = FFT_solver_QS_S_type(freqs, esc, inc, h, h, diag, ports, z0, le, exp, st, Zs,
                                    QS_Rcc_FW=solver_type, mode=mode, lanes=lanes,
-                                   stop_flag=stop_flag, records=records)
+                                   stop_flag=stop_flag, records=records, lu=lu)
     finally:
         exp.pop("gpu_ctx", None)
         op.close()
@@ -524,7 +548,7 @@ def do_solving_fft(request, id="job", mode="mixed", lanes=1, device=0, stop_flag
     return outd
 
 
-def sweep_many(requests, mode="mixed", concurrency=4, device=0, row_cache=None):
+def sweep_many(requests, mode="mixed", concurrency=4, device=0, row_cache=None, lu="host"):
     """Frequency sweeps of several geometries, concurrently: each geometry gets its own
     context (CUDA stream, fill, spectra, workspaces) and host thread, so the sweeps' kernels
     overlap on the GPU the way port lanes do. Per request: the mesher, the GPU fill, then
@@ -545,7 +569,7 @@ def sweep_many(requests, mode="mixed", concurrency=4, device=0, row_cache=None):
             st = {"Inner_Iter": settings["Inner_Iter"],
                   "tol": np.full(len(freqs), settings["tol"])}
             return FFT_solver_QS_S_type(freqs, esc, inc, h, h, diag, ports, z0, le, exp, st, Zs,
-                                        mode=mode)
+                                        mode=mode, lu=lu)
         finally:
             exp.pop("gpu_ctx", None)
             op.close()

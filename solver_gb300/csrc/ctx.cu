@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <array>
 #include <map>
+#include <queue>
 #include <mutex>
 #include <new>
 #include <stdexcept>
@@ -177,6 +178,12 @@ struct peec_ctx {
   int sf_total = 0, sf_nL = 0;
   int* sf_ctl = nullptr;  // [epoch, claim counter, error flag]
   LevelTri Lf, Uf;
+  // device refactorisation of SS in the current factors' pattern (refactor.cu)
+  RefactorPlan rf;
+  bool have_rf = false;
+  std::vector<int32_t> h_gin, h_gout;   // host copies of the LU row / column gathers
+  std::vector<int32_t> rf_yp, rf_yc;    // the Yle pattern (CSR) the plan was built for
+  int* rf_err = nullptr;
   // matvec work
   c64 *LpI = nullptr, *PQ = nullptr, *Y1 = nullptr, *U1 = nullptr, *Y2 = nullptr, *U2 = nullptr;
   c64 *tvec = nullptr, *Mvec = nullptr, *lutmp = nullptr, *lutmp2 = nullptr;
@@ -359,6 +366,12 @@ static int peec_ctx_create_body(peec_ctx** out, int device) {
   return PEEC_OK;
 }
 
+static void free_refactor(RefactorPlan& r) {
+  cudaFree(r.asm_ptr); cudaFree(r.asm_src); cudaFree(r.rows); cudaFree(r.upd_off);
+  cudaFree(r.upd_tgt); cudaFree(r.D);
+  r = RefactorPlan();
+}
+
 static void free_tri(LevelTri& t) {
   cudaFree(t.ptr); cudaFree(t.col); cudaFree(t.val); cudaFree(t.dinv); cudaFree(t.flag);
   t = LevelTri();
@@ -403,6 +416,8 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   free_tri(ctx->Uf);
   cudaFree(ctx->sf_ord);
   cudaFree(ctx->sf_ctl);
+  free_refactor(ctx->rf);
+  cudaFree(ctx->rf_err);
   for (int32_t* p : {ctx->cmp_off, ctx->cmp_rowsL, ctx->cmp_rowsU, ctx->cmp_segL, ctx->cmp_segU,
                      ctx->cmp_segLoff, ctx->cmp_segUoff, ctx->cmp_local})
     cudaFree(p);
@@ -1126,26 +1141,13 @@ static int build_solve_plan(peec_ctx* ctx, int64_t n) {
   return PEEC_OK;
 }
 
-static int peec_set_frequency_body(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,
-                                  const int64_t* yle_row, const int64_t* yle_col,
-                                  const double* yle_val, const int64_t* L_ptr,
-                                  const int64_t* L_col, const double* L_val,
-                                  const int64_t* U_ptr, const int64_t* U_col,
-                                  const double* U_val, const int64_t* perm_r,
-                                  const int64_t* perm_c, const double* row_scale) {
-  NvtxRange nvtx_range_("peec_set_frequency");
-  drop_graphs(ctx);
-  if (!ctx || !DZ || !L_ptr || !U_ptr || !perm_r || !perm_c) return badarg("peec_set_frequency");
-  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
-  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
-  const int64_t n = ctx->n, m = ctx->m;
-  ctx->w = w;
-  std::vector<c64> dz(m);
-  for (int64_t e = 0; e < m; ++e) dz[e] = mk<double>(DZ[2 * e], DZ[2 * e + 1]);
-  CTX_TRY(upload(&ctx->DZ, dz, ctx->st));
-  // Yle COO -> CSR (duplicates summed, as sparse() does)
-  std::vector<int32_t> yp(n + 1, 0), yc;
-  std::vector<c64> yv;
+// Yle from COO to CSR with duplicates summed, as sparse() does
+static int yle_csr(peec_ctx* ctx, int64_t n, int64_t yle_nnz, const int64_t* yle_row,
+                   const int64_t* yle_col, const double* yle_val, std::vector<int32_t>& yp,
+                   std::vector<int32_t>& yc, std::vector<c64>& yv) {
+  yp.assign(n + 1, 0);
+  yc.clear();
+  yv.clear();
   {
     std::vector<std::vector<std::pair<int32_t, cd>>> rowsv(n);
     for (int64_t q = 0; q < yle_nnz; ++q) {
@@ -1173,6 +1175,30 @@ static int peec_set_frequency_body(peec_ctx* ctx, double w, const double* DZ, in
       yp[r + 1] = (int32_t)yc.size();
     }
   }
+  return PEEC_OK;
+}
+
+static int peec_set_frequency_body(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,
+                                  const int64_t* yle_row, const int64_t* yle_col,
+                                  const double* yle_val, const int64_t* L_ptr,
+                                  const int64_t* L_col, const double* L_val,
+                                  const int64_t* U_ptr, const int64_t* U_col,
+                                  const double* U_val, const int64_t* perm_r,
+                                  const int64_t* perm_c, const double* row_scale) {
+  NvtxRange nvtx_range_("peec_set_frequency");
+  drop_graphs(ctx);
+  if (!ctx || !DZ || !L_ptr || !U_ptr || !perm_r || !perm_c) return badarg("peec_set_frequency");
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  const int64_t n = ctx->n, m = ctx->m;
+  ctx->w = w;
+  std::vector<c64> dz(m);
+  for (int64_t e = 0; e < m; ++e) dz[e] = mk<double>(DZ[2 * e], DZ[2 * e + 1]);
+  CTX_TRY(upload(&ctx->DZ, dz, ctx->st));
+  // Yle COO -> CSR (duplicates summed, as sparse() does)
+  std::vector<int32_t> yp, yc;
+  std::vector<c64> yv;
+  CTX_TRY(yle_csr(ctx, n, yle_nnz, yle_row, yle_col, yle_val, yp, yc, yv));
   CTX_TRY(upload(&ctx->yle_ptr, yp, ctx->st));
   CTX_TRY(upload(&ctx->yle_col, yc, ctx->st));
   CTX_TRY(upload(&ctx->yle_val, yv, ctx->st));
@@ -1186,6 +1212,11 @@ static int peec_set_frequency_body(peec_ctx* ctx, double w, const double* DZ, in
   }
   CTX_TRY(upload(&ctx->g_in, gin, ctx->st));
   CTX_TRY(upload(&ctx->g_out, gout, ctx->st));
+  // new factors: a refactorisation plan of the old ones no longer applies
+  free_refactor(ctx->rf);
+  ctx->have_rf = false;
+  ctx->h_gin = gin;
+  ctx->h_gout = gout;
   if (row_scale) {
     std::vector<double> rs(row_scale, row_scale + n);
     CTX_TRY(upload(&ctx->lu_rs, rs, ctx->st));
@@ -1199,6 +1230,251 @@ static int peec_set_frequency_body(peec_ctx* ctx, double w, const double* DZ, in
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->have_freq = true;
   return PEEC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// device refactorisation (refactor.cu)
+// ------------------------------------------------------------------------------------
+
+// position of column c in the sorted columns [b, e) of a CSR row, or -1
+static int64_t find_col(const std::vector<int32_t>& col, int64_t b, int64_t e, int32_t c) {
+  const auto it = std::lower_bound(col.begin() + b, col.begin() + e, c);
+  return (it != col.begin() + e && *it == c) ? it - col.begin() : -1;
+}
+
+// Device factorisation of SS from the permutations of the installed host factors (the
+// fill-reducing order and the pivot order): the symbolic fill of B = Pr SS Pc without
+// further pivoting (up-looking: row p's pattern is B(p,:) joined with U(k,:) for every k
+// of L(p,:), in increasing k, new entries left of p joining the queue), installed as
+// the solve's factor pattern (levels and solve plan rebuilt); then per slot its SS
+// contributions, and per L entry (p, k) the slots of row p that U(k,:) updates; then the
+// factors computed on the device at the installed frequency.
+static int refactor_run(peec_ctx* ctx);
+
+static int peec_lu_refactor_setup_body(peec_ctx* ctx, int64_t yle_nnz, const int64_t* yle_row,
+                                       const int64_t* yle_col) {
+  NvtxRange nvtx_range_("peec_lu_refactor_setup");
+  if (!ctx || (yle_nnz > 0 && (!yle_row || !yle_col))) return badarg("peec_lu_refactor_setup");
+  if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "no factors installed (peec_set_frequency)");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  free_refactor(ctx->rf);
+  ctx->have_rf = false;
+  const int64_t n = ctx->n, m = ctx->m, ns = ctx->ns;
+  // Yle pattern (CSR, duplicates merged, as set_frequency builds it)
+  std::vector<double> zeros(2 * std::max<int64_t>(yle_nnz, 1), 0.0);
+  std::vector<int32_t> yp, yc;
+  std::vector<c64> yv;
+  CTX_TRY(yle_csr(ctx, n, yle_nnz, yle_row, yle_col, zeros.data(), yp, yc, yv));
+  // topology on the host
+  std::vector<int32_t> e1(m), e2(m), sn(ns);
+  cudaMemcpy(e1.data(), ctx->n1, sizeof(int32_t) * m, cudaMemcpyDeviceToHost);
+  cudaMemcpy(e2.data(), ctx->n2, sizeof(int32_t) * m, cudaMemcpyDeviceToHost);
+  PEEC_CUDA_TRY(cudaMemcpy(sn.data(), ctx->snode, sizeof(int32_t) * ns, cudaMemcpyDeviceToHost));
+  std::vector<int32_t> prow(n);  // original row v -> permuted row
+  for (int64_t p = 0; p < n; ++p) prow[ctx->h_gin[p]] = (int32_t)p;
+  const std::vector<int32_t>& pcol = ctx->h_gout;  // original column u -> permuted column
+  // pattern of B, rows of permuted indices
+  std::vector<std::vector<int32_t>> brow(n);
+  auto add = [&](int32_t v, int32_t u) { brow[prow[v]].push_back(pcol[u]); };
+  for (int64_t e = 0; e < m; ++e) {
+    add(e1[e], e1[e]); add(e2[e], e2[e]); add(e1[e], e2[e]); add(e2[e], e1[e]);
+  }
+  for (int64_t i = 0; i < ns; ++i) add(sn[i], sn[i]);
+  for (int64_t r = 0; r < n; ++r)
+    for (int32_t q = yp[r]; q < yp[r + 1]; ++q) add((int32_t)r, yc[q]);
+  // symbolic up-looking factorisation
+  std::vector<int64_t> Lp(n + 1, 0), Up(n + 1, 0);
+  std::vector<int32_t> Lc, Uc;  // off-diagonal columns, sorted per row
+  std::vector<int32_t> mark(n, -1), row;
+  for (int64_t p = 0; p < n; ++p) {
+    row.clear();
+    std::priority_queue<int32_t, std::vector<int32_t>, std::greater<int32_t>> left;
+    mark[p] = (int32_t)p;  // the diagonal
+    for (int32_t j : brow[p])
+      if (mark[j] != p) {
+        mark[j] = (int32_t)p;
+        row.push_back(j);
+        if (j < p) left.push(j);
+      }
+    while (!left.empty()) {
+      const int32_t k = left.top();
+      left.pop();
+      for (int64_t t = Up[k]; t < Up[k + 1]; ++t) {
+        const int32_t j = Uc[t];
+        if (mark[j] != p) {
+          mark[j] = (int32_t)p;
+          row.push_back(j);
+          if (j < p) left.push(j);
+        }
+      }
+    }
+    std::sort(row.begin(), row.end());
+    for (int32_t j : row) (j < p ? Lc : Uc).push_back(j);
+    Lp[p + 1] = (int64_t)Lc.size();
+    Up[p + 1] = (int64_t)Uc.size();
+    if (Lc.size() >= (1u << 30) || Uc.size() >= (1u << 30))
+      return bad(ctx, PEEC_ERR_UNSUPPORTED, "factors too large for the device factorisation");
+  }
+  // install the pattern (diagonal included, placeholder values) with its levels and plan
+  {
+    auto tri = [&](const std::vector<int64_t>& op, const std::vector<int32_t>& oc, bool lower,
+                   LevelTri& T) {
+      std::vector<int64_t> ptr(n + 1, 0), col;
+      std::vector<double> val;
+      col.reserve(oc.size() + n);
+      val.reserve(2 * (oc.size() + n));
+      for (int64_t r = 0; r < n; ++r) {
+        if (!lower) { col.push_back(r); val.push_back(1.0); val.push_back(0.0); }
+        for (int64_t t = op[r]; t < op[r + 1]; ++t) {
+          col.push_back(oc[t]);
+          val.push_back(0.0);
+          val.push_back(0.0);
+        }
+        if (lower) { col.push_back(r); val.push_back(1.0); val.push_back(0.0); }
+        ptr[r + 1] = (int64_t)col.size();
+      }
+      return make_tri(ctx, T, n, ptr.data(), col.data(), val.data(), lower);
+    };
+    CTX_TRY(tri(Lp, Lc, true, ctx->Lf));
+    CTX_TRY(tri(Up, Uc, false, ctx->Uf));
+    CTX_TRY(build_solve_plan(ctx, n));
+  }
+  const LevelTri &L = ctx->Lf, &U = ctx->Uf;
+  const int64_t nL = L.hptr[n], nU = U.hptr[n];
+  // slot of B entry (p, q): L off-diagonal, diagonal, U off-diagonal
+  auto slot = [&](int32_t v, int32_t u) -> int64_t {
+    const int32_t p = prow[v], q = pcol[u];
+    if (q == p) return nL + p;
+    const int64_t at = q < p ? find_col(L.hcol, L.hptr[p], L.hptr[p + 1], q)
+                             : find_col(U.hcol, U.hptr[p], U.hptr[p + 1], q);
+    if (at < 0) return -1;
+    return q < p ? at : nL + n + at;
+  };
+  const int64_t nslot = nL + n + nU;
+  std::vector<std::pair<int64_t, uint32_t>> contrib;
+  contrib.reserve(4 * m + ns + yc.size());
+  for (int64_t e = 0; e < m; ++e) {
+    const int32_t a = e1[e], b = e2[e];
+    const int64_t s4[4] = {slot(a, a), slot(b, b), slot(a, b), slot(b, a)};
+    for (int t = 0; t < 4; ++t) {
+      if (s4[t] < 0) return bad(ctx, PEEC_ERR_STATE, "factor pattern misses an entry of SS");
+      contrib.push_back({s4[t], ((t < 2 ? 0u : 1u) << 30) | (uint32_t)e});
+    }
+  }
+  for (int64_t i = 0; i < ns; ++i) {
+    const int64_t sl = slot(sn[i], sn[i]);
+    if (sl < 0) return bad(ctx, PEEC_ERR_STATE, "factor pattern misses an entry of SS");
+    contrib.push_back({sl, (2u << 30) | (uint32_t)i});
+  }
+  for (int64_t r = 0; r < n; ++r)
+    for (int32_t q = yp[r]; q < yp[r + 1]; ++q) {
+      const int64_t sl = slot((int32_t)r, yc[q]);
+      if (sl < 0) return bad(ctx, PEEC_ERR_STATE, "factor pattern misses an entry of Yle");
+      contrib.push_back({sl, (3u << 30) | (uint32_t)q});
+    }
+  std::stable_sort(contrib.begin(), contrib.end(),
+                   [](const std::pair<int64_t, uint32_t>& x, const std::pair<int64_t, uint32_t>& y) {
+                     return x.first < y.first;
+                   });
+  std::vector<int64_t> aptr(nslot + 1, 0);
+  std::vector<uint32_t> asrc(contrib.size());
+  for (size_t i = 0; i < contrib.size(); ++i) {
+    aptr[contrib[i].first + 1]++;
+    asrc[i] = contrib[i].second;
+  }
+  for (int64_t s = 0; s < nslot; ++s) aptr[s + 1] += aptr[s];
+  // update targets: for L entry (p, k), each entry (k, j) of U(k,:) lands in row p at j
+  std::vector<int32_t> uoff(nL + 1, 0), utgt;
+  for (int64_t p = 0; p < n; ++p)
+    for (int32_t q = L.hptr[p]; q < L.hptr[p + 1]; ++q) {
+      const int32_t k = L.hcol[q];
+      for (int32_t t = U.hptr[k]; t < U.hptr[k + 1]; ++t) {
+        const int32_t j = U.hcol[t];
+        int64_t tg;
+        if (j == p) {
+          tg = -1;
+        } else if (j < p) {
+          tg = find_col(L.hcol, L.hptr[p], L.hptr[p + 1], j);
+        } else {
+          tg = find_col(U.hcol, U.hptr[p], U.hptr[p + 1], j);
+          if (tg >= 0) tg |= 0x40000000;
+        }
+        if (tg < -1 || (tg == -1 && j != p))
+          return bad(ctx, PEEC_ERR_STATE, "factor pattern misses a fill entry");
+        utgt.push_back((int32_t)tg);
+      }
+      if (utgt.size() > (size_t)INT32_MAX - 1)
+        return bad(ctx, PEEC_ERR_UNSUPPORTED, "device factorisation schedule too long");
+      uoff[q + 1] = (int32_t)utgt.size();
+    }
+  RefactorPlan& R = ctx->rf;
+  R.n = n;
+  R.nL = nL;
+  R.nU = nU;
+  R.lvl_off = L.lvl_off;
+  std::vector<int32_t> lrows(L.rows.begin(), L.rows.end());
+  CTX_TRY(upload(&R.asm_ptr, aptr, ctx->st));
+  CTX_TRY(upload(&R.asm_src, asrc, ctx->st));
+  CTX_TRY(upload(&R.rows, lrows, ctx->st));
+  CTX_TRY(upload(&R.upd_off, uoff, ctx->st));
+  if (utgt.empty()) utgt.push_back(0);
+  CTX_TRY(upload(&R.upd_tgt, utgt, ctx->st));
+  CTX_TRY(dalloc(&R.D, (size_t)n));
+  if (!ctx->rf_err) CTX_TRY(dalloc(&ctx->rf_err, 1));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  ctx->rf_yp = yp;
+  ctx->rf_yc = yc;
+  ctx->have_rf = true;
+  // the factors at the installed frequency, on the device
+  return refactor_run(ctx);
+}
+
+// assembles and factorises SS on the device from the state on the device (w, DZ, Yle)
+static int refactor_run(peec_ctx* ctx) {
+  ctx->have_freq = false;
+  PEEC_CUDA_TRY(cudaMemsetAsync(ctx->rf_err, 0, sizeof(int), ctx->st));
+  const LevelTri &L = ctx->Lf, &U = ctx->Uf;
+  const int nl = refactor_launch(ctx->rf, SfTri{L.ptr, L.col, L.val, L.dinv, L.flag},
+                                 SfTri{U.ptr, U.col, U.val, U.dinv, U.flag}, L.val, U.val, ctx->DZ,
+                                 ctx->invP, ctx->yle_val, ctx->w, ctx->rf_err, ctx->st);
+  if (nl < 0) return nl;
+  ctx->launches += nl;
+  int herr = 0;
+  cudaMemcpyAsync(&herr, ctx->rf_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->st);
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  if (herr)
+    return bad(ctx, PEEC_ERR_UNSUPPORTED,
+               "device factorisation met a zero or non-finite pivot: factorise this frequency "
+               "on the host (peec_set_frequency)");
+  ctx->have_freq = true;
+  return PEEC_OK;
+}
+
+// Per-frequency state with SS factorised on the device: DZ and Yle as for
+// peec_set_frequency (Yle with the pattern given to the set-up), then SS assembled and
+// factorised in the plan's pattern and permutations.
+static int peec_set_frequency_refactor_body(peec_ctx* ctx, double w, const double* DZ,
+                                            int64_t yle_nnz, const int64_t* yle_row,
+                                            const int64_t* yle_col, const double* yle_val) {
+  NvtxRange nvtx_range_("peec_set_frequency_refactor");
+  if (!ctx || !DZ || (yle_nnz > 0 && (!yle_row || !yle_col || !yle_val)))
+    return badarg("peec_set_frequency_refactor");
+  if (!ctx->have_rf) return bad(ctx, PEEC_ERR_STATE, "no refactorisation plan (peec_lu_refactor_setup)");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  drop_graphs(ctx);
+  const int64_t n = ctx->n, m = ctx->m;
+  std::vector<int32_t> yp, yc;
+  std::vector<c64> yv;
+  CTX_TRY(yle_csr(ctx, n, yle_nnz, yle_row, yle_col, yle_val, yp, yc, yv));
+  if (yp != ctx->rf_yp || yc != ctx->rf_yc)
+    return bad(ctx, PEEC_ERR_BADARG, "Yle pattern differs from the one of the refactorisation set-up");
+  ctx->have_freq = false;
+  ctx->w = w;
+  std::vector<c64> dz(m);
+  for (int64_t e = 0; e < m; ++e) dz[e] = mk<double>(DZ[2 * e], DZ[2 * e + 1]);
+  CTX_TRY(upload(&ctx->DZ, dz, ctx->st));
+  CTX_TRY(upload(&ctx->yle_val, yv, ctx->st));
+  return refactor_run(ctx);
 }
 
 // ------------------------------------------------------------------------------------
@@ -2217,6 +2493,20 @@ extern "C" int peec_set_rows_rcc(peec_ctx* ctx, const double* const rows[9],
 
 extern "C" int peec_set_rcc_frequency(peec_ctx* ctx, double freq_hz) {
   return guarded(ctx, __func__, [&] { return peec_set_rcc_frequency_body(ctx, freq_hz); });
+}
+
+extern "C" int peec_lu_refactor_setup(peec_ctx* ctx, int64_t yle_nnz, const int64_t* yle_row,
+                                      const int64_t* yle_col) {
+  return guarded(ctx, "peec_lu_refactor_setup",
+                 [&] { return peec_lu_refactor_setup_body(ctx, yle_nnz, yle_row, yle_col); });
+}
+
+extern "C" int peec_set_frequency_refactor(peec_ctx* ctx, double w, const double* DZ,
+                                           int64_t yle_nnz, const int64_t* yle_row,
+                                           const int64_t* yle_col, const double* yle_val) {
+  return guarded(ctx, "peec_set_frequency_refactor", [&] {
+    return peec_set_frequency_refactor_body(ctx, w, DZ, yle_nnz, yle_row, yle_col, yle_val);
+  });
 }
 
 extern "C" int peec_set_frequency(peec_ctx* ctx, double w, const double* DZ, int64_t yle_nnz,

@@ -40,6 +40,22 @@ struct CompPlan {
   int n;
 };
 
+// Device refactorisation of SS in a fixed pattern (refactor.cu): slots are the off-diagonal
+// entries of L, then the diagonal of U (D), then the off-diagonal entries of U
+struct RefactorPlan {
+  int64_t n = 0, nL = 0, nU = 0;
+  int64_t* asm_ptr = nullptr;    // per slot, its contributions in asm_src
+  uint32_t* asm_src = nullptr;   // contribution codes (type << 30 | index)
+  int32_t* rows = nullptr;       // rows grouped by L level
+  std::vector<int> lvl_off;      // level offsets into rows (host)
+  int32_t* upd_off = nullptr;    // per L entry (p, k): its targets in upd_tgt
+  int32_t* upd_tgt = nullptr;    // per entry of U(k,:): its slot in row p
+  c64* D = nullptr;              // diagonal of U
+};
+int refactor_launch(const RefactorPlan& R, const SfTri& L, const SfTri& U, c64* Lval, c64* Uval,
+                    const c64* DZ, const double* invP, const c64* yle, double w, int* err,
+                    cudaStream_t st);
+
 #define CTX_CHECK(expr)      \
   do {                       \
     int _r = (expr);         \

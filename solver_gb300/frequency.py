@@ -117,9 +117,11 @@ class FrequencyState:
     UMFPACK, FFT_solver_QS_S_type.jl:119; any sparse LU of SS gives the same operator)."""
 
     def __init__(self, w, escalings, incidence_selection, diagonals, Zs_info, lumped_elements,
-                 ports, z0, DZ=None):
+                 ports, z0, DZ=None, factor=True):
         """DZ (optional) replaces the edge impedances built from diagonals and Zs_info
-        (per-voxel conductivities, see gradient.dz_edges)."""
+        (per-voxel conductivities, see gradient.dz_edges). factor=False skips the host
+        factorisation (lu None): the state of a frequency the device factorises
+        (GpuOperator.set_frequency_refactor)."""
         A = incidence_selection["A"]
         Gamma = incidence_selection["Gamma"]
         n = A.shape[1]
@@ -138,6 +140,9 @@ class FrequencyState:
             self.DZ = np.asarray(DZ, dtype=np.complex128).ravel()
         self.invZ = sp.diags(1.0 / self.DZ)
         self.invP = sp.diags(1.0 / np.asarray(diagonals["P"]).ravel())
+        self.SS = self.lu = None
+        if not factor:
+            return
         SS = (self.Yle + A.T @ (self.invZ @ A) + 1j * w * ((Gamma @ self.invP) @ Gamma.T)).tocsc()
         self.SS = SS
         # SS is structurally symmetric: minimum degree on A'+A keeps the fill of COLAMD
@@ -233,7 +238,7 @@ class HostFrequency:
         self.w = w
         self.DZ = DZ
         self.Yle = Yle
-        self.lu = ExportedLU(lu_parts)
+        self.lu = ExportedLU(lu_parts) if lu_parts is not None else None
 
 
 _worker_static = None
@@ -244,9 +249,9 @@ def _worker_init(static):
     _worker_static = static
 
 
-def _worker_state(w):
-    fs = FrequencyState(w, *_worker_static)
-    return HostFrequency(w, fs.DZ, fs.Yle, export_lu(fs.lu))
+def _worker_state(w, factor=True):
+    fs = FrequencyState(w, *_worker_static, factor=factor)
+    return HostFrequency(w, fs.DZ, fs.Yle, export_lu(fs.lu) if factor else None)
 
 
 class FrequencyPool:
@@ -256,9 +261,11 @@ class FrequencyPool:
     the GIL for its allocations, so threads would serialise; processes do not.
 
     static: (escalings, incidence_selection, diagonals, Zs_info, lumped_elements,
-    ports, z0), sent to each worker once; w_of(k) the angular frequency of key k."""
+    ports, z0), sent to each worker once; w_of(k) the angular frequency of key k;
+    factor_of(k) (default: always) whether key k's state carries host factors."""
 
-    def __init__(self, static, w_of, order, workers=4, lookahead=4, keep=True, executor=None):
+    def __init__(self, static, w_of, order, workers=4, lookahead=4, keep=True, executor=None,
+                 factor_of=None):
         self._own = executor is None
         self._pool = FrequencyPool.executor(static, workers) if executor is None else executor
         self._w_of = w_of
@@ -269,6 +276,8 @@ class FrequencyPool:
         self._done = {}
         self._keep = keep
         self._lock = threading.Lock()
+        # key -> whether its state needs host factors (False: the device factorises)
+        self._factor_of = factor_of or (lambda k: True)
 
     @staticmethod
     def executor(static, workers):
@@ -283,7 +292,8 @@ class FrequencyPool:
 
     def _submit(self, k):
         if k not in self._done and k not in self._pending:
-            self._pending[k] = self._pool.submit(_worker_state, self._w_of(k))
+            self._pending[k] = self._pool.submit(_worker_state, self._w_of(k),
+                                                 bool(self._factor_of(k)))
 
     def get(self, k, pos=None):
         """The state of key k (blocking until a worker has built it). pos, the caller's

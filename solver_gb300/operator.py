@@ -268,6 +268,39 @@ class GpuOperator:
             _lib.ptr(Up), _lib.ptr(Uc), _lib.ptr(Uv), _lib.ptr(pr), _lib.ptr(pc), None))
         self._freq_key = key
 
+    @staticmethod
+    def _yle_coo(Yle):
+        Y = sp.coo_matrix(Yle)
+        return (Y.row.astype(np.int64), Y.col.astype(np.int64),
+                np.ascontiguousarray(Y.data.astype(np.complex128)))
+
+    def enable_refactor(self, Yle):
+        """Later frequencies may factorise SS on the device (set_frequency_refactor) in
+        the pattern and pivot order of the factors installed now; Yle gives the
+        admittance pattern those frequencies share."""
+        if tuple(Yle.shape) != (self.n, self.n):
+            raise ValueError(f"Yle must be {self.n} x {self.n}")
+        yr, yc, _ = self._yle_coo(Yle)
+        _lib.check(self.h, self.L.peec_lu_refactor_setup(self.h, int(yr.size), _lib.ptr(yr),
+                                                         _lib.ptr(yc)))
+
+    def set_frequency_refactor(self, w, DZ, Yle, key=None):
+        """One frequency's state with SS assembled and factorised on the device (after
+        enable_refactor); key as for set_frequency."""
+        if key is not None and self._same_key(key, self._freq_key):
+            return
+        DZ = np.ascontiguousarray(np.asarray(DZ, dtype=np.complex128).ravel())
+        if DZ.size != self.m:
+            raise ValueError(f"DZ has {DZ.size} entries, expected {self.m}")
+        if tuple(Yle.shape) != (self.n, self.n):
+            raise ValueError(f"Yle must be {self.n} x {self.n}")
+        yr, yc, yv = self._yle_coo(Yle)
+        self._freq_key = None
+        _lib.check(self.h, self.L.peec_set_frequency_refactor(
+            self.h, float(w), _lib.ptr(DZ.view(np.float64)), int(yr.size), _lib.ptr(yr),
+            _lib.ptr(yc), _lib.ptr(yv.view(np.float64))))
+        self._freq_key = key
+
     # -- operator ----------------------------------------------------------------------
     def matvec(self, x, precision=0):
         x = np.ascontiguousarray(np.asarray(x, dtype=np.complex128).ravel())
