@@ -4,24 +4,26 @@
 Metric: frequency-point solves per second at 1e-8 relative (left-preconditioned)
 residual on the 128x128x64 synthetic voxel geometry (Bernoulli(0.3) occupancy,
 copper / dielectric 50/50, 4 ports, 10 frequencies 10 MHz-10 GHz). One step = one
-frequency point: the host sparse-LU factorisation of that frequency's Schur
-complement, then for each of the 4 ports its right-hand side and a solve warm
-started from the previous frequency's solution (FFT_solver_QS_S_type.jl:60-209).
+frequency point: that frequency's state (DZ, Yle, the factorised SS), then for each of
+the 4 ports its right-hand side and a solve warm started from the previous
+frequency's solution (FFT_solver_QS_S_type.jl:60-209).
 
 * value: device throughput of the mixed-precision path (FP32 circulant
-  convolutions inside FP64 iterative refinement) -- CUDA events on the library's
-  stream around the GPU part of each step (frequency upload + 4 port solves), the
-  host LU of each frequency prepared beforehand;
-* e2e: the same steps end to end through the public API with host buffers, wall
-  clock including the host LU, H2D uploads and D2H of each solution;
-* fp64_plain: the reference algorithm (FP64 convolutions, Householder GMRES) timed
-  on the first frequency points;
+  convolutions inside iterative refinement) on 4 port lanes -- CUDA events spanning
+  the lanes' streams around the GPU part of each step (frequency state, SS
+  factorisation on the GPU with --lu device, 4 port solves), the host parts of the
+  states prepared beforehand;
+* e2e: the same steps end to end through the public API with host buffers, wall clock
+  including each point's host state (built in worker processes started on it inside the
+  timed region), uploads and the download of each solution;
+* fp64_plain: the reference algorithm (FP64 convolutions, Householder GMRES) on the
+  same lanes and points; mixed_fp64_residual: mixed with FP64 refinement residuals;
+* accuracy: port impedances of every arm against FP64 GMRES at 1e-12, per frequency;
 * roofline: the z passes of the FP32 convolutions (forward FFT, 3x3 spectral
   product, inverse FFT), algorithmic bytes from the family descriptors, duration from
   CUDA events around the pass;
 * cpu_baseline: the CPU oracle restatement (reference 2N extents, scipy FFT on all
-  host cores, SuperLU) -- one operator application + one factorisation, scaled by
-  the FP64 GMRES matvec count measured in this run.
+  host cores, SuperLU) timed on complete port solves.
 
 Multi-GPU: the path does not shard; --gpus N runs N independent replicas
 (torchrun, one rank per GPU) and reports their summed throughput.
@@ -72,6 +74,10 @@ def parse():
     ap.add_argument("--host-states", choices=["processes", "thread"], default="processes",
                     help="where the per-frequency host states (SuperLU) are built: spawned "
                          "worker processes (default) or one worker thread")
+    ap.add_argument("--lu", choices=["device", "host"], default="device",
+                    help="where SS is factorised at the timed frequencies: on the GPU in the "
+                         "pattern of one host factorisation made in the warm-up (device), or "
+                         "by SuperLU on the host at every frequency (host)")
     ap.add_argument("--lanes", type=int, default=4,
                     help="concurrent port solves (contexts + host threads), at most the ports")
     ap.add_argument("--inner-tol", type=float, default=1e-7,
@@ -280,11 +286,11 @@ def fill_report(P, with_cpu):
     return out
 
 
-def freq_state(P, k):
+def freq_state(P, k, factor=True):
     from solver_gb300 import frequency as fq
     w = 2 * np.pi * P["freqs"][k] * P["esc"]["freq"]
     return fq.FrequencyState(w, P["esc"], P["inc"], P["diag"], P["Zs"], P["le"], P["ports"],
-                             P["z0"])
+                             P["z0"], factor=factor)
 
 
 def solve_point_lanes(P, fs, Vrest, tol):
@@ -323,13 +329,18 @@ def solve_point_lanes(P, fs, Vrest, tol):
     return S, work, _point_bytes(P, fs, npt), npt * 2 * (m + ns + n) * 16
 
 
-def _point_bytes(P, fs, npt):
+def _point_bytes(P, fs, npt, nlanes=1):
+    """Host-to-device bytes of one frequency point: each lane's copy of the state (DZ,
+    Yle, and the host factors with their permutations when the host factorised), and
+    the ports' vectors."""
     from solver_gb300.frequency import export_lu
     m, n = P["inc"]["A"].shape
     N = m + P["inc"]["Gamma"].shape[1] + n
-    (_, Lc, _), (_, Uc, _), _, _ = export_lu(fs.lu)
-    return (fs.DZ.nbytes + (Lc.size + Uc.size) * 24 + (2 * n + 2) * 8 * 2 + 2 * n * 8 +
-            fs.Yle.nnz * 32 + npt * (2 * N * 16))
+    state = fs.DZ.nbytes + fs.Yle.nnz * 32
+    if fs.lu is not None:
+        (_, Lc, _), (_, Uc, _), _, _ = export_lu(fs.lu)
+        state += (Lc.size + Uc.size) * 24 + (2 * n + 2) * 8 * 2 + 2 * n * 8
+    return nlanes * state + npt * (2 * N * 16)
 
 
 def solve_point(P, fs, Vrest, mode, tol):
@@ -717,7 +728,7 @@ def lane_sweep(P, lanes, seq, get_state, Vrest, tol, mode, solve_kw, timer):
     if timer is not None:
         timer.start()
     lanes.sweep(seq, get_state, lambda k: None, pn, P["esc"]["Is"], Vrest, lambda k: tol,
-                solve_kw, record, mode=mode)
+                solve_kw, record, mode=mode, device_lu=P["device_lu"])
     gpu_ms = timer.stop() if timer is not None else None
     wall = time.perf_counter() - t0
     if gpu_ms is None:
@@ -754,6 +765,10 @@ def main():
     ws, rank, local = dist_init()
     P = setup_problem(device=local, grid=args.grid)
     P["inner_tol"] = args.inner_tol
+    P["device_lu"] = args.lu == "device"
+    # with device LU only the first state carries host factors (the pattern and pivot
+    # order); every later frequency's SS is assembled and factorised on the GPU
+    factor_first = (lambda k: k == 0) if P["device_lu"] else (lambda k: True)
     op = P["op"]
     nf = len(P["freqs"])
     tol = float(P["settings"]["tol"])
@@ -769,20 +784,21 @@ def main():
     # of frequency key_of(q), each state kept once built (lanes share it)
     if args.host_states == "processes":
         ex = FrequencyPool.executor(static, nworkers)
-        make_pool = lambda order, key_of: FrequencyPool(
+        make_pool = lambda order, key_of, factor_of=None: FrequencyPool(
             static, lambda q: w_of(key_of(q)), order, workers=nworkers, lookahead=nworkers,
-            keep=True, executor=ex)
+            keep=True, executor=ex, factor_of=factor_of)
     else:
         # one worker thread, no child processes (for runs under a profiler)
         from solver_gb300.frequency import StatePrefetcher
         ex = None
         nworkers = 1
-        make_pool = lambda order, key_of: StatePrefetcher(lambda q: freq_state(P, key_of(q)),
-                                                          order, keep=True)
+        make_pool = lambda order, key_of, factor_of=None: StatePrefetcher(
+            lambda q: freq_state(P, key_of(q), (factor_of or (lambda _: True))(q)), order,
+            keep=True)
     warm_seq = [i % nf for i in range(args.warmup)]
     seq = [i % nf for i in range(args.warmup, args.warmup + args.steps)]
     # cached states for the device-timed passes (inputs prepared before the timed region)
-    cache = make_pool([0] + warm_seq + seq, lambda k: k)
+    cache = make_pool([0] + warm_seq + seq, lambda k: k, factor_first)
     state = cache.get
 
     # -- operator profile and roofline (FP32 and FP64 convolutions) --------------------------
@@ -811,6 +827,12 @@ def main():
     from solver_gb300.api import PortLanes
     nlanes = max(1, min(args.lanes, npt))
     lanes = PortLanes(op, nlanes)
+    if P["device_lu"]:
+        # each lane's factor pattern and pivot order: one host factorisation (frequency 0),
+        # made here, outside the timed regions, as the fill is
+        from solver_gb300.api import install_state
+        for o in lanes.ops:
+            install_state(o, state(0), True)
     try:
         timer = LaneTimer(lanes, local)
     except Exception:
@@ -841,7 +863,8 @@ def main():
     sync()
     t_e0 = time.perf_counter()
     # keyed by position in the timed sequence: a frequency visited twice is built twice
-    fresh = make_pool(list(range(len(seq))), lambda pos: seq[pos])
+    fresh = make_pool(list(range(len(seq))), lambda pos: seq[pos],
+                      (lambda pos: False) if P["device_lu"] else None)
     waits = [0.0]
 
     def fresh_state(k, pos):
@@ -858,7 +881,7 @@ def main():
     clk = clocks.stop()
     m_, n_ = P["inc"]["A"].shape
     ns_ = P["inc"]["Gamma"].shape[1]
-    h2d = sum(_point_bytes(P, state(k), npt) for k in seq)
+    h2d = sum(_point_bytes(P, state(k), npt, nlanes) for k in seq)
     d2h = len(seq) * npt * 2 * (m_ + ns_ + n_) * 16
     value, e2e_v, gpu_s, wall_s = whole_job_rates(ws, args.steps, gpu_ms / 1e3, wall_e2e)
 
@@ -940,11 +963,17 @@ def main():
                    "m_edges": int(op.m), "ns_surfaces": int(op.ns), "n_nodes": int(op.n),
                    "l2": "inputs larger than L2 (Krylov basis and spectra > 129 MB)",
                    "parallelism": f"replicas x{ws}", "port_lanes": nlanes,
+                   "lu": args.lu,
                    "timed_points": [fkey(k) for k in seq]},
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps),
                 "host_states": "built inside the timed region by worker processes started on "
-                               "them only then (no state of a timed point exists before it)",
+                               "them only then (no state of a timed point exists before it)"
+                               + ("; DZ and Yle on the host, SS assembled and factorised on "
+                                  "the GPU (one host factorisation of frequency 0 in the "
+                                  "warm-up fixes the pattern and pivot order)"
+                                  if P["device_lu"] else
+                                  "; SS factorised by SuperLU on the host at every point"),
                 "host_state_wait_ms_per_step": waits[0] / max(1, nlanes) * 1e3 / args.steps,
                 "host_state_workers": nworkers},
         "gpu_launches": int(launches),
