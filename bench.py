@@ -609,12 +609,12 @@ def run_batched_sweep(args):
     reqs = configs.batched_sweep()
     cache = RowCache() if args.reuse_fills else None
     t = time.perf_counter()
-    res = api.sweep_many(reqs, mode="mixed", concurrency=args.lanes, row_cache=cache)
+    res = api.sweep_many(reqs, mode="mixed", concurrency=args.lanes, row_cache=cache, lu=args.lu)
     dt = time.perf_counter() - t
     systems = sum(len(r["info"]) for r in res)
     print(json.dumps({"metric": "batched sweep: port solves/s (12 grids x 64 frequencies, 1e-8)",
                       "value": systems / dt, "unit": "port solves/s", "systems": systems,
-                      "wall_s": dt, "concurrency": args.lanes,
+                      "wall_s": dt, "concurrency": args.lanes, "lu": args.lu,
                       "fills": None if cache is None else {"filled": cache.misses,
                                                            "reused": cache.hits},
                       "flags": sorted({r["flag"] for x in res for r in x["info"]}),
