@@ -250,7 +250,7 @@ def setup_problem(device=0, grid=None):
     from solver_gb300 import configs, mesher
     from solver_gb300.operator import GpuOperator
     req = configs.random_128x128x64() if grid is None else configs.random_mixed(tuple(grid))
-    out, freqs, settings, z0, grid = mesher.parse_request(req)
+    out, freqs, settings, z0, grid = mesher.parse_request(req, device=device)
     esc, inc, cc, diag, exp, ports, le, li, Zs = out
     op = GpuOperator(inc, exp, diag["P"], device=device)
     rows = op.fill(cc["origin"], cc["sx"], cc["sy"], cc["sz"], esc["Lp"], esc["P"],

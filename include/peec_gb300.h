@@ -167,6 +167,27 @@ int peec_set_frequency_refactor(peec_ctx* ctx, double w, const double* DZ, int64
                                 const int64_t* yle_row, const int64_t* yle_col,
                                 const double* yle_val);
 
+/*
+ * Voxel mesher on the GPU (mesher_FFT.jl's topology: create_volumes_mapping.jl,
+ * create_Grids_externals.jl, create_nodes_ref.jl, create_mapping_A{x,y,z}_v2.jl,
+ * create_A_mats_and_find_borders_with_map_Zs.jl, create_mapping_Gamma_no_rep.jl), no
+ * context needed. grids: G x Nx x Ny x Nz bytes (nonzero: occupied), x fastest per grid;
+ * dominant[k] != 0 for conductor grids; sigma[k] the conductivities. Runs on `device`
+ * (the caller's current device is restored); 27 Nx Ny Nz must fit in int32. Returns a
+ * handle or NULL (the reason in *err_out when err_out is not NULL). The handle's arrays
+ * (int64 unless noted): "vox_map" (per cell, 1-based voxel number, 0 empty), "vox_node",
+ * "counts" (voxels, nodes, x/y/z edges, surfaces per family), "edge_n1", "edge_n2",
+ * "edge_cell", "edge_mat", "edge_border1", "edge_border2", "edge_zs" (4 per edge),
+ * "surf_node", "surf_fam", "surf_cell", "nodes" and "nodes_red" (double). Lengths by
+ * peec_mesh_gpu_len (-1: no such array; *is_double set), contents by peec_mesh_gpu_copy.
+ */
+void* peec_mesh_gpu_build(const uint8_t* grids, int G, int Nx, int Ny, int Nz,
+                          const uint8_t* dominant, const double* sigma, int device,
+                          const char** err_out);
+int64_t peec_mesh_gpu_len(void* mesh, const char* name, int* is_double);
+int peec_mesh_gpu_copy(void* mesh, const char* name, void* out);
+void peec_mesh_gpu_free(void* mesh);
+
 /* y = M^-1 K x (ComputeMatrixVectorFTT); x, y host, length N = m + ns + n complex. */
 int peec_matvec(peec_ctx* ctx, const double* x, double* y, int precision);
 /* same on device pointers (complex double) */

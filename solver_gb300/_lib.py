@@ -27,7 +27,8 @@ EXPORTS = ("peec_version", "peec_ctx_create", "peec_ctx_destroy", "peec_last_err
            "peec_multidot_noalloc", "peec_set_residual_precision",
            "peec_set_lu_component_max", "peec_adjoint", "peec_check_wait_limit",
            "peec_fill_rcc", "peec_set_rows_rcc", "peec_set_rcc_frequency",
-           "peec_lu_refactor_setup", "peec_set_frequency_refactor")
+           "peec_lu_refactor_setup", "peec_set_frequency_refactor",
+           "peec_mesh_gpu_build", "peec_mesh_gpu_len", "peec_mesh_gpu_copy", "peec_mesh_gpu_free")
 
 
 PREC_FP64, PREC_FP32, PREC_FF = 0, 1, 2
@@ -87,6 +88,14 @@ def load(build_if_missing: bool = True):
                                     ctypes.c_double]
     L.peec_set_rcc_frequency.argtypes = [P, ctypes.c_double]
     L.peec_lu_refactor_setup.argtypes = [P, ctypes.c_int64, P, P]
+    L.peec_mesh_gpu_build.restype = ctypes.c_void_p
+    L.peec_mesh_gpu_build.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      P, P, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p)]
+    L.peec_mesh_gpu_len.restype = ctypes.c_int64
+    L.peec_mesh_gpu_len.argtypes = [P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+    L.peec_mesh_gpu_copy.argtypes = [P, ctypes.c_char_p, P]
+    L.peec_mesh_gpu_free.argtypes = [P]
+    L.peec_mesh_gpu_free.restype = None
     L.peec_set_frequency_refactor.argtypes = [P, ctypes.c_double, P, ctypes.c_int64, P, P, P]
     L.peec_set_frequency.argtypes = [P, ctypes.c_double, P, ctypes.c_int64, P, P, P, P, P, P, P,
                                      P, P, P, P, P]

@@ -521,7 +521,7 @@ def do_solving_fft(request, id="job", mode="mixed", lanes=1, device=0, stop_flag
     if solver_type not in (1, 2):
         raise NotImplementedError("solverType must be 1 (quasi-static) or 2 (Rcc); the "
                                   "reference's Taylor variant (3) is commented out")
-    out, freqs, settings, z0, grid = mesher.parse_request(request)
+    out, freqs, settings, z0, grid = mesher.parse_request(request, device=device)
     esc, inc, cc, diag, exp, ports, le, li, Zs = out
     op = GpuOperator(inc, exp, diag["P"], device=device)
     try:
@@ -559,7 +559,7 @@ def sweep_many(requests, mode="mixed", concurrency=4, device=0, row_cache=None, 
     from .operator import GpuOperator
 
     def one(req):
-        out, freqs, settings, z0, grid = mesher.parse_request(req)
+        out, freqs, settings, z0, grid = mesher.parse_request(req, device=device)
         esc, inc, cc, diag, exp, ports, le, li, Zs = out
         op = GpuOperator(inc, exp, diag["P"], device=device)
         try:

@@ -56,9 +56,16 @@ def _lib():
     return _mesh_lib
 
 
-def _raw_mesh(grids: np.ndarray, dominant, sigma) -> dict:
+MESH_ARRAYS = ("vox_map", "vox_node", "counts", "edge_n1", "edge_n2", "edge_cell", "edge_mat",
+               "edge_border1", "edge_border2", "edge_zs", "surf_node", "surf_fam", "surf_cell",
+               "nodes", "nodes_red")
+
+
+def _raw_mesh(grids: np.ndarray, dominant, sigma, device=None) -> dict:
     """Runs the native mesher; grids is (G, Nx, Ny, Nz) bool, dominant a length-G mask of
-    the conductor grids and sigma the G conductivities (the library reads G of each)."""
+    the conductor grids and sigma the G conductivities (the library reads G of each).
+    device None: the host mesher (C++, OpenMP); an int: the GPU mesher on that device
+    (the same arrays, index for index)."""
     G, Nx, Ny, Nz = grids.shape
     g = np.ascontiguousarray(np.transpose(grids.astype(np.uint8), (0, 3, 2, 1)))  # x fastest
     dom = np.ascontiguousarray(np.asarray(dominant, dtype=np.uint8))
@@ -66,23 +73,32 @@ def _raw_mesh(grids: np.ndarray, dominant, sigma) -> dict:
     if dom.shape != (G,) or sig.shape != (G,):
         raise ValueError(f"dominant and sigma need one entry per grid ({G}); "
                          f"got {dom.shape} and {sig.shape}")
-    L = _lib()
-    h = L.peec_mesh_build(g.ctypes.data, G, Nx, Ny, Nz, dom.ctypes.data, sig.ctypes.data)
-    if not h:
-        raise ValueError("mesher rejected the grid")
+    if device is None:
+        L = _lib()
+        h = L.peec_mesh_build(g.ctypes.data, G, Nx, Ny, Nz, dom.ctypes.data, sig.ctypes.data)
+        length, copy, free = L.peec_mesh_len, L.peec_mesh_copy, L.peec_mesh_free
+        if not h:
+            raise ValueError("mesher rejected the grid")
+    else:
+        from . import _lib as _glib
+        L = _glib.load()
+        err = ctypes.c_char_p()
+        h = L.peec_mesh_gpu_build(g.ctypes.data, G, Nx, Ny, Nz, dom.ctypes.data,
+                                  sig.ctypes.data, int(device), ctypes.byref(err))
+        length, copy, free = L.peec_mesh_gpu_len, L.peec_mesh_gpu_copy, L.peec_mesh_gpu_free
+        if not h:
+            raise RuntimeError((err.value or b"GPU mesher failed").decode())
     out = {}
     try:
-        for name in ("vox_map", "vox_node", "counts", "edge_n1", "edge_n2", "edge_cell",
-                     "edge_mat", "edge_border1", "edge_border2", "edge_zs", "surf_node",
-                     "surf_fam", "surf_cell", "nodes", "nodes_red"):
+        for name in MESH_ARRAYS:
             isd = ctypes.c_int(0)
-            n = L.peec_mesh_len(h, name.encode(), ctypes.byref(isd))
+            n = length(h, name.encode(), ctypes.byref(isd))
             arr = np.empty(n, dtype=np.float64 if isd.value else np.int64)
             if n > 0:
-                L.peec_mesh_copy(h, name.encode(), arr.ctypes.data)
+                copy(h, name.encode(), arr.ctypes.data)
             out[name] = arr
     finally:
-        L.peec_mesh_free(h)
+        free(h)
     return out
 
 
@@ -253,7 +269,7 @@ def _f1d(i, j, k, M, N):
 
 
 def mesher_FFT(materials, sx, sy, sz, grids, ports, lumped_elements, origin, dominant_list,
-               build_full_expansions=True):
+               build_full_expansions=True, device=None):
     """Host mesher producing the structures of mesher_FFT.jl:1-112.
 
     grids: (G, Nx, Ny, Nz) bool, in the same order as ``materials`` (the reference
@@ -267,7 +283,7 @@ def mesher_FFT(materials, sx, sy, sz, grids, ports, lumped_elements, origin, dom
     dominant = np.zeros(G, dtype=np.uint8)
     dominant[list(dominant_list)] = 1
     sigma = [materials[k]["sigmar"] for k in range(G)]
-    raw = _raw_mesh(grids, dominant, sigma)
+    raw = _raw_mesh(grids, dominant, sigma, device)
     num_vox, n, mx, my, mz, N1, N2, N3 = (int(v) for v in raw["counts"])
     m = mx + my + mz
     ns = N1 + N2 + N3
@@ -381,9 +397,12 @@ def mesher_FFT(materials, sx, sy, sz, grids, ports, lumped_elements, origin, dom
     vox_node = raw["vox_node"]
 
     def nearest(pt, skip):
+        # the first voxel (in voxel order) nearest to pt, skipping `skip`: the first entry of
+        # a stable sort by distance that is not `skip` (find_voxels_port_pp.jl:6-7)
         d = np.sqrt(np.sum((centri_vox - np.asarray(pt, dtype=np.float64)[None, :]) ** 2, axis=1))
-        order = np.argsort(d, kind="stable")
-        return int(order[0] if order[0] != skip else order[1])
+        if skip >= 0:
+            d[skip] = np.inf
+        return int(np.argmin(d))
 
     ports = dict(ports)
     P0 = np.asarray(ports["port_start"], dtype=np.float64).reshape(-1, 3)
@@ -453,12 +472,13 @@ def _compute_zs(materials, mats, b1, b2, zs, offs, sx, sy, sz):
 # request parsing
 # ----------------------------------------------------------------------------------------
 
-def parse_request(req: dict):
+def parse_request(req: dict, device=None):
     """Reads a solve request body (mesherOutput / solverInput / solverAlgoParams) the way
     doSolvingFFT does (do_solving_fft.jl:1-98) and runs the mesher.
 
     Grid order is the JSON key order of ``mesher_matrices`` (the reference iterates a
     Julia Dict there); ``materials`` is indexed by that grid order, as in the reference.
+    device: None meshes on the host (C++); an int meshes on that GPU (the same arrays).
     """
     mo, si = req["mesherOutput"], req["solverInput"]
     escal = get_escal_from(si.get("unit", "m"))
@@ -496,7 +516,8 @@ def parse_request(req: dict):
               "R_value": np.array([float(p["rlcParams"].get("resistance", 0.0)) for p in les]),
               "L_value": np.array([float(p["rlcParams"].get("inductance", 0.0)) for p in les]),
               "C_value": np.array([float(p["rlcParams"].get("capacitance", 0.0)) for p in les])}
-    out = mesher_FFT(MATERIALS, sx, sy, sz, grids, ports, lumped, origin, dominant)
+    out = mesher_FFT(MATERIALS, sx, sy, sz, grids, ports, lumped, origin, dominant,
+                     device=device)
     ap = req.get("solverAlgoParams", {})
     settings = {"Inner_Iter": int(ap.get("innerIteration", 100)),
                 "Outer_Iter": int(ap.get("outerIteration", 1)),
