@@ -78,6 +78,12 @@ def parse():
                     help="where SS is factorised at the timed frequencies: on the GPU in the "
                          "pattern of one host factorisation made in the warm-up (device), or "
                          "by SuperLU on the host at every frequency (host)")
+    ap.add_argument("--krylov-loop", choices=["device", "host"], default="device",
+                    help="GMRES iterations in the device-resident loop (a CUDA graph with a "
+                         "WHILE node) or one host round trip per iteration (same kernels)")
+    ap.add_argument("--lu-solve", choices=["groups", "global"], default="groups",
+                    help="LU solves per warp group of factor components (groups) or by the "
+                         "synchronisation-free global scheme alone (global)")
     ap.add_argument("--lanes", type=int, default=4,
                     help="concurrent port solves (contexts + host threads), at most the ports")
     ap.add_argument("--inner-tol", type=float, default=1e-7,
@@ -615,6 +621,7 @@ def run_batched_sweep(args):
     print(json.dumps({"metric": "batched sweep: port solves/s (12 grids x 64 frequencies, 1e-8)",
                       "value": systems / dt, "unit": "port solves/s", "systems": systems,
                       "wall_s": dt, "concurrency": args.lanes, "lu": args.lu,
+                      "krylov_loop": args.krylov_loop, "lu_solve": args.lu_solve,
                       "fills": None if cache is None else {"filled": cache.misses,
                                                            "reused": cache.hits},
                       "flags": sorted({r["flag"] for x in res for r in x["info"]}),
@@ -750,6 +757,10 @@ def z_errors(seq, cols, Zref, npt, z0):
 
 def main():
     args = parse()
+    if args.impl != "reference":
+        from solver_gb300.operator import GpuOperator
+        GpuOperator.DEVICE_LOOP = args.krylov_loop == "device"
+        GpuOperator.LU_COMPONENT_MAX = 512 if args.lu_solve == "groups" else 0
     if getattr(args, "adjoint", False):
         run_adjoint(args)
         return
@@ -963,7 +974,7 @@ def main():
                    "m_edges": int(op.m), "ns_surfaces": int(op.ns), "n_nodes": int(op.n),
                    "l2": "inputs larger than L2 (Krylov basis and spectra > 129 MB)",
                    "parallelism": f"replicas x{ws}", "port_lanes": nlanes,
-                   "lu": args.lu,
+                   "lu": args.lu, "krylov_loop": args.krylov_loop, "lu_solve": args.lu_solve,
                    "timed_points": [fkey(k) for k in seq]},
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps),

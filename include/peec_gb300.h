@@ -82,6 +82,30 @@ int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t mx, int64_t
                       int64_t ns, const int32_t* surf_fam, const int64_t* surf_cell,
                       const int64_t* surf_node, int64_t n);
 
+/*
+ * Topology of a mesh without voxel lattices (the dense RIS solver,
+ * solverRis/iter_solver_QS_S_type.jl): the edges' end nodes (A, -1 at n1 and +1 at
+ * n2, edges ordered x, y, z with mx, my, mz of each) and the surfaces' nodes (Gamma,
+ * one node per surface). The operator then needs peec_set_dense; the circulant entry
+ * points (peec_fill, peec_set_rows, the Rcc rows, peec_adjoint) return PEEC_ERR_STATE.
+ */
+int peec_set_incidence(peec_ctx* ctx, int64_t mx, int64_t my, int64_t mz,
+                       const int64_t* edge_n1, const int64_t* edge_n2, int64_t ns,
+                       const int64_t* surf_node, int64_t n);
+
+/*
+ * Dense operator blocks (ComputeMatrixVectorRis, solverRis/compute_matrix_vector.jl:1-33):
+ * Lp_x (mx x mx), Lp_y (my x my), Lp_z (mz x mz) and P (ns x ns), real, column-major
+ * (Lp_data[:Lp_x], ..., P_data[:P]). Each operator application multiplies them with the
+ * edge currents and surface charges (FP64, or an FP32 copy in PEEC_PREC_FP32), Lp without
+ * its diagonal; the frequency state (peec_set_frequency) takes DZ = Z_self + jw diag(Lp),
+ * the denominator of the RIS solver's invZ, so that the first block row is
+ * jw Lp I + Z_self I + A Phi and the preconditioner is the RIS solver's. Replaces a
+ * circulant operator set before; peec_fill / peec_set_rows replace the dense one.
+ */
+int peec_set_dense(peec_ctx* ctx, const double* Lp_x, const double* Lp_y, const double* Lp_z,
+                   const double* P);
+
 /* P self terms diag(P) per surface (diagonals["P"]); invP = 1 ./ diagP. */
 int peec_set_pdiag(peec_ctx* ctx, const double* diagP);
 
@@ -252,10 +276,12 @@ int peec_check_wait_limit(peec_ctx* ctx);
 
 /*
  * Work split of the LU solves inside the operator: rows of connected components of
- * the factors with at most max_rows rows (0..512, default 0) are solved one
- * component per warp; all other rows by the synchronisation-free global scheme. Both
- * give the same results to rounding; 0 routes every row through the global scheme.
- * Takes effect at once. No counterpart in the reference (UMFPACK solves, FFT_solver_QS_S_type.jl:119).
+ * the factors with at most max_rows rows (0..512, default 512) are solved per warp, the
+ * components of at most 32 rows packed several to a warp, each warp's rows, entries and
+ * right-hand sides first loaded into shared memory; all other rows by the
+ * synchronisation-free global scheme. Both give the same results to rounding; 0 routes
+ * every row through the global scheme. Takes effect at once. No counterpart in the
+ * reference (UMFPACK solves, FFT_solver_QS_S_type.jl:119).
  */
 int peec_set_lu_component_max(peec_ctx* ctx, int max_rows);
 
@@ -271,6 +297,26 @@ int peec_set_residual_precision(peec_ctx* ctx, int precision);
  * Krylov steps and return PEEC_ERR_CANCELLED (gmres flag 99). NULL disables.
  */
 int peec_set_stop_flag(peec_ctx* ctx, volatile int* flag);
+
+/*
+ * The GMRES iterations of peec_gmres and of peec_solve_mixed's inner solves run on the
+ * device: the scalar work of an iteration (reflector heads, Givens rotations, the
+ * least-squares right-hand side, the residual estimate) is one FP64 kernel, and a CUDA
+ * graph with a WHILE conditional node repeats the iteration until the estimate reaches
+ * the tolerance or the restart cycle is full, with no host synchronisation in between.
+ * The host keeps the reference's control flow (gmres_custom.jl:129-250): the checks on
+ * the true residual, stagnation, restarts. on = 0 runs the same kernels one iteration
+ * per host round trip instead (the same results, bit for bit); the stop flag is then
+ * polled every iteration rather than every run of iterations. Default 1.
+ * No counterpart in the reference.
+ */
+int peec_set_device_loop(peec_ctx* ctx, int on);
+
+/*
+ * Since the context was created: launches of the device-loop graph, and the GMRES
+ * iterations they ran.
+ */
+int peec_device_loop_stats(const peec_ctx* ctx, int64_t* graph_launches, int64_t* iterations);
 
 /*
  * Timing of the last peec_matvec / peec_matvec_dev call on the context stream

@@ -19,9 +19,10 @@ ERRORS = {-1: "PEEC_ERR_CUDA", -2: "PEEC_ERR_OOM", -3: "PEEC_ERR_CANCELLED",
 
 # every symbol declared in include/peec_gb300.h
 EXPORTS = ("peec_version", "peec_ctx_create", "peec_ctx_destroy", "peec_last_error",
-           "peec_set_topology", "peec_set_pdiag", "peec_set_rows", "peec_fill",
+           "peec_set_topology", "peec_set_incidence", "peec_set_dense", "peec_set_pdiag", "peec_set_rows", "peec_fill",
            "peec_set_frequency", "peec_matvec", "peec_matvec_dev", "peec_port_rhs",
-           "peec_gmres", "peec_solve_mixed", "peec_set_stop_flag", "peec_last_timing",
+           "peec_gmres", "peec_solve_mixed", "peec_set_stop_flag", "peec_set_device_loop",
+           "peec_device_loop_stats", "peec_last_timing",
            "peec_launch_count", "peec_sizes", "peec_stream", "peec_conv_count",
            "peec_conv_info", "peec_zpass_tuning", "peec_set_zpass_forms", "peec_profile_matvec", "peec_multidot",
            "peec_multidot_noalloc", "peec_set_residual_precision",
@@ -78,6 +79,9 @@ def load(build_if_missing: bool = True):
     L.peec_set_topology.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64,
                                     ctypes.c_int64, ctypes.c_int64, P, P, P, ctypes.c_int64, P, P,
                                     P, ctypes.c_int64]
+    L.peec_set_incidence.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, P, P,
+                                     ctypes.c_int64, P, ctypes.c_int64]
+    L.peec_set_dense.argtypes = [P, P, P, P, P]
     L.peec_set_pdiag.argtypes = [P, P]
     L.peec_set_rows.argtypes = [P, ctypes.POINTER(P)]
     L.peec_fill.argtypes = [P, P, ctypes.c_double, ctypes.c_double, ctypes.c_double,
@@ -110,6 +114,8 @@ def load(build_if_missing: bool = True):
                                    ctypes.c_int, ctypes.POINTER(ctypes.c_int), DP,
                                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.peec_set_stop_flag.argtypes = [P, P]
+    L.peec_set_device_loop.argtypes = [P, ctypes.c_int]
+    L.peec_device_loop_stats.argtypes = [P, I64P, I64P]
     L.peec_last_timing.argtypes = [P, DP, DP, DP]
     L.peec_launch_count.argtypes = [P]
     L.peec_launch_count.restype = ctypes.c_int64

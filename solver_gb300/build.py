@@ -30,7 +30,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 MESH_SOURCES = ["mesher.cpp"]
 CUDA_SOURCES = ["ctx.cu", "fftconv.cu", "fftconv_f32.cu", "fftconv_f64.cu", "fftconv_ff.cu",
                 "krylov.cu", "sparse.cu", "fill.cu", "adjoint.cu", "refactor.cu",
-                "mesher_gpu.cu"]
+                "mesher_gpu.cu", "dense.cu"]
 # the fill keeps the reference's scalar rounding: no FMA contraction
 FILE_FLAGS = {"fill.cu": ["-fmad=false"]}
 CUDA_HEADERS = ["common.cuh", "fft.cuh", "fft_reg.cuh", "fftconv_impl.cuh",

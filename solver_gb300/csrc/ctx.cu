@@ -51,17 +51,23 @@ int fail_cuda(cudaError_t e, const char* expr, const char* file, int line) {
 
 // launchers defined in the other translation units
 void launch_edge_rows(const c64*, const c64*, const c64*, const c64*, const int32_t*,
-                      const int32_t*, double, int, c64*, c64*, cudaStream_t);
+                      const int32_t*, const double*, int, c64*, c64*, cudaStream_t);
 void launch_surf_rows(const c64*, const c64*, const int32_t*, const double*, int, c64*, c64*,
                       cudaStream_t);
 void launch_node_rows(const c64*, const c64*, const c64*, const c64*, const c64*, const int32_t*,
                       const int32_t*, const int32_t*, const int32_t*, const int32_t*,
-                      const int32_t*, const c64*, double, int, c64*, cudaStream_t);
+                      const int32_t*, const c64*, const double*, int, c64*, cudaStream_t);
+void launch_set_scalar(double* p, double v, cudaStream_t st);
+int dense_chunks(int64_t n);
+int dense_apply(const void* M, bool fp32, int64_t n, const c64* x, int offdiag, c64* part,
+                c64* out, cudaStream_t st);
+void dense_round(const double* a, size_t cnt, float* out, cudaStream_t st);
 void launch_final_rows(const c64*, const c64*, const c64*, const c64*, const int32_t*,
                        const int32_t*, const int32_t*, const double*, int, int, int, c64*,
                        cudaStream_t);
 void launch_perm_gather(const c64*, const int32_t*, const double*, int, c64*, cudaStream_t);
-int launch_sptrsv(const CompPlan&, const int32_t*, int, int, const SfTri&, const SfTri&,
+int sptrsv_grp_prepare(size_t smem_bytes);
+int launch_sptrsv(const GrpPlan&, const int32_t*, int, int, const SfTri&, const SfTri&,
                   const c64*, const int32_t*, const double*, c64*, c64*, int*, cudaStream_t);
 int red_blocks(size_t N);
 int launch_multidot(const c64*, size_t, const c64*, size_t, int, c64*, c64*, cudaStream_t);
@@ -128,6 +134,13 @@ struct peec_ctx {
   int Nx = 0, Ny = 0, Nz = 0;
   int64_t mx = 0, my = 0, mz = 0, m = 0, ns = 0, n = 0, N = 0;
   bool have_topo = false, have_spec = false, have_freq = false, have_pdiag = false;
+  // lattice: the topology has voxel lattices (circulant operator); dense: the operator's
+  // Lp and P products come from dense matrices (the RIS solver): Lp_x, Lp_y, Lp_z, P,
+  // real column-major, FP64 and an FP32 copy, and the scratch of their partial sums
+  bool lattice = false, dense = false;
+  double* dn64[4] = {nullptr, nullptr, nullptr, nullptr};
+  float* dn32[4] = {nullptr, nullptr, nullptr, nullptr};
+  c64* dn_part = nullptr;
   // topology
   int32_t *n1 = nullptr, *n2 = nullptr, *snode = nullptr;
   double* invP = nullptr;
@@ -162,14 +175,19 @@ struct peec_ctx {
   // synchronisation-free triangular solves: claim order (L levels then U levels, each
   // padded with -1 to whole warps), its length, the L part's length, control words
   int32_t* sf_ord = nullptr;
-  // per-warp component solves: component offsets into the row lists, rows in L-level and
-  // U-level order, level segment ends and their per-component offsets, local indices
-  int cmp_n = 0;
-  int comp_max = 0;  // largest component solved per warp (0: global scheme only)
-  int32_t *cmp_off = nullptr, *cmp_rowsL = nullptr, *cmp_rowsU = nullptr, *cmp_segL = nullptr,
-          *cmp_segU = nullptr, *cmp_segLoff = nullptr, *cmp_segUoff = nullptr,
-          *cmp_local = nullptr;
+  // per-warp group solves (GrpPlan): components of at most comp_max rows; the device
+  // arrays of the plan (host-built with the factors' structure)
+  int comp_max = SF_COMP_MAX;  // largest component solved per warp (0: global scheme only)
+  GrpPlan grp;
+  int32_t *grp_goff = nullptr, *grp_seg = nullptr, *grp_segoff = nullptr, *grp_nsegL = nullptr;
+  GrpRow* grp_rows = nullptr;
+  int16_t *grp_uq = nullptr, *grp_lcolL = nullptr, *grp_lcolU = nullptr;
   c64 *ir_b = nullptr, *ir_x = nullptr, *ir_r = nullptr, *ir_d = nullptr;  // refinement vectors
+  // the frequency w on the device (the row kernels read it there, so captured graphs of
+  // the operator stay valid when only the frequency state changes) and the entries the
+  // Yle value array holds
+  double* d_w = nullptr;
+  size_t yle_cap = 0;
   // convolutions of the last converged mixed solve's final residual: x, Lp*I, P*Q and
   // the precision they were computed in (-1: none). They do not depend on the frequency.
   c64 *cc_x = nullptr, *cc_LpI = nullptr, *cc_PQ = nullptr;
@@ -220,13 +238,37 @@ struct peec_ctx {
   };
   std::map<std::tuple<const void*, void*, int>, GraphEntry> graphs;
   bool use_graphs = true;
+  // device-resident Arnoldi loop: the cycle state (GmDev header, res, wv, J, Utop, R) in
+  // one allocation for cycles of gm_inner iterations, its pinned mirrors (gm_up: the
+  // header, gm_down: header + res + wv), and per operator precision a graph whose WHILE
+  // node runs iterations until the scalar step ends the loop
+  unsigned char* gm_block = nullptr;
+  unsigned char* gm_up = nullptr;
+  unsigned char* gm_down = nullptr;
+  int gm_inner = -1;
+  struct KrylovGraph {
+    cudaGraphExec_t exec = nullptr;
+    int inner = -1;
+    int64_t kernels = 0;  // kernels per iteration
+  };
+  KrylovGraph kg[3];
+  bool dev_loop = true;
+  int64_t kg_launches = 0, kg_iterations = 0;
 };
+
+static void drop_krylov_graphs(peec_ctx* ctx) {
+  for (auto& k : ctx->kg) {
+    if (k.exec) cudaGraphExecDestroy(k.exec);
+    k = peec_ctx::KrylovGraph();
+  }
+}
 
 static void drop_graphs(peec_ctx* ctx) {
   if (!ctx) return;
   for (auto& kv : ctx->graphs)
     if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
   ctx->graphs.clear();
+  drop_krylov_graphs(ctx);
 }
 
 // Entry points make the context's device current for their work; this puts the
@@ -389,9 +431,13 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
                   ctx->Y2, ctx->U2, ctx->tvec, ctx->Mvec, ctx->lutmp, ctx->lutmp2, ctx->dx, ctx->dy, ctx->U, (c64*)ctx->U32,
                   ctx->gb, ctx->gx, ctx->gr, ctx->gv, ctx->gw, ctx->gxm, ctx->gxmin, ctx->gtmp,
                   ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal, ctx->dT,
-                  ctx->mdpart, ctx->LpI2, ctx->PQ2};
+                  ctx->mdpart, ctx->LpI2, ctx->PQ2, ctx->gm_block, ctx->d_w, ctx->dn_part,
+                  ctx->dn64[0], ctx->dn64[1], ctx->dn64[2], ctx->dn64[3], ctx->dn32[0],
+                  ctx->dn32[1], ctx->dn32[2], ctx->dn32[3]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  if (ctx->gm_up) cudaFreeHost(ctx->gm_up);
+  if (ctx->gm_down) cudaFreeHost(ctx->gm_down);
   for (double* p : ctx->rcc_qs)
     if (p) cudaFree(p);
   for (auto& f : ctx->fam) {
@@ -418,8 +464,9 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   cudaFree(ctx->sf_ctl);
   free_refactor(ctx->rf);
   cudaFree(ctx->rf_err);
-  for (int32_t* p : {ctx->cmp_off, ctx->cmp_rowsL, ctx->cmp_rowsU, ctx->cmp_segL, ctx->cmp_segU,
-                     ctx->cmp_segLoff, ctx->cmp_segUoff, ctx->cmp_local})
+  for (void* p : {(void*)ctx->grp_goff, (void*)ctx->grp_seg, (void*)ctx->grp_segoff,
+                  (void*)ctx->grp_nsegL, (void*)ctx->grp_rows, (void*)ctx->grp_uq,
+                  (void*)ctx->grp_lcolL, (void*)ctx->grp_lcolU})
     cudaFree(p);
   for (c64* p : {ctx->ir_b, ctx->ir_x, ctx->ir_r, ctx->ir_d, ctx->cc_x, ctx->cc_LpI, ctx->cc_PQ})
     cudaFree(p);
@@ -442,6 +489,20 @@ extern "C" int peec_set_stop_flag(peec_ctx* ctx, volatile int* flag) {
   return PEEC_OK;
 }
 
+extern "C" int peec_set_device_loop(peec_ctx* ctx, int on) {
+  if (!ctx || (on != 0 && on != 1)) return badarg(__func__);
+  ctx->dev_loop = on != 0;
+  return PEEC_OK;
+}
+
+extern "C" int peec_device_loop_stats(const peec_ctx* ctx, int64_t* graph_launches,
+                                      int64_t* iterations) {
+  if (!ctx || !graph_launches || !iterations) return badarg(__func__);
+  *graph_launches = ctx->kg_launches;
+  *iterations = ctx->kg_iterations;
+  return PEEC_OK;
+}
+
 // ------------------------------------------------------------------------------------
 // topology
 // ------------------------------------------------------------------------------------
@@ -451,6 +512,83 @@ extern "C" int peec_set_stop_flag(peec_ctx* ctx, volatile int* flag) {
 static int fft_len(int na, int nb, bool sym) {
   int need = sym ? (na > 1 ? 2 * na - 2 : 1) : na + nb - 1;
   return pow2ceil(need < 1 ? 1 : need);
+}
+
+// the sparse topology: edge end nodes (A), surface nodes (Gamma) and the node -> edge /
+// node -> surface lists the row kernels gather with
+static int set_incidence_lists(peec_ctx* ctx, int64_t m, int64_t ns, int64_t n,
+                               const int64_t* edge_n1, const int64_t* edge_n2,
+                               const int64_t* surf_node) {
+  std::vector<int32_t> hn1(m), hn2(m), hsn(ns);
+  std::vector<int32_t> deg(n + 1, 0), sdeg(n + 1, 0);
+  for (int64_t e = 0; e < m; ++e) {
+    if (edge_n1[e] < 0 || edge_n1[e] >= n || edge_n2[e] < 0 || edge_n2[e] >= n)
+      return bad(ctx, PEEC_ERR_BADARG, "edge node out of range");
+    hn1[e] = (int32_t)edge_n1[e];
+    hn2[e] = (int32_t)edge_n2[e];
+    deg[hn1[e] + 1]++;
+    deg[hn2[e] + 1]++;
+  }
+  for (int64_t s = 0; s < ns; ++s) {
+    if (surf_node[s] < 0 || surf_node[s] >= n) return bad(ctx, PEEC_ERR_BADARG, "surface node out of range");
+    hsn[s] = (int32_t)surf_node[s];
+    sdeg[hsn[s] + 1]++;
+  }
+  for (int64_t v = 0; v < n; ++v) {
+    deg[v + 1] += deg[v];
+    sdeg[v + 1] += sdeg[v];
+  }
+  std::vector<int32_t> nei(deg[n]), nsi(sdeg[n]);
+  {
+    std::vector<int32_t> fill(deg.begin(), deg.end() - 1);
+    for (int64_t e = 0; e < m; ++e) {
+      nei[fill[hn1[e]]++] = (int32_t)(2 * e);      // A = -1
+      nei[fill[hn2[e]]++] = (int32_t)(2 * e + 1);  // A = +1
+    }
+    std::vector<int32_t> sf(sdeg.begin(), sdeg.end() - 1);
+    for (int64_t s = 0; s < ns; ++s) nsi[sf[hsn[s]]++] = (int32_t)s;
+  }
+  CTX_TRY(upload(&ctx->n1, hn1, ctx->st));
+  CTX_TRY(upload(&ctx->n2, hn2, ctx->st));
+  CTX_TRY(upload(&ctx->snode, hsn, ctx->st));
+  CTX_TRY(upload(&ctx->ne_ptr, deg, ctx->st));
+  CTX_TRY(upload(&ctx->ne_idx, nei, ctx->st));
+  CTX_TRY(upload(&ctx->nsn_ptr, sdeg, ctx->st));
+  CTX_TRY(upload(&ctx->nsn_idx, nsi, ctx->st));
+  return PEEC_OK;
+}
+
+// work vectors and staging of an operator with the context's sizes
+static int alloc_work(peec_ctx* ctx) {
+  const int64_t m = ctx->m, ns = ctx->ns, n = ctx->n;
+  CTX_TRY(dalloc(&ctx->LpI, m));
+  CTX_TRY(dalloc(&ctx->PQ, ns));
+  CTX_TRY(dalloc(&ctx->LpI2, m));
+  CTX_TRY(dalloc(&ctx->PQ2, ns));
+  CTX_TRY(dalloc(&ctx->Y1, m));
+  CTX_TRY(dalloc(&ctx->U1, m));
+  CTX_TRY(dalloc(&ctx->Y2, ns));
+  CTX_TRY(dalloc(&ctx->U2, ns));
+  CTX_TRY(dalloc(&ctx->tvec, n));
+  CTX_TRY(dalloc(&ctx->Mvec, n));
+  CTX_TRY(dalloc(&ctx->lutmp, n));
+  CTX_TRY(dalloc(&ctx->lutmp2, n));
+  CTX_TRY(dalloc(&ctx->dx, ctx->N));
+  CTX_TRY(dalloc(&ctx->dy, ctx->N));
+  for (c64** p : {&ctx->ir_b, &ctx->ir_x, &ctx->ir_r, &ctx->ir_d, &ctx->cc_x}) CTX_TRY(dalloc(p, ctx->N));
+  CTX_TRY(dalloc(&ctx->cc_LpI, m));
+  CTX_TRY(dalloc(&ctx->cc_PQ, ns));
+  CTX_TRY(dalloc(&ctx->d_flag, 1));
+  ctx->cc_prec = -1;
+  if (ctx->hx) cudaFreeHost(ctx->hx);
+  if (ctx->hy) cudaFreeHost(ctx->hy);
+  PEEC_CUDA_TRY(cudaMallocHost(&ctx->hx, sizeof(c64) * ctx->N));
+  PEEC_CUDA_TRY(cudaMallocHost(&ctx->hy, sizeof(c64) * ctx->N));
+  ctx->kcap = 0;
+  ctx->have_topo = true;
+  ctx->have_spec = ctx->have_freq = ctx->have_pdiag = false;
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  return PEEC_OK;
 }
 
 static int peec_set_topology_body(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t mx, int64_t my,
@@ -496,43 +634,7 @@ static int peec_set_topology_body(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t
     maps[f][cell] = (int32_t)s;
   }
   for (int f = 0; f < 6; ++f) CTX_TRY(upload(&ctx->fam[f].map, maps[f], ctx->st));
-  // incidence lists
-  std::vector<int32_t> hn1(m), hn2(m), hsn(ns);
-  std::vector<int32_t> deg(n + 1, 0), sdeg(n + 1, 0);
-  for (int64_t e = 0; e < m; ++e) {
-    if (edge_n1[e] < 0 || edge_n1[e] >= n || edge_n2[e] < 0 || edge_n2[e] >= n)
-      return bad(ctx, PEEC_ERR_BADARG, "edge node out of range");
-    hn1[e] = (int32_t)edge_n1[e];
-    hn2[e] = (int32_t)edge_n2[e];
-    deg[hn1[e] + 1]++;
-    deg[hn2[e] + 1]++;
-  }
-  for (int64_t s = 0; s < ns; ++s) {
-    if (surf_node[s] < 0 || surf_node[s] >= n) return bad(ctx, PEEC_ERR_BADARG, "surface node out of range");
-    hsn[s] = (int32_t)surf_node[s];
-    sdeg[hsn[s] + 1]++;
-  }
-  for (int64_t v = 0; v < n; ++v) {
-    deg[v + 1] += deg[v];
-    sdeg[v + 1] += sdeg[v];
-  }
-  std::vector<int32_t> nei(deg[n]), nsi(sdeg[n]);
-  {
-    std::vector<int32_t> fill(deg.begin(), deg.end() - 1);
-    for (int64_t e = 0; e < m; ++e) {
-      nei[fill[hn1[e]]++] = (int32_t)(2 * e);      // A = -1
-      nei[fill[hn2[e]]++] = (int32_t)(2 * e + 1);  // A = +1
-    }
-    std::vector<int32_t> sf(sdeg.begin(), sdeg.end() - 1);
-    for (int64_t s = 0; s < ns; ++s) nsi[sf[hsn[s]]++] = (int32_t)s;
-  }
-  CTX_TRY(upload(&ctx->n1, hn1, ctx->st));
-  CTX_TRY(upload(&ctx->n2, hn2, ctx->st));
-  CTX_TRY(upload(&ctx->snode, hsn, ctx->st));
-  CTX_TRY(upload(&ctx->ne_ptr, deg, ctx->st));
-  CTX_TRY(upload(&ctx->ne_idx, nei, ctx->st));
-  CTX_TRY(upload(&ctx->nsn_ptr, sdeg, ctx->st));
-  CTX_TRY(upload(&ctx->nsn_idx, nsi, ctx->st));
+  CTX_TRY(set_incidence_lists(ctx, m, ns, n, edge_n1, edge_n2, surf_node));
   // lattice families and their circulant grids: the three face families share one
   // grid (every P block, diagonal or cross, lives on it); each edge family has its own
   const int rd[9][3] = {{Nx - 1, Ny, Nz}, {Nx, Ny - 1, Nz}, {Nx, Ny, Nz - 1},
@@ -589,34 +691,77 @@ static int peec_set_topology_body(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t
   ctx->have_rcc_rows = ctx->rcc = false;
   ctx->rcc_freq = -1.0;
   CTX_TRY(phase_tables(LP, ctx->ph64, ctx->ph32, ctx->st));
-  // work vectors
-  CTX_TRY(dalloc(&ctx->LpI, m));
-  CTX_TRY(dalloc(&ctx->PQ, ns));
-  CTX_TRY(dalloc(&ctx->LpI2, m));
-  CTX_TRY(dalloc(&ctx->PQ2, ns));
-  CTX_TRY(dalloc(&ctx->Y1, m));
-  CTX_TRY(dalloc(&ctx->U1, m));
-  CTX_TRY(dalloc(&ctx->Y2, ns));
-  CTX_TRY(dalloc(&ctx->U2, ns));
-  CTX_TRY(dalloc(&ctx->tvec, n));
-  CTX_TRY(dalloc(&ctx->Mvec, n));
-  CTX_TRY(dalloc(&ctx->lutmp, n));
-  CTX_TRY(dalloc(&ctx->lutmp2, n));
-  CTX_TRY(dalloc(&ctx->dx, ctx->N));
-  CTX_TRY(dalloc(&ctx->dy, ctx->N));
-  for (c64** p : {&ctx->ir_b, &ctx->ir_x, &ctx->ir_r, &ctx->ir_d, &ctx->cc_x}) CTX_TRY(dalloc(p, ctx->N));
-  CTX_TRY(dalloc(&ctx->cc_LpI, m));
-  CTX_TRY(dalloc(&ctx->cc_PQ, ns));
-  CTX_TRY(dalloc(&ctx->d_flag, 1));
-  ctx->cc_prec = -1;
-  if (ctx->hx) cudaFreeHost(ctx->hx);
-  if (ctx->hy) cudaFreeHost(ctx->hy);
-  PEEC_CUDA_TRY(cudaMallocHost(&ctx->hx, sizeof(c64) * ctx->N));
-  PEEC_CUDA_TRY(cudaMallocHost(&ctx->hy, sizeof(c64) * ctx->N));
-  ctx->kcap = 0;
-  ctx->have_topo = true;
-  ctx->have_spec = ctx->have_freq = ctx->have_pdiag = false;
+  ctx->lattice = true;
+  ctx->dense = false;
+  return alloc_work(ctx);
+}
+
+// A topology without voxel lattices (the RIS solver's meshes): the incidence of the edges
+// and surfaces only. The operator then needs dense Lp and P (peec_set_dense).
+static int peec_set_incidence_body(peec_ctx* ctx, int64_t mx, int64_t my, int64_t mz,
+                                   const int64_t* edge_n1, const int64_t* edge_n2, int64_t ns,
+                                   const int64_t* surf_node, int64_t n) {
+  NvtxRange nvtx_range_("peec_set_incidence");
+  if (!ctx) return badarg("peec_set_incidence");
+  drop_graphs(ctx);
+  if (mx < 0 || my < 0 || mz < 0 || ns < 0 || n < 1 || (mx + my + mz > 0 && (!edge_n1 || !edge_n2)) ||
+      (ns > 0 && !surf_node))
+    return bad(ctx, PEEC_ERR_BADARG, "peec_set_incidence: invalid sizes or pointers");
+  const int64_t m = mx + my + mz;
+  if (m + ns + n > INT32_MAX || 2 * m + 1 > INT32_MAX)
+    return bad(ctx, PEEC_ERR_UNSUPPORTED, "problem too large for int32 indexing");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  ctx->Nx = ctx->Ny = ctx->Nz = 0;
+  ctx->mx = mx; ctx->my = my; ctx->mz = mz; ctx->m = m; ctx->ns = ns; ctx->n = n;
+  ctx->N = m + ns + n;
+  CTX_TRY(set_incidence_lists(ctx, m, ns, n, edge_n1, edge_n2, surf_node));
+  for (auto& F : ctx->fam) {
+    for (int p = 0; p < 2; ++p) {
+      if (F.T[p]) cudaFree(F.T[p]);
+      F.T[p] = nullptr;
+    }
+    F.active = false;
+  }
+  ctx->have_rcc_rows = ctx->rcc = false;
+  ctx->rcc_freq = -1.0;
+  ctx->lattice = false;
+  ctx->dense = false;
+  return alloc_work(ctx);
+}
+
+// Dense Lp blocks (mx x mx, my x my, mz x mz) and dense P (ns x ns), real, column-major:
+// the operator's products Lp*I and P*Q become matrix-vector products with them. The
+// frequency state then takes DZ = Z_self + jw diag(Lp) (the RIS solver's invZ): the
+// products leave Lp's diagonal out, so that Y1 = jw Lp I + Z_self I + A Phi
+// (compute_matrix_vector.jl:14-22).
+static int peec_set_dense_body(peec_ctx* ctx, const double* Lpx, const double* Lpy,
+                               const double* Lpz, const double* P) {
+  NvtxRange nvtx_range_("peec_set_dense");
+  if (!ctx) return badarg("peec_set_dense");
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  const int64_t sz[4] = {ctx->mx, ctx->my, ctx->mz, ctx->ns};
+  const double* src[4] = {Lpx, Lpy, Lpz, P};
+  for (int b = 0; b < 4; ++b)
+    if (sz[b] > 0 && !src[b]) return bad(ctx, PEEC_ERR_BADARG, "peec_set_dense: missing block");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  drop_graphs(ctx);
+  ctx->dense = false;
+  size_t part = 1;
+  for (int b = 0; b < 4; ++b) {
+    const size_t cnt = (size_t)sz[b] * (size_t)sz[b];
+    CTX_TRY(dalloc(&ctx->dn64[b], cnt));
+    CTX_TRY(dalloc(&ctx->dn32[b], cnt));
+    if (cnt) {
+      PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->dn64[b], src[b], sizeof(double) * cnt,
+                                    cudaMemcpyHostToDevice, ctx->st));
+      dense_round(ctx->dn64[b], cnt, ctx->dn32[b], ctx->st);
+    }
+    part = std::max(part, (size_t)dense_chunks(sz[b]) * (size_t)std::max<int64_t>(sz[b], 1));
+  }
+  CTX_TRY(dalloc(&ctx->dn_part, part));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  ctx->dense = true;
+  ctx->have_spec = true;
   return PEEC_OK;
 }
 
@@ -752,6 +897,7 @@ static int build_spectra(peec_ctx* ctx, double* const d_rows[9]) {
   drop_graphs(ctx);
   ctx->cc_prec = -1;
   ctx->rcc = false;
+  ctx->dense = false;  // the circulant operator replaces dense matrices set before
   CTX_TRY(build_spectrum_set(ctx, ctx->spec, d_rows));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->have_spec = true;
@@ -763,6 +909,7 @@ static int peec_set_rows_body(peec_ctx* ctx, const double* const rows[9]) {
   NvtxRange nvtx_range_("peec_set_rows");
   if (!ctx || !rows) return badarg("peec_set_rows");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  if (!ctx->lattice) return bad(ctx, PEEC_ERR_STATE, "no voxel lattice (peec_set_incidence topology)");
   PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   double* d_rows[9] = {};
   int rc = PEEC_OK;
@@ -787,6 +934,7 @@ static int peec_fill_body(peec_ctx* ctx, const double origin[3], double sx, doub
   NvtxRange nvtx_range_("peec_fill");
   if (!ctx || !origin) return badarg("peec_fill");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  if (!ctx->lattice) return bad(ctx, PEEC_ERR_STATE, "no voxel lattice (peec_set_incidence topology)");
   PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   double* d_rows[9] = {};
   int64_t len[9];
@@ -859,6 +1007,7 @@ static int peec_fill_rcc_body(peec_ctx* ctx, const double origin[3], double sx, 
   NvtxRange nvtx_range_("peec_fill_rcc");
   if (!ctx || !origin) return badarg("peec_fill_rcc");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  if (!ctx->lattice) return bad(ctx, PEEC_ERR_STATE, "no voxel lattice (peec_set_incidence topology)");
   PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   int64_t len[9];
   ctx->have_rcc_rows = false;
@@ -900,6 +1049,7 @@ static int peec_set_rows_rcc_body(peec_ctx* ctx, const double* const rows[9],
   NvtxRange nvtx_range_("peec_set_rows_rcc");
   if (!ctx || !rows || !origin) return badarg("peec_set_rows_rcc");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  if (!ctx->lattice) return bad(ctx, PEEC_ERR_STATE, "no voxel lattice (peec_set_incidence topology)");
   PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   int64_t len[9];
   ctx->have_rcc_rows = false;
@@ -961,8 +1111,9 @@ static int peec_set_rcc_frequency_body(peec_ctx* ctx, double freq_hz) {
   const cudaError_t e = cudaStreamSynchronize(ctx->st);
   if (rc != PEEC_OK) return rc;
   if (e != cudaSuccess) return fail_cuda(e, "Rcc spectra", __FILE__, __LINE__);
-  const bool tuned = ctx->have_spec;
+  const bool tuned = ctx->have_spec && !ctx->dense;
   ctx->have_spec = true;
+  ctx->dense = false;
   ctx->rcc = true;
   ctx->rcc_freq = freq_hz;
   if (!tuned) CTX_TRY(tune_zpass(ctx));
@@ -1044,9 +1195,11 @@ static int make_tri(peec_ctx* ctx, LevelTri& T, int64_t n, const int64_t* ptr, c
 
 // Work split of the LU solves. The rows of L and U fall into connected components
 // (rows linked by a factor entry); rows of different components never depend on one
-// another. Components of at most SF_COMP_MAX rows are solved by one warp each, level by
-// level with __syncwarp between levels and the component's values in shared memory;
-// the rows of larger components go to the synchronisation-free global scheme.
+// another. Components of at most comp_max rows are solved per warp (k_sptrsv_grp): those
+// of at most 32 rows and SF_GRP_E entries packed into groups of at most 32 rows and
+// SF_GRP_E entries, in order of their level depth (so that a group's levels are mostly
+// full), larger ones one per group; the rows of components above comp_max (or too large
+// for a warp's shared memory) go to the synchronisation-free global scheme.
 static int build_solve_plan(peec_ctx* ctx, int64_t n) {
   const LevelTri &L = ctx->Lf, &U = ctx->Uf;
   // union-find over the factor entries
@@ -1065,58 +1218,134 @@ static int build_solve_plan(peec_ctx* ctx, int64_t n) {
         const int32_t a = find((int32_t)r), b = find(T->hcol[q]);
         if (a != b) parent[std::max(a, b)] = std::min(a, b);
       }
-  std::vector<int32_t> comp(n), csize(n, 0);
-  for (int64_t r = 0; r < n; ++r) {
-    comp[r] = find((int32_t)r);
-    csize[comp[r]]++;
-  }
+  std::vector<int32_t> comp(n), csize(n, 0), cent(n, 0), cdepth(n, 0);
   // per-row levels
   std::vector<int32_t> lvL(n), lvU(n);
   for (size_t l = 0; l + 1 < L.lvl_off.size(); ++l)
     for (int q = L.lvl_off[l]; q < L.lvl_off[l + 1]; ++q) lvL[L.rows[q]] = (int32_t)l;
   for (size_t l = 0; l + 1 < U.lvl_off.size(); ++l)
     for (int q = U.lvl_off[l]; q < U.lvl_off[l + 1]; ++q) lvU[U.rows[q]] = (int32_t)l;
-  // small components, largest first (they have the longest chains)
-  std::vector<int32_t> roots;
-  for (int64_t r = 0; r < n; ++r)
-    if (comp[r] == r && csize[r] <= ctx->comp_max) roots.push_back((int32_t)r);
-  std::stable_sort(roots.begin(), roots.end(),
-                   [&](int32_t a, int32_t b) { return csize[a] > csize[b]; });
-  std::vector<int32_t> cidx(n, -1);
-  for (size_t i = 0; i < roots.size(); ++i) cidx[roots[i]] = (int32_t)i;
-  const size_t nc = roots.size();
-  std::vector<int32_t> coff(nc + 1, 0);
-  for (size_t i = 0; i < nc; ++i) coff[i + 1] = coff[i] + csize[roots[i]];
-  std::vector<int32_t> rowsL(coff[nc]), fill(coff.begin(), coff.end() - 1);
   for (int64_t r = 0; r < n; ++r) {
-    const int32_t ci = cidx[comp[r]];
-    if (ci >= 0) rowsL[fill[ci]++] = (int32_t)r;
+    const int32_t c = comp[r] = find((int32_t)r);
+    csize[c]++;
+    cent[c] += (L.hptr[r + 1] - L.hptr[r]) + (U.hptr[r + 1] - U.hptr[r]);
+    cdepth[c] = std::max(cdepth[c], lvL[r] + lvU[r] + 2);
   }
-  std::vector<int32_t> rowsU(rowsL), local(n, -1), segL, segU, segLoff(nc + 1, 0),
-      segUoff(nc + 1, 0);
-  for (size_t ci = 0; ci < nc; ++ci) {
-    const auto b = rowsL.begin() + coff[ci], e = rowsL.begin() + coff[ci + 1];
-    std::stable_sort(b, e, [&](int32_t x, int32_t y) { return lvL[x] < lvL[y]; });
-    // local index of a row = its position in the L order of its component
-    for (int32_t q = coff[ci]; q < coff[ci + 1]; ++q) local[rowsL[q]] = q - coff[ci];
-    for (int32_t q = coff[ci]; q < coff[ci + 1]; ++q)
-      if (q + 1 == coff[ci + 1] || lvL[rowsL[q + 1]] != lvL[rowsL[q]]) segL.push_back(q + 1);
-    segLoff[ci + 1] = (int32_t)segL.size();
-    const auto bu = rowsU.begin() + coff[ci], eu = rowsU.begin() + coff[ci + 1];
+  // largest groups a warp's shared memory takes (a large component alone)
+  const size_t smem_cap = 160 * 1024;
+  std::vector<int32_t> big, small;
+  for (int64_t r = 0; r < n; ++r) {
+    if (comp[r] != r || csize[r] > ctx->comp_max) continue;
+    if (csize[r] <= 32 && cent[r] <= SF_GRP_E) small.push_back((int32_t)r);
+    else if (cent[r] < 32768 && grp_smem(csize[r], cent[r]) <= smem_cap) big.push_back((int32_t)r);
+  }
+  // large components, longest chains first; small ones by depth
+  std::stable_sort(big.begin(), big.end(),
+                   [&](int32_t a, int32_t b) { return cdepth[a] > cdepth[b]; });
+  std::stable_sort(small.begin(), small.end(),
+                   [&](int32_t a, int32_t b) { return cdepth[a] > cdepth[b]; });
+  std::vector<int32_t> gidx(n, -1);  // component root -> group
+  int ng = 0, rb = 0, eb = 0;
+  for (int32_t c : big) {
+    gidx[c] = ng++;
+    rb = std::max(rb, csize[c]);
+    eb = std::max(eb, cent[c]);
+  }
+  const int nbig = ng;
+  {
+    int rows = 0, ents = 0;
+    for (int32_t c : small) {
+      if (ng == nbig || rows + csize[c] > 32 || ents + cent[c] > SF_GRP_E) {
+        ++ng;
+        rows = ents = 0;
+      }
+      gidx[c] = ng - 1;
+      rows += csize[c];
+      ents += cent[c];
+    }
+  }
+  // the groups' rows, in L-level order within each group
+  std::vector<int32_t> goff(ng + 1, 0);
+  for (int64_t r = 0; r < n; ++r)
+    if (gidx[comp[r]] >= 0) goff[gidx[comp[r]] + 1]++;
+  for (int g = 0; g < ng; ++g) goff[g + 1] += goff[g];
+  std::vector<int32_t> rowsL(goff[ng]), fill(goff.begin(), goff.end() - 1);
+  for (int64_t r = 0; r < n; ++r)
+    if (gidx[comp[r]] >= 0) rowsL[fill[gidx[comp[r]]]++] = (int32_t)r;
+  std::vector<int32_t> rowsU(rowsL), local(n, -1), seg, segoff(ng + 1, 0), nsegL(ng, 0);
+  std::vector<GrpRow> grows(goff[ng]);
+  std::vector<int16_t> uq(goff[ng]);
+  for (int g = 0; g < ng; ++g) {
+    const auto b0 = rowsL.begin() + goff[g], e0 = rowsL.begin() + goff[g + 1];
+    std::stable_sort(b0, e0, [&](int32_t x, int32_t y) { return lvL[x] < lvL[y]; });
+    for (int32_t q = goff[g]; q < goff[g + 1]; ++q) local[rowsL[q]] = q - goff[g];
+    for (int32_t q = goff[g]; q < goff[g + 1]; ++q)
+      if (q + 1 == goff[g + 1] || lvL[rowsL[q + 1]] != lvL[rowsL[q]]) seg.push_back(q + 1 - goff[g]);
+    nsegL[g] = (int32_t)seg.size() - segoff[g];
+    const auto bu = rowsU.begin() + goff[g], eu = rowsU.begin() + goff[g + 1];
     std::stable_sort(bu, eu, [&](int32_t x, int32_t y) { return lvU[x] < lvU[y]; });
-    for (int32_t q = coff[ci]; q < coff[ci + 1]; ++q)
-      if (q + 1 == coff[ci + 1] || lvU[rowsU[q + 1]] != lvU[rowsU[q]]) segU.push_back(q + 1);
-    segUoff[ci + 1] = (int32_t)segU.size();
+    for (int32_t q = goff[g]; q < goff[g + 1]; ++q) {
+      uq[q] = (int16_t)local[rowsU[q]];
+      if (q + 1 == goff[g + 1] || lvU[rowsU[q + 1]] != lvU[rowsU[q]]) seg.push_back(q + 1 - goff[g]);
+    }
+    segoff[g + 1] = (int32_t)seg.size();
+    int e = 0;
+    for (int32_t q = goff[g]; q < goff[g + 1]; ++q) {
+      const int32_t r = rowsL[q];
+      GrpRow& gr = grows[q];
+      gr.r = r;
+      gr.pL = L.hptr[r];
+      gr.pU = U.hptr[r];
+      gr.j = ctx->h_gin.empty() ? r : ctx->h_gin[r];
+      gr.nL = (int16_t)(L.hptr[r + 1] - L.hptr[r]);
+      gr.nU = (int16_t)(U.hptr[r + 1] - U.hptr[r]);
+      gr.eL = (int16_t)e;
+      e += gr.nL;
+      gr.eU = (int16_t)e;
+      e += gr.nU;
+    }
   }
-  ctx->cmp_n = (int)nc;
-  CTX_TRY(upload(&ctx->cmp_off, coff, ctx->st));
-  CTX_TRY(upload(&ctx->cmp_rowsL, rowsL, ctx->st));
-  CTX_TRY(upload(&ctx->cmp_rowsU, rowsU, ctx->st));
-  CTX_TRY(upload(&ctx->cmp_segL, segL, ctx->st));
-  CTX_TRY(upload(&ctx->cmp_segU, segU, ctx->st));
-  CTX_TRY(upload(&ctx->cmp_segLoff, segLoff, ctx->st));
-  CTX_TRY(upload(&ctx->cmp_segUoff, segUoff, ctx->st));
-  CTX_TRY(upload(&ctx->cmp_local, local, ctx->st));
+  // entry columns as positions in the row's group
+  std::vector<int16_t> lcolL(std::max<size_t>(L.hcol.size(), 1), -1),
+      lcolU(std::max<size_t>(U.hcol.size(), 1), -1);
+  for (const auto* T : {&L, &U}) {
+    std::vector<int16_t>& lc = T == &L ? lcolL : lcolU;
+    for (int64_t r = 0; r < n; ++r)
+      if (local[r] >= 0)
+        for (int32_t q = T->hptr[r]; q < T->hptr[r + 1]; ++q) lc[q] = (int16_t)local[T->hcol[q]];
+  }
+  if (ng == 0) {  // keep the arrays non-empty
+    seg.push_back(0);
+    rowsL.push_back(0);
+    grows.push_back(GrpRow());
+    uq.push_back(0);
+    nsegL.push_back(0);
+  }
+  CTX_TRY(upload(&ctx->grp_goff, goff, ctx->st));
+  CTX_TRY(upload(&ctx->grp_rows, grows, ctx->st));
+  CTX_TRY(upload(&ctx->grp_uq, uq, ctx->st));
+  CTX_TRY(upload(&ctx->grp_seg, seg, ctx->st));
+  CTX_TRY(upload(&ctx->grp_segoff, segoff, ctx->st));
+  CTX_TRY(upload(&ctx->grp_nsegL, nsegL, ctx->st));
+  CTX_TRY(upload(&ctx->grp_lcolL, lcolL, ctx->st));
+  CTX_TRY(upload(&ctx->grp_lcolU, lcolU, ctx->st));
+  GrpPlan& P = ctx->grp;
+  P.goff = ctx->grp_goff;
+  P.rows = ctx->grp_rows;
+  P.uq = ctx->grp_uq;
+  P.seg = ctx->grp_seg;
+  P.segoff = ctx->grp_segoff;
+  P.nsegL = ctx->grp_nsegL;
+  P.lcolL = ctx->grp_lcolL;
+  P.lcolU = ctx->grp_lcolU;
+  P.nbig = nbig;
+  P.ngroups = ng;
+  P.rb = rb;
+  P.eb = eb;
+  const size_t need = std::max(grp_smem(rb, eb), SF_GRP_WARPS * grp_smem(32, SF_GRP_E));
+  if (sptrsv_grp_prepare(need)) return PEEC_ERR_CUDA;
+  std::vector<int32_t> cidx(n, -1);
+  for (int64_t r = 0; r < n; ++r) cidx[r] = gidx[comp[r]];
   // claim order of the global scheme: rows of the large components only
   std::vector<int32_t> ord;
   for (const LevelTri* T : {&L, &U}) {
@@ -1202,6 +1431,9 @@ static int peec_set_frequency_body(peec_ctx* ctx, double w, const double* DZ, in
   CTX_TRY(upload(&ctx->yle_ptr, yp, ctx->st));
   CTX_TRY(upload(&ctx->yle_col, yc, ctx->st));
   CTX_TRY(upload(&ctx->yle_val, yv, ctx->st));
+  ctx->yle_cap = yv.size();
+  if (!ctx->d_w) CTX_TRY(dalloc(&ctx->d_w, 1));
+  launch_set_scalar(ctx->d_w, w, ctx->st);
   // LU: b' = b[iperm_r]; x = z[perm_c]
   std::vector<int32_t> gin(n), gout(n);
   for (int64_t i = 0; i < n; ++i) {
@@ -1257,6 +1489,7 @@ static int peec_lu_refactor_setup_body(peec_ctx* ctx, int64_t yle_nnz, const int
   if (!ctx || (yle_nnz > 0 && (!yle_row || !yle_col))) return badarg("peec_lu_refactor_setup");
   if (!ctx->have_freq) return bad(ctx, PEEC_ERR_STATE, "no factors installed (peec_set_frequency)");
   PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  drop_graphs(ctx);  // the factors and the solve plan are rebuilt below
   free_refactor(ctx->rf);
   ctx->have_rf = false;
   const int64_t n = ctx->n, m = ctx->m, ns = ctx->ns;
@@ -1461,7 +1694,6 @@ static int peec_set_frequency_refactor_body(peec_ctx* ctx, double w, const doubl
     return badarg("peec_set_frequency_refactor");
   if (!ctx->have_rf) return bad(ctx, PEEC_ERR_STATE, "no refactorisation plan (peec_lu_refactor_setup)");
   PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
-  drop_graphs(ctx);
   const int64_t n = ctx->n, m = ctx->m;
   std::vector<int32_t> yp, yc;
   std::vector<c64> yv;
@@ -1472,8 +1704,24 @@ static int peec_set_frequency_refactor_body(peec_ctx* ctx, double w, const doubl
   ctx->w = w;
   std::vector<c64> dz(m);
   for (int64_t e = 0; e < m; ++e) dz[e] = mk<double>(DZ[2 * e], DZ[2 * e + 1]);
-  CTX_TRY(upload(&ctx->DZ, dz, ctx->st));
-  CTX_TRY(upload(&ctx->yle_val, yv, ctx->st));
+  // The new values go into the arrays in place, and w into its device word, behind the
+  // stream's earlier work: every pointer the captured graphs of this context hold stays
+  // valid, so they are kept (the factors' pattern, permutations and solve plan do not
+  // change either).
+  if (!ctx->DZ || !ctx->d_w || ctx->yle_cap != yv.size()) {
+    drop_graphs(ctx);
+    CTX_TRY(upload(&ctx->DZ, dz, ctx->st));
+    CTX_TRY(upload(&ctx->yle_val, yv, ctx->st));
+    ctx->yle_cap = yv.size();
+    if (!ctx->d_w) CTX_TRY(dalloc(&ctx->d_w, 1));
+  } else {
+    PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->DZ, dz.data(), sizeof(c64) * m, cudaMemcpyHostToDevice,
+                                  ctx->st));
+    if (!yv.empty())
+      PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->yle_val, yv.data(), sizeof(c64) * yv.size(),
+                                    cudaMemcpyHostToDevice, ctx->st));
+  }
+  launch_set_scalar(ctx->d_w, w, ctx->st);
   return refactor_run(ctx);
 }
 
@@ -1484,11 +1732,8 @@ static int peec_set_frequency_refactor_body(peec_ctx* ctx, double w, const doubl
 static void lu_solve(peec_ctx* ctx, const c64* b, c64* x) {
   const int n = (int)ctx->n;
   const LevelTri &L = ctx->Lf, &U = ctx->Uf;
-  const CompPlan C{ctx->cmp_off,    ctx->cmp_rowsL,   ctx->cmp_rowsU,   ctx->cmp_segL,
-                   ctx->cmp_segU,   ctx->cmp_segLoff, ctx->cmp_segUoff, ctx->cmp_local,
-                   ctx->cmp_n};
   ctx->launches += launch_sptrsv(
-      C, ctx->sf_ord, ctx->sf_nL, ctx->sf_total, SfTri{L.ptr, L.col, L.val, L.dinv, L.flag},
+      ctx->grp, ctx->sf_ord, ctx->sf_nL, ctx->sf_total, SfTri{L.ptr, L.col, L.val, L.dinv, L.flag},
       SfTri{U.ptr, U.col, U.val, U.dinv, U.flag}, b, ctx->g_in, ctx->lu_rs, ctx->lutmp,
       ctx->lutmp2, ctx->sf_ctl, ctx->st);
   launch_perm_gather(ctx->lutmp2, ctx->g_out, nullptr, n, x, ctx->st);
@@ -1523,10 +1768,10 @@ static void sparse_enqueue(peec_ctx* ctx, const c64* x, c64* y, const c64* LpI, 
   const c64* I = x;
   const c64* Q = x + m;
   const c64* Phi = x + m + ns;
-  launch_edge_rows(I, Phi, LpI, ctx->DZ, ctx->n1, ctx->n2, ctx->w, (int)m, ctx->Y1, ctx->U1, st);
+  launch_edge_rows(I, Phi, LpI, ctx->DZ, ctx->n1, ctx->n2, ctx->d_w, (int)m, ctx->Y1, ctx->U1, st);
   launch_surf_rows(PQ, Phi, ctx->snode, ctx->invP, (int)ns, ctx->Y2, ctx->U2, st);
   launch_node_rows(I, Q, Phi, ctx->U1, ctx->U2, ctx->ne_ptr, ctx->ne_idx, ctx->nsn_ptr,
-                   ctx->nsn_idx, ctx->yle_ptr, ctx->yle_col, ctx->yle_val, ctx->w, (int)n,
+                   ctx->nsn_idx, ctx->yle_ptr, ctx->yle_col, ctx->yle_val, ctx->d_w, (int)n,
                    ctx->tvec, st);
   ctx->launches += 3;
   lu_solve(ctx, ctx->tvec, ctx->Mvec);
@@ -1539,6 +1784,26 @@ static void sparse_enqueue(peec_ctx* ctx, const c64* x, c64* y, const c64* LpI, 
 static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool events) {
   cudaStream_t st = ctx->st;
   if (events) cudaEventRecord(ctx->ev[0], st);
+  if (ctx->dense) {
+    // Lp blocks (without their diagonals) and P: FP32 copies for the FP32 operator, FP64
+    // for the others (more accurate than float-float, at FP64 speed). The pass events of
+    // a profile put the products in the z-pass slot.
+    const bool f32 = prec == PEEC_PREC_FP32;
+    cudaEvent_t* pe = ctx->prof ? ctx->pev.data() : nullptr;
+    if (pe) for (int e = 0; e < 3; ++e) cudaEventRecord(pe[e], st);
+    const int64_t off[3] = {0, ctx->mx, ctx->mx + ctx->my};
+    const int64_t sz[3] = {ctx->mx, ctx->my, ctx->mz};
+    for (int b = 0; b < 3; ++b)
+      ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[b] : (const void*)ctx->dn64[b], f32,
+                                   sz[b], x + off[b], 1, ctx->dn_part, ctx->LpI + off[b], st);
+    ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[3] : (const void*)ctx->dn64[3], f32,
+                                 ctx->ns, x + ctx->m, 0, ctx->dn_part, ctx->PQ, st);
+    if (pe) for (int e = 3; e < 6; ++e) cudaEventRecord(pe[e], st);
+    if (events) cudaEventRecord(ctx->ev[1], st);
+    sparse_enqueue(ctx, x, y, ctx->LpI, ctx->PQ);
+    if (events) cudaEventRecord(ctx->ev[2], st);
+    return PEEC_OK;
+  }
   const void* tw[3] = {ctx->tw64, ctx->tw32, ctx->twff};
   const void* ph[6] = {ctx->ph64[0], ctx->ph64[1], ctx->ph64[2],
                        ctx->ph32[0], ctx->ph32[1], ctx->ph32[2]};
@@ -1775,6 +2040,7 @@ static int peec_adjoint_body(peec_ctx* ctx, const double* x, const int32_t* v1,
   if (!ctx || !x || !v1 || !v2 || !d1 || !d2 || !g || nvox < 0 || Is == 0)
     return badarg("peec_adjoint");
   if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  if (!ctx->lattice) return bad(ctx, PEEC_ERR_STATE, "no voxel lattice (peec_set_incidence topology)");
   PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   const int64_t m = ctx->m;
   int32_t *dv1 = nullptr, *dv2 = nullptr;
@@ -1824,14 +2090,17 @@ static int ensure_krylov(peec_ctx* ctx, int k, int prec) {
   const size_t N = ctx->N;
   if (prec == PEEC_PREC_FP32) {
     if (ctx->kcap_u32 < k) {
+      drop_krylov_graphs(ctx);
       CTX_TRY(dalloc(&ctx->U32, N * (size_t)k));
       ctx->kcap_u32 = k;
     }
   } else if (ctx->kcap_u < k) {
+    drop_krylov_graphs(ctx);
     CTX_TRY(dalloc(&ctx->U, N * (size_t)k));
     ctx->kcap_u = k;
   }
   if (ctx->kcap >= k) return PEEC_OK;
+  drop_krylov_graphs(ctx);
   for (c64** p : {&ctx->gb, &ctx->gx, &ctx->gr, &ctx->gv, &ctx->gw, &ctx->gxm, &ctx->gxmin,
                   &ctx->gtmp, &ctx->gzero})
     CTX_TRY(dalloc(p, N));
@@ -1847,14 +2116,137 @@ static int ensure_krylov(peec_ctx* ctx, int k, int prec) {
   return PEEC_OK;
 }
 
+// byte offsets of the arrays of a cycle state with `inner` iterations (16-byte aligned)
+struct GmLayout {
+  size_t res, wv, J, Utop, R, total;
+};
+static GmLayout gm_layout(int inner) {
+  auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  GmLayout L;
+  size_t o = up16(sizeof(GmDev));
+  L.res = o;
+  o = up16(o + sizeof(double) * ((size_t)inner + 2));
+  L.wv = o;
+  o += sizeof(c64) * ((size_t)inner + 1);
+  L.J = o;
+  o += sizeof(c64) * 2 * (size_t)inner;
+  L.Utop = o;
+  o += sizeof(c64) * ((size_t)inner + 1) * ((size_t)inner + 1);
+  L.R = o;
+  o += sizeof(c64) * (size_t)inner * inner;
+  L.total = o;
+  return L;
+}
+
+static int ensure_gm(peec_ctx* ctx, int inner) {
+  if (ctx->gm_inner == inner && ctx->gm_block) return PEEC_OK;
+  drop_krylov_graphs(ctx);
+  const GmLayout L = gm_layout(inner);
+  CTX_TRY(dalloc(&ctx->gm_block, L.total));
+  if (ctx->gm_up) cudaFreeHost(ctx->gm_up);
+  if (ctx->gm_down) cudaFreeHost(ctx->gm_down);
+  ctx->gm_up = ctx->gm_down = nullptr;
+  ctx->gm_inner = -1;
+  PEEC_CUDA_TRY(cudaMallocHost(&ctx->gm_up, sizeof(GmDev)));
+  PEEC_CUDA_TRY(cudaMallocHost(&ctx->gm_down, L.J));
+  ctx->gm_inner = inner;
+  return PEEC_OK;
+}
+
+// whether the operator application (x, y, prec) has run once outside a capture, so that
+// its one-time set-up is done and it may be captured
+static bool matvec_warm(peec_ctx* ctx, const c64* x, c64* y, int prec) {
+  auto it = ctx->graphs.find(std::make_tuple((const void*)x, (void*)y, prec));
+  return it != ctx->graphs.end() && (it->second.calls > 0 || it->second.exec);
+}
+
+// The graph of the device loop: a WHILE conditional node whose body is one Arnoldi
+// iteration (v = P1..Pj e_j, w = A v, orthogonalisation, scalar step, new reflector).
+// The condition starts at 1 on every launch, so the body runs at least once; the scalar
+// step sets it after every iteration.
+static int build_krylov_graph(peec_ctx* ctx, GmBody B, int prec, int inner) {
+  peec_ctx::KrylovGraph& kg = ctx->kg[prec];
+  if (kg.exec) cudaGraphExecDestroy(kg.exec);
+  kg = peec_ctx::KrylovGraph();
+  cudaGraph_t g = nullptr;
+  PEEC_CUDA_TRY(cudaGraphCreate(&g, 0));
+  auto fail = [&](cudaError_t e, const char* what) {
+    cudaGraphDestroy(g);
+    return fail_cuda(e, what, __FILE__, __LINE__);
+  };
+  cudaGraphConditionalHandle h = 0;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) return fail(e, "cudaGraphConditionalHandleCreate");
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+  if (e != cudaSuccess) return fail(e, "cudaGraphAddNode (while)");
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(ctx->st, body, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return fail(e, "cudaStreamBeginCaptureToGraph");
+  B.cond = h;
+  B.use_cond = 1;
+  const int64_t l0 = ctx->launches;
+  ctx->launches += gm_pre(B);
+  const int rc = matvec_enqueue(ctx, B.v, B.w, prec, false);
+  ctx->launches += gm_post(B);
+  const int64_t kernels = ctx->launches - l0;
+  ctx->launches = l0;
+  cudaGraph_t cap = nullptr;
+  e = cudaStreamEndCapture(ctx->st, &cap);
+  if (rc != PEEC_OK) {
+    cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(e, "cudaStreamEndCapture (while body)");
+  e = cudaGraphInstantiate(&kg.exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    kg.exec = nullptr;
+    return fail_cuda(e, "cudaGraphInstantiate (device loop)", __FILE__, __LINE__);
+  }
+  kg.inner = inner;
+  kg.kernels = kernels;
+  return PEEC_OK;
+}
+
+// Runs Arnoldi iterations of the current cycle from the state's iteration index: as one
+// launch of the device-loop graph (iterations until the scalar step ends the loop), or
+// one iteration of eager launches (the first application of the operator on these
+// buffers, profiling, or the device loop switched off). *graph_kernels: kernels per
+// iteration of a graph launch, 0 for an eager iteration (counted here).
+static int gm_iterate(peec_ctx* ctx, GmBody& B, int prec, int inner, int64_t* graph_kernels) {
+  *graph_kernels = 0;
+  if (ctx->dev_loop && !ctx->prof && matvec_warm(ctx, B.v, B.w, prec)) {
+    peec_ctx::KrylovGraph& kg = ctx->kg[prec];
+    if (!kg.exec || kg.inner != inner) CTX_TRY(build_krylov_graph(ctx, B, prec, inner));
+    PEEC_CUDA_TRY(cudaGraphLaunch(kg.exec, ctx->st));
+    *graph_kernels = kg.kernels;
+    ctx->kg_launches++;
+    return PEEC_OK;
+  }
+  B.use_cond = 0;
+  ctx->launches += gm_pre(B);
+  CTX_TRY(matvec_dev(ctx, B.v, B.w, prec, false));
+  ctx->launches += gm_post(B);
+  PEEC_CUDA_TRY(cudaGetLastError());
+  return PEEC_OK;
+}
+
 namespace {
 
 // Host side of the Householder GMRES. Vectors of length N live on the device; the
 // compact-WY matrix T (reflector products P1..Pk = I - U T U^H) lives on the device
-// and is only touched by small kernels; the leading rows Utop of the reflectors, the
-// Givens rotations, R and w are host FP64 arrays. Host -> device coefficient vectors
-// go through a ring of pinned slots, so only reads of scalars the control flow needs
-// synchronise the stream.
+// and is only touched by small kernels; so does the scalar work of an iteration
+// (k_gm_step: reflector heads, Givens rotations, R, w, the residual estimate). The host
+// runs the reference's control flow around it: the convergence checks on the true
+// residual, stagnation, restarts. Host -> device coefficient vectors go through a ring
+// of pinned slots.
 struct Gm {
   peec_ctx* ctx;
   size_t N;
@@ -2017,12 +2409,54 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
   resvec[0] = normr;
   double normrmin = normr;
   const int ld = inner + 1;
-  std::vector<cd> J(2 * (size_t)inner), R((size_t)inner * inner), wv(inner + 1);
+  std::vector<cd> R((size_t)inner * inner), wv(inner + 1);
   std::vector<cd> Utop((size_t)ld * ld);
   int outitercount = 0, initercount = 0;
   double normr_act = normr;
   int it0 = 0, it1 = 0;
   const int headlen = (int)std::min<size_t>(N, (size_t)ld);
+  // the cycle's device state and the buffers of the device loop's body
+  CTX_TRY(ensure_gm(ctx, inner));
+  const GmLayout GL = gm_layout(inner);
+  unsigned char* gblk = ctx->gm_block;
+  GmDev hdr = {};
+  hdr.inner = inner;
+  hdr.n = n;
+  hdr.headlen = headlen;
+  hdr.ld = ld;
+  hdr.tolb = tolb;
+  hdr.res = (double*)(gblk + GL.res);
+  hdr.wv = (c64*)(gblk + GL.wv);
+  hdr.J = (c64*)(gblk + GL.J);
+  hdr.Utop = (c64*)(gblk + GL.Utop);
+  hdr.R = (c64*)(gblk + GL.R);
+  GmBody B;
+  if (f32) B.U32 = ctx->U32;
+  else B.U = ctx->U;
+  B.N = N;
+  B.T = ctx->dT;
+  B.ldT = ldT;
+  B.kmax = inner;
+  B.gs = (GmDev*)gblk;
+  B.v = v;
+  B.w = add;
+  B.coef = ctx->dcoef;
+  B.coef2 = ctx->dcoef2;
+  B.part = ctx->dpart;
+  B.red = ctx->dred;
+  B.scal = ctx->dscal;
+  B.st = ctx->st;
+  // the first k columns of R and Utop, read back for the host's least-squares solves
+  // (the convergence checks on the true residual and the end of a cycle)
+  auto pull = [&](int k) -> int {
+    if (k <= 0) return PEEC_OK;
+    cudaMemcpyAsync(Utop.data(), hdr.Utop, sizeof(c64) * (size_t)k * ld, cudaMemcpyDeviceToHost,
+                    ctx->st);
+    cudaMemcpyAsync(R.data(), hdr.R, sizeof(c64) * (size_t)k * inner, cudaMemcpyDeviceToHost,
+                    ctx->st);
+    PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+    return PEEC_OK;
+  };
   for (int outiter = 1; outiter <= outer; ++outiter) {
     outitercount++;
     std::fill(Utop.begin(), Utop.end(), cd(0));
@@ -2045,179 +2479,142 @@ static int gmres_run(peec_ctx* ctx, const c64* b_dev, c64* x_dev, double tol, in
       ctx->launches++;
       wv.assign(inner + 1, cd(0));
       wv[0] = -beta;
+      g.to_dev(hdr.Utop, std::vector<cd>(Utop.begin(), Utop.begin() + headlen));
+      g.to_dev(hdr.wv, wv);
     }
     initercount = 0;
-    for (int initer = 1; initer <= inner; ++initer) {
+    int jdone = 0;       // iterations of this cycle done on the device
+    bool leave = false;  // the cycle ended before its last iteration
+    while (jdone < inner && !leave) {
       if (ctx->stop && *ctx->stop) {
-        *flag_out = 99; *relres_out = 0; iter_out[0] = outiter; iter_out[1] = initer;
+        *flag_out = 99; *relres_out = 0; iter_out[0] = outiter; iter_out[1] = jdone + 1;
         resvec_out.assign(1, 0.0);
         return bad(ctx, PEEC_ERR_CANCELLED, "cancelled by stop flag");
       }
-      initercount++;
-      const int j = initer - 1;
-      const int k = initer;
-      // v = P1..Pj e_j = e_j - U T conj(Utop(j,0:j+1))
-      {
-        std::vector<cd> rb(k);
-        for (int col = 0; col < k; ++col) rb[col] = std::conj(Utop[(size_t)col * ld + j]);
-        g.to_dev(ctx->dcoef2, rb);
-        launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dcoef, 0, ctx->st);
-        if (f32) launch_multiaxpy(ctx->U32, N, nullptr, j, ctx->dcoef, k, N, v, N, nullptr, ctx->st);
-        else launch_multiaxpy(ctx->U, N, nullptr, j, ctx->dcoef, k, N, v, N, nullptr, ctx->st);
-        launch_norm2(v, N, 0, ctx->dred, ctx->dscal, ctx->st);
-        launch_scale_rnorm(v, N, ctx->dscal, ctx->st);
-        ctx->launches += 5;
-      }
-      g.matvec(v, add);  // add <- A v
+      // Iterations run on the device until the residual estimate reaches tolb, the cycle
+      // is full, or (exit_now) the host's stagnation / extra-step logic wants each one.
+      // Those that went on had none of the conditions of the check below, so only the
+      // last one needs it: the reference's control flow, iteration for iteration.
+      hdr.j = jdone;
+      hdr.exit_now = (stag >= maxstagsteps || moresteps == 1) ? 1 : 0;
+      hdr.normr = normr;
+      std::memcpy(ctx->gm_up, &hdr, sizeof(GmDev));
+      PEEC_CUDA_TRY(cudaMemcpyAsync(gblk, ctx->gm_up, sizeof(GmDev), cudaMemcpyHostToDevice,
+                                    ctx->st));
+      int64_t per_it = 0;
+      CTX_TRY(gm_iterate(ctx, B, prec, inner, &per_it));
+      PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->gm_down, gblk, GL.J, cudaMemcpyDeviceToHost, ctx->st));
+      PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
       if (g.rc) return g.rc;
-      // v = Pj..P1 A v = (I - U T^H U^H) A v, with the tail norm from index initer
-      double alpha2 = 0.0;
-      std::vector<cd> vh;
-      {
-        ctx->launches += f32 ? launch_multidot(ctx->U32, N, add, N, k, ctx->dpart, ctx->dcoef2, ctx->st)
-                             : launch_multidot(ctx->U, N, add, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
-        launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dcoef, 1, ctx->st);  // c = T^H z
-        if (f32)
-          launch_multiaxpy(ctx->U32, N, add, 0, ctx->dcoef, k, N, v, (size_t)initer, ctx->dred,
-                           ctx->st);
-        else
-          launch_multiaxpy(ctx->U, N, add, 0, ctx->dcoef, k, N, v, (size_t)initer, ctx->dred,
-                           ctx->st);
-        launch_sum_parts(ctx->dred, red_blocks(N), ctx->dscal, ctx->st);
-        ctx->launches += 3;
-        cudaMemcpyAsync(ctx->hscal, ctx->dscal, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
-        vh = g.from_dev(v, headlen);
-        alpha2 = ctx->hscal[0];
-        if (g.rc) return g.rc;
+      const GmDev* hd = (const GmDev*)ctx->gm_down;
+      const double* hres = (const double*)(ctx->gm_down + GL.res);
+      const c64* hwv = (const c64*)(ctx->gm_down + GL.wv);
+      const int jafter = hd->j;
+      if (jafter <= jdone || jafter > inner)
+        return bad(ctx, PEEC_ERR_CUDA, "device Arnoldi loop: the iteration count did not advance");
+      if (per_it) {
+        ctx->launches += per_it * (jafter - jdone);
+        ctx->kg_iterations += jafter - jdone;
       }
-      std::vector<cd> vs(inner + 1, cd(0));
-      for (int i = 0; i < std::min(inner + 1, headlen); ++i) vs[i] = vh[i];
-      if (initer != n) {
-        double alpha = std::sqrt(alpha2);
-        if (alpha != 0) {
-          const cd vj1 = vh[initer];
-          const cd a = sgn(vj1) * alpha;
-          const double nu2 = alpha2 - std::norm(vj1) + std::norm(vj1 + a);
-          const double sc = 1.0 / std::sqrt(nu2);
-          c64* unew = f32 ? nullptr : ctx->U + (size_t)initer * N;
-          cff* unew32 = f32 ? ctx->U32 + (size_t)initer * N : nullptr;
-          if (f32)
-            launch_make_reflector(v, N, initer, mk<double>(a.real(), a.imag()), sc, unew32, ctx->st);
-          else
-            launch_make_reflector(v, N, initer, mk<double>(a.real(), a.imag()), sc, unew, ctx->st);
-          for (int i = 0; i < headlen; ++i)
-            Utop[(size_t)initer * ld + i] =
-                i < initer ? cd(0) : (i == initer ? (vh[i] + a) * sc : vh[i] * sc);
-          // T(0:k, k) = -2 T(0:k,0:k) (U(:,0:k)^H u_k), T(k,k) = 2 -- all on the device
-          ctx->launches +=
-              f32 ? launch_multidot(ctx->U32, N, unew32, N, k, ctx->dpart, ctx->dcoef2, ctx->st)
-                  : launch_multidot(ctx->U, N, unew, N, k, ctx->dpart, ctx->dcoef2, ctx->st);
-          launch_tri(ctx->dT, ldT, k, ctx->dcoef2, ctx->dT + (size_t)k * ldT, 2, ctx->st);
-          ctx->launches += 2;
-          for (int i = initer + 1; i <= inner; ++i) vs[i] = 0;
-          vs[initer] = -a;
+      for (int i = 0; i <= inner; ++i) wv[i] = cd(hwv[i].x, hwv[i].y);
+      for (int initer = jdone + 1; initer <= jafter; ++initer) {
+        initercount++;
+        const int j = initer - 1;
+        normr = hres[initer];
+        resvec[(size_t)(outiter - 1) * inner + initer] = normr;
+        normr_act = normr;
+        if (initer == jafter && (normr <= tolb || stag >= maxstagsteps || moresteps == 1)) {
+          CTX_TRY(pull(initer));
+          do {
+            if (evalxm == 0) {
+              std::vector<cd> rhs(wv.begin(), wv.begin() + initer);
+              std::vector<cd> ytmp = utri_solve(R, inner, initer, rhs);
+              apply_Q(g, Utop, ld, initer, ytmp, nullptr, add);
+              const double na = g.norm(add), nx = g.norm(x);
+              if (na < 2.220446049250313e-16 * nx) stag++;
+              else stag = 0;
+              // xm = x + additive
+              apply_Q(g, Utop, ld, initer, ytmp, x, xm);
+              evalxm = 1;
+            } else {
+              const cd wr = wv[j] / R[(size_t)j * inner + j];
+              std::vector<cd> addvc(initer);
+              if (initer > 1) {
+                std::vector<cd> rhs(initer - 1);
+                for (int i = 0; i < initer - 1; ++i) rhs[i] = R[(size_t)j * inner + i];
+                std::vector<cd> hsol = utri_solve(R, inner, initer - 1, rhs);
+                for (int i = 0; i < initer - 1; ++i) addvc[i] = -hsol[i] * wr;
+              }
+              addvc[initer - 1] = wr;
+              double nav = 0;
+              for (auto& q : addvc) nav += std::norm(q);
+              nav = std::sqrt(nav);
+              const double nxm = g.norm(xm);
+              if (nav < 2.220446049250313e-16 * nxm) stag++;
+              else stag = 0;
+              g.copy(ctx->gtmp, xm);
+              apply_Q(g, Utop, ld, initer, addvc, ctx->gtmp, xm);
+            }
+            g.residual(b, xm, r);
+            const double nr = g.norm(r);
+            if (g.rc) return g.rc;
+            if (nr <= tol * n2b) {
+              g.copy(x, xm);
+              flag = 0;
+              it0 = outiter;
+              it1 = initer;
+              leave = true;
+              break;
+            }
+            normr_act = nr;
+            resvec[(size_t)(outiter - 1) * inner + initer] = normr_act;
+            if (normr_act <= normrmin) {
+              normrmin = normr_act;
+              imin = outiter;
+              jmin = initer;
+              g.copy(xmin, xm);
+              minupdated = 1;
+            }
+            if (normr_act <= tolb) {
+              g.copy(x, xm);
+              flag = 0;
+              it0 = outiter;
+              it1 = initer;
+              leave = true;
+              break;
+            } else {
+              if (stag >= maxstagsteps && moresteps == 0) stag = 0;
+              moresteps++;
+              if (moresteps >= maxmsteps) {
+                flag = 3;
+                it0 = outiter;
+                it1 = initer;
+                leave = true;
+                break;
+              }
+            }
+          } while (false);
+          if (leave) break;
         }
-      }
-      // Givens
-      for (int colJ = 0; colJ < initer - 1; ++colJ) {
-        const cd tmpv = vs[colJ];
-        vs[colJ] = std::conj(J[2 * colJ]) * vs[colJ] + std::conj(J[2 * colJ + 1]) * vs[colJ + 1];
-        vs[colJ + 1] = -J[2 * colJ + 1] * tmpv + J[2 * colJ] * vs[colJ + 1];
-      }
-      if (initer != n) {
-        const double rho = std::sqrt(std::norm(vs[j]) + std::norm(vs[j + 1]));
-        J[2 * j] = vs[j] / rho;
-        J[2 * j + 1] = vs[j + 1] / rho;
-        wv[j + 1] = -J[2 * j + 1] * wv[j];
-        wv[j] = std::conj(J[2 * j]) * wv[j];
-        vs[j] = rho;
-        vs[j + 1] = 0;
-      }
-      for (int i = 0; i < inner; ++i) R[(size_t)j * inner + i] = vs[i];
-      normr = std::abs(wv[j + 1]);
-      resvec[(size_t)(outiter - 1) * inner + initer] = normr;
-      normr_act = normr;
-      if (normr <= tolb || stag >= maxstagsteps || moresteps == 1) {
-        if (evalxm == 0) {
-          std::vector<cd> rhs(wv.begin(), wv.begin() + initer);
-          std::vector<cd> ytmp = utri_solve(R, inner, initer, rhs);
-          apply_Q(g, Utop, ld, initer, ytmp, nullptr, add);
-          const double na = g.norm(add), nx = g.norm(x);
-          if (na < 2.220446049250313e-16 * nx) stag++;
-          else stag = 0;
-          // xm = x + additive
-          apply_Q(g, Utop, ld, initer, ytmp, x, xm);
-          evalxm = 1;
-        } else {
-          const cd wr = wv[j] / R[(size_t)j * inner + j];
-          std::vector<cd> addvc(initer);
-          if (initer > 1) {
-            std::vector<cd> rhs(initer - 1);
-            for (int i = 0; i < initer - 1; ++i) rhs[i] = R[(size_t)j * inner + i];
-            std::vector<cd> hsol = utri_solve(R, inner, initer - 1, rhs);
-            for (int i = 0; i < initer - 1; ++i) addvc[i] = -hsol[i] * wr;
-          }
-          addvc[initer - 1] = wr;
-          double nav = 0;
-          for (auto& q : addvc) nav += std::norm(q);
-          nav = std::sqrt(nav);
-          const double nxm = g.norm(xm);
-          if (nav < 2.220446049250313e-16 * nxm) stag++;
-          else stag = 0;
-          g.copy(ctx->gtmp, xm);
-          apply_Q(g, Utop, ld, initer, addvc, ctx->gtmp, xm);
-        }
-        g.residual(b, xm, r);
-        const double nr = g.norm(r);
-        if (g.rc) return g.rc;
-        if (nr <= tol * n2b) {
-          g.copy(x, xm);
-          flag = 0;
-          it0 = outiter;
-          it1 = initer;
-          break;
-        }
-        normr_act = nr;
-        resvec[(size_t)(outiter - 1) * inner + initer] = normr_act;
         if (normr_act <= normrmin) {
           normrmin = normr_act;
           imin = outiter;
           jmin = initer;
-          g.copy(xmin, xm);
           minupdated = 1;
         }
-        if (normr_act <= tolb) {
-          g.copy(x, xm);
-          flag = 0;
-          it0 = outiter;
-          it1 = initer;
+        if (stag >= maxstagsteps) {
+          flag = 3;
+          leave = true;
           break;
-        } else {
-          if (stag >= maxstagsteps && moresteps == 0) stag = 0;
-          moresteps++;
-          if (moresteps >= maxmsteps) {
-            flag = 3;
-            it0 = outiter;
-            it1 = initer;
-            break;
-          }
         }
       }
-      if (normr_act <= normrmin) {
-        normrmin = normr_act;
-        imin = outiter;
-        jmin = initer;
-        minupdated = 1;
-      }
-      if (stag >= maxstagsteps) {
-        flag = 3;
-        break;
-      }
+      jdone = jafter;
     }
     evalxm = 0;
     if (flag != 0) {
       const int idx = minupdated == 1 ? jmin : initercount;
       if (idx > 0) {
+        CTX_TRY(pull(idx));
         std::vector<cd> rhs(wv.begin(), wv.begin() + idx);
         std::vector<cd> y = utri_solve(R, inner, idx, rhs);
         g.copy(ctx->gtmp, x);
@@ -2457,6 +2854,19 @@ extern "C" int peec_set_topology(peec_ctx* ctx, int Nx, int Ny, int Nz, int64_t 
     return peec_set_topology_body(ctx, Nx, Ny, Nz, mx, my, mz, edge_cell, edge_n1, edge_n2, ns,
         surf_fam, surf_cell, surf_node, n);
   });
+}
+
+extern "C" int peec_set_incidence(peec_ctx* ctx, int64_t mx, int64_t my, int64_t mz,
+                                  const int64_t* edge_n1, const int64_t* edge_n2, int64_t ns,
+                                  const int64_t* surf_node, int64_t n) {
+  return guarded(ctx, "peec_set_incidence", [&] {
+    return peec_set_incidence_body(ctx, mx, my, mz, edge_n1, edge_n2, ns, surf_node, n);
+  });
+}
+
+extern "C" int peec_set_dense(peec_ctx* ctx, const double* Lp_x, const double* Lp_y,
+                              const double* Lp_z, const double* P) {
+  return guarded(ctx, "peec_set_dense", [&] { return peec_set_dense_body(ctx, Lp_x, Lp_y, Lp_z, P); });
 }
 
 extern "C" int peec_set_pdiag(peec_ctx* ctx, const double* diagP) {

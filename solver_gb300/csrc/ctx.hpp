@@ -25,20 +25,42 @@ struct SfTri {
 };
 constexpr int SF_TPB = 128;
 
-// components of the LU factors solved by one warp each (rows at most SF_COMP_MAX)
+// Groups of the LU solves (sparse.cu, k_sptrsv_grp). The rows of L and U fall into
+// connected components (rows linked by a factor entry) that never depend on one another.
+// Components of at most 32 rows (and SF_GRP_E entries) are packed into groups of at most
+// 32 rows; larger ones (up to SF_COMP_MAX rows) form a group each. One warp solves a
+// group: it loads all of the group's rows, entries and right-hand sides into shared
+// memory with parallel loads, then runs the group's L levels and U levels there.
 constexpr int SF_COMP_MAX = 512;
-constexpr int SFC_TPB = 128;
-struct CompPlan {
-  const int32_t* off;     // ncomp + 1 offsets into the row lists
-  const int32_t* rowsL;   // rows of each component in L-level order
-  const int32_t* rowsU;   // same rows in U-level order
-  const int32_t* segL;    // end offset of each L level segment
-  const int32_t* segU;    // end offset of each U level segment
-  const int32_t* segLoff; // ncomp + 1 offsets into segL
-  const int32_t* segUoff; // ncomp + 1 offsets into segU
-  const int32_t* local;   // row -> position in its component's L order
-  int n;
+constexpr int SF_GRP_E = 256;  // entries (L and U off-diagonal) of a packed group
+constexpr int SF_GRP_WARPS = 4;
+struct GrpRow {
+  int32_t r;       // factor row
+  int32_t pL, pU;  // first entry of the row in L and in U (CSR)
+  int32_t j;       // original row of its right-hand side (Pr)
+  int16_t nL, nU;  // entries of the row in L and in U
+  int16_t eL, eU;  // their offsets in the group's shared entry array
 };
+struct GrpPlan {
+  const int32_t* goff = nullptr;    // ngroups + 1 offsets into rows
+  const GrpRow* rows = nullptr;     // per position: the group's rows in L-level order
+  const int16_t* uq = nullptr;      // per position in U-level order: that row's L position
+  const int32_t* seg = nullptr;     // per group: ends of its L levels, then of its U levels
+  const int32_t* segoff = nullptr;  // ngroups + 1 offsets into seg
+  const int32_t* nsegL = nullptr;   // per group: the number of its L level ends
+  const int16_t* lcolL = nullptr;   // per L entry (CSR order): its column's L position
+  const int16_t* lcolU = nullptr;   // per U entry
+  int nbig = 0, ngroups = 0;        // groups [0, nbig) hold one large component each
+  int rb = 0, eb = 0;               // the large groups' largest row and entry counts
+};
+// shared memory of one group of R rows and E entries
+__host__ __device__ inline size_t grp_smem(int R, int E) {
+  size_t o = 48 * (size_t)R + 16 * (size_t)E;  // x, 1/L(i,i), 1/U(i,i), entry values
+  o += 8 * (size_t)R + 2 * (size_t)E + 2 * (size_t)R;  // row metadata, entry columns, U order
+  o = (o + 3) & ~(size_t)3;
+  o += 8 * (size_t)R;  // level ends (at most 2R)
+  return (o + 15) & ~(size_t)15;
+}
 
 // Device refactorisation of SS in a fixed pattern (refactor.cu): slots are the off-diagonal
 // entries of L, then the diagonal of U (D), then the off-diagonal entries of U
@@ -55,6 +77,50 @@ struct RefactorPlan {
 int refactor_launch(const RefactorPlan& R, const SfTri& L, const SfTri& U, c64* Lval, c64* Uval,
                     const c64* DZ, const double* invP, const c64* yle, double w, int* err,
                     cudaStream_t st);
+
+// Device-resident state of one Householder GMRES cycle (the Arnoldi loop's scalar work
+// runs in k_gm_step, krylov.cu). The host writes the header before a run of iterations
+// and reads back the header, res and wv after it; Utop and R only when its convergence
+// check needs them. All arrays live in one allocation after the header.
+struct GmDev {
+  int j;          // inner iterations done in this cycle (the next one's 0-based index)
+  int inner;      // iterations per cycle
+  int n;          // system size (the reference's initer != n tests)
+  int headlen;    // min(N, inner + 1): rows of the reflectors kept in Utop
+  int ld;         // inner + 1, leading dimension of Utop
+  int exit_now;   // host: leave the loop after the next iteration
+  int refl_on;    // the last iteration appended a reflector (alpha != 0)
+  int pad_;
+  double tolb;    // tol * |b|: the loop continues while |w(j+1)| > tolb
+  double normr;   // |w(j+1)| after the last iteration
+  double refl_scale;
+  double pad2_;
+  c64 refl_add;   // the new reflector: u = (v with rows < j zeroed, v(j) += add) * scale
+  double* res;    // [inner + 2] residual estimates, res[initer] = |w(initer)|
+  c64* wv;        // [inner + 1] Givens-rotated right-hand side w
+  c64* J;         // [2 * inner] Givens rotations (c, s) per column
+  c64* Utop;      // [ld * ld] leading rows of the reflectors, column-major
+  c64* R;         // [inner * inner] upper-triangular R, column-major, ld = inner
+};
+
+// Buffers of the device loop's Arnoldi body (krylov.cu): the basis is U (complex double)
+// or U32 (complex float-float), whichever is set; T the compact-WY factor (ld ldT); v the
+// iteration's vector, w = A v; kmax the largest column count of the cycle (inner).
+struct GmBody {
+  c64* U = nullptr;
+  cff* U32 = nullptr;
+  size_t N = 0;
+  c64* T = nullptr;
+  int ldT = 0, kmax = 0;
+  GmDev* gs = nullptr;
+  c64 *v = nullptr, *w = nullptr, *coef = nullptr, *coef2 = nullptr, *part = nullptr;
+  double *red = nullptr, *scal = nullptr;
+  cudaGraphConditionalHandle cond = 0;
+  int use_cond = 0;  // 1 inside the WHILE node's body graph, 0 for a single eager iteration
+  cudaStream_t st = nullptr;
+};
+int gm_pre(const GmBody& B);   // returns the kernels launched
+int gm_post(const GmBody& B);
 
 #define CTX_CHECK(expr)      \
   do {                       \

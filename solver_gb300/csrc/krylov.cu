@@ -46,13 +46,27 @@ __device__ __forceinline__ double warp_sum(double v) {
 // partial[c0+c][blk] (complex) = sum over the CTA's rows of conj(U[i,c0+c]) * v[i],
 // c < NC: the tile's columns are a template parameter, so loads, products and the
 // shuffle reductions are exactly the ones needed; each thread walks at least eight rows
-template <int NC, typename UT, typename VT>
+// DYN: the column count and the vector come from the device loop's iteration index
+// (k = *dj + koff, v += *dj * vstep); column tiles past k leave at once, the last tile
+// masks its columns. Per column the arithmetic and the summation order are those of the
+// fixed-count form.
+template <int NC, typename UT, typename VT, bool DYN = false>
 __global__ void __launch_bounds__(RED_TPB) k_multidot(const UT* __restrict__ U, size_t ldu,
                                                       const VT* __restrict__ v, size_t N,
-                                                      int c0, c64* partial) {
+                                                      int c0, c64* partial,
+                                                      const int* __restrict__ dj = nullptr,
+                                                      int koff = 0, size_t vstep = 0) {
   using A = typename BasisArith<UT>::A;
   __shared__ double red[RED_TPB / 32][2 * NC];
   c0 += blockIdx.y * NC;
+  int nc = NC;
+  if (DYN) {
+    const int jj = *dj;
+    v += (size_t)jj * vstep;
+    nc = jj + koff - c0;
+    if (nc <= 0) return;  // the whole CTA: no barrier has been reached
+    if (nc > NC) nc = NC;
+  }
   const UT* __restrict__ Uc = U + (size_t)c0 * ldu;
   A ar[NC], ai[NC];
 #pragma unroll
@@ -62,11 +76,14 @@ __global__ void __launch_bounds__(RED_TPB) k_multidot(const UT* __restrict__ U, 
     cx<A> u[NC];
     const cx<A> x = as<A>(v[i]);
 #pragma unroll
-    for (int c = 0; c < NC; ++c) u[c] = as<A>(Uc[(size_t)c * ldu + i]);
+    for (int c = 0; c < NC; ++c)
+      if (!DYN || c < nc) u[c] = as<A>(Uc[(size_t)c * ldu + i]);
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-      ar[c] = ar[c] + (u[c].x * x.x + u[c].y * x.y);
-      ai[c] = ai[c] + (u[c].x * x.y - u[c].y * x.x);
+      if (!DYN || c < nc) {
+        ar[c] = ar[c] + (u[c].x * x.x + u[c].y * x.y);
+        ai[c] = ai[c] + (u[c].x * x.y - u[c].y * x.x);
+      }
     }
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -79,7 +96,7 @@ __global__ void __launch_bounds__(RED_TPB) k_multidot(const UT* __restrict__ U, 
     }
   }
   __syncthreads();
-  if (threadIdx.x < 2 * NC) {
+  if (threadIdx.x < 2 * nc) {
     double s = 0.0;
     for (int w = 0; w < RED_TPB / 32; ++w) s += red[w][threadIdx.x];
     const int c = threadIdx.x >> 1;
@@ -90,7 +107,9 @@ __global__ void __launch_bounds__(RED_TPB) k_multidot(const UT* __restrict__ U, 
 
 // out[c] = sum_b partial[c][b]: one warp per column, lane-strided then a shuffle tree
 // (fixed order for a fixed block count)
-__global__ void k_reduce_cols(const c64* __restrict__ partial, int nblk, int k, c64* out) {
+__global__ void k_reduce_cols(const c64* __restrict__ partial, int nblk, int k, c64* out,
+                              const int* __restrict__ dj = nullptr) {
+  if (dj) k += *dj;  // device loop: k is an offset from the iteration index
   const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (c >= k) return;  // whole warps leave together
@@ -111,8 +130,15 @@ __global__ void __launch_bounds__(RED_TPB) k_multiaxpy(const UT* __restrict__ U,
                                                        const c64* __restrict__ base, int unit,
                                                        const c64* __restrict__ coef, int k,
                                                        size_t N, c64* out, size_t tail0,
-                                                       double* tailpart) {
+                                                       double* tailpart,
+                                                       const int* __restrict__ dj = nullptr) {
   using A = typename BasisArith<UT>::A;
+  if (dj) {  // device loop: k, unit and tail0 are offsets from the iteration index
+    const int jj = *dj;
+    k += jj;
+    unit += jj;
+    tail0 += (size_t)jj;
+  }
   extern __shared__ unsigned char sc_raw[];
   cx<A>* sc = reinterpret_cast<cx<A>*>(sc_raw);
   for (int c = threadIdx.x; c < k; c += blockDim.x) sc[c] = as<A>(coef[c]);
@@ -271,6 +297,162 @@ __global__ void k_tri(c64* T, int ld, int k, const c64* __restrict__ in, c64* ou
   if (mode == 2 && threadIdx.x == 0) out[k] = mk<double>(2.0, 0.0);
 }
 
+// The device loop's forms of k_tri, with the iteration index j read from the cycle state
+// (same sums in the same order as k_tri):
+// mode 0: out = T(0:k,0:k) * conj(Utop(j, 0:k)), k = j + 1 (the coefficients of
+//         v = P1..Pj e_j = e_j - U T conj(Utop(j, :)));
+// mode 1: out = T(0:k,0:k)^H * in, k = j + 1;
+// mode 2: after the scalar step (j = the new column k): T(0:k, k) = -2 T(0:k,0:k) * in,
+//         T(k,k) = 2, only when that step appended a reflector.
+__global__ void k_tri_dyn(c64* T, int ld, const GmDev* __restrict__ gs,
+                          const c64* __restrict__ in, c64* out, int mode) {
+  const int j = gs->j;
+  if (mode == 2 && !gs->refl_on) return;
+  const int k = mode == 2 ? j : j + 1;
+  if (mode == 2) out = T + (size_t)k * ld;
+  const c64* __restrict__ ut = gs->Utop;
+  const int ldu = gs->ld;
+  for (int i = threadIdx.x; i < k; i += blockDim.x) {
+    c64 s = mk<double>(0, 0);
+    if (mode == 1) {
+      for (int q = 0; q <= i; ++q) s = s + cconj(T[(size_t)i * ld + q]) * in[q];
+    } else if (mode == 0) {
+      for (int q = i; q < k; ++q) s = s + T[(size_t)q * ld + i] * cconj(ut[(size_t)q * ldu + j]);
+    } else {
+      for (int q = i; q < k; ++q) s = s + T[(size_t)q * ld + i] * in[q];
+    }
+    if (mode == 2) out[i] = cscale(s, -2.0);
+    else out[i] = s;
+  }
+  if (mode == 2 && threadIdx.x == 0) out[k] = mk<double>(2.0, 0.0);
+}
+
+// k_make_reflector with the column, the head correction and the scale from the scalar
+// step: column j of U (j the new iteration count) when that step appended a reflector
+template <typename UT>
+__global__ void k_make_reflector_dyn(const c64* __restrict__ w, size_t N,
+                                     const GmDev* __restrict__ gs, UT* U) {
+  using A = typename BasisArith<UT>::A;
+  if (!gs->refl_on) return;
+  const size_t j = (size_t)gs->j;
+  const c64 add = gs->refl_add;
+  const double scale = gs->refl_scale;
+  UT* u = U + j * N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
+       i += (size_t)gridDim.x * blockDim.x) {
+    c64 x = (i < j) ? mk<double>(0, 0) : w[i];
+    if (i == j) x = x + add;
+    const c64 y = cscale(x, scale);
+    u[i] = mk<A>((A)y.x, (A)y.y);
+  }
+}
+
+__device__ __forceinline__ double cabs2(c64 z) { return z.x * z.x + z.y * z.y; }
+__device__ __forceinline__ c64 csign(c64 d) {
+  if (d.x == 0.0 && d.y == 0.0) return mk<double>(1.0, 0.0);
+  const double a = hypot(d.x, d.y);
+  return mk<double>(d.x / a, d.y / a);
+}
+__device__ __forceinline__ c64 cdivr(c64 z, double r) { return mk<double>(z.x / r, z.y / r); }
+
+// The scalar work of one Householder GMRES iteration (gmres_custom.jl:129-171), in FP64 on
+// the device, given the orthogonalised vector v = Pj..P1 A v_j (its head rows) and the
+// squared norm alpha2 of its rows from initer on:
+//   * the new reflector's head correction a = sign(v(initer)) * alpha and scale, and its
+//     leading rows in Utop (the reflector itself is written by k_make_reflector_dyn);
+//   * the earlier Givens rotations applied to the new column, a new rotation that zeroes
+//     its subdiagonal, the rotated right-hand side w, the column of R;
+//   * |w(initer+1)|, the residual estimate, into res[initer] and the state;
+// and sets the WHILE node's condition: go on while the estimate is above tolb, the cycle
+// has iterations left and the host asked for no early exit. Every path sets it, and the
+// iteration count grows by one per call, so a loop ends after at most `inner` iterations.
+// One warp: its lanes bring v's head and the earlier rotations into shared memory (when
+// they fit), then lane 0 does the scalar work; the rotations form a chain.
+constexpr int GM_SMEM_MAX = 768;  // head entries staged in shared memory (36 KB in all)
+__global__ void k_gm_step(const c64* __restrict__ v_g, const double* __restrict__ alpha2p,
+                          GmDev* gs, cudaGraphConditionalHandle cond, int use_cond) {
+  __shared__ c64 s_v[GM_SMEM_MAX];
+  __shared__ c64 s_J[2 * GM_SMEM_MAX];
+  GmDev& g = *gs;
+  const int j = g.j, initer = j + 1, inner = g.inner, ld = g.ld, headlen = g.headlen, n = g.n;
+  const int nv = min(inner + 1, headlen);
+  const bool staged = nv <= GM_SMEM_MAX && 2 * j <= 2 * GM_SMEM_MAX && j >= 0;
+  if (staged) {
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) s_v[i] = v_g[i];
+    for (int i = threadIdx.x; i < 2 * j; i += blockDim.x) s_J[i] = g.J[i];
+    __syncthreads();
+  }
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const c64* __restrict__ v = staged ? s_v : v_g;
+  const c64* __restrict__ Jold = staged ? s_J : g.J;
+  if (j < 0 || initer > inner) {
+    g.refl_on = 0;
+    if (use_cond) cudaGraphSetConditional(cond, 0u);
+    return;
+  }
+  const c64 zero = mk<double>(0, 0);
+  c64* __restrict__ ucol = g.Utop + (size_t)initer * ld;
+  int refl = 0;
+  c64 a = zero;
+  if (initer != n) {
+    const double alpha2 = *alpha2p;
+    const double alpha = sqrt(alpha2);
+    if (alpha != 0) {
+      const c64 vj1 = v[initer];
+      a = cscale(csign(vj1), alpha);
+      const double nu2 = alpha2 - cabs2(vj1) + cabs2(vj1 + a);
+      const double sc = 1.0 / sqrt(nu2);
+      for (int i = 0; i < headlen; ++i)
+        ucol[i] = i < initer ? zero : (i == initer ? cscale(v[i] + a, sc) : cscale(v[i], sc));
+      g.refl_add = a;
+      g.refl_scale = sc;
+      refl = 1;
+    }
+  }
+  if (!refl)
+    for (int i = 0; i < headlen; ++i) ucol[i] = zero;
+  g.refl_on = refl;
+  // the new column before the rotations: v's head, with the reflector's rows below initer
+  // zeroed and -a at initer
+  auto vs = [&](int i) -> c64 {
+    if (refl && i > initer) return zero;
+    if (refl && i == initer) return mk<double>(-a.x, -a.y);
+    return i < nv ? v[i] : zero;
+  };
+  c64* __restrict__ Rc = g.R + (size_t)j * inner;
+  c64 cur = vs(0);
+  for (int c = 0; c < j; ++c) {
+    const c64 nxt = vs(c + 1);
+    const c64 Jc = Jold[2 * c], Js = Jold[2 * c + 1];
+    Rc[c] = cconj(Jc) * cur + cconj(Js) * nxt;
+    const c64 t = Js * cur;
+    cur = mk<double>(-t.x, -t.y) + Jc * nxt;
+  }
+  c64 vj = cur, vj1 = vs(j + 1);
+  if (initer != n) {
+    const double rho = sqrt(cabs2(vj) + cabs2(vj1));
+    const c64 Jc = cdivr(vj, rho), Js = cdivr(vj1, rho);
+    g.J[2 * j] = Jc;
+    g.J[2 * j + 1] = Js;
+    const c64 wj = g.wv[j];
+    const c64 t = Js * wj;
+    g.wv[j + 1] = mk<double>(-t.x, -t.y);
+    g.wv[j] = cconj(Jc) * wj;
+    vj = mk<double>(rho, 0.0);
+    vj1 = zero;
+  }
+  Rc[j] = vj;
+  if (j + 1 < inner) Rc[j + 1] = vj1;
+  for (int i = j + 2; i < inner; ++i) Rc[i] = vs(i);
+  const c64 w1 = g.wv[j + 1];
+  const double normr = hypot(w1.x, w1.y);
+  g.res[initer] = normr;
+  g.normr = normr;
+  g.j = initer;
+  const bool go = normr > g.tolb && initer < inner && initer != n && !g.exit_now;
+  if (use_cond) cudaGraphSetConditional(cond, go ? 1u : 0u);
+}
+
 __global__ void k_cast_down(const c64* __restrict__ a, size_t N, c32* out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N;
        i += (size_t)gridDim.x * blockDim.x)
@@ -391,6 +573,12 @@ __global__ void k_add_i(const c64* __restrict__ b, size_t N, c64* out) {
   }
 }
 
+__global__ void k_set_scalar(double* p, double v) { *p = v; }
+
+// *p = v in stream order (the value travels as a kernel argument, so no host buffer has to
+// outlive the call)
+void launch_set_scalar(double* p, double v, cudaStream_t st) { k_set_scalar<<<1, 1, 0, st>>>(p, v); }
+
 void launch_add_i(const c64* b, size_t N, c64* out, cudaStream_t st) {
   k_add_i<<<g_stream(N), 256, 0, st>>>(b, N, out);
 }
@@ -415,6 +603,53 @@ void launch_differs(const c64* a, const c64* b, size_t N, int* flag, cudaStream_
 void launch_tri(c64* T, int ld, int k, const c64* in, c64* out, int mode, cudaStream_t st) {
   k_tri<<<1, 256, 0, st>>>(T, ld, k, in, out, mode);
 }
+
+// The device loop's Arnoldi body around one operator application w = A v (the host
+// loop's kernels in the same order, with the iteration index read on the device):
+//   pre:  v = P1..Pj e_j = e_j - U T conj(Utop(j,:)), normalised (as the host loop does);
+//   post: v = w - U T^H U^H w with the tail norm from row initer; the scalar step; the new
+//         reflector and its column of T.
+template <typename UT>
+static int gm_pre_t(const GmBody& B, const UT* U) {
+  using A = typename BasisArith<UT>::A;
+  cudaStream_t st = B.st;
+  const int* dj = &B.gs->j;
+  k_tri_dyn<<<1, 256, 0, st>>>(B.T, B.ldT, B.gs, nullptr, B.coef, 0);
+  k_multiaxpy<UT><<<g_stream(B.N), RED_TPB, sizeof(cx<A>) * (B.kmax + 1), st>>>(
+      U, B.N, nullptr, 0, B.coef, 1, B.N, B.v, 0, nullptr, dj);
+  launch_norm2(B.v, B.N, 0, B.red, B.scal, st);
+  launch_scale_rnorm(B.v, B.N, B.scal, st);
+  return 5;
+}
+
+template <typename UT>
+static int gm_post_t(const GmBody& B, UT* U) {
+  using A = typename BasisArith<UT>::A;
+  cudaStream_t st = B.st;
+  const int* dj = &B.gs->j;
+  const unsigned nb = md_blocks(B.N);
+  const unsigned tiles = (unsigned)((B.kmax + KB - 1) / KB);
+  const unsigned rblk = (unsigned)((B.kmax + 7) / 8);
+  // z = U(:,0:k)^H w, c = T^H z, v = w - U c with the tail norm from row initer
+  k_multidot<KB, UT, c64, true><<<dim3(nb, tiles), RED_TPB, 0, st>>>(U, B.N, B.w, B.N, 0, B.part,
+                                                                     dj, 1, 0);
+  k_reduce_cols<<<rblk, 256, 0, st>>>(B.part, nb, 1, B.coef2, dj);
+  k_tri_dyn<<<1, 256, 0, st>>>(B.T, B.ldT, B.gs, B.coef2, B.coef, 1);
+  k_multiaxpy<UT><<<g_stream(B.N), RED_TPB, sizeof(cx<A>) * (B.kmax + 1), st>>>(
+      U, B.N, B.w, 0, B.coef, 1, B.N, B.v, 1, B.red, dj);
+  k_sum_parts<<<1, 1024, 0, st>>>(B.red, (int)g_stream(B.N), B.scal);
+  k_gm_step<<<1, 32, 0, st>>>(B.v, B.scal, B.gs, B.cond, B.use_cond);
+  // the new reflector u_k (k = the new iteration count) and T(0:k, k) = -2 T (U^H u_k)
+  k_make_reflector_dyn<UT><<<g_stream(B.N), 256, 0, st>>>(B.v, B.N, B.gs, U);
+  k_multidot<KB, UT, UT, true><<<dim3(nb, tiles), RED_TPB, 0, st>>>(U, B.N, U, B.N, 0, B.part, dj,
+                                                                    0, B.N);
+  k_reduce_cols<<<rblk, 256, 0, st>>>(B.part, nb, 0, B.coef2, dj);
+  k_tri_dyn<<<1, 256, 0, st>>>(B.T, B.ldT, B.gs, B.coef2, nullptr, 2);
+  return 10;
+}
+
+int gm_pre(const GmBody& B) { return B.U32 ? gm_pre_t<cff>(B, B.U32) : gm_pre_t<c64>(B, B.U); }
+int gm_post(const GmBody& B) { return B.U32 ? gm_post_t<cff>(B, B.U32) : gm_post_t<c64>(B, B.U); }
 
 void launch_xupdate(const c64* x, const c64* U, size_t ldu, const c64* coef, const c64* ypad,
                     int k, size_t N, c64* out, cudaStream_t st) {

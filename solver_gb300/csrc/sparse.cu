@@ -10,6 +10,9 @@
 //   y1 = invZ.*(Y1 - A*M),  y2 = invP.*(Y2 + Gamma'*M),  y3 = M.
 // A has two entries per edge (-1 at n1, +1 at n2); Gamma one entry per surface.
 // Node-side sums use host-built CSR lists (node -> edges, node -> surfaces).
+#include <algorithm>
+#include <mutex>
+
 #include "ctx.hpp"
 
 namespace peec {
@@ -17,7 +20,8 @@ namespace peec {
 __global__ void k_edge_rows(const c64* __restrict__ I, const c64* __restrict__ Phi,
                             const c64* __restrict__ LpI, const c64* __restrict__ DZ,
                             const int32_t* __restrict__ n1, const int32_t* __restrict__ n2,
-                            double w, int m, c64* Y1, c64* U1) {
+                            const double* __restrict__ wp, int m, c64* Y1, c64* U1) {
+  const double w = *wp;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m; e += gridDim.x * blockDim.x) {
     const c64 l = LpI[e], d = DZ[e], i = I[e];
     const c64 a = Phi[n2[e]] - Phi[n1[e]];
@@ -48,7 +52,8 @@ __global__ void k_node_rows(const c64* __restrict__ I, const c64* __restrict__ Q
                             const int32_t* __restrict__ ne_idx, const int32_t* __restrict__ ns_ptr,
                             const int32_t* __restrict__ ns_idx, const int32_t* __restrict__ yle_ptr,
                             const int32_t* __restrict__ yle_col, const c64* __restrict__ yle_val,
-                            double w, int n, c64* t) {
+                            const double* __restrict__ wp, int n, c64* t) {
+  const double w = *wp;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     c64 au = mk<double>(0, 0), ai = mk<double>(0, 0);
     for (int p = ne_ptr[v]; p < ne_ptr[v + 1]; ++p) {
@@ -140,62 +145,85 @@ __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// ctl[0] epoch, ctl[1] row claim counter, ctl[2] error flag, ctl[3] component claim counter
+// ctl[0] epoch, ctl[1] row claim counter, ctl[2] error flag, ctl[3] unused
 __global__ void k_sptrsv_begin(int* ctl) {
   ctl[0] += 1;
   ctl[1] = 0;
   ctl[3] = 0;
 }
 
-// One warp per small component (rows linked by factor entries, at most SF_COMP_MAX):
-// L levels then U levels of the component, rows of a level spread over the lanes,
-// __syncwarp between levels, the component's values in shared memory. Per row the
-// arithmetic is the same as in k_sptrsv (right-hand side, entries subtracted in row
-// order, times the inverse diagonal). The U pass works in place: a U row reads its own
-// L value and the U values of rows of earlier U levels.
-__global__ void __launch_bounds__(SFC_TPB) k_sptrsv_comp(CompPlan C, SfTri L, SfTri U,
-                                                         const c64* __restrict__ b,
-                                                         const int32_t* __restrict__ g_in,
-                                                         const double* __restrict__ rs, c64* z,
-                                                         int* ctl) {
-  __shared__ c64 xs_all[SFC_TPB / 32][SF_COMP_MAX];
+// One warp per group (GrpPlan): components of the factors, several small ones packed
+// together or one large one. The warp first brings everything the group's solve reads
+// into its slice of shared memory -- per row the right-hand side (gathered through Pr
+// and scaled by Rs), both inverse diagonals, its L and U entries with their columns as
+// positions in the group -- with every row's loads independent of the others', so the
+// whole group costs a few round trips to memory. Then the L levels, the U levels (in
+// place: a U row reads its own L value and the U values of rows of earlier U levels),
+// __syncwarp between levels, and the results go out to z. Per row the arithmetic is that
+// of k_sptrsv (right-hand side, entries subtracted in row order, times the inverse
+// diagonal). R, E: the shared-memory capacity of a warp's slice (rows, entries).
+__global__ void k_sptrsv_grp(GrpPlan P, int g0, int g1, int R, int E, SfTri L, SfTri U,
+                             const c64* __restrict__ b, const double* __restrict__ rs, c64* z) {
+  extern __shared__ __align__(16) unsigned char grp_sm[];
   const int lane = threadIdx.x & 31;
-  c64* xs = xs_all[threadIdx.x >> 5];
-  for (;;) {
-    int ci = 0;
-    if (lane == 0) ci = atomicAdd(ctl + 3, 1);
-    ci = __shfl_sync(0xffffffffu, ci, 0);
-    if (ci >= C.n) break;
-    const int base = C.off[ci], end = C.off[ci + 1];
-    int prev = base;
-    for (int s = C.segLoff[ci]; s < C.segLoff[ci + 1]; ++s) {
-      const int se = C.segL[s];
+  const int wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  unsigned char* base = grp_sm + (size_t)wib * grp_smem(R, E);
+  c64* xs = reinterpret_cast<c64*>(base);
+  c64* dl = xs + R;
+  c64* du = dl + R;
+  c64* ev = du + R;
+  short4* meta = reinterpret_cast<short4*>(ev + E);  // (eL, nL, eU, nU)
+  int16_t* ec = reinterpret_cast<int16_t*>(meta + R);
+  int16_t* uqs = ec + E;
+  int32_t* segs = reinterpret_cast<int32_t*>(
+      (reinterpret_cast<uintptr_t>(uqs + R) + 3) & ~(uintptr_t)3);
+  for (int g = g0 + blockIdx.x * wpb + wib; g < g1; g += gridDim.x * wpb) {
+    const int q0 = P.goff[g], nr = P.goff[g + 1] - q0;
+    const int s0 = P.segoff[g], ns = P.segoff[g + 1] - s0, nsl = P.nsegL[g];
+    for (int q = lane; q < nr; q += 32) {
+      const GrpRow pr = P.rows[q0 + q];
+      xs[q] = rs ? cscale(b[pr.j], rs[pr.j]) : b[pr.j];
+      dl[q] = L.dinv[pr.r];
+      du[q] = U.dinv[pr.r];
+      meta[q] = make_short4(pr.eL, pr.nL, pr.eU, pr.nU);
+      for (int t = 0; t < pr.nL; ++t) {
+        ev[pr.eL + t] = L.val[pr.pL + t];
+        ec[pr.eL + t] = P.lcolL[pr.pL + t];
+      }
+      for (int t = 0; t < pr.nU; ++t) {
+        ev[pr.eU + t] = U.val[pr.pU + t];
+        ec[pr.eU + t] = P.lcolU[pr.pU + t];
+      }
+      uqs[q] = P.uq[q0 + q];
+    }
+    for (int t = lane; t < ns; t += 32) segs[t] = P.seg[s0 + t];
+    __syncwarp();
+    int prev = 0;
+    for (int s = 0; s < nsl; ++s) {
+      const int se = segs[s];
       for (int q = prev + lane; q < se; q += 32) {
-        const int r = C.rowsL[q];
-        const int j = g_in[r];
-        c64 acc = rs ? cscale(b[j], rs[j]) : b[j];
-        for (int p = L.ptr[r]; p < L.ptr[r + 1]; ++p)
-          acc = acc - L.val[p] * xs[C.local[L.col[p]]];
-        xs[q - base] = acc * L.dinv[r];
+        const short4 m = meta[q];
+        c64 acc = xs[q];
+        for (int t = 0; t < m.y; ++t) acc = acc - ev[m.x + t] * xs[ec[m.x + t]];
+        xs[q] = acc * dl[q];
       }
       __syncwarp();
       prev = se;
     }
-    prev = base;
-    for (int s = C.segUoff[ci]; s < C.segUoff[ci + 1]; ++s) {
-      const int se = C.segU[s];
-      for (int q = prev + lane; q < se; q += 32) {
-        const int r = C.rowsU[q];
-        const int lr = C.local[r];
-        c64 acc = xs[lr];
-        for (int p = U.ptr[r]; p < U.ptr[r + 1]; ++p)
-          acc = acc - U.val[p] * xs[C.local[U.col[p]]];
-        xs[lr] = acc * U.dinv[r];
+    prev = 0;
+    for (int s = nsl; s < ns; ++s) {
+      const int se = segs[s];
+      for (int t = prev + lane; t < se; t += 32) {
+        const int q = uqs[t];
+        const short4 m = meta[q];
+        c64 acc = xs[q];
+        for (int e = 0; e < m.w; ++e) acc = acc - ev[m.z + e] * xs[ec[m.z + e]];
+        xs[q] = acc * du[q];
       }
       __syncwarp();
       prev = se;
     }
-    for (int q = base + lane; q < end; q += 32) z[C.rowsL[q]] = xs[q - base];
+    for (int q = lane; q < nr; q += 32) z[P.rows[q0 + q].r] = xs[q];
     __syncwarp();
   }
 }
@@ -291,8 +319,8 @@ static inline unsigned grid_for(long long n, int tpb = 256) {
 }
 
 void launch_edge_rows(const c64* I, const c64* Phi, const c64* LpI, const c64* DZ,
-                      const int32_t* n1, const int32_t* n2, double w, int m, c64* Y1, c64* U1,
-                      cudaStream_t st) {
+                      const int32_t* n1, const int32_t* n2, const double* w, int m, c64* Y1,
+                      c64* U1, cudaStream_t st) {
   if (m > 0) k_edge_rows<<<grid_for(m), 256, 0, st>>>(I, Phi, LpI, DZ, n1, n2, w, m, Y1, U1);
 }
 void launch_surf_rows(const c64* PQ, const c64* Phi, const int32_t* snode, const double* invP,
@@ -302,7 +330,7 @@ void launch_surf_rows(const c64* PQ, const c64* Phi, const int32_t* snode, const
 void launch_node_rows(const c64* I, const c64* Q, const c64* Phi, const c64* U1, const c64* U2,
                       const int32_t* ne_ptr, const int32_t* ne_idx, const int32_t* ns_ptr,
                       const int32_t* ns_idx, const int32_t* yle_ptr, const int32_t* yle_col,
-                      const c64* yle_val, double w, int n, c64* t, cudaStream_t st) {
+                      const c64* yle_val, const double* w, int n, c64* t, cudaStream_t st) {
   k_node_rows<<<grid_for(n), 256, 0, st>>>(I, Q, Phi, U1, U2, ne_ptr, ne_idx, ns_ptr, ns_idx,
                                            yle_ptr, yle_col, yle_val, w, n, t);
 }
@@ -319,20 +347,45 @@ void launch_perm_gather(const c64* b, const int32_t* perm, const double* rs, int
 void launch_perm_scatter(const c64* z, const int32_t* perm, int n, c64* out, cudaStream_t st) {
   k_perm_scatter<<<grid_for(n), 256, 0, st>>>(z, perm, n, out);
 }
+// Raises the shared memory the group kernel may be launched with on the current device
+// to at least smem_bytes (the default limit is 48 KB per block). The limit belongs to the
+// kernel, not to a context, so it only ever grows: contexts of other geometries on the
+// same device keep what their plans need.
+int sptrsv_grp_prepare(size_t smem_bytes) {
+  static std::mutex mu;
+  static size_t granted[256] = {};
+  int dev = 0;
+  PEEC_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) return fail_cuda(cudaErrorInvalidDevice, "device", __FILE__, __LINE__);
+  std::lock_guard<std::mutex> lock(mu);
+  // set every time (a re-created context starts from the default again)
+  const size_t v = std::max(smem_bytes, granted[dev]);
+  PEEC_CUDA_TRY(cudaFuncSetAttribute(k_sptrsv_grp, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)v));
+  granted[dev] = v;
+  return 0;
+}
+
 // returns the number of kernels launched
-int launch_sptrsv(const CompPlan& C, const int32_t* ord, int nL, int total, const SfTri& L,
+int launch_sptrsv(const GrpPlan& P, const int32_t* ord, int nL, int total, const SfTri& L,
                   const SfTri& U, const c64* b, const int32_t* g_in, const double* rs, c64* y,
                   c64* z, int* ctl, cudaStream_t st) {
-  int launches = 1;
-  k_sptrsv_begin<<<1, 1, 0, st>>>(ctl);
-  if (C.n > 0) {
-    int cb = (C.n + SFC_TPB / 32 - 1) / (SFC_TPB / 32);
-    if (cb > 152 * 8) cb = 152 * 8;
-    k_sptrsv_comp<<<cb, SFC_TPB, 0, st>>>(C, L, U, b, g_in, rs, z, ctl);
+  int launches = 0;
+  if (P.nbig > 0) {  // one warp per large component, shared memory sized for the largest
+    k_sptrsv_grp<<<P.nbig, 32, grp_smem(P.rb, P.eb), st>>>(P, 0, P.nbig, P.rb, P.eb, L, U, b, rs,
+                                                             z);
+    ++launches;
+  }
+  if (P.ngroups > P.nbig) {
+    const int nsmall = P.ngroups - P.nbig;
+    const int blocks = (nsmall + SF_GRP_WARPS - 1) / SF_GRP_WARPS;
+    k_sptrsv_grp<<<blocks, 32 * SF_GRP_WARPS, SF_GRP_WARPS * grp_smem(32, SF_GRP_E), st>>>(
+        P, P.nbig, P.ngroups, 32, SF_GRP_E, L, U, b, rs, z);
     ++launches;
   }
   if (total <= 0) return launches;
-  ++launches;
+  k_sptrsv_begin<<<1, 1, 0, st>>>(ctl);
+  launches += 2;
   // at most two CTAs (eight warps) per SM: warps that wait on earlier rows take issue
   // slots from kernels of other streams, and more warps do not shorten the chain of
   // levels (the widest level at 128x128x64 is about 1,400 warp batches)

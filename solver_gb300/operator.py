@@ -58,6 +58,11 @@ def _surf_cells(expansions, ns):
 class GpuOperator:
     """Device-resident PEEC operator for one geometry."""
 
+    # settings every new context starts with (process-wide; the library's defaults): the
+    # device-resident GMRES loop, and the largest LU component solved per warp group
+    DEVICE_LOOP = True
+    LU_COMPONENT_MAX = 512
+
     def __init__(self, incidence_selection, expansions, diagP, grid=None, device=0):
         self.L = _lib.load()
         self._init_args = (incidence_selection, expansions, diagP, grid, device)
@@ -67,6 +72,10 @@ class GpuOperator:
         if rc != 0:
             raise _lib.PeecError(rc, self.L.peec_last_error(None).decode())
         self.h = h
+        if not GpuOperator.DEVICE_LOOP:
+            self.set_device_loop(False)
+        if GpuOperator.LU_COMPONENT_MAX != 512:
+            self.set_lu_component_max(GpuOperator.LU_COMPONENT_MAX)
         A = incidence_selection["A"].tocsr()
         Gamma = incidence_selection["Gamma"].tocsc()
         self.m, self.n = A.shape
@@ -229,6 +238,10 @@ class GpuOperator:
         if self._rcc is not None:
             rows, o, (sx, sy, sz) = self._rcc
             c.set_rows_rcc(rows, o, sx, sy, sz)
+        # the same FP32 z-pass forms as this context (the tuner's timings can differ by a
+        # few percent between contexts), so that every lane computes the same numbers
+        t = self.zpass_tuning()
+        c.set_zpass_forms(t["face"], t["edge"], t["edge_plan"])
         return c
 
     # -- frequency ------------------------------------------------------------------
@@ -402,6 +415,17 @@ class GpuOperator:
             return x, 99, 0.0, [it[0], it[1]], np.zeros(1)
         _lib.check(self.h, rc)
         return x, flag.value, relres.value, [it[0], it[1]], resvec[:nres.value].copy()
+
+    def set_device_loop(self, on: bool):
+        """GMRES iterations in a device-resident loop (default) or one host round trip per
+        iteration (the same kernels and results)."""
+        _lib.check(self.h, self.L.peec_set_device_loop(self.h, 1 if on else 0))
+
+    def device_loop_stats(self):
+        """(graph launches, GMRES iterations they ran) since the context was created."""
+        a, b = ctypes.c_int64(0), ctypes.c_int64(0)
+        _lib.check(self.h, self.L.peec_device_loop_stats(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return int(a.value), int(b.value)
 
     def set_lu_component_max(self, max_rows):
         """Rows of LU components up to max_rows (<= 512) are solved one component per

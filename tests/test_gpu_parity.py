@@ -123,18 +123,18 @@ def test_matvec_ff(case):
 
 
 def test_lu_solve_paths(case):
-    """The per-warp component solves and the synchronisation-free global scheme do the
+    """The per-warp group solves and the synchronisation-free global scheme do the
     same arithmetic per row (up to where the compiler fuses multiply-adds), so the
     operator applications agree to rounding, and both match the oracle."""
     w, fs = _freq(case)
     rng = np.random.default_rng(6)
     x = rng.standard_normal(case["op"].N) + 1j * rng.standard_normal(case["op"].N)
-    y_glob = case["op"].matvec(x, 0)
-    case["op"].set_lu_component_max(512)
+    y_comp = case["op"].matvec(x, 0)  # the default: every component per warp group
+    case["op"].set_lu_component_max(0)
     try:
-        y_comp = case["op"].matvec(x, 0)
+        y_glob = case["op"].matvec(x, 0)
     finally:
-        case["op"].set_lu_component_max(0)
+        case["op"].set_lu_component_max(512)
     y_ref = _oracle_mv(case, w, fs)(x)
     noise = _rel(_single_solve_oracle(case, w, fs)(x), y_ref)
     assert _rel(y_comp, y_glob) < max(1e-11, 2 * noise)

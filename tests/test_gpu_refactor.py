@@ -141,3 +141,38 @@ def test_refactor_rejects_another_yle_pattern(case):
     from solver_gb300 import _lib
     with pytest.raises(_lib.PeecError):
         c["op"].set_frequency_refactor(w0, fs0["DZ"], Y.tocsr())
+
+
+def test_graphs_kept_across_device_factorised_frequencies(case):
+    """A frequency change with SS factorised on the device writes DZ, Yle, w and the
+    factors in place and keeps the context's captured graphs (operator applications and
+    the device GMRES loop). Solves through kept graphs equal, bit for bit, those of a
+    context that captures its graphs afresh at that frequency."""
+    c = case
+    w0, fs0 = _setup(c, 1e9)
+    pn = np.asarray(c["ports"]["port_nodes"], dtype=np.int64).reshape(-1, 2)
+    tn0 = c["op"].port_rhs(pn[0, 0], pn[0, 1], c["esc"]["Is"])
+    c["op"].solve_mixed(tn0, None, 1e-8)
+    c["op"].gmres(tn0, None, 1e-8, 60)  # graphs of both kinds captured at 1 GHz
+    w1, fs1 = _state(c, 3e8)
+    other = c["op"].clone()
+    try:
+        other.set_frequency(w0, fs0["DZ"], fs0["Yle"], fs0["lu"])
+        other.enable_refactor(fs0["Yle"])
+        for op in (c["op"], other):
+            op.set_frequency_refactor(w1, fs1["DZ"], fs1["Yle"])
+        tn1 = c["op"].port_rhs(pn[0, 0], pn[0, 1], c["esc"]["Is"])
+        assert np.array_equal(tn1, other.port_rhs(pn[0, 0], pn[0, 1], c["esc"]["Is"]))
+        g0 = c["op"].device_loop_stats()[0]
+        xa = c["op"].solve_mixed(tn1, None, 1e-8)
+        ya = c["op"].gmres(tn1, None, 1e-8, 60)
+        assert c["op"].device_loop_stats()[0] > g0
+        xb = other.solve_mixed(tn1, None, 1e-8)
+        yb = other.gmres(tn1, None, 1e-8, 60)
+        assert xa[1:] == xb[1:] and np.array_equal(xa[0], xb[0])
+        assert (ya[1], list(ya[3])) == (yb[1], list(yb[3])) and np.array_equal(ya[0], yb[0])
+        # and the kept graphs solve the new frequency's system
+        r = tn1 - _mv(c, w1, fs1)(xa[0])
+        assert np.linalg.norm(r) <= 1e-6 * np.linalg.norm(tn1)
+    finally:
+        other.close()
