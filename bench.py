@@ -63,6 +63,8 @@ def parse():
                     help="run the adjoint-gradient configuration instead")
     ap.add_argument("--batched-sweep", action="store_true",
                     help="run the batched multi-geometry sweep configuration instead")
+    ap.add_argument("--ris", action="store_true",
+                    help="run the dense RIS solver configuration instead")
     ap.add_argument("--reuse-fills", action="store_true",
                     help="batched sweep: geometries on the same lattice share one fill "
                          "(fill_cache.RowCache)")
@@ -606,6 +608,154 @@ def loaded_native_libs():
     return [os.path.relpath(p_, root) for p_ in libs]
 
 
+def ris_problem(grid=(48, 48, 16), seed=3):
+    """A dense RIS workload on a voxel mesh: the mesh's incidence and ports; dense Lp blocks
+    and P with the mesh's self terms on the diagonal and off-diagonal couplings
+    sqrt(d_i d_j) exp(-r_ij / 1.5 cells) between edge / surface centres (positive
+    definite, like the partial inductances and potentials the reference fills); R, Cd
+    and the dielectric edges from the mesh's diagonals. Seeded and synthetic."""
+    from solver_gb300 import configs, mesher
+    from solver_gb300.operator import _edge_cells, _surf_cells, row_dims
+    req = configs.random_mixed(tuple(grid), s=5e-5, p=0.3, seed=seed, nports=4,
+                               freqs=[1e8, 1e9, 3e9, 1e10], tol=1e-8)
+    out, freqs, settings, z0, g = mesher.parse_request(req)
+    esc, inc, cc, diag, exp, ports, le, li, Zs = out
+    Nx, Ny, Nz = g
+    mx, my, mz = inc["mx"], inc["my"], inc["mz"]
+    ns = inc["Gamma"].shape[1]
+    dims = row_dims(Nx, Ny, Nz)
+
+    def coords(cell, d, shift):
+        cell = np.asarray(cell, dtype=np.int64)
+        ix, iy, iz = cell % d[0], (cell // d[0]) % d[1], cell // (d[0] * d[1])
+        return np.stack([ix + shift[0], iy + shift[1], iz + shift[2]], axis=1).astype(np.float64)
+
+    ecell = _edge_cells(exp, mx, my, mz)
+    epos = [coords(ecell[:mx], dims["Lpx"], (1.0, 0.5, 0.5)),
+            coords(ecell[mx:mx + my], dims["Lpy"], (0.5, 1.0, 0.5)),
+            coords(ecell[mx + my:], dims["Lpz"], (0.5, 0.5, 1.0))]
+    fam, scell = _surf_cells(exp, ns)
+    spos = np.zeros((ns, 3))
+    for f, (key, sh) in enumerate((("p12_se", (0.5, 0.0, 0.5)), ("p34_se", (0.0, 0.5, 0.5)),
+                                   ("p56_se", (0.5, 0.5, 0.0)))):
+        sel = fam == f
+        spos[sel] = coords(scell[sel], dims[key], sh)
+
+    def kernel(pos, d, out):
+        sq = np.sqrt(d)
+        for a in range(0, pos.shape[0], 2048):
+            r = np.sqrt(((pos[a:a + 2048, None, :] - pos[None, :, :]) ** 2).sum(-1))
+            out[a:a + 2048] = np.exp(-r / 1.5) * sq[a:a + 2048, None] * sq[None, :]
+        return out
+
+    dLp = np.real(np.asarray(diag["Lp"])).ravel()
+    offs = [0, mx, mx + my, mx + my + mz]
+    Lp = {}
+    for k, key in enumerate(("Lp_x", "Lp_y", "Lp_z")):
+        n_k = offs[k + 1] - offs[k]
+        Lp[key] = kernel(epos[k], dLp[offs[k]:offs[k + 1]], np.empty((n_k, n_k), order="F"))
+    dP = np.real(np.asarray(diag["P"])).ravel()
+    P = {"P": kernel(spos, dP, np.empty((ns, ns), order="F"))}
+    R = np.real(np.asarray(diag["R"])).sum(axis=1)
+    Cd = np.real(np.asarray(diag["Cd"]))
+    has = (Cd > 0).any(axis=1)
+    Cd_eff = np.zeros(R.size)
+    Cd_eff[has] = 1.0 / np.where(Cd[has] > 0, 1.0 / np.where(Cd[has] > 0, Cd[has], 1.0),
+                                 0.0).sum(axis=1)
+    volumi = {"R": R, "Cd": Cd_eff, "indici_dielettrici": np.flatnonzero((R == 0) & (Cd_eff > 0)),
+              "Zs_part": np.zeros(R.size)}
+    return dict(esc=esc, inc=inc, ports=ports, Lp=Lp, P=P, volumi=volumi, freqs=list(freqs),
+                grid=list(g))
+
+
+def run_ris(args):
+    """The dense RIS configuration: the dense operator's FP32 and FP64 applications against
+    the HBM roofline, and the RIS frequency x port loop (4 ports x 4 frequencies, 1e-8) in
+    FP64 and mixed precision with SS factorised on the GPU; beside it the oracle's RIS
+    operator and GMRES on the host cores for one port solve. One JSON line."""
+    import torch
+    from solver_gb300 import ris
+    t0 = time.perf_counter()
+    P = ris_problem(tuple(args.grid) if args.grid else (48, 48, 16))
+    setup_s = time.perf_counter() - t0
+    op = ris.DenseOperator(P["inc"], P["Lp"], P["P"])
+    mx, my, mz = P["inc"]["mx"], P["inc"]["my"], P["inc"]["mz"]
+    ns = P["inc"]["Gamma"].shape[1]
+    entries = mx * mx + my * my + mz * mz + ns * ns
+    gs = {"Inner_Iter": 300, "tol": [1e-8] * len(P["freqs"])}
+    run = lambda mode: ris.iter_solver_QS_S_type(P["freqs"], P["esc"], P["inc"], P["P"], P["Lp"],
+                                                 P["ports"], {}, gs, P["volumi"], False, 1, 50.0,
+                                                 mode=mode, op=op, lu="device")
+    run("mixed")  # warm-up: graphs, the z tuner's absence, module load
+    w = 2 * np.pi * P["freqs"][0] * P["esc"]["freq"]
+    st = ris.RisState(w, P["esc"], P["inc"], op.diag_Lp, np.diag(P["P"]["P"]), P["ports"], {},
+                      P["volumi"], False, 50.0)
+    op.set_frequency(w, st.DZ, st.Yle, st.lu)
+    prof32 = op.profile_matvec(1, 20)
+    prof64 = op.profile_matvec(0, 5)
+    peak, peak_kind = load_peaks()
+    res = {}
+    clocks = Clocks(0)
+    for mode in ("fp64", "mixed"):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        out = run(mode)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        res[mode] = {"port_solves_per_s": len(out["info"]) / dt, "wall_s": dt,
+                     "flags": sorted({r["flag"] for r in out["info"]}),
+                     "iters_mean": float(np.mean([r["niter"] for r in out["info"]]))}
+        res[mode]["S"] = out["S"]
+    clk = clocks.stop()
+    zerr = float(np.max(np.abs(res["mixed"]["S"] - res["fp64"]["S"])) /
+                 np.max(np.abs(res["fp64"]["S"])))
+    for mode in res:
+        del res[mode]["S"]
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import peec_oracle as O
+        from oracle import ris_ref as RO
+        stc = RO.frequency_setup(w, P["esc"], P["inc"], P["P"], P["Lp"], P["ports"], {},
+                                 P["volumi"], False, 50.0)
+        mv = lambda x: RO.ComputeMatrixVectorRis(x, w, P["inc"], stc["P"], stc["Lp"],
+                                                 stc["Z_self"], stc["Yle"], stc["invZ"],
+                                                 stc["invP"], stc["F"])
+        pn = np.asarray(P["ports"]["port_nodes"]).reshape(-1, 2)
+        isv = np.zeros(op.n)
+        isv[pn[0, 0]], isv[pn[0, 1]] = P["esc"]["Is"], -P["esc"]["Is"]
+        tn = RO.precond_3_3_Kt_S(stc["F"], stc["invZ"], stc["invP"], P["inc"]["A"],
+                                 P["inc"]["Gamma"], op.m, ns, isv)
+        t = time.perf_counter()
+        _x, fl, _rr, it, rv = O.gmres_custom(tn, False, 1e-8, 300, None, mv)
+        dt = time.perf_counter() - t
+        cpu = {"value": 1.0 / dt, "unit": "port solves/s", "cores": os.cpu_count() or 1,
+               "kind": "port", "sample": f"one FP64 port solve at {P['freqs'][0]:.3g} Hz from "
+               f"a zero guess ({len(rv) - 1} GMRES iterations, flag {fl}); the oracle's RIS "
+               "operator with numpy/BLAS dense products on every host core"}
+    ms32, ms64 = prof32["z"], prof64["z"]
+    op.close()
+    print(json.dumps({
+        "metric": "dense RIS solver: port solves/s at 1e-8 (4 ports x 4 frequencies); dense "
+                  "operator GB/s", "value": res["mixed"]["port_solves_per_s"],
+        "unit": "port solves/s", "higher_is_better": True, "dtype": "f32 dense products, "
+        "float-float refinement residuals over FP64 products", "data": "synthetic",
+        "config": {"workload": f"RIS dense operator on random_mixed {P['grid']} (Bernoulli 0.3,"
+                   f" seed 3): m = {op.m}, ns = {ns}, n = {op.n}; Lp blocks {mx}/{my}/{mz}, "
+                   f"P {ns} x {ns}", "entries": int(entries), "lu": "device",
+                   "setup_s": setup_s},
+        "fp64": res["fp64"], "mixed": res["mixed"], "mixed_vs_fp64_S_rel": zerr,
+        "dense_products": {"fp32_ms": ms32, "fp64_ms": ms64,
+                           "fp32_gbs": 4.0 * entries / (ms32 * 1e-3) / 1e9,
+                           "fp64_gbs": 8.0 * entries / (ms64 * 1e-3) / 1e9,
+                           "sparse_ms": prof32["sparse"]},
+        "roofline": {"bound": "hbm", "kernel": "k_dense_gemv<float> (4 blocks)",
+                     "achieved": 4.0 * entries / (ms32 * 1e-3) / 1e9, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": 4.0 * entries / (ms32 * 1e-3) / 1e9 / peak,
+                     "bytes_per_application": int(4 * entries)},
+        "cpu_baseline": cpu, "clocks": clk}), flush=True)
+
+
 def run_batched_sweep(args):
     """The batched-sweep configuration: 12 uneven copper grids (32x32x16 .. 96x96x48),
     64 frequencies each, one port, mixed precision to 1e-8, geometries swept concurrently
@@ -769,6 +919,9 @@ def main():
         return
     if args.batched_sweep:
         run_batched_sweep(args)
+        return
+    if args.ris:
+        run_ris(args)
         return
     if args.small_configs:
         run_small_configs(args)

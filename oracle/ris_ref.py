@@ -48,12 +48,15 @@ def ComputeMatrixVectorRis(x, w, incidence_selection, P_data, Lp_data, Z_self, Y
     x = np.asarray(x, dtype=np.complex128).ravel()
     I, Q, Phi = x[:m], x[m:m + ns], x[m + ns:]
     mx, my, mz = incidence_selection["mx"], incidence_selection["my"], incidence_selection["mz"]
+    # real matrices times complex vectors as two real products (what the reference's
+    # real-by-complex multiplication amounts to)
+    mul = lambda M, v: prod_real_complex(M, v) if np.isrealobj(M) else M @ v
     Y1 = np.zeros(m, dtype=np.complex128)
-    Y1[:mx] = Lp_data["Lp_x"] @ I[:mx]
-    Y1[mx:mx + my] = Lp_data["Lp_y"] @ I[mx:mx + my]
-    Y1[mx + my:mx + my + mz] = Lp_data["Lp_z"] @ I[mx + my:mx + my + mz]
+    Y1[:mx] = mul(Lp_data["Lp_x"], I[:mx])
+    Y1[mx:mx + my] = mul(Lp_data["Lp_y"], I[mx:mx + my])
+    Y1[mx + my:mx + my + mz] = mul(Lp_data["Lp_z"], I[mx + my:mx + my + mz])
     Y1 = 1j * w * Y1 + np.asarray(Z_self).ravel() * I + A @ Phi
-    Y2 = P_data["P"] @ Q - Gamma.T @ Phi
+    Y2 = mul(P_data["P"], Q) - Gamma.T @ Phi
     Y3 = -(A.T @ I) + Yle @ Phi + 1j * w * (Gamma @ Q)
     return precond_3_3_vector(F, invZ, invP, A, Gamma, w, Y1, Y2, Y3)
 
@@ -63,7 +66,7 @@ def precond_3_3_vector(F, invZ, invP, A, Gamma, w, X1, X2, X3):
     and imaginary parts."""
     n1, n2 = X1.size, X2.size
     Y = np.zeros(n1 + n2 + X3.size, dtype=np.complex128)
-    M1 = prod_real_complex(invZ, X1) if np.isrealobj(invZ.data) else invZ @ X1
+    M1 = prod_real_complex(invZ, X1)
     M2 = F(prod_real_complex(A.T, M1))
     M3 = prod_real_complex(invP, X2)
     M4 = F(prod_real_complex(Gamma, M3))
@@ -84,12 +87,81 @@ def precond_3_3_Kt_S(F, invZ, invP, A, Gamma, m, ns, X3):
     return np.concatenate([-(invZ @ (A @ M5)), invP @ (Gamma.T @ M5), M5])
 
 
+def lumped_admittance_S(typ, R, L, C, w):
+    """get_lumped_elements_admittance_S (build_Yle_S.jl:70-151), statement by statement
+    (numpy scalars give Julia's IEEE results for divisions by zero). Its type-2 case differs
+    from the voxel path's in the fifth network: 1/(1/(jwC)) + jwC."""
+    R, L, C = np.float64(R), np.float64(L), np.float64(C)
+    jw = np.complex128(1j * w)
+
+    def bad(v):
+        return np.isnan(v) or np.isinf(v) or abs(v) < 1e-16
+
+    with np.errstate(all="ignore"):
+        y = np.complex128(0.0)
+        if typ == 1:
+            z = R + jw * L + 1 / (jw * C)
+            if np.isnan(z) or np.isinf(z) or abs(z) < 1e-16:
+                z = R + jw * L
+            y = 1 / z
+        elif typ == 2:
+            y = 1 / (R + jw * L) + jw * C
+            if bad(y):
+                y = 1 / R + jw * C
+            if bad(y):
+                y = 1 / (R + jw * L)
+            if bad(y):
+                y = 1 / R
+            if bad(y):
+                y = 1 / (1 / (jw * C)) + jw * C
+            if bad(y):
+                y = jw * C
+        elif typ == 3:
+            y = 1 / (R + 1 / (jw * C)) + 1 / (jw * L)
+            if bad(y):
+                y = 1 / (R + 1 / (jw * C))
+            if bad(y):
+                y = 1 / R + 1 / (jw * L)
+            if bad(y):
+                y = 1 / R
+            if bad(y):
+                y = 1 / (1 / (jw * C)) + 1 / (jw * L)
+            if bad(y):
+                y = 1 / (jw * L)
+            if bad(y):
+                y = 1 / (1 / (jw * C))
+        elif typ == 4:
+            y = 1 / R + jw * C + 1 / (jw * L)
+            if bad(y):
+                y = 1 / R + jw * C
+            if bad(y):
+                y = jw * C + 1 / (jw * L)
+            if bad(y):
+                y = jw * C
+        elif typ == 5:
+            y = 1 / R + 1 / (jw * L + 1 / (jw * C))
+            if bad(y):
+                y = 1 / R + 1 / (1 / (jw * C))
+            if bad(y):
+                y = 1 / R + 1 / (jw * L)
+            if bad(y):
+                y = 1 / R
+            if bad(y):
+                y = 1 / (jw * L + 1 / (jw * C))
+            if bad(y):
+                y = 1 / (jw * L)
+            if bad(y):
+                y = 1 / (1 / (jw * C))
+        if np.isnan(y) or np.isinf(y):
+            y = 0.0
+        return complex(y)
+
+
 def build_Yle_S(lumped_elements, grounding_nodes, ports, escalings, n, w, val_chiusura):
-    """build_Yle_S.jl:1-68: lumped elements (the admittances of get_lumped_elements_
-    admittance_S, the same case tree as the voxel path's), port closures 1/R and
-    grounding nodes 1e-12, summed per (row, column). The reference keeps the sums in a
-    Float64 dictionary, which holds only real admittances (resistive elements and the port
-    closures); complex ones are kept complex here."""
+    """build_Yle_S.jl:1-68: lumped elements, port closures 1/R and grounding nodes 1e-12,
+    summed per (row, column). The reference keeps the sums in a Float64 dictionary, which
+    holds only real admittances (resistive elements and the port closures); complex ones
+    are kept complex here."""
     acc = {}
 
     def add(r, c, v):
@@ -98,7 +170,7 @@ def build_Yle_S(lumped_elements, grounding_nodes, ports, escalings, n, w, val_ch
     le = lumped_elements
     for k in range(len(le.get("le_nodes", []))):
         n1, n2 = int(le["le_nodes"][k][0]), int(le["le_nodes"][k][1])
-        y = O.lumped_admittance(int(le["type"][k]), le["R"][k], le["L"][k], le["C"][k], w)
+        y = lumped_admittance_S(int(le["type"][k]), le["R"][k], le["L"][k], le["C"][k], w)
         add(n1, n1, y)
         add(n2, n2, y)
         add(n1, n2, -y)

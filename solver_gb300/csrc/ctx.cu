@@ -67,7 +67,8 @@ void launch_final_rows(const c64*, const c64*, const c64*, const c64*, const int
                        cudaStream_t);
 void launch_perm_gather(const c64*, const int32_t*, const double*, int, c64*, cudaStream_t);
 int sptrsv_grp_prepare(size_t smem_bytes);
-int launch_sptrsv(const GrpPlan&, const int32_t*, int, int, const SfTri&, const SfTri&,
+int launch_sptrsv(const GrpPlan&, cudaStream_t, cudaEvent_t, cudaEvent_t, const int32_t*, int,
+                  int, const SfTri&, const SfTri&,
                   const c64*, const int32_t*, const double*, c64*, c64*, int*, cudaStream_t);
 int red_blocks(size_t N);
 int launch_multidot(const c64*, size_t, const c64*, size_t, int, c64*, c64*, cudaStream_t);
@@ -121,6 +122,10 @@ struct LevelTri {  // triangular factor without its diagonal (CSR) and its level
 struct peec_ctx {
   int dev = 0;
   cudaStream_t st = nullptr;
+  // a second stream for the LU solve's large groups (forked from st and joined back with
+  // the two events, so the packed groups run beside them)
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   std::string err;
   int64_t launches = 0;
@@ -368,8 +373,12 @@ static int peec_ctx_create_body(peec_ctx** out, int device) {
     return rc;
   };
   if (cudaSetDevice(device) != cudaSuccess) return fail(fail_cuda(cudaGetLastError(), "cudaSetDevice", __FILE__, __LINE__));
-  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking) != cudaSuccess)
     return fail(fail_cuda(cudaGetLastError(), "cudaStreamCreate", __FILE__, __LINE__));
+  if (cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess)
+    return fail(fail_cuda(cudaGetLastError(), "cudaEventCreate", __FILE__, __LINE__));
   for (auto& ev : ctx->ev) cudaEventCreate(&ev);
   // twiddle master table exp(-2 pi i e / twmax), long-double accurate
   ctx->twmax = 8192;
@@ -479,6 +488,12 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   for (auto e : ctx->pev) cudaEventDestroy(e);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->st2) {
+    cudaStreamSynchronize(ctx->st2);
+    cudaStreamDestroy(ctx->st2);
+  }
   if (ctx->st) cudaStreamDestroy(ctx->st);
   delete ctx;
 }
@@ -1733,7 +1748,7 @@ static void lu_solve(peec_ctx* ctx, const c64* b, c64* x) {
   const int n = (int)ctx->n;
   const LevelTri &L = ctx->Lf, &U = ctx->Uf;
   ctx->launches += launch_sptrsv(
-      ctx->grp, ctx->sf_ord, ctx->sf_nL, ctx->sf_total, SfTri{L.ptr, L.col, L.val, L.dinv, L.flag},
+      ctx->grp, ctx->st2, ctx->ev_fork, ctx->ev_join, ctx->sf_ord, ctx->sf_nL, ctx->sf_total, SfTri{L.ptr, L.col, L.val, L.dinv, L.flag},
       SfTri{U.ptr, U.col, U.val, U.dinv, U.flag}, b, ctx->g_in, ctx->lu_rs, ctx->lutmp,
       ctx->lutmp2, ctx->sf_ctl, ctx->st);
   launch_perm_gather(ctx->lutmp2, ctx->g_out, nullptr, n, x, ctx->st);

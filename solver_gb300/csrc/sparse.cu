@@ -367,15 +367,26 @@ int sptrsv_grp_prepare(size_t smem_bytes) {
 }
 
 // returns the number of kernels launched
-int launch_sptrsv(const GrpPlan& P, const int32_t* ord, int nL, int total, const SfTri& L,
-                  const SfTri& U, const c64* b, const int32_t* g_in, const double* rs, c64* y,
-                  c64* z, int* ctl, cudaStream_t st) {
+// The large groups go to st2 (forked from st with ev_fork, joined back with ev_join) so
+// that they run beside the packed groups: the two launches are independent (different
+// rows), and each is set by its own deepest groups' chain of levels. Under stream capture
+// the fork and join become graph edges.
+int launch_sptrsv(const GrpPlan& P, cudaStream_t st2, cudaEvent_t ev_fork, cudaEvent_t ev_join,
+                  const int32_t* ord, int nL, int total, const SfTri& L, const SfTri& U,
+                  const c64* b, const int32_t* g_in, const double* rs, c64* y, c64* z, int* ctl,
+                  cudaStream_t st) {
   int launches = 0;
+  const bool fork = st2 && P.nbig > 0 && P.ngroups > P.nbig;
+  if (fork) {
+    cudaEventRecord(ev_fork, st);
+    cudaStreamWaitEvent(st2, ev_fork, 0);
+  }
   if (P.nbig > 0) {  // one warp per large component, shared memory sized for the largest
-    k_sptrsv_grp<<<P.nbig, 32, grp_smem(P.rb, P.eb), st>>>(P, 0, P.nbig, P.rb, P.eb, L, U, b, rs,
-                                                             z);
+    k_sptrsv_grp<<<P.nbig, 32, grp_smem(P.rb, P.eb), fork ? st2 : st>>>(P, 0, P.nbig, P.rb, P.eb,
+                                                                          L, U, b, rs, z);
     ++launches;
   }
+  if (fork) cudaEventRecord(ev_join, st2);
   if (P.ngroups > P.nbig) {
     const int nsmall = P.ngroups - P.nbig;
     const int blocks = (nsmall + SF_GRP_WARPS - 1) / SF_GRP_WARPS;
@@ -383,6 +394,7 @@ int launch_sptrsv(const GrpPlan& P, const int32_t* ord, int nL, int total, const
         P, P.nbig, P.ngroups, 32, SF_GRP_E, L, U, b, rs, z);
     ++launches;
   }
+  if (fork) cudaStreamWaitEvent(st, ev_join, 0);
   if (total <= 0) return launches;
   k_sptrsv_begin<<<1, 1, 0, st>>>(ctl);
   launches += 2;

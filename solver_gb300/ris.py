@@ -1,0 +1,285 @@
+"""The dense RIS solver on the GPU (src/lib/solverRis): the reference's entry point
+``iter_solver_QS_S_type`` (iter_solver_QS_S_type.jl:1-165) with its operator
+``ComputeMatrixVectorRis`` (compute_matrix_vector.jl:1-33) and Householder GMRES
+(gmres_custom.jl) running through the C ABI (peec_set_incidence, peec_set_dense and the
+solver entry points shared with the voxel path).
+
+The dense Lp and P matrices (``Lp_data``, ``P_data``) are inputs, as they are to the
+reference's solver: the reference fills them on the host (sharedRis/calcola_{Lp,P}.jl),
+and so does a caller of this module.
+
+Mapping onto the library's operator: the library forms the first block row as
+jw LpI + DZ I + A Phi and the preconditioner with invZ = 1/DZ. With DZ = Z_self +
+jw diag(Lp) (the RIS solver's invZ, iter_solver_QS_S_type.jl:103) and LpI the product
+with Lp's off-diagonal part (peec_set_dense), that is the RIS operator exactly:
+jw Lp I + Z_self I + A Phi. The RIS preconditioner's three LU solves
+(compute_matrix_vector.jl:35-57) become one by linearity, as on the voxel path.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from . import _lib
+from .operator import GpuOperator
+
+MU0 = 4 * math.pi * 1e-7
+EPS0 = 8.854187816997944e-12
+
+
+class DenseOperator(GpuOperator):
+    """A GPU operator with dense Lp blocks and a dense P over a mesh without voxel
+    lattices. Solver entry points (set_frequency, gmres, solve_mixed, port_rhs,
+    set_frequency_refactor, ...) are those of GpuOperator; DZ = Z_self + jw diag(Lp)."""
+
+    def __init__(self, incidence_selection, Lp_data, P_data, device=0):
+        self.L = _lib.load()
+        self._init_args = (incidence_selection, Lp_data, P_data, device)
+        self._rows = None
+        self._rcc = None
+        self._rcc_freq = None
+        self._freq_key = None
+        self._spec_src = None
+        self._stop = None
+        self.grid = None
+        h = ctypes.c_void_p()
+        rc = self.L.peec_ctx_create(ctypes.byref(h), device)
+        if rc != 0:
+            raise _lib.PeecError(rc, self.L.peec_last_error(None).decode())
+        self.h = h
+        if not GpuOperator.DEVICE_LOOP:
+            self.set_device_loop(False)
+        if GpuOperator.LU_COMPONENT_MAX != 512:
+            self.set_lu_component_max(GpuOperator.LU_COMPONENT_MAX)
+        A = incidence_selection["A"].tocsr()
+        Gamma = incidence_selection["Gamma"].tocsc()
+        self.m, self.n = A.shape
+        self.ns = Gamma.shape[1]
+        self.N = self.m + self.ns + self.n
+        mx, my, mz = (int(incidence_selection[k]) for k in ("mx", "my", "mz"))
+        if mx + my + mz != self.m:
+            raise ValueError(f"mx+my+mz={mx + my + mz} must equal the {self.m} rows of A")
+        if np.any(np.diff(A.indptr) != 2):
+            raise ValueError("A must have two entries per edge row")
+        a, b = A.indices[A.indptr[:-1]], A.indices[A.indptr[:-1] + 1]
+        va = A.data[A.indptr[:-1]]
+        n1 = np.ascontiguousarray(np.where(va < 0, a, b), dtype=np.int64)
+        n2 = np.ascontiguousarray(np.where(va < 0, b, a), dtype=np.int64)
+        if np.any(np.diff(Gamma.indptr) != 1):
+            raise ValueError("Gamma must have one entry per surface column")
+        snode = np.ascontiguousarray(Gamma.indices, dtype=np.int64)
+        _lib.check(self.h, self.L.peec_set_incidence(self.h, mx, my, mz, _lib.ptr(n1),
+                                                     _lib.ptr(n2), self.ns, _lib.ptr(snode),
+                                                     self.n))
+        blocks = []
+        for key, size in (("Lp_x", mx), ("Lp_y", my), ("Lp_z", mz)):
+            M = np.asfortranarray(np.asarray(Lp_data[key], dtype=np.float64))
+            if M.shape != (size, size):
+                raise ValueError(f"{key} must be {size} x {size}, got {M.shape}")
+            blocks.append(M)
+        P = np.asfortranarray(np.asarray(P_data["P"], dtype=np.float64))
+        if P.shape != (self.ns, self.ns):
+            raise ValueError(f"P must be {self.ns} x {self.ns}, got {P.shape}")
+        blocks.append(P)
+        dP = np.ascontiguousarray(np.diag(P))  # kept referenced while the library reads it
+        _lib.check(self.h, self.L.peec_set_pdiag(self.h, _lib.ptr(dP)))
+        ptrs = [_lib.ptr(M) if M.size else None for M in blocks]
+        _lib.check(self.h, self.L.peec_set_dense(self.h, *ptrs))
+        self.diag_Lp = np.concatenate([np.diag(M) for M in blocks[:3]])
+
+    def clone(self):
+        """A second context with the same mesh and matrices (its own stream and
+        workspaces), for concurrent port solves."""
+        inc, Lp, P, dev = self._init_args
+        return DenseOperator(inc, Lp, P, device=dev)
+
+
+def lumped_admittance_S(typ, R, L, C, w):
+    """get_lumped_elements_admittance_S (build_Yle_S.jl:70-151): the element's network,
+    then while the value is not finite or below 1e-16 in magnitude the next network of the
+    cascade (IEEE divisions by zero, as in Julia). The RIS cascade of type 2 differs from
+    the voxel path's in its fifth network: 1/(1/(jwC)) + jwC."""
+    R, L, C = np.float64(R), np.float64(L), np.float64(C)
+    jw = np.complex128(1j * w)
+    bad = lambda v: np.isnan(v) or np.isinf(v) or abs(v) < 1e-16
+    with np.errstate(all="ignore"):
+        if typ == 1:
+            z = R + jw * L + 1 / (jw * C)
+            if bad(z):
+                z = R + jw * L
+            y = 1 / z
+        else:
+            nets = {
+                2: (lambda: 1 / (R + jw * L) + jw * C, lambda: 1 / R + jw * C,
+                    lambda: 1 / (R + jw * L), lambda: 1 / R,
+                    lambda: 1 / (1 / (jw * C)) + jw * C, lambda: jw * C),
+                3: (lambda: 1 / (R + 1 / (jw * C)) + 1 / (jw * L), lambda: 1 / (R + 1 / (jw * C)),
+                    lambda: 1 / R + 1 / (jw * L), lambda: 1 / R,
+                    lambda: 1 / (1 / (jw * C)) + 1 / (jw * L), lambda: 1 / (jw * L),
+                    lambda: 1 / (1 / (jw * C))),
+                4: (lambda: 1 / R + jw * C + 1 / (jw * L), lambda: 1 / R + jw * C,
+                    lambda: jw * C + 1 / (jw * L), lambda: jw * C),
+                5: (lambda: 1 / R + 1 / (jw * L + 1 / (jw * C)), lambda: 1 / R + 1 / (1 / (jw * C)),
+                    lambda: 1 / R + 1 / (jw * L), lambda: 1 / R,
+                    lambda: 1 / (jw * L + 1 / (jw * C)), lambda: 1 / (jw * L),
+                    lambda: 1 / (1 / (jw * C))),
+            }.get(int(typ), (lambda: np.complex128(0.0),))
+            y = nets[0]()
+            for f in nets[1:]:
+                if not bad(y):
+                    break
+                y = f()
+        if np.isnan(y) or np.isinf(y):
+            y = 0.0
+    return complex(y)
+
+
+def build_yle_s(lumped_elements, grounding_nodes, ports, escalings, n, w, val_chiusura):
+    """Sparse n x n admittance of the lumped elements, the port closures (1/R between each
+    port's nodes) and the grounding nodes (1e-12), summed per entry and scaled by
+    escalings["Yle"] (build_Yle_S.jl:1-68). Complex element admittances stay complex (the
+    reference sums into a Float64 dictionary, which holds real ones only)."""
+    acc = {}
+
+    def add(r, c, v):
+        acc[(r, c)] = acc.get((r, c), 0.0) + v
+
+    le = lumped_elements or {}
+    for k in range(len(le.get("le_nodes", []))):
+        a, b = int(le["le_nodes"][k][0]), int(le["le_nodes"][k][1])
+        y = lumped_admittance_S(le["type"][k], le["R"][k], le["L"][k], le["C"][k], w)
+        add(a, a, y)
+        add(b, b, y)
+        add(a, b, -y)
+        add(b, a, -y)
+    for k in range(len(ports["port_nodes"])):
+        a, b = int(ports["port_nodes"][k][0]), int(ports["port_nodes"][k][1])
+        y = 1.0 / val_chiusura
+        add(a, a, y)
+        add(b, b, y)
+        add(a, b, -y)
+        add(b, a, -y)
+    for g in grounding_nodes:
+        add(int(g), int(g), 1.0 / 1e12)
+    if not acc:
+        return sp.csr_matrix((n, n), dtype=np.complex128)
+    rc = np.array(list(acc.keys()), dtype=np.int64)
+    v = np.array(list(acc.values()), dtype=np.complex128) * escalings["Yle"]
+    return sp.csr_matrix((v, (rc[:, 0], rc[:, 1])), shape=(n, n))
+
+
+def z_self(volumi, w, use_Zs_in):
+    """Self impedance per edge (iter_solver_QS_S_type.jl:82-101): R, or with use_Zs_in the
+    surface impedance Re(sqrt(jw) Zs_part) where it is not below R; plus 1/(jw Cd) on the
+    dielectric volumes."""
+    R = np.asarray(volumi["R"], dtype=np.float64).ravel()
+    diel = np.asarray(volumi.get("indici_dielettrici", []), dtype=np.int64).ravel()
+    invCd = np.zeros(len(volumi["Cd"]) if diel.size else R.size, dtype=np.complex128)
+    if diel.size:
+        Cd = np.asarray(volumi["Cd"], dtype=np.float64).ravel()
+        invCd[diel] = 1.0 / (1j * w * Cd[diel])
+    if use_Zs_in:
+        Zs = (np.sqrt(1j * w) * np.asarray(volumi["Zs_part"], dtype=np.complex128).ravel()).real
+        Z = np.where(R > Zs, R, Zs).astype(np.complex128)
+        return Z + invCd
+    return R + invCd
+
+
+class RisState:
+    """One frequency's host state: Z_self, DZ = Z_self + jw diag(Lp), Yle and the LU of
+    SS = Yle + A' diag(1/DZ) A + jw Gamma diag(1/P) Gamma' (iter_solver_QS_S_type.jl:82-115)."""
+
+    def __init__(self, w, escalings, incidence_selection, diag_Lp, diag_P, ports,
+                 lumped_elements, volumi, use_Zs_in, val_chiusura, factor=True):
+        A = incidence_selection["A"]
+        Gamma = incidence_selection["Gamma"]
+        n = A.shape[1]
+        self.w = w
+        self.Yle = build_yle_s(lumped_elements, [], ports, escalings, n, w / escalings["freq"],
+                               val_chiusura)
+        self.Z_self = z_self(volumi, w, use_Zs_in)
+        self.DZ = self.Z_self + 1j * w * np.asarray(diag_Lp, dtype=np.float64)
+        self.lu = None
+        if factor:
+            invZ = sp.diags(1.0 / self.DZ)
+            invP = sp.diags(1.0 / np.asarray(diag_P, dtype=np.float64))
+            SS = (self.Yle + A.T @ (invZ @ A) + 1j * w * ((Gamma @ invP) @ Gamma.T)).tocsc()
+            self.lu = spla.splu(SS, permc_spec="MMD_AT_PLUS_A", options={"Equil": False})
+
+
+def iter_solver_QS_S_type(freq, escalings, incidence_selection, P_data, Lp_data, ports,
+                          lumped_elements, GMRES_settings, volumi, use_Zs_in, QS_Rcc_FW,
+                          ports_scatter_value, mode="fp64", op=None, device=0, lu="host"):
+    """The RIS solver's frequency x port loop on the GPU (iter_solver_QS_S_type.jl:1-165):
+    per frequency the state, per port the right-hand side M^-1 [0; 0; is], GMRES warm
+    started from that port's previous solution, and the S entries
+    S(c1,c2) = (2 (V(n3) - V(n4)) - R delta) / R. mode "fp64": the reference's FP64 GMRES;
+    "mixed": FP32 dense products with float-float / FP64 refinement. lu="device": SS is
+    factorised on the GPU after the first frequency, in that frequency's pattern.
+    Returns the reference's dict (S, Z, Y, f) plus the per-solve records (info)."""
+    if int(QS_Rcc_FW) != 1:
+        raise NotImplementedError("the dense RIS operator on the GPU is quasi-static "
+                                  "(QS_Rcc_FW = 1)")
+    if mode not in ("fp64", "mixed"):
+        raise ValueError("mode must be 'fp64' or 'mixed'")
+    freq = np.asarray(freq, dtype=np.float64).ravel() * escalings["freq"]
+    A = incidence_selection["A"]
+    m, n = A.shape
+    ns = incidence_selection["Gamma"].shape[1]
+    pn = np.asarray(ports["port_nodes"], dtype=np.int64).reshape(-1, 2)
+    npt = pn.shape[0]
+    R = float(ports_scatter_value)
+    own = op is None
+    if own:
+        op = DenseOperator(incidence_selection, Lp_data, P_data, device=device)
+    diag_P = np.diag(np.asarray(P_data["P"]))
+    S = np.zeros((npt, npt, freq.size), dtype=np.complex128)
+    Vrest = np.zeros((m + ns + n, npt), dtype=np.complex128)
+    info = []
+    tol = np.broadcast_to(np.asarray(GMRES_settings["tol"], dtype=np.float64), freq.shape)
+    maxit = int(GMRES_settings["Inner_Iter"])
+    try:
+        for k, f in enumerate(freq):
+            w = 2 * math.pi * f
+            dev_lu = lu == "device" and k > 0
+            st = RisState(w, escalings, incidence_selection, op.diag_Lp, diag_P, ports,
+                          lumped_elements, volumi, use_Zs_in, R, factor=not dev_lu)
+            if dev_lu:
+                op.set_frequency_refactor(w, st.DZ, st.Yle)
+            else:
+                op.set_frequency(w, st.DZ, st.Yle, st.lu)
+                if lu == "device":
+                    op.enable_refactor(st.Yle)
+            for c1 in range(npt):
+                n1, n2 = pn[c1]
+                tn = op.port_rhs(n1, n2, escalings["Is"])
+                x0 = Vrest[:, c1]
+                if mode == "fp64":
+                    V, flag, relres, it, rv = op.gmres(tn, x0, float(tol[k]), maxit)
+                    rec = dict(freq=k, port=c1, flag=flag, relres=relres, iter=list(it),
+                               niter=len(rv) - 1)
+                else:
+                    V, flag, relres, outer, inner = op.solve_mixed(tn, x0, float(tol[k]),
+                                                                   inner_maxit=maxit)
+                    rec = dict(freq=k, port=c1, flag=flag, relres=relres, outer=outer,
+                               niter=inner)
+                info.append(rec)
+                Vrest[:, c1] = V
+                for c2 in range(c1, npt):
+                    n3, n4 = pn[c2]
+                    d = 2 * (V[m + ns + n3] - V[m + ns + n4])
+                    S[c1, c2, k] = (d - R) / R if c1 == c2 else d / R
+                    S[c2, c1, k] = S[c1, c2, k]
+    finally:
+        if own:
+            op.close()
+    Id = np.eye(npt)
+    Z = np.stack([R * np.linalg.solve(Id - S[:, :, k], Id + S[:, :, k]) for k in range(freq.size)],
+                 axis=2) if freq.size else S.copy()
+    Y = np.stack([R * np.linalg.solve(Id + S[:, :, k], Id - S[:, :, k]) for k in range(freq.size)],
+                 axis=2) if freq.size else S.copy()
+    return {"S": S, "Z": Z, "Y": Y, "f": freq / escalings["freq"], "info": info, "Vrest": Vrest}
