@@ -14,8 +14,9 @@ frequency's solution (FFT_solver_QS_S_type.jl:60-209).
   factorisation on the GPU with --lu device, 4 port solves), the host parts of the
   states prepared beforehand;
 * e2e: the same steps end to end through the public API with host buffers, wall clock
-  including each point's host state (built in worker processes started on it inside the
-  timed region), uploads and the download of each solution;
+  including each point's state built inside the timed region (with --lu device: Yle on
+  the host, DZ and the factorisation of SS on the GPU; with --lu host: worker processes
+  building DZ, Yle and the SuperLU factors), uploads and the download of each solution;
 * fp64_plain: the reference algorithm (FP64 convolutions, Householder GMRES) on the
   same lanes and points; mixed_fp64_residual: mixed with FP64 refinement residuals;
 * accuracy: port impedances of every arm against FP64 GMRES at 1e-12, per frequency;
@@ -344,7 +345,7 @@ def _point_bytes(P, fs, npt, nlanes=1):
     from solver_gb300.frequency import export_lu
     m, n = P["inc"]["A"].shape
     N = m + P["inc"]["Gamma"].shape[1] + n
-    state = fs.DZ.nbytes + fs.Yle.nnz * 32
+    state = (fs.DZ.nbytes if fs.DZ is not None else 0) + fs.Yle.nnz * 32
     if fs.lu is not None:
         (_, Lc, _), (_, Uc, _), _, _ = export_lu(fs.lu)
         state += (Lc.size + Uc.size) * 24 + (2 * n + 2) * 8 * 2 + 2 * n * 8
@@ -997,13 +998,25 @@ def main():
         from solver_gb300.api import install_state
         for o in lanes.ops:
             install_state(o, state(0), True)
+            # the per-edge data from which the device forms each timed point's DZ
+            o.set_edge_state(P["diag"], P["Zs"], P["esc"])
     try:
         timer = LaneTimer(lanes, local)
     except Exception:
         timer = None
     mixed_kw = dict(inner_tol=P["inner_tol"], inner_maxit=P["settings"]["Inner_Iter"])
     fp64_kw = dict(maxit=P["settings"]["Inner_Iter"])
-    cached = lambda k, pos: state(k)
+    if P["device_lu"]:
+        # device-formed states of the mixed sweeps: the host builds Yle only; DZ and the
+        # factorisation of SS happen on the GPU (peec_set_frequency_device)
+        from solver_gb300.frequency import DeviceFrequencyState
+        n_nodes = P["inc"]["A"].shape[1]
+        dev_state = lambda k: DeviceFrequencyState(w_of(k), P["esc"], n_nodes, P["le"], P["ports"],
+                                                   P["z0"])
+        dev_cache = {}
+        cached = lambda k, pos: dev_cache[k] if k in dev_cache else dev_cache.setdefault(k, dev_state(k))
+    else:
+        cached = lambda k, pos: state(k)
     # warm-up: the first points of the sequence, untimed; they also build the warm starts
     if warm_seq:
         lane_sweep(P, lanes, warm_seq, cached, Vrest, tol, "mixed", mixed_kw, None)
@@ -1027,25 +1040,27 @@ def main():
     sync()
     t_e0 = time.perf_counter()
     # keyed by position in the timed sequence: a frequency visited twice is built twice
-    fresh = make_pool(list(range(len(seq))), lambda pos: seq[pos],
-                      (lambda pos: False) if P["device_lu"] else None)
+    # (host states by the worker processes; device states by the lane's own thread, Yle only)
+    fresh = None if P["device_lu"] else make_pool(list(range(len(seq))), lambda pos: seq[pos])
     waits = [0.0]
 
     def fresh_state(k, pos):
         th = time.perf_counter()
-        st = fresh.get(pos, pos=pos)
+        st = dev_state(k) if fresh is None else fresh.get(pos, pos=pos)
         waits[0] += time.perf_counter() - th
         return st
     _, wall_e2e, cols_e2e, _, _ = lane_sweep(P, lanes, seq, fresh_state, V_e2e, tol, "mixed",
                                              mixed_kw, None)
     sync()
     wall_e2e = time.perf_counter() - t_e0
-    fresh.close()
+    if fresh is not None:
+        fresh.close()
     barrier(ws)
     clk = clocks.stop()
     m_, n_ = P["inc"]["A"].shape
     ns_ = P["inc"]["Gamma"].shape[1]
-    h2d = sum(_point_bytes(P, state(k), npt, nlanes) for k in seq)
+    h2d = sum(_point_bytes(P, cached(k, None) if P["device_lu"] else state(k), npt, nlanes)
+              for k in seq)
     d2h = len(seq) * npt * 2 * (m_ + ns_ + n_) * 16
     value, e2e_v, gpu_s, wall_s = whole_job_rates(ws, args.steps, gpu_ms / 1e3, wall_e2e)
 
@@ -1131,15 +1146,17 @@ def main():
                    "timed_points": [fkey(k) for k in seq]},
         "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": int(d2h / args.steps),
-                "host_states": "built inside the timed region by worker processes started on "
-                               "them only then (no state of a timed point exists before it)"
-                               + ("; DZ and Yle on the host, SS assembled and factorised on "
-                                  "the GPU (one host factorisation of frequency 0 in the "
-                                  "warm-up fixes the pattern and pivot order)"
-                                  if P["device_lu"] else
-                                  "; SS factorised by SuperLU on the host at every point"),
+                "host_states": ("built inside the timed region, no state of a timed point "
+                                "existing before it: Yle on the host by each lane's thread; "
+                                "DZ formed and SS assembled and factorised on the GPU (one "
+                                "host factorisation of frequency 0 in the warm-up fixes the "
+                                "pattern and pivot order)")
+                               if P["device_lu"] else
+                               ("built inside the timed region by worker processes started "
+                                "on them only then (no state of a timed point exists before "
+                                "it); SS factorised by SuperLU on the host at every point"),
                 "host_state_wait_ms_per_step": waits[0] / max(1, nlanes) * 1e3 / args.steps,
-                "host_state_workers": nworkers},
+                "host_state_workers": 0 if P["device_lu"] else nworkers},
         "gpu_launches": int(launches),
         "clocks": clk,
         "fp64_plain": fp64,

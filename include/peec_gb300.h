@@ -106,6 +106,29 @@ int peec_set_incidence(peec_ctx* ctx, int64_t mx, int64_t my, int64_t mz,
 int peec_set_dense(peec_ctx* ctx, const double* Lp_x, const double* Lp_y, const double* Lp_z,
                    const double* P);
 
+/*
+ * Per-edge data from which the device forms each frequency's edge impedances DZ
+ * (FFT_solver_QS_S_type.jl:105-114, compute_Z_self.jl): R4 and Cd4 the resistances and
+ * capacitances of the four edge halves (m x 4, row-major; diagonals["R"], ["Cd"]), Lp_self
+ * the Lp self terms (diagonals["Lp"]), Zs0 the real surface-impedance base (the
+ * frequency's Zs is escal_R * Zs0 * sqrt(w / escal_freq)) and the nse surface edges.
+ * Copied; used by peec_set_frequency_device.
+ */
+int peec_set_edge_state(peec_ctx* ctx, const double* R4, const double* Cd4, const double* Lp_self,
+                        const double* Zs0, const int64_t* surface_edges, int64_t nse,
+                        double escal_R, double escal_freq);
+
+/*
+ * One frequency's state formed on the device: DZ from the edge data
+ * (peec_set_edge_state) -- Z_self, the surface-impedance selection on surface edges and
+ * jw Lp_self, as the reference forms them on the host each frequency -- and SS assembled
+ * and factorised in the pattern of peec_lu_refactor_setup (Yle with that set-up's
+ * pattern). The caller passes only w and Yle. Keeps the captured graphs, like
+ * peec_set_frequency_refactor. No counterpart in the reference.
+ */
+int peec_set_frequency_device(peec_ctx* ctx, double w, int64_t yle_nnz, const int64_t* yle_row,
+                              const int64_t* yle_col, const double* yle_val);
+
 /* P self terms diag(P) per surface (diagonals["P"]); invP = 1 ./ diagP. */
 int peec_set_pdiag(peec_ctx* ctx, const double* diagP);
 

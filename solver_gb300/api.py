@@ -170,8 +170,20 @@ def s2y_fft(S, Zo):
 def install_state(op, fs, device_lu=False):
     """Sets a frequency state on a context: with host factors (fs.lu) through
     peec_set_frequency, and with device_lu the later states factorised on the device in
-    their pattern (fs.lu None: peec_set_frequency_refactor)."""
-    if device_lu and fs.lu is None:
+    their pattern (fs.lu None: peec_set_frequency_refactor); a DeviceFrequencyState has
+    its DZ formed on the device too (peec_set_frequency_device)."""
+    if getattr(fs, "device_dz", False):
+        src = getattr(op, "_edge_src", None)
+        if fs.edge is not None and (src is None or src[0] is not fs.edge[0]
+                                    or src[1] is not fs.edge[1]):
+            # the context's edge data comes from these diagonals (kept referenced, so the
+            # identity test cannot match a reused object)
+            op.set_edge_state(fs.edge[0], fs.edge[1], fs.escalings)
+            op._edge_src = fs.edge
+        elif fs.edge is None and not getattr(op, "_edge_state", False):
+            raise ValueError("a device-formed state on a context without edge data")
+        op.set_frequency_device(fs.w, fs.Yle)
+    elif device_lu and fs.lu is None:
         op.set_frequency_refactor(fs.w, fs.DZ, fs.Yle)
     else:
         op.set_frequency(fs.w, fs.DZ, fs.Yle, fs.lu)
@@ -353,7 +365,17 @@ def FFT_solver_QS_S_type(freq, escalings, incidence_selection, FFTCP, FFTCLp, di
     nl = min(int(lanes), npt)
     # lanes read each state once per lane: keep states until every lane has set them
     keep = mode == "mixed" and mixed_warm_start and nl > 1
-    if n >= POOL_MIN_NODES and w.size > 2:
+    if device_lu:
+        # the first frequency factorised on the host (its pattern and pivot order); the
+        # others formed on the device (DZ, SS and its factors), the host building Yle only
+        first = lambda k: fq.FrequencyState(w[k], escalings, incidence_selection, diagonals,
+                                            Zs_info, lumped_elements, ports,
+                                            ports_scatter_value, factor=True)
+        later = lambda k: fq.DeviceFrequencyState(w[k], escalings, n, lumped_elements, ports,
+                                                  ports_scatter_value, (diagonals, Zs_info))
+        pf = fq.StatePrefetcher(lambda k: first(k) if k == 0 else later(k), range(w.size),
+                                keep=keep)
+    elif n >= POOL_MIN_NODES and w.size > 2:
         # large node systems: factorise ahead in spawned worker processes
         pf = fq.FrequencyPool((escalings, incidence_selection, diagonals, Zs_info,
                                lumped_elements, ports, ports_scatter_value),

@@ -58,9 +58,13 @@ void launch_node_rows(const c64*, const c64*, const c64*, const c64*, const c64*
                       const int32_t*, const int32_t*, const int32_t*, const int32_t*,
                       const int32_t*, const c64*, const double*, int, c64*, cudaStream_t);
 void launch_set_scalar(double* p, double v, cudaStream_t st);
+void launch_edge_dz(int64_t m, const double* R4, const double* Cd4, const double* Lpd,
+                    const double* Zs0, const uint8_t* surf, double escal_R, double sq, double w,
+                    c64* DZ, cudaStream_t st);
 int dense_chunks(int64_t n);
-int dense_apply(const void* M, bool fp32, int64_t n, const c64* x, int offdiag, c64* part,
-                c64* out, cudaStream_t st);
+int64_t dense_ld(int64_t n);
+int dense_apply(const void* M, bool fp32, int64_t n, int64_t ld, const c64* x, int offdiag,
+                c64* part, c64* out, cudaStream_t st);
 void dense_round(const double* a, size_t cnt, float* out, cudaStream_t st);
 void launch_final_rows(const c64*, const c64*, const c64*, const c64*, const int32_t*,
                        const int32_t*, const int32_t*, const double*, int, int, int, c64*,
@@ -144,6 +148,7 @@ struct peec_ctx {
   // real column-major, FP64 and an FP32 copy, and the scratch of their partial sums
   bool lattice = false, dense = false;
   double* dn64[4] = {nullptr, nullptr, nullptr, nullptr};
+  int64_t dn_ld[4] = {4, 4, 4, 4};  // padded leading dimensions
   float* dn32[4] = {nullptr, nullptr, nullptr, nullptr};
   c64* dn_part = nullptr;
   // topology
@@ -193,6 +198,12 @@ struct peec_ctx {
   // Yle value array holds
   double* d_w = nullptr;
   size_t yle_cap = 0;
+  // per-edge data of the device frequency state (peec_set_edge_state): R and Cd of the four
+  // edge halves, Lp self terms, the surface-impedance base and the surface-edge flags
+  double *es_R4 = nullptr, *es_Cd4 = nullptr, *es_Lpd = nullptr, *es_Zs0 = nullptr;
+  uint8_t* es_surf = nullptr;
+  double es_escal_R = 1.0, es_escal_freq = 1.0;
+  bool have_es = false;
   // convolutions of the last converged mixed solve's final residual: x, Lp*I, P*Q and
   // the precision they were computed in (-1: none). They do not depend on the frequency.
   c64 *cc_x = nullptr, *cc_LpI = nullptr, *cc_PQ = nullptr;
@@ -442,7 +453,8 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
                   ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal, ctx->dT,
                   ctx->mdpart, ctx->LpI2, ctx->PQ2, ctx->gm_block, ctx->d_w, ctx->dn_part,
                   ctx->dn64[0], ctx->dn64[1], ctx->dn64[2], ctx->dn64[3], ctx->dn32[0],
-                  ctx->dn32[1], ctx->dn32[2], ctx->dn32[3]};
+                  ctx->dn32[1], ctx->dn32[2], ctx->dn32[3], ctx->es_R4, ctx->es_Cd4,
+                  ctx->es_Lpd, ctx->es_Zs0, ctx->es_surf};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->gm_up) cudaFreeHost(ctx->gm_up);
@@ -763,12 +775,18 @@ static int peec_set_dense_body(peec_ctx* ctx, const double* Lpx, const double* L
   ctx->dense = false;
   size_t part = 1;
   for (int b = 0; b < 4; ++b) {
-    const size_t cnt = (size_t)sz[b] * (size_t)sz[b];
+    // column-major with the leading dimension padded to a multiple of 4 (zero rows), so
+    // every column starts on a 16-byte boundary for the kernels' vector loads
+    const int64_t ld = dense_ld(sz[b]);
+    ctx->dn_ld[b] = ld;
+    const size_t cnt = (size_t)ld * (size_t)sz[b];
     CTX_TRY(dalloc(&ctx->dn64[b], cnt));
     CTX_TRY(dalloc(&ctx->dn32[b], cnt));
     if (cnt) {
-      PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->dn64[b], src[b], sizeof(double) * cnt,
-                                    cudaMemcpyHostToDevice, ctx->st));
+      PEEC_CUDA_TRY(cudaMemsetAsync(ctx->dn64[b], 0, sizeof(double) * cnt, ctx->st));
+      PEEC_CUDA_TRY(cudaMemcpy2DAsync(ctx->dn64[b], sizeof(double) * ld, src[b],
+                                      sizeof(double) * sz[b], sizeof(double) * sz[b], sz[b],
+                                      cudaMemcpyHostToDevice, ctx->st));
       dense_round(ctx->dn64[b], cnt, ctx->dn32[b], ctx->st);
     }
     part = std::max(part, (size_t)dense_chunks(sz[b]) * (size_t)std::max<int64_t>(sz[b], 1));
@@ -1740,6 +1758,76 @@ static int peec_set_frequency_refactor_body(peec_ctx* ctx, double w, const doubl
   return refactor_run(ctx);
 }
 
+// Per-edge data from which the device forms DZ at every frequency
+// (FFT_solver_QS_S_type.jl:105-114): R and Cd of the four edge halves (m x 4, row-major,
+// compute_Z_self.jl), the Lp self terms, the real surface-impedance base Zs0 (the
+// frequency's Zs is escal_R * Zs0 * sqrt(w / escal_freq)) and the surface edges.
+static int peec_set_edge_state_body(peec_ctx* ctx, const double* R4, const double* Cd4,
+                                    const double* Lp_self, const double* Zs0,
+                                    const int64_t* surface_edges, int64_t nse, double escal_R,
+                                    double escal_freq) {
+  if (!ctx || !R4 || !Cd4 || !Lp_self || !Zs0 || (nse > 0 && !surface_edges))
+    return badarg("peec_set_edge_state");
+  if (!ctx->have_topo) return bad(ctx, PEEC_ERR_STATE, "topology not set");
+  if (!(escal_freq > 0)) return bad(ctx, PEEC_ERR_BADARG, "escal_freq must be positive");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  const int64_t m = ctx->m;
+  std::vector<uint8_t> surf(std::max<int64_t>(m, 1), 0);
+  for (int64_t i = 0; i < nse; ++i) {
+    if (surface_edges[i] < 0 || surface_edges[i] >= m)
+      return bad(ctx, PEEC_ERR_BADARG, "surface edge out of range");
+    surf[surface_edges[i]] = 1;
+  }
+  ctx->have_es = false;
+  CTX_TRY(upload(&ctx->es_R4, std::vector<double>(R4, R4 + 4 * m), ctx->st));
+  CTX_TRY(upload(&ctx->es_Cd4, std::vector<double>(Cd4, Cd4 + 4 * m), ctx->st));
+  CTX_TRY(upload(&ctx->es_Lpd, std::vector<double>(Lp_self, Lp_self + m), ctx->st));
+  CTX_TRY(upload(&ctx->es_Zs0, std::vector<double>(Zs0, Zs0 + m), ctx->st));
+  CTX_TRY(upload(&ctx->es_surf, surf, ctx->st));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  ctx->es_escal_R = escal_R;
+  ctx->es_escal_freq = escal_freq;
+  ctx->have_es = true;
+  return PEEC_OK;
+}
+
+// One frequency's state formed on the device: DZ from the edge data, w, Yle (the pattern
+// of the refactorisation set-up), and SS assembled and factorised in the plan's pattern.
+// Like peec_set_frequency_refactor, it writes in place and keeps the captured graphs.
+static int peec_set_frequency_device_body(peec_ctx* ctx, double w, int64_t yle_nnz,
+                                          const int64_t* yle_row, const int64_t* yle_col,
+                                          const double* yle_val) {
+  NvtxRange nvtx_range_("peec_set_frequency_device");
+  if (!ctx || (yle_nnz > 0 && (!yle_row || !yle_col || !yle_val)))
+    return badarg("peec_set_frequency_device");
+  if (!ctx->have_es) return bad(ctx, PEEC_ERR_STATE, "no edge data (peec_set_edge_state)");
+  if (!ctx->have_rf) return bad(ctx, PEEC_ERR_STATE, "no refactorisation plan (peec_lu_refactor_setup)");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  const int64_t n = ctx->n, m = ctx->m;
+  std::vector<int32_t> yp, yc;
+  std::vector<c64> yv;
+  CTX_TRY(yle_csr(ctx, n, yle_nnz, yle_row, yle_col, yle_val, yp, yc, yv));
+  if (yp != ctx->rf_yp || yc != ctx->rf_yc)
+    return bad(ctx, PEEC_ERR_BADARG, "Yle pattern differs from the one of the refactorisation set-up");
+  ctx->have_freq = false;
+  ctx->w = w;
+  if (!ctx->DZ || !ctx->d_w || ctx->yle_cap != yv.size()) {
+    drop_graphs(ctx);
+    CTX_TRY(dalloc(&ctx->DZ, (size_t)m));
+    CTX_TRY(upload(&ctx->yle_val, yv, ctx->st));
+    ctx->yle_cap = yv.size();
+    if (!ctx->d_w) CTX_TRY(dalloc(&ctx->d_w, 1));
+  } else if (!yv.empty()) {
+    PEEC_CUDA_TRY(cudaMemcpyAsync(ctx->yle_val, yv.data(), sizeof(c64) * yv.size(),
+                                  cudaMemcpyHostToDevice, ctx->st));
+  }
+  launch_edge_dz(m, ctx->es_R4, ctx->es_Cd4, ctx->es_Lpd, ctx->es_Zs0, ctx->es_surf,
+                 ctx->es_escal_R, std::sqrt(w / ctx->es_escal_freq), w, ctx->DZ, ctx->st);
+  launch_set_scalar(ctx->d_w, w, ctx->st);
+  ctx->launches += 2;
+  return refactor_run(ctx);
+}
+
 // ------------------------------------------------------------------------------------
 // operator
 // ------------------------------------------------------------------------------------
@@ -1810,9 +1898,10 @@ static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool ev
     const int64_t sz[3] = {ctx->mx, ctx->my, ctx->mz};
     for (int b = 0; b < 3; ++b)
       ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[b] : (const void*)ctx->dn64[b], f32,
-                                   sz[b], x + off[b], 1, ctx->dn_part, ctx->LpI + off[b], st);
+                                   sz[b], ctx->dn_ld[b], x + off[b], 1, ctx->dn_part,
+                                   ctx->LpI + off[b], st);
     ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[3] : (const void*)ctx->dn64[3], f32,
-                                 ctx->ns, x + ctx->m, 0, ctx->dn_part, ctx->PQ, st);
+                                 ctx->ns, ctx->dn_ld[3], x + ctx->m, 0, ctx->dn_part, ctx->PQ, st);
     if (pe) for (int e = 3; e < 6; ++e) cudaEventRecord(pe[e], st);
     if (events) cudaEventRecord(ctx->ev[1], st);
     sparse_enqueue(ctx, x, y, ctx->LpI, ctx->PQ);
@@ -2882,6 +2971,24 @@ extern "C" int peec_set_incidence(peec_ctx* ctx, int64_t mx, int64_t my, int64_t
 extern "C" int peec_set_dense(peec_ctx* ctx, const double* Lp_x, const double* Lp_y,
                               const double* Lp_z, const double* P) {
   return guarded(ctx, "peec_set_dense", [&] { return peec_set_dense_body(ctx, Lp_x, Lp_y, Lp_z, P); });
+}
+
+extern "C" int peec_set_edge_state(peec_ctx* ctx, const double* R4, const double* Cd4,
+                                   const double* Lp_self, const double* Zs0,
+                                   const int64_t* surface_edges, int64_t nse, double escal_R,
+                                   double escal_freq) {
+  return guarded(ctx, "peec_set_edge_state", [&] {
+    return peec_set_edge_state_body(ctx, R4, Cd4, Lp_self, Zs0, surface_edges, nse, escal_R,
+                                    escal_freq);
+  });
+}
+
+extern "C" int peec_set_frequency_device(peec_ctx* ctx, double w, int64_t yle_nnz,
+                                         const int64_t* yle_row, const int64_t* yle_col,
+                                         const double* yle_val) {
+  return guarded(ctx, "peec_set_frequency_device", [&] {
+    return peec_set_frequency_device_body(ctx, w, yle_nnz, yle_row, yle_col, yle_val);
+  });
 }
 
 extern "C" int peec_set_pdiag(peec_ctx* ctx, const double* diagP) {

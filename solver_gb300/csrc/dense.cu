@@ -6,11 +6,14 @@
 // The work is a matrix-vector product that reads every matrix entry once: 8 bytes (FP64
 // storage) or 4 bytes (FP32 storage, the inner solves of the mixed solve) for four flops
 // (the real and imaginary parts). In FP64 that is bound by GB300's FP64 rate (about 1/60 of
-// FP32); the FP32 copy runs at HBM speed. Layout: a CTA owns 256 consecutive rows and one
-// chunk of columns; a warp reads 32 consecutive rows of one column per step (128 or 256
-// contiguous bytes), the chunk's vector entries sit in shared memory, and eight columns
-// are in flight per thread. Each chunk writes its partial sums; a second kernel adds them
-// in chunk order, so results do not depend on scheduling.
+// FP32); the FP32 copy runs at HBM speed. Layout: the matrices are stored column-major
+// with the leading dimension padded to a multiple of 4; a thread owns 4 (FP32) or 2 (FP64)
+// consecutive rows and reads them with one 16-byte load per column (a warp: 512 contiguous
+// bytes); a CTA owns 256 threads' rows and one chunk of columns, whose vector entries sit
+// in shared memory; eight columns are in flight per thread. Each chunk writes its partial
+// sums; a second kernel adds them in chunk order, so results do not depend on scheduling.
+#include <algorithm>
+
 #include "ctx.hpp"
 
 namespace peec {
@@ -18,10 +21,23 @@ namespace peec {
 constexpr int DN_TPB = 256;
 constexpr int DN_CHUNK_MAX = 2048;  // columns per chunk (the vector slice in shared memory)
 
+// rows per thread: one 16-byte load per column (4 floats or 2 doubles)
+template <typename T> struct DnVec;
+template <> struct DnVec<float> { using V = float4; static constexpr int R = 4; };
+template <> struct DnVec<double> { using V = double2; static constexpr int R = 2; };
+template <typename T, typename V>
+__device__ __forceinline__ T dn_at(const V& v, int r) {
+  return reinterpret_cast<const T*>(&v)[r];
+}
+
+// M: n x n, column-major with leading dimension ld (a multiple of 4, rows n..ld zero)
 template <typename T>
 __global__ void __launch_bounds__(DN_TPB) k_dense_gemv(const T* __restrict__ M, int64_t n,
-                                                       const c64* __restrict__ x, int cols,
-                                                       int offdiag, c64* __restrict__ part) {
+                                                       int64_t ld, const c64* __restrict__ x,
+                                                       int cols, int offdiag,
+                                                       c64* __restrict__ part) {
+  using V = typename DnVec<T>::V;
+  constexpr int R = DnVec<T>::R;
   __shared__ cx<T> xs[DN_CHUNK_MAX];
   const int64_t c0 = (int64_t)blockIdx.y * cols;
   const int64_t c1 = min(c0 + cols, n);
@@ -30,70 +46,126 @@ __global__ void __launch_bounds__(DN_TPB) k_dense_gemv(const T* __restrict__ M, 
     xs[j - c0] = mk<T>((T)v.x, (T)v.y);
   }
   __syncthreads();
-  const int64_t i = (int64_t)blockIdx.x * DN_TPB + threadIdx.x;
-  if (i >= n) return;
-  T ar = 0, ai = 0;
-  const T* __restrict__ col = M + c0 * n + i;
+  const int64_t i0 = ((int64_t)blockIdx.x * DN_TPB + threadIdx.x) * R;
+  if (i0 >= n) return;
+  T ar[R], ai[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) ar[r] = ai[r] = T(0);
+  const V* __restrict__ col = reinterpret_cast<const V*>(M + c0 * ld + i0);
+  const int64_t vld = ld / R;
+  // the diagonal entries of this thread's rows sit in columns i0 .. i0 + R - 1
+  const bool diag_here = offdiag && i0 + R > c0 && i0 < c1;
   int64_t j = c0;
   for (; j + 8 <= c1; j += 8) {
-    T mv[8];
+    V mv[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) mv[q] = col[(size_t)q * n];
+    for (int q = 0; q < 8; ++q) mv[q] = col[(size_t)q * vld];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      const T m = (offdiag && j + q == i) ? T(0) : mv[q];
       const cx<T> xv = xs[j + q - c0];
-      ar = ar + m * xv.x;
-      ai = ai + m * xv.y;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const T m = (diag_here && j + q == i0 + r) ? T(0) : dn_at<T>(mv[q], r);
+        ar[r] = ar[r] + m * xv.x;
+        ai[r] = ai[r] + m * xv.y;
+      }
     }
-    col += (size_t)8 * n;
+    col += (size_t)8 * vld;
   }
-  for (; j < c1; ++j, col += n) {
-    const T m = (offdiag && j == i) ? T(0) : *col;
+  for (; j < c1; ++j, col += vld) {
+    const V mv = *col;
     const cx<T> xv = xs[j - c0];
-    ar = ar + m * xv.x;
-    ai = ai + m * xv.y;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const T m = (diag_here && j == i0 + r) ? T(0) : dn_at<T>(mv, r);
+      ar[r] = ar[r] + m * xv.x;
+      ai[r] = ai[r] + m * xv.y;
+    }
   }
-  part[(size_t)blockIdx.y * n + i] = mk<double>((double)ar, (double)ai);
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (i0 + r < n) part[(size_t)blockIdx.y * n + i0 + r] = mk<double>((double)ar[r], (double)ai[r]);
 }
 
-// out[i] = sum over chunks of part[chunk][i], chunks in order
+// out[i] = sum over chunks of part[chunk][i]: eight lanes per row, lane k summing chunks
+// k, k + 8, ... in order, then a fixed shuffle tree over the eight (the same order on
+// every run)
+constexpr int DN_SUM_LANES = 8;
 __global__ void k_dense_sum(const c64* __restrict__ part, int nchunk, int64_t n, c64* out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    c64 s = part[i];
-    for (int c = 1; c < nchunk; ++c) s = s + part[(size_t)c * n + i];
-    out[i] = s;
+  const int sub = threadIdx.x % DN_SUM_LANES;
+  const int64_t rows_per_block = blockDim.x / DN_SUM_LANES;
+  for (int64_t i0 = blockIdx.x * rows_per_block; i0 < n; i0 += (int64_t)gridDim.x * rows_per_block) {
+    const int64_t i = i0 + threadIdx.x / DN_SUM_LANES;
+    double sr = 0.0, si = 0.0;
+    if (i < n)
+      for (int c = sub; c < nchunk; c += DN_SUM_LANES) {
+        const c64 v = part[(size_t)c * n + i];
+        sr += v.x;
+        si += v.y;
+      }
+#pragma unroll
+    for (int o = DN_SUM_LANES / 2; o > 0; o >>= 1) {
+      sr += __shfl_xor_sync(0xffffffffu, sr, o, DN_SUM_LANES);
+      si += __shfl_xor_sync(0xffffffffu, si, o, DN_SUM_LANES);
+    }
+    if (i < n && sub == 0) out[i] = mk<double>(sr, si);
   }
 }
 
-// column chunks of an n x n product: enough CTAs for every SM (about 8 per SM), at most
-// DN_CHUNK_MAX columns each
-int dense_chunks(int64_t n) {
+// padded leading dimension of an n x n block
+int64_t dense_ld(int64_t n) { return std::max<int64_t>(4, (n + 3) / 4 * 4); }
+
+// resident CTAs of the product kernel per SM times the SMs (queried once per process;
+// the kernel's registers and shared memory set it, not a guess)
+static int dense_slots(bool fp32) {
+  static int cached[2] = {0, 0};
+  int& c = cached[fp32 ? 1 : 0];
+  if (c == 0) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (fp32)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dense_gemv<float>, DN_TPB, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dense_gemv<double>, DN_TPB, 0);
+    cudaGetLastError();
+    c = std::max(1, sms) * std::max(1, per);
+  }
+  return c;
+}
+
+// column chunks of an n x n product with R rows per thread: the row tiles times the
+// chunks fill one wave of resident CTAs (a partial second wave would double the tail),
+// at most DN_CHUNK_MAX columns each
+static int dense_chunks_r(int64_t n, int R) {
   if (n <= 0) return 1;
-  const int64_t tiles = (n + DN_TPB - 1) / DN_TPB;
-  int64_t c = (152 * 8 + tiles - 1) / tiles;
+  const int64_t tiles = (n + (int64_t)DN_TPB * R - 1) / ((int64_t)DN_TPB * R);
+  int64_t c = dense_slots(R == 4) / tiles;
   const int64_t cmin = (n + DN_CHUNK_MAX - 1) / DN_CHUNK_MAX;
   const int64_t cmax = std::max<int64_t>(1, n / 64);
   if (c > cmax) c = cmax;
   if (c < cmin) c = cmin;
+  if (c < 1) c = 1;
   return (int)c;
 }
+// the larger of the two layouts' chunk counts (the partial-sum scratch serves both)
+int dense_chunks(int64_t n) { return std::max(dense_chunks_r(n, 2), dense_chunks_r(n, 4)); }
 
-// out = M x (offdiag: without M's diagonal) for one real n x n block; part holds
+// out = M x (offdiag: without M's diagonal) for one real block; part holds
 // dense_chunks(n) * n entries. Returns the kernels launched.
-int dense_apply(const void* M, bool fp32, int64_t n, const c64* x, int offdiag, c64* part,
-                c64* out, cudaStream_t st) {
+int dense_apply(const void* M, bool fp32, int64_t n, int64_t ld, const c64* x, int offdiag,
+                c64* part, c64* out, cudaStream_t st) {
   if (n <= 0) return 0;
-  const int nc = dense_chunks(n);
+  const int R = fp32 ? 4 : 2;
+  const int nc = dense_chunks_r(n, R);
   const int cols = (int)((n + nc - 1) / nc);
-  const dim3 grid((unsigned)((n + DN_TPB - 1) / DN_TPB), (unsigned)nc);
+  const dim3 grid((unsigned)((n + (int64_t)DN_TPB * R - 1) / ((int64_t)DN_TPB * R)), (unsigned)nc);
   if (fp32)
-    k_dense_gemv<float><<<grid, DN_TPB, 0, st>>>((const float*)M, n, x, cols, offdiag, part);
+    k_dense_gemv<float><<<grid, DN_TPB, 0, st>>>((const float*)M, n, ld, x, cols, offdiag, part);
   else
-    k_dense_gemv<double><<<grid, DN_TPB, 0, st>>>((const double*)M, n, x, cols, offdiag, part);
-  int64_t b = (n + 255) / 256;
-  if (b > 152 * 8) b = 152 * 8;
+    k_dense_gemv<double><<<grid, DN_TPB, 0, st>>>((const double*)M, n, ld, x, cols, offdiag, part);
+  int64_t b = (n + 256 / DN_SUM_LANES - 1) / (256 / DN_SUM_LANES);
+  if (b > 152 * 16) b = 152 * 16;
   k_dense_sum<<<(unsigned)b, 256, 0, st>>>(part, nc, n, out);
   return 2;
 }

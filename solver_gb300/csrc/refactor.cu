@@ -103,4 +103,54 @@ int refactor_launch(const RefactorPlan& R, const SfTri& L, const SfTri& U, c64* 
   return launches;
 }
 
+// The per-frequency edge impedances DZ on the device (FFT_solver_QS_S_type.jl:105-114):
+//   Z_self = sum over the four edge halves of 1/(1/R + jw Cd), R, or 1/(jw Cd) where only
+//            one of them is present (compute_Z_self.jl:1-15);
+//   Zs     = escal_R * Zs0 * sqrt(w / escal_freq) (real part);
+//   on surface edges: Z_self keeps only its imaginary part where Zs > Re(Z_self), Zs is
+//            dropped where Zs < Re(Z_self);
+//   DZ     = Z_self + Zs + jw Lp_self.
+// The arithmetic is that of the host state (frequency.FrequencyState): the same
+// operations on doubles, one edge per thread.
+__global__ void k_edge_dz(int64_t m, const double* __restrict__ R4, const double* __restrict__ Cd4,
+                          const double* __restrict__ Lpd, const double* __restrict__ Zs0,
+                          const uint8_t* __restrict__ surf, double escal_R, double sq, double w,
+                          c64* DZ) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double zr = 0.0, zi = 0.0;
+    for (int a = 0; a < 4; ++a) {
+      const double r = R4[4 * e + a], cd = Cd4[4 * e + a];
+      if (r != 0.0 && cd != 0.0) {
+        // 1 / (1/r + j w cd)
+        const double p = 1.0 / r, q = w * cd;
+        const double den = p * p + q * q;
+        zr += p / den;
+        zi += -q / den;
+      } else if (r != 0.0) {
+        zr += r;
+      } else if (cd != 0.0) {
+        // 1 / (j w cd) = -j / (w cd)
+        zi += -1.0 / (w * cd);
+      }
+    }
+    double zs = escal_R * (Zs0[e] * sq);
+    if (surf[e]) {
+      const double d = zs - zr;
+      if (d > 0) zr = 0.0;
+      else if (d < 0) zs = 0.0;
+    }
+    DZ[e] = mk<double>(zr + zs, zi + w * Lpd[e]);
+  }
+}
+
+void launch_edge_dz(int64_t m, const double* R4, const double* Cd4, const double* Lpd,
+                    const double* Zs0, const uint8_t* surf, double escal_R, double sq, double w,
+                    c64* DZ, cudaStream_t st) {
+  int64_t b = (m + 255) / 256;
+  if (b > 152 * 8) b = 152 * 8;
+  if (b < 1) b = 1;
+  k_edge_dz<<<(unsigned)b, 256, 0, st>>>(m, R4, Cd4, Lpd, Zs0, surf, escal_R, sq, w, DZ);
+}
+
 }  // namespace peec

@@ -151,6 +151,25 @@ class FrequencyState:
         self.lu = spla.splu(SS, permc_spec="MMD_AT_PLUS_A", options={"Equil": False})
 
 
+class DeviceFrequencyState:
+    """A frequency state whose edge impedances DZ the device forms (GpuOperator.
+    set_frequency_device, after set_edge_state and enable_refactor): the host builds only
+    the termination / lumped admittance Yle, microseconds of work."""
+
+    device_dz = True
+
+    def __init__(self, w, escalings, n, lumped_elements, ports, z0, edge=None):
+        """edge: (diagonals, Zs_info), uploaded to a context that lacks its edge data when
+        the state is installed (api.install_state)."""
+        self.w = w
+        self.Yle = yle_matrix(lumped_elements, ports, n, w / escalings["freq"], z0,
+                              escalings["Yle"])
+        self.DZ = None
+        self.lu = None
+        self.edge = edge
+        self.escalings = escalings
+
+
 class ExportedLU:
     """Factors already in the exported CSR form (picklable, unlike a SuperLU object)."""
 

@@ -297,6 +297,38 @@ class GpuOperator:
         _lib.check(self.h, self.L.peec_lu_refactor_setup(self.h, int(yr.size), _lib.ptr(yr),
                                                          _lib.ptr(yc)))
 
+    def set_edge_state(self, diagonals, Zs_info, escalings):
+        """Uploads the per-edge data from which set_frequency_device forms DZ on the device:
+        R and Cd of the four edge halves, the Lp self terms, the real surface-impedance
+        base and the surface edges (the inputs of frequency.FrequencyState)."""
+        R4 = np.ascontiguousarray(np.real(np.asarray(diagonals["R"])), dtype=np.float64)
+        Cd4 = np.ascontiguousarray(np.real(np.asarray(diagonals["Cd"])), dtype=np.float64)
+        Lpd = np.ascontiguousarray(np.real(np.asarray(diagonals["Lp"])).ravel(), dtype=np.float64)
+        Zs0 = np.ascontiguousarray(np.real(np.asarray(Zs_info["Zs"])).ravel(), dtype=np.float64)
+        se = np.ascontiguousarray(np.asarray(Zs_info["surface_edges"]).ravel(), dtype=np.int64)
+        if R4.shape != (self.m, 4) or Cd4.shape != (self.m, 4) or Lpd.size != self.m \
+                or Zs0.size != self.m:
+            raise ValueError(f"edge data must hold {self.m} edges (R and Cd m x 4)")
+        _lib.check(self.h, self.L.peec_set_edge_state(
+            self.h, _lib.ptr(R4), _lib.ptr(Cd4), _lib.ptr(Lpd), _lib.ptr(Zs0),
+            _lib.ptr(se) if se.size else None, int(se.size), float(escalings["R"]),
+            float(escalings["freq"])))
+        self._edge_state = True
+
+    def set_frequency_device(self, w, Yle, key=None):
+        """One frequency's state formed on the device (DZ from the edge data, SS factorised
+        in the pattern of enable_refactor); the host passes w and Yle only."""
+        if key is not None and self._same_key(key, self._freq_key):
+            return
+        if tuple(Yle.shape) != (self.n, self.n):
+            raise ValueError(f"Yle must be {self.n} x {self.n}")
+        yr, yc, yv = self._yle_coo(Yle)
+        self._freq_key = None
+        _lib.check(self.h, self.L.peec_set_frequency_device(
+            self.h, float(w), int(yr.size), _lib.ptr(yr), _lib.ptr(yc),
+            _lib.ptr(yv.view(np.float64))))
+        self._freq_key = key
+
     def set_frequency_refactor(self, w, DZ, Yle, key=None):
         """One frequency's state with SS assembled and factorised on the device (after
         enable_refactor); key as for set_frequency."""

@@ -47,6 +47,10 @@ def test_entry_points_reject_a_null_context_with_their_own_name(cuda_lib):
         "peec_set_incidence": lambda: L.peec_set_incidence(None, 0, 0, 0, None, None, 0, None, 1),
         "peec_set_dense": lambda: L.peec_set_dense(None, None, None, None, None),
         "peec_set_device_loop": lambda: L.peec_set_device_loop(None, 1),
+        "peec_set_edge_state": lambda: L.peec_set_edge_state(None, None, None, None, None, None,
+                                                             0, 1.0, 1.0),
+        "peec_set_frequency_device": lambda: L.peec_set_frequency_device(None, 1.0, 0, None,
+                                                                         None, None),
         "peec_set_rows": lambda: L.peec_set_rows(None, None),
         "peec_matvec": lambda: L.peec_matvec(None, None, None, 0),
         "peec_matvec_dev": lambda: L.peec_matvec_dev(None, None, None, 0),

@@ -176,3 +176,38 @@ def test_graphs_kept_across_device_factorised_frequencies(case):
         assert np.linalg.norm(r) <= 1e-6 * np.linalg.norm(tn1)
     finally:
         other.close()
+
+
+def test_device_formed_state_matches_the_host_state(case):
+    """peec_set_frequency_device forms DZ on the device from the edge data (Z_self of the
+    four edge halves, the surface-impedance selection on surface edges, jw Lp_self), as
+    frequency.FrequencyState does on the host: the operators agree to the last bits of DZ
+    (division orders), and a sweep through device-formed states gives the same port
+    impedances as one through host states."""
+    from solver_gb300.frequency import DeviceFrequencyState, FrequencyState
+    c = case
+    p = c["prod"]
+    _setup(c, 1e9)
+    op = c["op"]
+    op.set_edge_state(p["diag"], p["Zs"], p["esc"])
+    rng = np.random.default_rng(17)
+    x = rng.standard_normal(op.N) + 1j * rng.standard_normal(op.N)
+    n = p["inc"]["A"].shape[1]
+    for f in (1e7, 3e8, 1e9, 5e9):
+        w = 2 * np.pi * f * p["esc"]["freq"]
+        hs = FrequencyState(w, p["esc"], p["inc"], p["diag"], p["Zs"], p["le"], p["ports"],
+                            c["z0"], factor=False)
+        op.set_frequency_refactor(w, hs.DZ, hs.Yle)
+        y_host = op.matvec(x, 0)
+        ds = DeviceFrequencyState(w, p["esc"], n, p["le"], p["ports"], c["z0"])
+        op.set_frequency_device(w, ds.Yle)
+        y_dev = op.matvec(x, 0)
+        assert _rel(y_dev, y_host) < 1e-12, (c["name"], f, _rel(y_dev, y_host))
+    # a refused call leaves a clear error: no edge data on a fresh context
+    other = op.clone()
+    try:
+        from solver_gb300 import _lib
+        with pytest.raises(_lib.PeecError, match="edge data"):
+            other.set_frequency_device(w, ds.Yle)
+    finally:
+        other.close()
