@@ -129,6 +129,19 @@ int peec_set_edge_state(peec_ctx* ctx, const double* R4, const double* Cd4, cons
 int peec_set_frequency_device(peec_ctx* ctx, double w, int64_t yle_nnz, const int64_t* yle_row,
                               const int64_t* yle_col, const double* yle_val);
 
+/*
+ * The dense retarded operator (the RIS solver with QS_Rcc_FW == 2,
+ * iter_solver_QS_S_type.jl:39-59): the centre distances of the blocks peec_set_dense
+ * installed (Lp_data[:Rx], [:Ry], [:Rz], P_data[:R_cc]; real, column-major, zero on the
+ * diagonal). From then on the operator multiplies with the blocks times exp(-j beta R)
+ * of the frequency set by peec_set_dense_rcc_frequency (beta = 2 pi f sqrt(eps0 mu0), f
+ * in Hz), formed on the device (FP64 and an FP32 copy) in place. All four pointers NULL
+ * (or peec_set_dense) return the context to the quasi-static blocks.
+ */
+int peec_set_dense_rcc(peec_ctx* ctx, const double* Rx, const double* Ry, const double* Rz,
+                       const double* Rcc);
+int peec_set_dense_rcc_frequency(peec_ctx* ctx, double beta);
+
 /* P self terms diag(P) per surface (diagonals["P"]); invP = 1 ./ diagP. */
 int peec_set_pdiag(peec_ctx* ctx, const double* diagP);
 

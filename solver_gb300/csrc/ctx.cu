@@ -66,6 +66,11 @@ int64_t dense_ld(int64_t n);
 int dense_apply(const void* M, bool fp32, int64_t n, int64_t ld, const c64* x, int offdiag,
                 c64* part, c64* out, cudaStream_t st);
 void dense_round(const double* a, size_t cnt, float* out, cudaStream_t st);
+int64_t dense_part_c(int64_t n);
+int dense_apply_c(const void* M, bool fp32, int64_t n, int64_t ld, const c64* x, int offdiag,
+                  c64* part, c64* out, cudaStream_t st);
+void dense_phase(const double* M, const double* R, size_t cnt, double beta, c64* Mc, c32* Mc32,
+                 cudaStream_t st);
 void launch_final_rows(const c64*, const c64*, const c64*, const c64*, const int32_t*,
                        const int32_t*, const int32_t*, const double*, int, int, int, c64*,
                        cudaStream_t);
@@ -151,6 +156,12 @@ struct peec_ctx {
   int64_t dn_ld[4] = {4, 4, 4, 4};  // padded leading dimensions
   float* dn32[4] = {nullptr, nullptr, nullptr, nullptr};
   c64* dn_part = nullptr;
+  // the dense retarded operator (peec_set_dense_rcc): centre distances R per block, and the
+  // blocks times exp(-j beta R) of the installed frequency (FP64 and FP32 copies)
+  bool dense_rcc = false, dense_rcc_ready = false;
+  double* dnR[4] = {nullptr, nullptr, nullptr, nullptr};
+  c64* dnc64[4] = {nullptr, nullptr, nullptr, nullptr};
+  c32* dnc32[4] = {nullptr, nullptr, nullptr, nullptr};
   // topology
   int32_t *n1 = nullptr, *n2 = nullptr, *snode = nullptr;
   double* invP = nullptr;
@@ -453,7 +464,10 @@ extern "C" void peec_ctx_destroy(peec_ctx* ctx) {
                   ctx->gzero, ctx->dcoef, ctx->dcoef2, ctx->dpart, ctx->dred, ctx->dscal, ctx->dT,
                   ctx->mdpart, ctx->LpI2, ctx->PQ2, ctx->gm_block, ctx->d_w, ctx->dn_part,
                   ctx->dn64[0], ctx->dn64[1], ctx->dn64[2], ctx->dn64[3], ctx->dn32[0],
-                  ctx->dn32[1], ctx->dn32[2], ctx->dn32[3], ctx->es_R4, ctx->es_Cd4,
+                  ctx->dn32[1], ctx->dn32[2], ctx->dn32[3], ctx->dnR[0], ctx->dnR[1],
+                  ctx->dnR[2], ctx->dnR[3], ctx->dnc64[0], ctx->dnc64[1], ctx->dnc64[2],
+                  ctx->dnc64[3], ctx->dnc32[0], ctx->dnc32[1], ctx->dnc32[2], ctx->dnc32[3],
+                  ctx->es_R4, ctx->es_Cd4,
                   ctx->es_Lpd, ctx->es_Zs0, ctx->es_surf};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -773,6 +787,7 @@ static int peec_set_dense_body(peec_ctx* ctx, const double* Lpx, const double* L
   PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   drop_graphs(ctx);
   ctx->dense = false;
+  ctx->dense_rcc = ctx->dense_rcc_ready = false;
   size_t part = 1;
   for (int b = 0; b < 4; ++b) {
     // column-major with the leading dimension padded to a multiple of 4 (zero rows), so
@@ -795,6 +810,70 @@ static int peec_set_dense_body(peec_ctx* ctx, const double* Lpx, const double* L
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   ctx->dense = true;
   ctx->have_spec = true;
+  return PEEC_OK;
+}
+
+// The dense retarded operator (iter_solver_QS_S_type.jl:39-59, QS_Rcc_FW == 2): the
+// centre distances of the blocks (Lp_data[:Rx], [:Ry], [:Rz], P_data[:R_cc]; real,
+// column-major, zero on the diagonal). Each frequency's blocks are the dense blocks times
+// exp(-j beta R), formed on the device by peec_set_dense_rcc_frequency.
+static int peec_set_dense_rcc_body(peec_ctx* ctx, const double* Rx, const double* Ry,
+                                   const double* Rz, const double* Rcc) {
+  if (!ctx) return badarg("peec_set_dense_rcc");
+  if (!ctx->dense) return bad(ctx, PEEC_ERR_STATE, "no dense operator (peec_set_dense)");
+  if (!Rx && !Ry && !Rz && !Rcc) {  // back to the quasi-static blocks
+    drop_graphs(ctx);
+    ctx->dense_rcc = ctx->dense_rcc_ready = false;
+    return PEEC_OK;
+  }
+  const int64_t sz[4] = {ctx->mx, ctx->my, ctx->mz, ctx->ns};
+  const double* src[4] = {Rx, Ry, Rz, Rcc};
+  for (int b = 0; b < 4; ++b) {
+    if (sz[b] > 0 && !src[b]) return bad(ctx, PEEC_ERR_BADARG, "peec_set_dense_rcc: missing block");
+    for (int64_t i = 0; i < sz[b]; ++i)
+      if (src[b][i * sz[b] + i] != 0.0)
+        return bad(ctx, PEEC_ERR_BADARG, "peec_set_dense_rcc: distances must be zero on the diagonal");
+  }
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  drop_graphs(ctx);
+  ctx->dense_rcc = ctx->dense_rcc_ready = false;
+  size_t part = 1;
+  for (int b = 0; b < 4; ++b) {
+    const int64_t ld = ctx->dn_ld[b];
+    const size_t cnt = (size_t)ld * (size_t)sz[b];
+    CTX_TRY(dalloc(&ctx->dnR[b], cnt));
+    CTX_TRY(dalloc(&ctx->dnc64[b], cnt));
+    CTX_TRY(dalloc(&ctx->dnc32[b], cnt));
+    if (cnt) {
+      PEEC_CUDA_TRY(cudaMemsetAsync(ctx->dnR[b], 0, sizeof(double) * cnt, ctx->st));
+      PEEC_CUDA_TRY(cudaMemcpy2DAsync(ctx->dnR[b], sizeof(double) * ld, src[b],
+                                      sizeof(double) * sz[b], sizeof(double) * sz[b], sz[b],
+                                      cudaMemcpyHostToDevice, ctx->st));
+    }
+    // the scratch serves the real products too (a later peec_set_dense drops the phases)
+    part = std::max({part, (size_t)dense_part_c(sz[b]),
+                     (size_t)dense_chunks(sz[b]) * (size_t)std::max<int64_t>(sz[b], 1)});
+  }
+  CTX_TRY(dalloc(&ctx->dn_part, std::max(part, (size_t)1)));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  ctx->dense_rcc = true;
+  return PEEC_OK;
+}
+
+// the retarded blocks at beta = 2 pi f sqrt(eps0 mu0) (f in Hz): formed in place, so the
+// captured graphs of the context stay valid
+static int peec_set_dense_rcc_frequency_body(peec_ctx* ctx, double beta) {
+  if (!ctx) return badarg("peec_set_dense_rcc_frequency");
+  if (!ctx->dense_rcc) return bad(ctx, PEEC_ERR_STATE, "no dense distances (peec_set_dense_rcc)");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  const int64_t sz[4] = {ctx->mx, ctx->my, ctx->mz, ctx->ns};
+  for (int b = 0; b < 4; ++b) {
+    const size_t cnt = (size_t)ctx->dn_ld[b] * (size_t)sz[b];
+    if (cnt) dense_phase(ctx->dn64[b], ctx->dnR[b], cnt, beta, ctx->dnc64[b], ctx->dnc32[b], ctx->st);
+  }
+  ctx->launches += 4;
+  PEEC_CUDA_TRY(cudaGetLastError());
+  ctx->dense_rcc_ready = true;
   return PEEC_OK;
 }
 
@@ -1896,12 +1975,25 @@ static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool ev
     if (pe) for (int e = 0; e < 3; ++e) cudaEventRecord(pe[e], st);
     const int64_t off[3] = {0, ctx->mx, ctx->mx + ctx->my};
     const int64_t sz[3] = {ctx->mx, ctx->my, ctx->mz};
-    for (int b = 0; b < 3; ++b)
-      ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[b] : (const void*)ctx->dn64[b], f32,
-                                   sz[b], ctx->dn_ld[b], x + off[b], 1, ctx->dn_part,
-                                   ctx->LpI + off[b], st);
-    ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[3] : (const void*)ctx->dn64[3], f32,
-                                 ctx->ns, ctx->dn_ld[3], x + ctx->m, 0, ctx->dn_part, ctx->PQ, st);
+    if (ctx->dense_rcc) {
+      if (!ctx->dense_rcc_ready)
+        return bad(ctx, PEEC_ERR_STATE, "retarded blocks not formed (peec_set_dense_rcc_frequency)");
+      for (int b = 0; b < 3; ++b)
+        ctx->launches += dense_apply_c(f32 ? (const void*)ctx->dnc32[b] : (const void*)ctx->dnc64[b],
+                                       f32, sz[b], ctx->dn_ld[b], x + off[b], 1, ctx->dn_part,
+                                       ctx->LpI + off[b], st);
+      ctx->launches += dense_apply_c(f32 ? (const void*)ctx->dnc32[3] : (const void*)ctx->dnc64[3],
+                                     f32, ctx->ns, ctx->dn_ld[3], x + ctx->m, 0, ctx->dn_part,
+                                     ctx->PQ, st);
+    } else {
+      for (int b = 0; b < 3; ++b)
+        ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[b] : (const void*)ctx->dn64[b],
+                                     f32, sz[b], ctx->dn_ld[b], x + off[b], 1, ctx->dn_part,
+                                     ctx->LpI + off[b], st);
+      ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[3] : (const void*)ctx->dn64[3], f32,
+                                   ctx->ns, ctx->dn_ld[3], x + ctx->m, 0, ctx->dn_part, ctx->PQ,
+                                   st);
+    }
     if (pe) for (int e = 3; e < 6; ++e) cudaEventRecord(pe[e], st);
     if (events) cudaEventRecord(ctx->ev[1], st);
     sparse_enqueue(ctx, x, y, ctx->LpI, ctx->PQ);
@@ -2989,6 +3081,16 @@ extern "C" int peec_set_frequency_device(peec_ctx* ctx, double w, int64_t yle_nn
   return guarded(ctx, "peec_set_frequency_device", [&] {
     return peec_set_frequency_device_body(ctx, w, yle_nnz, yle_row, yle_col, yle_val);
   });
+}
+
+extern "C" int peec_set_dense_rcc(peec_ctx* ctx, const double* Rx, const double* Ry,
+                                  const double* Rz, const double* Rcc) {
+  return guarded(ctx, "peec_set_dense_rcc", [&] { return peec_set_dense_rcc_body(ctx, Rx, Ry, Rz, Rcc); });
+}
+
+extern "C" int peec_set_dense_rcc_frequency(peec_ctx* ctx, double beta) {
+  return guarded(ctx, "peec_set_dense_rcc_frequency",
+                 [&] { return peec_set_dense_rcc_frequency_body(ctx, beta); });
 }
 
 extern "C" int peec_set_pdiag(peec_ctx* ctx, const double* diagP) {

@@ -95,7 +95,40 @@ class DenseOperator(GpuOperator):
         """A second context with the same mesh and matrices (its own stream and
         workspaces), for concurrent port solves."""
         inc, Lp, P, dev = self._init_args
-        return DenseOperator(inc, Lp, P, device=dev)
+        c = DenseOperator(inc, Lp, P, device=dev)
+        if getattr(self, "_rcc_dist", None) is not None:
+            c.set_rcc(*self._rcc_dist)
+        return c
+
+    def set_rcc(self, Lp_data, P_data):
+        """The retarded operator (QS_Rcc_FW == 2): the centre distances Lp_data[:Rx],
+        [:Ry], [:Rz] and P_data[:R_cc] of the dense blocks; set_rcc_frequency forms the
+        blocks times exp(-j beta R) of a frequency on the device. None, None: back to the
+        quasi-static blocks."""
+        if Lp_data is None and P_data is None:
+            _lib.check(self.h, self.L.peec_set_dense_rcc(self.h, None, None, None, None))
+            self._rcc_dist = None
+            return
+        mats = []
+        for key, size in (("Rx", self._init_args[0]["mx"]), ("Ry", self._init_args[0]["my"]),
+                          ("Rz", self._init_args[0]["mz"])):
+            M = np.asfortranarray(np.asarray(Lp_data[key], dtype=np.float64))
+            if M.shape != (int(size), int(size)):
+                raise ValueError(f"{key} must be {size} x {size}, got {M.shape}")
+            mats.append(M)
+        R = np.asfortranarray(np.asarray(P_data["R_cc"], dtype=np.float64))
+        if R.shape != (self.ns, self.ns):
+            raise ValueError(f"R_cc must be {self.ns} x {self.ns}, got {R.shape}")
+        mats.append(R)
+        _lib.check(self.h, self.L.peec_set_dense_rcc(self.h, *[_lib.ptr(M) if M.size else None
+                                                              for M in mats]))
+        self._rcc_dist = (Lp_data, P_data)
+
+    def set_rcc_frequency(self, f_hz):
+        """Forms the retarded blocks at frequency f_hz (Hz): beta = 2 pi f sqrt(eps0 mu0)
+        (iter_solver_QS_S_type.jl:41-44)."""
+        beta = 2 * math.pi * float(f_hz) * math.sqrt(EPS0 * MU0)
+        _lib.check(self.h, self.L.peec_set_dense_rcc_frequency(self.h, beta))
 
 
 def lumped_admittance_S(typ, R, L, C, w):
@@ -221,9 +254,9 @@ def iter_solver_QS_S_type(freq, escalings, incidence_selection, P_data, Lp_data,
     "mixed": FP32 dense products with float-float / FP64 refinement. lu="device": SS is
     factorised on the GPU after the first frequency, in that frequency's pattern.
     Returns the reference's dict (S, Z, Y, f) plus the per-solve records (info)."""
-    if int(QS_Rcc_FW) != 1:
-        raise NotImplementedError("the dense RIS operator on the GPU is quasi-static "
-                                  "(QS_Rcc_FW = 1)")
+    if int(QS_Rcc_FW) not in (1, 2):
+        raise NotImplementedError("QS_Rcc_FW must be 1 (quasi-static) or 2 (retarded)")
+    rcc = int(QS_Rcc_FW) == 2
     if mode not in ("fp64", "mixed"):
         raise ValueError("mode must be 'fp64' or 'mixed'")
     freq = np.asarray(freq, dtype=np.float64).ravel() * escalings["freq"]
@@ -236,6 +269,8 @@ def iter_solver_QS_S_type(freq, escalings, incidence_selection, P_data, Lp_data,
     own = op is None
     if own:
         op = DenseOperator(incidence_selection, Lp_data, P_data, device=device)
+    if rcc:
+        op.set_rcc(Lp_data, P_data)
     diag_P = np.diag(np.asarray(P_data["P"]))
     S = np.zeros((npt, npt, freq.size), dtype=np.complex128)
     Vrest = np.zeros((m + ns + n, npt), dtype=np.complex128)
@@ -246,6 +281,10 @@ def iter_solver_QS_S_type(freq, escalings, incidence_selection, P_data, Lp_data,
         for k, f in enumerate(freq):
             w = 2 * math.pi * f
             dev_lu = lu == "device" and k > 0
+            if rcc:
+                # the retarded blocks of this frequency (their diagonals are the quasi-static
+                # ones: the distances are zero there)
+                op.set_rcc_frequency(f / escalings["freq"])
             st = RisState(w, escalings, incidence_selection, op.diag_Lp, diag_P, ports,
                           lumped_elements, volumi, use_Zs_in, R, factor=not dev_lu)
             if dev_lu:
@@ -277,6 +316,8 @@ def iter_solver_QS_S_type(freq, escalings, incidence_selection, P_data, Lp_data,
     finally:
         if own:
             op.close()
+        elif rcc:
+            op.set_rcc(None, None)  # back to the quasi-static blocks for later users
     Id = np.eye(npt)
     Z = np.stack([R * np.linalg.solve(Id - S[:, :, k], Id + S[:, :, k]) for k in range(freq.size)],
                  axis=2) if freq.size else S.copy()

@@ -82,3 +82,39 @@ def volumi_of(c, seed=0):
     pick = rng.choice(cond, size=max(1, cond.size // 4), replace=False) if cond.size else []
     Zs_part[pick] = R[pick] * rng.uniform(0.2, 3.0, size=len(pick)) / np.sqrt(2 * np.pi * 1e9)
     return {"R": R, "Cd": Cd_eff, "indici_dielettrici": diel, "Zs_part": Zs_part}
+
+
+def with_distances(c, Lp, P):
+    """Lp_data / P_data with the centre distances of the retarded RIS operator: Rx, Ry, Rz
+    between the edges of each direction and R_cc between the surfaces (metres, from the
+    lattice cells of the case's mesh; zero on the diagonal)."""
+    from solver_gb300.operator import _edge_cells, _surf_cells, row_dims
+    inc, exp = c["inc"], c["exp"]
+    mx, my, mz = inc["mx"], inc["my"], inc["mz"]
+    ns = inc["Gamma"].shape[1]
+    Nx, Ny, Nz = c["grid"][:3]
+    cell = np.array([c["cc"]["sx"], c["cc"]["sy"], c["cc"]["sz"]], dtype=np.float64)
+    dims = row_dims(Nx, Ny, Nz)
+
+    def coords(ids, d, shift):
+        ids = np.asarray(ids, dtype=np.int64)
+        ix, iy, iz = ids % d[0], (ids // d[0]) % d[1], ids // (d[0] * d[1])
+        return (np.stack([ix, iy, iz], axis=1) + np.asarray(shift)) * cell
+
+    def dist(pos):
+        return np.sqrt(((pos[:, None, :] - pos[None, :, :]) ** 2).sum(-1))
+
+    ec = _edge_cells(exp, mx, my, mz)
+    Lp = dict(Lp)
+    Lp["Rx"] = dist(coords(ec[:mx], dims["Lpx"], (1.0, 0.5, 0.5)))
+    Lp["Ry"] = dist(coords(ec[mx:mx + my], dims["Lpy"], (0.5, 1.0, 0.5)))
+    Lp["Rz"] = dist(coords(ec[mx + my:], dims["Lpz"], (0.5, 0.5, 1.0)))
+    fam, scell = _surf_cells(exp, ns)
+    spos = np.zeros((ns, 3))
+    for f, (key, sh) in enumerate((("p12_se", (0.5, 0.0, 0.5)), ("p34_se", (0.0, 0.5, 0.5)),
+                                   ("p56_se", (0.5, 0.5, 0.0)))):
+        sel = fam == f
+        spos[sel] = coords(scell[sel], dims[key], sh)
+    P = dict(P)
+    P["R_cc"] = dist(spos)
+    return Lp, P

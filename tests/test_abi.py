@@ -46,6 +46,8 @@ def test_entry_points_reject_a_null_context_with_their_own_name(cuda_lib):
         "peec_set_pdiag": lambda: L.peec_set_pdiag(None, None),
         "peec_set_incidence": lambda: L.peec_set_incidence(None, 0, 0, 0, None, None, 0, None, 1),
         "peec_set_dense": lambda: L.peec_set_dense(None, None, None, None, None),
+        "peec_set_dense_rcc": lambda: L.peec_set_dense_rcc(None, None, None, None, None),
+        "peec_set_dense_rcc_frequency": lambda: L.peec_set_dense_rcc_frequency(None, 1.0),
         "peec_set_device_loop": lambda: L.peec_set_device_loop(None, 1),
         "peec_set_edge_state": lambda: L.peec_set_edge_state(None, None, None, None, None, None,
                                                              0, 1.0, 1.0),

@@ -165,3 +165,53 @@ def test_incidence_context_refuses_circulant_calls(case):
     _install(case, w, st)
     x = np.ones(op.N, dtype=np.complex128)
     assert _rel(op.matvec(x, 0), _ris_mv(case, w, st)(x)) < max(1e-11, 4 * _noise(case, w, st, x))
+
+
+@pytest.mark.parametrize("f", [3e8, 1e10])
+def test_retarded_dense_operator_matches_the_oracle(case, f):
+    """QS_Rcc_FW == 2: the blocks times exp(-j beta R), formed on the device per frequency,
+    against the oracle's rebuilt blocks (iter_solver_QS_S_type.jl:39-59)."""
+    c = case
+    Lp, P = ris_cases.with_distances(c, c["Lp_data"], c["P_data"])
+    op = c["op"]
+    op.set_rcc(Lp, P)
+    try:
+        w = 2 * np.pi * f * c["esc"]["freq"]
+        st = RO.frequency_setup(w, c["esc"], c["inc"], P, Lp, c["ports"], {}, c["volumi"], True,
+                                50.0, QS_Rcc_FW=2, freq_unscaled=f)
+        op.set_rcc_frequency(f)
+        _install(c, w, st)
+        rng = np.random.default_rng(12)
+        x = rng.standard_normal(op.N) + 1j * rng.standard_normal(op.N)
+        y_ref = _ris_mv(c, w, st)(x)
+        y64 = op.matvec(x, _lib.PREC_FP64)
+        tol = max(1e-11, 4 * _noise(c, w, st, x))
+        assert _rel(y64, y_ref) < tol, (c["name"], f, _rel(y64, y_ref), tol)
+        assert _rel(op.matvec(x, _lib.PREC_FP32), y_ref) < 2e-5
+        # the phases matter at this size: the quasi-static blocks give another operator
+        op.set_rcc(None, None)
+        assert _rel(op.matvec(x, _lib.PREC_FP64), y_ref) > 100 * tol
+    finally:
+        op.set_rcc(None, None)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "mixed"])
+def test_retarded_ris_solver_matches_the_oracle(case, mode):
+    from solver_gb300 import ris
+    c = case
+    Lp, P = ris_cases.with_distances(c, c["Lp_data"], c["P_data"])
+    freqs = [1e8, 3e9, 1e10]
+    gs = {"Inner_Iter": 200, "tol": [1e-8] * len(freqs)}
+    ref = RO.iter_solver_QS_S_type(freqs, c["esc"], c["inc"], P, Lp, c["ports"], {}, gs,
+                                   c["volumi"], True, 2, 50.0)
+    out = ris.iter_solver_QS_S_type(freqs, c["esc"], c["inc"], P, Lp, c["ports"], {}, gs,
+                                    c["volumi"], True, 2, 50.0, mode=mode, op=c["op"], lu="host")
+    assert all(r["flag"] == 0 for r in out["info"]), out["info"]
+    tol = 1e-7 if mode == "fp64" else 1e-6
+    for k in range(len(freqs)):
+        assert _rel(out["S"][:, :, k], ref["S"][:, :, k]) < tol, (mode, k)
+    # the context is back on the quasi-static blocks afterwards
+    w, st = _ris_state(c, 1e9)
+    _install(c, w, st)
+    x = np.ones(c["op"].N, dtype=np.complex128)
+    assert _rel(c["op"].matvec(x, 0), _ris_mv(c, w, st)(x)) < max(1e-11, 4 * _noise(c, w, st, x))

@@ -127,3 +127,24 @@ def test_dense_entry_points_reject_a_null_context():
         pytest.skip("library not built")
     assert L.peec_set_incidence(None, 0, 0, 0, None, None, 0, None, 1) == -5
     assert L.peec_set_dense(None, None, None, None, None) == -5
+
+
+def test_retarded_blocks_reduce_to_the_quasi_static_ones_at_zero_phase(crossbar):
+    """QS_Rcc_FW == 2 rebuilds the blocks as Lp exp(-j beta R) (iter_solver_QS_S_type.jl:
+    39-59): with zero distances they are the quasi-static blocks, and with the case's
+    distances the phases grow with frequency while the diagonals (R = 0) stay real."""
+    c = crossbar
+    Lp, P = ris_cases.with_distances(c, c["Lp_data"], c["P_data"])
+    vol = ris_cases.volumi_of(c, seed=2)
+    w = 2 * np.pi * 1e9 * c["esc"]["freq"]
+    zero = dict(Lp, Rx=0 * Lp["Rx"], Ry=0 * Lp["Ry"], Rz=0 * Lp["Rz"])
+    zp = dict(P, R_cc=0 * P["R_cc"])
+    st0 = RO.frequency_setup(w, c["esc"], c["inc"], zp, zero, c["ports"], {}, vol, True, 50.0,
+                             QS_Rcc_FW=2, freq_unscaled=1e9)
+    stq = RO.frequency_setup(w, c["esc"], c["inc"], P, Lp, c["ports"], {}, vol, True, 50.0)
+    assert np.array_equal(st0["Lp"]["Lp_x"].real, stq["Lp"]["Lp_x"])
+    assert not np.any(st0["Lp"]["Lp_x"].imag)
+    st = RO.frequency_setup(w, c["esc"], c["inc"], P, Lp, c["ports"], {}, vol, True, 50.0,
+                            QS_Rcc_FW=2, freq_unscaled=1e9)
+    assert np.any(st["P"]["P"].imag) and not np.any(np.diag(st["P"]["P"]).imag)
+    assert np.array_equal(st["diag_Lp"], stq["diag_Lp"])
