@@ -34,6 +34,7 @@ constexpr int SF_TPB = 128;
 constexpr int SF_COMP_MAX = 512;
 constexpr int SF_GRP_E = 256;  // entries (L and U off-diagonal) of a packed group
 constexpr int SF_GRP_WARPS = 4;
+constexpr int SF_BIG_LANES = 4;  // lanes per row in the large components' level loops
 struct GrpRow {
   int32_t r;       // factor row
   int32_t pL, pU;  // first entry of the row in L and in U (CSR)

@@ -162,6 +162,11 @@ __global__ void k_sptrsv_begin(int* ctl) {
 // __syncwarp between levels, and the results go out to z. Per row the arithmetic is that
 // of k_sptrsv (right-hand side, entries subtracted in row order, times the inverse
 // diagonal). R, E: the shared-memory capacity of a warp's slice (rows, entries).
+// W lanes per row in the level loops: 1 for the packed groups (short rows, one lane each);
+// more for the large components, whose rows carry tens of entries on a chain of dozens
+// of levels: the lanes of a row split its entries and combine their partial sums with a
+// fixed shuffle tree (the same order on every run).
+template <int W>
 __global__ void k_sptrsv_grp(GrpPlan P, int g0, int g1, int R, int E, SfTri L, SfTri U,
                              const c64* __restrict__ b, const double* __restrict__ rs, c64* z) {
   extern __shared__ __align__(16) unsigned char grp_sm[];
@@ -198,30 +203,59 @@ __global__ void k_sptrsv_grp(GrpPlan P, int g0, int g1, int R, int E, SfTri L, S
     }
     for (int t = lane; t < ns; t += 32) segs[t] = P.seg[s0 + t];
     __syncwarp();
-    int prev = 0;
-    for (int s = 0; s < nsl; ++s) {
-      const int se = segs[s];
-      for (int q = prev + lane; q < se; q += 32) {
-        const short4 m = meta[q];
-        c64 acc = xs[q];
-        for (int t = 0; t < m.y; ++t) acc = acc - ev[m.x + t] * xs[ec[m.x + t]];
-        xs[q] = acc * dl[q];
+    if constexpr (W == 1) {
+      int prev = 0;
+      for (int s = 0; s < nsl; ++s) {
+        const int se = segs[s];
+        for (int q = prev + lane; q < se; q += 32) {
+          const short4 m = meta[q];
+          c64 acc = xs[q];
+          for (int t = 0; t < m.y; ++t) acc = acc - ev[m.x + t] * xs[ec[m.x + t]];
+          xs[q] = acc * dl[q];
+        }
+        __syncwarp();
+        prev = se;
       }
-      __syncwarp();
-      prev = se;
-    }
-    prev = 0;
-    for (int s = nsl; s < ns; ++s) {
-      const int se = segs[s];
-      for (int t = prev + lane; t < se; t += 32) {
-        const int q = uqs[t];
-        const short4 m = meta[q];
-        c64 acc = xs[q];
-        for (int e = 0; e < m.w; ++e) acc = acc - ev[m.z + e] * xs[ec[m.z + e]];
-        xs[q] = acc * du[q];
+      prev = 0;
+      for (int s = nsl; s < ns; ++s) {
+        const int se = segs[s];
+        for (int t = prev + lane; t < se; t += 32) {
+          const int q = uqs[t];
+          const short4 m = meta[q];
+          c64 acc = xs[q];
+          for (int e = 0; e < m.w; ++e) acc = acc - ev[m.z + e] * xs[ec[m.z + e]];
+          xs[q] = acc * du[q];
+        }
+        __syncwarp();
+        prev = se;
       }
-      __syncwarp();
-      prev = se;
+    } else {
+      constexpr int G = 32 / W;  // rows in flight per step
+      const int sub = lane % W, grp = lane / W;
+      int prev = 0;
+      for (int s = 0; s < ns; ++s) {
+        const bool upper = s >= nsl;
+        const int se = segs[s];
+        for (int t0 = prev; t0 < se; t0 += G) {  // warp-uniform: every lane shuffles
+          const int t = t0 + grp;
+          const bool valid = t < se;
+          const int q = valid ? (upper ? (int)uqs[t] : t) : 0;
+          c64 part = mk<double>(0, 0);
+          if (valid) {
+            const short4 m = meta[q];
+            const int e0 = upper ? m.z : m.x, ne = upper ? m.w : m.y;
+            for (int e = sub; e < ne; e += W) part = part + ev[e0 + e] * xs[ec[e0 + e]];
+          }
+#pragma unroll
+          for (int o = W / 2; o > 0; o >>= 1) {
+            part.x += __shfl_xor_sync(0xffffffffu, part.x, o, W);
+            part.y += __shfl_xor_sync(0xffffffffu, part.y, o, W);
+          }
+          if (valid && sub == 0) xs[q] = (xs[q] - part) * (upper ? du[q] : dl[q]);
+        }
+        __syncwarp();
+        prev = s + 1 == nsl ? 0 : se;
+      }
     }
     for (int q = lane; q < nr; q += 32) z[P.rows[q0 + q].r] = xs[q];
     __syncwarp();
@@ -360,8 +394,10 @@ int sptrsv_grp_prepare(size_t smem_bytes) {
   std::lock_guard<std::mutex> lock(mu);
   // set every time (a re-created context starts from the default again)
   const size_t v = std::max(smem_bytes, granted[dev]);
-  PEEC_CUDA_TRY(cudaFuncSetAttribute(k_sptrsv_grp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)v));
+  PEEC_CUDA_TRY(cudaFuncSetAttribute(k_sptrsv_grp<1>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v));
+  PEEC_CUDA_TRY(cudaFuncSetAttribute(k_sptrsv_grp<SF_BIG_LANES>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v));
   granted[dev] = v;
   return 0;
 }
@@ -382,15 +418,15 @@ int launch_sptrsv(const GrpPlan& P, cudaStream_t st2, cudaEvent_t ev_fork, cudaE
     cudaStreamWaitEvent(st2, ev_fork, 0);
   }
   if (P.nbig > 0) {  // one warp per large component, shared memory sized for the largest
-    k_sptrsv_grp<<<P.nbig, 32, grp_smem(P.rb, P.eb), fork ? st2 : st>>>(P, 0, P.nbig, P.rb, P.eb,
-                                                                          L, U, b, rs, z);
+    k_sptrsv_grp<SF_BIG_LANES><<<P.nbig, 32, grp_smem(P.rb, P.eb), fork ? st2 : st>>>(
+        P, 0, P.nbig, P.rb, P.eb, L, U, b, rs, z);
     ++launches;
   }
   if (fork) cudaEventRecord(ev_join, st2);
   if (P.ngroups > P.nbig) {
     const int nsmall = P.ngroups - P.nbig;
     const int blocks = (nsmall + SF_GRP_WARPS - 1) / SF_GRP_WARPS;
-    k_sptrsv_grp<<<blocks, 32 * SF_GRP_WARPS, SF_GRP_WARPS * grp_smem(32, SF_GRP_E), st>>>(
+    k_sptrsv_grp<1><<<blocks, 32 * SF_GRP_WARPS, SF_GRP_WARPS * grp_smem(32, SF_GRP_E), st>>>(
         P, P.nbig, P.ngroups, 32, SF_GRP_E, L, U, b, rs, z);
     ++launches;
   }
