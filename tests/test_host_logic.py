@@ -218,3 +218,40 @@ def test_lanes_sweep_fp64_mode_runs_the_reference_gmres():
     with pytest.raises(ValueError):
         lanes.sweep([0], lambda k, pos: State(1.0), lambda k: None, pn, 1.0, V, lambda k: 1e-8,
                     {}, lambda *a: None, mode="fp32")
+
+
+def test_install_state_routes_device_formed_states():
+    """A DeviceFrequencyState goes through set_frequency_device; the context's edge data is
+    uploaded once per source (the diagonals and Zs objects it came from) and again when
+    the source changes; host states with device_lu keep the refactorisation path."""
+    import scipy.sparse as sp
+    from solver_gb300.frequency import DeviceFrequencyState
+
+    calls = []
+
+    class Op:
+        def set_edge_state(self, diag, zs, esc):
+            calls.append(("edge", id(diag)))
+            self._edge_state = True
+
+        def set_frequency_device(self, w, Yle):
+            calls.append(("device", w))
+
+        def set_frequency_refactor(self, w, DZ, Yle):
+            calls.append(("refactor", w))
+
+    esc = {"freq": 1.0, "Yle": 1.0}
+    ports = {"port_nodes": np.array([[0, 1]])}
+    d1, z1, d2 = {"R": 1}, {"Zs": 1}, {"R": 2}
+    op = Op()
+    for w, edge in ((1.0, (d1, z1)), (2.0, (d1, z1)), (3.0, (d2, z1))):
+        api.install_state(op, DeviceFrequencyState(w, esc, 4, {}, ports, 50.0, edge), True)
+    assert calls == [("edge", id(d1)), ("device", 1.0), ("device", 2.0), ("edge", id(d2)),
+                     ("device", 3.0)]
+    st = State(4.0)
+    st.Yle = sp.csr_matrix((4, 4))
+    api.install_state(op, st, True)
+    assert calls[-1] == ("refactor", 4.0)
+    # a device-formed state without edge data on a context that has none is refused
+    with pytest.raises(ValueError):
+        api.install_state(Op(), DeviceFrequencyState(5.0, esc, 4, {}, ports, 50.0), True)
