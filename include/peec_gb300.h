@@ -136,11 +136,45 @@ int peec_set_frequency_device(peec_ctx* ctx, double w, int64_t yle_nnz, const in
  * diagonal). From then on the operator multiplies with the blocks times exp(-j beta R)
  * of the frequency set by peec_set_dense_rcc_frequency (beta = 2 pi f sqrt(eps0 mu0), f
  * in Hz), formed on the device (FP64 and an FP32 copy) in place. All four pointers NULL
- * (or peec_set_dense) return the context to the quasi-static blocks.
+ * (or peec_set_dense) return the context to the quasi-static blocks; with distances on the
+ * device (peec_ris_fill), a later peec_set_dense_rcc_frequency returns it to the retarded
+ * operator.
  */
 int peec_set_dense_rcc(peec_ctx* ctx, const double* Rx, const double* Ry, const double* Rz,
                        const double* Rcc);
 int peec_set_dense_rcc_frequency(peec_ctx* ctx, double beta);
+
+/*
+ * The dense RIS matrices filled on the device from the bodies' vertex coordinates:
+ * replaces calcola_Lp (sharedRis/calcola_Lp.jl:1-97) and calcola_P (sharedRis/calcola_P.jl:
+ * 1-47), and takes the place of peec_set_dense + peec_set_pdiag (+ peec_set_dense_rcc when
+ * distances != 0). Needs the topology of peec_set_incidence (mx, my, mz, ns).
+ *   vol_coords   m x 24 row-major: volumi[:coordinate], eight vertices (x, y, z) per volume
+ *   vol_S        m: volumi[:S], the cross-sections
+ *   vol_centres  m x 3: volumi[:centri] (read when distances != 0)
+ *   escal_Lp     escalings[:Lp]
+ *   surf_ends    ns x 12 row-major: superfici["estremi_celle"], four vertices per surface
+ *   surf_S       ns: superfici["S"]
+ *   surf_centres ns x 3: superfici["centri"] (read when distances != 0)
+ *   escal_P      escalings[:P]
+ * Lp blocks: Compute_Lp_Self on the diagonal, 1e-7 / (S_m S_n) * integral * escal_Lp off it
+ * (Song_improved_Ivana_strategy2); P: integral / (4 pi eps0 S_m S_n) * escal_P
+ * (Song_P_improved_Ivana_strategy), the diagonal included; distances |c_m - c_n|
+ * (calculate_Rx/_Ry/_Rz, calculate_R_cc!). Either group of pointers may be NULL: its
+ * blocks are left as they are. *nonfinite (may be NULL) gets the count of non-finite
+ * entries (the reference's closed forms give NaN in a few degenerate configurations).
+ */
+int peec_ris_fill(peec_ctx* ctx, const double* vol_coords, const double* vol_S,
+                  const double* vol_centres, double escal_Lp, const double* surf_ends,
+                  const double* surf_S, const double* surf_centres, double escal_P, int distances,
+                  int64_t* nonfinite);
+
+/*
+ * A dense block back to the host: block 0..2 = Lp_x, Lp_y, Lp_z, 3 = P; what 0 = the
+ * matrix (n x n, column-major), 1 = its centre distances, 2 = its diagonal (n values).
+ * No counterpart in the reference (its matrices live on the host).
+ */
+int peec_dense_get(peec_ctx* ctx, int block, int what, double* out);
 
 /* P self terms diag(P) per surface (diagonals["P"]); invP = 1 ./ diagP. */
 int peec_set_pdiag(peec_ctx* ctx, const double* diagP);

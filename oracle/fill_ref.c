@@ -53,6 +53,8 @@
 #define SQRT sqrtl
 #define LOG logl
 #define ATAN2 atan2l
+#define ATAN atanl
+#define ASINH asinhl
 #define FABS fabsl
 #define RINT nearbyintl
 #define ISFIN isfinite
@@ -60,6 +62,8 @@
 #define SQRT sqrt
 #define LOG log
 #define ATAN2 atan2
+#define ATAN atan
+#define ASINH asinh
 #define FABS fabs
 #define RINT nearbyint
 #define ISFIN isfinite
@@ -154,9 +158,12 @@ static REAL line_point(const REAL* xv, REAL y3, REAL z3, REAL x1, REAL y1, REAL 
 }
 
 /* integ_point_sup_fft / _P (compute_Lp_Voxels.jl:469-489): point, surface in the
- * (x, y) plane at z2 */
+ * (x, y) plane at z2. pform 3: integ_point_sup_sharedRis
+ * (sharedRis/Song_improved_Ivana_strategy.jl:449-478), whose arctangent takes the
+ * quotient, atan(X*Y / (|Z| R)) (NaN when both vanish: the point in the surface's plane,
+ * on a corner's line) */
 static REAL point_sup(REAL x1, REAL y1, REAL z1, const REAL* x2v, const REAL* y2v, REAL z2,
-                      REAL* acc) {
+                      int pform, REAL* acc) {
   REAL sol = 0;
   for (int c1 = 0; c1 < 2; ++c1)
     for (int c2 = 0; c2 < 2; ++c2) {
@@ -164,7 +171,8 @@ static REAL point_sup(REAL x1, REAL y1, REAL z1, const REAL* x2v, const REAL* y2
       REAL R = SQRT(X * X + Y * Y + Z * Z);
       REAL t1 = fin(X * lg(Y + R));
       REAL t2 = fin(Y * lg(X + R));
-      REAL t3 = -FABS(Z) * ATAN2(X * Y, FABS(Z) * R);
+      REAL t3 = pform == 3 ? -FABS(Z) * ATAN(X * Y / (FABS(Z) * R))
+                           : -FABS(Z) * ATAN2(X * Y, FABS(Z) * R);
       sol += sgnp(c1 + c2) * (t1 + t2 + t3);
       *acc += FABS(t1) + FABS(t2) + FABS(t3);
     }
@@ -173,8 +181,8 @@ static REAL point_sup(REAL x1, REAL y1, REAL z1, const REAL* x2v, const REAL* y2
 
 /* integ_line_line_sp_fft (compute_Lp_Voxels.jl:514-529) and integ_line_line_sp_P
  * (compute_row_P_sup.jl:461-476), collinear lines. As the reference writes them these
- * take absolute coordinates, not differences; pform selects the _P variant's extra
- * x1*log|x1-x2| term. */
+ * take absolute coordinates, not differences; pform 1 selects the _P variant's extra
+ * x1*log|x1-x2| term, pform >= 2 the forms that put it inside the (x1-x2)/R factor. */
 static REAL ll_sp(const REAL* x1v, const REAL* x2v, int pform, REAL* acc) {
   REAL sol = 0;
   for (int c1 = 0; c1 < 2; ++c1)
@@ -182,8 +190,10 @@ static REAL ll_sp(const REAL* x1v, const REAL* x2v, int pform, REAL* acc) {
       REAL x1 = x1v[c1], x2 = x2v[c2];
       REAL R = SQRT((x1 - x2) * (x1 - x2));
       REAL t1;
-      if (pform == 2) /* integ_line_line_sp (compute_Lp_Voxels_QS.jl:501-520): the
-                         x1*log|x1-x2| term inside the (x1-x2)/R factor */
+      if (pform >= 2) /* integ_line_line_sp (compute_Lp_Voxels_QS.jl:501-520) and the
+                         sharedRis forms (Song_improved_Ivana_strategy.jl:510-532,
+                         Song_P_improved_Ivana_strategy.jl:360-382): the x1*log|x1-x2|
+                         term inside the (x1-x2)/R factor */
         t1 = (x1 - x2) / R * (x1 - x2 * lg(x2 - x1) + x1 * lg(x1 - x2));
       else {
         t1 = (x1 - x2) / R * (x1 - x2 * lg(x2 - x1));
@@ -381,9 +391,10 @@ static REAL ss_ortho(const REAL* x1v, const REAL* y1v, REAL z1, const REAL* x2v,
   return sol;
 }
 
-/* integ_vol_surf_fft (compute_Lp_Voxels.jl:728-764) and, with pform == 2,
- * integ_vol_surf (compute_Lp_Voxels_QS.jl:777-824, whose second and third terms carry an
- * extra factor (z1 - z2)): volume, surface in the (x, y) plane at z2 */
+/* integ_vol_surf_fft (compute_Lp_Voxels.jl:728-764) and, with pform 2 or 3,
+ * integ_vol_surf (compute_Lp_Voxels_QS.jl:777-824) / integ_vol_surf_sharedRis
+ * (Song_improved_Ivana_strategy.jl:818-868), whose second and third terms carry an
+ * extra factor (z1 - z2): volume, surface in the (x, y) plane at z2 */
 static REAL vol_surf(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REAL* x2v,
                      const REAL* y2v, REAL z2, int pform, REAL* acc) {
   REAL sol = 0;
@@ -396,9 +407,9 @@ static REAL vol_surf(const REAL* x1v, const REAL* y1v, const REAL* z1v, const RE
             REAL X2 = X * X, Y2 = Y * Y, Z2 = Z * Z;
             REAL R = SQRT(X2 + Y2 + Z2);
             REAL t1 = (Z2 / 12 - (X2 + Y2) / 8) * Z * R;
-            REAL t2 = pform == 2 ? fin((Y2 / 2 - Z2 / 6) * X * Z * lg(X + R))
+            REAL t2 = (pform == 2 || pform == 3) ? fin((Y2 / 2 - Z2 / 6) * X * Z * lg(X + R))
                                  : fin((Y2 / 2 - Z2 / 6) * X * lg(X + R));
-            REAL t3 = pform == 2 ? fin((X2 / 2 - Z2 / 6) * Y * Z * lg(Y + R))
+            REAL t3 = (pform == 2 || pform == 3) ? fin((X2 / 2 - Z2 / 6) * Y * Z * lg(Y + R))
                                  : fin((X2 / 2 - Z2 / 6) * Y * lg(Y + R));
             REAL t4 = fin((-(X2 * X2) / 24 - (Y2 * Y2) / 24 + (Y2 * X2) / 4) * lg(Z + R));
             REAL t5 = -(FABS(X) * FABS(X) * FABS(X)) * Y / 6 * ATAN2(Y * Z, FABS(X) * R);
@@ -462,7 +473,12 @@ static void lp_supp(const REAL* x1v, const REAL* y1v, const REAL* z1v, const REA
  * integ_line_surf_ortho, its own integ_line_line_sp and integ_vol_surf, and in the
  * orthogonal surface-surface case a call whose arguments Julia cannot apply (an
  * interval where the primitive takes a coordinate, compute_Lp_Voxels_QS.jl:330-352):
- * that entry returns NaN and the row driver counts it. */
+ * that entry returns NaN and the row driver counts it. pform 3 is the dense RIS Lp tree
+ * (Song_improved_Ivana_strategy2, sharedRis/Song_improved_Ivana_strategy.jl:1-404): the
+ * Rcc tree's primitives, with the seven-term orthogonal surface-surface form and the
+ * one-argument arctangent of integ_point_sup_sharedRis. pform 4 is the dense RIS P tree
+ * (Song_P_improved_Ivana_strategy, sharedRis/Song_P_improved_Ivana_strategy.jl:1-256):
+ * the _P primitives with the collinear-line form of pform 2. */
 static REAL integ_bodies(const REAL* x1v, const REAL* y1v, const REAL* z1v, REAL xc1, REAL yc1,
                          REAL zc1, REAL a1, REAL b1, REAL c1, const REAL* x2v, const REAL* y2v,
                          const REAL* z2v, REAL xc2, REAL yc2, REAL zc2, REAL a2, REAL b2,
@@ -495,13 +511,13 @@ static REAL integ_bodies(const REAL* x1v, const REAL* y1v, const REAL* z1v, REAL
     case 4: {
       REAL v;
       if (n1 == 3) { /* point-surface */
-        if (s2[0]) { w = V1 * a2; v = point_sup(zc1, yc1, xc1, z2v, y2v, xc2, acc); }
-        else if (s2[1]) { w = V1 * b2; v = point_sup(xc1, zc1, yc1, x2v, z2v, yc2, acc); }
-        else { w = V1 * c2; v = point_sup(xc1, yc1, zc1, x2v, y2v, zc2, acc); }
+        if (s2[0]) { w = V1 * a2; v = point_sup(zc1, yc1, xc1, z2v, y2v, xc2, pform, acc); }
+        else if (s2[1]) { w = V1 * b2; v = point_sup(xc1, zc1, yc1, x2v, z2v, yc2, pform, acc); }
+        else { w = V1 * c2; v = point_sup(xc1, yc1, zc1, x2v, y2v, zc2, pform, acc); }
       } else if (n2 == 3) {
-        if (s1[0]) { w = V2 * a1; v = point_sup(zc2, yc2, xc2, z1v, y1v, xc1, acc); }
-        else if (s1[1]) { w = V2 * b1; v = point_sup(xc2, zc2, yc2, x1v, z1v, yc1, acc); }
-        else { w = V2 * c1; v = point_sup(xc2, yc2, zc2, x1v, y1v, zc1, acc); }
+        if (s1[0]) { w = V2 * a1; v = point_sup(zc2, yc2, xc2, z1v, y1v, xc1, pform, acc); }
+        else if (s1[1]) { w = V2 * b1; v = point_sup(xc2, zc2, yc2, x1v, z1v, yc1, pform, acc); }
+        else { w = V2 * c1; v = point_sup(xc2, yc2, zc2, x1v, y1v, zc1, pform, acc); }
       } else if (s1[1] && s1[2]) { /* line-line, line 1 along x */
         if (s2[1] && s2[2]) { w = b1 * c1 * b2 * c2; v = ll_parall(x1v, yc1, zc1, x2v, yc2, zc2, pform, acc); }
         else if (s2[0] && s2[2]) { w = b1 * c1 * a2 * c2; v = ll_ortho(x1v, yc1, zc1, xc2, y2v, zc2, acc); }
@@ -756,6 +772,227 @@ int64_t FN(oracle_p_row)(int caser, int caser2, const double* src, const double*
     REAL pref = (REAL)1 / ((REAL)4 * pi * eps0 * A1 * d2[0] * d2[1]);
     out[k] = (double)((REAL)escal_P * (pref * v));
     if (scale) scale[k] = (double)((REAL)escal_P * (pref * acc));
+  }
+  return bad;
+}
+
+/* ---------------------------------------------------------------------------------
+ * Dense RIS fill: sharedRis/calcola_Lp.jl and sharedRis/calcola_P.jl. Bodies are given
+ * by their vertex coordinates (a volume: 8 vertices x (x, y, z), volumi[:coordinate];
+ * a surface: 4 vertices, superfici["estremi_celle"]), rounded to 14 digits as the
+ * reference rounds them (in double in both builds, so that both see the same boxes).
+ * --------------------------------------------------------------------------------- */
+
+static double round14d(double v) { return nearbyint(v * 1e14) / 1e14; }
+
+/* isequal, which Julia's unique uses: 0.0 and -0.0 are different values */
+static int same_value(REAL a, REAL b) { return a == b && signbit(a) == signbit(b); }
+
+/* calcola_Lp.jl:22-28,43-47: per axis the first and the last entry of
+ * unique(round.(coords[[min indices; max indices]], digits=14)), in that order */
+static const int RIS_VOL_IDX[3][8] = {{0, 6, 12, 18, 3, 9, 15, 21},
+                                      {1, 4, 13, 16, 7, 10, 19, 22},
+                                      {2, 5, 8, 11, 14, 17, 20, 23}};
+
+static void ris_vol_box(const double* c24, REAL iv[3][2]) {
+  for (int d = 0; d < 3; ++d) {
+    REAL v[8];
+    for (int i = 0; i < 8; ++i) v[i] = (REAL)round14d(c24[RIS_VOL_IDX[d][i]]);
+    REAL last = v[0];
+    for (int i = 1; i < 8; ++i) {
+      int seen = 0;
+      for (int j = 0; j < i; ++j) seen |= same_value(v[i], v[j]);
+      if (!seen) last = v[i];
+    }
+    iv[d][0] = v[0];
+    iv[d][1] = last;
+  }
+}
+
+/* mean_length_rev (sharedRis/Compute_Lp_Self.jl:39-74): distance between the centroids of
+ * the two end faces of the brick along curr_dir (1, 2, 3) */
+static REAL mean_length_rev(const double* c24, int dir) {
+  static const int ends[3][2][4] = {{{0, 2, 4, 6}, {1, 3, 5, 7}},
+                                    {{0, 1, 4, 5}, {2, 3, 6, 7}},
+                                    {{0, 1, 2, 3}, {4, 5, 6, 7}}};
+  REAL d2 = 0;
+  for (int k = 0; k < 3; ++k) {
+    REAL a = 0, b = 0;
+    for (int i = 0; i < 4; ++i) {
+      a = a + (REAL)c24[3 * ends[dir - 1][0][i] + k];
+      b = b + (REAL)c24[3 * ends[dir - 1][1][i] + k];
+    }
+    REAL e = (REAL)0.25 * a - (REAL)0.25 * b;
+    d2 += e * e;
+  }
+  return SQRT(d2);
+}
+
+/* Compute_Lp_Self (sharedRis/Compute_Lp_Self.jl:1-37), the closed-form self inductance of
+ * a rectangular bar of length l, width W, thickness T; 0 when 1/(l W T) is not finite.
+ * *mag gets the sum of the magnitudes of its five groups times the prefactor. */
+static REAL lp_self(REAL l, REAL W, REAL T, REAL* mag) {
+  const REAL pi = 3.14159265358979323846264338327950288L;
+  REAL inv = (REAL)1 / (l * W * T);
+  *mag = 0;
+  if (!ISFIN(inv)) return 0;
+  REAL w = W / l, t = T / l;
+  REAL r = SQRT(w * w + t * t), aw = SQRT(w * w + 1), at = SQRT(t * t + 1);
+  REAL ar = SQRT(w * w + t * t + 1);
+  REAL mu0 = 4 * pi * (REAL)1e-7;
+  REAL g1 = (REAL)1 / 4 * ((REAL)1 / w * ASINH(w / at) + (REAL)1 / t * ASINH(t / aw) + ASINH((REAL)1 / r));
+  REAL g2 = (REAL)1 / 24 *
+            (t * t / w * ASINH(w / (t * at * (r + ar))) + w * w / t * ASINH(t / (w * aw * (r + ar))) +
+             t * t / (w * w) * ASINH(w * w / (t * r * (at + ar))) +
+             w * w / (t * t) * ASINH(t * t / (w * r * (aw + ar))) +
+             (REAL)1 / (w * (t * t)) * ASINH(w * (t * t) / (at * (aw + ar))) +
+             (REAL)1 / (t * (w * w)) * ASINH(t * (w * w) / (aw * (at + ar))));
+  REAL g3 = (REAL)1 / 6 *
+            ((REAL)1 / (w * t) * ATAN(w * t / ar) + t / w * ATAN(w / (t * ar)) + w / t * ATAN(t / (w * ar)));
+  REAL g4 = (REAL)1 / 60 *
+            ((ar + r + t + at) * (t * t) / ((ar + r) * (r + t) * (t + at) * (at + ar)) +
+             (ar + r + w + aw) * (w * w) / ((ar + r) * (r + w) * (w + aw) * (aw + ar)) +
+             (ar + aw + 1 + at) / ((ar + aw) * (aw + 1) * (1 + at) * (at + ar)));
+  REAL g5 = (REAL)1 / 20 * ((REAL)1 / (r + ar) + (REAL)1 / (aw + ar) + (REAL)1 / (at + ar));
+  REAL pre = 2 * mu0 * l / pi;
+  *mag = FABS(pre) * (FABS(g1) + FABS(g2) + FABS(g3) + FABS(g4) + FABS(g5));
+  return pre * (g1 + g2 - g3 - g4 - g5);
+}
+
+/* the bar dimensions (l, W, T) Compute_Lp_Self takes for a volume of current direction
+ * dir (calcola_Lp.jl:59-77) */
+static void ris_lwt(const double* c24, int dir, REAL* l, REAL* W, REAL* T) {
+  REAL m1 = FABS(mean_length_rev(c24, 1)), m2 = FABS(mean_length_rev(c24, 2)),
+       m3 = FABS(mean_length_rev(c24, 3));
+  if (dir == 1) { *l = m1; *W = m3; *T = m2; }
+  else if (dir == 2) { *T = m1; *W = m3; *l = m2; }
+  else { *W = m1; *l = m3; *T = m2; }
+}
+
+double FN(oracle_ris_lp_self)(const double* c24, int dir, double* mag) {
+  REAL l, W, T, m;
+  ris_lwt(c24, dir, &l, &W, &T);
+  REAL v = lp_self(l, W, T, &m);
+  if (mag) *mag = (double)m;
+  return (double)v;
+}
+
+/* One dense Lp block (calculate_Lp_matrix, calcola_Lp.jl:254-306): volumes off .. off+dim-1
+ * of coords (24 per volume) with cross-sections S, current direction dir (1, 2, 3).
+ * out (dim x dim, column-major, symmetric): 1e-7 / (S_m S_n) * integral * esc off the
+ * diagonal (Song_improved_Ivana_strategy2 with suppression), Compute_Lp_Self * esc on
+ * it; scale the same prefactors times the sum of |terms|. Returns the count of
+ * non-finite entries. */
+int64_t FN(oracle_ris_lp_block)(const double* coords, const double* S, int64_t off, int64_t dim,
+                                int dir, double esc, double* out, double* scale, int* forms) {
+  int64_t bad = 0;
+#pragma omp parallel for schedule(dynamic, 8) reduction(+ : bad)
+  for (int64_t m = 0; m < dim; ++m) {
+    const double* cm = coords + 24 * (off + m);
+    REAL l, W, T, mag;
+    ris_lwt(cm, dir, &l, &W, &T);
+    REAL self = lp_self(l, W, T, &mag);
+    out[m + m * dim] = (double)(self * (REAL)esc);
+    if (scale) scale[m + m * dim] = (double)(mag * FABS((REAL)esc));
+    if (!ISFIN(self)) ++bad;
+    REAL b1[3][2];
+    ris_vol_box(cm, b1);
+    for (int64_t n = m + 1; n < dim; ++n) {
+      REAL b2[3][2];
+      ris_vol_box(coords + 24 * (off + n), b2);
+      REAL acc;
+      int far = 0;
+      REAL v = lp_integ(b1[0], b1[1], b1[2], b2[0], b2[1], b2[2], 1, 3, &acc, &far);
+      if (forms) {
+        int f1[3], f2[3];
+        lp_supp(b1[0], b1[1], b1[2], b2[0], b2[1], b2[2], f1, f2);
+        forms[m + n * dim] = forms[n + m * dim] = f1[0] + f1[1] + f1[2] + f2[0] + f2[1] + f2[2];
+      }
+      REAL pre = (REAL)1e-7 / ((REAL)S[off + m] * (REAL)S[off + n]);
+      REAL e = pre * v * (REAL)esc;
+      out[m + n * dim] = out[n + m * dim] = (double)e;
+      if (scale) scale[m + n * dim] = scale[n + m * dim] = (double)(FABS(pre) * acc * FABS((REAL)esc));
+      if (!ISFIN(e)) ++bad;
+    }
+  }
+  return bad;
+}
+
+/* process_surfaces! (calcola_P.jl:94-160): the surface's box from vertices 1 and 4,
+ * rounded; the normal (the smallest extent) gets length 1 */
+static int ris_surf_box(const double* e12, REAL iv[3][2], REAL len[3]) {
+  const int lo[3] = {0, 1, 2}, hi[3] = {9, 10, 11};
+  for (int d = 0; d < 3; ++d) {
+    double a = e12[lo[d]], b = e12[hi[d]];
+    iv[d][0] = (REAL)round14d(a < b ? a : b);
+    iv[d][1] = (REAL)round14d(a < b ? b : a);
+    len[d] = FABS(iv[d][1] - iv[d][0]);
+  }
+  int nrm = 2;
+  if (len[0] <= len[1] && len[0] <= len[2]) nrm = 0;
+  else if (len[1] <= len[0] && len[1] <= len[2]) nrm = 1;
+  len[nrm] = 1;
+  return nrm;
+}
+
+/* Song_P_improved_Ivana_strategy (Song_P_improved_Ivana_strategy.jl:1-256) */
+static REAL ris_p_integ(REAL iv1[3][2], const REAL* l1, int p1, REAL iv2[3][2], const REAL* l2,
+                        int p2, REAL* acc, int* nsum) {
+  const REAL e1 = 5e-3, e2 = 1e-3, e3 = 1e-3, e4 = 3e-1;
+  REAL s1 = l1[0] * l1[1] * l1[2], s2 = l2[0] * l2[1] * l2[2];
+  REAL ax[4] = {iv1[0][0] - iv2[0][0], iv1[0][0] - iv2[0][1], iv1[0][1] - iv2[0][0], iv1[0][1] - iv2[0][1]};
+  REAL ay[4] = {iv1[1][0] - iv2[1][0], iv1[1][0] - iv2[1][1], iv1[1][1] - iv2[1][0], iv1[1][1] - iv2[1][1]};
+  REAL az[4] = {iv1[2][0] - iv2[2][0], iv1[2][0] - iv2[2][1], iv1[2][1] - iv2[2][0], iv1[2][1] - iv2[2][1]};
+  REAL mx = minabs4(ax[0], ax[1], ax[2], ax[3]), my = minabs4(ay[0], ay[1], ay[2], ay[3]),
+       mz = minabs4(az[0], az[1], az[2], az[3]);
+  REAL min_R = SQRT(mx * mx + my * my + mz * mz);
+  REAL dx = maxabs4(ax[0], ax[1], ax[2], ax[3]), dy = maxabs4(ay[0], ay[1], ay[2], ay[3]),
+       dz = maxabs4(az[0], az[1], az[2], az[3]);
+  int f1[3], f2[3];
+  f1[0] = check_pp(e1, e2, e3, e4, s1, s2, dx, min_R, l1[0], l1[1], l1[2]);
+  f2[0] = check_pp(e1, e2, e3, e4, s1, s2, dx, min_R, l2[0], l2[1], l2[2]);
+  f1[1] = check_pp(e1, e2, e3, e4, s1, s2, dy, min_R, l1[1], l1[0], l1[2]);
+  f2[1] = check_pp(e1, e2, e3, e4, s1, s2, dy, min_R, l2[1], l2[0], l2[2]);
+  f1[2] = check_pp(e1, e2, e3, e4, s1, s2, dz, min_R, l1[2], l1[0], l1[1]);
+  f2[2] = check_pp(e1, e2, e3, e4, s1, s2, dz, min_R, l2[2], l2[0], l2[1]);
+  f1[p1] = 1;
+  f2[p2] = 1;
+  *nsum = f1[0] + f1[1] + f1[2] + f2[0] + f2[1] + f2[2];
+  REAL c1[3], c2[3];
+  for (int d = 0; d < 3; ++d) {
+    c1[d] = (REAL)0.5 * (iv1[d][1] + iv1[d][0]);
+    c2[d] = (REAL)0.5 * (iv2[d][1] + iv2[d][0]);
+  }
+  return integ_bodies(iv1[0], iv1[1], iv1[2], c1[0], c1[1], c1[2], l1[0], l1[1], l1[2], iv2[0],
+                      iv2[1], iv2[2], c2[0], c2[1], c2[2], l2[0], l2[1], l2[2], f1, f2, 4, acc);
+}
+
+/* The dense P (calculate_P_matrix, calcola_P.jl:162-222): surfaces ends (12 per surface),
+ * areas S; out (ns x ns, column-major, symmetric) = integral / (4 pi eps0 S_m S_n) * esc,
+ * the diagonal included; scale and forms (2: surface-surface .. 6) as for the Lp block.
+ * Returns the count of non-finite entries. */
+int64_t FN(oracle_ris_p)(const double* ends, const double* S, int64_t ns, double esc, double* out,
+                         double* scale, int* forms) {
+  const REAL eps0 = 8.854187816997944e-12L;
+  const REAL pi = 3.14159265358979323846264338327950288L;
+  int64_t bad = 0;
+#pragma omp parallel for schedule(dynamic, 8) reduction(+ : bad)
+  for (int64_t m = 0; m < ns; ++m) {
+    REAL iv1[3][2], l1[3];
+    int p1 = ris_surf_box(ends + 12 * m, iv1, l1);
+    for (int64_t n = m; n < ns; ++n) {
+      REAL iv2[3][2], l2[3];
+      int p2 = ris_surf_box(ends + 12 * n, iv2, l2);
+      REAL acc;
+      int nsum;
+      REAL v = ris_p_integ(iv1, l1, p1, iv2, l2, p2, &acc, &nsum);
+      if (forms) forms[m + n * ns] = forms[n + m * ns] = nsum;
+      REAL inv = (REAL)1 / (4 * pi * eps0 * (REAL)S[m] * (REAL)S[n]);
+      REAL e = inv * v * (REAL)esc;
+      out[m + n * ns] = out[n + m * ns] = (double)e;
+      if (scale) scale[m + n * ns] = scale[n + m * ns] = (double)(FABS(inv) * acc * FABS((REAL)esc));
+      if (!ISFIN(e)) ++bad;
+    }
   }
   return bad;
 }

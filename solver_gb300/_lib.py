@@ -20,7 +20,8 @@ ERRORS = {-1: "PEEC_ERR_CUDA", -2: "PEEC_ERR_OOM", -3: "PEEC_ERR_CANCELLED",
 # every symbol declared in include/peec_gb300.h
 EXPORTS = ("peec_version", "peec_ctx_create", "peec_ctx_destroy", "peec_last_error",
            "peec_set_topology", "peec_set_incidence", "peec_set_dense", "peec_set_dense_rcc",
-           "peec_set_dense_rcc_frequency", "peec_set_edge_state",
+           "peec_set_dense_rcc_frequency", "peec_ris_fill", "peec_dense_get",
+           "peec_set_edge_state",
            "peec_set_frequency_device", "peec_set_pdiag", "peec_set_rows", "peec_fill",
            "peec_set_frequency", "peec_matvec", "peec_matvec_dev", "peec_port_rhs",
            "peec_gmres", "peec_solve_mixed", "peec_set_stop_flag", "peec_set_device_loop",
@@ -86,6 +87,9 @@ def load(build_if_missing: bool = True):
     L.peec_set_dense.argtypes = [P, P, P, P, P]
     L.peec_set_dense_rcc.argtypes = [P, P, P, P, P]
     L.peec_set_dense_rcc_frequency.argtypes = [P, ctypes.c_double]
+    L.peec_ris_fill.argtypes = [P, P, P, P, ctypes.c_double, P, P, P, ctypes.c_double,
+                                ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]
+    L.peec_dense_get.argtypes = [P, ctypes.c_int, ctypes.c_int, P]
     L.peec_set_edge_state.argtypes = [P, P, P, P, P, P, ctypes.c_int64, ctypes.c_double,
                                       ctypes.c_double]
     L.peec_set_frequency_device.argtypes = [P, ctypes.c_double, ctypes.c_int64, P, P, P]

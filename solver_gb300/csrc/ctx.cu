@@ -110,6 +110,13 @@ int rcc_rows_gpu(const double origin[3], double sx, double sy, double sz, int Nx
 int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, double escal_Lp,
                   double escal_P, int Nx, int Ny, int Nz, double* const d_rows[9],
                   const int64_t row_len[9], int* d_bad, cudaStream_t st);
+size_t ris_box_bytes();
+int ris_prep_gpu(int surfaces, const double* d_geom, int64_t count, int64_t mx, int64_t my,
+                 void* boxes, double* self, int* nrm, cudaStream_t st);
+int ris_pairs_gpu(int kind, const void* boxes, const int* nrm, const double* S, const double* self,
+                  int64_t dim, double esc, double* M, int64_t ld, int* d_bad, cudaStream_t st);
+int ris_dist_gpu(const double* d_ctr, int64_t dim, double* R, int64_t ld, cudaStream_t st);
+int inv_diag_gpu(const double* M, int64_t ld, int64_t n, double* inv, cudaStream_t st);
 void launch_adjoint(const c64*, const int32_t*, const int32_t*, const c64*, const c64*, double,
                     int64_t, int64_t, double*, cudaStream_t);
 int selftest_wait_limit(int limit, cudaStream_t st, int* err_out);
@@ -160,6 +167,9 @@ struct peec_ctx {
   // blocks times exp(-j beta R) of the installed frequency (FP64 and FP32 copies)
   bool dense_rcc = false, dense_rcc_ready = false;
   double* dnR[4] = {nullptr, nullptr, nullptr, nullptr};
+  // which blocks hold a matrix / distances (peec_set_dense, peec_set_dense_rcc, peec_ris_fill)
+  bool dn_set[4] = {false, false, false, false};
+  bool dnR_set[4] = {false, false, false, false};
   c64* dnc64[4] = {nullptr, nullptr, nullptr, nullptr};
   c32* dnc32[4] = {nullptr, nullptr, nullptr, nullptr};
   // topology
@@ -767,6 +777,7 @@ static int peec_set_incidence_body(peec_ctx* ctx, int64_t mx, int64_t my, int64_
   ctx->rcc_freq = -1.0;
   ctx->lattice = false;
   ctx->dense = false;
+  for (int b = 0; b < 4; ++b) ctx->dn_set[b] = ctx->dnR_set[b] = false;
   return alloc_work(ctx);
 }
 
@@ -808,6 +819,10 @@ static int peec_set_dense_body(peec_ctx* ctx, const double* Lpx, const double* L
   }
   CTX_TRY(dalloc(&ctx->dn_part, part));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  for (int b = 0; b < 4; ++b) {
+    ctx->dn_set[b] = true;
+    ctx->dnR_set[b] = false;
+  }
   ctx->dense = true;
   ctx->have_spec = true;
   return PEEC_OK;
@@ -856,15 +871,24 @@ static int peec_set_dense_rcc_body(peec_ctx* ctx, const double* Rx, const double
   }
   CTX_TRY(dalloc(&ctx->dn_part, std::max(part, (size_t)1)));
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+  for (int b = 0; b < 4; ++b) ctx->dnR_set[b] = true;
   ctx->dense_rcc = true;
   return PEEC_OK;
 }
 
 // the retarded blocks at beta = 2 pi f sqrt(eps0 mu0) (f in Hz): formed in place, so the
-// captured graphs of the context stay valid
+// captured graphs of the context stay valid. A context whose distances are on the device
+// but which was switched back to the quasi-static blocks (peec_set_dense_rcc with NULLs)
+// returns to the retarded operator here.
 static int peec_set_dense_rcc_frequency_body(peec_ctx* ctx, double beta) {
   if (!ctx) return badarg("peec_set_dense_rcc_frequency");
-  if (!ctx->dense_rcc) return bad(ctx, PEEC_ERR_STATE, "no dense distances (peec_set_dense_rcc)");
+  if (!ctx->dense_rcc) {
+    if (!ctx->dense || !ctx->dnR_set[0] || !ctx->dnR_set[1] || !ctx->dnR_set[2] || !ctx->dnR_set[3])
+      return bad(ctx, PEEC_ERR_STATE, "no dense distances (peec_set_dense_rcc)");
+    drop_graphs(ctx);
+    ctx->dense_rcc = true;
+    ctx->dense_rcc_ready = false;
+  }
   PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
   const int64_t sz[4] = {ctx->mx, ctx->my, ctx->mz, ctx->ns};
   for (int b = 0; b < 4; ++b) {
@@ -874,6 +898,152 @@ static int peec_set_dense_rcc_frequency_body(peec_ctx* ctx, double beta) {
   ctx->launches += 4;
   PEEC_CUDA_TRY(cudaGetLastError());
   ctx->dense_rcc_ready = true;
+  return PEEC_OK;
+}
+
+// The dense RIS matrices filled on the device (sharedRis/calcola_Lp.jl, calcola_P.jl)
+// from the bodies' vertex coordinates, in place of peec_set_dense (+ peec_set_pdiag, and
+// peec_set_dense_rcc with distances): vol_coords (m x 24, row-major: volumi[:coordinate]),
+// vol_S (m, the cross-sections volumi[:S]), vol_centres (m x 3, volumi[:centri], read when
+// distances); surf_ends (ns x 12, superfici["estremi_celle"]), surf_S (ns, superfici["S"]),
+// surf_centres (ns x 3, superfici["centri"]). Either group may be NULL (its blocks are left
+// as they are). *nonfinite (if given) gets the count of non-finite matrix entries.
+static int peec_ris_fill_body(peec_ctx* ctx, const double* vol_coords, const double* vol_S,
+                              const double* vol_centres, double escal_Lp, const double* surf_ends,
+                              const double* surf_S, const double* surf_centres, double escal_P,
+                              int distances, int64_t* nonfinite) {
+  NvtxRange nvtx_range_("peec_ris_fill");
+  if (!ctx) return badarg("peec_ris_fill");
+  if (!ctx->have_topo || ctx->lattice)
+    return bad(ctx, PEEC_ERR_STATE, "peec_ris_fill: needs the topology of peec_set_incidence");
+  const bool vol = vol_coords != nullptr, surf = surf_ends != nullptr;
+  if (!vol && !surf) return bad(ctx, PEEC_ERR_BADARG, "peec_ris_fill: no volumes and no surfaces");
+  if ((vol && ctx->m > 0 && (!vol_S || (distances && !vol_centres))) ||
+      (surf && ctx->ns > 0 && (!surf_S || (distances && !surf_centres))))
+    return bad(ctx, PEEC_ERR_BADARG, "peec_ris_fill: missing cross-sections, areas or centres");
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  drop_graphs(ctx);
+  ctx->dense = false;
+  ctx->dense_rcc = ctx->dense_rcc_ready = false;
+  const int64_t sz[4] = {ctx->mx, ctx->my, ctx->mz, ctx->ns};
+  const int64_t off[3] = {0, ctx->mx, ctx->mx + ctx->my};
+  const size_t bb = ris_box_bytes();
+  double *d_geom = nullptr, *d_S = nullptr, *d_ctr = nullptr, *d_self = nullptr;
+  unsigned char* d_box = nullptr;
+  int* d_nrm = nullptr;
+  int* d_bad = nullptr;
+  auto release = [&] {
+    for (void* p : {(void*)d_geom, (void*)d_S, (void*)d_ctr, (void*)d_self, (void*)d_box,
+                    (void*)d_nrm, (void*)d_bad})
+      if (p) cudaFree(p);
+  };
+  int rc = PEEC_OK;
+  auto put = [&](double** d, const double* h, size_t cnt) -> int {
+    int r = dalloc(d, cnt);
+    if (r) return r;
+    if (cnt) PEEC_CUDA_TRY(cudaMemcpyAsync(*d, h, cnt * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    return PEEC_OK;
+  };
+  auto block = [&](int b) -> int {
+    const int64_t ld = dense_ld(sz[b]);
+    ctx->dn_ld[b] = ld;
+    const size_t cnt = (size_t)ld * (size_t)sz[b];
+    int r = dalloc(&ctx->dn64[b], cnt);
+    if (!r) r = dalloc(&ctx->dn32[b], cnt);
+    if (r) return r;
+    if (cnt) PEEC_CUDA_TRY(cudaMemsetAsync(ctx->dn64[b], 0, sizeof(double) * cnt, ctx->st));
+    if (distances) {
+      r = dalloc(&ctx->dnR[b], cnt);
+      if (!r) r = dalloc(&ctx->dnc64[b], cnt);
+      if (!r) r = dalloc(&ctx->dnc32[b], cnt);
+      if (r) return r;
+      if (cnt) PEEC_CUDA_TRY(cudaMemsetAsync(ctx->dnR[b], 0, sizeof(double) * cnt, ctx->st));
+    }
+    return PEEC_OK;
+  };
+  rc = [&]() -> int {
+    if ((rc = dalloc(&d_bad, 1))) return rc;
+    PEEC_CUDA_TRY(cudaMemsetAsync(d_bad, 0, sizeof(int), ctx->st));
+    if (vol) {
+      const int64_t m = ctx->m;
+      if ((rc = put(&d_geom, vol_coords, (size_t)m * 24)) || (rc = put(&d_S, vol_S, (size_t)m)) ||
+          (distances && (rc = put(&d_ctr, vol_centres, (size_t)m * 3))) ||
+          (rc = dalloc(&d_self, (size_t)m)) || (rc = dalloc(&d_box, (size_t)m * bb)))
+        return rc;
+      if ((rc = ris_prep_gpu(0, d_geom, m, ctx->mx, ctx->my, d_box, d_self, nullptr, ctx->st))) return rc;
+      for (int b = 0; b < 3 && !rc; ++b) {
+        if ((rc = block(b))) return rc;
+        rc = ris_pairs_gpu(0, d_box + (size_t)off[b] * bb, nullptr, d_S + off[b], d_self + off[b],
+                           sz[b], escal_Lp, ctx->dn64[b], ctx->dn_ld[b], d_bad, ctx->st);
+        if (!rc && distances)
+          rc = ris_dist_gpu(d_ctr + 3 * off[b], sz[b], ctx->dnR[b], ctx->dn_ld[b], ctx->st);
+        if (!rc && sz[b])
+          dense_round(ctx->dn64[b], (size_t)ctx->dn_ld[b] * sz[b], ctx->dn32[b], ctx->st);
+        ctx->dn_set[b] = !rc;
+        ctx->dnR_set[b] = !rc && distances;
+      }
+      if (rc) return rc;
+    }
+    if (surf) {
+      const int64_t ns = ctx->ns;
+      if ((rc = put(&d_geom, surf_ends, (size_t)ns * 12)) || (rc = put(&d_S, surf_S, (size_t)ns)) ||
+          (distances && (rc = put(&d_ctr, surf_centres, (size_t)ns * 3))) ||
+          (rc = dalloc(&d_nrm, (size_t)ns)) || (rc = dalloc(&d_box, (size_t)ns * bb)))
+        return rc;
+      if ((rc = ris_prep_gpu(1, d_geom, ns, 0, 0, d_box, nullptr, d_nrm, ctx->st))) return rc;
+      if ((rc = block(3))) return rc;
+      rc = ris_pairs_gpu(1, d_box, d_nrm, d_S, nullptr, ns, escal_P, ctx->dn64[3], ctx->dn_ld[3],
+                         d_bad, ctx->st);
+      if (!rc && distances) rc = ris_dist_gpu(d_ctr, ns, ctx->dnR[3], ctx->dn_ld[3], ctx->st);
+      if (!rc && ns) dense_round(ctx->dn64[3], (size_t)ctx->dn_ld[3] * ns, ctx->dn32[3], ctx->st);
+      if (!rc) rc = dalloc(&ctx->invP, (size_t)ns);
+      if (!rc) rc = inv_diag_gpu(ctx->dn64[3], ctx->dn_ld[3], ns, ctx->invP, ctx->st);
+      ctx->dn_set[3] = !rc;
+      ctx->dnR_set[3] = !rc && distances;
+      if (rc) return rc;
+      ctx->have_pdiag = true;
+    }
+    size_t part = 1;
+    for (int b = 0; b < 4; ++b) {
+      part = std::max(part, (size_t)dense_chunks(sz[b]) * (size_t)std::max<int64_t>(sz[b], 1));
+      if (distances) part = std::max(part, (size_t)dense_part_c(sz[b]));
+    }
+    if ((rc = dalloc(&ctx->dn_part, part))) return rc;
+    int hbad = 0;
+    PEEC_CUDA_TRY(cudaMemcpyAsync(&hbad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
+    if (nonfinite) *nonfinite = hbad;
+    return PEEC_OK;
+  }();
+  release();
+  if (rc) return rc;
+  ctx->dense = ctx->dn_set[0] && ctx->dn_set[1] && ctx->dn_set[2] && ctx->dn_set[3];
+  ctx->have_spec = ctx->dense;
+  ctx->dense_rcc = ctx->dense && ctx->dnR_set[0] && ctx->dnR_set[1] && ctx->dnR_set[2] &&
+                   ctx->dnR_set[3];
+  return PEEC_OK;
+}
+
+// One dense block back to the host (column-major, n x n): what 0 the matrix, 1 its centre
+// distances, 2 its diagonal (n values). block 0..2: Lp_x, Lp_y, Lp_z; 3: P.
+static int peec_dense_get_body(peec_ctx* ctx, int block, int what, double* out) {
+  if (!ctx) return badarg("peec_dense_get");
+  if (block < 0 || block > 3 || what < 0 || what > 2 || !out)
+    return bad(ctx, PEEC_ERR_BADARG, "peec_dense_get: block 0..3, what 0..2, out required");
+  if (!ctx->dn_set[block] || (what == 1 && !ctx->dnR_set[block]))
+    return bad(ctx, PEEC_ERR_STATE, "peec_dense_get: block not set");
+  const int64_t n = block < 3 ? (block == 0 ? ctx->mx : (block == 1 ? ctx->my : ctx->mz)) : ctx->ns;
+  if (n == 0) return PEEC_OK;
+  PEEC_CUDA_TRY(cudaSetDevice(ctx->dev));
+  const int64_t ld = ctx->dn_ld[block];
+  const double* src = what == 1 ? ctx->dnR[block] : ctx->dn64[block];
+  if (what == 2)
+    PEEC_CUDA_TRY(cudaMemcpy2DAsync(out, sizeof(double), src, sizeof(double) * (ld + 1),
+                                    sizeof(double), n, cudaMemcpyDeviceToHost, ctx->st));
+  else
+    PEEC_CUDA_TRY(cudaMemcpy2DAsync(out, sizeof(double) * n, src, sizeof(double) * ld,
+                                    sizeof(double) * n, n, cudaMemcpyDeviceToHost, ctx->st));
+  PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   return PEEC_OK;
 }
 
@@ -3063,6 +3233,20 @@ extern "C" int peec_set_incidence(peec_ctx* ctx, int64_t mx, int64_t my, int64_t
 extern "C" int peec_set_dense(peec_ctx* ctx, const double* Lp_x, const double* Lp_y,
                               const double* Lp_z, const double* P) {
   return guarded(ctx, "peec_set_dense", [&] { return peec_set_dense_body(ctx, Lp_x, Lp_y, Lp_z, P); });
+}
+
+extern "C" int peec_ris_fill(peec_ctx* ctx, const double* vol_coords, const double* vol_S,
+                             const double* vol_centres, double escal_Lp, const double* surf_ends,
+                             const double* surf_S, const double* surf_centres, double escal_P,
+                             int distances, int64_t* nonfinite) {
+  return guarded(ctx, "peec_ris_fill", [&] {
+    return peec_ris_fill_body(ctx, vol_coords, vol_S, vol_centres, escal_Lp, surf_ends, surf_S,
+                              surf_centres, escal_P, distances, nonfinite);
+  });
+}
+
+extern "C" int peec_dense_get(peec_ctx* ctx, int block, int what, double* out) {
+  return guarded(ctx, "peec_dense_get", [&] { return peec_dense_get_body(ctx, block, what, out); });
 }
 
 extern "C" int peec_set_edge_state(peec_ctx* ctx, const double* R4, const double* Cd4,

@@ -24,6 +24,8 @@
 // Lattice centres are recomputed from the origin with the reference's expression
 // order (build_center_P_Voxels.jl:15-80, build_centers_Lp_with_air.jl:1-60).
 #include <math.h>
+
+#include <algorithm>
 #include <math_constants.h>
 
 #include "ctx.hpp"
@@ -130,16 +132,19 @@ __device__ double line_point(const double* xv, double y3, double z3, double x1, 
   return Ip;
 }
 
-// point (x1, y1, z1) against the surface [x2v] x [y2v] at height z2
+// point (x1, y1, z1) against the surface [x2v] x [y2v] at height z2; pform 3 (the dense
+// RIS Lp tree, integ_point_sup_sharedRis, Song_improved_Ivana_strategy.jl:449-478) takes
+// the arctangent of the quotient, NaN where both of its parts vanish
 __device__ double point_sup(double x1, double y1, double z1, const double* x2v, const double* y2v,
-                            double z2) {
+                            double z2, int pform) {
   double sol = 0.0;
   for (int c = 0; c < 4; ++c) {
     const int c1 = c >> 1, c2 = c & 1;
     const double X = x1 - x2v[c1], Y = y1 - y2v[c2], Z = z1 - z2;
     const double R = sqrt(X * X + Y * Y + Z * Z);
-    sol += sgn(c1 + c2) *
-           (fin(X * lgc(Y + R)) + fin(Y * lgc(X + R)) - fabs(Z) * atan2(X * Y, fabs(Z) * R));
+    const double t3 = pform == 3 ? -fabs(Z) * atan(X * Y / (fabs(Z) * R))
+                                 : -fabs(Z) * atan2(X * Y, fabs(Z) * R);
+    sol += sgn(c1 + c2) * (fin(X * lgc(Y + R)) + fin(Y * lgc(X + R)) + t3);
   }
   return sol;
 }
@@ -152,7 +157,9 @@ __device__ double ll_sp(const double* x1v, const double* x2v, int pform) {
     const double x1 = x1v[c1], x2 = x2v[c2];
     const double R = sqrt((x1 - x2) * (x1 - x2));
     double t;
-    if (pform == 2)  // integ_line_line_sp of compute_Lp_Voxels_QS.jl:501-520
+    if (pform >= 2)  // integ_line_line_sp of compute_Lp_Voxels_QS.jl:501-520 and the dense
+                     // RIS forms (Song_improved_Ivana_strategy.jl:510-532,
+                     // Song_P_improved_Ivana_strategy.jl:360-382)
       t = (x1 - x2) / R * (x1 - x2 * lgc(x2 - x1) + x1 * lgc(x1 - x2));
     else {
       t = (x1 - x2) / R * (x1 - x2 * lgc(x2 - x1));
@@ -286,9 +293,9 @@ __device__ double vol_surf(const double* x1v, const double* y1v, const double* z
     const double R = sqrt(X2 + Y2 + Z2);
     const double aX = fabs(X), aY = fabs(Y);
     const double t1 = (Z2 / 12 - (X2 + Y2) / 8) * Z * R;
-    const double t2 = pform == 2 ? fin((Y2 / 2 - Z2 / 6) * X * Z * lgc(X + R))
+    const double t2 = (pform == 2 || pform == 3) ? fin((Y2 / 2 - Z2 / 6) * X * Z * lgc(X + R))
                                  : fin((Y2 / 2 - Z2 / 6) * X * lgc(X + R));
-    const double t3 = pform == 2 ? fin((X2 / 2 - Z2 / 6) * Y * Z * lgc(Y + R))
+    const double t3 = (pform == 2 || pform == 3) ? fin((X2 / 2 - Z2 / 6) * Y * Z * lgc(Y + R))
                                  : fin((X2 / 2 - Z2 / 6) * Y * lgc(Y + R));
     const double t4 = fin((-(X2 * X2) / 24 - (Y2 * Y2) / 24 + (Y2 * X2) / 4) * lgc(Z + R));
     const double t5 = -(aX * aX * aX) * Y / 6 * atan2(Y * Z, aX * R);
@@ -325,7 +332,11 @@ __device__ __forceinline__ int shut_axis(const Box& b) { return b.s[0] ? 0 : (b.
 // pform 2 those of compute_Lp_Voxels_QS.jl). In the Rcc tree's orthogonal surface-surface
 // case the reference calls integ_surf_surf_ortho with an interval where it takes a
 // coordinate (compute_Lp_Voxels_QS.jl:330-352), which Julia cannot apply: NaN here, which
-// the row kernel reports.
+// the row kernel reports. pform 3 is the dense RIS Lp tree (Song_improved_Ivana_strategy2,
+// Song_improved_Ivana_strategy.jl:1-404): the pform 2 primitives with the seven-term
+// orthogonal surface-surface form and the quotient arctangent of the point-surface form.
+// pform 4 is the dense RIS P tree (Song_P_improved_Ivana_strategy.jl:1-256): the _P
+// primitives with the collinear-line form of pform 2.
 __device__ __noinline__ double integ_boxes(const Box& A, const Box& B, int pform) {
   const double V1 = A.len[0] * A.len[1] * A.len[2], V2 = B.len[0] * B.len[1] * B.len[2];
   switch (A.n + B.n) {
@@ -348,7 +359,8 @@ __device__ __noinline__ double integ_boxes(const Box& A, const Box& B, int pform
         const int nrm = shut_axis(S);
         const int u = nrm == 0 ? 2 : 0, v = nrm == 1 ? 2 : 1;
         const double Vp = A.n == 3 ? V1 : V2;
-        return Vp * S.len[nrm] * point_sup(P.c[u], P.c[v], P.c[nrm], S.iv[u], S.iv[v], S.c[nrm]);
+        return Vp * S.len[nrm] *
+               point_sup(P.c[u], P.c[v], P.c[nrm], S.iv[u], S.iv[v], S.c[nrm], pform);
       }
       // line - line
       const int i = open_axis(A), j = open_axis(B);
@@ -559,11 +571,10 @@ __device__ __forceinline__ int face_box(Box& b, const double fc[3], const double
   return nrm;
 }
 
-// Integ_sup_sup_P (compute_row_P_sup.jl:106-381)
-__device__ double sup_sup(const double f1[3], const double e1[3], const double f2[3],
-                          const double e2[3]) {
-  Box A, B;
-  const int p1 = face_box(A, f1, e1), p2 = face_box(B, f2, e2);
+// Integ_sup_sup_P (compute_row_P_sup.jl:106-381) over two face boxes with normals p1, p2
+// (pform 1); pform 4: Song_P_improved_Ivana_strategy (Song_P_improved_Ivana_strategy.jl:
+// 1-256), the same tree over the dense RIS surfaces
+__device__ double sup_sup_boxes(Box& A, Box& B, int p1, int p2, int pform) {
   const double s1 = A.len[0] * A.len[1] * A.len[2], s2 = B.len[0] * B.len[1] * B.len[2];
   double mxd[3];
   const double min_R = box_gaps(A, B, mxd);
@@ -585,9 +596,16 @@ __device__ double sup_sup(const double f1[3], const double e1[3], const double f
       return w * ss_para(A.iv[u], A.iv[v], A.c[p1], B.iv[u], B.iv[v], B.c[p1]);
     }
     const int a = 3 - p1 - p2;
-    return w * ss_ortho(A.iv[a], A.iv[p2], A.c[p1], B.iv[a], B.c[p2], B.iv[p1], 1);
+    return w * ss_ortho(A.iv[a], A.iv[p2], A.c[p1], B.iv[a], B.c[p2], B.iv[p1], pform);
   }
-  return integ_boxes(A, B, 1);
+  return integ_boxes(A, B, pform);
+}
+
+__device__ double sup_sup(const double f1[3], const double e1[3], const double f2[3],
+                          const double e2[3]) {
+  Box A, B;
+  const int p1 = face_box(A, f1, e1), p2 = face_box(B, f2, e2);
+  return sup_sup_boxes(A, B, p1, p2, 1);
 }
 
 struct PRowArgs {
@@ -791,6 +809,275 @@ int rcc_rows_gpu(const double origin[3], double sx, double sy, double sz, int Nx
     a.beta = beta;
     k_rcc_phase<<<grid, tpb, 0, st>>>(a, d_qs[r], d_re[r], d_im[r], row_len[r]);
   }
+  PEEC_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------
+// Dense RIS fill (sharedRis/calcola_Lp.jl, sharedRis/calcola_P.jl): every pair of volumes
+// of one current direction (an Lp block) and every pair of surfaces (P), from the bodies'
+// vertex coordinates. One thread per pair of a 32 x 32 tile of the upper triangle; each
+// tile is written to both triangles of the column-major matrix (padded leading
+// dimension), the mirrored half through a shared-memory transpose so that both writes
+// are coalesced. FP64 throughout, in the reference's expression order.
+// ---------------------------------------------------------------------------------
+
+// calcola_Lp.jl:22-28: the coordinates holding each axis' minimum, then its maximum
+__constant__ int c_ris_vol_idx[3][8] = {{0, 6, 12, 18, 3, 9, 15, 21},
+                                        {1, 4, 13, 16, 7, 10, 19, 22},
+                                        {2, 5, 8, 11, 14, 17, 20, 23}};
+// mean_length_rev (Compute_Lp_Self.jl:39-74): the two end faces' vertices per direction
+__constant__ int c_ris_ends[3][2][4] = {{{0, 2, 4, 6}, {1, 3, 5, 7}},
+                                        {{0, 1, 4, 5}, {2, 3, 6, 7}},
+                                        {{0, 1, 2, 3}, {4, 5, 6, 7}}};
+
+// isequal, which Julia's unique uses (0.0 and -0.0 are different values)
+__device__ __forceinline__ bool same_value(double a, double b) {
+  return a == b && signbit(a) == signbit(b);
+}
+
+// calcola_Lp.jl:43-57: per axis the first and the last entry of
+// unique(round.(coords[[min; max]], digits=14)), the centre 0.5*(last + first) and the
+// length |last - first|
+__device__ void ris_vol_box(const double* __restrict__ c24, Box& b) {
+  for (int d = 0; d < 3; ++d) {
+    double v[8];
+    for (int i = 0; i < 8; ++i) v[i] = round14(c24[c_ris_vol_idx[d][i]]);
+    double last = v[0];
+    for (int i = 1; i < 8; ++i) {
+      bool seen = false;
+      for (int j = 0; j < i; ++j) seen = seen || same_value(v[i], v[j]);
+      if (!seen) last = v[i];
+    }
+    b.iv[d][0] = v[0];
+    b.iv[d][1] = last;
+    b.c[d] = 0.5 * (last + v[0]);
+    b.len[d] = fabs(last - v[0]);
+  }
+}
+
+// mean_length_rev (Compute_Lp_Self.jl:39-74): the distance between the centroids of the
+// brick's two end faces along direction dir (1, 2, 3)
+__device__ double mean_length_rev(const double* __restrict__ c24, int dir) {
+  double d2 = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < 4; ++i) {
+      a = a + c24[3 * c_ris_ends[dir - 1][0][i] + k];
+      b = b + c24[3 * c_ris_ends[dir - 1][1][i] + k];
+    }
+    const double e = 0.25 * a - 0.25 * b;
+    d2 += e * e;
+  }
+  return sqrt(d2);
+}
+
+// Compute_Lp_Self (Compute_Lp_Self.jl:1-37): the closed-form self inductance of a bar of
+// length l, width W, thickness T; 0 when 1/(l W T) is not finite
+__device__ double lp_self(double l, double W, double T) {
+  if (!isfinite(1.0 / (l * W * T))) return 0.0;
+  const double w = W / l, t = T / l;
+  const double r = sqrt(w * w + t * t), aw = sqrt(w * w + 1), at = sqrt(t * t + 1);
+  const double ar = sqrt(w * w + t * t + 1);
+  const double mu0 = 4 * CUDART_PI * 1e-7;
+  const double g1 = 1.0 / 4 * (1 / w * asinh(w / at) + 1 / t * asinh(t / aw) + asinh(1 / r));
+  const double g2 =
+      1.0 / 24 *
+      (t * t / w * asinh(w / (t * at * (r + ar))) + w * w / t * asinh(t / (w * aw * (r + ar))) +
+       t * t / (w * w) * asinh(w * w / (t * r * (at + ar))) +
+       w * w / (t * t) * asinh(t * t / (w * r * (aw + ar))) +
+       1 / (w * (t * t)) * asinh(w * (t * t) / (at * (aw + ar))) +
+       1 / (t * (w * w)) * asinh(t * (w * w) / (aw * (at + ar))));
+  const double g3 =
+      1.0 / 6 * (1 / (w * t) * atan(w * t / ar) + t / w * atan(w / (t * ar)) + w / t * atan(t / (w * ar)));
+  const double g4 = 1.0 / 60 *
+                    ((ar + r + t + at) * (t * t) / ((ar + r) * (r + t) * (t + at) * (at + ar)) +
+                     (ar + r + w + aw) * (w * w) / ((ar + r) * (r + w) * (w + aw) * (aw + ar)) +
+                     (ar + aw + 1 + at) / ((ar + aw) * (aw + 1) * (1 + at) * (at + ar)));
+  const double g5 = 1.0 / 20 * (1 / (r + ar) + 1 / (aw + ar) + 1 / (at + ar));
+  return 2 * mu0 * l / CUDART_PI * (g1 + g2 - g3 - g4 - g5);
+}
+
+// per volume: its box and its self inductance (calcola_Lp.jl:43-77; the current
+// direction from the volume's index: x for the first mx volumes, then y, then z)
+__global__ void k_ris_vol_prep(const double* __restrict__ coords, int64_t m, int64_t mx,
+                               int64_t my, Box* __restrict__ out, double* __restrict__ self) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double* c = coords + 24 * i;
+    Box b;
+    ris_vol_box(c, b);
+    b.s[0] = b.s[1] = b.s[2] = 0;
+    b.n = 0;
+    out[i] = b;
+    const int dir = i < mx ? 1 : (i < mx + my ? 2 : 3);
+    const double m1 = fabs(mean_length_rev(c, 1)), m2 = fabs(mean_length_rev(c, 2)),
+                 m3 = fabs(mean_length_rev(c, 3));
+    double l, W, T;
+    if (dir == 1) { l = m1; W = m3; T = m2; }
+    else if (dir == 2) { T = m1; W = m3; l = m2; }
+    else { W = m1; l = m3; T = m2; }
+    self[i] = lp_self(l, W, T);
+  }
+}
+
+// per surface (process_surfaces!, calcola_P.jl:94-160): the box from vertices 1 and 4,
+// rounded, the normal (the smallest extent) given length 1
+__global__ void k_ris_surf_prep(const double* __restrict__ ends, int64_t ns, Box* __restrict__ out,
+                                int* __restrict__ nrm) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ns;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double* e = ends + 12 * i;
+    Box b;
+    for (int d = 0; d < 3; ++d) {
+      const double p = e[d], q = e[9 + d];
+      b.iv[d][0] = round14(fmin(p, q));
+      b.iv[d][1] = round14(fmax(p, q));
+      b.c[d] = 0.5 * (b.iv[d][1] + b.iv[d][0]);
+      b.len[d] = fabs(b.iv[d][1] - b.iv[d][0]);
+    }
+    const double* l = b.len;
+    const int k = (l[0] <= l[1] && l[0] <= l[2]) ? 0 : ((l[1] <= l[0] && l[1] <= l[2]) ? 1 : 2);
+    b.len[k] = 1.0;
+    b.s[0] = b.s[1] = b.s[2] = 0;
+    b.n = 0;
+    out[i] = b;
+    nrm[i] = k;
+  }
+}
+
+// KIND 0: an Lp block (Song_improved_Ivana_strategy2 off the diagonal, the self term
+// on it, 1e-7 / (S_m S_n) * integral * esc; calculate_Lp_matrix, calcola_Lp.jl:254-306);
+// KIND 1: P (Song_P_improved_Ivana_strategy on and off the diagonal,
+// integral / (4 pi eps0 S_m S_n) * esc; calculate_P_matrix, calcola_P.jl:162-222).
+// Grid (tiles, tiles): CTA (x, y) takes the tile of rows 32y.. and columns 32x.., x >= y.
+template <int KIND>
+__global__ void __launch_bounds__(256) k_ris_pairs(const Box* __restrict__ bodies,
+                                                   const int* __restrict__ nrm,
+                                                   const double* __restrict__ S,
+                                                   const double* __restrict__ self, int64_t dim,
+                                                   double esc, double* __restrict__ M, int64_t ld,
+                                                   int* bad) {
+  __shared__ Box rb[32], cb[32];
+  __shared__ int rn[32], cn[32];
+  __shared__ double tile[32][33];
+  const int64_t ti = blockIdx.y, tj = blockIdx.x;
+  if (ti > tj) return;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int64_t m0 = ti * 32, n0 = tj * 32;
+  if (ty == 0 && m0 + tx < dim) {
+    rb[tx] = bodies[m0 + tx];
+    rn[tx] = KIND ? nrm[m0 + tx] : 0;
+  } else if (ty == 1 && n0 + tx < dim) {
+    cb[tx] = bodies[n0 + tx];
+    cn[tx] = KIND ? nrm[n0 + tx] : 0;
+  }
+  __syncthreads();
+  const double pi = CUDART_PI;
+  const double eps0 = 8.854187816997944e-12;
+  const int64_t m = m0 + tx;
+  for (int k = 0; k < 4; ++k) {
+    const int nl = ty + 8 * k;
+    const int64_t n = n0 + nl;
+    double e = 0.0;
+    if (m < dim && n < dim && (KIND ? m <= n : m < n)) {
+      Box A = rb[tx], B = cb[nl];
+      double v;
+      if (KIND == 0) {
+        lp_flags(A, B);
+        v = (A.n + B.n == 0) ? vol_vol(A.iv[0], A.iv[1], A.iv[2], B.iv[0], B.iv[1], B.iv[2])
+                             : integ_boxes(A, B, 3);
+        e = 1e-7 / (S[m] * S[n]) * v * esc;
+      } else {
+        v = sup_sup_boxes(A, B, rn[tx], cn[nl], 4);
+        e = 1.0 / (4 * pi * eps0 * S[m] * S[n]) * v * esc;
+      }
+      if (!isfinite(e)) atomicAdd(bad, 1);
+      M[m + n * ld] = e;
+    }
+    tile[nl][tx] = e;
+  }
+  __syncthreads();
+  for (int k = 0; k < 4; ++k) {  // the mirrored entries (n, m), m < n
+    const int ml = ty + 8 * k;
+    const int64_t mm = m0 + ml, nn = n0 + tx;
+    if (mm < dim && nn < dim && mm < nn) M[nn + mm * ld] = tile[tx][ml];
+  }
+  if (KIND == 0 && ti == tj && ty == 0 && m < dim) {
+    const double e = self[m] * esc;
+    if (!isfinite(e)) atomicAdd(bad, 1);
+    M[m + m * ld] = e;
+  }
+}
+
+// centre distances (calculate_Rx / _Ry / _Rz, calcola_Lp.jl:99-252; calculate_R_cc!,
+// calcola_P.jl:49-92): R[m, n] = |c_m - c_n|, column-major, leading dimension ld
+__global__ void k_ris_dist(const double* __restrict__ ctr, int64_t dim, double* __restrict__ R,
+                           int64_t ld) {
+  for (int64_t n = blockIdx.y; n < dim; n += gridDim.y) {
+    const double x = ctr[3 * n], y = ctr[3 * n + 1], z = ctr[3 * n + 2];
+    for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < dim;
+         m += (int64_t)gridDim.x * blockDim.x) {
+      const double dx = ctr[3 * m] - x, dy = ctr[3 * m + 1] - y, dz = ctr[3 * m + 2] - z;
+      R[m + n * ld] = sqrt(dx * dx + dy * dy + dz * dz);
+    }
+  }
+}
+
+__global__ void k_inv_diag(const double* __restrict__ M, int64_t ld, int64_t n,
+                           double* __restrict__ inv) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    inv[i] = 1.0 / M[i + i * ld];
+}
+
+size_t ris_box_bytes() { return sizeof(Box); }
+
+// The bodies' boxes (and the volumes' self terms) into the scratch: boxes (count Box),
+// self (count doubles, volumes) or nrm (count ints, surfaces)
+int ris_prep_gpu(int surfaces, const double* d_geom, int64_t count, int64_t mx, int64_t my,
+                 void* boxes, double* self, int* nrm, cudaStream_t st) {
+  if (count <= 0) return 0;
+  const int tpb = 128;
+  const int blocks = (int)std::min<int64_t>((count + tpb - 1) / tpb, 152 * 16);
+  if (surfaces)
+    k_ris_surf_prep<<<blocks, tpb, 0, st>>>(d_geom, count, (Box*)boxes, nrm);
+  else
+    k_ris_vol_prep<<<blocks, tpb, 0, st>>>(d_geom, count, mx, my, (Box*)boxes, self);
+  PEEC_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// one dense block: KIND 0 (Lp, boxes/self/S of its volumes) or 1 (P); M zeroed by the
+// caller (padding rows stay zero)
+int ris_pairs_gpu(int kind, const void* boxes, const int* nrm, const double* S, const double* self,
+                  int64_t dim, double esc, double* M, int64_t ld, int* d_bad, cudaStream_t st) {
+  if (dim <= 0) return 0;
+  const int64_t nt = (dim + 31) / 32;
+  if (nt > 65535) return PEEC_ERR_UNSUPPORTED_INTERNAL;
+  const dim3 grid((unsigned)nt, (unsigned)nt);
+  if (kind == 0)
+    k_ris_pairs<0><<<grid, 256, 0, st>>>((const Box*)boxes, nrm, S, self, dim, esc, M, ld, d_bad);
+  else
+    k_ris_pairs<1><<<grid, 256, 0, st>>>((const Box*)boxes, nrm, S, self, dim, esc, M, ld, d_bad);
+  PEEC_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int ris_dist_gpu(const double* d_ctr, int64_t dim, double* R, int64_t ld, cudaStream_t st) {
+  if (dim <= 0) return 0;
+  const int tpb = 256;
+  const dim3 grid((unsigned)std::min<int64_t>((dim + tpb - 1) / tpb, 64),
+                  (unsigned)std::min<int64_t>(dim, 65535));
+  k_ris_dist<<<grid, tpb, 0, st>>>(d_ctr, dim, R, ld);
+  PEEC_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int inv_diag_gpu(const double* M, int64_t ld, int64_t n, double* inv, cudaStream_t st) {
+  if (n <= 0) return 0;
+  const int tpb = 256;
+  k_inv_diag<<<(unsigned)std::min<int64_t>((n + tpb - 1) / tpb, 1024), tpb, 0, st>>>(M, ld, n, inv);
   PEEC_CUDA_TRY(cudaGetLastError());
   return 0;
 }

@@ -5,8 +5,9 @@
 solver entry points shared with the voxel path).
 
 The dense Lp and P matrices (``Lp_data``, ``P_data``) are inputs, as they are to the
-reference's solver: the reference fills them on the host (sharedRis/calcola_{Lp,P}.jl),
-and so does a caller of this module.
+reference's solver, or are filled on the device from the bodies' vertex coordinates
+(``DenseOperator.from_geometry``; ``calcola_Lp`` / ``calcola_P`` return them on the host as
+sharedRis/calcola_{Lp,P}.jl do) through peec_ris_fill.
 
 Mapping onto the library's operator: the library forms the first block row as
 jw LpI + DZ I + A Phi and the preconditioner with invZ = 1/DZ. With DZ = Z_self +
@@ -36,9 +37,11 @@ class DenseOperator(GpuOperator):
     lattices. Solver entry points (set_frequency, gmres, solve_mixed, port_rhs,
     set_frequency_refactor, ...) are those of GpuOperator; DZ = Z_self + jw diag(Lp)."""
 
-    def __init__(self, incidence_selection, Lp_data, P_data, device=0):
+    def __init__(self, incidence_selection, Lp_data, P_data, device=0, geometry=None):
         self.L = _lib.load()
         self._init_args = (incidence_selection, Lp_data, P_data, device)
+        self._geometry = geometry
+        self._device_dist = False
         self._rows = None
         self._rcc = None
         self._rcc_freq = None
@@ -75,6 +78,9 @@ class DenseOperator(GpuOperator):
         _lib.check(self.h, self.L.peec_set_incidence(self.h, mx, my, mz, _lib.ptr(n1),
                                                      _lib.ptr(n2), self.ns, _lib.ptr(snode),
                                                      self.n))
+        if geometry is not None:
+            self._fill(*geometry)
+            return
         blocks = []
         for key, size in (("Lp_x", mx), ("Lp_y", my), ("Lp_z", mz)):
             M = np.asfortranarray(np.asarray(Lp_data[key], dtype=np.float64))
@@ -90,12 +96,59 @@ class DenseOperator(GpuOperator):
         ptrs = [_lib.ptr(M) if M.size else None for M in blocks]
         _lib.check(self.h, self.L.peec_set_dense(self.h, *ptrs))
         self.diag_Lp = np.concatenate([np.diag(M) for M in blocks[:3]])
+        self.diag_P = np.diag(P).copy()
+
+    @classmethod
+    def from_geometry(cls, incidence_selection, volumi, superfici, escalings, QS_Rcc_FW=1,
+                      device=0):
+        """The operator with its Lp blocks and P filled on the device from the bodies'
+        vertex coordinates (calcola_Lp.jl / calcola_P.jl through peec_ris_fill); with
+        QS_Rcc_FW >= 2 also their centre distances, so that set_rcc_frequency forms the
+        retarded blocks without host data."""
+        return cls(incidence_selection, None, None, device=device,
+                   geometry=(volumi, superfici, escalings, int(QS_Rcc_FW)))
+
+    def _fill(self, volumi, superfici, escalings, QS_Rcc_FW):
+        vol = ris_volumes(volumi, self.m)
+        surf = ris_surfaces(superfici, self.ns)
+        dist = int(QS_Rcc_FW) >= 2
+        bad = ctypes.c_int64(0)
+        _lib.check(self.h, self.L.peec_ris_fill(
+            self.h, _lib.ptr(vol["coordinate"]), _lib.ptr(vol["S"]),
+            _lib.ptr(vol["centri"]) if dist else None, float(escalings["Lp"]),
+            _lib.ptr(surf["estremi_celle"]), _lib.ptr(surf["S"]),
+            _lib.ptr(surf["centri"]) if dist else None, float(escalings["P"]), int(dist),
+            ctypes.byref(bad)))
+        self.nonfinite = int(bad.value)
+        self._device_dist = dist
+        self.diag_Lp = np.concatenate([self.dense_get(b, 2) for b in range(3)])
+        self.diag_P = self.dense_get(3, 2)
+
+    def dense_get(self, block, what=0):
+        """Block 0..2 (Lp_x, Lp_y, Lp_z) or 3 (P) from the device: what 0 the matrix,
+        1 its centre distances, 2 its diagonal."""
+        inc = self._init_args[0]
+        n = (int(inc["mx"]), int(inc["my"]), int(inc["mz"]), self.ns)[block]
+        out = np.zeros(n if what == 2 else (n, n), dtype=np.float64, order="F")
+        if n:
+            _lib.check(self.h, self.L.peec_dense_get(self.h, int(block), int(what), _lib.ptr(out)))
+        return out
+
+    def dense_data(self):
+        """(Lp_data, P_data) as calcola_Lp / calcola_P return them: Lp_x, Lp_y, Lp_z (and Rx,
+        Ry, Rz when the distances are on the device); P (and R_cc)."""
+        Lp = {k: self.dense_get(b) for b, k in enumerate(("Lp_x", "Lp_y", "Lp_z"))}
+        P = {"P": self.dense_get(3)}
+        if self._device_dist:
+            Lp.update({k: self.dense_get(b, 1) for b, k in enumerate(("Rx", "Ry", "Rz"))})
+            P["R_cc"] = self.dense_get(3, 1)
+        return Lp, P
 
     def clone(self):
         """A second context with the same mesh and matrices (its own stream and
         workspaces), for concurrent port solves."""
         inc, Lp, P, dev = self._init_args
-        c = DenseOperator(inc, Lp, P, device=dev)
+        c = DenseOperator(inc, Lp, P, device=dev, geometry=self._geometry)
         if getattr(self, "_rcc_dist", None) is not None:
             c.set_rcc(*self._rcc_dist)
         return c
@@ -109,6 +162,9 @@ class DenseOperator(GpuOperator):
             _lib.check(self.h, self.L.peec_set_dense_rcc(self.h, None, None, None, None))
             self._rcc_dist = None
             return
+        if self._device_dist:
+            raise ValueError("the distances of this operator are on the device: "
+                             "set_rcc_frequency forms the retarded blocks")
         mats = []
         for key, size in (("Rx", self._init_args[0]["mx"]), ("Ry", self._init_args[0]["my"]),
                           ("Rz", self._init_args[0]["mz"])):
@@ -129,6 +185,94 @@ class DenseOperator(GpuOperator):
         (iter_solver_QS_S_type.jl:41-44)."""
         beta = 2 * math.pi * float(f_hz) * math.sqrt(EPS0 * MU0)
         _lib.check(self.h, self.L.peec_set_dense_rcc_frequency(self.h, beta))
+
+
+def _key(d, name):
+    """d[name] for string- or symbol-keyed dicts (the reference's volumi uses symbols,
+    superfici strings)."""
+    return d[name] if name in d else d[":" + name]
+
+
+def _rows(a, width, count, name):
+    """An array of count rows of width values, row-major: accepts the (count, width)
+    matrix or the reference's JSON layout, width lists of count values (what
+    hcat(...) turns into the matrix, calcola_P.jl:11-12)."""
+    a = np.asarray(a, dtype=np.float64)
+    if a.shape == (width, count) and a.shape != (count, width):
+        a = a.T
+    if a.shape != (count, width):
+        raise ValueError(f"{name} must be {count} x {width}, got {a.shape}")
+    return np.ascontiguousarray(a)
+
+
+def ris_volumes(volumi, m):
+    """volumi[:coordinate] (m x 24), [:S] (m), [:centri] (m x 3) as contiguous arrays."""
+    out = {"coordinate": _rows(_key(volumi, "coordinate"), 24, m, "volumi coordinate"),
+           "S": np.ascontiguousarray(np.asarray(_key(volumi, "S"), dtype=np.float64).ravel())}
+    if out["S"].size != m:
+        raise ValueError(f"volumi S must have {m} entries")
+    c = volumi.get("centri", volumi.get(":centri"))
+    out["centri"] = _rows(c, 3, m, "volumi centri") if c is not None else np.zeros((m, 3))
+    return out
+
+
+def ris_surfaces(superfici, ns):
+    """superfici["estremi_celle"] (ns x 12), ["S"] (ns), ["centri"] (ns x 3)."""
+    out = {"estremi_celle": _rows(_key(superfici, "estremi_celle"), 12, ns,
+                                  "superfici estremi_celle"),
+           "S": np.ascontiguousarray(np.asarray(_key(superfici, "S"), dtype=np.float64).ravel())}
+    if out["S"].size != ns:
+        raise ValueError(f"superfici S must have {ns} entries")
+    c = superfici.get("centri", superfici.get(":centri"))
+    out["centri"] = _rows(c, 3, ns, "superfici centri") if c is not None else np.zeros((ns, 3))
+    return out
+
+
+def _sizes_only(mx, my, mz, ns):
+    """An incidence_selection that carries only the block sizes (every edge on one node,
+    every surface on it), for a context that only fills and returns dense blocks."""
+    inc = {"mx": mx, "my": my, "mz": mz,
+           "A": sp.csr_matrix((np.tile([-1.0, 1.0], mx + my + mz),
+                               np.zeros(2 * (mx + my + mz), dtype=np.int64),
+                               np.arange(0, 2 * (mx + my + mz) + 1, 2)), shape=(mx + my + mz, 1)),
+           "Gamma": sp.csc_matrix((np.ones(ns), np.zeros(ns, dtype=np.int64), np.arange(ns + 1)),
+                                  shape=(1, ns))}
+    return inc
+
+
+def calcola_Lp(volumi, incidence_selection, escalings, QS_Rcc_FW, device=0):
+    """calcola_Lp (sharedRis/calcola_Lp.jl:1-97) on the GPU: the dense Lp_x, Lp_y, Lp_z
+    (and Rx, Ry, Rz when QS_Rcc_FW >= 2), returned on the host. For QS_Rcc_FW < 2 the
+    reference's function reads its unassigned Rx at the return and raises; here the
+    distances are left out."""
+    mx, my, mz = (int(incidence_selection[k]) for k in ("mx", "my", "mz"))
+    inc = _sizes_only(mx, my, mz, 0)
+    op = DenseOperator(inc, None, None, device=device,
+                       geometry=(volumi, {"estremi_celle": np.zeros((0, 12)), "S": np.zeros(0)},
+                                 escalings, int(QS_Rcc_FW)))
+    try:
+        Lp, _ = op.dense_data()
+        Lp["nonfinite"] = op.nonfinite
+        return Lp
+    finally:
+        op.close()
+
+
+def calcola_P(superfici, escalings, QS_Rcc_FW, device=0):
+    """calcola_P (sharedRis/calcola_P.jl:1-47) on the GPU: the dense P (and R_cc when
+    QS_Rcc_FW >= 2), returned on the host. For QS_Rcc_FW < 2 the reference returns
+    R_cc = nothing into a matrix-typed Dict and raises; here R_cc is left out."""
+    ns = len(np.asarray(_key(superfici, "S")).ravel())
+    inc = _sizes_only(0, 0, 0, ns)
+    op = DenseOperator(inc, None, None, device=device,
+                       geometry=({"coordinate": np.zeros((0, 24)), "S": np.zeros(0)}, superfici,
+                                 escalings, int(QS_Rcc_FW)))
+    try:
+        _, P = op.dense_data()
+        P["nonfinite"] = op.nonfinite
+        return P
+    finally:
+        op.close()
 
 
 def lumped_admittance_S(typ, R, L, C, w):
@@ -269,9 +413,9 @@ def iter_solver_QS_S_type(freq, escalings, incidence_selection, P_data, Lp_data,
     own = op is None
     if own:
         op = DenseOperator(incidence_selection, Lp_data, P_data, device=device)
-    if rcc:
+    if rcc and not op._device_dist:
         op.set_rcc(Lp_data, P_data)
-    diag_P = np.diag(np.asarray(P_data["P"]))
+    diag_P = op.diag_P
     S = np.zeros((npt, npt, freq.size), dtype=np.complex128)
     Vrest = np.zeros((m + ns + n, npt), dtype=np.complex128)
     info = []
@@ -318,6 +462,7 @@ def iter_solver_QS_S_type(freq, escalings, incidence_selection, P_data, Lp_data,
             op.close()
         elif rcc:
             op.set_rcc(None, None)  # back to the quasi-static blocks for later users
+            # (with the distances on the device, set_rcc_frequency returns to the retarded ones)
     Id = np.eye(npt)
     Z = np.stack([R * np.linalg.solve(Id - S[:, :, k], Id + S[:, :, k]) for k in range(freq.size)],
                  axis=2) if freq.size else S.copy()

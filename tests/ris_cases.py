@@ -118,3 +118,171 @@ def with_distances(c, Lp, P):
     P = dict(P)
     P["R_cc"] = dist(spos)
     return Lp, P
+
+
+def _brick24(lo, hi):
+    """The 24 vertex coordinates of an axis-aligned brick in the reference's vertex order
+    (x alternating fastest, then y, then z: the min/max index sets of calcola_Lp.jl:22-28
+    and the end faces of mean_length_rev)."""
+    v = []
+    for z in (lo[2], hi[2]):
+        for y in (lo[1], hi[1]):
+            for x in (lo[0], hi[0]):
+                v += [x, y, z]
+    return v
+
+
+def _rect12(lo, hi):
+    """Four vertices of an axis-aligned rectangle; vertices 1 and 4 are the opposite
+    corners process_surfaces! reads (calcola_P.jl:110-121)."""
+    lo, hi = list(lo), list(hi)
+    mid1 = [hi[0], lo[1], lo[2]] if hi[0] != lo[0] else [lo[0], hi[1], lo[2]]
+    mid2 = [lo[0], hi[1], hi[2]] if hi[0] != lo[0] else [lo[0], lo[1], hi[2]]
+    return lo + mid1 + mid2 + hi
+
+
+def ris_geometry(c):
+    """volumi / superfici of the voxel case's bodies as the RIS solver's mesher describes
+    them: each edge's Lp cell (one voxel length along the edge, centred between the two
+    voxel centres) and each surface's voxel face, with cross-sections, areas and centres."""
+    from solver_gb300.operator import _edge_cells, _surf_cells, row_dims
+    inc, exp = c["inc"], c["exp"]
+    mx, my, mz = inc["mx"], inc["my"], inc["mz"]
+    ns = inc["Gamma"].shape[1]
+    Nx, Ny, Nz = c["grid"][:3]
+    cell = np.array([c["cc"]["sx"], c["cc"]["sy"], c["cc"]["sz"]], dtype=np.float64)
+    dims = row_dims(Nx, Ny, Nz)
+
+    def idx3(ids, d):
+        ids = np.asarray(ids, dtype=np.int64)
+        return np.stack([ids % d[0], (ids // d[0]) % d[1], ids // (d[0] * d[1])], axis=1)
+
+    ec = _edge_cells(exp, mx, my, mz)
+    coords, S, ctr = [], [], []
+    for d, (key, sl) in enumerate((("Lpx", slice(0, mx)), ("Lpy", slice(mx, mx + my)),
+                                   ("Lpz", slice(mx + my, mx + my + mz)))):
+        for ijk in idx3(ec[sl], dims[key]):
+            lo = ijk.astype(np.float64)
+            lo[d] += 0.5
+            hi = lo + 1.0
+            coords.append(_brick24(lo * cell, hi * cell))
+            t = [q for q in range(3) if q != d]
+            S.append(cell[t[0]] * cell[t[1]])
+            ctr.append((0.5 * (lo + hi) * cell).tolist())
+    volumi = {"coordinate": np.array(coords).reshape(-1, 24), "S": np.array(S),
+              "centri": np.array(ctr).reshape(-1, 3)}
+    fam, scell = _surf_cells(exp, ns)
+    ends, A, sc = [], [], []
+    for s_ in range(ns):
+        f = int(fam[s_])
+        key = ("p12_se", "p34_se", "p56_se")[f]
+        nrm = (1, 0, 2)[f]
+        lo = idx3([scell[s_]], dims[key])[0].astype(np.float64)
+        hi = lo + 1.0
+        hi[nrm] = lo[nrm]
+        ends.append(_rect12((lo * cell).tolist(), (hi * cell).tolist()))
+        t = [q for q in range(3) if q != nrm]
+        A.append(cell[t[0]] * cell[t[1]])
+        sc.append((0.5 * (lo + hi) * cell).tolist())
+    superfici = {"estremi_celle": np.array(ends).reshape(-1, 12), "S": np.array(A),
+                 "centri": np.array(sc).reshape(-1, 3)}
+    return volumi, superfici
+
+
+def random_bodies(seed, mx, my, mz, ns, span=0.2):
+    """Seeded bricks (mx along x, my along y, mz along z) and rectangles (ns, random
+    normals) of widely varying sizes and aspect ratios, some clustered and some far apart,
+    so that every branch of the dense fill's case trees (the full closed forms and the
+    surface, line and point forms of the suppressed dimensions) is taken."""
+    rng = np.random.default_rng(seed)
+
+    def sizes(k):
+        base = 10.0 ** rng.uniform(-4.3, -3.0, size=(k, 3))
+        thin = rng.random(k) < 0.3  # a thin dimension: surface-like bodies
+        ax = rng.integers(0, 3, size=k)
+        base[thin, ax[thin]] *= 10.0 ** rng.uniform(-3, -1.5, size=thin.sum())
+        return base
+
+    def places(k):
+        near = rng.random(k) < 0.5
+        p = rng.uniform(0, span, size=(k, 3))
+        p[near] = rng.uniform(0, span * 0.01, size=(near.sum(), 3))
+        return p
+
+    coords, S, ctr = [], [], []
+    for d, k in enumerate((mx, my, mz)):
+        sz = sizes(k)
+        sz[:, d] *= rng.uniform(1.0, 6.0, size=k)  # longer along the current
+        lo = places(k)
+        for i in range(k):
+            hi = lo[i] + sz[i]
+            coords.append(_brick24(lo[i], hi))
+            t = [q for q in range(3) if q != d]
+            S.append(sz[i, t[0]] * sz[i, t[1]])
+            ctr.append((0.5 * (lo[i] + hi)).tolist())
+    volumi = {"coordinate": np.array(coords, dtype=np.float64).reshape(-1, 24),
+              "S": np.array(S), "centri": np.array(ctr).reshape(-1, 3)}
+    sz = sizes(ns)
+    nrm = rng.integers(0, 3, size=ns)
+    lo = places(ns)
+    ends, A, sc = [], [], []
+    for i in range(ns):
+        hi = lo[i] + sz[i]
+        hi[nrm[i]] = lo[i][nrm[i]]
+        ends.append(_rect12(lo[i].tolist(), hi.tolist()))
+        t = [q for q in range(3) if q != nrm[i]]
+        A.append(sz[i, t[0]] * sz[i, t[1]])
+        sc.append((0.5 * (lo[i] + hi)).tolist())
+    superfici = {"estremi_celle": np.array(ends).reshape(-1, 12), "S": np.array(A),
+                 "centri": np.array(sc).reshape(-1, 3)}
+    return volumi, superfici
+
+
+def oracle_dense_fill(volumi, superfici, mx, my, mz, esc_Lp=1.0, esc_P=1.0, ld=False,
+                      forms=None):
+    """The oracle's dense Lp blocks and P (oracle/fill_ref.c, double or long double) with
+    their error scales (the prefactors times the sum of |terms|). forms: a dict that
+    receives, per block, the number of collapsed dimensions of each pair."""
+    import ctypes
+    from oracle import build
+    L = ctypes.CDLL(str(build.build()))
+    sfx = "_ld" if ld else "_d"
+    dp = ctypes.POINTER(ctypes.c_double)
+    f_lp = getattr(L, "oracle_ris_lp_block" + sfx)
+    f_lp.restype = ctypes.c_int64
+    ip = ctypes.POINTER(ctypes.c_int)
+    f_lp.argtypes = [dp, dp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_double, dp, dp,
+                     ip]
+    f_p = getattr(L, "oracle_ris_p" + sfx)
+    f_p.restype = ctypes.c_int64
+    f_p.argtypes = [dp, dp, ctypes.c_int64, ctypes.c_double, dp, dp, ip]
+
+    def P_(a):
+        return a.ctypes.data_as(dp)
+    coords = np.ascontiguousarray(volumi["coordinate"], dtype=np.float64)
+    S = np.ascontiguousarray(volumi["S"], dtype=np.float64)
+    Lp, scale, bad = {}, {}, 0
+    off = 0
+    for d, (key, k) in enumerate((("Lp_x", mx), ("Lp_y", my), ("Lp_z", mz))):
+        out = np.zeros(k * k)
+        sc = np.zeros(k * k)
+        fm = np.full(k * k, -1, dtype=np.int32)
+        if k:
+            bad += f_lp(P_(coords), P_(S), off, k, d + 1, esc_Lp, P_(out), P_(sc),
+                        fm.ctypes.data_as(ip))
+        if forms is not None:
+            forms[key] = fm.reshape(k, k, order="F")
+        Lp[key] = out.reshape(k, k, order="F")
+        scale[key] = sc.reshape(k, k, order="F")
+        off += k
+    ends = np.ascontiguousarray(superfici["estremi_celle"], dtype=np.float64)
+    A = np.ascontiguousarray(superfici["S"], dtype=np.float64)
+    ns = A.size
+    out = np.zeros(ns * ns)
+    sc = np.zeros(ns * ns)
+    fm = np.full(ns * ns, -1, dtype=np.int32)
+    if ns:
+        bad += f_p(P_(ends), P_(A), ns, esc_P, P_(out), P_(sc), fm.ctypes.data_as(ip))
+    if forms is not None:
+        forms["P"] = fm.reshape(ns, ns, order="F")
+    return Lp, {"P": out.reshape(ns, ns, order="F")}, scale, sc.reshape(ns, ns, order="F"), bad

@@ -48,6 +48,9 @@ def test_entry_points_reject_a_null_context_with_their_own_name(cuda_lib):
         "peec_set_dense": lambda: L.peec_set_dense(None, None, None, None, None),
         "peec_set_dense_rcc": lambda: L.peec_set_dense_rcc(None, None, None, None, None),
         "peec_set_dense_rcc_frequency": lambda: L.peec_set_dense_rcc_frequency(None, 1.0),
+        "peec_ris_fill": lambda: L.peec_ris_fill(None, None, None, None, 1.0, None, None, None,
+                                                 1.0, 0, None),
+        "peec_dense_get": lambda: L.peec_dense_get(None, 0, 0, None),
         "peec_set_device_loop": lambda: L.peec_set_device_loop(None, 1),
         "peec_set_edge_state": lambda: L.peec_set_edge_state(None, None, None, None, None, None,
                                                              0, 1.0, 1.0),
