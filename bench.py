@@ -610,86 +610,79 @@ def loaded_native_libs():
 
 
 def ris_problem(grid=(48, 48, 16), seed=3):
-    """A dense RIS workload on a voxel mesh: the mesh's incidence and ports; dense Lp blocks
-    and P with the mesh's self terms on the diagonal and off-diagonal couplings
-    sqrt(d_i d_j) exp(-r_ij / 1.5 cells) between edge / surface centres (positive
-    definite, like the partial inductances and potentials the reference fills); R, Cd
-    and the dielectric edges from the mesh's diagonals. Seeded and synthetic."""
-    from solver_gb300 import configs, mesher
-    from solver_gb300.operator import _edge_cells, _surf_cells, row_dims
+    """A dense RIS workload on a voxel mesh: the mesh's incidence and ports, and its bodies
+    as the RIS solver takes them (each edge's Lp brick, each surface's voxel face: vertex
+    coordinates, cross-sections / areas, centres), from which the device fills the dense
+    Lp blocks and P; R, Cd and the dielectric edges from the mesh's diagonals. Seeded and
+    synthetic."""
+    from solver_gb300 import configs, mesher, ris
     req = configs.random_mixed(tuple(grid), s=5e-5, p=0.3, seed=seed, nports=4,
                                freqs=[1e8, 1e9, 3e9, 1e10], tol=1e-8)
     out, freqs, settings, z0, g = mesher.parse_request(req)
     esc, inc, cc, diag, exp, ports, le, li, Zs = out
-    Nx, Ny, Nz = g
-    mx, my, mz = inc["mx"], inc["my"], inc["mz"]
-    ns = inc["Gamma"].shape[1]
-    dims = row_dims(Nx, Ny, Nz)
-
-    def coords(cell, d, shift):
-        cell = np.asarray(cell, dtype=np.int64)
-        ix, iy, iz = cell % d[0], (cell // d[0]) % d[1], cell // (d[0] * d[1])
-        return np.stack([ix + shift[0], iy + shift[1], iz + shift[2]], axis=1).astype(np.float64)
-
-    ecell = _edge_cells(exp, mx, my, mz)
-    epos = [coords(ecell[:mx], dims["Lpx"], (1.0, 0.5, 0.5)),
-            coords(ecell[mx:mx + my], dims["Lpy"], (0.5, 1.0, 0.5)),
-            coords(ecell[mx + my:], dims["Lpz"], (0.5, 0.5, 1.0))]
-    fam, scell = _surf_cells(exp, ns)
-    spos = np.zeros((ns, 3))
-    for f, (key, sh) in enumerate((("p12_se", (0.5, 0.0, 0.5)), ("p34_se", (0.0, 0.5, 0.5)),
-                                   ("p56_se", (0.5, 0.5, 0.0)))):
-        sel = fam == f
-        spos[sel] = coords(scell[sel], dims[key], sh)
-
-    def kernel(pos, d, out):
-        sq = np.sqrt(d)
-        for a in range(0, pos.shape[0], 2048):
-            r = np.sqrt(((pos[a:a + 2048, None, :] - pos[None, :, :]) ** 2).sum(-1))
-            out[a:a + 2048] = np.exp(-r / 1.5) * sq[a:a + 2048, None] * sq[None, :]
-        return out
-
-    dLp = np.real(np.asarray(diag["Lp"])).ravel()
-    offs = [0, mx, mx + my, mx + my + mz]
-    Lp = {}
-    for k, key in enumerate(("Lp_x", "Lp_y", "Lp_z")):
-        n_k = offs[k + 1] - offs[k]
-        Lp[key] = kernel(epos[k], dLp[offs[k]:offs[k + 1]], np.empty((n_k, n_k), order="F"))
-    dP = np.real(np.asarray(diag["P"])).ravel()
-    P = {"P": kernel(spos, dP, np.empty((ns, ns), order="F"))}
+    volumi, superfici = ris.voxel_bodies(inc, exp, g, (cc["sx"], cc["sy"], cc["sz"]))
     R = np.real(np.asarray(diag["R"])).sum(axis=1)
     Cd = np.real(np.asarray(diag["Cd"]))
     has = (Cd > 0).any(axis=1)
     Cd_eff = np.zeros(R.size)
     Cd_eff[has] = 1.0 / np.where(Cd[has] > 0, 1.0 / np.where(Cd[has] > 0, Cd[has], 1.0),
                                  0.0).sum(axis=1)
-    volumi = {"R": R, "Cd": Cd_eff, "indici_dielettrici": np.flatnonzero((R == 0) & (Cd_eff > 0)),
-              "Zs_part": np.zeros(R.size)}
-    return dict(esc=esc, inc=inc, ports=ports, Lp=Lp, P=P, volumi=volumi, freqs=list(freqs),
-                grid=list(g))
+    volumi.update({"R": R, "Cd": Cd_eff,
+                   "indici_dielettrici": np.flatnonzero((R == 0) & (Cd_eff > 0)),
+                   "Zs_part": np.zeros(R.size)})
+    return dict(esc=esc, inc=inc, ports=ports, volumi=volumi, superfici=superfici,
+                freqs=list(freqs), grid=list(g))
+
+
+def ris_fill_cpu(P, k=1500):
+    """The oracle's dense fill (oracle/ris_fill.py, C with OpenMP on every host core) on a
+    sample: P of the first k surfaces. Returns (pairs per second, sample text)."""
+    from oracle import ris_fill
+    sup = {"estremi_celle": np.asarray(P["superfici"]["estremi_celle"])[:k],
+           "S": np.asarray(P["superfici"]["S"])[:k]}
+    empty = {"coordinate": np.zeros((0, 24)), "S": np.zeros(0)}
+    ris_fill.dense_fill(empty, {"estremi_celle": sup["estremi_celle"][:50],
+                                "S": sup["S"][:50]}, 0, 0, 0)  # build and load
+    t = time.perf_counter()
+    ris_fill.dense_fill(empty, sup, 0, 0, 0, esc_P=P["esc"]["P"])
+    dt = time.perf_counter() - t
+    pairs = k * (k + 1) // 2
+    return pairs / dt, (f"P of the first {k} surfaces ({pairs} pairs, {dt:.2f} s) with the "
+                        f"oracle's C fill on {os.cpu_count() or 1} threads")
 
 
 def run_ris(args):
-    """The dense RIS configuration: the dense operator's FP32 and FP64 applications against
-    the HBM roofline, and the RIS frequency x port loop (4 ports x 4 frequencies, 1e-8) in
-    FP64 and mixed precision with SS factorised on the GPU; beside it the oracle's RIS
-    operator and GMRES on the host cores for one port solve. One JSON line."""
+    """The dense RIS configuration: the dense Lp blocks and P filled on the device from the
+    mesh's bodies (calcola_Lp / calcola_P), the dense operator's FP32 and FP64 applications
+    against the HBM roofline, and the RIS frequency x port loop (4 ports x 4 frequencies,
+    1e-8) in FP64 and mixed precision with SS factorised on the GPU; beside them the
+    oracle's fill (a sample) and its RIS operator and GMRES (one port solve) on the host
+    cores. One JSON line."""
     import torch
     from solver_gb300 import ris
     t0 = time.perf_counter()
     P = ris_problem(tuple(args.grid) if args.grid else (48, 48, 16))
     setup_s = time.perf_counter() - t0
-    op = ris.DenseOperator(P["inc"], P["Lp"], P["P"])
+    op = ris.DenseOperator.from_geometry(P["inc"], P["volumi"], P["superfici"], P["esc"], 1)
     mx, my, mz = P["inc"]["mx"], P["inc"]["my"], P["inc"]["mz"]
     ns = P["inc"]["Gamma"].shape[1]
     entries = mx * mx + my * my + mz * mz + ns * ns
+    # the dense fill (calcola_Lp + calcola_P on the device), timed as a second fill of the
+    # operator in place: every pair of the upper triangles, the Lp self terms, P's diagonal
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    op.fill(P["volumi"], P["superfici"], P["esc"], 1)
+    fill_s = time.perf_counter() - t
+    pairs = sum(k * (k + 1) // 2 for k in (mx, my, mz, ns))
+    fill = {"ms": fill_s * 1e3, "pairs": int(pairs), "pairs_per_s": pairs / fill_s,
+            "nonfinite": op.nonfinite, "kernel": "k_ris_pairs (FP64, one thread per pair)"}
     gs = {"Inner_Iter": 300, "tol": [1e-8] * len(P["freqs"])}
-    run = lambda mode: ris.iter_solver_QS_S_type(P["freqs"], P["esc"], P["inc"], P["P"], P["Lp"],
+    run = lambda mode: ris.iter_solver_QS_S_type(P["freqs"], P["esc"], P["inc"], None, None,
                                                  P["ports"], {}, gs, P["volumi"], False, 1, 50.0,
                                                  mode=mode, op=op, lu="device")
-    run("mixed")  # warm-up: graphs, the z tuner's absence, module load
+    run("mixed")  # warm-up: graphs, module load
     w = 2 * np.pi * P["freqs"][0] * P["esc"]["freq"]
-    st = ris.RisState(w, P["esc"], P["inc"], op.diag_Lp, np.diag(P["P"]["P"]), P["ports"], {},
+    st = ris.RisState(w, P["esc"], P["inc"], op.diag_Lp, op.diag_P, P["ports"], {},
                       P["volumi"], False, 50.0)
     op.set_frequency(w, st.DZ, st.Yle, st.lu)
     prof32 = op.profile_matvec(1, 20)
@@ -716,7 +709,8 @@ def run_ris(args):
     if not args.no_cpu_baseline:
         from oracle import peec_oracle as O
         from oracle import ris_ref as RO
-        stc = RO.frequency_setup(w, P["esc"], P["inc"], P["P"], P["Lp"], P["ports"], {},
+        Lp_h, P_h = op.dense_data()
+        stc = RO.frequency_setup(w, P["esc"], P["inc"], P_h, Lp_h, P["ports"], {},
                                  P["volumi"], False, 50.0)
         mv = lambda x: RO.ComputeMatrixVectorRis(x, w, P["inc"], stc["P"], stc["Lp"],
                                                  stc["Z_self"], stc["Yle"], stc["invZ"],
@@ -733,18 +727,22 @@ def run_ris(args):
                "kind": "port", "sample": f"one FP64 port solve at {P['freqs'][0]:.3g} Hz from "
                f"a zero guess ({len(rv) - 1} GMRES iterations, flag {fl}); the oracle's RIS "
                "operator with numpy/BLAS dense products on every host core"}
+        del Lp_h, P_h
+        rate, sample = ris_fill_cpu(P)
+        fill["cpu_baseline"] = {"value": rate, "unit": "pairs/s", "kind": "port",
+                                "cores": os.cpu_count() or 1, "sample": sample}
     ms32, ms64 = prof32["z"], prof64["z"]
     op.close()
     print(json.dumps({
         "metric": "dense RIS solver: port solves/s at 1e-8 (4 ports x 4 frequencies); dense "
-                  "operator GB/s", "value": res["mixed"]["port_solves_per_s"],
+                  "fill pairs/s; dense operator GB/s", "value": res["mixed"]["port_solves_per_s"],
         "unit": "port solves/s", "higher_is_better": True, "dtype": "f32 dense products, "
         "float-float refinement residuals over FP64 products", "data": "synthetic",
-        "config": {"workload": f"RIS dense operator on random_mixed {P['grid']} (Bernoulli 0.3,"
+        "config": {"workload": f"RIS dense fill and solver on random_mixed {P['grid']} (Bernoulli 0.3,"
                    f" seed 3): m = {op.m}, ns = {ns}, n = {op.n}; Lp blocks {mx}/{my}/{mz}, "
                    f"P {ns} x {ns}", "entries": int(entries), "lu": "device",
                    "setup_s": setup_s},
-        "fp64": res["fp64"], "mixed": res["mixed"], "mixed_vs_fp64_S_rel": zerr,
+        "fill": fill, "fp64": res["fp64"], "mixed": res["mixed"], "mixed_vs_fp64_S_rel": zerr,
         "dense_products": {"fp32_ms": ms32, "fp64_ms": ms64,
                            "fp32_gbs": 4.0 * entries / (ms32 * 1e-3) / 1e9,
                            "fp64_gbs": 8.0 * entries / (ms64 * 1e-3) / 1e9,

@@ -79,7 +79,7 @@ class DenseOperator(GpuOperator):
                                                      _lib.ptr(n2), self.ns, _lib.ptr(snode),
                                                      self.n))
         if geometry is not None:
-            self._fill(*geometry)
+            self.fill(*geometry)
             return
         blocks = []
         for key, size in (("Lp_x", mx), ("Lp_y", my), ("Lp_z", mz)):
@@ -108,7 +108,10 @@ class DenseOperator(GpuOperator):
         return cls(incidence_selection, None, None, device=device,
                    geometry=(volumi, superfici, escalings, int(QS_Rcc_FW)))
 
-    def _fill(self, volumi, superfici, escalings, QS_Rcc_FW):
+    def fill(self, volumi, superfici, escalings, QS_Rcc_FW=1):
+        """(Re)fills the dense blocks on the device from the bodies (peec_ris_fill); with
+        QS_Rcc_FW >= 2 also their centre distances."""
+        self._geometry = (volumi, superfici, escalings, int(QS_Rcc_FW))
         vol = ris_volumes(volumi, self.m)
         surf = ris_surfaces(superfici, self.ns)
         dist = int(QS_Rcc_FW) >= 2
@@ -226,6 +229,65 @@ def ris_surfaces(superfici, ns):
     c = superfici.get("centri", superfici.get(":centri"))
     out["centri"] = _rows(c, 3, ns, "superfici centri") if c is not None else np.zeros((ns, 3))
     return out
+
+
+def voxel_bodies(incidence_selection, expansions, grid, cell):
+    """The RIS bodies of a voxel mesh, as the RIS solver's inputs describe them: per edge
+    the brick of its Lp cell (one voxel length along the edge, between the two voxel
+    centres; volumi[:coordinate], [:S] the cross-section, [:centri]) and per surface its
+    voxel face (superfici["estremi_celle"], ["S"] the area, ["centri"]). cell = (sx, sy,
+    sz); lattice origin at 0."""
+    from .operator import _edge_cells, _surf_cells, row_dims
+    mx, my, mz = (int(incidence_selection[k]) for k in ("mx", "my", "mz"))
+    ns = incidence_selection["Gamma"].shape[1]
+    Nx, Ny, Nz = grid[:3]
+    cell = np.asarray(cell, dtype=np.float64)
+    dims = row_dims(Nx, Ny, Nz)
+
+    def ijk(ids, d):
+        ids = np.asarray(ids, dtype=np.int64)
+        return np.stack([ids % d[0], (ids // d[0]) % d[1], ids // (d[0] * d[1])],
+                        axis=1).astype(np.float64)
+
+    def corners(lo, hi):
+        # vertex k at (x, y, z) bits (k & 1, k >> 1 & 1, k >> 2): the reference's order
+        out = np.empty((lo.shape[0], 8, 3))
+        for k in range(8):
+            for a in range(3):
+                out[:, k, a] = hi[:, a] if (k >> a) & 1 else lo[:, a]
+        return out
+
+    ec = _edge_cells(expansions, mx, my, mz)
+    los, S = [], []
+    for d, (key, sl) in enumerate((("Lpx", slice(0, mx)), ("Lpy", slice(mx, mx + my)),
+                                   ("Lpz", slice(mx + my, mx + my + mz)))):
+        lo = ijk(ec[sl], dims[key])
+        lo[:, d] += 0.5
+        los.append(lo)
+        t = [q for q in range(3) if q != d]
+        S.append(np.full(lo.shape[0], cell[t[0]] * cell[t[1]]))
+    lo = np.concatenate(los) * cell
+    hi = lo + cell
+    volumi = {"coordinate": corners(lo, hi).reshape(-1, 24), "S": np.concatenate(S),
+              "centri": 0.5 * (lo + hi)}
+    fam, scell = _surf_cells(expansions, ns)
+    lo = np.zeros((ns, 3))
+    nrm = np.array([1, 0, 2])[fam]
+    for f, key in enumerate(("p12_se", "p34_se", "p56_se")):
+        sel = fam == f
+        lo[sel] = ijk(scell[sel], dims[key])
+    lo = lo * cell
+    ext = np.tile(cell, (ns, 1))
+    ext[np.arange(ns), nrm] = 0.0
+    hi = lo + ext
+    area = np.prod(np.where(ext > 0, ext, 1.0), axis=1)
+    ends = np.zeros((ns, 12))
+    ends[:, 0:3] = lo
+    ends[:, 9:12] = hi
+    ends[:, 3:6] = np.where(np.arange(3) == (nrm[:, None] + 1) % 3, hi, lo)
+    ends[:, 6:9] = np.where(np.arange(3) == (nrm[:, None] + 2) % 3, hi, lo)
+    superfici = {"estremi_celle": ends, "S": area, "centri": 0.5 * (lo + hi)}
+    return volumi, superfici
 
 
 def _sizes_only(mx, my, mz, ns):
