@@ -113,8 +113,9 @@ int fill_rows_gpu(const double origin[3], double sx, double sy, double sz, doubl
 size_t ris_box_bytes();
 int ris_prep_gpu(int surfaces, const double* d_geom, int64_t count, int64_t mx, int64_t my,
                  void* boxes, double* self, int* nrm, cudaStream_t st);
-int ris_pairs_gpu(int kind, const void* boxes, const int* nrm, const double* S, const double* self,
-                  int64_t dim, double esc, double* M, int64_t ld, int* d_bad, cudaStream_t st);
+int ris_pairs_gpu(int kind, int nb, const void* const* boxes, const int* nrm,
+                  const double* const* S, const double* const* self, const int64_t* dim,
+                  double esc, double* const* M, const int64_t* ld, int* d_bad, cudaStream_t st);
 int ris_dist_gpu(const double* d_ctr, int64_t dim, double* R, int64_t ld, cudaStream_t st);
 int inv_diag_gpu(const double* M, int64_t ld, int64_t n, double* inv, cudaStream_t st);
 void launch_adjoint(const c64*, const int32_t*, const int32_t*, const c64*, const c64*, double,
@@ -971,11 +972,22 @@ static int peec_ris_fill_body(peec_ctx* ctx, const double* vol_coords, const dou
           (rc = dalloc(&d_self, (size_t)m)) || (rc = dalloc(&d_box, (size_t)m * bb)))
         return rc;
       if ((rc = ris_prep_gpu(0, d_geom, m, ctx->mx, ctx->my, d_box, d_self, nullptr, ctx->st))) return rc;
-      for (int b = 0; b < 3 && !rc; ++b) {
+      const void* bx[3];
+      const double *bS[3], *bself[3];
+      double* bM[3];
+      for (int b = 0; b < 3; ++b) {
         if ((rc = block(b))) return rc;
-        rc = ris_pairs_gpu(0, d_box + (size_t)off[b] * bb, nullptr, d_S + off[b], d_self + off[b],
-                           sz[b], escal_Lp, ctx->dn64[b], ctx->dn_ld[b], d_bad, ctx->st);
-        if (!rc && distances)
+        bx[b] = d_box + (size_t)off[b] * bb;
+        bS[b] = d_S + off[b];
+        bself[b] = d_self + off[b];
+        bM[b] = ctx->dn64[b];
+      }
+      // the three blocks in one launch
+      if ((rc = ris_pairs_gpu(0, 3, bx, nullptr, bS, bself, sz, escal_Lp, bM, ctx->dn_ld, d_bad,
+                              ctx->st)))
+        return rc;
+      for (int b = 0; b < 3 && !rc; ++b) {
+        if (distances)
           rc = ris_dist_gpu(d_ctr + 3 * off[b], sz[b], ctx->dnR[b], ctx->dn_ld[b], ctx->st);
         if (!rc && sz[b])
           dense_round(ctx->dn64[b], (size_t)ctx->dn_ld[b] * sz[b], ctx->dn32[b], ctx->st);
@@ -992,8 +1004,11 @@ static int peec_ris_fill_body(peec_ctx* ctx, const double* vol_coords, const dou
         return rc;
       if ((rc = ris_prep_gpu(1, d_geom, ns, 0, 0, d_box, nullptr, d_nrm, ctx->st))) return rc;
       if ((rc = block(3))) return rc;
-      rc = ris_pairs_gpu(1, d_box, d_nrm, d_S, nullptr, ns, escal_P, ctx->dn64[3], ctx->dn_ld[3],
-                         d_bad, ctx->st);
+      const void* bx[1] = {d_box};
+      const double* bS[1] = {d_S};
+      double* bM[1] = {ctx->dn64[3]};
+      rc = ris_pairs_gpu(1, 1, bx, d_nrm, bS, nullptr, &sz[3], escal_P, bM, &ctx->dn_ld[3], d_bad,
+                         ctx->st);
       if (!rc && distances) rc = ris_dist_gpu(d_ctr, ns, ctx->dnR[3], ctx->dn_ld[3], ctx->st);
       if (!rc && ns) dense_round(ctx->dn64[3], (size_t)ctx->dn_ld[3] * ns, ctx->dn32[3], ctx->st);
       if (!rc) rc = dalloc(&ctx->invP, (size_t)ns);

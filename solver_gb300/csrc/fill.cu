@@ -946,38 +946,55 @@ __global__ void k_ris_surf_prep(const double* __restrict__ ends, int64_t ns, Box
   }
 }
 
+// One block of the dense fill: its bodies (with their normals for P), cross-sections or
+// areas, self terms (Lp), size and output matrix.
+struct RisBlock {
+  const Box* bodies;
+  const int* nrm;
+  const double* S;
+  const double* self;
+  int64_t dim;
+  double* M;
+  int64_t ld;
+};
+struct RisBlocks {
+  RisBlock b[3];
+};
+
 // KIND 0: an Lp block (Song_improved_Ivana_strategy2 off the diagonal, the self term
 // on it, 1e-7 / (S_m S_n) * integral * esc; calculate_Lp_matrix, calcola_Lp.jl:254-306);
 // KIND 1: P (Song_P_improved_Ivana_strategy on and off the diagonal,
 // integral / (4 pi eps0 S_m S_n) * esc; calculate_P_matrix, calcola_P.jl:162-222).
-// Grid (tiles, tiles): CTA (x, y) takes the tile of rows 32y.. and columns 32x.., x >= y.
-template <int KIND>
-__global__ void __launch_bounds__(256) k_ris_pairs(const Box* __restrict__ bodies,
-                                                   const int* __restrict__ nrm,
-                                                   const double* __restrict__ S,
-                                                   const double* __restrict__ self, int64_t dim,
-                                                   double esc, double* __restrict__ M, int64_t ld,
-                                                   int* bad) {
-  __shared__ Box rb[32], cb[32];
-  __shared__ int rn[32], cn[32];
-  __shared__ double tile[32][33];
+// Grid (tiles, tiles, blocks): CTA (x, y, z) takes the T x T tile of rows Ty.. and columns
+// Tx.. of block z, x >= y; 256 threads, T*T/256 pairs each. The three Lp blocks share one
+// launch, and small blocks take T = 16, so that the GPU fills with CTAs.
+template <int KIND, int T>
+__global__ void __launch_bounds__(256) k_ris_pairs(RisBlocks blocks, double esc, int* bad) {
+  constexpr int ROWS = 256 / T;
+  __shared__ Box rb[T], cb[T];
+  __shared__ int rn[T], cn[T];
+  __shared__ double tile[T][T + 1];
+  const RisBlock& blk = blocks.b[blockIdx.z];
+  const int64_t dim = blk.dim, ld = blk.ld;
   const int64_t ti = blockIdx.y, tj = blockIdx.x;
-  if (ti > tj) return;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int64_t m0 = ti * 32, n0 = tj * 32;
+  if (ti > tj || tj * T >= dim) return;
+  const int tx = threadIdx.x % T, ty = threadIdx.x / T;
+  const int64_t m0 = ti * T, n0 = tj * T;
   if (ty == 0 && m0 + tx < dim) {
-    rb[tx] = bodies[m0 + tx];
-    rn[tx] = KIND ? nrm[m0 + tx] : 0;
+    rb[tx] = blk.bodies[m0 + tx];
+    rn[tx] = KIND ? blk.nrm[m0 + tx] : 0;
   } else if (ty == 1 && n0 + tx < dim) {
-    cb[tx] = bodies[n0 + tx];
-    cn[tx] = KIND ? nrm[n0 + tx] : 0;
+    cb[tx] = blk.bodies[n0 + tx];
+    cn[tx] = KIND ? blk.nrm[n0 + tx] : 0;
   }
   __syncthreads();
   const double pi = CUDART_PI;
   const double eps0 = 8.854187816997944e-12;
+  const double* S = blk.S;
+  double* M = blk.M;
   const int64_t m = m0 + tx;
-  for (int k = 0; k < 4; ++k) {
-    const int nl = ty + 8 * k;
+  for (int k = 0; k < T / ROWS; ++k) {
+    const int nl = ty + ROWS * k;
     const int64_t n = n0 + nl;
     double e = 0.0;
     if (m < dim && n < dim && (KIND ? m <= n : m < n)) {
@@ -998,13 +1015,13 @@ __global__ void __launch_bounds__(256) k_ris_pairs(const Box* __restrict__ bodie
     tile[nl][tx] = e;
   }
   __syncthreads();
-  for (int k = 0; k < 4; ++k) {  // the mirrored entries (n, m), m < n
-    const int ml = ty + 8 * k;
+  for (int k = 0; k < T / ROWS; ++k) {  // the mirrored entries (n, m), m < n
+    const int ml = ty + ROWS * k;
     const int64_t mm = m0 + ml, nn = n0 + tx;
     if (mm < dim && nn < dim && mm < nn) M[nn + mm * ld] = tile[tx][ml];
   }
   if (KIND == 0 && ti == tj && ty == 0 && m < dim) {
-    const double e = self[m] * esc;
+    const double e = blk.self[m] * esc;
     if (!isfinite(e)) atomicAdd(bad, 1);
     M[m + m * ld] = e;
   }
@@ -1048,18 +1065,44 @@ int ris_prep_gpu(int surfaces, const double* d_geom, int64_t count, int64_t mx, 
   return 0;
 }
 
-// one dense block: KIND 0 (Lp, boxes/self/S of its volumes) or 1 (P); M zeroed by the
-// caller (padding rows stay zero)
-int ris_pairs_gpu(int kind, const void* boxes, const int* nrm, const double* S, const double* self,
-                  int64_t dim, double esc, double* M, int64_t ld, int* d_bad, cudaStream_t st) {
-  if (dim <= 0) return 0;
-  const int64_t nt = (dim + 31) / 32;
+// the dense blocks of one fill: kind 0, up to three Lp blocks in one launch (boxes, self
+// terms and S of their volumes); kind 1, P. M zeroed by the caller (padding rows stay zero).
+template <int KIND, int T>
+static void launch_pairs(const RisBlocks& rb, int nb, int64_t nt, double esc, int* d_bad,
+                         cudaStream_t st) {
+  const dim3 grid((unsigned)nt, (unsigned)nt, (unsigned)nb);
+  k_ris_pairs<KIND, T><<<grid, 256, 0, st>>>(rb, esc, d_bad);
+}
+
+int ris_pairs_gpu(int kind, int nb, const void* const* boxes, const int* nrm,
+                  const double* const* S, const double* const* self, const int64_t* dim,
+                  double esc, double* const* M, const int64_t* ld, int* d_bad, cudaStream_t st) {
+  RisBlocks rb;
+  int64_t maxdim = 0, tiles32 = 0;
+  for (int b = 0; b < 3; ++b) {
+    const bool on = b < nb;
+    rb.b[b] = RisBlock{on ? (const Box*)boxes[b] : nullptr, kind ? nrm : nullptr,
+                       on ? S[b] : nullptr, on ? (self ? self[b] : nullptr) : nullptr,
+                       on ? dim[b] : 0, on ? M[b] : nullptr, on ? ld[b] : 1};
+    if (on) {
+      maxdim = std::max(maxdim, dim[b]);
+      const int64_t t = (dim[b] + 31) / 32;
+      tiles32 += t * (t + 1) / 2;
+    }
+  }
+  if (maxdim <= 0) return 0;
+  // 32 x 32 tiles once they give every SM a few CTAs, else 16 x 16
+  const bool big = tiles32 >= 152 * 4;
+  const int T = big ? 32 : 16;
+  const int64_t nt = (maxdim + T - 1) / T;
   if (nt > 65535) return PEEC_ERR_UNSUPPORTED_INTERNAL;
-  const dim3 grid((unsigned)nt, (unsigned)nt);
-  if (kind == 0)
-    k_ris_pairs<0><<<grid, 256, 0, st>>>((const Box*)boxes, nrm, S, self, dim, esc, M, ld, d_bad);
-  else
-    k_ris_pairs<1><<<grid, 256, 0, st>>>((const Box*)boxes, nrm, S, self, dim, esc, M, ld, d_bad);
+  if (kind == 0) {
+    if (big) launch_pairs<0, 32>(rb, nb, nt, esc, d_bad, st);
+    else launch_pairs<0, 16>(rb, nb, nt, esc, d_bad, st);
+  } else {
+    if (big) launch_pairs<1, 32>(rb, nb, nt, esc, d_bad, st);
+    else launch_pairs<1, 16>(rb, nb, nt, esc, d_bad, st);
+  }
   PEEC_CUDA_TRY(cudaGetLastError());
   return 0;
 }
