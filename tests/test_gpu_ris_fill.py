@@ -148,3 +148,19 @@ def test_ris_solver_on_device_filled_matrices(case, QS_Rcc_FW):
             assert np.array_equal(out2["S"], out["S"])
     finally:
         op.close()
+
+
+def test_device_fill_reproduces_the_reference_nan():
+    """The point-surface form's 0/0 (a point in a surface's plane, on an edge's line) is NaN
+    on the device as in the oracle, and counted."""
+    from tests.test_oracle_ris_fill import _nan_case
+    vol = _nan_case()
+    surf = {"estremi_celle": np.zeros((0, 12)), "S": np.zeros(0)}
+    op = _fill_op(vol, surf, 2, 0, 0, {"Lp": 1.0, "P": 1.0})
+    try:
+        Lp, _ = op.dense_data()
+        assert np.isnan(Lp["Lp_x"][0, 1]) and np.isnan(Lp["Lp_x"][1, 0])
+        assert np.isfinite(np.diag(Lp["Lp_x"])).all()
+        assert op.nonfinite == 1
+    finally:
+        op.close()

@@ -148,3 +148,29 @@ def test_voxel_bodies_give_the_voxel_dense_blocks():
         # formula of one voxel, the RIS fill's self term of the same brick
         assert np.allclose(np.diag(A), np.min(np.diag(B)), rtol=1e-13, atol=0), k
     assert np.max(np.abs(P_r["P"] - P_v["P"])) <= 1e-9 * np.max(np.abs(P_v["P"]))
+
+
+def _nan_case():
+    """Two x-directed bodies: a small cube far from a thin plate, its centre in the plate's
+    mid-plane and on the line of one of the plate's edges. The suppression tests make them
+    a point and a surface, and the point-surface form's arctangent of the quotient
+    (integ_point_sup_sharedRis, Song_improved_Ivana_strategy.jl:449-478) meets 0/0 there.
+    Every coordinate is a short dyadic fraction, exact in binary and under 14 decimals."""
+    h = 2.0 ** -12
+    mid = 2.0 ** -14
+    cube_lo, cube_hi = np.array([-h, 0.5 - h, mid - h]), np.array([h, 0.5 + h, mid + h])
+    plate_lo, plate_hi = np.array([0.0, 0.0, 0.0]), np.array([2.0 ** -5, 2.0 ** -5, 2 * mid])
+    vol = {"coordinate": np.array([ris_cases._brick24(cube_lo, cube_hi),
+                                   ris_cases._brick24(plate_lo, plate_hi)]),
+           "S": np.array([4 * h * h, 2 * mid * 2.0 ** -5])}
+    return vol
+
+
+def test_point_in_a_surface_plane_gives_the_reference_nan():
+    vol = _nan_case()
+    forms = {}
+    Lp, _, _, _, bad = ris_cases.oracle_dense_fill(
+        vol, {"estremi_celle": np.zeros((0, 12)), "S": np.zeros(0)}, 2, 0, 0, forms=forms)
+    assert forms["Lp_x"][0, 1] == 4  # point (3 collapsed) against surface (1)
+    assert np.isnan(Lp["Lp_x"][0, 1]) and np.isnan(Lp["Lp_x"][1, 0])
+    assert bad == 1
