@@ -163,7 +163,10 @@ struct peec_ctx {
   double* dn64[4] = {nullptr, nullptr, nullptr, nullptr};
   int64_t dn_ld[4] = {4, 4, 4, 4};  // padded leading dimensions
   float* dn32[4] = {nullptr, nullptr, nullptr, nullptr};
+  // partial sums of the chunked products: the Lp blocks (one after another on st2) use the
+  // first dn_part_half entries, P (on st, beside them) the second
   c64* dn_part = nullptr;
+  size_t dn_part_half = 0;
   // the dense retarded operator (peec_set_dense_rcc): centre distances R per block, and the
   // blocks times exp(-j beta R) of the installed frequency (FP64 and FP32 copies)
   bool dense_rcc = false, dense_rcc_ready = false;
@@ -818,7 +821,8 @@ static int peec_set_dense_body(peec_ctx* ctx, const double* Lpx, const double* L
     }
     part = std::max(part, (size_t)dense_chunks(sz[b]) * (size_t)std::max<int64_t>(sz[b], 1));
   }
-  CTX_TRY(dalloc(&ctx->dn_part, part));
+  CTX_TRY(dalloc(&ctx->dn_part, 2 * part));
+  ctx->dn_part_half = part;
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   for (int b = 0; b < 4; ++b) {
     ctx->dn_set[b] = true;
@@ -870,7 +874,9 @@ static int peec_set_dense_rcc_body(peec_ctx* ctx, const double* Rx, const double
     part = std::max({part, (size_t)dense_part_c(sz[b]),
                      (size_t)dense_chunks(sz[b]) * (size_t)std::max<int64_t>(sz[b], 1)});
   }
-  CTX_TRY(dalloc(&ctx->dn_part, std::max(part, (size_t)1)));
+  part = std::max(part, (size_t)1);
+  CTX_TRY(dalloc(&ctx->dn_part, 2 * part));
+  ctx->dn_part_half = part;
   PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
   for (int b = 0; b < 4; ++b) ctx->dnR_set[b] = true;
   ctx->dense_rcc = true;
@@ -1023,7 +1029,8 @@ static int peec_ris_fill_body(peec_ctx* ctx, const double* vol_coords, const dou
       part = std::max(part, (size_t)dense_chunks(sz[b]) * (size_t)std::max<int64_t>(sz[b], 1));
       if (distances) part = std::max(part, (size_t)dense_part_c(sz[b]));
     }
-    if ((rc = dalloc(&ctx->dn_part, part))) return rc;
+    if ((rc = dalloc(&ctx->dn_part, 2 * part))) return rc;
+    ctx->dn_part_half = part;
     int hbad = 0;
     PEEC_CUDA_TRY(cudaMemcpyAsync(&hbad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
     PEEC_CUDA_TRY(cudaStreamSynchronize(ctx->st));
@@ -2160,25 +2167,37 @@ static int matvec_enqueue(peec_ctx* ctx, const c64* x, c64* y, int prec, bool ev
     if (pe) for (int e = 0; e < 3; ++e) cudaEventRecord(pe[e], st);
     const int64_t off[3] = {0, ctx->mx, ctx->mx + ctx->my};
     const int64_t sz[3] = {ctx->mx, ctx->my, ctx->mz};
-    if (ctx->dense_rcc) {
-      if (!ctx->dense_rcc_ready)
-        return bad(ctx, PEEC_ERR_STATE, "retarded blocks not formed (peec_set_dense_rcc_frequency)");
-      for (int b = 0; b < 3; ++b)
-        ctx->launches += dense_apply_c(f32 ? (const void*)ctx->dnc32[b] : (const void*)ctx->dnc64[b],
-                                       f32, sz[b], ctx->dn_ld[b], x + off[b], 1, ctx->dn_part,
-                                       ctx->LpI + off[b], st);
-      ctx->launches += dense_apply_c(f32 ? (const void*)ctx->dnc32[3] : (const void*)ctx->dnc64[3],
-                                     f32, ctx->ns, ctx->dn_ld[3], x + ctx->m, 0, ctx->dn_part,
-                                     ctx->PQ, st);
-    } else {
-      for (int b = 0; b < 3; ++b)
-        ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[b] : (const void*)ctx->dn64[b],
-                                     f32, sz[b], ctx->dn_ld[b], x + off[b], 1, ctx->dn_part,
-                                     ctx->LpI + off[b], st);
-      ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[3] : (const void*)ctx->dn64[3], f32,
-                                   ctx->ns, ctx->dn_ld[3], x + ctx->m, 0, ctx->dn_part, ctx->PQ,
-                                   st);
+    if (ctx->dense_rcc && !ctx->dense_rcc_ready)
+      return bad(ctx, PEEC_ERR_STATE, "retarded blocks not formed (peec_set_dense_rcc_frequency)");
+    // the three Lp blocks on st2, beside P on st (fork and join events; under capture,
+    // graph edges): the small blocks' products and reductions hide behind P's stream
+    const bool fork = ctx->st2 && ctx->m > 0;
+    cudaStream_t sl = fork ? ctx->st2 : st;
+    c64* part_lp = ctx->dn_part;
+    c64* part_p = ctx->dn_part + ctx->dn_part_half;
+    if (fork) {
+      cudaEventRecord(ctx->ev_fork, st);
+      cudaStreamWaitEvent(ctx->st2, ctx->ev_fork, 0);
     }
+    for (int b = 0; b < 3; ++b) {
+      if (ctx->dense_rcc)
+        ctx->launches += dense_apply_c(f32 ? (const void*)ctx->dnc32[b] : (const void*)ctx->dnc64[b],
+                                       f32, sz[b], ctx->dn_ld[b], x + off[b], 1, part_lp,
+                                       ctx->LpI + off[b], sl);
+      else
+        ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[b] : (const void*)ctx->dn64[b],
+                                     f32, sz[b], ctx->dn_ld[b], x + off[b], 1, part_lp,
+                                     ctx->LpI + off[b], sl);
+    }
+    if (fork) cudaEventRecord(ctx->ev_join, ctx->st2);
+    if (ctx->dense_rcc)
+      ctx->launches += dense_apply_c(f32 ? (const void*)ctx->dnc32[3] : (const void*)ctx->dnc64[3],
+                                     f32, ctx->ns, ctx->dn_ld[3], x + ctx->m, 0, part_p, ctx->PQ,
+                                     st);
+    else
+      ctx->launches += dense_apply(f32 ? (const void*)ctx->dn32[3] : (const void*)ctx->dn64[3], f32,
+                                   ctx->ns, ctx->dn_ld[3], x + ctx->m, 0, part_p, ctx->PQ, st);
+    if (fork) cudaStreamWaitEvent(st, ctx->ev_join, 0);
     if (pe) for (int e = 3; e < 6; ++e) cudaEventRecord(pe[e], st);
     if (events) cudaEventRecord(ctx->ev[1], st);
     sparse_enqueue(ctx, x, y, ctx->LpI, ctx->PQ);
