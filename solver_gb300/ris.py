@@ -304,9 +304,9 @@ def _sizes_only(mx, my, mz, ns):
 
 def calcola_Lp(volumi, incidence_selection, escalings, QS_Rcc_FW, device=0):
     """calcola_Lp (sharedRis/calcola_Lp.jl:1-97) on the GPU: the dense Lp_x, Lp_y, Lp_z
-    (and Rx, Ry, Rz when QS_Rcc_FW >= 2), returned on the host. For QS_Rcc_FW < 2 the
-    reference's function reads its unassigned Rx at the return and raises; here the
-    distances are left out."""
+    (and Rx, Ry, Rz when QS_Rcc_FW >= 2), returned on the host, with "nonfinite" the
+    count of non-finite entries. For QS_Rcc_FW < 2 the reference's function reads its
+    unassigned Rx at the return and raises; here the distances are left out."""
     mx, my, mz = (int(incidence_selection[k]) for k in ("mx", "my", "mz"))
     inc = _sizes_only(mx, my, mz, 0)
     op = DenseOperator(inc, None, None, device=device,
@@ -322,8 +322,9 @@ def calcola_Lp(volumi, incidence_selection, escalings, QS_Rcc_FW, device=0):
 
 def calcola_P(superfici, escalings, QS_Rcc_FW, device=0):
     """calcola_P (sharedRis/calcola_P.jl:1-47) on the GPU: the dense P (and R_cc when
-    QS_Rcc_FW >= 2), returned on the host. For QS_Rcc_FW < 2 the reference returns
-    R_cc = nothing into a matrix-typed Dict and raises; here R_cc is left out."""
+    QS_Rcc_FW >= 2), returned on the host, with "nonfinite" the count of non-finite
+    entries. For QS_Rcc_FW < 2 the reference returns R_cc = nothing into a matrix-typed
+    Dict and raises; here R_cc is left out."""
     ns = len(np.asarray(_key(superfici, "S")).ravel())
     inc = _sizes_only(0, 0, 0, ns)
     op = DenseOperator(inc, None, None, device=device,
