@@ -4,7 +4,8 @@ Song_*_Ivana_strategy case trees), pinned by independent closed forms and quadra
 * Compute_Lp_Self (the FastHenry bar formula) equals the six-fold volume integral of the
   same bar (the 64-term closed form) in long double.
 * The P self term of a rectangle equals a numerical quadrature of its area integral.
-* Far apart, every entry tends to the point-point value.
+* Far apart, every entry tends to the point-point value; every suppressed (collapsed-
+  dimension) form of both trees lies within 0.5 (size / R)^2 of it.
 * The double restatement agrees with the long double one within 64 eps of each entry's
   sum of |terms| on seeded bodies that take every branch.
 * On a voxel geometry written as RIS bodies the dense fill gives the voxel path's dense
@@ -174,3 +175,42 @@ def test_point_in_a_surface_plane_gives_the_reference_nan():
     assert forms["Lp_x"][0, 1] == 4  # point (3 collapsed) against surface (1)
     assert np.isnan(Lp["Lp_x"][0, 1]) and np.isnan(Lp["Lp_x"][1, 0])
     assert bad == 1
+
+
+def test_suppressed_forms_tend_to_the_point_value():
+    """Every collapsed-dimension form of both trees (a body replaced by a surface, a line or
+    a point once its dimension passes the suppression test) is a far-field approximation of
+    the same integral: against the point-point value V1 V2 / R it errs by at most a small
+    multiple of (size / R)^2. A mistyped form would miss by O(1)."""
+    mx, my, mz, ns = 40, 30, 25, 60
+    vol, surf = ris_cases.random_bodies(7, mx, my, mz, ns)
+    forms = {}
+    Lp, P, _, _, _ = ris_cases.oracle_dense_fill(vol, surf, mx, my, mz, ld=True, forms=forms)
+    C = np.asarray(vol["coordinate"]).reshape(-1, 8, 3)
+    lo, hi = C.min(1), C.max(1)
+    ctr, ext = 0.5 * (lo + hi), hi - lo
+    V, S, size = ext.prod(1), np.asarray(vol["S"]), ext.max(1)
+
+    def check(M, f, pp, r, first):
+        iu = np.triu_indices(M.shape[0], 1)
+        sel = f[iu] >= first
+        assert sel.sum() > 50
+        rel = np.abs(M[iu][sel] - pp[iu][sel]) / pp[iu][sel]
+        assert np.all(rel <= 0.5 * r[iu][sel] ** 2), float(np.max(rel / r[iu][sel] ** 2))
+
+    off = 0
+    for k, n in (("Lp_x", mx), ("Lp_y", my), ("Lp_z", mz)):
+        sl = slice(off, off + n)
+        off += n
+        R = np.linalg.norm(ctr[sl][:, None] - ctr[sl][None], axis=-1)
+        R = np.where(R > 0, R, 1.0)
+        pp = 1e-7 * np.outer(V[sl], V[sl]) / np.outer(S[sl], S[sl]) / R
+        r = np.maximum.outer(size[sl], size[sl]) / R
+        check(Lp[k], forms[k], pp, r, 1)
+    E = np.asarray(surf["estremi_celle"])
+    slo, shi = np.minimum(E[:, :3], E[:, 9:]), np.maximum(E[:, :3], E[:, 9:])
+    R = np.linalg.norm(0.5 * (slo + shi)[:, None] - 0.5 * (slo + shi)[None], axis=-1)
+    R = np.where(R > 0, R, 1.0)
+    pp = 1 / (4 * np.pi * 8.854187816997944e-12 * R)
+    r = np.maximum.outer((shi - slo).max(1), (shi - slo).max(1)) / R
+    check(P["P"], forms["P"], pp, r, 3)
