@@ -338,6 +338,67 @@ def calcola_P(superfici, escalings, QS_Rcc_FW, device=0):
         op.close()
 
 
+def find_nodes_ports_or_le(port_objects, lumped_elements_objects, nodi_coord, escal):
+    """find_nodes_ports_or_le (sharedRis/find_nodes_ports_or_le.jl:1-103): each port's and
+    lumped element's terminal positions, every coordinate rounded to 5 decimals then scaled
+    by escal, mapped to the first node at the smallest Euclidean distance (nodes_find_rev
+    with distfcm, :105-119). Returns (ports, lumped_elements) in the form the RIS loop
+    takes, node indices 0-based."""
+    nodes = np.asarray(nodi_coord, dtype=np.float64)
+    if nodes.ndim == 2 and nodes.shape[0] == 3 and nodes.shape[1] != 3:
+        nodes = nodes.T  # the JSON layout: three lists of node coordinates
+    nodes = nodes.reshape(-1, 3)
+
+    def pos(p):
+        return np.array([np.rint(float(p[i]) * 1e5) / 1e5 * escal for i in range(3)])
+
+    def nearest(q):
+        d = np.sqrt(((nodes - q) ** 2).sum(axis=1))
+        return int(np.flatnonzero(d == d.min())[0])
+
+    def terminals(objs):
+        return np.array([[nearest(pos(o["inputElement"])), nearest(pos(o["outputElement"]))]
+                         for o in objs], dtype=np.int64).reshape(-1, 2)
+
+    ports = {"port_start": [pos(o["inputElement"]) for o in port_objects],
+             "port_end": [pos(o["outputElement"]) for o in port_objects],
+             "port_nodes": terminals(port_objects)}
+    les = list(lumped_elements_objects or [])
+    rlc = lambda o, k: float(o.get("rlcParams", {}).get(k, 0.0))
+    lumped = {"le_start": [pos(o["inputElement"]) for o in les],
+              "le_end": [pos(o["outputElement"]) for o in les],
+              "le_nodes": terminals(les), "type": [o["type"] for o in les],
+              "R": [rlc(o, "resistance") for o in les], "L": [rlc(o, "inductance") for o in les],
+              "C": [rlc(o, "capacitance") for o in les]}
+    return ports, lumped
+
+
+def do_solving_ris(incidence_selection, volumi, superfici, nodi_coord, escalings, solverInput,
+                   solverAlgoParams, solverType, mode="fp64", device=0, lu="host"):
+    """doSolvingRis (solverRis/do_solving_ris.jl:1-78) without its service parts (S3, AMQP,
+    stop flags): ports and lumped elements mapped to nodes, the dense Lp blocks and P filled
+    on the GPU, and the frequency x port loop (GMRES settings from solverAlgoParams; 1e-8
+    below 100 kHz; QS_Rcc_FW = solverType; surface impedance on). Returns the loop's dict
+    (S, Z, Y, f)."""
+    from .mesher import get_escal_from
+    escal = get_escal_from(solverInput.get("unit", "m"))
+    R = float(solverInput.get("ports_scattering_value", 50.0))
+    freq = np.asarray(solverInput["frequencies"], dtype=np.float64).ravel()
+    ports, le = find_nodes_ports_or_le(solverInput["ports"], solverInput.get("lumped_elements", []),
+                                       nodi_coord, escal)
+    tol = float(solverAlgoParams["convergenceThreshold"]) * np.ones(freq.size)
+    tol[freq < 1e5] = 1e-8
+    gs = {"Inner_Iter": int(solverAlgoParams["innerIteration"]),
+          "Outer_Iter": int(solverAlgoParams["outerIteration"]), "tol": tol}
+    op = DenseOperator.from_geometry(incidence_selection, volumi, superfici, escalings,
+                                     int(solverType), device=device)
+    try:
+        return iter_solver_QS_S_type(freq, escalings, incidence_selection, None, None, ports, le,
+                                     gs, volumi, True, int(solverType), R, mode=mode, op=op, lu=lu)
+    finally:
+        op.close()
+
+
 def lumped_admittance_S(typ, R, L, C, w):
     """get_lumped_elements_admittance_S (build_Yle_S.jl:70-151): the element's network,
     then while the value is not finite or below 1e-16 in magnitude the next network of the

@@ -164,3 +164,26 @@ def test_device_fill_reproduces_the_reference_nan():
         assert op.nonfinite == 1
     finally:
         op.close()
+
+
+def test_do_solving_ris_end_to_end(case):
+    """doSolvingRis without its service parts: ports given by coordinates are mapped back to
+    the mesh's nodes, the matrices filled on the device, the loop run; its S parameters
+    match the oracle's loop on the oracle's matrices."""
+    c = case
+    n = c["inc"]["A"].shape[1]
+    k = np.arange(n)
+    nodi = np.stack([k * 1e-3, (k % 7) * 1e-3, np.zeros(n)], axis=1)  # distinct nodes
+    pn = np.asarray(c["ports"]["port_nodes"]).reshape(-1, 2)
+    freqs = [1e8, 1e9, 3e9]
+    si = {"unit": "m", "frequencies": freqs, "lumped_elements": [],
+          "ports": [{"inputElement": nodi[a].tolist(), "outputElement": nodi[b].tolist()}
+                    for a, b in pn]}
+    algo = {"innerIteration": 200, "outerIteration": 1, "convergenceThreshold": 1e-8}
+    out = ris.do_solving_ris(c["inc"], c["volumi"], c["superfici"], nodi, c["esc"], si, algo, 1)
+    gs = {"Inner_Iter": 200, "tol": [1e-8] * len(freqs)}
+    ref = RO.iter_solver_QS_S_type(freqs, c["esc"], c["inc"], c["P_data"], c["Lp_data"],
+                                   c["ports"], {}, gs, c["volumi"], True, 1, 50.0)
+    assert all(r["flag"] == 0 for r in out["info"])
+    for q in range(len(freqs)):
+        assert _rel(out["S"][:, :, q], ref["S"][:, :, q]) < 1e-7, q

@@ -48,3 +48,25 @@ def test_body_arrays_take_the_reference_layouts():
         ris.ris_volumes({"coordinate": np.zeros((m, 23)), "S": np.ones(m)}, m)
     with pytest.raises(ValueError, match="S must have"):
         ris.ris_surfaces({"estremi_celle": surf["estremi_celle"], "S": np.ones(ns + 1)}, ns)
+
+
+def test_ports_map_to_the_nearest_node():
+    """find_nodes_ports_or_le: positions rounded to 5 decimals, scaled, then the first node
+    at the smallest distance (ties to the lower index)."""
+    nodes = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [1.0, 0.0, 0.0]])
+    ports = [{"inputElement": [0.9, 0.1, 0.0], "outputElement": [0.1, 0.8, 0.0]},
+             {"inputElement": [0.000004, 0.0, 0.0], "outputElement": [2.0, 0.0, 0.0]}]
+    les = [{"inputElement": [0.0, 0.0, 0.0], "outputElement": [0.0, 1.0, 0.0], "type": 1,
+            "rlcParams": {"resistance": 50.0}}]
+    p, le = ris.find_nodes_ports_or_le(ports, les, nodes, 1.0)
+    # node 3 duplicates node 1: the first one wins
+    assert p["port_nodes"].tolist() == [[1, 2], [0, 1]]
+    assert le["le_nodes"].tolist() == [[0, 2]] and le["R"] == [50.0] and le["L"] == [0.0]
+    # rounding to 5 decimals before scaling: 0.000004 m rounds to 0
+    assert p["port_start"][1][0] == 0.0
+    # the JSON layout of the node coordinates (three lists) and a unit scale
+    p2, _ = ris.find_nodes_ports_or_le(ports, [], nodes.T, 1.0)
+    assert np.array_equal(p2["port_nodes"], p["port_nodes"])
+    p3, _ = ris.find_nodes_ports_or_le([{"inputElement": [900.0, 100.0, 0.0],
+                                         "outputElement": [0.0, 0.0, 0.0]}], [], nodes, 1e-3)
+    assert p3["port_nodes"].tolist() == [[1, 0]]
