@@ -477,14 +477,15 @@ def z_self(volumi, w, use_Zs_in):
     """Self impedance per edge (iter_solver_QS_S_type.jl:82-101): R, or with use_Zs_in the
     surface impedance Re(sqrt(jw) Zs_part) where it is not below R; plus 1/(jw Cd) on the
     dielectric volumes."""
-    R = np.asarray(volumi["R"], dtype=np.float64).ravel()
-    diel = np.asarray(volumi.get("indici_dielettrici", []), dtype=np.int64).ravel()
-    invCd = np.zeros(len(volumi["Cd"]) if diel.size else R.size, dtype=np.complex128)
+    R = np.asarray(_key(volumi, "R"), dtype=np.float64).ravel()
+    diel = np.asarray(volumi.get("indici_dielettrici", volumi.get(":indici_dielettrici", [])),
+                      dtype=np.int64).ravel()
+    invCd = np.zeros(len(_key(volumi, "Cd")) if diel.size else R.size, dtype=np.complex128)
     if diel.size:
-        Cd = np.asarray(volumi["Cd"], dtype=np.float64).ravel()
+        Cd = np.asarray(_key(volumi, "Cd"), dtype=np.float64).ravel()
         invCd[diel] = 1.0 / (1j * w * Cd[diel])
     if use_Zs_in:
-        Zs = (np.sqrt(1j * w) * np.asarray(volumi["Zs_part"], dtype=np.complex128).ravel()).real
+        Zs = (np.sqrt(1j * w) * np.asarray(_key(volumi, "Zs_part"), dtype=np.complex128).ravel()).real
         Z = np.where(R > Zs, R, Zs).astype(np.complex128)
         return Z + invCd
     return R + invCd

@@ -70,3 +70,13 @@ def test_ports_map_to_the_nearest_node():
     p3, _ = ris.find_nodes_ports_or_le([{"inputElement": [900.0, 100.0, 0.0],
                                          "outputElement": [0.0, 0.0, 0.0]}], [], nodes, 1e-3)
     assert p3["port_nodes"].tolist() == [[1, 0]]
+
+
+def test_z_self_reads_symbol_keyed_volumi():
+    rng = np.random.default_rng(4)
+    vol = {"R": rng.uniform(0, 1, 10), "Cd": rng.uniform(1e-12, 2e-12, 10),
+           "indici_dielettrici": np.array([2, 5]), "Zs_part": rng.uniform(0, 1e-6, 10)}
+    sym = {":" + k: v for k, v in vol.items()}
+    w = 2 * np.pi * 1e9
+    for zs in (False, True):
+        assert np.array_equal(ris.z_self(vol, w, zs), ris.z_self(sym, w, zs))
